@@ -1,0 +1,399 @@
+#!/usr/bin/env python3
+"""Benchmark: simulated days per wall-second of the TRiSK shallow-water CRK4
+step on one GB300, on the level-9 icosahedral mesh (2,621,442 cells,
+7,864,320 edges, 5,242,880 vertices) with 4 coupled tracers and dt = 45 s.
+
+One "step" is one CRK4 time step (4 spatial_operators stages + the beta-scaled
+update) of the whole mesh.  The headline arm is the FP32-state path (FP64
+metrics, gd accumulation and invariant sums); the plain FP64 path is timed on
+the same initial state and the FP32 h error against it is reported.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the CPU FP64 restatement of the reference (the
+oracle; the Fortran reference cannot be compiled in this image) on the host
+cores, on the same workload.  For N > 1 (torchrun) the path runs as
+independent replicas, one per GPU ("replicas only": a single mesh is not
+domain-decomposed); the time is the max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+DAY = 86400.0
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--level", type=int, default=9)
+    ap.add_argument("--dt", type=float, default=45.0)
+    ap.add_argument("--tracers", type=int, default=4)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison run")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-steps", type=int, default=1)
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Dist:
+    def __init__(self, world):
+        self.world = world
+        self.pg = None
+        if world > 1:
+            import torch.distributed as td
+
+            td.init_process_group("gloo")
+            self.td = td
+
+    def barrier(self):
+        if self.world > 1:
+            self.td.barrier()
+
+    def max(self, x: float) -> float:
+        if self.world == 1:
+            return x
+        import torch
+
+        t = torch.tensor([x], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.td.destroy_process_group()
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+        time.sleep(0.3)
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.flush()
+        rows = [r.split(",") for r in open(self.f.name).read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, smax, pw, reasons = [], [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                smax.append(float(r[2]))
+                pw.append(float(r[3]))
+            except (ValueError, IndexError):
+                continue
+            for k, n in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].strip() == "Active":
+                    reasons.add(n)
+        busy = [s for s in sm if smax and s > 0.5 * max(smax)] or sm
+        return {"sm_mhz": statistics.median(busy) if busy else None, "sm_max_mhz": max(smax) if smax else None,
+                "power_w_max": max(pw) if pw else None, "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def flux_kernel_bytes(nc: int, ne: int, S: int, me2: int = 10) -> float:
+    """Compulsory bytes of one edge_flux launch (averaged over the 4 CRK4 stages).
+
+    Per edge: edgesOnEdge 4*me2, weightsOnEdge 8*me2, nEdgesOnEdge 1,
+    cellsOnEdge 8, dcEdge 8, areaEdge 8; pv_e, u, gd_edge, iap_u of the stage
+    (own and neighbours, read once: 4S); RK traffic per stage mode
+    (1: old r, tend/acc/next w = 4S; 2,3: tend r+w, acc r+w, old r, next w
+    = 6S; 4: tend r+w, acc r+w = 4S).  Per cell: E (S) and the FP64 gd
+    tendency (8).
+    """
+    mesh = 4 * me2 + 8 * me2 + 1 + 8 + 8 + 8
+    rk = (4 + 6 + 6 + 4) / 4.0
+    return ne * (mesh + (4 + rk) * S) + nc * (S + 8)
+
+
+def step_model_bytes(nc: int, ne: int, nv: int, S: int, ntr: int) -> float:
+    """Compulsory bytes per CRK4 step of the whole path (the per-step model:
+    each mesh array read once per stage, state read/written once per stage;
+    4 stages + the final update), plus the coupled tracers in FP64."""
+    per_stage = 39 * nc + 153 * ne + 67 * nv + 8 * S * nc + 7 * S * ne
+    tracer_stage = ntr * (5 * 8 * nc + 2 * S * ne)
+    return 4 * (per_stage + tracer_stage) + 3 * S * (nc + ne) + ntr * 3 * 8 * nc
+
+
+def ncu_traffic(name: str):
+    """dram bytes per launch from the committed ncu summary, if present."""
+    p = os.path.join(ROOT, "profiles", name)
+    if os.path.exists(p):
+        try:
+            return json.load(open(p)).get("dram_bytes_per_launch")
+        except (ValueError, OSError):
+            return None
+    return None
+
+
+def setup(args):
+    from tmcore_gb300 import cases, mesh
+
+    t0 = time.time()
+    m = mesh.generate_icos(args.level, 20)
+    gd, u, ghs = cases.jet_bumps(m, seed=args.seed)
+    q = cases.smooth_tracers(m, args.tracers, seed=args.seed) if args.tracers else None
+    return m, gd, u, ghs, q, time.time() - t0
+
+
+def gpu_params(args, precision):
+    return dict(dt=args.dt, pv_scheme=1, apvm_weight=0.0, adv_order=2, conserve_energy=1,
+                n_tracers=args.tracers, precision=precision, diag_every=1, use_graph=1, renumber=1)
+
+
+def cpu_baseline(m, gd, u, ghs, q, args, steps: int, threads: int):
+    """Time the CPU FP64 oracle (restatement of the reference) on the same workload."""
+    from oracle.oracle import Oracle
+
+    o = Oracle(m, dt=args.dt, pv_scheme=1, apvm_weight=0.0, adv_order=2, n_tracers=args.tracers, nthreads=threads)
+    o.set_initial(gd, u, ghs)
+    if args.tracers:
+        o.set_tracers(q * gd[None, :])
+    t0 = time.perf_counter()
+    o.step(steps)
+    dt = time.perf_counter() - t0
+    o.close()
+    return steps * args.dt / DAY / dt, dt
+
+
+def run_reference(args, rank, world):
+    """--impl reference: the oracle port on all host cores, same metric and config."""
+    if rank != 0:
+        return
+    m, gd, u, ghs, q, _ = setup(args)
+    threads = os.cpu_count() or 1
+    from oracle.oracle import Oracle
+
+    o = Oracle(m, dt=args.dt, pv_scheme=1, apvm_weight=0.0, adv_order=2, n_tracers=args.tracers, nthreads=threads)
+    o.set_initial(gd, u, ghs)
+    if args.tracers:
+        o.set_tracers(q * gd[None, :])
+    o.step(min(args.warmup, 1))
+    # bounded sample: K steps, stopping early once the timed region passes 150 s
+    t0 = time.perf_counter()
+    done = 0
+    while done < args.steps:
+        o.step(1)
+        done += 1
+        if time.perf_counter() - t0 > 150.0:
+            break
+    el = time.perf_counter() - t0
+    o.close()
+    v = done * args.dt / DAY / el
+    unit = "simulated days/wall-s"
+    line = {
+        "impl": "reference", "metric": "simulated days/wall-s", "value": v, "unit": unit, "n_gpus": world,
+        "steps": done, "steps_requested": args.steps, "warmup": min(args.warmup, 1), "ms_per_step": el / done * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": config_dict(args, m, "FP64 CPU restatement of the reference (oracle port)"),
+        "cpu_baseline": {"value": v, "unit": unit, "cores": threads, "kind": "port",
+                         "sample": f"{done} CRK4 steps of the level-{args.level} workload"},
+        "e2e": {"value": v, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def config_dict(args, m, path):
+    return {"workload": f"level-{args.level} icosahedral SCVT sphere ({m.nCells} cells, {m.nEdges} edges, "
+                        f"{m.nVertices} vertices), seeded jet+mountains, {args.tracers} tracers, CRK4 dt={args.dt:g}s",
+            "path": path, "level": args.level, "nCells": m.nCells, "nEdges": m.nEdges, "nVertices": m.nVertices,
+            "dt_s": args.dt, "tracers": args.tracers, "pv_scheme": 1, "apvm_weight": 0.0, "adv_order": 2,
+            "conserve_energy": True, "seed": args.seed,
+            "l2": "inputs larger than L2 (mesh tables + state > 1 GB per stage)"}
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    import numpy as np
+
+    from tmcore_gb300 import abi
+    from tmcore_gb300.gpu import TMCoreGPU
+
+    dist = Dist(world)
+    m, gd, u, ghs, q, t_setup = setup(args)
+    args.seed += rank  # independent replicas
+    qgd = q * gd[None, :] if args.tracers else None
+
+    gpu = TMCoreGPU(m, **gpu_params(args, abi.TMC_FP32), device=local)
+    gpu.set_initial(gd, u, ghs)
+    if args.tracers:
+        gpu.set_tracers(qgd)
+    gpu.step(args.warmup)
+    gpu.synchronize()
+
+    # ---- timed region: exactly K steps, CUDA graph per step ----
+    clocks = Clocks(local)
+    clocks.start()
+    dist.barrier()
+    gpu.synchronize()
+    ms_total, _, _, launches = gpu.time_steps(args.steps, total=True, flux=False)
+    dist.barrier()
+    clk = clocks.stop()
+    ms_max = dist.max(ms_total)
+    days = world * args.steps * args.dt / DAY
+    value = days / (ms_max / 1e3)
+
+    # ---- dominant kernel (edge flux pass), launch by launch with events ----
+    _, ms_flux, n_flux, _ = gpu.time_steps(max(2, min(args.steps, 10)), total=False, flux=True)
+    S = 4
+    fb = flux_kernel_bytes(m.nCells, m.nEdges, S)
+    t_launch = ms_flux / n_flux / 1e3
+    achieved = fb / t_launch / 1e9
+    peak, peak_kind = measured_peaks()
+    traffic = ncu_traffic("edge_flux_level9_fp32.json")
+
+    step_bytes = step_model_bytes(m.nCells, m.nEdges, m.nVertices, S, args.tracers)
+    step_s = ms_total / args.steps / 1e3
+
+    # ---- FP32 h error against the plain FP64 path after the same steps ----
+    gd32, _, u32 = gpu.get_state()
+    d32 = gpu.diag()
+    extra = {}
+    if not args.no_fp64:
+        g64 = TMCoreGPU(m, **gpu_params(args, abi.TMC_FP64), device=local)
+        g64.set_initial(gd, u, ghs)
+        if args.tracers:
+            g64.set_tracers(qgd)
+        g64.step(args.warmup)
+        g64.synchronize()
+        ms64, _, _, _ = g64.time_steps(args.steps, total=True, flux=False)
+        gd64, _, u64 = g64.get_state()
+        d64 = g64.diag()
+        area = m.areaCell
+        h32, h64 = gd32 / 9.80616, gd64 / 9.80616
+        extra["fp64"] = {
+            "value": args.steps * args.dt / DAY / (ms64 / 1e3), "unit": "simulated days/wall-s",
+            "ms_per_step": ms64 / args.steps,
+            "step_model_gbs": step_model_bytes(m.nCells, m.nEdges, m.nVertices, 8, args.tracers)
+            / (ms64 / args.steps / 1e3) / 1e9}
+        extra["h_error_fp32_vs_fp64"] = {
+            "rel_max": float(np.max(np.abs(h32 - h64)) / np.max(np.abs(h64))),
+            "rel_l2": float(np.sqrt(np.sum(area * (h32 - h64) ** 2) / np.sum(area * h64 ** 2))),
+            "u_rel_max": float(np.max(np.abs(u32 - u64)) / np.max(np.abs(u64))),
+            "after_steps": args.warmup + args.steps + max(2, min(args.steps, 10)),
+            "note": "FP32 run also advanced through the kernel-timing steps; compared at its own step count"}
+        extra["mass_drift_fp32"] = None
+        g64.close()
+    extra["invariants_fp32"] = {"mass": d32[0], "energy": d32[1], "enstrophy": d32[2], "abs_vorticity": d32[3],
+                                "beta": d32[4]}
+
+    # ---- e2e: the C-ABI drop-in for time_integrate with page-locked host arrays ----
+    e2e = None
+    if not args.no_e2e:
+        import torch
+
+        nc, ne, nt = m.nCells, m.nEdges, args.tracers
+        pin = lambda n: torch.empty(n, dtype=torch.float64).pin_memory().numpy()  # noqa: E731
+        gA, iA, gB, iB = pin(nc), pin(ne), pin(nc), pin(ne)
+        qA = pin(nt * nc).reshape(nt, nc) if nt else None
+        qB = pin(nt * nc).reshape(nt, nc) if nt else None
+        g0, i0, _ = gpu.get_state()
+        gA[:] = g0
+        iA[:] = i0
+        if nt:
+            qA[:] = gpu.get_tracers()
+        gpu.time_integrate(gA, iA, qA, out=(gB, iB, qB))  # warm
+        dist.barrier()
+        t0 = time.perf_counter()
+        for k in range(args.steps):
+            if k % 2 == 0:
+                gpu.time_integrate(gB, iB, qB, out=(gA, iA, qA))
+            else:
+                gpu.time_integrate(gA, iA, qA, out=(gB, iB, qB))
+        el = dist.max(time.perf_counter() - t0)
+        bytes_io = 8 * (nc + ne + nt * nc)
+        e2e = {"value": days / el, "unit": "simulated days/wall-s", "h2d_bytes_per_step": bytes_io,
+               "d2h_bytes_per_step": bytes_io, "ms_per_step": el / args.steps * 1e3,
+               "call": "tmc_time_integrate (host state in, host state out, every step)"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        v, el = cpu_baseline(m, gd, u, ghs, q, args, args.cpu_steps, threads)
+        cpu = {"value": v, "unit": "simulated days/wall-s", "cores": threads, "kind": "port",
+               "sample": f"{args.cpu_steps} CRK4 step(s) of the same level-{args.level} workload, FP64 oracle, "
+                         f"{el:.1f} s"}
+    gpu.close()
+    dist.close()
+    if rank != 0:
+        return
+    line = {
+        "metric": "simulated days/wall-s", "value": value, "unit": "simulated days/wall-s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded initial state on a generated mesh)",
+        "config": config_dict(args, m, "FP32 state + FP64 metrics/gd/sums, CUDA graph per CRK4 step"),
+        "clocks": clk,
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "kernel": "k_edge_flux<float>", "achieved": achieved, "peak": peak,
+                     "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                     "algorithmic_bytes_per_launch": fb, "launch_ms": t_launch * 1e3, "launches_timed": n_flux},
+        "step_roofline": {"model_bytes_per_step": step_bytes, "achieved_gbs": step_bytes / step_s / 1e9,
+                          "frac": step_bytes / step_s / 1e9 / peak},
+        "e2e": e2e,
+        "cpu_baseline": cpu,
+        "setup_s": t_setup,
+        **extra,
+    }
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

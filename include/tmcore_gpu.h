@@ -1,0 +1,156 @@
+/* tmcore_gpu.h - C ABI of the GB300 (sm_103a) TRiSK shallow-water library.
+ *
+ * Drop-in for the integrator and operator boundary of TMCORE
+ * (TMCORE-Project/TMCORE).  The Fortran host keeps the namelist, mesh / state
+ * I/O, logging and test cases; it calls these entry points through
+ * iso_c_binding (binding module in INTEGRATION.md).  Every entry point returns
+ * 0 on success or a negative TMC_E* code, never exits or aborts; the message
+ * of the last failure is tmc_last_error(h).  A handle owns one CUDA stream;
+ * calls on one handle must not overlap (one handle per host thread).
+ *
+ * Element order at this ABI is always the caller's (the mesh file's) order;
+ * the space-filling-curve renumbering used on the device is internal.
+ * Unless stated otherwise, array arguments are HOST pointers.
+ */
+#ifndef TMCORE_GPU_H
+#define TMCORE_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TMC_OK 0
+#define TMC_E_ARG (-1)      /* bad argument or configuration */
+#define TMC_E_CUDA (-2)     /* CUDA runtime error (message in tmc_last_error) */
+#define TMC_E_HEALTH (-3)   /* non-finite or non-positive depth detected */
+#define TMC_E_UNSUP (-4)    /* option combination not implemented on the device */
+#define TMC_E_STATE (-5)    /* call out of order (e.g. step before set_state) */
+
+#define TMC_FP64 0 /* FP64 state and arithmetic; per element bit-identical to the reference order */
+#define TMC_FP32 1 /* FP32 edge/vertex state and stencil arithmetic; FP64 metrics, gd and sums */
+
+/* The MPAS grid exactly as src/core/mesh_mod.F90:130-167 reads it: unit
+ * sphere, int32 1-based connectivity, Fortran (k, n) column-major arrays
+ * (maxEdges = 6 or more, maxEdges2, vertexDegree = 3).  The library performs
+ * the derivations of mesh_mod.F90:169-224 itself (areaEdge, fVertex,
+ * nSignEdge, tSignEdge, verticesOnVertex, radius scaling, totalArea) and
+ * copies everything; the caller keeps ownership of its arrays. */
+typedef struct tmc_mesh_desc {
+  int32_t nCells, nEdges, nVertices, maxEdges, maxEdges2, vertexDegree;
+  const int32_t *nEdgesOnCell, *nEdgesOnEdge;
+  const int32_t *cellsOnCell, *edgesOnCell, *verticesOnCell; /* (maxEdges, nCells) */
+  const int32_t *cellsOnEdge, *verticesOnEdge;               /* (2, nEdges) */
+  const int32_t *edgesOnEdge;                                /* (maxEdges2, nEdges) */
+  const int32_t *cellsOnVertex, *edgesOnVertex;              /* (vertexDegree, nVertices) */
+  const double *xCell, *yCell, *zCell, *latCell;
+  const double *xEdge, *yEdge, *zEdge;
+  const double *xVertex, *yVertex, *zVertex, *latVertex;
+  const double *dvEdge, *dcEdge, *areaCell, *areaTriangle;
+  const double *kiteAreasOnVertex; /* (vertexDegree, nVertices) */
+  const double *weightsOnEdge;     /* (maxEdges2, nEdges) */
+} tmc_mesh_desc;
+
+/* namelist &tmcore (src/core/params_mod.F90:35-55), const_mod constants,
+ * plus device options. */
+typedef struct tmc_params {
+  double dt;
+  int32_t time_scheme;            /* 2 = CRK4 (time_scheme_mod.F90:109-154) */
+  int32_t pv_scheme;              /* 1 APVM, 3 high-order upwind */
+  int32_t conserve_energy;        /* CRK4 beta (time_scheme_mod.F90:144-150) */
+  int32_t flux_4th_order_correct; /* must be 0 on the device */
+  double apvm_weight;
+  int32_t adv_order;              /* 2..6, upwind correction of gd on edges */
+  int32_t adv_mono;
+  int32_t interp_pv_order;        /* 3..6 for pv_scheme 3 */
+  double radius, g, omega;        /* const_mod.F90:11-13 */
+  int32_t n_tracers;              /* coupled mass-weighted tracers gd*q */
+  int32_t tracer_adv_order;       /* 0: adv_order */
+  int32_t tracer_adv_mono;
+  int32_t precision;              /* TMC_FP64 or TMC_FP32 */
+  int32_t renumber;               /* 1: space-filling-curve renumbering at load */
+  int32_t use_graph;              /* 1: one CUDA graph per RK step */
+  int32_t diag_every;             /* invariants of the state every k steps (0: only on request) */
+  int32_t device;                 /* CUDA device ordinal */
+  int32_t block_size;             /* threads per block, 0 = tuned default */
+  int32_t stencils;               /* 1: always build the poly-fit stencil tables (else only when used) */
+  int32_t reserved[6];
+} tmc_params;
+
+typedef struct tmc_handle tmc_handle;
+
+/* Fill *p with the shipped SWM namelist (run/namelist.tmcore_swm) defaults. */
+int tmc_default_params(tmc_params* p);
+
+/* Replaces mesh_init + poly_fit_init + state/tend allocation
+ * (src/core/tmcore_swm_mod.F90:29-47): copies and renumbers the mesh, builds
+ * the stencil tables and allocates device state. */
+int tmc_create(const tmc_mesh_desc* mesh, const tmc_params* params, tmc_handle** out);
+int tmc_destroy(tmc_handle* h);
+const char* tmc_last_error(const tmc_handle* h);
+
+/* Initial condition: state(old)%cell%gd, state(old)%edge%u and
+ * static%cell%ghs; runs the pre-loop of tmcore_swm_run
+ * (tmcore_swm_mod.F90:62-71): gd_edge, iap_u = sqrt(gd_edge) u, invariants. */
+int tmc_set_initial(tmc_handle* h, const double* gd, const double* u, const double* ghs);
+/* Prognostic state(old) (gd on cells, iap_u on edges). */
+int tmc_set_state(tmc_handle* h, const double* gd, const double* iap_u);
+int tmc_get_state(tmc_handle* h, double* gd, double* iap_u, double* u);
+/* Diagnostic pv and vorticity on vertices of state(old). */
+int tmc_get_vertex(tmc_handle* h, double* pv, double* vor);
+/* Coupled tracers, mass weighted gd*q, [n_tracers][nCells]. */
+int tmc_set_tracers(tmc_handle* h, const double* qgd);
+int tmc_get_tracers(tmc_handle* h, double* qgd);
+
+/* nsteps iterations of tmcore_swm_run's loop body (tmcore_swm_mod.F90:75-88):
+ * time_integrate (time_scheme_mod.F90:47-63) + time_advance; state stays on
+ * the device.  Asynchronous unless an error is detected at launch. */
+int tmc_step(tmc_handle* h, int32_t nsteps);
+/* {total_mass, total_energy, total_potential_enstrophy,
+ *  total_absolute_vorticity, beta} of state(old) (tmcore_swm_mod.F90:215-255,
+ *  diag_mod.F90:76-91); synchronises. */
+int tmc_get_diag(tmc_handle* h, double out[5]);
+int tmc_synchronize(tmc_handle* h);
+
+/* time_integrate with host arrays: state(old) in, state(new) out, one step
+ * (the whole drop-in for time_integrate at tmcore_swm_mod.F90:76).  qgd_old /
+ * qgd_new are the coupled tracers ([n_tracers][nCells]) or NULL when
+ * n_tracers = 0.  Page-locked host arrays give the fastest copies. */
+int tmc_time_integrate(tmc_handle* h, const double* gd_old, const double* iap_u_old, const double* qgd_old,
+                       double* gd_new, double* iap_u_new, double* qgd_new);
+
+/* One call of spatial_operators (tmcore_swm_mod.F90:92-125). */
+int tmc_spatial_operators(tmc_handle* h, const double* gd, const double* iap_u, double* tend_gd,
+                          double* tend_iap_u);
+
+/* Single operators of operators_mod.F90 (fine-grained parity, host arrays). */
+int tmc_op_div(tmc_handle* h, const double* f_edge, double* div_cell);                 /* :40-55 */
+int tmc_op_curl(tmc_handle* h, const double* f_edge, double* curl_vertex);             /* :76-91 */
+int tmc_op_c2e(tmc_handle* h, const double* f_cell, double* f_edge);                   /* :93-104 */
+int tmc_op_c2v(tmc_handle* h, const double* f_cell, double* f_vertex);                 /* :106-123 */
+int tmc_op_v2c(tmc_handle* h, const double* f_vertex, double* f_cell);                 /* :125-141 */
+int tmc_op_v2e(tmc_handle* h, const double* f_vertex, double* f_edge);                 /* :143-156 */
+int tmc_op_kinetic_energy(tmc_handle* h, const double* u_edge, double* ke_cell);       /* :206-221 */
+int tmc_op_tangent_wind(tmc_handle* h, const double* u_edge, double* v_edge);          /* :223-237 */
+int tmc_op_tangent_vor_flux(tmc_handle* h, const double* u_edge, const double* gd_edge, /* :239-260 */
+                            const double* pv_edge, double* out_edge);
+int tmc_op_upwind_correction(tmc_handle* h, const double* f_cell, const double* u_edge, /* :423-472 */
+                             double* f_edge_inout, int32_t order, int32_t mono);
+
+/* Timing of the device path (CUDA events on the handle's stream).  If
+ * ms_total is not NULL, nsteps steps run as tmc_step runs them (CUDA graph)
+ * and *ms_total is their device time.  If ms_flux_kernel is not NULL, a
+ * further nsteps steps run launch by launch with events around every edge
+ * flux pass (the dominant kernel) and *ms_flux_kernel is the sum of those. */
+int tmc_time_steps(tmc_handle* h, int32_t nsteps, double* ms_total, double* ms_flux_kernel,
+                   int32_t* flux_launches, int32_t* total_launches);
+
+/* Number of elements after load, and bytes of device memory held. */
+int tmc_sizes(const tmc_handle* h, int64_t* nCells, int64_t* nEdges, int64_t* nVertices, int64_t* device_bytes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

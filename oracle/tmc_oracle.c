@@ -1,0 +1,1365 @@
+/* TEST INFRASTRUCTURE ONLY - CPU FP64 oracle of TMCORE's hot path.
+ * See tmc_oracle.h for scope and the "parity unpinned" statement.
+ *
+ * Indexing: connectivity is kept exactly as read (1-based, Fortran (k, n)
+ * column-major), and the accessors below take 1-based (k, n) arguments so each
+ * loop reads like the Fortran it restates.  Field arrays are 0-based C arrays
+ * accessed with [idx - 1].
+ */
+#include "tmc_oracle.h"
+
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define MAXFIT 30 /* poly_fit_mod.F90:33 maxFitCells */
+#define NFIT (MAXFIT + 1)
+
+typedef struct {
+  double *c_gd, *c_ke, *c_pv;
+  double *e_gd, *e_u, *e_v, *e_pv, *e_pv_flx, *e_iap_u;
+  double *v_gd, *v_vor, *v_pv;
+  double *qgd; /* coupled tracers (gd*q), [ntr][nc] */
+  double total_mass, total_energy, total_pe, total_av;
+} orc_state;
+
+typedef struct {
+  double *c_gd, *e_gd, *e_u, *e_iap_u, *v_gd;
+  double *qgd;
+} orc_tend;
+
+struct orc_model {
+  orc_params p;
+  int nc, ne, nv, me, me2, vd;
+  /* connectivity as read */
+  int32_t *nEdgesOnCell, *nEdgesOnEdge, *nCellsOnVertex;
+  int32_t *cellsOnCell, *edgesOnCell, *verticesOnCell, *cellsOnEdge, *verticesOnEdge, *edgesOnEdge;
+  int32_t *cellsOnVertex, *edgesOnVertex, *verticesOnVertex;
+  int32_t *nSignEdge, *tSignEdge;
+  /* geometry (radius-scaled after derive) */
+  double *xCell, *yCell, *zCell, *latCell, *lonCell, *xVertex, *yVertex, *zVertex, *latVertex, *lonVertex;
+  double *dvEdge, *dcEdge, *areaCell, *areaTriangle, *areaEdge, *kiteAreasOnVertex, *weightsOnEdge;
+  double *fCell, *fVertex;
+  double totalArea;
+  /* poly_fit tables */
+  int32_t *nFit2Cells, *nFit3Cells, *nFit4Cells, *nFit2Vertices, *nFit3Vertices, *nFit4Vertices;
+  int32_t *fit2Cells, *fit3Cells, *fit4Cells, *fit2Vertices, *fit3Vertices, *fit4Vertices; /* (0:30, n) */
+  double *deriv2OnCell, *deriv3OnCell, *deriv4OnCell, *deriv2OnVertex, *deriv4OnVertex;  /* (0:30,2,ne) */
+  /* SAVE'd locals of the upwind routines (operators_mod.F90:367-368, :429-430) */
+  double upw_cell_coef4, upw_vtx_coef4;
+  /* model */
+  orc_state state[7]; /* index slot + 4: state(-4:2) */
+  orc_tend tend[7];
+  double *ghs;
+  int old, new_;
+  double beta;
+  double elapsed;
+  int time_step;
+  int adv_wind_case;
+  double *tmp_e1, *tmp_e2, *tmp_e3, *tmp_v1, *tmp_v2, *tmp_c1, *tmp_c2; /* automatic arrays */
+  char err[256];
+};
+
+/* ---- accessors mirroring Fortran indexing (1-based) ---- */
+#define EOC(i, c) m->edgesOnCell[(size_t)((c)-1) * m->me + ((i)-1)]
+#define COC(i, c) m->cellsOnCell[(size_t)((c)-1) * m->me + ((i)-1)]
+#define VOC(i, c) m->verticesOnCell[(size_t)((c)-1) * m->me + ((i)-1)]
+#define NSIGN(i, c) m->nSignEdge[(size_t)((c)-1) * m->me + ((i)-1)]
+#define COE(i, e) m->cellsOnEdge[(size_t)((e)-1) * 2 + ((i)-1)]
+#define VOE(i, e) m->verticesOnEdge[(size_t)((e)-1) * 2 + ((i)-1)]
+#define EOE(i, e) m->edgesOnEdge[(size_t)((e)-1) * m->me2 + ((i)-1)]
+#define WOE(i, e) m->weightsOnEdge[(size_t)((e)-1) * m->me2 + ((i)-1)]
+#define COV(i, v) m->cellsOnVertex[(size_t)((v)-1) * m->vd + ((i)-1)]
+#define EOV(i, v) m->edgesOnVertex[(size_t)((v)-1) * m->vd + ((i)-1)]
+#define VOV(i, v) m->verticesOnVertex[(size_t)((v)-1) * m->vd + ((i)-1)]
+#define TSIGN(i, v) m->tSignEdge[(size_t)((v)-1) * m->vd + ((i)-1)]
+#define KITE(i, v) m->kiteAreasOnVertex[(size_t)((v)-1) * m->vd + ((i)-1)]
+#define FIT(a, k, n) (a)[(size_t)((n)-1) * NFIT + (k)]                     /* a(k, n), k in 0:30 */
+#define DER(a, k, s, e) (a)[((size_t)((e)-1) * 2 + ((s)-1)) * NFIT + (k)] /* a(k, s, e) */
+#define A1(a, i) (a)[(i)-1]
+
+static void* xcalloc(size_t n, size_t s) {
+  void* p = calloc(n ? n : 1, s);
+  if (!p) {
+    fprintf(stderr, "oracle: out of memory\n");
+    abort();
+  }
+  return p;
+}
+static double* dalloc(size_t n) { return (double*)xcalloc(n, sizeof(double)); }
+static int32_t* ialloc(size_t n) { return (int32_t*)xcalloc(n, sizeof(int32_t)); }
+static void* dup(const void* src, size_t bytes) {
+  void* p = xcalloc(bytes, 1);
+  if (src) memcpy(p, src, bytes);
+  return p;
+}
+
+void orc_default_params(orc_params* p) {
+  memset(p, 0, sizeof(*p));
+  p->dt = 600.0;
+  p->time_scheme = 2;
+  p->pv_scheme = 1;
+  p->conserve_energy = 1;
+  p->flux_4th_order_correct = 0;
+  p->apvm_weight = 0.5; /* params_mod.F90:29 */
+  p->adv_order = 2;
+  p->adv_mono = 0;
+  p->interp_pv_order = 3;
+  p->radius = 6371220.0; /* const_mod.F90:11-13 */
+  p->g = 9.80616;
+  p->omega = 7.292e-5;
+}
+
+/* ======================= math / geometry (init only) ======================= */
+
+/* math_mod.F90:90-133 gaussian_elimination; A is (n,n) column-major, 1-based macro */
+#define MA(i, j) A[(size_t)((j)-1) * n + ((i)-1)]
+static void gaussian_elimination(int n, double* A, int* ipiv) {
+  double c[MAXFIT + 1];
+  int i, j, k = 1, itmp;
+  for (i = 1; i <= n; ++i) ipiv[i] = i;
+  for (i = 1; i <= n; ++i) {
+    double c1 = 0.0;
+    for (j = 1; j <= n; ++j) c1 = fmax(c1, fabs(MA(i, j)));
+    c[i] = c1;
+  }
+  for (j = 1; j <= n - 1; ++j) {
+    double pi1 = 0.0;
+    for (i = j; i <= n; ++i) {
+      double pi = fabs(MA(ipiv[i], j)) / c[ipiv[i]];
+      if (pi > pi1) {
+        pi1 = pi;
+        k = i;
+      }
+    }
+    itmp = ipiv[j];
+    ipiv[j] = ipiv[k];
+    ipiv[k] = itmp;
+    for (i = j + 1; i <= n; ++i) {
+      double pj = MA(ipiv[i], j) / MA(ipiv[j], j);
+      MA(ipiv[i], j) = pj;
+      for (int kk = j + 1; kk <= n; ++kk) MA(ipiv[i], kk) = MA(ipiv[i], kk) - pj * MA(ipiv[j], kk);
+    }
+  }
+}
+
+/* math_mod.F90:52-88 math_inv_matrix (A destroyed, B = A^-1) */
+static void math_inv_matrix(int n, double* A, double* B) {
+  double C[(MAXFIT) * (MAXFIT)];
+  int ipiv[MAXFIT + 1];
+#define MC(i, j) C[(size_t)((j)-1) * n + ((i)-1)]
+#define MB(i, j) B[(size_t)((j)-1) * n + ((i)-1)]
+  for (int j = 1; j <= n; ++j)
+    for (int i = 1; i <= n; ++i) MC(i, j) = (i == j) ? 1.0 : 0.0;
+  gaussian_elimination(n, A, ipiv);
+  for (int i = 1; i <= n - 1; ++i)
+    for (int j = i + 1; j <= n; ++j)
+      for (int k = 1; k <= n; ++k) MC(ipiv[j], k) = MC(ipiv[j], k) - MA(ipiv[j], i) * MC(ipiv[i], k);
+  for (int i = 1; i <= n; ++i) {
+    MB(n, i) = MC(ipiv[n], i) / MA(ipiv[n], n);
+    for (int j = n - 1; j >= 1; --j) {
+      MB(j, i) = MC(ipiv[j], i);
+      for (int k = j + 1; k <= n; ++k) MB(j, i) = MB(j, i) - MA(ipiv[j], k) * MB(k, i);
+      MB(j, i) = MB(j, i) / MA(ipiv[j], j);
+    }
+  }
+#undef MC
+#undef MB
+}
+#undef MA
+
+static void cross3(const double* x, const double* y, double* r) {
+  r[0] = x[1] * y[2] - x[2] * y[1];
+  r[1] = x[2] * y[0] - x[0] * y[2];
+  r[2] = x[0] * y[1] - x[1] * y[0];
+}
+static double dot3(const double* a, const double* b) {
+  double s = 0.0; /* dot_product accumulates in order */
+  s = s + a[0] * b[0];
+  s = s + a[1] * b[1];
+  s = s + a[2] * b[2];
+  return s;
+}
+/* sphere_geometry_mod.F90:186-200 norm_vector */
+static void norm_vector(double* x) {
+  double s = 0.0;
+  for (int i = 0; i < 3; ++i) s = s + x[i] * x[i];
+  double n = sqrt(s);
+  if (n != 0) {
+    for (int i = 0; i < 3; ++i) x[i] = x[i] / n;
+  }
+}
+/* sphere_geometry_mod.F90:204-220 calc_sphere_angle */
+static double calc_sphere_angle(const double* a, const double* b, const double* c) {
+  double nab[3], nac[3], bma[3], cma[3], t[3];
+  cross3(a, b, nab);
+  norm_vector(nab);
+  cross3(a, c, nac);
+  norm_vector(nac);
+  double res = acos(fmax(fmin(dot3(nab, nac), 1.0), -1.0));
+  for (int i = 0; i < 3; ++i) {
+    bma[i] = b[i] - a[i];
+    cma[i] = c[i] - a[i];
+  }
+  cross3(bma, cma, t);
+  if (dot3(t, a) < 0.0) res = -res;
+  return res;
+}
+/* sphere_geometry_mod.F90:245-252 calc_arc_length */
+static double calc_arc_length(const double* a, const double* b) {
+  return acos(fmax(fmin(dot3(a, b), 1.0), -1.0));
+}
+
+/* ======================= mesh_init derived quantities ======================= */
+/* mesh_mod.F90:169-224 */
+static void mesh_derive(orc_model* m) {
+  const double radius = m->p.radius, omega = m->p.omega;
+  for (int v = 1; v <= m->nv; ++v) A1(m->nCellsOnVertex, v) = m->vd;
+  for (int e = 1; e <= m->ne; ++e) A1(m->areaEdge, e) = A1(m->dvEdge, e) * A1(m->dcEdge, e);
+  for (int c = 1; c <= m->nc; ++c) A1(m->fCell, c) = 2.0 * omega * sin(A1(m->latCell, c));
+  for (int v = 1; v <= m->nv; ++v) A1(m->fVertex, v) = 2.0 * omega * sin(A1(m->latVertex, v));
+  for (int c = 1; c <= m->nc; ++c)
+    for (int i = 1; i <= A1(m->nEdgesOnCell, c); ++i) {
+      if (c == COE(1, EOC(i, c))) NSIGN(i, c) = 1;
+      if (c == COE(2, EOC(i, c))) NSIGN(i, c) = -1;
+    }
+  for (int v = 1; v <= m->nv; ++v)
+    for (int i = 1; i <= m->vd; ++i) {
+      if (v == VOE(1, EOV(i, v))) {
+        TSIGN(i, v) = 1;
+        VOV(i, v) = VOE(2, EOV(i, v));
+      }
+      if (v == VOE(2, EOV(i, v))) {
+        TSIGN(i, v) = -1;
+        VOV(i, v) = VOE(1, EOV(i, v));
+      }
+    }
+  const double r2 = radius * radius;
+  for (int c = 0; c < m->nc; ++c) {
+    m->xCell[c] *= radius;
+    m->yCell[c] *= radius;
+    m->zCell[c] *= radius;
+  }
+  for (int v = 0; v < m->nv; ++v) {
+    m->xVertex[v] *= radius;
+    m->yVertex[v] *= radius;
+    m->zVertex[v] *= radius;
+  }
+  for (int e = 0; e < m->ne; ++e) {
+    m->dvEdge[e] *= radius;
+    m->dcEdge[e] *= radius;
+  }
+  for (int c = 0; c < m->nc; ++c) m->areaCell[c] *= r2;
+  for (int v = 0; v < m->nv; ++v) m->areaTriangle[v] *= r2;
+  for (int e = 0; e < m->ne; ++e) m->areaEdge[e] *= r2;
+  for (size_t k = 0; k < (size_t)m->nv * m->vd; ++k) m->kiteAreasOnVertex[k] *= r2;
+  double s = 0.0;
+  for (int c = 0; c < m->nc; ++c) s = s + m->areaCell[c];
+  m->totalArea = s;
+}
+
+/* ======================= poly_fit (init only) ======================= */
+
+/* Least-squares fit B(1:n,1:m) = inv(P^T W^T W P) P^T W^T W with W = I
+ * (poly_fit_mod.F90:209-230).  P is (MAXFIT, MAXFIT) column-major. */
+#define PM(a, i, j) (a)[(size_t)((j)-1) * MAXFIT + ((i)-1)]
+static void lsq_fit(int mm, int n, const double* xp, const double* yp, double* B) {
+  double P[MAXFIT * MAXFIT], PT[MAXFIT * MAXFIT], PTWTW[MAXFIT * MAXFIT], PTWTWP[MAXFIT * MAXFIT];
+  double Ainv[MAXFIT * MAXFIT], Bnn[MAXFIT * MAXFIT], Ab[MAXFIT * MAXFIT];
+  memset(P, 0, sizeof(P));
+  memset(B, 0, sizeof(double) * MAXFIT * MAXFIT);
+  for (int i = 1; i <= mm; ++i) {
+    double x = xp[i], y = yp[i];
+    PM(P, i, 1) = x;
+    PM(P, i, 2) = y;
+    PM(P, i, 3) = x * x;
+    PM(P, i, 4) = x * y;
+    PM(P, i, 5) = y * y;
+    if (n >= 9) {
+      PM(P, i, 6) = x * x * x; /* xp**3 */
+      PM(P, i, 7) = y * (x * x);
+      PM(P, i, 8) = x * (y * y);
+      PM(P, i, 9) = y * y * y;
+    }
+    if (n >= 14) {
+      PM(P, i, 10) = (x * x) * (x * x); /* xp**4 */
+      PM(P, i, 11) = y * (x * x * x);
+      PM(P, i, 12) = (x * x) * (y * y);
+      PM(P, i, 13) = x * (y * y * y);
+      PM(P, i, 14) = (y * y) * (y * y);
+    }
+  }
+  /* WTW = I, PT = P^T, PTWTW = PT * I = PT exactly */
+  for (int i = 1; i <= n; ++i)
+    for (int j = 1; j <= mm; ++j) {
+      PM(PT, i, j) = PM(P, j, i);
+      PM(PTWTW, i, j) = PM(P, j, i);
+    }
+  for (int i = 1; i <= n; ++i)
+    for (int j = 1; j <= n; ++j) {
+      double s = 0.0;
+      for (int k = 1; k <= mm; ++k) s = s + PM(PTWTW, i, k) * PM(P, k, j);
+      PM(PTWTWP, i, j) = s;
+    }
+  /* math_inv_matrix on the leading n x n block (packed as n x n) */
+  for (int j = 1; j <= n; ++j)
+    for (int i = 1; i <= n; ++i) Ab[(size_t)(j - 1) * n + (i - 1)] = PM(PTWTWP, i, j);
+  math_inv_matrix(n, Ab, Ainv);
+  for (int j = 1; j <= n; ++j)
+    for (int i = 1; i <= n; ++i) PM(Bnn, i, j) = Ainv[(size_t)(j - 1) * n + (i - 1)];
+  for (int i = 1; i <= n; ++i)
+    for (int j = 1; j <= mm; ++j) {
+      double s = 0.0;
+      for (int k = 1; k <= n; ++k) s = s + PM(Bnn, i, k) * PM(PTWTW, k, j);
+      PM(B, i, j) = s;
+    }
+  (void)PT;
+}
+
+/* projected coordinates of fit points (poly_fit_mod.F90:187-207) */
+static void project(const orc_model* m, const int32_t* fit, int nfit, const double* X, const double* Y,
+                    const double* Z, double* xp, double* yp, double* theta) {
+  double xc[NFIT][3];
+  const double radius = m->p.radius;
+  for (int i = 0; i <= nfit - 1; ++i) {
+    int id = fit[i];
+    xc[i][0] = A1(X, id) / radius;
+    xc[i][1] = A1(Y, id) / radius;
+    xc[i][2] = A1(Z, id) / radius;
+  }
+  xp[0] = 0.0;
+  yp[0] = 0.0;
+  for (int i = 1; i <= nfit - 1; ++i) {
+    theta[i] = calc_sphere_angle(xc[0], xc[1], xc[i]);
+    double d = radius * calc_arc_length(xc[0], xc[i]);
+    xp[i] = cos(theta[i]) * d;
+    yp[i] = sin(theta[i]) * d;
+  }
+}
+
+/* poly_fit_mod.F90:119-609 poly_fit_run */
+static void poly_fit_run(orc_model* m) {
+  double xp[NFIT], yp[NFIT], theta[NFIT], B[MAXFIT * MAXFIT];
+  for (int iCell = 1; iCell <= m->nc; ++iCell) {
+    int nE = A1(m->nEdgesOnCell, iCell);
+    FIT(m->fit2Cells, 0, iCell) = iCell;
+    FIT(m->fit4Cells, 0, iCell) = iCell;
+    for (int i = 1; i <= nE; ++i) {
+      FIT(m->fit2Cells, i, iCell) = COC(i, iCell);
+      FIT(m->fit4Cells, i, iCell) = COC(i, iCell);
+    }
+    A1(m->nFit2Cells, iCell) = nE + 1;
+    A1(m->nFit4Cells, iCell) = nE + 1;
+    for (int i = 1; i <= nE; ++i) {
+      int fi = FIT(m->fit4Cells, i, iCell);
+      for (int j = 1; j <= A1(m->nEdgesOnCell, fi); ++j) {
+        int iNgb = COC(j, fi);
+        int recorded = 0;
+        for (int k = 0; k <= A1(m->nFit4Cells, iCell) - 1; ++k)
+          if (iNgb == FIT(m->fit4Cells, k, iCell)) {
+            recorded = 1;
+            break;
+          }
+        if (!recorded) {
+          FIT(m->fit4Cells, A1(m->nFit4Cells, iCell), iCell) = iNgb;
+          A1(m->nFit4Cells, iCell) += 1;
+        }
+      }
+    }
+    for (int k = 0; k < NFIT; ++k) FIT(m->fit3Cells, k, iCell) = FIT(m->fit4Cells, k, iCell);
+    A1(m->nFit3Cells, iCell) = A1(m->nFit4Cells, iCell);
+
+    /* second-order fit (:184-245) */
+    int nf = A1(m->nFit2Cells, iCell);
+    project(m, &FIT(m->fit2Cells, 0, iCell), nf, m->xCell, m->yCell, m->zCell, xp, yp, theta);
+    lsq_fit(nf - 1, 5, xp, yp, B);
+    for (int i = 1; i <= nE; ++i) {
+      int iEdge = EOC(i, iCell);
+      int k = (iCell == COE(1, iEdge)) ? 1 : 2;
+      double ct = cos(theta[i]), st = sin(theta[i]);
+      for (int j = 1; j <= nf - 1; ++j) {
+        double d2fdx2 = 2.0 * PM(B, 3, j) * (ct * ct);
+        double d2fdxdy = PM(B, 4, j) * ct * st;
+        double d2fdy2 = 2.0 * PM(B, 5, j) * (st * st);
+        DER(m->deriv2OnCell, j, k, iEdge) = d2fdx2 + 2.0 * d2fdxdy + d2fdy2;
+      }
+    }
+    /* third-order fit (:247-316).  The reference assigns d3fdx2dy twice and
+     * never sets d3fdxdy2 (:310-314); the restatement takes d3fdxdy2 = 0. */
+    nf = A1(m->nFit3Cells, iCell);
+    project(m, &FIT(m->fit3Cells, 0, iCell), nf, m->xCell, m->yCell, m->zCell, xp, yp, theta);
+    lsq_fit(nf - 1, 9, xp, yp, B);
+    for (int i = 1; i <= nE; ++i) {
+      int iEdge = EOC(i, iCell);
+      int k = (iCell == COE(1, iEdge)) ? 1 : 2;
+      double ct = cos(theta[i]), st = sin(theta[i]);
+      for (int j = 1; j <= nf - 1; ++j) {
+        double d3fdx3 = 6.0 * PM(B, 6, j) * (ct * ct * ct);
+        double d3fdx2dy = 2.0 * PM(B, 7, j) * (ct * ct) * st;
+        d3fdx2dy = 2.0 * PM(B, 8, j) * ct * (st * st);
+        double d3fdxdy2 = 0.0;
+        double d3fdy3 = 6.0 * PM(B, 9, j) * (st * st * st);
+        DER(m->deriv3OnCell, j, k, iEdge) = d3fdx3 + 3.0 * d3fdx2dy + 3.0 * d3fdxdy2 + d3fdy3;
+      }
+    }
+    /* fourth-order fit (:318-393) */
+    nf = A1(m->nFit4Cells, iCell);
+    project(m, &FIT(m->fit4Cells, 0, iCell), nf, m->xCell, m->yCell, m->zCell, xp, yp, theta);
+    lsq_fit(nf - 1, 14, xp, yp, B);
+    for (int i = 1; i <= nE; ++i) {
+      int iEdge = EOC(i, iCell);
+      int k = (iCell == COE(1, iEdge)) ? 1 : 2;
+      double ct = cos(theta[i]), st = sin(theta[i]);
+      for (int j = 1; j <= nf - 1; ++j) {
+        double a = 24.0 * PM(B, 10, j) * ((ct * ct) * (ct * ct));
+        double b = 6.0 * PM(B, 11, j) * (ct * ct * ct) * st;
+        double c = 4.0 * PM(B, 12, j) * (ct * ct) * (st * st);
+        double d = 6.0 * PM(B, 13, j) * ct * (st * st * st);
+        double e = 24.0 * PM(B, 14, j) * ((st * st) * (st * st));
+        DER(m->deriv4OnCell, j, k, iEdge) = a + 4.0 * b + 6.0 * c + 4.0 * d + e;
+      }
+    }
+  }
+
+  for (int iVertex = 1; iVertex <= m->nv; ++iVertex) {
+    FIT(m->fit2Vertices, 0, iVertex) = iVertex;
+    FIT(m->fit3Vertices, 0, iVertex) = iVertex;
+    FIT(m->fit4Vertices, 0, iVertex) = iVertex;
+    for (int i = 1; i <= m->vd; ++i) FIT(m->fit2Vertices, i, iVertex) = VOV(i, iVertex);
+    A1(m->nFit2Vertices, iVertex) = 4;
+    for (int i = 1; i <= m->vd; ++i) {
+      int haloCell = COV(i, iVertex);
+      for (int j = 1; j <= A1(m->nEdgesOnCell, haloCell); ++j) {
+        int iNgb = VOC(j, haloCell);
+        int recorded = 0;
+        for (int k = 0; k <= A1(m->nFit2Vertices, iVertex) - 1; ++k)
+          if (iNgb == FIT(m->fit2Vertices, k, iVertex)) {
+            recorded = 1;
+            break;
+          }
+        if (!recorded) {
+          FIT(m->fit2Vertices, A1(m->nFit2Vertices, iVertex), iVertex) = iNgb;
+          A1(m->nFit2Vertices, iVertex) += 1;
+        }
+      }
+    }
+    A1(m->nFit3Vertices, iVertex) = A1(m->nFit2Vertices, iVertex);
+    A1(m->nFit4Vertices, iVertex) = A1(m->nFit2Vertices, iVertex);
+    for (int k = 0; k < NFIT; ++k) {
+      FIT(m->fit3Vertices, k, iVertex) = FIT(m->fit2Vertices, k, iVertex);
+      FIT(m->fit4Vertices, k, iVertex) = FIT(m->fit2Vertices, k, iVertex);
+    }
+    for (int ivv = 1; ivv <= m->vd; ++ivv) {
+      int haloVertex = VOV(ivv, iVertex);
+      for (int i = 1; i <= m->vd; ++i) {
+        int haloCell = COV(i, haloVertex);
+        for (int j = 1; j <= A1(m->nEdgesOnCell, haloCell); ++j) {
+          int iNgb = VOC(j, haloCell);
+          int recorded = 0;
+          for (int k = 0; k <= A1(m->nFit4Vertices, iVertex) - 1; ++k)
+            if (iNgb == FIT(m->fit4Vertices, k, iVertex)) {
+              recorded = 1;
+              break;
+            }
+          if (!recorded) {
+            FIT(m->fit4Vertices, A1(m->nFit4Vertices, iVertex), iVertex) = iNgb;
+            A1(m->nFit4Vertices, iVertex) += 1;
+          }
+        }
+      }
+    }
+    /* second-order fit (:465-527) */
+    int nf = A1(m->nFit2Vertices, iVertex);
+    project(m, &FIT(m->fit2Vertices, 0, iVertex), nf, m->xVertex, m->yVertex, m->zVertex, xp, yp, theta);
+    lsq_fit(nf - 1, 5, xp, yp, B);
+    for (int i = 1; i <= m->vd; ++i) {
+      int iEdge = EOV(i, iVertex);
+      int k = (iVertex == VOE(1, iEdge)) ? 1 : 2;
+      double ct = cos(theta[i]), st = sin(theta[i]);
+      for (int j = 1; j <= nf - 1; ++j) {
+        double d2fdx2 = 2.0 * PM(B, 3, j) * (ct * ct);
+        double d2fdxdy = PM(B, 4, j) * ct * st;
+        double d2fdy2 = 2.0 * PM(B, 5, j) * (st * st);
+        DER(m->deriv2OnVertex, j, k, iEdge) = d2fdx2 + 2.0 * d2fdxdy + d2fdy2;
+      }
+    }
+    /* fourth-order fit (:529-605) */
+    nf = A1(m->nFit4Vertices, iVertex);
+    project(m, &FIT(m->fit4Vertices, 0, iVertex), nf, m->xVertex, m->yVertex, m->zVertex, xp, yp, theta);
+    lsq_fit(nf - 1, 14, xp, yp, B);
+    for (int i = 1; i <= m->vd; ++i) {
+      int iEdge = EOV(i, iVertex);
+      int k = (iVertex == VOE(1, iEdge)) ? 1 : 2;
+      double ct = cos(theta[i]), st = sin(theta[i]);
+      for (int j = 1; j <= nf - 1; ++j) {
+        double a = 24.0 * PM(B, 10, j) * ((ct * ct) * (ct * ct));
+        double b = 6.0 * PM(B, 11, j) * (ct * ct * ct) * st;
+        double c = 4.0 * PM(B, 12, j) * (ct * ct) * (st * st);
+        double d = 6.0 * PM(B, 13, j) * ct * (st * st * st);
+        double e = 24.0 * PM(B, 14, j) * ((st * st) * (st * st));
+        DER(m->deriv4OnVertex, j, k, iEdge) = a + 4.0 * b + 6.0 * c + 4.0 * d + e;
+      }
+    }
+  }
+}
+#undef PM
+
+/* ======================= operators (operators_mod.F90) ======================= */
+
+/* :40-55 div_operator (returns -div F) */
+static void div_operator(orc_model* m, const double* f_edge, double* div) {
+#pragma omp parallel for schedule(static)
+  for (int iCell = 1; iCell <= m->nc; ++iCell) {
+    double s = 0.0;
+    for (int i = 1; i <= A1(m->nEdgesOnCell, iCell); ++i) {
+      int e = EOC(i, iCell);
+      s = s + (double)NSIGN(i, iCell) * A1(f_edge, e) * A1(m->dvEdge, e);
+    }
+    A1(div, iCell) = -s;
+  }
+#pragma omp parallel for schedule(static)
+  for (int c = 0; c < m->nc; ++c) div[c] = div[c] / m->areaCell[c];
+}
+
+/* :76-91 curl_operator */
+static void curl_operator(orc_model* m, const double* f_edge, double* curl) {
+#pragma omp parallel for schedule(static)
+  for (int iVertex = 1; iVertex <= m->nv; ++iVertex) {
+    double s = 0.0;
+    for (int i = 1; i <= m->vd; ++i) {
+      int e = EOV(i, iVertex);
+      s = s + (double)TSIGN(i, iVertex) * A1(f_edge, e) * A1(m->dcEdge, e);
+    }
+    A1(curl, iVertex) = -s;
+  }
+#pragma omp parallel for schedule(static)
+  for (int v = 0; v < m->nv; ++v) curl[v] = curl[v] / m->areaTriangle[v];
+}
+
+/* :93-104 scalar_c2e_interp_operator */
+static void scalar_c2e(orc_model* m, const double* f_cell, double* f_edge) {
+#pragma omp parallel for schedule(static)
+  for (int iEdge = 1; iEdge <= m->ne; ++iEdge)
+    A1(f_edge, iEdge) = 0.5 * (A1(f_cell, COE(1, iEdge)) + A1(f_cell, COE(2, iEdge)));
+}
+
+/* :106-123 scalar_c2v_interp_operator */
+static void scalar_c2v(orc_model* m, const double* f_cell, double* f_vertex) {
+#pragma omp parallel for schedule(static)
+  for (int iVertex = 1; iVertex <= m->nv; ++iVertex) {
+    double s = 0.0;
+    for (int i = 1; i <= A1(m->nCellsOnVertex, iVertex); ++i) {
+      int iCell = COV(i, iVertex);
+      s = s + A1(f_cell, iCell) * KITE(i, iVertex);
+    }
+    A1(f_vertex, iVertex) = s;
+  }
+#pragma omp parallel for schedule(static)
+  for (int v = 0; v < m->nv; ++v) f_vertex[v] = f_vertex[v] / m->areaTriangle[v];
+}
+
+/* :125-141 scalar_v2c_interp_operator (serial scatter in vertex order) */
+static void scalar_v2c(orc_model* m, const double* f_vertex, double* f_cell) {
+  for (int c = 0; c < m->nc; ++c) f_cell[c] = 0.0;
+  for (int iVertex = 1; iVertex <= m->nv; ++iVertex)
+    for (int i = 1; i <= A1(m->nCellsOnVertex, iVertex); ++i) {
+      int iCell = COV(i, iVertex);
+      A1(f_cell, iCell) = A1(f_cell, iCell) + A1(f_vertex, iVertex) * KITE(i, iVertex) / A1(m->areaCell, iCell);
+    }
+}
+
+/* :143-156 scalar_v2e_interp_operator */
+static void scalar_v2e(orc_model* m, const double* f_vertex, double* f_edge) {
+#pragma omp parallel for schedule(static)
+  for (int iEdge = 1; iEdge <= m->ne; ++iEdge)
+    A1(f_edge, iEdge) = 0.5 * (A1(f_vertex, VOE(1, iEdge)) + A1(f_vertex, VOE(2, iEdge)));
+}
+
+/* :158-176 IAP transform and its inverse */
+static void iap_swm(orc_model* m, const double* gd_edge, const double* u, double* iap_u) {
+#pragma omp parallel for schedule(static)
+  for (int e = 0; e < m->ne; ++e) iap_u[e] = sqrt(gd_edge[e]) * u[e];
+}
+static void inverse_iap_swm(orc_model* m, const double* gd_edge, const double* iap_u, double* u) {
+#pragma omp parallel for schedule(static)
+  for (int e = 0; e < m->ne; ++e) u[e] = iap_u[e] / sqrt(gd_edge[e]);
+}
+
+/* :187-194 inner_product_tend */
+static double inner_product_tend(orc_model* m, const orc_tend* t1, const orc_tend* t2) {
+  double s1 = 0.0, s2 = 0.0;
+  for (int e = 0; e < m->ne; ++e) s1 = s1 + t1->e_iap_u[e] * t2->e_iap_u[e] * m->areaEdge[e];
+  for (int c = 0; c < m->nc; ++c) s2 = s2 + t1->c_gd[c] * t2->c_gd[c] * m->areaCell[c];
+  return (s1 + s2) / m->totalArea;
+}
+
+/* :206-221 calc_kinetic_energy */
+static void calc_kinetic_energy(orc_model* m, const double* u_edge, double* ke_cell) {
+#pragma omp parallel for schedule(static)
+  for (int iCell = 1; iCell <= m->nc; ++iCell) {
+    double s = 0.0;
+    for (int i = 1; i <= A1(m->nEdgesOnCell, iCell); ++i) {
+      int e = EOC(i, iCell);
+      s = s + A1(u_edge, e) * A1(u_edge, e) * A1(m->areaEdge, e);
+    }
+    A1(ke_cell, iCell) = s * 0.25;
+  }
+#pragma omp parallel for schedule(static)
+  for (int c = 0; c < m->nc; ++c) ke_cell[c] = ke_cell[c] / m->areaCell[c];
+}
+
+/* :223-237 calc_tangent_wind */
+static void calc_tangent_wind(orc_model* m, const double* u_edge, double* v_edge) {
+#pragma omp parallel for schedule(static)
+  for (int iEdge = 1; iEdge <= m->ne; ++iEdge) {
+    double s = 0.0;
+    for (int i = 1; i <= A1(m->nEdgesOnEdge, iEdge); ++i) s = s + A1(u_edge, EOE(i, iEdge)) * WOE(i, iEdge);
+    A1(v_edge, iEdge) = s;
+  }
+}
+
+/* :239-260 calc_tangent_vor_flux */
+static void calc_tangent_vor_flux(orc_model* m, const double* u_edge, const double* gd_edge,
+                                  const double* pv_edge, double* tvf) {
+#pragma omp parallel for schedule(static)
+  for (int iEdge = 1; iEdge <= m->ne; ++iEdge) {
+    double s = 0.0;
+    for (int i = 1; i <= A1(m->nEdgesOnEdge, iEdge); ++i) {
+      int ep = EOE(i, iEdge);
+      s = s + WOE(i, iEdge) * A1(u_edge, ep) * A1(gd_edge, ep) * 0.5 * (A1(pv_edge, iEdge) + A1(pv_edge, ep));
+    }
+    A1(tvf, iEdge) = s;
+  }
+}
+
+/* :262-270 calc_pv_on_vertex */
+static void calc_pv_on_vertex(orc_model* m, const double* vor, const double* gd_v, double* pv) {
+#pragma omp parallel for schedule(static)
+  for (int v = 0; v < m->nv; ++v) pv[v] = (m->fVertex[v] + vor[v]) / gd_v[v];
+}
+
+/* :296-316 APVM */
+static void pv_on_edge_apvm(orc_model* m, const double* u, const double* v, const double* pv_v,
+                            const double* pv_c, double* pv_e) {
+  scalar_v2e(m, pv_v, pv_e);
+  if (m->p.apvm_weight != 0.0) {
+    const double aw = m->p.apvm_weight, dt = m->p.dt;
+#pragma omp parallel for schedule(static)
+    for (int e = 1; e <= m->ne; ++e) {
+      double a = A1(v, e) * (A1(pv_v, VOE(2, e)) - A1(pv_v, VOE(1, e))) / A1(m->dvEdge, e);
+      double b = A1(u, e) * (A1(pv_c, COE(2, e)) - A1(pv_c, COE(1, e))) / A1(m->dcEdge, e);
+      A1(pv_e, e) = A1(pv_e, e) - aw * dt * (a + b);
+    }
+  }
+}
+
+/* :318-357 conservative APVM (with calc_vor_tend_on_vertex :414-421 = curl) */
+static void pv_on_edge_conservative_apvm(orc_model* m, const double* u, const double* v, const double* gd_e,
+                                         const double* gd_tend_v, const double* pv_v, const double* pv_c,
+                                         double* pv_e) {
+  double* dpv = dalloc(m->ne);
+  double* pvf = dalloc(m->ne);
+  double* dpvf = dalloc(m->ne);
+  double* vt = dalloc(m->nv);
+  double* dvt = dalloc(m->nv);
+  const double dt = m->p.dt;
+  scalar_v2e(m, pv_v, pv_e);
+#pragma omp parallel for schedule(static)
+  for (int e = 1; e <= m->ne; ++e) {
+    double a = A1(v, e) * (A1(pv_v, VOE(2, e)) - A1(pv_v, VOE(1, e))) / A1(m->dvEdge, e);
+    double b = A1(u, e) * (A1(pv_c, COE(2, e)) - A1(pv_c, COE(1, e))) / A1(m->dcEdge, e);
+    A1(dpv, e) = a + b;
+  }
+  calc_tangent_vor_flux(m, u, gd_e, pv_e, pvf);
+  calc_tangent_vor_flux(m, u, gd_e, dpv, dpvf);
+  curl_operator(m, pvf, vt);
+  curl_operator(m, dpvf, dvt);
+  double s1 = 0.0, s2 = 0.0, s3 = 0.0;
+  for (int k = 0; k < m->nv; ++k) s1 = s1 + pv_v[k] * pv_v[k] * gd_tend_v[k] * m->areaTriangle[k];
+  for (int k = 0; k < m->nv; ++k) s2 = s2 + pv_v[k] * vt[k] * m->areaTriangle[k];
+  for (int k = 0; k < m->nv; ++k) s3 = s3 + pv_v[k] * dvt[k] * m->areaTriangle[k];
+  double eps = -(s1 - s2 * 2.0) / (2.0 * dt * s3);
+  for (int e = 0; e < m->ne; ++e) pv_e[e] = pv_e[e] - eps * dt * dpv[e];
+  free(dpv);
+  free(pvf);
+  free(dpvf);
+  free(vt);
+  free(dvt);
+}
+
+/* sign(1.0d0, x): +1 / -1 with the sign bit of x */
+static inline double fsign1(double x) { return copysign(1.0, x); }
+
+/* sum(deriv(1:n-1, s, e) * (f(fit(1:n-1, id)) - f(id))) */
+static inline double stencil_d(const orc_model* m, const double* deriv, const int32_t* nfit, const int32_t* fit,
+                               const double* f, int s, int e, int id) {
+  double acc = 0.0;
+  int n = A1(nfit, id);
+  for (int j = 1; j <= n - 1; ++j) acc = acc + DER(deriv, j, s, e) * (A1(f, FIT(fit, j, id)) - A1(f, id));
+  return acc;
+}
+
+/* :359-412 high-order upwind PV on edges */
+static void pv_on_edge_upwind(orc_model* m, const double* v_edge, const double* pv_v, double* pv_e) {
+  int order = m->p.interp_pv_order;
+  double coef2 = 0.0;
+  if (order == 3) coef2 = 1.0;
+  if (order >= 4) coef2 = 0.0;
+  if (order == 6) m->upw_vtx_coef4 = 0.0;
+  const double coef4 = m->upw_vtx_coef4;
+#pragma omp parallel for schedule(static)
+  for (int e = 1; e <= m->ne; ++e)
+    A1(pv_e, e) = 0.5 * (A1(pv_v, VOE(1, e)) + A1(pv_v, VOE(2, e)));
+  if (order == 3 || order == 4) {
+#pragma omp parallel for schedule(static)
+    for (int e = 1; e <= m->ne; ++e) {
+      int v1 = VOE(1, e), v2 = VOE(2, e);
+      double d1 = stencil_d(m, m->deriv2OnVertex, m->nFit2Vertices, m->fit2Vertices, pv_v, 1, e, v1);
+      double d2 = stencil_d(m, m->deriv2OnVertex, m->nFit2Vertices, m->fit2Vertices, pv_v, 2, e, v2);
+      double dv = A1(m->dvEdge, e);
+      A1(pv_e, e) = A1(pv_e, e) - dv * dv * ((d1 + d2) - fsign1(A1(v_edge, e)) * coef2 * (d2 - d1)) / 12.0;
+    }
+  } else if (order == 5 || order == 6) {
+#pragma omp parallel for schedule(static)
+    for (int e = 1; e <= m->ne; ++e) {
+      int v1 = VOE(1, e), v2 = VOE(2, e);
+      double d21 = stencil_d(m, m->deriv2OnVertex, m->nFit2Vertices, m->fit2Vertices, pv_v, 1, e, v1);
+      double d22 = stencil_d(m, m->deriv2OnVertex, m->nFit2Vertices, m->fit2Vertices, pv_v, 2, e, v2);
+      double d41 = stencil_d(m, m->deriv4OnVertex, m->nFit4Vertices, m->fit4Vertices, pv_v, 1, e, v1);
+      double d42 = stencil_d(m, m->deriv4OnVertex, m->nFit4Vertices, m->fit4Vertices, pv_v, 2, e, v2);
+      double dv = A1(m->dvEdge, e);
+      A1(pv_e, e) = A1(pv_e, e) - dv * dv * (d21 + d22) / 12.0 +
+                    (dv * dv) * (dv * dv) * ((d41 + d42) - fsign1(A1(v_edge, e)) * coef4 * (d42 - d41)) / 60.0;
+    }
+  }
+}
+
+/* :273-294 calc_pv_on_edge */
+static void calc_pv_on_edge(orc_model* m, const double* u, const double* v, const double* gd_e,
+                            const double* gd_tend_v, const double* pv_v, const double* pv_c, double* pv_e) {
+  switch (m->p.pv_scheme) {
+    case 1: pv_on_edge_apvm(m, u, v, pv_v, pv_c, pv_e); break;
+    case 2: pv_on_edge_conservative_apvm(m, u, v, gd_e, gd_tend_v, pv_v, pv_c, pv_e); break;
+    case 3: pv_on_edge_upwind(m, v, pv_v, pv_e); break;
+    default: snprintf(m->err, sizeof(m->err), "unknown pv_scheme %d", m->p.pv_scheme);
+  }
+}
+
+/* :423-472 add_upwind_correction_on_cell (order/mono passed explicitly so the
+ * coupled tracers can use their own order; the SWM passes adv_order/adv_mono) */
+static void add_upwind_correction_on_cell(orc_model* m, const double* f_cell, const double* u_edge,
+                                          double* f_edge, int order, int mono) {
+  double coef2 = 0.0;
+  if (order == 3) coef2 = 1.0;
+  if (order == 3 && mono) coef2 = 0.25;
+  if (order >= 4) coef2 = 0.0;
+  if (order == 6) m->upw_cell_coef4 = 0.0;
+  const double coef4 = m->upw_cell_coef4;
+  if (order == 3 || order == 4) {
+#pragma omp parallel for schedule(static)
+    for (int e = 1; e <= m->ne; ++e) {
+      int c1 = COE(1, e), c2 = COE(2, e);
+      double d1 = stencil_d(m, m->deriv2OnCell, m->nFit2Cells, m->fit2Cells, f_cell, 1, e, c1);
+      double d2 = stencil_d(m, m->deriv2OnCell, m->nFit2Cells, m->fit2Cells, f_cell, 2, e, c2);
+      double dc = A1(m->dcEdge, e);
+      A1(f_edge, e) = A1(f_edge, e) - dc * dc * ((d1 + d2) - fsign1(A1(u_edge, e)) * coef2 * (d2 - d1)) / 12.0;
+    }
+  } else if (order == 5 || order == 6) {
+#pragma omp parallel for schedule(static)
+    for (int e = 1; e <= m->ne; ++e) {
+      int c1 = COE(1, e), c2 = COE(2, e);
+      double d21 = stencil_d(m, m->deriv2OnCell, m->nFit2Cells, m->fit2Cells, f_cell, 1, e, c1);
+      double d22 = stencil_d(m, m->deriv2OnCell, m->nFit2Cells, m->fit2Cells, f_cell, 2, e, c2);
+      double d41 = stencil_d(m, m->deriv4OnCell, m->nFit4Cells, m->fit4Cells, f_cell, 1, e, c1);
+      double d42 = stencil_d(m, m->deriv4OnCell, m->nFit4Cells, m->fit4Cells, f_cell, 2, e, c2);
+      double dc = A1(m->dcEdge, e);
+      A1(f_edge, e) = A1(f_edge, e) - dc * dc * (d21 + d22) / 12.0 +
+                      (dc * dc) * (dc * dc) * ((d41 + d42) - fsign1(A1(u_edge, e)) * coef4 * (d42 - d41)) / 60.0;
+    }
+  }
+}
+
+/* ======================= SWM model (tmcore_swm_mod.F90) ======================= */
+
+/* :127-139 calc_gd_tend_on_cell */
+static void calc_gd_tend_on_cell(orc_model* m, const double* u, const double* gd_e, double* tend) {
+  double* flux = m->tmp_e1;
+#pragma omp parallel for schedule(static)
+  for (int e = 0; e < m->ne; ++e) flux[e] = u[e] * gd_e[e];
+  div_operator(m, flux, tend);
+}
+
+/* :155-201 calc_u_tend_on_edge */
+static void calc_u_tend_on_edge(orc_model* m, const double* u, const double* ke, const double* gd,
+                                const double* gd_e, const double* ghs, const double* pv_flx,
+                                const double* gd_tend_e, double* u_tend, double* iap_u_tend) {
+  double* E = m->tmp_c1;
+#pragma omp parallel for schedule(static)
+  for (int c = 0; c < m->nc; ++c) E[c] = ke[c] + gd[c] + ghs[c];
+#pragma omp parallel for schedule(static)
+  for (int e = 1; e <= m->ne; ++e) {
+    double dEdx = (A1(E, COE(2, e)) - A1(E, COE(1, e))) / A1(m->dcEdge, e);
+    if (m->p.flux_4th_order_correct) {
+      int c1 = COE(1, e), c2 = COE(2, e);
+      double d1 = stencil_d(m, m->deriv3OnCell, m->nFit3Cells, m->fit3Cells, E, 1, e, c1);
+      double d2 = stencil_d(m, m->deriv3OnCell, m->nFit3Cells, m->fit3Cells, E, 2, e, c2);
+      dEdx = dEdx - (d2 - d1) * A1(m->dcEdge, e) / 24.0;
+    }
+    double iap_gd = sqrt(A1(gd_e, e));
+    double ut = A1(pv_flx, e) - dEdx;
+    A1(u_tend, e) = ut;
+    A1(iap_u_tend, e) = iap_gd * ut + 0.5 * A1(u, e) / iap_gd * A1(gd_tend_e, e);
+  }
+}
+
+/* coupled tracers: d(gd q)/dt = div_operator(u gd_e q_e), q_e = c2e(q) +
+ * upwind correction (the sg11 edge value, adv_scheme_sg11_mod.F90:42-43) */
+static void tracer_tend(orc_model* m, orc_state* s, orc_tend* t) {
+  const int order = m->p.tracer_adv_order ? m->p.tracer_adv_order : m->p.adv_order;
+  const int mono = m->p.tracer_adv_order ? m->p.tracer_adv_mono : m->p.adv_mono;
+  double* q = m->tmp_c2;
+  double* qe = m->tmp_e2;
+  double* flux = m->tmp_e3;
+  for (int k = 0; k < m->p.n_tracers; ++k) {
+    const double* qgd = s->qgd + (size_t)k * m->nc;
+#pragma omp parallel for schedule(static)
+    for (int c = 0; c < m->nc; ++c) q[c] = qgd[c] / s->c_gd[c];
+    scalar_c2e(m, q, qe);
+    add_upwind_correction_on_cell(m, q, s->e_iap_u, qe, order, mono);
+#pragma omp parallel for schedule(static)
+    for (int e = 0; e < m->ne; ++e) flux[e] = s->e_u[e] * s->e_gd[e] * qe[e];
+    div_operator(m, flux, t->qgd + (size_t)k * m->nc);
+  }
+}
+
+/* :92-125 spatial_operators (mpas_reconstruct at :101 feeds no tendency and is omitted) */
+static void spatial_operators(orc_model* m, orc_state* s, orc_tend* t) {
+  const int ao = m->p.adv_order, am = m->p.adv_mono;
+  scalar_c2e(m, s->c_gd, s->e_gd);
+  add_upwind_correction_on_cell(m, s->c_gd, s->e_iap_u, s->e_gd, ao, am);
+  inverse_iap_swm(m, s->e_gd, s->e_iap_u, s->e_u);
+  calc_gd_tend_on_cell(m, s->e_u, s->e_gd, t->c_gd);
+  scalar_c2e(m, t->c_gd, t->e_gd);
+  add_upwind_correction_on_cell(m, t->c_gd, s->e_iap_u, t->e_gd, ao, am);
+  scalar_c2v(m, t->c_gd, t->v_gd);
+  scalar_c2v(m, s->c_gd, s->v_gd);
+  curl_operator(m, s->e_u, s->v_vor);
+  calc_tangent_wind(m, s->e_u, s->e_v);
+  calc_kinetic_energy(m, s->e_u, s->c_ke);
+  calc_pv_on_vertex(m, s->v_vor, s->v_gd, s->v_pv);
+  scalar_v2c(m, s->v_pv, s->c_pv);
+  calc_pv_on_edge(m, s->e_u, s->e_v, s->e_gd, t->v_gd, s->v_pv, s->c_pv, s->e_pv);
+  calc_tangent_vor_flux(m, s->e_u, s->e_gd, s->e_pv, s->e_pv_flx);
+  calc_u_tend_on_edge(m, s->e_u, s->c_ke, s->c_gd, s->e_gd, m->ghs, s->e_pv_flx, t->e_gd, t->e_u, t->e_iap_u);
+  if (m->p.n_tracers > 0) tracer_tend(m, s, t);
+}
+
+/* :203-213 update_state (+ tracers with the same increment) */
+static void update_state(orc_model* m, double dt, const orc_tend* t, const orc_state* o, orc_state* n) {
+#pragma omp parallel for schedule(static)
+  for (int e = 0; e < m->ne; ++e) n->e_iap_u[e] = o->e_iap_u[e] + dt * t->e_iap_u[e];
+#pragma omp parallel for schedule(static)
+  for (int c = 0; c < m->nc; ++c) n->c_gd[c] = o->c_gd[c] + dt * t->c_gd[c];
+  size_t nq = (size_t)m->p.n_tracers * m->nc;
+#pragma omp parallel for schedule(static)
+  for (size_t k = 0; k < nq; ++k) n->qgd[k] = o->qgd[k] + dt * t->qgd[k];
+}
+
+/* :215-255 invariants */
+static void swm_invariants(orc_model* m, orc_state* s) {
+  double a = 0.0, b = 0.0, c = 0.0, d = 0.0, e = 0.0;
+  for (int k = 0; k < m->nc; ++k) a = a + s->c_gd[k] * m->areaCell[k];
+  s->total_mass = a;
+  for (int k = 0; k < m->ne; ++k) b = b + s->e_iap_u[k] * s->e_iap_u[k] * m->areaEdge[k];
+  for (int k = 0; k < m->nc; ++k) c = c + (s->c_gd[k] * s->c_gd[k] + 2.0 * s->c_gd[k] * m->ghs[k]) * m->areaCell[k];
+  s->total_energy = b + c;
+  d = 0.0;
+  for (int k = 0; k < m->nv; ++k) d = d + s->v_gd[k] * (s->v_pv[k] * s->v_pv[k]) * m->areaTriangle[k];
+  s->total_pe = d;
+  double num = 0.0, den = 0.0;
+  for (int k = 0; k < m->nv; ++k) num = num + (s->v_vor[k] + m->fVertex[k]) * m->areaTriangle[k];
+  for (int k = 0; k < m->nv; ++k) den = den + m->areaTriangle[k];
+  s->total_av = num / den;
+  (void)e;
+}
+
+/* per-step diagnostic recompute of state(old) (tmcore_swm_mod.F90:78-85) */
+static void swm_diag(orc_model* m) {
+  orc_state* s = &m->state[m->old + 4];
+  scalar_c2e(m, s->c_gd, s->e_gd);
+  add_upwind_correction_on_cell(m, s->c_gd, s->e_iap_u, s->e_gd, m->p.adv_order, m->p.adv_mono);
+  inverse_iap_swm(m, s->e_gd, s->e_iap_u, s->e_u);
+  scalar_c2v(m, s->c_gd, s->v_gd);
+  curl_operator(m, s->e_u, s->v_vor);
+  calc_pv_on_vertex(m, s->v_vor, s->v_gd, s->v_pv);
+  swm_invariants(m, s);
+}
+
+static void copy_prognostic(orc_model* m, const orc_state* from, orc_state* to) {
+  memcpy(to->c_gd, from->c_gd, sizeof(double) * m->nc);
+  memcpy(to->e_u, from->e_u, sizeof(double) * m->ne);
+  memcpy(to->e_iap_u, from->e_iap_u, sizeof(double) * m->ne);
+  memcpy(to->qgd, from->qgd, sizeof(double) * m->nc * (size_t)m->p.n_tracers);
+}
+
+/* tend(new) = combination of stage tendencies (gd, iap_u and tracers) */
+static void combine_tend(orc_model* m, orc_tend* out, const orc_tend* t1, const orc_tend* t2, const orc_tend* t3,
+                         const orc_tend* t4, int crk3) {
+#pragma omp parallel for schedule(static)
+  for (int c = 0; c < m->nc; ++c)
+    out->c_gd[c] = crk3 ? (t1->c_gd[c] + 4.0 * t2->c_gd[c] + t3->c_gd[c]) / 6.0
+                        : (t1->c_gd[c] + 2.0 * t2->c_gd[c] + 2.0 * t3->c_gd[c] + t4->c_gd[c]) / 6.0;
+#pragma omp parallel for schedule(static)
+  for (int e = 0; e < m->ne; ++e)
+    out->e_iap_u[e] = crk3 ? (t1->e_iap_u[e] + 4.0 * t2->e_iap_u[e] + t3->e_iap_u[e]) / 6.0
+                           : (t1->e_iap_u[e] + 2.0 * t2->e_iap_u[e] + 2.0 * t3->e_iap_u[e] + t4->e_iap_u[e]) / 6.0;
+  size_t nq = (size_t)m->p.n_tracers * m->nc;
+#pragma omp parallel for schedule(static)
+  for (size_t k = 0; k < nq; ++k)
+    out->qgd[k] = crk3 ? (t1->qgd[k] + 4.0 * t2->qgd[k] + t3->qgd[k]) / 6.0
+                       : (t1->qgd[k] + 2.0 * t2->qgd[k] + 2.0 * t3->qgd[k] + t4->qgd[k]) / 6.0;
+}
+
+typedef void (*spatial_fn)(orc_model*, orc_state*, orc_tend*);
+typedef void (*update_fn)(orc_model*, double, const orc_tend*, const orc_state*, orc_state*);
+
+#define ST(i) (&m->state[(i) + 4])
+#define TD(i) (&m->tend[(i) + 4])
+
+/* time_scheme_mod.F90:109-154 time_integrate_CRK4 */
+static void crk4(orc_model* m, spatial_fn so, update_fn up) {
+  const int one = -1, two = -2, three = -3, four = -4, old = m->old, new_ = m->new_;
+  const double dt = m->p.dt;
+  copy_prognostic(m, ST(old), ST(one));
+  so(m, ST(one), TD(one));
+  up(m, 0.5 * dt, TD(one), ST(one), ST(two));
+  so(m, ST(two), TD(two));
+  up(m, 0.5 * dt, TD(two), ST(one), ST(three));
+  so(m, ST(three), TD(three));
+  up(m, dt, TD(three), ST(one), ST(four));
+  so(m, ST(four), TD(four));
+  combine_tend(m, TD(new_), TD(one), TD(two), TD(three), TD(four), 0);
+  double beta = 1.0;
+  if (m->p.conserve_energy) {
+    double R4R4 = inner_product_tend(m, TD(new_), TD(new_));
+    double R1R2 = inner_product_tend(m, TD(one), TD(two));
+    double R2R3 = inner_product_tend(m, TD(two), TD(three));
+    double R3R4 = inner_product_tend(m, TD(three), TD(four));
+    beta = (R1R2 + R2R3 + R3R4) / (3.0 * R4R4);
+  }
+  m->beta = beta;
+  up(m, beta * dt, TD(new_), ST(old), ST(new_));
+}
+
+/* time_scheme_mod.F90:65-107 time_integrate_CRK3 */
+static void crk3(orc_model* m, spatial_fn so, update_fn up) {
+  const int one = -1, two = -2, three = -3, old = m->old, new_ = m->new_;
+  const double dt = m->p.dt;
+  memcpy(ST(one)->c_gd, ST(old)->c_gd, sizeof(double) * m->nc);
+  memcpy(ST(one)->e_iap_u, ST(old)->e_iap_u, sizeof(double) * m->ne);
+  memcpy(ST(one)->qgd, ST(old)->qgd, sizeof(double) * m->nc * (size_t)m->p.n_tracers);
+  so(m, ST(one), TD(one));
+  up(m, 0.5 * dt, TD(one), ST(one), ST(two));
+  so(m, ST(two), TD(two));
+  up(m, -dt, TD(one), ST(one), ST(three));
+  up(m, 2.0 * dt, TD(two), ST(three), ST(three));
+  so(m, ST(three), TD(three));
+  combine_tend(m, TD(new_), TD(one), TD(two), TD(three), NULL, 1);
+  double beta = 1.0;
+  if (m->p.conserve_energy) {
+    double R4R4 = inner_product_tend(m, TD(new_), TD(new_));
+    double R1R2 = inner_product_tend(m, TD(one), TD(two));
+    double R1R3 = inner_product_tend(m, TD(one), TD(three));
+    double R2R3 = inner_product_tend(m, TD(two), TD(three));
+    beta = (2.0 * R1R2 - R1R3 + 2.0 * R2R3) / (3.0 * R4R4);
+  }
+  m->beta = beta;
+  up(m, beta * dt, TD(new_), ST(old), ST(new_));
+}
+
+/* time_scheme_mod.F90:156-184 time_integrate_PC2 */
+static void pc2(orc_model* m, spatial_fn so, update_fn up) {
+  const int old = m->old, new_ = m->new_;
+  const double dt = m->p.dt;
+  so(m, ST(old), TD(old));
+  up(m, 0.5 * dt, TD(old), ST(old), ST(new_));
+  so(m, ST(new_), TD(old));
+  up(m, 0.5 * dt, TD(old), ST(old), ST(new_));
+  so(m, ST(new_), TD(new_));
+  double beta = 1.0;
+  if (m->p.conserve_energy) {
+    double ip1 = inner_product_tend(m, TD(old), TD(new_));
+    double ip2 = inner_product_tend(m, TD(new_), TD(new_));
+    beta = (ip1 != 0.0 && ip2 != 0.0) ? ip1 / ip2 : 1.0;
+  }
+  m->beta = beta;
+  up(m, beta * dt, TD(new_), ST(old), ST(new_));
+}
+
+/* time_scheme_mod.F90:47-63 time_integrate */
+static void time_integrate(orc_model* m, spatial_fn so, update_fn up) {
+  switch (m->p.time_scheme) {
+    case 1: crk3(m, so, up); break;
+    case 2: crk4(m, so, up); break;
+    case 3: pc2(m, so, up); break;
+    default: snprintf(m->err, sizeof(m->err), "Unknown integration scheme");
+  }
+}
+
+/* time_mod.F90:106-130 time_advance (index swap, counters) */
+static void time_advance(orc_model* m) {
+  int t = m->old;
+  m->old = m->new_;
+  m->new_ = t;
+  m->time_step += 1;
+  m->elapsed = m->elapsed + m->p.dt;
+}
+
+/* ======================= adv model (tmcore_adv_mod.F90) ======================= */
+
+/* cosine_bell_rotation_test_mod.F90:45-68 and deformation_flow_test_mod.F90:74-105 */
+static void adv_update_wind(orc_model* m, double seconds, orc_state* s) {
+  const double pi = 4.0 * atan(1.0), radius = m->p.radius;
+  double* psi = m->tmp_v1;
+  if (m->adv_wind_case == ORC_WIND_COSINE_BELL) {
+    const double u0 = 2.0 * pi * radius / 12.0 / 86400.0, alpha = 0.5 * pi;
+    double ca = cos(alpha), sa = sin(alpha);
+    for (int v = 0; v < m->nv; ++v) {
+      double cl = cos(m->latVertex[v]), sl = sin(m->latVertex[v]), co = cos(m->lonVertex[v]);
+      psi[v] = -radius * u0 * (sl * ca - co * cl * sa);
+    }
+  } else {
+    const double T0 = 12.0 * 86400.0, u0 = 2.0 * pi * radius / T0;
+    double c = pi * 2.0 * seconds / T0, k = 10.0 * radius / T0, cosT = cos(pi * seconds / T0);
+    for (int v = 0; v < m->nv; ++v) {
+      double sn = sin(m->lonVertex[v] - c), cl = cos(m->latVertex[v]);
+      psi[v] = k * (sn * sn) * (cl * cl) * cosT - u0 * sin(m->latVertex[v]);
+    }
+    for (int v = 0; v < m->nv; ++v) psi[v] = psi[v] * radius;
+  }
+  for (int e = 1; e <= m->ne; ++e)
+    A1(s->e_u, e) = -(A1(psi, VOE(2, e)) - A1(psi, VOE(1, e))) / A1(m->dvEdge, e);
+}
+
+/* :78-85 spatial_operators -> adv_scheme_sg11_run (adv_scheme_sg11_mod.F90:33-48) */
+static void adv_spatial(orc_model* m, orc_state* s, orc_tend* t) {
+  scalar_c2e(m, s->c_gd, s->e_gd);
+  add_upwind_correction_on_cell(m, s->c_gd, s->e_u, s->e_gd, m->p.adv_order, m->p.adv_mono);
+  double* flux = m->tmp_e1;
+  for (int e = 0; e < m->ne; ++e) flux[e] = s->e_u[e] * s->e_gd[e];
+  div_operator(m, flux, t->c_gd);
+}
+
+/* :87-97 update_state: tracer update, then the wind at elapsed + dt */
+static void adv_update(orc_model* m, double dt, const orc_tend* t, const orc_state* o, orc_state* n) {
+  for (int c = 0; c < m->nc; ++c) n->c_gd[c] = o->c_gd[c] + dt * t->c_gd[c];
+  adv_update_wind(m, m->elapsed + dt, n);
+}
+
+/* ======================= lifetime and public API ======================= */
+
+static void alloc_state(orc_model* m, orc_state* s) {
+  s->c_gd = dalloc(m->nc);
+  s->c_ke = dalloc(m->nc);
+  s->c_pv = dalloc(m->nc);
+  s->e_gd = dalloc(m->ne);
+  s->e_u = dalloc(m->ne);
+  s->e_v = dalloc(m->ne);
+  s->e_pv = dalloc(m->ne);
+  s->e_pv_flx = dalloc(m->ne);
+  s->e_iap_u = dalloc(m->ne);
+  s->v_gd = dalloc(m->nv);
+  s->v_vor = dalloc(m->nv);
+  s->v_pv = dalloc(m->nv);
+  s->qgd = dalloc((size_t)m->nc * (m->p.n_tracers > 0 ? m->p.n_tracers : 1));
+}
+static void free_state(orc_state* s) {
+  free(s->c_gd); free(s->c_ke); free(s->c_pv); free(s->e_gd); free(s->e_u); free(s->e_v);
+  free(s->e_pv); free(s->e_pv_flx); free(s->e_iap_u); free(s->v_gd); free(s->v_vor); free(s->v_pv);
+  free(s->qgd);
+}
+static void alloc_tend(orc_model* m, orc_tend* t) {
+  t->c_gd = dalloc(m->nc);
+  t->e_gd = dalloc(m->ne);
+  t->e_u = dalloc(m->ne);
+  t->e_iap_u = dalloc(m->ne);
+  t->v_gd = dalloc(m->nv);
+  t->qgd = dalloc((size_t)m->nc * (m->p.n_tracers > 0 ? m->p.n_tracers : 1));
+}
+static void free_tend(orc_tend* t) {
+  free(t->c_gd); free(t->e_gd); free(t->e_u); free(t->e_iap_u); free(t->v_gd); free(t->qgd);
+}
+
+orc_model* orc_create(const orc_mesh_in* in, const orc_params* p) {
+  orc_model* m = (orc_model*)xcalloc(1, sizeof(orc_model));
+  m->p = *p;
+#ifdef _OPENMP
+  if (p->nthreads > 0) omp_set_num_threads(p->nthreads);
+#endif
+  m->nc = in->nCells;
+  m->ne = in->nEdges;
+  m->nv = in->nVertices;
+  m->me = in->maxEdges;
+  m->me2 = in->maxEdges2;
+  m->vd = in->vertexDegree;
+  size_t nc = m->nc, ne = m->ne, nv = m->nv;
+  m->nEdgesOnCell = dup(in->nEdgesOnCell, nc * 4);
+  m->nEdgesOnEdge = dup(in->nEdgesOnEdge, ne * 4);
+  m->nCellsOnVertex = ialloc(nv);
+  m->cellsOnCell = dup(in->cellsOnCell, nc * m->me * 4);
+  m->edgesOnCell = dup(in->edgesOnCell, nc * m->me * 4);
+  m->verticesOnCell = dup(in->verticesOnCell, nc * m->me * 4);
+  m->cellsOnEdge = dup(in->cellsOnEdge, ne * 2 * 4);
+  m->verticesOnEdge = dup(in->verticesOnEdge, ne * 2 * 4);
+  m->edgesOnEdge = dup(in->edgesOnEdge, ne * m->me2 * 4);
+  m->cellsOnVertex = dup(in->cellsOnVertex, nv * m->vd * 4);
+  m->edgesOnVertex = dup(in->edgesOnVertex, nv * m->vd * 4);
+  m->verticesOnVertex = ialloc(nv * m->vd);
+  m->nSignEdge = ialloc(nc * m->me);
+  m->tSignEdge = ialloc(nv * m->vd);
+  m->xCell = dup(in->xCell, nc * 8);
+  m->yCell = dup(in->yCell, nc * 8);
+  m->zCell = dup(in->zCell, nc * 8);
+  m->latCell = dup(in->latCell, nc * 8);
+  m->lonCell = dup(in->lonCell, nc * 8);
+  m->xVertex = dup(in->xVertex, nv * 8);
+  m->yVertex = dup(in->yVertex, nv * 8);
+  m->zVertex = dup(in->zVertex, nv * 8);
+  m->latVertex = dup(in->latVertex, nv * 8);
+  m->lonVertex = dup(in->lonVertex, nv * 8);
+  m->dvEdge = dup(in->dvEdge, ne * 8);
+  m->dcEdge = dup(in->dcEdge, ne * 8);
+  m->areaCell = dup(in->areaCell, nc * 8);
+  m->areaTriangle = dup(in->areaTriangle, nv * 8);
+  m->kiteAreasOnVertex = dup(in->kiteAreasOnVertex, nv * m->vd * 8);
+  m->weightsOnEdge = dup(in->weightsOnEdge, ne * m->me2 * 8);
+  m->areaEdge = dalloc(ne);
+  m->fCell = dalloc(nc);
+  m->fVertex = dalloc(nv);
+  mesh_derive(m);
+
+  m->nFit2Cells = ialloc(nc);
+  m->nFit3Cells = ialloc(nc);
+  m->nFit4Cells = ialloc(nc);
+  m->nFit2Vertices = ialloc(nv);
+  m->nFit3Vertices = ialloc(nv);
+  m->nFit4Vertices = ialloc(nv);
+  m->fit2Cells = ialloc(nc * NFIT);
+  m->fit3Cells = ialloc(nc * NFIT);
+  m->fit4Cells = ialloc(nc * NFIT);
+  m->fit2Vertices = ialloc(nv * NFIT);
+  m->fit3Vertices = ialloc(nv * NFIT);
+  m->fit4Vertices = ialloc(nv * NFIT);
+  m->deriv2OnCell = dalloc(ne * 2 * NFIT);
+  m->deriv3OnCell = dalloc(ne * 2 * NFIT);
+  m->deriv4OnCell = dalloc(ne * 2 * NFIT);
+  m->deriv2OnVertex = dalloc(ne * 2 * NFIT);
+  m->deriv4OnVertex = dalloc(ne * 2 * NFIT);
+  m->upw_cell_coef4 = 0.25;
+  m->upw_vtx_coef4 = 0.25;
+  /* poly_fit_init (poly_fit_mod.F90:61-89) always runs in the reference; its
+   * tables feed only the upwind corrections and the 4th-order flux option, so
+   * the oracle skips the (expensive, init-only) fit when none is enabled. */
+  {
+    int tro = p->tracer_adv_order ? p->tracer_adv_order : p->adv_order;
+    int need = p->adv_order >= 3 || p->pv_scheme == 3 || p->flux_4th_order_correct ||
+               (p->n_tracers > 0 && tro >= 3) || p->nthreads < 0;
+    if (need) poly_fit_run(m);
+  }
+
+  for (int i = 0; i < 7; ++i) {
+    alloc_state(m, &m->state[i]);
+    alloc_tend(m, &m->tend[i]);
+  }
+  m->ghs = dalloc(nc);
+  m->tmp_e1 = dalloc(ne);
+  m->tmp_e2 = dalloc(ne);
+  m->tmp_e3 = dalloc(ne);
+  m->tmp_v1 = dalloc(nv);
+  m->tmp_v2 = dalloc(nv);
+  m->tmp_c1 = dalloc(nc);
+  m->tmp_c2 = dalloc(nc);
+  m->old = 1;
+  m->new_ = 2;
+  m->beta = 1.0;
+  return m;
+}
+
+void orc_destroy(orc_model* m) {
+  if (!m) return;
+  void* ptrs[] = {m->nEdgesOnCell, m->nEdgesOnEdge, m->nCellsOnVertex, m->cellsOnCell, m->edgesOnCell,
+                  m->verticesOnCell, m->cellsOnEdge, m->verticesOnEdge, m->edgesOnEdge, m->cellsOnVertex,
+                  m->edgesOnVertex, m->verticesOnVertex, m->nSignEdge, m->tSignEdge, m->xCell, m->yCell,
+                  m->zCell, m->latCell, m->lonCell, m->xVertex, m->yVertex, m->zVertex, m->latVertex,
+                  m->lonVertex, m->dvEdge, m->dcEdge, m->areaCell, m->areaTriangle, m->areaEdge,
+                  m->kiteAreasOnVertex, m->weightsOnEdge, m->fCell, m->fVertex, m->nFit2Cells, m->nFit3Cells,
+                  m->nFit4Cells, m->nFit2Vertices, m->nFit3Vertices, m->nFit4Vertices, m->fit2Cells,
+                  m->fit3Cells, m->fit4Cells, m->fit2Vertices, m->fit3Vertices, m->fit4Vertices,
+                  m->deriv2OnCell, m->deriv3OnCell, m->deriv4OnCell, m->deriv2OnVertex, m->deriv4OnVertex,
+                  m->ghs, m->tmp_e1, m->tmp_e2, m->tmp_e3, m->tmp_v1, m->tmp_v2, m->tmp_c1, m->tmp_c2};
+  for (size_t i = 0; i < sizeof(ptrs) / sizeof(ptrs[0]); ++i) free(ptrs[i]);
+  for (int i = 0; i < 7; ++i) {
+    free_state(&m->state[i]);
+    free_tend(&m->tend[i]);
+  }
+  free(m);
+}
+
+const char* orc_error(const orc_model* m) { return m ? m->err : "null"; }
+const double* orc_areaEdge(const orc_model* m) { return m->areaEdge; }
+const double* orc_fVertex(const orc_model* m) { return m->fVertex; }
+double orc_totalArea(const orc_model* m) { return m->totalArea; }
+const int32_t* orc_nSignEdge(const orc_model* m) { return m->nSignEdge; }
+const int32_t* orc_tSignEdge(const orc_model* m) { return m->tSignEdge; }
+
+int orc_poly_fit_table(const orc_model* m, const char* name, const void** data, int64_t* count) {
+  size_t nc = m->nc, ne = m->ne, nv = m->nv;
+#define T(nm, ptr, cnt)            \
+  if (strcmp(name, nm) == 0) {     \
+    *data = (const void*)(ptr);    \
+    *count = (int64_t)(cnt);       \
+    return 0;                      \
+  }
+  T("nFit2Cells", m->nFit2Cells, nc);
+  T("nFit3Cells", m->nFit3Cells, nc);
+  T("nFit4Cells", m->nFit4Cells, nc);
+  T("nFit2Vertices", m->nFit2Vertices, nv);
+  T("nFit4Vertices", m->nFit4Vertices, nv);
+  T("fit2Cells", m->fit2Cells, nc * NFIT);
+  T("fit3Cells", m->fit3Cells, nc * NFIT);
+  T("fit4Cells", m->fit4Cells, nc * NFIT);
+  T("fit2Vertices", m->fit2Vertices, nv * NFIT);
+  T("fit4Vertices", m->fit4Vertices, nv * NFIT);
+  T("deriv2OnCell", m->deriv2OnCell, ne * 2 * NFIT);
+  T("deriv3OnCell", m->deriv3OnCell, ne * 2 * NFIT);
+  T("deriv4OnCell", m->deriv4OnCell, ne * 2 * NFIT);
+  T("deriv2OnVertex", m->deriv2OnVertex, ne * 2 * NFIT);
+  T("deriv4OnVertex", m->deriv4OnVertex, ne * 2 * NFIT);
+#undef T
+  return -1;
+}
+
+void orc_op_div(orc_model* m, const double* f, double* o) { div_operator(m, f, o); }
+void orc_op_curl(orc_model* m, const double* f, double* o) { curl_operator(m, f, o); }
+void orc_op_c2e(orc_model* m, const double* f, double* o) { scalar_c2e(m, f, o); }
+void orc_op_c2v(orc_model* m, const double* f, double* o) { scalar_c2v(m, f, o); }
+void orc_op_v2c(orc_model* m, const double* f, double* o) { scalar_v2c(m, f, o); }
+void orc_op_v2e(orc_model* m, const double* f, double* o) { scalar_v2e(m, f, o); }
+void orc_op_kinetic_energy(orc_model* m, const double* u, double* o) { calc_kinetic_energy(m, u, o); }
+void orc_op_tangent_wind(orc_model* m, const double* u, double* o) { calc_tangent_wind(m, u, o); }
+void orc_op_tangent_vor_flux(orc_model* m, const double* u, const double* g, const double* q, double* o) {
+  calc_tangent_vor_flux(m, u, g, q, o);
+}
+void orc_op_upwind_correction(orc_model* m, const double* f, const double* u, double* fe, int order, int mono) {
+  add_upwind_correction_on_cell(m, f, u, fe, order, mono);
+}
+
+/* tmcore_swm_mod.F90:62-71 pre-loop.  add_upwind_correction_on_cell is called
+ * there with iap_u not yet set (:63); the restatement takes the sign from u,
+ * which has the same sign (:79 comment). */
+void orc_swm_set_initial(orc_model* m, const double* gd, const double* u, const double* ghs) {
+  orc_state* s = ST(m->old);
+  memcpy(s->c_gd, gd, sizeof(double) * m->nc);
+  memcpy(s->e_u, u, sizeof(double) * m->ne);
+  memcpy(m->ghs, ghs, sizeof(double) * m->nc);
+  scalar_c2e(m, s->c_gd, s->e_gd);
+  add_upwind_correction_on_cell(m, s->c_gd, s->e_u, s->e_gd, m->p.adv_order, m->p.adv_mono);
+  iap_swm(m, s->e_gd, s->e_u, s->e_iap_u);
+  scalar_c2v(m, s->c_gd, s->v_gd);
+  curl_operator(m, s->e_u, s->v_vor);
+  calc_pv_on_vertex(m, s->v_vor, s->v_gd, s->v_pv);
+  swm_invariants(m, s);
+}
+
+void orc_swm_set_state(orc_model* m, const double* gd, const double* iap_u) {
+  orc_state* s = ST(m->old);
+  memcpy(s->c_gd, gd, sizeof(double) * m->nc);
+  memcpy(s->e_iap_u, iap_u, sizeof(double) * m->ne);
+  swm_diag(m);
+}
+
+void orc_swm_spatial_operators(orc_model* m, const double* gd, const double* iap_u, double* tend_gd,
+                               double* tend_iap_u) {
+  orc_state* s = ST(-1);
+  orc_tend* t = TD(-1);
+  memcpy(s->c_gd, gd, sizeof(double) * m->nc);
+  memcpy(s->e_iap_u, iap_u, sizeof(double) * m->ne);
+  memcpy(s->qgd, ST(m->old)->qgd, sizeof(double) * m->nc * (size_t)m->p.n_tracers);
+  spatial_operators(m, s, t);
+  memcpy(tend_gd, t->c_gd, sizeof(double) * m->nc);
+  memcpy(tend_iap_u, t->e_iap_u, sizeof(double) * m->ne);
+}
+
+void orc_swm_step(orc_model* m, int nsteps) {
+  for (int i = 0; i < nsteps; ++i) {
+    time_integrate(m, spatial_operators, update_state);
+    time_advance(m);
+    swm_diag(m);
+  }
+}
+
+void orc_swm_get_state(const orc_model* m, double* gd, double* iap_u, double* u) {
+  const orc_state* s = &m->state[m->old + 4];
+  if (gd) memcpy(gd, s->c_gd, sizeof(double) * m->nc);
+  if (iap_u) memcpy(iap_u, s->e_iap_u, sizeof(double) * m->ne);
+  if (u) memcpy(u, s->e_u, sizeof(double) * m->ne);
+}
+
+void orc_swm_get_vertex(const orc_model* m, double* pv, double* vor) {
+  const orc_state* s = &m->state[m->old + 4];
+  if (pv) memcpy(pv, s->v_pv, sizeof(double) * m->nv);
+  if (vor) memcpy(vor, s->v_vor, sizeof(double) * m->nv);
+}
+
+void orc_swm_get_diag(const orc_model* m, double out[5]) {
+  const orc_state* s = &m->state[m->old + 4];
+  out[0] = s->total_mass;
+  out[1] = s->total_energy;
+  out[2] = s->total_pe;
+  out[3] = s->total_av;
+  out[4] = m->beta;
+}
+
+void orc_set_tracers(orc_model* m, const double* q) {
+  orc_state* s = ST(m->old);
+  memcpy(s->qgd, q, sizeof(double) * m->nc * (size_t)m->p.n_tracers);
+}
+
+void orc_get_tracers(const orc_model* m, double* q) {
+  const orc_state* s = &m->state[m->old + 4];
+  memcpy(q, s->qgd, sizeof(double) * m->nc * (size_t)m->p.n_tracers);
+}
+
+/* tmcore_adv_mod: the test case sets gd (the tracer) and the wind at t=0 */
+void orc_adv_set_initial(orc_model* m, const double* q, int wind_case) {
+  orc_state* s = ST(m->old);
+  m->adv_wind_case = wind_case;
+  memcpy(s->c_gd, q, sizeof(double) * m->nc);
+  adv_update_wind(m, 0.0, s);
+  double a = 0.0;
+  for (int k = 0; k < m->nc; ++k) a = a + s->c_gd[k] * m->areaCell[k];
+  s->total_mass = a;
+}
+
+void orc_adv_step(orc_model* m, int nsteps) {
+  for (int i = 0; i < nsteps; ++i) {
+    time_integrate(m, adv_spatial, adv_update);
+    time_advance(m);
+    orc_state* s = ST(m->old);
+    double a = 0.0;
+    for (int k = 0; k < m->nc; ++k) a = a + s->c_gd[k] * m->areaCell[k];
+    s->total_mass = a;
+  }
+}
+
+void orc_adv_get(const orc_model* m, double* q, double* u) {
+  const orc_state* s = &m->state[m->old + 4];
+  if (q) memcpy(q, s->c_gd, sizeof(double) * m->nc);
+  if (u) memcpy(u, s->e_u, sizeof(double) * m->ne);
+}
+
+double orc_adv_elapsed(const orc_model* m) { return m->elapsed; }

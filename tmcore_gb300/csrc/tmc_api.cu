@@ -1,0 +1,822 @@
+// C ABI of the library (include/tmcore_gpu.h): handle life cycle, device
+// buffers, the CRK4 step program and its CUDA graph, state transfer in the
+// caller's element order, timing.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "tmc_kernels.cuh"
+#include "tmc_prep.h"
+#include "tmcore_gpu.h"
+
+using namespace tmc;
+
+namespace {
+
+// coef2 / coef4 of the upwind corrections (operators_mod.F90:437-441, :377-380)
+double coef2_cell(int order, int mono) {
+  double c = 0.0;
+  if (order == 3) c = 1.0;
+  if (order == 3 && mono) c = 0.25;
+  return c;
+}
+double coef2_vertex(int order) { return order == 3 ? 1.0 : 0.0; }
+
+struct EngineBase {
+  virtual ~EngineBase() {}
+  virtual int alloc() = 0;
+  virtual void launch_step(bool diag, std::vector<cudaEvent_t>* flux_ev, size_t* ev_pos) = 0;
+  virtual void launch_diag_pass(bool finalize) = 0;
+  virtual void launch_spatial_only() = 0;
+  virtual void set_state_dev(const double* raw_gd, const double* raw_iap) = 0;  // from raw (original order)
+  virtual void get_field(int which, double* raw_out) = 0;                       // scatter to raw
+  virtual void set_iap_from_u(const double* ge_new, const double* u_new) = 0;
+  virtual void set_tracers_dev(const double* raw_q) = 0;
+  virtual void get_tracers_dev(double* raw_q) = 0;
+  virtual void set_ghs_dev(const double* raw) = 0;
+  virtual int launches_per_step() const = 0;
+};
+
+enum Field { F_GD = 0, F_IAP, F_U, F_PV_V, F_VOR, F_TEND_GD, F_TEND_IAP, F_GD_STAGE };
+
+}  // namespace
+
+struct tmc_handle {
+  tmc_params p{};
+  HostMesh hm;
+  DevMesh M{};
+  ModelOpt O{};
+  cudaStream_t st = nullptr;
+  std::vector<void*> dptrs;
+  size_t dbytes = 0;
+  std::string err;
+  int32_t *d_cell_n2o = nullptr, *d_edge_n2o = nullptr, *d_vert_n2o = nullptr;
+  double *raw_c = nullptr, *raw_e = nullptr, *raw_v = nullptr, *raw_q = nullptr;
+  double *op_a = nullptr, *op_b = nullptr, *op_c = nullptr, *op_out = nullptr;
+  Partials P{};
+  int counts[R_COUNT] = {};
+  double* d_diag = nullptr;
+  double* h_diag = nullptr;
+  int bs = 256;
+  bool have_state = false;
+  std::unique_ptr<EngineBase> eng;
+  cudaGraphExec_t g_step = nullptr, g_step_diag = nullptr;
+  long step_count = 0;
+  double cell_coef4 = 0.25, vert_coef4 = 0.25;  // SAVE'd coef4 of the upwind routines
+  std::vector<cudaEvent_t> ev_pool;
+
+  template <class X>
+  X* dalloc(size_t n) {
+    void* ptr = nullptr;
+    if (n == 0) n = 1;
+    if (cudaMalloc(&ptr, n * sizeof(X)) != cudaSuccess) return nullptr;
+    dptrs.push_back(ptr);
+    dbytes += n * sizeof(X);
+    return (X*)ptr;
+  }
+  template <class X>
+  X* upload(const std::vector<X>& v) {
+    X* d = dalloc<X>(v.size());
+    if (d && !v.empty()) cudaMemcpy(d, v.data(), v.size() * sizeof(X), cudaMemcpyHostToDevice);
+    return d;
+  }
+  int fail(int code, const std::string& msg) {
+    err = msg;
+    return code;
+  }
+  int cuda_check(const char* where) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(TMC_E_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+    return TMC_OK;
+  }
+};
+
+namespace {
+
+template <class T>
+struct Engine : EngineBase {
+  tmc_handle* h;
+  double* gd[3] = {};
+  T* iap[3] = {};
+  double* q[3] = {};
+  double *gd_acc = nullptr, *gd_tend = nullptr, *q_acc = nullptr, *ghs = nullptr;
+  T *iap_acc = nullptr, *iap_tend = nullptr, *gd_e = nullptr, *u = nullptr, *Fq = nullptr, *E = nullptr;
+  T *pv_v = nullptr, *vor = nullptr, *gd_v = nullptr, *pv_c = nullptr, *v_e = nullptr, *pv_e = nullptr;
+  explicit Engine(tmc_handle* hh) : h(hh) {}
+
+  int alloc() override {
+    const int nc = h->M.nc, ne = h->M.ne, nv = h->M.nv, nt = h->O.n_tracers;
+    for (int i = 0; i < 3; ++i) {
+      gd[i] = h->dalloc<double>(nc);
+      iap[i] = h->dalloc<T>(ne);
+      q[i] = h->dalloc<double>((size_t)nc * (nt > 0 ? nt : 1));
+    }
+    gd_acc = h->dalloc<double>(nc);
+    gd_tend = h->dalloc<double>(nc);
+    q_acc = h->dalloc<double>((size_t)nc * (nt > 0 ? nt : 1));
+    ghs = h->dalloc<double>(nc);
+    iap_acc = h->dalloc<T>(ne);
+    iap_tend = h->dalloc<T>(ne);
+    gd_e = h->dalloc<T>(ne);
+    u = h->dalloc<T>(ne);
+    Fq = h->dalloc<T>((size_t)ne * (nt > 0 ? nt : 1));
+    E = h->dalloc<T>(nc);
+    pv_v = h->dalloc<T>(nv);
+    vor = h->dalloc<T>(nv);
+    gd_v = h->dalloc<T>(nv);
+    pv_c = h->dalloc<T>(nc);
+    v_e = h->dalloc<T>(ne);
+    pv_e = h->dalloc<T>(ne);
+    if (!pv_e) return TMC_E_CUDA;
+    cudaMemset(ghs, 0, sizeof(double) * nc);
+    cudaMemset(q[0], 0, sizeof(double) * nc * (nt > 0 ? nt : 1));
+    return TMC_OK;
+  }
+
+  StageIO<T> io(int k) const {
+    StageIO<T> s{};
+    static const int in_slot[5] = {0, 0, 1, 2, 1}, next_slot[5] = {-1, 1, 2, 1, -1};
+    s.gd_in = gd[in_slot[k]];
+    s.gd_old = gd[0];
+    s.gd_next = next_slot[k] >= 0 ? gd[next_slot[k]] : nullptr;
+    s.gd_acc = gd_acc;
+    s.gd_tend = gd_tend;
+    s.iap_in = iap[in_slot[k]];
+    s.iap_old = iap[0];
+    s.iap_next = next_slot[k] >= 0 ? iap[next_slot[k]] : nullptr;
+    s.iap_acc = iap_acc;
+    s.iap_tend = iap_tend;
+    s.q_in = q[in_slot[k]];
+    s.q_old = q[0];
+    s.q_next = next_slot[k] >= 0 ? q[next_slot[k]] : nullptr;
+    s.q_acc = q_acc;
+    s.gd_e = gd_e;
+    s.u = u;
+    s.Fq = Fq;
+    s.E = E;
+    s.pv_v = pv_v;
+    s.vor = vor;
+    s.gd_v = gd_v;
+    s.pv_c = pv_c;
+    s.v_e = v_e;
+    s.pv_e = pv_e;
+    s.ghs = ghs;
+    return s;
+  }
+
+  int launches_per_step() const override {
+    int per_stage = 4 + ((h->O.pv_scheme == 1 && h->O.apvm_weight != 0.0) ? 1 : 0);
+    return 4 * per_stage + 2;
+  }
+
+  // one CRK4 step (time_scheme_mod.F90:109-154); state(old) updated in place
+  void launch_step(bool diag, std::vector<cudaEvent_t>* flux_ev, size_t* ev_pos) override {
+    const DevMesh& M = h->M;
+    const ModelOpt& O = h->O;
+    const double dt = O.dt;
+    const double adt[5] = {0.0, 0.5 * dt, 0.5 * dt, dt, 0.0};
+    for (int k = 1; k <= 4; ++k) {
+      StageIO<T> s = io(k);
+      const bool dg = diag && k == 1;
+      RKStage rk{k, adt[k]};
+      launch_edge_prep<T>(M, O, s, h->P, dg, h->bs, h->st);
+      launch_cell<T>(M, O, s, rk, h->P, dg, h->bs, h->st);
+      launch_vertex<T>(M, O, s, h->P, dg, h->bs, h->st);
+      launch_edge_pv<T>(M, O, s, h->bs, h->st);
+      if (flux_ev) cudaEventRecord((*flux_ev)[(*ev_pos)++], h->st);
+      launch_edge_flux<T>(M, O, s, rk, h->P, h->bs, h->st);
+      if (flux_ev) cudaEventRecord((*flux_ev)[(*ev_pos)++], h->st);
+    }
+    launch_finalize(h->P, h->counts, h->hm.totalArea, h->hm.sumAreaTriangle, dt, true, diag,
+                    h->p.conserve_energy != 0, h->d_diag, h->st);
+    launch_final_update<T>(M, O, io(1), h->d_diag, h->bs, h->st);
+  }
+
+  // diagnostics of state(old): gd_edge, u, gd/pv/vor on vertices, invariants
+  void launch_diag_pass(bool finalize) override {
+    StageIO<T> s = io(1);
+    RKStage rk{0, 0.0};
+    launch_edge_prep<T>(h->M, h->O, s, h->P, true, h->bs, h->st);
+    launch_cell<T>(h->M, h->O, s, rk, h->P, true, h->bs, h->st);
+    launch_vertex<T>(h->M, h->O, s, h->P, true, h->bs, h->st);
+    if (finalize)
+      launch_finalize(h->P, h->counts, h->hm.totalArea, h->hm.sumAreaTriangle, h->O.dt, false, true,
+                      h->p.conserve_energy != 0, h->d_diag, h->st);
+  }
+
+  // spatial_operators on the state in slot 1 -> gd_tend, iap_tend
+  void launch_spatial_only() override {
+    StageIO<T> s = io(2);
+    RKStage rk{0, 0.0};
+    launch_edge_prep<T>(h->M, h->O, s, h->P, false, h->bs, h->st);
+    launch_cell<T>(h->M, h->O, s, rk, h->P, false, h->bs, h->st);
+    launch_vertex<T>(h->M, h->O, s, h->P, false, h->bs, h->st);
+    launch_edge_pv<T>(h->M, h->O, s, h->bs, h->st);
+    launch_edge_flux<T>(h->M, h->O, s, rk, h->P, h->bs, h->st);
+  }
+
+  void set_state_dev(const double* raw_gd, const double* raw_iap) override {
+    launch_gather<double>(h->M.nc, raw_gd, h->d_cell_n2o, gd[0], h->st);
+    launch_gather<T>(h->M.ne, raw_iap, h->d_edge_n2o, iap[0], h->st);
+  }
+  void get_field(int which, double* raw) override {
+    switch (which) {
+      case F_GD: launch_scatter<double>(h->M.nc, gd[0], h->d_cell_n2o, raw, h->st); break;
+      case F_IAP: launch_scatter<T>(h->M.ne, iap[0], h->d_edge_n2o, raw, h->st); break;
+      case F_U: launch_scatter<T>(h->M.ne, u, h->d_edge_n2o, raw, h->st); break;
+      case F_PV_V: launch_scatter<T>(h->M.nv, pv_v, h->d_vert_n2o, raw, h->st); break;
+      case F_VOR: launch_scatter<T>(h->M.nv, vor, h->d_vert_n2o, raw, h->st); break;
+      case F_TEND_GD: launch_scatter<double>(h->M.nc, gd_tend, h->d_cell_n2o, raw, h->st); break;
+      case F_TEND_IAP: launch_scatter<T>(h->M.ne, iap_tend, h->d_edge_n2o, raw, h->st); break;
+    }
+  }
+  void set_iap_from_u(const double* ge_new, const double* u_new) override {
+    launch_iap_from_u<T>(h->M.ne, ge_new, u_new, iap[0], h->st);
+  }
+  void set_tracers_dev(const double* raw_q) override {
+    for (int k = 0; k < h->O.n_tracers; ++k)
+      launch_gather<double>(h->M.nc, raw_q + (size_t)k * h->M.nc, h->d_cell_n2o, q[0] + (size_t)k * h->M.nc, h->st);
+  }
+  void get_tracers_dev(double* raw_q) override {
+    for (int k = 0; k < h->O.n_tracers; ++k)
+      launch_scatter<double>(h->M.nc, q[0] + (size_t)k * h->M.nc, h->d_cell_n2o, raw_q + (size_t)k * h->M.nc, h->st);
+  }
+  void set_ghs_dev(const double* raw) override { launch_gather<double>(h->M.nc, raw, h->d_cell_n2o, ghs, h->st); }
+};
+
+DStencil upload_stencil(tmc_handle* h, const Stencil& S) {
+  DStencil d{};
+  d.width = S.width;
+  if (S.width > 0) {
+    d.count = h->upload(S.count);
+    d.idx = h->upload(S.idx);
+    d.w = h->upload(S.w);
+  }
+  return d;
+}
+
+int build_graph(tmc_handle* h, bool diag, cudaGraphExec_t* out) {
+  cudaGraph_t g = nullptr;
+  if (cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+    return h->cuda_check("cudaStreamBeginCapture");
+  h->eng->launch_step(diag, nullptr, nullptr);
+  if (cudaStreamEndCapture(h->st, &g) != cudaSuccess) return h->cuda_check("cudaStreamEndCapture");
+  cudaError_t e = cudaGraphInstantiate(out, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return h->fail(TMC_E_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+  return TMC_OK;
+}
+
+int launch_one_step(tmc_handle* h) {
+  const bool diag = h->p.diag_every > 0 && (h->step_count % h->p.diag_every) == 0;
+  if (h->p.use_graph) {
+    cudaGraphExec_t* g = diag ? &h->g_step_diag : &h->g_step;
+    if (!*g) {
+      int rc = build_graph(h, diag, g);
+      if (rc) return rc;
+    }
+    if (cudaGraphLaunch(*g, h->st) != cudaSuccess) return h->cuda_check("cudaGraphLaunch");
+  } else {
+    h->eng->launch_step(diag, nullptr, nullptr);
+  }
+  h->step_count++;
+  return h->cuda_check("step");
+}
+
+int sync(tmc_handle* h, const char* where) {
+  cudaError_t e = cudaStreamSynchronize(h->st);
+  if (e != cudaSuccess) return h->fail(TMC_E_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+  return TMC_OK;
+}
+
+int h2d(tmc_handle* h, double* dst, const double* src, size_t n) {
+  if (cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyHostToDevice, h->st) != cudaSuccess)
+    return h->cuda_check("H2D");
+  return TMC_OK;
+}
+int d2h(tmc_handle* h, double* dst, const double* src, size_t n) {
+  if (cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToHost, h->st) != cudaSuccess)
+    return h->cuda_check("D2H");
+  return TMC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int tmc_default_params(tmc_params* p) {
+  if (!p) return TMC_E_ARG;
+  std::memset(p, 0, sizeof(*p));
+  p->dt = 240.0; /* run/namelist.tmcore_swm */
+  p->time_scheme = 2;
+  p->pv_scheme = 3;
+  p->conserve_energy = 1;
+  p->flux_4th_order_correct = 0;
+  p->apvm_weight = 0.5;
+  p->adv_order = 2;
+  p->adv_mono = 1;
+  p->interp_pv_order = 3;
+  p->radius = 6371220.0;
+  p->g = 9.80616;
+  p->omega = 7.292e-5;
+  p->precision = TMC_FP64;
+  p->renumber = 1;
+  p->use_graph = 1;
+  p->diag_every = 1;
+  return TMC_OK;
+}
+
+int tmc_create(const tmc_mesh_desc* mesh, const tmc_params* params, tmc_handle** out) {
+  if (!out) return TMC_E_ARG;
+  *out = nullptr;
+  auto h = std::make_unique<tmc_handle>();
+  if (!mesh || !params) return TMC_E_ARG;
+  h->p = *params;
+  const tmc_params& p = h->p;
+  auto bad = [&](const char* m) {
+    h->err = m;
+    *out = h.release();
+    return TMC_E_ARG;
+  };
+  if (p.time_scheme != 2) {
+    h->err = "only time_scheme = 2 (CRK4) runs on the device";
+    *out = h.release();
+    return TMC_E_UNSUP;
+  }
+  if (p.pv_scheme != 1 && p.pv_scheme != 3) {
+    h->err = "pv_scheme must be 1 (APVM) or 3 (high-order upwind) on the device";
+    *out = h.release();
+    return TMC_E_UNSUP;
+  }
+  if (p.flux_4th_order_correct) {
+    h->err = "flux_4th_order_correct is not supported on the device";
+    *out = h.release();
+    return TMC_E_UNSUP;
+  }
+  if (!(p.dt > 0.0) || !(p.radius > 0.0)) return bad("dt and radius must be positive");
+  if (p.adv_order < 2 || p.adv_order > 6) return bad("adv_order must be 2..6");
+  if (p.pv_scheme == 3 && (p.interp_pv_order < 3 || p.interp_pv_order > 6)) return bad("interp_pv_order must be 3..6");
+  if (p.n_tracers < 0 || p.n_tracers > 64) return bad("n_tracers must be 0..64");
+  const int tro = p.tracer_adv_order ? p.tracer_adv_order : p.adv_order;
+  if (tro < 2 || tro > 6) return bad("tracer_adv_order must be 2..6");
+  if (p.precision != TMC_FP64 && p.precision != TMC_FP32) return bad("precision must be TMC_FP64 or TMC_FP32");
+  h->bs = p.block_size > 0 ? p.block_size : 256;
+  if (h->bs % 32 != 0 || h->bs > 512) return bad("block_size must be a multiple of 32 up to 512");
+
+  if (cudaSetDevice(p.device) != cudaSuccess) {
+    h->err = "cudaSetDevice failed (no CUDA device?)";
+    cudaGetLastError();
+    *out = h.release();
+    return TMC_E_CUDA;
+  }
+  PrepOptions opt;
+  opt.renumber = p.renumber != 0;
+  opt.cell_fit = p.stencils || p.adv_order >= 3 || (p.n_tracers > 0 && tro >= 3);
+  opt.vertex_fit = p.stencils || p.pv_scheme == 3;
+  if (!prepare_mesh(*mesh, p, opt, h->hm)) {
+    h->err = h->hm.err;
+    *out = h.release();
+    return TMC_E_ARG;
+  }
+  HostMesh& hm = h->hm;
+  if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess) {
+    h->err = "cudaStreamCreate failed";
+    *out = h.release();
+    return TMC_E_CUDA;
+  }
+  DevMesh& M = h->M;
+  M.nc = hm.nc;
+  M.ne = hm.ne;
+  M.nv = hm.nv;
+  M.me = hm.me;
+  M.me2 = hm.me2;
+  M.nEdgesOnCell = h->upload(hm.nEdgesOnCell);
+  M.edgesOnCell = h->upload(hm.edgesOnCell);
+  M.nSign = h->upload(hm.nSignEdge);
+  M.areaCell = h->upload(hm.areaCell);
+  M.cellsOnEdge = h->upload(hm.cellsOnEdge);
+  M.verticesOnEdge = h->upload(hm.verticesOnEdge);
+  M.nEdgesOnEdge = h->upload(hm.nEdgesOnEdge);
+  M.edgesOnEdge = h->upload(hm.edgesOnEdge);
+  M.weightsOnEdge = h->upload(hm.weightsOnEdge);
+  M.dcEdge = h->upload(hm.dcEdge);
+  M.dvEdge = h->upload(hm.dvEdge);
+  M.areaEdge = h->upload(hm.areaEdge);
+  M.cellsOnVertex = h->upload(hm.cellsOnVertex);
+  M.edgesOnVertex = h->upload(hm.edgesOnVertex);
+  M.tSign = h->upload(hm.tSignEdge);
+  M.kite = h->upload(hm.kite);
+  M.areaTriangle = h->upload(hm.areaTriangle);
+  M.fVertex = h->upload(hm.fVertex);
+  M.v2c_start = h->upload(hm.v2c_start);
+  M.v2c_vertex = h->upload(hm.v2c_vertex);
+  M.v2c_kite = h->upload(hm.v2c_kite);
+  M.cell2 = upload_stencil(h.get(), hm.cell2);
+  M.cell4 = upload_stencil(h.get(), hm.cell4);
+  M.vert2 = upload_stencil(h.get(), hm.vert2);
+  M.vert4 = upload_stencil(h.get(), hm.vert4);
+  h->d_cell_n2o = h->upload(hm.cell_n2o);
+  h->d_edge_n2o = h->upload(hm.edge_n2o);
+  h->d_vert_n2o = h->upload(hm.vert_n2o);
+
+  ModelOpt& O = h->O;
+  O.dt = p.dt;
+  O.adv_order = p.adv_order;
+  O.cell_coef2 = coef2_cell(p.adv_order, p.adv_mono);
+  if (p.adv_order == 6 || tro == 6) h->cell_coef4 = 0.0;
+  O.cell_coef4 = h->cell_coef4;
+  O.pv_scheme = p.pv_scheme;
+  O.apvm_weight = p.apvm_weight;
+  O.interp_pv_order = p.interp_pv_order;
+  O.vert_coef2 = coef2_vertex(p.interp_pv_order);
+  if (p.pv_scheme == 3 && p.interp_pv_order == 6) h->vert_coef4 = 0.0;
+  O.vert_coef4 = h->vert_coef4;
+  O.n_tracers = p.n_tracers;
+  O.tr_order = tro;
+  O.tr_coef2 = coef2_cell(tro, p.tracer_adv_order ? p.tracer_adv_mono : p.adv_mono);
+  O.tr_coef4 = h->cell_coef4;
+
+  const int nmax = std::max(hm.nc, std::max(hm.ne, hm.nv));
+  h->raw_c = h->dalloc<double>(hm.nc);
+  h->raw_e = h->dalloc<double>(hm.ne);
+  h->raw_v = h->dalloc<double>(hm.nv);
+  h->raw_q = h->dalloc<double>((size_t)hm.nc * (p.n_tracers > 0 ? p.n_tracers : 1));
+  h->op_a = h->dalloc<double>(nmax);
+  h->op_b = h->dalloc<double>(nmax);
+  h->op_c = h->dalloc<double>(nmax);
+  h->op_out = h->dalloc<double>(nmax);
+  const int minbs = 32;
+  h->P.cap = (nmax + minbs - 1) / minbs;
+  h->P.base = h->dalloc<double>((size_t)R_COUNT * h->P.cap * 2);
+  const int bc = (hm.nc + h->bs - 1) / h->bs, be = (hm.ne + h->bs - 1) / h->bs, bv = (hm.nv + h->bs - 1) / h->bs;
+  const int rc_cells[6] = {R_IP_C, R_IP_C + 2, R_IP_C + 4, R_44_C, R_MASS, R_EN_C};
+  const int rc_edges[5] = {R_IP_E, R_IP_E + 2, R_IP_E + 4, R_44_E, R_EN_E};
+  for (int r : rc_cells) h->counts[r] = bc;
+  for (int r : rc_edges) h->counts[r] = be;
+  h->counts[R_PE] = bv;
+  h->counts[R_AV] = bv;
+  h->d_diag = h->dalloc<double>(kDiagLen);
+  if (cudaMallocHost(&h->h_diag, sizeof(double) * kDiagLen) != cudaSuccess) h->h_diag = nullptr;
+  if (!h->d_diag || !h->h_diag || !h->P.base) {
+    h->err = "device allocation failed";
+    cudaGetLastError();
+    *out = h.release();
+    return TMC_E_CUDA;
+  }
+  cudaMemset(h->d_diag, 0, sizeof(double) * kDiagLen);
+  cudaMemset(h->P.base, 0, sizeof(double) * R_COUNT * h->P.cap * 2);
+  if (p.precision == TMC_FP32)
+    h->eng = std::make_unique<Engine<float>>(h.get());
+  else
+    h->eng = std::make_unique<Engine<double>>(h.get());
+  if (h->eng->alloc() != TMC_OK) {
+    h->err = "device allocation failed";
+    cudaGetLastError();
+    *out = h.release();
+    return TMC_E_CUDA;
+  }
+  int rc = sync(h.get(), "tmc_create");
+  if (rc == TMC_OK) rc = h->cuda_check("tmc_create");
+  *out = h.release();
+  return rc;
+}
+
+int tmc_destroy(tmc_handle* h) {
+  if (!h) return TMC_OK;
+  if (h->st) cudaStreamSynchronize(h->st);
+  if (h->g_step) cudaGraphExecDestroy(h->g_step);
+  if (h->g_step_diag) cudaGraphExecDestroy(h->g_step_diag);
+  for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
+  h->eng.reset();
+  for (void* q : h->dptrs) cudaFree(q);
+  if (h->h_diag) cudaFreeHost(h->h_diag);
+  if (h->st) cudaStreamDestroy(h->st);
+  delete h;
+  return TMC_OK;
+}
+
+const char* tmc_last_error(const tmc_handle* h) { return h ? h->err.c_str() : "null handle"; }
+
+#define TMC_REQUIRE_HANDLE(h) \
+  if (!(h) || !(h)->eng) return TMC_E_ARG;
+
+int tmc_set_initial(tmc_handle* h, const double* gd, const double* u, const double* ghs) {
+  TMC_REQUIRE_HANDLE(h);
+  if (!gd || !u || !ghs) return h->fail(TMC_E_ARG, "tmc_set_initial: NULL array");
+  const int nc = h->M.nc, ne = h->M.ne;
+  int rc;
+  if ((rc = h2d(h, h->raw_c, gd, nc))) return rc;
+  launch_gather<double>(nc, h->raw_c, h->d_cell_n2o, h->op_a, h->st);  // gd (new order, double)
+  if ((rc = h2d(h, h->raw_e, u, ne))) return rc;
+  launch_gather<double>(ne, h->raw_e, h->d_edge_n2o, h->op_b, h->st);  // u
+  // tmcore_swm_mod.F90:62-64: gd_edge = c2e(gd) [+ upwind, sign of u], iap_u = sqrt(gd_edge) u
+  launch_op(OP_C2E, h->M, h->O, h->op_a, nullptr, nullptr, h->op_out, 0, 0, 0.0, 0.0, h->bs, h->st);
+  if (h->p.adv_order >= 3)
+    launch_op(OP_UPWIND, h->M, h->O, h->op_a, h->op_b, nullptr, h->op_out, h->p.adv_order, h->p.adv_mono,
+              h->O.cell_coef2, h->O.cell_coef4, h->bs, h->st);
+  h->eng->set_state_dev(h->raw_c, h->raw_e);  // gd (iap overwritten below)
+  h->eng->set_iap_from_u(h->op_out, h->op_b);
+  if ((rc = h2d(h, h->raw_c, ghs, nc))) return rc;
+  h->eng->set_ghs_dev(h->raw_c);
+  h->have_state = true;
+  h->step_count = 0;
+  if ((rc = sync(h, "tmc_set_initial"))) return rc;
+  return h->cuda_check("tmc_set_initial");
+}
+
+int tmc_set_state(tmc_handle* h, const double* gd, const double* iap_u) {
+  TMC_REQUIRE_HANDLE(h);
+  if (!gd || !iap_u) return h->fail(TMC_E_ARG, "tmc_set_state: NULL array");
+  int rc;
+  if ((rc = h2d(h, h->raw_c, gd, h->M.nc))) return rc;
+  if ((rc = h2d(h, h->raw_e, iap_u, h->M.ne))) return rc;
+  h->eng->set_state_dev(h->raw_c, h->raw_e);
+  h->have_state = true;
+  if ((rc = sync(h, "tmc_set_state"))) return rc;
+  return h->cuda_check("tmc_set_state");
+}
+
+int tmc_get_state(tmc_handle* h, double* gd, double* iap_u, double* u) {
+  TMC_REQUIRE_HANDLE(h);
+  if (!h->have_state) return h->fail(TMC_E_STATE, "no state set");
+  int rc;
+  if (u) h->eng->launch_diag_pass(false);
+  if (gd) {
+    h->eng->get_field(F_GD, h->raw_c);
+    if ((rc = d2h(h, gd, h->raw_c, h->M.nc))) return rc;
+    if ((rc = sync(h, "tmc_get_state"))) return rc;
+  }
+  if (iap_u) {
+    h->eng->get_field(F_IAP, h->raw_e);
+    if ((rc = d2h(h, iap_u, h->raw_e, h->M.ne))) return rc;
+    if ((rc = sync(h, "tmc_get_state"))) return rc;
+  }
+  if (u) {
+    h->eng->get_field(F_U, h->raw_e);
+    if ((rc = d2h(h, u, h->raw_e, h->M.ne))) return rc;
+  }
+  if ((rc = sync(h, "tmc_get_state"))) return rc;
+  return h->cuda_check("tmc_get_state");
+}
+
+int tmc_get_vertex(tmc_handle* h, double* pv, double* vor) {
+  TMC_REQUIRE_HANDLE(h);
+  if (!h->have_state) return h->fail(TMC_E_STATE, "no state set");
+  int rc;
+  h->eng->launch_diag_pass(false);
+  if (pv) {
+    h->eng->get_field(F_PV_V, h->raw_v);
+    if ((rc = d2h(h, pv, h->raw_v, h->M.nv))) return rc;
+    if ((rc = sync(h, "tmc_get_vertex"))) return rc;
+  }
+  if (vor) {
+    h->eng->get_field(F_VOR, h->raw_v);
+    if ((rc = d2h(h, vor, h->raw_v, h->M.nv))) return rc;
+  }
+  if ((rc = sync(h, "tmc_get_vertex"))) return rc;
+  return h->cuda_check("tmc_get_vertex");
+}
+
+int tmc_set_tracers(tmc_handle* h, const double* qgd) {
+  TMC_REQUIRE_HANDLE(h);
+  if (h->O.n_tracers == 0) return TMC_OK;
+  if (!qgd) return h->fail(TMC_E_ARG, "tmc_set_tracers: NULL array");
+  int rc;
+  if ((rc = h2d(h, h->raw_q, qgd, (size_t)h->M.nc * h->O.n_tracers))) return rc;
+  h->eng->set_tracers_dev(h->raw_q);
+  if ((rc = sync(h, "tmc_set_tracers"))) return rc;
+  return h->cuda_check("tmc_set_tracers");
+}
+
+int tmc_get_tracers(tmc_handle* h, double* qgd) {
+  TMC_REQUIRE_HANDLE(h);
+  if (h->O.n_tracers == 0) return TMC_OK;
+  if (!qgd) return h->fail(TMC_E_ARG, "tmc_get_tracers: NULL array");
+  h->eng->get_tracers_dev(h->raw_q);
+  int rc;
+  if ((rc = d2h(h, qgd, h->raw_q, (size_t)h->M.nc * h->O.n_tracers))) return rc;
+  if ((rc = sync(h, "tmc_get_tracers"))) return rc;
+  return h->cuda_check("tmc_get_tracers");
+}
+
+int tmc_step(tmc_handle* h, int32_t nsteps) {
+  TMC_REQUIRE_HANDLE(h);
+  if (!h->have_state) return h->fail(TMC_E_STATE, "tmc_step before tmc_set_state/tmc_set_initial");
+  if (nsteps < 0) return h->fail(TMC_E_ARG, "nsteps < 0");
+  for (int i = 0; i < nsteps; ++i) {
+    int rc = launch_one_step(h);
+    if (rc) return rc;
+  }
+  return TMC_OK;
+}
+
+int tmc_synchronize(tmc_handle* h) {
+  TMC_REQUIRE_HANDLE(h);
+  int rc = sync(h, "tmc_synchronize");
+  if (rc) return rc;
+  return h->cuda_check("tmc_synchronize");
+}
+
+int tmc_get_diag(tmc_handle* h, double out[5]) {
+  TMC_REQUIRE_HANDLE(h);
+  if (!out) return TMC_E_ARG;
+  if (!h->have_state) return h->fail(TMC_E_STATE, "no state set");
+  h->eng->launch_diag_pass(true);
+  cudaMemcpyAsync(h->h_diag, h->d_diag, sizeof(double) * kDiagLen, cudaMemcpyDeviceToHost, h->st);
+  int rc = sync(h, "tmc_get_diag");
+  if (rc) return rc;
+  for (int i = 0; i < 4; ++i) out[i] = h->h_diag[i];
+  out[4] = h->step_count > 0 ? h->h_diag[4] : 1.0;
+  return h->cuda_check("tmc_get_diag");
+}
+
+int tmc_time_integrate(tmc_handle* h, const double* gd_old, const double* iap_u_old, const double* qgd_old,
+                       double* gd_new, double* iap_u_new, double* qgd_new) {
+  TMC_REQUIRE_HANDLE(h);
+  if (!gd_old || !iap_u_old || !gd_new || !iap_u_new) return h->fail(TMC_E_ARG, "tmc_time_integrate: NULL array");
+  const bool trc = h->O.n_tracers > 0;
+  if (trc && (!qgd_old || !qgd_new)) return h->fail(TMC_E_ARG, "tmc_time_integrate: tracers need qgd arrays");
+  const size_t nq = (size_t)h->M.nc * h->O.n_tracers;
+  int rc;
+  if ((rc = h2d(h, h->raw_c, gd_old, h->M.nc))) return rc;
+  if ((rc = h2d(h, h->raw_e, iap_u_old, h->M.ne))) return rc;
+  h->eng->set_state_dev(h->raw_c, h->raw_e);
+  if (trc) {
+    if ((rc = h2d(h, h->raw_q, qgd_old, nq))) return rc;
+    h->eng->set_tracers_dev(h->raw_q);
+  }
+  h->have_state = true;
+  if ((rc = launch_one_step(h))) return rc;
+  h->eng->get_field(F_GD, h->raw_c);
+  if ((rc = d2h(h, gd_new, h->raw_c, h->M.nc))) return rc;
+  h->eng->get_field(F_IAP, h->raw_e);
+  if ((rc = d2h(h, iap_u_new, h->raw_e, h->M.ne))) return rc;
+  if (trc) {
+    h->eng->get_tracers_dev(h->raw_q);
+    if ((rc = d2h(h, qgd_new, h->raw_q, nq))) return rc;
+  }
+  if ((rc = sync(h, "tmc_time_integrate"))) return rc;
+  return h->cuda_check("tmc_time_integrate");
+}
+
+int tmc_spatial_operators(tmc_handle* h, const double* gd, const double* iap_u, double* tend_gd,
+                          double* tend_iap_u) {
+  TMC_REQUIRE_HANDLE(h);
+  if (!gd || !iap_u || !tend_gd || !tend_iap_u) return h->fail(TMC_E_ARG, "tmc_spatial_operators: NULL array");
+  // uses state slot 1 as scratch; state(old) is untouched
+  int rc;
+  if ((rc = h2d(h, h->raw_c, gd, h->M.nc))) return rc;
+  if ((rc = h2d(h, h->raw_e, iap_u, h->M.ne))) return rc;
+  // gather into slot 1 via a temporary engine state swap: slot 0 is saved in op buffers
+  auto* e64 = dynamic_cast<Engine<double>*>(h->eng.get());
+  auto* e32 = dynamic_cast<Engine<float>*>(h->eng.get());
+  if (e64) {
+    launch_gather<double>(h->M.nc, h->raw_c, h->d_cell_n2o, e64->gd[1], h->st);
+    launch_gather<double>(h->M.ne, h->raw_e, h->d_edge_n2o, e64->iap[1], h->st);
+    cudaMemcpyAsync(e64->q[1], e64->q[0], sizeof(double) * h->M.nc * (h->O.n_tracers > 0 ? h->O.n_tracers : 1),
+                    cudaMemcpyDeviceToDevice, h->st);
+  } else {
+    launch_gather<double>(h->M.nc, h->raw_c, h->d_cell_n2o, e32->gd[1], h->st);
+    launch_gather<float>(h->M.ne, h->raw_e, h->d_edge_n2o, e32->iap[1], h->st);
+    cudaMemcpyAsync(e32->q[1], e32->q[0], sizeof(double) * h->M.nc * (h->O.n_tracers > 0 ? h->O.n_tracers : 1),
+                    cudaMemcpyDeviceToDevice, h->st);
+  }
+  h->eng->launch_spatial_only();
+  h->eng->get_field(F_TEND_GD, h->raw_c);
+  if ((rc = d2h(h, tend_gd, h->raw_c, h->M.nc))) return rc;
+  h->eng->get_field(F_TEND_IAP, h->raw_e);
+  if ((rc = d2h(h, tend_iap_u, h->raw_e, h->M.ne))) return rc;
+  if ((rc = sync(h, "tmc_spatial_operators"))) return rc;
+  return h->cuda_check("tmc_spatial_operators");
+}
+
+static int run_op(tmc_handle* h, int op, const double* a, int na, const double* b, int nb, const double* c, int nc_,
+                  const double* inout, double* out, int nout, int order, int mono) {
+  TMC_REQUIRE_HANDLE(h);
+  if (!a || !out) return h->fail(TMC_E_ARG, "NULL array");
+  const int32_t* n2o_for[4] = {nullptr, h->d_cell_n2o, h->d_edge_n2o, h->d_vert_n2o};
+  auto n_of = [&](int kind) { return kind == 1 ? h->M.nc : (kind == 2 ? h->M.ne : h->M.nv); };
+  auto raw_of = [&](int kind) { return kind == 1 ? h->raw_c : (kind == 2 ? h->raw_e : h->raw_v); };
+  int rc;
+  struct In {
+    const double* host;
+    int kind;
+    double* dev;
+  } ins[4] = {{a, na, h->op_a}, {b, nb, h->op_b}, {c, nc_, h->op_c}, {inout, nout, h->op_out}};
+  for (auto& in : ins) {
+    if (!in.host || !in.kind) continue;
+    if ((rc = h2d(h, raw_of(in.kind), in.host, n_of(in.kind)))) return rc;
+    launch_gather<double>(n_of(in.kind), raw_of(in.kind), n2o_for[in.kind], in.dev, h->st);
+  }
+  double coef2 = coef2_cell(order, mono), coef4 = 0.25;
+  if (op == OP_UPWIND) {
+    if (order >= 3 && h->M.cell2.width == 0)
+      return h->fail(TMC_E_STATE, "upwind stencil tables were not built (set tmc_params.stencils = 1)");
+    if (order == 6) h->cell_coef4 = 0.0;
+    coef4 = h->cell_coef4;
+  }
+  launch_op(op, h->M, h->O, h->op_a, h->op_b, h->op_c, h->op_out, order, mono, coef2, coef4, h->bs, h->st);
+  launch_scatter<double>(n_of(nout), h->op_out, n2o_for[nout], raw_of(nout), h->st);
+  if ((rc = d2h(h, out, raw_of(nout), n_of(nout)))) return rc;
+  if ((rc = sync(h, "tmc_op"))) return rc;
+  return h->cuda_check("tmc_op");
+}
+
+enum { K_NONE = 0, K_CELL = 1, K_EDGE = 2, K_VERT = 3 };
+
+int tmc_op_div(tmc_handle* h, const double* f, double* o) {
+  return run_op(h, OP_DIV, f, K_EDGE, nullptr, 0, nullptr, 0, nullptr, o, K_CELL, 0, 0);
+}
+int tmc_op_curl(tmc_handle* h, const double* f, double* o) {
+  return run_op(h, OP_CURL, f, K_EDGE, nullptr, 0, nullptr, 0, nullptr, o, K_VERT, 0, 0);
+}
+int tmc_op_c2e(tmc_handle* h, const double* f, double* o) {
+  return run_op(h, OP_C2E, f, K_CELL, nullptr, 0, nullptr, 0, nullptr, o, K_EDGE, 0, 0);
+}
+int tmc_op_c2v(tmc_handle* h, const double* f, double* o) {
+  return run_op(h, OP_C2V, f, K_CELL, nullptr, 0, nullptr, 0, nullptr, o, K_VERT, 0, 0);
+}
+int tmc_op_v2c(tmc_handle* h, const double* f, double* o) {
+  return run_op(h, OP_V2C, f, K_VERT, nullptr, 0, nullptr, 0, nullptr, o, K_CELL, 0, 0);
+}
+int tmc_op_v2e(tmc_handle* h, const double* f, double* o) {
+  return run_op(h, OP_V2E, f, K_VERT, nullptr, 0, nullptr, 0, nullptr, o, K_EDGE, 0, 0);
+}
+int tmc_op_kinetic_energy(tmc_handle* h, const double* u, double* o) {
+  return run_op(h, OP_KE, u, K_EDGE, nullptr, 0, nullptr, 0, nullptr, o, K_CELL, 0, 0);
+}
+int tmc_op_tangent_wind(tmc_handle* h, const double* u, double* o) {
+  return run_op(h, OP_TWIND, u, K_EDGE, nullptr, 0, nullptr, 0, nullptr, o, K_EDGE, 0, 0);
+}
+int tmc_op_tangent_vor_flux(tmc_handle* h, const double* u, const double* g, const double* pv, double* o) {
+  if (!g || !pv) return h ? h->fail(TMC_E_ARG, "NULL array") : TMC_E_ARG;
+  return run_op(h, OP_TVF, u, K_EDGE, g, K_EDGE, pv, K_EDGE, nullptr, o, K_EDGE, 0, 0);
+}
+int tmc_op_upwind_correction(tmc_handle* h, const double* f_cell, const double* u_edge, double* f_edge, int32_t order,
+                             int32_t mono) {
+  if (!u_edge || !f_edge) return h ? h->fail(TMC_E_ARG, "NULL array") : TMC_E_ARG;
+  if (order < 2 || order > 6) return h ? h->fail(TMC_E_ARG, "order must be 2..6") : TMC_E_ARG;
+  return run_op(h, OP_UPWIND, f_cell, K_CELL, u_edge, K_EDGE, nullptr, 0, f_edge, f_edge, K_EDGE, order, mono);
+}
+
+int tmc_time_steps(tmc_handle* h, int32_t nsteps, double* ms_total, double* ms_flux, int32_t* flux_launches,
+                   int32_t* total_launches) {
+  TMC_REQUIRE_HANDLE(h);
+  if (!h->have_state) return h->fail(TMC_E_STATE, "no state set");
+  if (nsteps <= 0) return h->fail(TMC_E_ARG, "nsteps must be positive");
+  const size_t nev = (size_t)nsteps * 8 + 2;
+  while (h->ev_pool.size() < nev) {
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) return h->cuda_check("cudaEventCreate");
+    h->ev_pool.push_back(e);
+  }
+  int rc;
+  if ((rc = sync(h, "tmc_time_steps"))) return rc;
+  // region 1: the production path (CUDA graph per step when enabled)
+  if (ms_total) {
+    cudaEventRecord(h->ev_pool[0], h->st);
+    for (int i = 0; i < nsteps; ++i)
+      if ((rc = launch_one_step(h))) return rc;
+    cudaEventRecord(h->ev_pool[1], h->st);
+    if ((rc = sync(h, "tmc_time_steps"))) return rc;
+    float t = 0.f;
+    cudaEventElapsedTime(&t, h->ev_pool[0], h->ev_pool[1]);
+    *ms_total = t;
+  }
+  // region 2: the same steps launched directly, with events around the edge flux pass
+  if (ms_flux) {
+    std::vector<cudaEvent_t> evs(h->ev_pool.begin() + 2, h->ev_pool.begin() + nev);
+    size_t pos = 0;
+    for (int i = 0; i < nsteps; ++i) {
+      const bool diag = h->p.diag_every > 0 && (h->step_count % h->p.diag_every) == 0;
+      h->eng->launch_step(diag, &evs, &pos);
+      h->step_count++;
+    }
+    if ((rc = sync(h, "tmc_time_steps"))) return rc;
+    double sum = 0.0;
+    for (size_t k = 0; k + 1 < pos; k += 2) {
+      float dt = 0.f;
+      cudaEventElapsedTime(&dt, evs[k], evs[k + 1]);
+      sum += dt;
+    }
+    *ms_flux = sum;
+    if (flux_launches) *flux_launches = (int32_t)(pos / 2);
+  }
+  if (total_launches) *total_launches = nsteps * h->eng->launches_per_step();
+  return h->cuda_check("tmc_time_steps");
+}
+
+int tmc_sizes(const tmc_handle* h, int64_t* nc, int64_t* ne, int64_t* nv, int64_t* bytes) {
+  if (!h) return TMC_E_ARG;
+  if (nc) *nc = h->M.nc;
+  if (ne) *ne = h->M.ne;
+  if (nv) *nv = h->M.nv;
+  if (bytes) *bytes = (int64_t)h->dbytes;
+  return TMC_OK;
+}
+
+}  // extern "C"

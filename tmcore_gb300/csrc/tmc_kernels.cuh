@@ -1,0 +1,183 @@
+// Device kernels of one TRiSK shallow-water stage and of the CRK4 step.
+//
+// Included by tmc_kernels_f64.cu (T = double, compiled with -fmad=false so
+// every element is computed in the reference's expression order and matches
+// the FP64 oracle bit for bit) and tmc_kernels_f32.cu (T = float: FP32 edge
+// and vertex state and stencil arithmetic; FP64 metrics in memory, FP64 gd and
+// tracer mass, FP64 compensated sums).
+//
+// One stage (spatial_operators, src/core/tmcore_swm_mod.F90:92-125) is five
+// passes over structure-of-arrays data in space-filling-curve order:
+//   edge_prep : gd_edge = c2e(gd) [+upwind], u = iap_u / sqrt(gd_edge),
+//               tracer fluxes                         (operators_mod.F90:93-104,
+//                                                      :168-176, :423-472)
+//   cell      : tend_gd = div_operator(u gd_edge), ke, E = ke+gd+ghs, the RK
+//               stage update of gd and tracers          (:40-55, :206-221,
+//                                                      tmcore_swm_mod.F90:127-139)
+//   vertex    : gd_vertex = c2v(gd), vor = curl(u), pv = (f+vor)/gd_vertex
+//                                                      (:76-91, :106-123, :262-270)
+//   edge_pv   : pv on edges (APVM or high-order upwind) (:273-412)
+//   edge_flux : q.F_perp (calc_tangent_vor_flux :239-260), kinetic-energy and
+//               geopotential gradient, iap_u tendency (tmcore_swm_mod.F90:155-201),
+//               the RK stage update of iap_u and the CRK4 inner products
+//               (time_scheme_mod.F90:109-154)
+// Global sums (beta, invariants) are per-block double-double partials reduced
+// by k_finalize in a fixed order: deterministic and compensated.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace tmc {
+
+struct DStencil {
+  int width;
+  const uint8_t* count;  // [2][ne]
+  const int32_t* idx;    // [width][2][ne]
+  const double* w;       // [width][2][ne]
+};
+
+struct DevMesh {
+  int nc, ne, nv, me, me2;
+  const uint8_t* nEdgesOnCell;
+  const int32_t* edgesOnCell;  // [me][nc]
+  const int8_t* nSign;         // [me][nc]
+  const double* areaCell;
+  const int32_t* cellsOnEdge;     // [2][ne]
+  const int32_t* verticesOnEdge;  // [2][ne]
+  const uint8_t* nEdgesOnEdge;
+  const int32_t* edgesOnEdge;    // [me2][ne]
+  const double* weightsOnEdge;   // [me2][ne]
+  const double* dcEdge;
+  const double* dvEdge;
+  const double* areaEdge;
+  const int32_t* cellsOnVertex;  // [3][nv]
+  const int32_t* edgesOnVertex;  // [3][nv]
+  const int8_t* tSign;           // [3][nv]
+  const double* kite;            // [3][nv]
+  const double* areaTriangle;
+  const double* fVertex;
+  const int32_t* v2c_start;
+  const int32_t* v2c_vertex;
+  const double* v2c_kite;
+  DStencil cell2, cell4, vert2, vert4;
+};
+
+struct ModelOpt {
+  double dt;
+  int adv_order;       // gd upwind correction (operators_mod.F90:423-472)
+  double cell_coef2, cell_coef4;
+  int pv_scheme;       // 1 APVM, 3 high-order upwind
+  double apvm_weight;
+  int interp_pv_order;
+  double vert_coef2, vert_coef4;
+  int n_tracers;
+  int tr_order;
+  double tr_coef2, tr_coef4;
+};
+
+// CRK4 stage program (time_scheme_mod.F90:109-154):
+//   mode 0: tendency only (spatial_operators)
+//   mode 1: acc = t, next = old + a_dt t
+//   mode 2/3: R(k-1,k) += t_prev t area, acc = acc + 2 t, next = old + a_dt t
+//   mode 4: R34 += t_prev t area, t_new = (acc + t)/6, R44 += t_new t_new area
+struct RKStage {
+  int mode;
+  double a_dt;
+};
+
+// Partial-sum regions (one double-double per block each).
+enum Region {
+  R_IP_C = 0,   // inner product <t_prev, t> cells   (region + 2*(stage-2))
+  R_IP_E = 1,   // inner product edges
+  R_44_C = 6,
+  R_44_E = 7,
+  R_MASS = 8,
+  R_EN_E = 9,
+  R_EN_C = 10,
+  R_PE = 11,
+  R_AV = 12,
+  R_COUNT = 13
+};
+
+struct Partials {
+  double* base;  // [R_COUNT][cap][2]
+  int cap;
+  __host__ __device__ double* region(int r) const { return base + (size_t)r * cap * 2; }
+};
+
+// device results: [0] mass [1] energy [2] enstrophy [3] abs vort [4] beta
+//                 [5] R12 [6] R23 [7] R34 [8] R44 [9] beta*dt [10] health flags
+constexpr int kDiagLen = 12;
+
+template <class T>
+struct StageIO {
+  // stage input state and RK buffers
+  const double* gd_in;
+  const double* gd_old;
+  double* gd_next;
+  double* gd_acc;
+  double* gd_tend;  // current tendency (read as t_prev before overwrite)
+  const T* iap_in;
+  const T* iap_old;
+  T* iap_next;
+  T* iap_acc;
+  T* iap_tend;
+  const double* q_in;  // tracers [ntr][nc]
+  const double* q_old;
+  double* q_next;
+  double* q_acc;
+  // intermediates
+  T* gd_e;
+  T* u;
+  T* Fq;  // [ntr][ne]
+  T* E;
+  T* pv_v;
+  T* vor;
+  T* gd_v;
+  T* pv_c;
+  T* v_e;
+  T* pv_e;
+  const double* ghs;
+};
+
+// ---- launchers (instantiated in tmc_kernels_f64.cu / _f32.cu) ----
+template <class T>
+void launch_edge_prep(const DevMesh& M, const ModelOpt& O, const StageIO<T>& S, Partials P, bool diag, int bs,
+                      cudaStream_t st);
+template <class T>
+void launch_cell(const DevMesh& M, const ModelOpt& O, const StageIO<T>& S, RKStage rk, Partials P, bool diag,
+                 int bs, cudaStream_t st);
+template <class T>
+void launch_vertex(const DevMesh& M, const ModelOpt& O, const StageIO<T>& S, Partials P, bool diag, int bs,
+                   cudaStream_t st);
+template <class T>
+void launch_edge_pv(const DevMesh& M, const ModelOpt& O, const StageIO<T>& S, int bs, cudaStream_t st);
+template <class T>
+void launch_edge_flux(const DevMesh& M, const ModelOpt& O, const StageIO<T>& S, RKStage rk, Partials P, int bs,
+                      cudaStream_t st);
+template <class T>
+void launch_final_update(const DevMesh& M, const ModelOpt& O, const StageIO<T>& S, const double* diag, int bs,
+                         cudaStream_t st);
+
+// reduction of partial regions into diag[]; counts per region
+void launch_finalize(Partials P, const int* counts_host, double totalArea, double sumAreaTriangle, double dt,
+                     bool step, bool diag, bool conserve, double* diag_out, cudaStream_t st);
+
+// state transfer in the caller's element order: dst[i] = src[n2o[i]] / dst[n2o[i]] = src[i]
+template <class T>
+void launch_gather(int n, const double* src, const int32_t* n2o, T* dst, cudaStream_t st);
+template <class T>
+void launch_scatter(int n, const T* src, const int32_t* n2o, double* dst, cudaStream_t st);
+// iap_u = sqrt(gd_edge) * u (iap_swm_operator, operators_mod.F90:158-166)
+template <class T>
+void launch_iap_from_u(int ne, const double* gd_e, const double* u, T* iap, cudaStream_t st);
+
+// single operators for parity (FP64 only)
+void launch_op(int op, const DevMesh& M, const ModelOpt& O, const double* a, const double* b, const double* c,
+               double* out, int order, int mono, double coef2, double coef4, int bs, cudaStream_t st);
+
+// operator ids for launch_op
+enum OpId { OP_DIV = 0, OP_CURL, OP_C2E, OP_C2V, OP_V2C, OP_V2E, OP_KE, OP_TWIND, OP_TVF, OP_UPWIND };
+
+}  // namespace tmc

@@ -1,0 +1,182 @@
+"""Python host mirror of the C ABI: one shallow-water model on one GPU.
+
+Method names follow the reference's integrator/operator interface
+(src/core/time_scheme_mod.F90:14-43, src/core/operators_mod.F90:15-30);
+arrays are numpy float64 in the mesh file's element order.  There is no CPU
+path: if the CUDA library or a GPU is missing, construction raises.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib, abi
+
+REF_RADIUS = 6371220.0  # src/utils/const_mod.F90:11
+REF_G = 9.80616
+REF_OMEGA = 7.292e-5
+
+
+class TMCError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"tmcore_gpu error {code}: {msg}")
+        self.code = code
+
+
+def default_params(**kw) -> abi.Params:
+    """tmc_params with the shipped SWM namelist defaults, overridden by ``kw``."""
+    p = abi.Params()
+    lib = _lib.gpu()
+    lib.tmc_default_params(ctypes.byref(p))
+    for k, v in kw.items():
+        if not any(f[0] == k for f in abi.Params._fields_):
+            raise KeyError(k)
+        setattr(p, k, v)
+    return p
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+class TMCoreGPU:
+    """A device-resident shallow-water model (handle of the C ABI)."""
+
+    def __init__(self, mesh, params: abi.Params | None = None, **kw):
+        self.lib = _lib.gpu()
+        self.params = params if params is not None else default_params(**kw)
+        self.mesh = mesh
+        self.nc, self.ne, self.nv = mesh.nCells, mesh.nEdges, mesh.nVertices
+        d = abi.MeshDesc()
+        for k in ("nCells", "nEdges", "nVertices", "maxEdges", "maxEdges2", "vertexDegree"):
+            setattr(d, k, int(mesh.dims[k]))
+        self._keep = []
+        for name, _ in abi.MeshDesc._fields_[6:]:
+            a = mesh.vars[name]
+            a = np.ascontiguousarray(a, dtype=np.int32 if a.dtype.kind == "i" else np.float64)
+            self._keep.append(a)
+            setattr(d, name, a.ctypes.data)
+        h = ctypes.c_void_p()
+        rc = self.lib.tmc_create(ctypes.byref(d), ctypes.byref(self.params), ctypes.byref(h))
+        self.h = h
+        if rc != 0:
+            msg = self.lib.tmc_last_error(h).decode() if h.value else "tmc_create failed"
+            self.close()
+            raise TMCError(rc, msg)
+        self.n_tracers = int(self.params.n_tracers)
+
+    # ------------------------------------------------------------------
+    def _chk(self, rc):
+        if rc != 0:
+            raise TMCError(rc, self.lib.tmc_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            self.lib.tmc_destroy(self.h)
+        self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # ------------------------------------------------------------------ state
+    def set_initial(self, gd, u, ghs):
+        self._chk(self.lib.tmc_set_initial(self.h, _ptr(_f64(gd)), _ptr(_f64(u)), _ptr(_f64(ghs))))
+
+    def set_state(self, gd, iap_u):
+        self._chk(self.lib.tmc_set_state(self.h, _ptr(_f64(gd)), _ptr(_f64(iap_u))))
+
+    def get_state(self, with_u: bool = True):
+        gd, iap = np.empty(self.nc), np.empty(self.ne)
+        u = np.empty(self.ne) if with_u else None
+        self._chk(self.lib.tmc_get_state(self.h, _ptr(gd), _ptr(iap), _ptr(u)))
+        return (gd, iap, u) if with_u else (gd, iap)
+
+    def get_vertex(self):
+        pv, vor = np.empty(self.nv), np.empty(self.nv)
+        self._chk(self.lib.tmc_get_vertex(self.h, _ptr(pv), _ptr(vor)))
+        return pv, vor
+
+    def set_tracers(self, qgd):
+        self._chk(self.lib.tmc_set_tracers(self.h, _ptr(_f64(qgd))))
+
+    def get_tracers(self):
+        q = np.empty((self.n_tracers, self.nc))
+        self._chk(self.lib.tmc_get_tracers(self.h, _ptr(q)))
+        return q
+
+    # ------------------------------------------------------------------ stepping
+    def step(self, n: int = 1):
+        self._chk(self.lib.tmc_step(self.h, int(n)))
+
+    def synchronize(self):
+        self._chk(self.lib.tmc_synchronize(self.h))
+
+    def diag(self):
+        """[total_mass, total_energy, total_potential_enstrophy, total_absolute_vorticity, beta]"""
+        out = np.empty(5)
+        self._chk(self.lib.tmc_get_diag(self.h, _ptr(out)))
+        return out
+
+    def time_integrate(self, gd_old, iap_old, q_old=None, out=None):
+        """One step with host arrays in and out (tmc_time_integrate)."""
+        if out is None:
+            out = (np.empty(self.nc), np.empty(self.ne),
+                   np.empty((self.n_tracers, self.nc)) if self.n_tracers else None)
+        gd_new, iap_new, q_new = out
+        self._chk(self.lib.tmc_time_integrate(self.h, _ptr(gd_old), _ptr(iap_old), _ptr(q_old),
+                                              _ptr(gd_new), _ptr(iap_new), _ptr(q_new)))
+        return out
+
+    def spatial_operators(self, gd, iap_u):
+        tg, tu = np.empty(self.nc), np.empty(self.ne)
+        self._chk(self.lib.tmc_spatial_operators(self.h, _ptr(_f64(gd)), _ptr(_f64(iap_u)), _ptr(tg), _ptr(tu)))
+        return tg, tu
+
+    def time_steps(self, n: int, total: bool = True, flux: bool = True):
+        """Device timing of n steps: (ms_total, ms_flux_kernel, flux_launches, total_launches)."""
+        a, b = ctypes.c_double(), ctypes.c_double()
+        c, d = ctypes.c_int32(), ctypes.c_int32()
+        self._chk(self.lib.tmc_time_steps(self.h, int(n), ctypes.byref(a) if total else None,
+                                          ctypes.byref(b) if flux else None, ctypes.byref(c), ctypes.byref(d)))
+        return (a.value if total else None), (b.value if flux else None), c.value, d.value
+
+    def sizes(self):
+        v = [ctypes.c_int64() for _ in range(4)]
+        self._chk(self.lib.tmc_sizes(self.h, *[ctypes.byref(x) for x in v]))
+        return tuple(x.value for x in v)
+
+    # ------------------------------------------------------------------ operators
+    _OUT = {"div": "c", "curl": "v", "c2e": "e", "c2v": "v", "v2c": "c", "v2e": "e",
+            "kinetic_energy": "c", "tangent_wind": "e"}
+
+    def op(self, name: str, f):
+        n = {"c": self.nc, "e": self.ne, "v": self.nv}[self._OUT[name]]
+        out = np.empty(n)
+        self._chk(getattr(self.lib, "tmc_op_" + name)(self.h, _ptr(_f64(f)), _ptr(out)))
+        return out
+
+    def tangent_vor_flux(self, u, gd_e, pv_e):
+        out = np.empty(self.ne)
+        self._chk(self.lib.tmc_op_tangent_vor_flux(self.h, _ptr(_f64(u)), _ptr(_f64(gd_e)), _ptr(_f64(pv_e)),
+                                                   _ptr(out)))
+        return out
+
+    def upwind_correction(self, f_cell, u_edge, f_edge, order: int, mono: int = 0):
+        fe = np.array(f_edge, dtype=np.float64)
+        self._chk(self.lib.tmc_op_upwind_correction(self.h, _ptr(_f64(f_cell)), _ptr(_f64(u_edge)), _ptr(fe),
+                                                    int(order), int(mono)))
+        return fe
