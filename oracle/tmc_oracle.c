@@ -51,6 +51,7 @@ struct orc_model {
   double *deriv2OnCell, *deriv3OnCell, *deriv4OnCell, *deriv2OnVertex, *deriv4OnVertex;  /* (0:30,2,ne) */
   /* SAVE'd locals of the upwind routines (operators_mod.F90:367-368, :429-430) */
   double upw_cell_coef4, upw_vtx_coef4;
+  int fit_built;
   /* model */
   orc_state state[7]; /* index slot + 4: state(-4:2) */
   orc_tend tend[7];
@@ -1167,8 +1168,11 @@ orc_model* orc_create(const orc_mesh_in* in, const orc_params* p) {
   {
     int tro = p->tracer_adv_order ? p->tracer_adv_order : p->adv_order;
     int need = p->adv_order >= 3 || p->pv_scheme == 3 || p->flux_4th_order_correct ||
-               (p->n_tracers > 0 && tro >= 3) || p->nthreads < 0;
-    if (need) poly_fit_run(m);
+               (p->n_tracers > 0 && tro >= 3);
+    if (need) {
+      poly_fit_run(m);
+      m->fit_built = 1;
+    }
   }
 
   for (int i = 0; i < 7; ++i) {
@@ -1217,6 +1221,10 @@ const int32_t* orc_nSignEdge(const orc_model* m) { return m->nSignEdge; }
 const int32_t* orc_tSignEdge(const orc_model* m) { return m->tSignEdge; }
 
 int orc_poly_fit_table(const orc_model* m, const char* name, const void** data, int64_t* count) {
+  if (!m->fit_built) {
+    poly_fit_run((orc_model*)m);
+    ((orc_model*)m)->fit_built = 1;
+  }
   size_t nc = m->nc, ne = m->ne, nv = m->nv;
 #define T(nm, ptr, cnt)            \
   if (strcmp(name, nm) == 0) {     \
@@ -1255,6 +1263,10 @@ void orc_op_tangent_vor_flux(orc_model* m, const double* u, const double* g, con
   calc_tangent_vor_flux(m, u, g, q, o);
 }
 void orc_op_upwind_correction(orc_model* m, const double* f, const double* u, double* fe, int order, int mono) {
+  if (order >= 3 && !m->fit_built) {
+    poly_fit_run(m);
+    m->fit_built = 1;
+  }
   add_upwind_correction_on_cell(m, f, u, fe, order, mono);
 }
 

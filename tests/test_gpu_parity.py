@@ -87,10 +87,13 @@ def test_initial_state_and_diag(mesh4):
     g.set_initial(gd, u, ghs)
     go, io, uo = o.state()
     gg, ig, ug = g.get_state()
-    assert np.array_equal(gg, go) and np.array_equal(ig, io) and np.array_equal(ug, uo)
+    assert np.array_equal(gg, go) and np.array_equal(ig, io)
+    # the oracle keeps the initial-condition u; the device reports iap_u / sqrt(gd_edge)
+    assert rel_max(ug, uo) < 4e-16
     pvo, voro = o.vertex()
     pvg, vorg = g.get_vertex()
-    assert np.array_equal(pvg, pvo) and np.array_equal(vorg, voro)
+    # vorticity and pv of the device follow from that u (1-ulp differences in u)
+    assert rel_max(pvg, pvo) < 1e-14 and rel_max(vorg, voro) < 1e-12
     do, dg = o.diag(), g.diag()
     assert abs(dg[0] - do[0]) <= 1e-14 * abs(do[0])
     assert abs(dg[1] - do[1]) <= 1e-14 * abs(do[1])
@@ -161,7 +164,7 @@ def test_tracers_match_oracle(mesh4):
     g.set_tracers(qgd)
     o.step(10)
     g.step(10)
-    qo, qg = o.tracers(), g.tracers()
+    qo, qg = o.tracers(), g.get_tracers()
     assert rel_max(qg, qo) < 1e-13
     gg, _, _ = g.get_state()
     assert np.max(np.abs(qg[2] / gg - 1.0)) < 1e-12

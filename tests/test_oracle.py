@@ -1,0 +1,192 @@
+"""The CPU FP64 oracle against physics-level known answers of the reference.
+
+TMCORE ships no golden vectors (no test data, no expected outputs, meshes
+git-ignored) and cannot be compiled here, so the oracle's parity with the
+Fortran is UNPINNED; these tests pin what the reference's own test cases and
+design guarantee:
+
+* steady geostrophic flow (steady_geostrophic_flow_test_mod.F90:20-54) stays
+  steady up to truncation error, converging with resolution;
+* total mass and total absolute vorticity are conserved to round-off, and
+  total energy is conserved to round-off by the CRK4 beta
+  (time_scheme_mod.F90:144-150);
+* q.F_perp does no work (calc_tangent_vor_flux, operators_mod.F90:239-260):
+  sum(areaEdge * F * pv_flx) = 0 for any F and symmetric pv average;
+* the cosine bell returns to its initial position after one period
+  (cosine_bell_rotation_test_mod.F90:15-20), mass conserved;
+* operator identities: curl of a discrete gradient vanishes, div of a
+  constant normal flux vanishes over the sphere.
+"""
+import numpy as np
+import pytest
+
+from conftest import icos, rel_max
+
+ORACLE = pytest.importorskip("oracle.oracle")
+
+
+def make(mesh, **kw):
+    return ORACLE.Oracle(mesh, **kw)
+
+
+def test_steady_geostrophic_converges():
+    from tmcore_gb300 import cases
+
+    errs = []
+    for level, dt in ((3, 1800.0), (4, 900.0)):
+        m = icos(level)
+        gd, u, ghs = cases.steady_geostrophic_flow(m)
+        o = make(m, dt=dt, pv_scheme=1, apvm_weight=0.0)
+        o.set_initial(gd, u, ghs)
+        o.step(int(86400 / dt))
+        g1, _, _ = o.state()
+        errs.append(rel_max(g1, gd))
+    assert errs[1] < errs[0] and errs[1] < 2e-3
+
+
+@pytest.mark.parametrize("pv_scheme,adv_order", [(1, 2), (3, 2), (1, 3), (3, 4)])
+def test_conservation(pv_scheme, adv_order):
+    from tmcore_gb300 import cases
+
+    m = icos(4)
+    gd, u, ghs = cases.jet_bumps(m, seed=11)
+    o = make(m, dt=900.0, pv_scheme=pv_scheme, adv_order=adv_order, adv_mono=1, apvm_weight=0.5)
+    o.set_initial(gd, u, ghs)
+    d0 = o.diag()
+    o.step(24)
+    d1 = o.diag()
+    assert abs(d1[0] - d0[0]) / d0[0] < 1e-13  # mass
+    if adv_order == 2:
+        # energy, beta-scaled CRK4.  With adv_order >= 3 the upwind-corrected
+        # tend_gd_edge is no longer c2e(tend_gd), which the kinetic-energy
+        # budget of the IAP form needs, so the scheme itself stops conserving.
+        assert abs(d1[1] - d0[1]) / d0[1] < 1e-13
+    else:
+        assert abs(d1[1] - d0[1]) / d0[1] < 1e-5
+    _, vor = o.vertex()
+    assert abs(d1[3] - d0[3]) < 1e-12 * np.max(np.abs(vor))  # absolute vorticity
+    assert 0.9 < d1[4] < 1.1  # beta near 1
+
+
+def test_energy_not_conserved_without_beta():
+    from tmcore_gb300 import cases
+
+    m = icos(4)
+    gd, u, ghs = cases.jet_bumps(m, seed=11)
+    o = make(m, dt=900.0, pv_scheme=1, apvm_weight=0.0, conserve_energy=0)
+    o.set_initial(gd, u, ghs)
+    d0 = o.diag()
+    o.step(24)
+    d1 = o.diag()
+    assert d1[4] == 1.0
+    assert abs(d1[1] - d0[1]) / d0[1] > 1e-12
+
+
+def test_tangent_vor_flux_does_no_work():
+    m = icos(3)
+    o = make(m)
+    rng = np.random.default_rng(0)
+    u = rng.standard_normal(m.nEdges)
+    ge = rng.uniform(1.0, 2.0, m.nEdges)
+    pe = rng.standard_normal(m.nEdges)
+    flx = o.op("tangent_vor_flux", u, ge, pe, out_size=m.nEdges)
+    ae = o.area_edge()
+    work = np.sum(ae * u * ge * flx)
+    scale = np.sum(np.abs(ae * u * ge * flx))
+    assert abs(work) < 1e-13 * scale
+
+
+def test_operator_identities():
+    m = icos(3)
+    o = make(m)
+    rng = np.random.default_rng(1)
+    f = rng.standard_normal(m.nCells)
+    # discrete gradient on edges, (f(c2)-f(c1))/dc; its curl vanishes
+    dc = m.dcEdge * 6371220.0
+    grad = (f[m.cellsOnEdge[:, 1] - 1] - f[m.cellsOnEdge[:, 0] - 1]) / dc
+    curl = o.op("curl", grad, out_size=m.nVertices)
+    assert np.max(np.abs(curl)) < 1e-12 * np.max(np.abs(grad)) / np.min(dc)
+    # area-weighted divergence sums to zero (every edge flux leaves one cell, enters another)
+    fe = rng.standard_normal(m.nEdges)
+    div = o.op("div", fe, out_size=m.nCells)
+    area = m.areaCell * 6371220.0 ** 2
+    assert abs(np.sum(div * area)) < 1e-9 * np.sum(np.abs(div * area))
+    # c2e / c2v of a constant
+    one = np.ones(m.nCells)
+    assert np.allclose(o.op("c2e", one, out_size=m.nEdges), 1.0, rtol=0, atol=1e-15)
+    assert np.allclose(o.op("c2v", one, out_size=m.nVertices), 1.0, rtol=0, atol=1e-14)
+
+
+def test_upwind_correction_is_exact_for_quadratics_and_zero_for_constants():
+    m = icos(4)
+    o = make(m, adv_order=3)
+    u = np.ones(m.nEdges)
+    const = np.full(m.nCells, 5.0)
+    fe = o.op("c2e", const, out_size=m.nEdges)
+    for order in (3, 4, 5):
+        out = o.upwind_correction(const, u, fe, order, 0)
+        assert np.max(np.abs(out - 5.0)) < 1e-12
+
+
+def test_cosine_bell_returns():
+    """Solid-body rotation (alpha = pi/2) brings the bell back after 12 days."""
+    from tmcore_gb300 import cases
+
+    m = icos(4)
+    q0 = cases.cosine_bell(m)
+    dt = 3600.0
+    o = make(m, dt=dt, adv_order=3, adv_mono=1, conserve_energy=0)
+    o.adv_set_initial(q0, 1)  # ORC_WIND_COSINE_BELL
+    m0 = np.sum(q0 * m.areaCell)
+    o.adv_step(int(12 * 86400 / dt))
+    q1, _ = o.adv_state()
+    assert abs(np.sum(q1 * m.areaCell) - m0) / m0 < 1e-12
+    l2 = np.sqrt(np.sum(m.areaCell * (q1 - q0) ** 2) / np.sum(m.areaCell * q0 ** 2))
+    assert l2 < 0.35
+
+
+def test_deformation_flow_returns():
+    """Nondivergent deformation flow case 4 (deformation_flow_test_mod.F90:74-105)."""
+    from tmcore_gb300 import cases
+
+    m = icos(4)
+    q0 = cases.deformation_flow(m, "gaussian_hills")
+    dt = 3600.0
+    o = make(m, dt=dt, adv_order=5, adv_mono=1, conserve_energy=0)
+    o.adv_set_initial(q0, 2)  # ORC_WIND_DEFORMATION_CASE4
+    o.adv_step(int(12 * 86400 / dt))
+    q1, _ = o.adv_state()
+    l2 = np.sqrt(np.sum(m.areaCell * (q1 - q0) ** 2) / np.sum(m.areaCell * q0 ** 2))
+    assert l2 < 0.3
+    assert abs(np.sum(q1 * m.areaCell) - np.sum(q0 * m.areaCell)) / np.sum(q0 * m.areaCell) < 1e-12
+
+
+def test_coupled_tracer_constant_stays_constant():
+    from tmcore_gb300 import cases
+
+    m = icos(3)
+    gd, u, ghs = cases.jet_bumps(m, seed=3)
+    o = make(m, dt=1800.0, pv_scheme=1, apvm_weight=0.0, n_tracers=2, tracer_adv_order=3, tracer_adv_mono=1)
+    o.set_initial(gd, u, ghs)
+    q = np.stack([np.ones(m.nCells), cases.smooth_tracers(m, 1, seed=3)[0]])
+    o.set_tracers(q * gd[None, :])
+    m0 = np.sum(q[1] * gd * m.areaCell)
+    o.step(12)
+    g1, _, _ = o.state()
+    qt = o.tracers()
+    assert np.max(np.abs(qt[0] / g1 - 1.0)) < 1e-12
+    assert abs(np.sum(qt[1] * m.areaCell) - m0) / m0 < 1e-12
+
+
+def test_poly_fit_tables_shape():
+    m = icos(3)
+    o = make(m, adv_order=3, pv_scheme=3)
+    n2 = o.poly_table("nFit2Cells")
+    assert np.all(n2 == m.nEdgesOnCell + 1)
+    n4 = o.poly_table("nFit4Cells")
+    assert np.all((n4 >= 16) & (n4 <= 19)) and np.median(n4) == 19  # 2-ring: 1 + 6 + 12 away from pentagons
+    nv = o.poly_table("nFit2Vertices")
+    assert np.all((nv >= 10) & (nv <= 13))
+    # second-derivative weights of a centre-relative stencil sum to a finite number
+    d2 = o.poly_table("deriv2OnCell").reshape(m.nEdges, 2, 31)
+    assert np.all(np.isfinite(d2))

@@ -6,6 +6,7 @@
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <type_traits>
 #include <string>
 #include <vector>
 
@@ -36,6 +37,7 @@ struct EngineBase {
   virtual void get_field(int which, double* raw_out) = 0;                       // scatter to raw
   virtual void set_iap_from_u(const double* ge_new, const double* u_new) = 0;
   virtual void set_tracers_dev(const double* raw_q) = 0;
+  virtual void refresh_shadows(int slot) = 0;
   virtual void get_tracers_dev(double* raw_q) = 0;
   virtual void set_ghs_dev(const double* raw) = 0;
   virtual int launches_per_step() const = 0;
@@ -102,8 +104,14 @@ struct Engine : EngineBase {
   tmc_handle* h;
   double* gd[3] = {};
   T* iap[3] = {};
-  double* q[3] = {};
-  double *gd_acc = nullptr, *gd_tend = nullptr, *q_acc = nullptr, *ghs = nullptr;
+  T* q[3] = {};
+  float* tendf = nullptr;  // FP32 path: gd tendency and topography shadows
+  float* ghsf = nullptr;
+  float* gdf[3] = {};  // FP32 path: shadows of gd and tracer mixing ratios per slot
+  float* qr[3] = {};
+  T* F = nullptr;
+  double *gd_acc = nullptr, *gd_tend = nullptr, *ghs = nullptr;
+  T* q_acc = nullptr;
   T *iap_acc = nullptr, *iap_tend = nullptr, *gd_e = nullptr, *u = nullptr, *Fq = nullptr, *E = nullptr;
   T *pv_v = nullptr, *vor = nullptr, *gd_v = nullptr, *pv_c = nullptr, *v_e = nullptr, *pv_e = nullptr;
   explicit Engine(tmc_handle* hh) : h(hh) {}
@@ -113,11 +121,11 @@ struct Engine : EngineBase {
     for (int i = 0; i < 3; ++i) {
       gd[i] = h->dalloc<double>(nc);
       iap[i] = h->dalloc<T>(ne);
-      q[i] = h->dalloc<double>((size_t)nc * (nt > 0 ? nt : 1));
+      q[i] = h->dalloc<T>((size_t)nc * (nt > 0 ? nt : 1));
     }
     gd_acc = h->dalloc<double>(nc);
     gd_tend = h->dalloc<double>(nc);
-    q_acc = h->dalloc<double>((size_t)nc * (nt > 0 ? nt : 1));
+    q_acc = h->dalloc<T>((size_t)nc * (nt > 0 ? nt : 1));
     ghs = h->dalloc<double>(nc);
     iap_acc = h->dalloc<T>(ne);
     iap_tend = h->dalloc<T>(ne);
@@ -131,9 +139,22 @@ struct Engine : EngineBase {
     pv_c = h->dalloc<T>(nc);
     v_e = h->dalloc<T>(ne);
     pv_e = h->dalloc<T>(ne);
-    if (!pv_e) return TMC_E_CUDA;
+    F = h->dalloc<T>(ne);
+    if (!std::is_same<T, double>::value) {
+      for (int i = 0; i < 3; ++i) {
+        gdf[i] = h->dalloc<float>(nc);
+        qr[i] = h->dalloc<float>((size_t)nc * (nt > 0 ? nt : 1));
+      }
+    }
+    if (!pv_e || !F) return TMC_E_CUDA;
     cudaMemset(ghs, 0, sizeof(double) * nc);
-    cudaMemset(q[0], 0, sizeof(double) * nc * (nt > 0 ? nt : 1));
+    if (!std::is_same<T, double>::value) {
+      tendf = h->dalloc<float>(nc);
+      ghsf = h->dalloc<float>(nc);
+      if (!tendf || !ghsf) return TMC_E_CUDA;
+      cudaMemset(ghsf, 0, sizeof(float) * nc);
+    }
+    cudaMemset(q[0], 0, sizeof(T) * nc * (nt > 0 ? nt : 1));
     return TMC_OK;
   }
 
@@ -165,11 +186,18 @@ struct Engine : EngineBase {
     s.v_e = v_e;
     s.pv_e = pv_e;
     s.ghs = ghs;
+    s.F = F;
+    s.gdf_in = gdf[in_slot[k]];
+    s.gdf_next = next_slot[k] >= 0 ? gdf[next_slot[k]] : nullptr;
+    s.qr_in = qr[in_slot[k]];
+    s.qr_next = next_slot[k] >= 0 ? qr[next_slot[k]] : nullptr;
+    s.tendf = tendf;
+    s.ghsf = ghsf;
     return s;
   }
 
   int launches_per_step() const override {
-    int per_stage = 4 + ((h->O.pv_scheme == 1 && h->O.apvm_weight != 0.0) ? 1 : 0);
+    int per_stage = 5 + ((h->O.pv_scheme == 1 && h->O.apvm_weight != 0.0) ? 1 : 0);
     return 4 * per_stage + 2;
   }
 
@@ -222,6 +250,11 @@ struct Engine : EngineBase {
   void set_state_dev(const double* raw_gd, const double* raw_iap) override {
     launch_gather<double>(h->M.nc, raw_gd, h->d_cell_n2o, gd[0], h->st);
     launch_gather<T>(h->M.ne, raw_iap, h->d_edge_n2o, iap[0], h->st);
+    refresh_shadows(0);
+  }
+  void refresh_shadows(int slot) override {
+    if constexpr (!std::is_same<T, double>::value)
+      launch_shadows(h->M.nc, h->O.n_tracers, gd[slot], q[slot], gdf[slot], qr[slot], h->st);
   }
   void get_field(int which, double* raw) override {
     switch (which) {
@@ -239,13 +272,21 @@ struct Engine : EngineBase {
   }
   void set_tracers_dev(const double* raw_q) override {
     for (int k = 0; k < h->O.n_tracers; ++k)
-      launch_gather<double>(h->M.nc, raw_q + (size_t)k * h->M.nc, h->d_cell_n2o, q[0] + (size_t)k * h->M.nc, h->st);
+      launch_gather<T>(h->M.nc, raw_q + (size_t)k * h->M.nc, h->d_cell_n2o, q[0] + (size_t)k * h->M.nc, h->st);
+    refresh_shadows(0);
   }
   void get_tracers_dev(double* raw_q) override {
     for (int k = 0; k < h->O.n_tracers; ++k)
-      launch_scatter<double>(h->M.nc, q[0] + (size_t)k * h->M.nc, h->d_cell_n2o, raw_q + (size_t)k * h->M.nc, h->st);
+      launch_scatter<T>(h->M.nc, q[0] + (size_t)k * h->M.nc, h->d_cell_n2o, raw_q + (size_t)k * h->M.nc, h->st);
   }
-  void set_ghs_dev(const double* raw) override { launch_gather<double>(h->M.nc, raw, h->d_cell_n2o, ghs, h->st); }
+  void set_ghs_dev(const double* raw) override {
+    launch_gather<double>(h->M.nc, raw, h->d_cell_n2o, ghs, h->st);
+    if (ghsf) launch_to_f32((size_t)h->M.nc, ghs, ghsf, h->st);
+  }
+  void copy_tracers_to_slot1() {
+    cudaMemcpyAsync(q[1], q[0], sizeof(T) * h->M.nc * (h->O.n_tracers > 0 ? h->O.n_tracers : 1),
+                    cudaMemcpyDeviceToDevice, h->st);
+  }
 };
 
 DStencil upload_stencil(tmc_handle* h, const Stencil& S) {
@@ -375,6 +416,16 @@ int tmc_create(const tmc_mesh_desc* mesh, const tmc_params* params, tmc_handle**
   }
   PrepOptions opt;
   opt.renumber = p.renumber != 0;
+  if (p.precision == TMC_FP32) {
+    // the FP32 kernels unroll over 6 edges per cell and 10 edges per edge
+    if (mesh->maxEdges > 6 || mesh->maxEdges2 > 10) {
+      h->err = "the FP32 path supports maxEdges <= 6 and maxEdges2 <= 10";
+      *out = h.release();
+      return TMC_E_UNSUP;
+    }
+    opt.min_me = 6;
+    opt.min_me2 = 10;
+  }
   opt.cell_fit = p.stencils || p.adv_order >= 3 || (p.n_tracers > 0 && tro >= 3);
   opt.vertex_fit = p.stencils || p.pv_scheme == 3;
   if (!prepare_mesh(*mesh, p, opt, h->hm)) {
@@ -415,6 +466,25 @@ int tmc_create(const tmc_mesh_desc* mesh, const tmc_params* params, tmc_handle**
   M.v2c_start = h->upload(hm.v2c_start);
   M.v2c_vertex = h->upload(hm.v2c_vertex);
   M.v2c_kite = h->upload(hm.v2c_kite);
+  if (p.precision == TMC_FP32) {
+    auto f32 = [](const std::vector<double>& v) { return std::vector<float>(v.begin(), v.end()); };
+    auto inv32 = [](const std::vector<double>& v) {
+      std::vector<float> o(v.size());
+      for (size_t i = 0; i < v.size(); ++i) o[i] = (float)(1.0 / v[i]);
+      return o;
+    };
+    std::vector<double> invA(hm.areaCell.size());
+    for (size_t i = 0; i < invA.size(); ++i) invA[i] = 1.0 / hm.areaCell[i];
+    M.weightsOnEdge_f = h->upload(f32(hm.weightsOnEdge));
+    M.dcEdge_f = h->upload(f32(hm.dcEdge));
+    M.dvEdge_f = h->upload(f32(hm.dvEdge));
+    M.areaEdge_f = h->upload(f32(hm.areaEdge));
+    M.kite_f = h->upload(f32(hm.kite));
+    M.invAreaTriangle_f = h->upload(inv32(hm.areaTriangle));
+    M.fVertex_f = h->upload(f32(hm.fVertex));
+    M.invAreaCell_f = h->upload(inv32(hm.areaCell));
+    M.invAreaCell = h->upload(invA);
+  }
   M.cell2 = upload_stencil(h.get(), hm.cell2);
   M.cell4 = upload_stencil(h.get(), hm.cell4);
   M.vert2 = upload_stencil(h.get(), hm.vert2);
@@ -452,14 +522,14 @@ int tmc_create(const tmc_mesh_desc* mesh, const tmc_params* params, tmc_handle**
   const int minbs = 32;
   h->P.cap = (nmax + minbs - 1) / minbs;
   h->P.base = h->dalloc<double>((size_t)R_COUNT * h->P.cap * 2);
-  const int bc = (hm.nc + h->bs - 1) / h->bs, be = (hm.ne + h->bs - 1) / h->bs, bv = (hm.nv + h->bs - 1) / h->bs;
+  const int bc = grid_for(hm.nc, h->bs), be = grid_for(hm.ne, h->bs), bv = grid_for(hm.nv, h->bs);
   const int rc_cells[6] = {R_IP_C, R_IP_C + 2, R_IP_C + 4, R_44_C, R_MASS, R_EN_C};
   const int rc_edges[5] = {R_IP_E, R_IP_E + 2, R_IP_E + 4, R_44_E, R_EN_E};
   for (int r : rc_cells) h->counts[r] = bc;
   for (int r : rc_edges) h->counts[r] = be;
   h->counts[R_PE] = bv;
   h->counts[R_AV] = bv;
-  h->d_diag = h->dalloc<double>(kDiagLen);
+  h->d_diag = h->dalloc<double>(kDiagLen + R_COUNT + 2);  // outputs, region sums, finaliser counter
   if (cudaMallocHost(&h->h_diag, sizeof(double) * kDiagLen) != cudaSuccess) h->h_diag = nullptr;
   if (!h->d_diag || !h->h_diag || !h->P.base) {
     h->err = "device allocation failed";
@@ -467,7 +537,7 @@ int tmc_create(const tmc_mesh_desc* mesh, const tmc_params* params, tmc_handle**
     *out = h.release();
     return TMC_E_CUDA;
   }
-  cudaMemset(h->d_diag, 0, sizeof(double) * kDiagLen);
+  cudaMemset(h->d_diag, 0, sizeof(double) * (kDiagLen + R_COUNT + 2));
   cudaMemset(h->P.base, 0, sizeof(double) * R_COUNT * h->P.cap * 2);
   if (p.precision == TMC_FP32)
     h->eng = std::make_unique<Engine<float>>(h.get());
@@ -677,13 +747,12 @@ int tmc_spatial_operators(tmc_handle* h, const double* gd, const double* iap_u, 
   if (e64) {
     launch_gather<double>(h->M.nc, h->raw_c, h->d_cell_n2o, e64->gd[1], h->st);
     launch_gather<double>(h->M.ne, h->raw_e, h->d_edge_n2o, e64->iap[1], h->st);
-    cudaMemcpyAsync(e64->q[1], e64->q[0], sizeof(double) * h->M.nc * (h->O.n_tracers > 0 ? h->O.n_tracers : 1),
-                    cudaMemcpyDeviceToDevice, h->st);
+    e64->copy_tracers_to_slot1();
   } else {
     launch_gather<double>(h->M.nc, h->raw_c, h->d_cell_n2o, e32->gd[1], h->st);
     launch_gather<float>(h->M.ne, h->raw_e, h->d_edge_n2o, e32->iap[1], h->st);
-    cudaMemcpyAsync(e32->q[1], e32->q[0], sizeof(double) * h->M.nc * (h->O.n_tracers > 0 ? h->O.n_tracers : 1),
-                    cudaMemcpyDeviceToDevice, h->st);
+    e32->copy_tracers_to_slot1();
+    e32->refresh_shadows(1);
   }
   h->eng->launch_spatial_only();
   h->eng->get_field(F_TEND_GD, h->raw_c);

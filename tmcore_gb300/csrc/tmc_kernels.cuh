@@ -3,32 +3,37 @@
 // Included by tmc_kernels_f64.cu (T = double, compiled with -fmad=false so
 // every element is computed in the reference's expression order and matches
 // the FP64 oracle bit for bit) and tmc_kernels_f32.cu (T = float: FP32 edge
-// and vertex state and stencil arithmetic; FP64 metrics in memory, FP64 gd and
-// tracer mass, FP64 compensated sums).
+// and vertex state and stencil arithmetic from FP32-rounded copies of the
+// metrics; FP64 gd and tracer mass with the mass-flux divergence accumulated
+// in FP64; FP64 compensated sums).
 //
 // One stage (spatial_operators, src/core/tmcore_swm_mod.F90:92-125) is five
 // passes over structure-of-arrays data in space-filling-curve order:
 //   edge_prep : gd_edge = c2e(gd) [+upwind], u = iap_u / sqrt(gd_edge),
-//               tracer fluxes                         (operators_mod.F90:93-104,
-//                                                      :168-176, :423-472)
-//   cell      : tend_gd = div_operator(u gd_edge), ke, E = ke+gd+ghs, the RK
-//               stage update of gd and tracers          (:40-55, :206-221,
-//                                                      tmcore_swm_mod.F90:127-139)
+//               F = u gd_edge, tracer fluxes       (operators_mod.F90:93-104,
+//                                                   :168-176, :423-472)
+//   cell      : tend_gd = div_operator(F), ke, E = ke+gd+ghs, the RK stage
+//               update of gd and tracers            (:40-55, :206-221,
+//                                                   tmcore_swm_mod.F90:127-139)
 //   vertex    : gd_vertex = c2v(gd), vor = curl(u), pv = (f+vor)/gd_vertex
-//                                                      (:76-91, :106-123, :262-270)
+//                                                   (:76-91, :106-123, :262-270)
 //   edge_pv   : pv on edges (APVM or high-order upwind) (:273-412)
 //   edge_flux : q.F_perp (calc_tangent_vor_flux :239-260), kinetic-energy and
 //               geopotential gradient, iap_u tendency (tmcore_swm_mod.F90:155-201),
 //               the RK stage update of iap_u and the CRK4 inner products
 //               (time_scheme_mod.F90:109-154)
-// Global sums (beta, invariants) are per-block double-double partials reduced
-// by k_finalize in a fixed order: deterministic and compensated.
+// Each thread handles kEPT elements (block-strided, so loads stay coalesced).
+// Global sums (beta, invariants) are per-thread sums, a warp shuffle tree and
+// a double-double combination of the warp sums per block; k_finalize reduces
+// the per-block partials in a fixed order: deterministic and compensated.
 #pragma once
 
 #include <cstdint>
 #include <cuda_runtime.h>
 
 namespace tmc {
+
+constexpr int kEPT = 4;  // elements per thread
 
 struct DStencil {
   int width;
@@ -61,6 +66,17 @@ struct DevMesh {
   const int32_t* v2c_vertex;
   const double* v2c_kite;
   DStencil cell2, cell4, vert2, vert4;
+  // FP32 path: FP32-rounded copies of the metrics used in FP32 arithmetic
+  // and FP64 reciprocals of the areas used in FP64 arithmetic (null in FP64 mode)
+  const float* weightsOnEdge_f;
+  const float* dcEdge_f;
+  const float* dvEdge_f;
+  const float* areaEdge_f;
+  const float* kite_f;
+  const float* invAreaTriangle_f;
+  const float* fVertex_f;
+  const float* invAreaCell_f;
+  const double* invAreaCell;
 };
 
 struct ModelOpt {
@@ -88,8 +104,8 @@ struct RKStage {
 
 // Partial-sum regions (one double-double per block each).
 enum Region {
-  R_IP_C = 0,   // inner product <t_prev, t> cells   (region + 2*(stage-2))
-  R_IP_E = 1,   // inner product edges
+  R_IP_C = 0,  // inner product <t_prev, t> cells   (region + 2*(stage-2))
+  R_IP_E = 1,  // inner product edges
   R_44_C = 6,
   R_44_E = 7,
   R_MASS = 8,
@@ -107,7 +123,7 @@ struct Partials {
 };
 
 // device results: [0] mass [1] energy [2] enstrophy [3] abs vort [4] beta
-//                 [5] R12 [6] R23 [7] R34 [8] R44 [9] beta*dt [10] health flags
+//                 [5] R12 [6] R23 [7] R34 [8] R44 [9] beta*dt
 constexpr int kDiagLen = 12;
 
 template <class T>
@@ -123,13 +139,22 @@ struct StageIO {
   T* iap_next;
   T* iap_acc;
   T* iap_tend;
-  const double* q_in;  // tracers [ntr][nc]
-  const double* q_old;
-  double* q_next;
-  double* q_acc;
+  const T* q_in;  // tracer mass gd*q [ntr][nc] (FP32 in the FP32 path)
+  const T* q_old;
+  T* q_next;
+  T* q_acc;
+  // FP32 shadows (FP32 path only): gd and tracer mixing ratio of the stage,
+  // the current gd tendency, topography
+  const float* gdf_in;
+  float* gdf_next;
+  const float* qr_in;  // [ntr][nc]
+  float* qr_next;
+  float* tendf;        // gd tendency of the stage (read as t_prev before overwrite)
+  const float* ghsf;
   // intermediates
   T* gd_e;
   T* u;
+  T* F;   // u * gd_e
   T* Fq;  // [ntr][ne]
   T* E;
   T* pv_v;
@@ -159,6 +184,8 @@ void launch_edge_flux(const DevMesh& M, const ModelOpt& O, const StageIO<T>& S, 
 template <class T>
 void launch_final_update(const DevMesh& M, const ModelOpt& O, const StageIO<T>& S, const double* diag, int bs,
                          cudaStream_t st);
+// number of blocks a launcher uses for n elements
+inline int grid_for(int n, int bs) { return (n + bs * kEPT - 1) / (bs * kEPT); }
 
 // reduction of partial regions into diag[]; counts per region
 void launch_finalize(Partials P, const int* counts_host, double totalArea, double sumAreaTriangle, double dt,
@@ -172,6 +199,9 @@ void launch_scatter(int n, const T* src, const int32_t* n2o, double* dst, cudaSt
 // iap_u = sqrt(gd_edge) * u (iap_swm_operator, operators_mod.F90:158-166)
 template <class T>
 void launch_iap_from_u(int ne, const double* gd_e, const double* u, T* iap, cudaStream_t st);
+// FP32 shadows of gd and tracer mixing ratios of a state slot (FP32 path)
+void launch_shadows(int nc, int ntr, const double* gd, const float* q, float* gdf, float* qr, cudaStream_t st);
+void launch_to_f32(size_t n, const double* src, float* dst, cudaStream_t st);
 
 // single operators for parity (FP64 only)
 void launch_op(int op, const DevMesh& M, const ModelOpt& O, const double* a, const double* b, const double* c,

@@ -1,6 +1,7 @@
 // FP64 instantiation (compiled with -fmad=false: no FMA contraction, so each
 // element follows the reference's IEEE operation order), the reduction
-// finaliser and the single-operator kernels used for parity.
+// finaliser, the FP32 shadow helpers and the single-operator kernels used for
+// parity.
 #include "tmc_kernels_impl.cuh"
 
 namespace tmc {
@@ -13,57 +14,59 @@ struct FinalizeArgs {
   int step, diag, conserve;
 };
 
-// Fixed-order reduction of the per-block partials into diag_out
-// (time_scheme_mod.F90:144-150 beta; tmcore_swm_mod.F90:215-255 invariants).
-__global__ void __launch_bounds__(256) k_finalize(Partials P, FinalizeArgs a, double* out) {
-  __shared__ double res[R_COUNT];
-  for (int r = 0; r < R_COUNT; ++r) {
-    const bool want = (r <= R_44_E) ? a.step : a.diag;
-    if (!want) continue;  // uniform across the block
+// One block per partial region: a fixed-order double-double reduction of the
+// region's per-block partials; the last block to finish (atomic counter, no
+// waiting) combines the region sums into beta and the invariants
+// (time_scheme_mod.F90:144-150; tmcore_swm_mod.F90:215-255) and re-arms the
+// counter.
+__global__ void __launch_bounds__(256) k_finalize(Partials P, FinalizeArgs a, double* out, double* res,
+                                                  unsigned int* counter) {
+  const int r = blockIdx.x;
+  const bool want = (r <= R_44_E) ? a.step : a.diag;
+  if (want) {
     DD acc{0.0, 0.0};
     const double* reg = P.region(r);
     for (int i = threadIdx.x; i < a.counts[r]; i += blockDim.x) acc = dd_add(acc, DD{reg[2 * i], reg[2 * i + 1]});
-    DD v[1] = {acc};
-    const int rr[1] = {r};
-    // reduce into a scratch slot: reuse region r's first entry after the loop
+    __shared__ DD sm[8];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    DD w = warp_reduce_dd(acc);
+    if (lane == 0) sm[warp] = w;
     __syncthreads();
-    {
-      __shared__ DD sm[8];
-      const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
-      DD w = warp_reduce(v[0]);
-      if (lane == 0) sm[warp] = w;
-      __syncthreads();
-      if (warp == 0) {
-        w = (lane < nw) ? sm[lane] : DD{0.0, 0.0};
-        w = warp_reduce(w);
-        if (lane == 0) res[r] = w.hi;
-      }
-      __syncthreads();
+    if (warp == 0) {
+      w = (lane < nw) ? sm[lane] : DD{0.0, 0.0};
+      w = warp_reduce_dd(w);
+      if (lane == 0) res[r] = w.hi;
     }
-    (void)rr;
+  }
+  __shared__ bool last;
+  if (threadIdx.x == 0) {
+    __threadfence();
+    last = (atomicAdd(counter, 1u) == gridDim.x - 1);
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    if (a.step) {
-      double R[4];
-      for (int k = 0; k < 3; ++k) R[k] = (res[R_IP_E + 2 * k] + res[R_IP_C + 2 * k]) / a.totalArea;
-      R[3] = (res[R_44_E] + res[R_44_C]) / a.totalArea;
-      double beta = 1.0;
-      if (a.conserve) beta = (R[0] + R[1] + R[2]) / (3.0 * R[3]);
-      out[4] = beta;
-      out[5] = R[0];
-      out[6] = R[1];
-      out[7] = R[2];
-      out[8] = R[3];
-      out[9] = beta * a.dt;
-    }
-    if (a.diag) {
-      out[0] = res[R_MASS];
-      out[1] = res[R_EN_E] + res[R_EN_C];
-      out[2] = res[R_PE];
-      out[3] = res[R_AV] / a.sumAreaTriangle;
-    }
+  if (!last || threadIdx.x != 0) return;
+  __threadfence();
+  volatile const double* rv = res;
+  if (a.step) {
+    double R[4];
+    for (int k = 0; k < 3; ++k) R[k] = (rv[R_IP_E + 2 * k] + rv[R_IP_C + 2 * k]) / a.totalArea;
+    R[3] = (rv[R_44_E] + rv[R_44_C]) / a.totalArea;
+    double beta = 1.0;
+    if (a.conserve) beta = (R[0] + R[1] + R[2]) / (3.0 * R[3]);
+    out[4] = beta;
+    out[5] = R[0];
+    out[6] = R[1];
+    out[7] = R[2];
+    out[8] = R[3];
+    out[9] = beta * a.dt;
   }
+  if (a.diag) {
+    out[0] = rv[R_MASS];
+    out[1] = rv[R_EN_E] + rv[R_EN_C];
+    out[2] = rv[R_PE];
+    out[3] = rv[R_AV] / a.sumAreaTriangle;
+  }
+  *counter = 0u;
 }
 
 void launch_finalize(Partials P, const int* counts_host, double totalArea, double sumAreaTriangle, double dt,
@@ -76,7 +79,31 @@ void launch_finalize(Partials P, const int* counts_host, double totalArea, doubl
   a.step = step ? 1 : 0;
   a.diag = diag ? 1 : 0;
   a.conserve = conserve ? 1 : 0;
-  k_finalize<<<1, 256, 0, st>>>(P, a, diag_out);
+  // scratch after the kDiagLen outputs: R_COUNT region sums, then the counter
+  double* res = diag_out + kDiagLen;
+  unsigned int* counter = reinterpret_cast<unsigned int*>(diag_out + kDiagLen + R_COUNT);
+  k_finalize<<<R_COUNT, 256, 0, st>>>(P, a, diag_out, res, counter);
+}
+
+__global__ void k_shadows(int nc, int ntr, const double* gd, const float* q, float* gdf, float* qr) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  const float g = (float)gd[c];
+  gdf[c] = g;
+  for (int k = 0; k < ntr; ++k) qr[(size_t)k * nc + c] = q[(size_t)k * nc + c] / g;
+}
+
+void launch_shadows(int nc, int ntr, const double* gd, const float* q, float* gdf, float* qr, cudaStream_t st) {
+  k_shadows<<<nblk(nc, 256), 256, 0, st>>>(nc, ntr, gd, q, gdf, qr);
+}
+
+__global__ void k_to_f32(size_t n, const double* src, float* dst) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = (float)src[i];
+}
+
+void launch_to_f32(size_t n, const double* src, float* dst, cudaStream_t st) {
+  k_to_f32<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, src, dst);
 }
 
 // ---------------------------------------------------------------------------
@@ -87,7 +114,7 @@ __global__ void __launch_bounds__(kMaxBlock) k_op(int op, DevMesh M, const doubl
                                                   double coef4) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   switch (op) {
-    case OP_DIV:
+    case OP_DIV:  // :40-55
       if (i < M.nc) {
         double s = 0.0;
         for (int k = 0; k < M.nEdgesOnCell[i]; ++k) {
@@ -97,7 +124,7 @@ __global__ void __launch_bounds__(kMaxBlock) k_op(int op, DevMesh M, const doubl
         out[i] = (-s) / M.areaCell[i];
       }
       break;
-    case OP_CURL:
+    case OP_CURL:  // :76-91
       if (i < M.nv) {
         double s = 0.0;
         for (int k = 0; k < 3; ++k) {
@@ -107,17 +134,17 @@ __global__ void __launch_bounds__(kMaxBlock) k_op(int op, DevMesh M, const doubl
         out[i] = (-s) / M.areaTriangle[i];
       }
       break;
-    case OP_C2E:
+    case OP_C2E:  // :93-104
       if (i < M.ne) out[i] = 0.5 * (a[M.cellsOnEdge[i]] + a[M.cellsOnEdge[M.ne + i]]);
       break;
-    case OP_C2V:
+    case OP_C2V:  // :106-123
       if (i < M.nv) {
         double s = 0.0;
         for (int k = 0; k < 3; ++k) s = s + a[M.cellsOnVertex[(size_t)k * M.nv + i]] * M.kite[(size_t)k * M.nv + i];
         out[i] = s / M.areaTriangle[i];
       }
       break;
-    case OP_V2C:
+    case OP_V2C:  // :125-141
       if (i < M.nc) {
         double s = 0.0;
         for (int k = M.v2c_start[i]; k < M.v2c_start[i + 1]; ++k)
@@ -125,10 +152,10 @@ __global__ void __launch_bounds__(kMaxBlock) k_op(int op, DevMesh M, const doubl
         out[i] = s;
       }
       break;
-    case OP_V2E:
+    case OP_V2E:  // :143-156
       if (i < M.ne) out[i] = 0.5 * (a[M.verticesOnEdge[i]] + a[M.verticesOnEdge[M.ne + i]]);
       break;
-    case OP_KE:
+    case OP_KE:  // :206-221
       if (i < M.nc) {
         double s = 0.0;
         for (int k = 0; k < M.nEdgesOnCell[i]; ++k) {
@@ -138,7 +165,7 @@ __global__ void __launch_bounds__(kMaxBlock) k_op(int op, DevMesh M, const doubl
         out[i] = (s * 0.25) / M.areaCell[i];
       }
       break;
-    case OP_TWIND:
+    case OP_TWIND:  // :223-237
       if (i < M.ne) {
         double s = 0.0;
         for (int k = 0; k < M.nEdgesOnEdge[i]; ++k)
@@ -146,7 +173,7 @@ __global__ void __launch_bounds__(kMaxBlock) k_op(int op, DevMesh M, const doubl
         out[i] = s;
       }
       break;
-    case OP_TVF:
+    case OP_TVF:  // :239-260
       if (i < M.ne) {
         double s = 0.0;
         for (int k = 0; k < M.nEdgesOnEdge[i]; ++k) {
@@ -156,7 +183,7 @@ __global__ void __launch_bounds__(kMaxBlock) k_op(int op, DevMesh M, const doubl
         out[i] = s;
       }
       break;
-    case OP_UPWIND:
+    case OP_UPWIND:  // :423-472
       if (i < M.ne) {
         const int c1 = M.cellsOnEdge[i], c2 = M.cellsOnEdge[M.ne + i];
         out[i] = upwind_edge<double>(M.cell2, M.cell4, order, coef2, coef4, M.ne, i, c1, c2, out[i], b[i],

@@ -1,11 +1,27 @@
 // Kernel bodies for tmc_kernels.cuh (included once per precision TU).
+//
+// Every kernel has two branches selected at compile time:
+//  * T = double: the reference's arithmetic, element by element, in its
+//    expression order (no FMA: the TU is compiled with -fmad=false);
+//  * T = float: the fast path.  Neighbour indices and weights are loaded
+//    first (fixed unrolled widths: maxEdges 6, maxEdges2 10, padded entries
+//    carry zero weights or zero signs), then the neighbour gathers, then the
+//    arithmetic, so each thread keeps tens of independent loads in flight.
+//    GB300 executes FP64 at a small fraction of its FP32 rate, so the FP32
+//    path keeps FP64 only for the gd tendency (from an FP32 two-sum
+//    compensated flux divergence), the gd RK accumulation and the per-thread
+//    invariant sums.
 #pragma once
+
+#include <type_traits>
 
 #include "tmc_kernels.cuh"
 
 namespace tmc {
 
 constexpr int kMaxBlock = 512;
+constexpr int kME = 6;    // unrolled maxEdges of the FP32 path
+constexpr int kME2 = 10;  // unrolled maxEdges2 of the FP32 path
 
 // ---------------------------------------------------------------------------
 // double-double accumulation (Knuth TwoSum), never contracted into FMA
@@ -22,7 +38,7 @@ __device__ __forceinline__ DD dd_add(DD a, DD b) {
   double lo = __dsub_rn(e, __dsub_rn(hi, s));
   return {hi, lo};
 }
-__device__ __forceinline__ DD warp_reduce(DD v) {
+__device__ __forceinline__ DD warp_reduce_dd(DD v) {
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) {
     DD o;
@@ -32,22 +48,28 @@ __device__ __forceinline__ DD warp_reduce(DD v) {
   }
   return v;
 }
-// Reduce N values over the block; thread 0 writes region[r[k]][block] for each k.
-template <int N>
-__device__ __forceinline__ void block_reduce_store(DD (&v)[N], const Partials& P, const int (&r)[N]) {
-  __shared__ DD sm[N][kMaxBlock / 32];
+
+// Reduce N per-thread partial sums over the block and store region[r[k]][block]
+// as (hi, lo).  Each warp sums its lanes with a shuffle tree in A (double or
+// float); warp 0 combines the warp sums in double-double.  Every thread of the
+// block must call this (it synchronises).
+template <class A, int N>
+__device__ __forceinline__ void block_store(const A (&v)[N], const Partials& P, const int (&r)[N]) {
+  __shared__ double sm[N][kMaxBlock / 32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
 #pragma unroll
   for (int k = 0; k < N; ++k) {
-    DD w = warp_reduce(v[k]);
-    if (lane == 0) sm[k][warp] = w;
+    A w = v[k];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) w += __shfl_down_sync(0xffffffffu, w, off);
+    if (lane == 0) sm[k][warp] = (double)w;
   }
   __syncthreads();
   if (warp == 0) {
 #pragma unroll
     for (int k = 0; k < N; ++k) {
-      DD w = (lane < nw) ? sm[k][lane] : DD{0.0, 0.0};
-      w = warp_reduce(w);
+      DD w = (lane < nw) ? DD{sm[k][lane], 0.0} : DD{0.0, 0.0};
+      w = warp_reduce_dd(w);
       if (lane == 0) {
         double* reg = P.region(r[k]);
         reg[2 * blockIdx.x] = w.hi;
@@ -55,12 +77,40 @@ __device__ __forceinline__ void block_reduce_store(DD (&v)[N], const Partials& P
       }
     }
   }
+  __syncthreads();
+}
+
+template <class T>
+constexpr bool kF64 = std::is_same<T, double>::value;
+
+// metric in the arithmetic type: FP64 array in FP64 mode, FP32 copy otherwise
+template <class T>
+__device__ __forceinline__ T met(const double* d, const float* f, size_t i) {
+  if constexpr (kF64<T>)
+    return d[i];
+  else
+    return f[i];
 }
 
 template <class T>
 __device__ __forceinline__ T sgn1(T x) {
   return copysign(T(1), x);
 }
+
+// FP32 error-free addition (TwoSum): hi + lo accumulates p exactly
+__device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float p) {
+  const float t = __fadd_rn(hi, p);
+  const float bp = __fsub_rn(t, hi);
+  const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(t, bp)), __fsub_rn(p, bp));
+  hi = t;
+  lo = __fadd_rn(lo, err);
+}
+
+// block-strided loop: thread handles i = base + k*blockDim.x, k < kEPT
+#define TMC_FOR_EPT(i, n)                                                              \
+  for (int _k = 0, i = blockIdx.x * (kEPT * blockDim.x) + threadIdx.x; _k < kEPT; \
+       ++_k, i += blockDim.x)                                                          \
+    if (i < (n))
 
 // Upwind correction of an edge value from two-sided polynomial-fit stencils
 // (operators_mod.F90:423-472 for cells, :359-412 for vertices).  `f(i)`
@@ -69,89 +119,117 @@ template <class T, class F>
 __device__ __forceinline__ T upwind_edge(const DStencil& S2, const DStencil& S4, int order, T coef2, T coef4, int ne,
                                          int e, int ctr0, int ctr1, T fe, T sgn_of, T dist, F f) {
   if (order == 3 || order == 4) {
-    T d[2];
-    const int ctr[2] = {ctr0, ctr1};
+    T d0, d1;
 #pragma unroll
     for (int s = 0; s < 2; ++s) {
-      T fc = f(ctr[s]);
+      const T fc = f(s == 0 ? ctr0 : ctr1);
       T acc = T(0);
-      int n = S2.count[(size_t)s * ne + e];
+      const int n = S2.count[(size_t)s * ne + e];
       for (int j = 0; j < n; ++j) {
-        size_t k = ((size_t)j * 2 + s) * ne + e;
+        const size_t k = ((size_t)j * 2 + s) * ne + e;
         acc = acc + T(S2.w[k]) * (f(S2.idx[k]) - fc);
       }
-      d[s] = acc;
+      if (s == 0)
+        d0 = acc;
+      else
+        d1 = acc;
     }
-    fe = fe - dist * dist * ((d[0] + d[1]) - sgn1(sgn_of) * coef2 * (d[1] - d[0])) / T(12);
+    fe = fe - dist * dist * ((d0 + d1) - sgn1(sgn_of) * coef2 * (d1 - d0)) / T(12);
   } else if (order == 5 || order == 6) {
-    T d2[2], d4[2];
-    const int ctr[2] = {ctr0, ctr1};
+    T a0, a1, b0, b1;
 #pragma unroll
     for (int s = 0; s < 2; ++s) {
-      T fc = f(ctr[s]);
+      const T fc = f(s == 0 ? ctr0 : ctr1);
       T acc = T(0);
       int n = S2.count[(size_t)s * ne + e];
       for (int j = 0; j < n; ++j) {
-        size_t k = ((size_t)j * 2 + s) * ne + e;
+        const size_t k = ((size_t)j * 2 + s) * ne + e;
         acc = acc + T(S2.w[k]) * (f(S2.idx[k]) - fc);
       }
-      d2[s] = acc;
-      acc = T(0);
+      T acc4 = T(0);
       n = S4.count[(size_t)s * ne + e];
       for (int j = 0; j < n; ++j) {
-        size_t k = ((size_t)j * 2 + s) * ne + e;
-        acc = acc + T(S4.w[k]) * (f(S4.idx[k]) - fc);
+        const size_t k = ((size_t)j * 2 + s) * ne + e;
+        acc4 = acc4 + T(S4.w[k]) * (f(S4.idx[k]) - fc);
       }
-      d4[s] = acc;
+      if (s == 0) {
+        a0 = acc;
+        b0 = acc4;
+      } else {
+        a1 = acc;
+        b1 = acc4;
+      }
     }
-    fe = fe - dist * dist * (d2[0] + d2[1]) / T(12) +
-         (dist * dist) * (dist * dist) * ((d4[0] + d4[1]) - sgn1(sgn_of) * coef4 * (d4[1] - d4[0])) / T(60);
+    fe = fe - dist * dist * (a0 + a1) / T(12) +
+         (dist * dist) * (dist * dist) * ((b0 + b1) - sgn1(sgn_of) * coef4 * (b1 - b0)) / T(60);
   }
   return fe;
 }
 
 // ---------------------------------------------------------------------------
-// edge_prep
+// edge_prep: gd_edge, u, mass flux F, tracer fluxes
 // ---------------------------------------------------------------------------
 template <class T>
 __global__ void __launch_bounds__(kMaxBlock) k_edge_prep(DevMesh M, ModelOpt O, StageIO<T> S, Partials P, int diag) {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  DD en{0.0, 0.0};
-  if (e < M.ne) {
+  double en = 0.0;
+  TMC_FOR_EPT(e, M.ne) {
     const int c1 = M.cellsOnEdge[e], c2 = M.cellsOnEdge[M.ne + e];
-    const T g1 = T(S.gd_in[c1]), g2 = T(S.gd_in[c2]);
-    T ge = T(0.5) * (g1 + g2);
     const T ia = S.iap_in[e];
+    T g1, g2;
+    if constexpr (kF64<T>) {
+      g1 = S.gd_in[c1];
+      g2 = S.gd_in[c2];
+    } else {
+      g1 = S.gdf_in[c1];
+      g2 = S.gdf_in[c2];
+    }
+    T ge = T(0.5) * (g1 + g2);
     if (O.adv_order >= 3) {
-      const double* gd = S.gd_in;
-      ge = upwind_edge<T>(M.cell2, M.cell4, O.adv_order, T(O.cell_coef2), T(O.cell_coef4), M.ne, e, c1, c2, ge, ia,
-                          T(M.dcEdge[e]), [gd](int i) { return T(gd[i]); });
+      if constexpr (kF64<T>) {
+        const double* gd = S.gd_in;
+        ge = upwind_edge<T>(M.cell2, M.cell4, O.adv_order, T(O.cell_coef2), T(O.cell_coef4), M.ne, e, c1, c2, ge,
+                            ia, M.dcEdge[e], [gd](int i) { return gd[i]; });
+      } else {
+        const float* gd = S.gdf_in;
+        ge = upwind_edge<T>(M.cell2, M.cell4, O.adv_order, T(O.cell_coef2), T(O.cell_coef4), M.ne, e, c1, c2, ge,
+                            ia, M.dcEdge_f[e], [gd](int i) { return gd[i]; });
+      }
     }
     const T sq = sqrt(ge);
     const T uu = ia / sq;
+    const T F = uu * ge;
     S.gd_e[e] = ge;
     S.u[e] = uu;
-    if (O.n_tracers > 0) {
-      const T F = uu * ge;
-      for (int k = 0; k < O.n_tracers; ++k) {
+    S.F[e] = F;
+    for (int k = 0; k < O.n_tracers; ++k) {
+      T qe;
+      if constexpr (kF64<T>) {
         const double* q = S.q_in + (size_t)k * M.nc;
         const double* gd = S.gd_in;
-        T qe = T(0.5) * (T(q[c1]) / g1 + T(q[c2]) / g2);
+        qe = 0.5 * (q[c1] / g1 + q[c2] / g2);
         if (O.tr_order >= 3)
           qe = upwind_edge<T>(M.cell2, M.cell4, O.tr_order, T(O.tr_coef2), T(O.tr_coef4), M.ne, e, c1, c2, qe, ia,
-                              T(M.dcEdge[e]), [q, gd](int i) { return T(q[i]) / T(gd[i]); });
-        S.Fq[(size_t)k * M.ne + e] = F * qe;
+                              M.dcEdge[e], [q, gd](int i) { return q[i] / gd[i]; });
+      } else {
+        const float* qr = S.qr_in + (size_t)k * M.nc;
+        qe = 0.5f * (qr[c1] + qr[c2]);
+        if (O.tr_order >= 3)
+          qe = upwind_edge<T>(M.cell2, M.cell4, O.tr_order, T(O.tr_coef2), T(O.tr_coef4), M.ne, e, c1, c2, qe, ia,
+                              M.dcEdge_f[e], [qr](int i) { return qr[i]; });
       }
+      S.Fq[(size_t)k * M.ne + e] = F * qe;
     }
     if (diag) {
-      const double a = (double)ia;
-      en.hi = __dmul_rn(__dmul_rn(a, a), M.areaEdge[e]);
+      if constexpr (kF64<T>)
+        en = en + ia * ia * M.areaEdge[e];
+      else
+        en += (double)(ia * ia * M.areaEdge_f[e]);
     }
   }
   if (diag) {
-    DD v[1] = {en};
+    const double v[1] = {en};
     const int r[1] = {R_EN_E};
-    block_reduce_store<1>(v, P, r);
+    block_store<double, 1>(v, P, r);
   }
 }
 
@@ -161,95 +239,187 @@ __global__ void __launch_bounds__(kMaxBlock) k_edge_prep(DevMesh M, ModelOpt O, 
 template <class T>
 __global__ void __launch_bounds__(kMaxBlock) k_cell(DevMesh M, ModelOpt O, StageIO<T> S, RKStage rk, Partials P,
                                                     int diag) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  DD rip{0.0, 0.0}, r44{0.0, 0.0}, mass{0.0, 0.0}, enc{0.0, 0.0};
-  if (c < M.nc) {
+  T rip = T(0), r44 = T(0);
+  double mass = 0.0, enc = 0.0;
+  TMC_FOR_EPT(c, M.nc) {
+    double t;  // gd tendency, FP64 in both modes
+    T tT, ke;
+    int eidx[kME];
     const int n = M.nEdgesOnCell[c];
-    T s = T(0), k = T(0);
-    for (int i = 0; i < n; ++i) {
-      const int e = M.edgesOnCell[(size_t)i * M.nc + c];
-      const T uu = S.u[e], ge = S.gd_e[e];
-      const T F = uu * ge;
-      s = s + T(M.nSign[(size_t)i * M.nc + c]) * F * T(M.dvEdge[e]);
-      k = k + uu * uu * T(M.areaEdge[e]);
-    }
-    const double Ad = M.areaCell[c];
-    const T A = T(Ad);
-    const T tend = (-s) / A;
-    const T ke = (k * T(0.25)) / A;
-    const double gd = S.gd_in[c];
-    S.E[c] = ke + T(gd) + T(S.ghs[c]);
-    const double t = (double)tend;
-    double* tb = S.gd_tend;
-    switch (rk.mode) {
-      case 0:
-        tb[c] = t;
-        break;
-      case 1:
-        S.gd_acc[c] = t;
-        tb[c] = t;
-        S.gd_next[c] = S.gd_old[c] + rk.a_dt * t;
-        break;
-      case 2:
-      case 3: {
-        const double tp = tb[c];
-        rip.hi = __dmul_rn(__dmul_rn(tp, t), Ad);
-        S.gd_acc[c] = S.gd_acc[c] + 2.0 * t;
-        tb[c] = t;
-        S.gd_next[c] = S.gd_old[c] + rk.a_dt * t;
-        break;
+    if constexpr (kF64<T>) {
+      // operators_mod.F90:40-55 (div_operator of u*gd_edge) and :206-221, in order
+      double s = 0.0, k = 0.0;
+      for (int i = 0; i < n; ++i) {
+        const int e = M.edgesOnCell[(size_t)i * M.nc + c];
+        const double uu = S.u[e];
+        s = s + (double)M.nSign[(size_t)i * M.nc + c] * S.F[e] * M.dvEdge[e];
+        k = k + uu * uu * M.areaEdge[e];
       }
-      case 4: {
-        const double tp = tb[c];
-        rip.hi = __dmul_rn(__dmul_rn(tp, t), Ad);
-        const double tn = (S.gd_acc[c] + t) / 6.0;
-        S.gd_acc[c] = tn;
-        r44.hi = __dmul_rn(__dmul_rn(tn, tn), Ad);
-        tb[c] = t;
-        break;
+      const double A = M.areaCell[c];
+      t = (-s) / A;
+      tT = t;
+      ke = (k * 0.25) / A;
+      S.E[c] = ke + S.gd_in[c] + S.ghs[c];
+      (void)eidx;
+    } else {
+      float nsg[kME], uu[kME], Fv[kME], dv[kME], ae[kME];
+#pragma unroll
+      for (int i = 0; i < kME; ++i) {
+        eidx[i] = M.edgesOnCell[(size_t)i * M.nc + c];  // padded slots: index 0, sign 0
+        nsg[i] = (float)M.nSign[(size_t)i * M.nc + c];
+      }
+#pragma unroll
+      for (int i = 0; i < kME; ++i) {
+        uu[i] = S.u[eidx[i]];
+        Fv[i] = S.F[eidx[i]];
+        dv[i] = M.dvEdge_f[eidx[i]];
+        ae[i] = M.areaEdge_f[eidx[i]];
+      }
+      float hi = 0.f, lo = 0.f, k = 0.f;
+#pragma unroll
+      for (int i = 0; i < kME; ++i) {
+        // the FP32 flux of an edge is bit-identical in its two cells; the two-sum
+        // keeps their sum exact enough for mass conservation to FP64 round-off
+        two_sum_acc(hi, lo, __fmul_rn(__fmul_rn(nsg[i], Fv[i]), dv[i]));
+        k += fabsf(nsg[i]) * uu[i] * uu[i] * ae[i];
+      }
+      t = -((double)hi + (double)lo) * M.invAreaCell[c];
+      tT = (float)t;
+      ke = k * 0.25f * M.invAreaCell_f[c];
+      S.E[c] = ke + S.gdf_in[c] + S.ghsf[c];
+    }
+    (void)n;
+    const double Ad = M.areaCell[c];
+    double gnext = 0.0;
+    if constexpr (kF64<T>) {
+      double* tb = S.gd_tend;
+      switch (rk.mode) {
+        case 0:
+          tb[c] = t;
+          break;
+        case 1:
+          S.gd_acc[c] = t;
+          tb[c] = t;
+          gnext = S.gd_old[c] + rk.a_dt * t;
+          S.gd_next[c] = gnext;
+          break;
+        case 2:
+        case 3: {
+          const double tp = tb[c];
+          rip = rip + tp * t * Ad;
+          S.gd_acc[c] = S.gd_acc[c] + 2.0 * t;
+          tb[c] = t;
+          gnext = S.gd_old[c] + rk.a_dt * t;
+          S.gd_next[c] = gnext;
+          break;
+        }
+        case 4: {
+          const double tp = tb[c];
+          rip = rip + tp * t * Ad;
+          const double tn = (S.gd_acc[c] + t) / 6.0;
+          S.gd_acc[c] = tn;
+          r44 = r44 + tn * tn * Ad;
+          tb[c] = t;
+          break;
+        }
+      }
+    } else {
+      float* tb = S.tendf;
+      const float Af = (float)Ad;
+      switch (rk.mode) {
+        case 0:
+          S.gd_tend[c] = t;
+          tb[c] = tT;
+          break;
+        case 1:
+          S.gd_acc[c] = t;
+          tb[c] = tT;
+          gnext = S.gd_old[c] + rk.a_dt * t;
+          S.gd_next[c] = gnext;
+          S.gdf_next[c] = (float)gnext;
+          break;
+        case 2:
+        case 3: {
+          const float tp = tb[c];
+          rip += tp * tT * Af;
+          S.gd_acc[c] = S.gd_acc[c] + 2.0 * t;
+          tb[c] = tT;
+          gnext = S.gd_old[c] + rk.a_dt * t;
+          S.gd_next[c] = gnext;
+          S.gdf_next[c] = (float)gnext;
+          break;
+        }
+        case 4: {
+          const float tp = tb[c];
+          rip += tp * tT * Af;
+          const double tn = (S.gd_acc[c] + t) * (1.0 / 6.0);
+          S.gd_acc[c] = tn;
+          const float tnf = (float)tn;
+          r44 += tnf * tnf * Af;
+          tb[c] = tT;
+          break;
+        }
       }
     }
     for (int q = 0; q < O.n_tracers; ++q) {
-      T sq = T(0);
-      for (int i = 0; i < n; ++i) {
-        const int e = M.edgesOnCell[(size_t)i * M.nc + c];
-        sq = sq + T(M.nSign[(size_t)i * M.nc + c]) * S.Fq[(size_t)q * M.ne + e] * T(M.dvEdge[e]);
+      T tq;
+      if constexpr (kF64<T>) {
+        double sq = 0.0;
+        for (int i = 0; i < n; ++i) {
+          const int e = M.edgesOnCell[(size_t)i * M.nc + c];
+          sq = sq + (double)M.nSign[(size_t)i * M.nc + c] * S.Fq[(size_t)q * M.ne + e] * M.dvEdge[e];
+        }
+        tq = (-sq) / M.areaCell[c];
+      } else {
+        float sq = 0.f;
+#pragma unroll
+        for (int i = 0; i < kME; ++i)
+          sq += (float)M.nSign[(size_t)i * M.nc + c] * S.Fq[(size_t)q * M.ne + eidx[i]] * M.dvEdge_f[eidx[i]];
+        tq = -sq * M.invAreaCell_f[c];
       }
-      const double tq = (double)((-sq) / A);
       const size_t qi = (size_t)q * M.nc + c;
+      T qnext = T(0);
+      const T adt = T(rk.a_dt);
       switch (rk.mode) {
         case 1:
           S.q_acc[qi] = tq;
-          S.q_next[qi] = S.q_old[qi] + rk.a_dt * tq;
+          qnext = S.q_old[qi] + adt * tq;
+          S.q_next[qi] = qnext;
           break;
         case 2:
         case 3:
-          S.q_acc[qi] = S.q_acc[qi] + 2.0 * tq;
-          S.q_next[qi] = S.q_old[qi] + rk.a_dt * tq;
+          S.q_acc[qi] = S.q_acc[qi] + T(2) * tq;
+          qnext = S.q_old[qi] + adt * tq;
+          S.q_next[qi] = qnext;
           break;
         case 4:
-          S.q_acc[qi] = (S.q_acc[qi] + tq) / 6.0;
+          if constexpr (kF64<T>)
+            S.q_acc[qi] = (S.q_acc[qi] + tq) / 6.0;
+          else
+            S.q_acc[qi] = (S.q_acc[qi] + tq) * (1.0f / 6.0f);
           break;
         default:
           S.q_acc[qi] = tq;
       }
+      if constexpr (!kF64<T>) {
+        if (rk.mode >= 1 && rk.mode <= 3) S.qr_next[qi] = qnext / (float)gnext;
+      }
     }
     if (diag) {
-      mass.hi = __dmul_rn(gd, Ad);
-      const double gh = S.ghs[c];
-      enc.hi = __dmul_rn(__dadd_rn(__dmul_rn(gd, gd), __dmul_rn(__dmul_rn(2.0, gd), gh)), Ad);
+      const double gd = S.gd_in[c], gh = S.ghs[c];
+      mass = mass + gd * Ad;
+      enc = enc + (gd * gd + 2.0 * gd * gh) * Ad;
     }
   }
   if (rk.mode >= 2) {
-    DD v[2] = {rip, r44};
+    const T v[2] = {rip, r44};
     const int r[2] = {R_IP_C + 2 * (rk.mode - 2), R_44_C};
-    block_reduce_store<2>(v, P, r);
+    block_store<T, 2>(v, P, r);
   }
   if (diag) {
-    __syncthreads();
-    DD v[2] = {mass, enc};
+    const double v[2] = {mass, enc};
     const int r[2] = {R_MASS, R_EN_C};
-    block_reduce_store<2>(v, P, r);
+    block_store<double, 2>(v, P, r);
   }
 }
 
@@ -258,51 +428,80 @@ __global__ void __launch_bounds__(kMaxBlock) k_cell(DevMesh M, ModelOpt O, Stage
 // ---------------------------------------------------------------------------
 template <class T>
 __global__ void __launch_bounds__(kMaxBlock) k_vertex(DevMesh M, ModelOpt O, StageIO<T> S, Partials P, int diag) {
-  const int v = blockIdx.x * blockDim.x + threadIdx.x;
-  DD pe{0.0, 0.0}, av{0.0, 0.0};
-  if (v < M.nv) {
-    T gv = T(0), s = T(0);
+  double pe = 0.0, av = 0.0;
+  TMC_FOR_EPT(v, M.nv) {
+    T gv, vo, pv;
+    if constexpr (kF64<T>) {
+      // operators_mod.F90:106-123 (c2v), :76-91 (curl), :262-270 (pv)
+      double s = 0.0;
+      gv = 0.0;
 #pragma unroll
-    for (int i = 0; i < 3; ++i) {
-      const int c = M.cellsOnVertex[(size_t)i * M.nv + v];
-      gv = gv + T(S.gd_in[c]) * T(M.kite[(size_t)i * M.nv + v]);
-    }
-    const double Atd = M.areaTriangle[v];
-    const T At = T(Atd);
-    gv = gv / At;
+      for (int i = 0; i < 3; ++i)
+        gv = gv + S.gd_in[M.cellsOnVertex[(size_t)i * M.nv + v]] * M.kite[(size_t)i * M.nv + v];
+      const double At = M.areaTriangle[v];
+      gv = gv / At;
 #pragma unroll
-    for (int i = 0; i < 3; ++i) {
-      const int e = M.edgesOnVertex[(size_t)i * M.nv + v];
-      s = s + T(M.tSign[(size_t)i * M.nv + v]) * S.u[e] * T(M.dcEdge[e]);
+      for (int i = 0; i < 3; ++i) {
+        const int e = M.edgesOnVertex[(size_t)i * M.nv + v];
+        s = s + (double)M.tSign[(size_t)i * M.nv + v] * S.u[e] * M.dcEdge[e];
+      }
+      vo = (-s) / At;
+      pv = (M.fVertex[v] + vo) / gv;
+    } else {
+      int ci[3], ei[3];
+      float kt[3], ts[3];
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        ci[i] = M.cellsOnVertex[(size_t)i * M.nv + v];
+        ei[i] = M.edgesOnVertex[(size_t)i * M.nv + v];
+        kt[i] = M.kite_f[(size_t)i * M.nv + v];
+        ts[i] = (float)M.tSign[(size_t)i * M.nv + v];
+      }
+      float g[3], uu[3], dc[3];
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        g[i] = S.gdf_in[ci[i]];
+        uu[i] = S.u[ei[i]];
+        dc[i] = M.dcEdge_f[ei[i]];
+      }
+      const float iA = M.invAreaTriangle_f[v];
+      gv = (g[0] * kt[0] + g[1] * kt[1] + g[2] * kt[2]) * iA;
+      const float s = ts[0] * uu[0] * dc[0] + ts[1] * uu[1] * dc[1] + ts[2] * uu[2] * dc[2];
+      vo = -s * iA;
+      pv = (M.fVertex_f[v] + vo) / gv;
     }
-    const T vo = (-s) / At;
-    const T pv = (T(M.fVertex[v]) + vo) / gv;
     S.pv_v[v] = pv;
     if (S.vor) S.vor[v] = vo;
     if (S.gd_v) S.gd_v[v] = gv;
     if (diag) {
-      const double p = (double)pv;
-      pe.hi = __dmul_rn(__dmul_rn((double)gv, __dmul_rn(p, p)), Atd);
-      av.hi = __dmul_rn(__dadd_rn((double)vo, M.fVertex[v]), Atd);
+      if constexpr (kF64<T>) {
+        const double At = M.areaTriangle[v];
+        pe = pe + gv * (pv * pv) * At;
+        av = av + (vo + M.fVertex[v]) * At;
+      } else {
+        const double At = M.areaTriangle[v];
+        pe += (double)(gv * (pv * pv)) * At;
+        av += ((double)vo + M.fVertex[v]) * At;
+      }
     }
   }
   (void)O;
   if (diag) {
-    DD vv[2] = {pe, av};
+    const double vv[2] = {pe, av};
     const int r[2] = {R_PE, R_AV};
-    block_reduce_store<2>(vv, P, r);
+    block_store<double, 2>(vv, P, r);
   }
 }
 
 // pv on cells: scalar_v2c_interp_operator as a gather (operators_mod.F90:125-141)
 template <class T>
 __global__ void __launch_bounds__(kMaxBlock) k_v2c(DevMesh M, const T* pv_v, T* pv_c) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= M.nc) return;
-  const T A = T(M.areaCell[c]);
-  T s = T(0);
-  for (int k = M.v2c_start[c]; k < M.v2c_start[c + 1]; ++k) s = s + pv_v[M.v2c_vertex[k]] * T(M.v2c_kite[k]) / A;
-  pv_c[c] = s;
+  TMC_FOR_EPT(c, M.nc) {
+    const T A = T(M.areaCell[c]);
+    T s = T(0);
+    for (int k = M.v2c_start[c]; k < M.v2c_start[c + 1]; ++k) s = s + pv_v[M.v2c_vertex[k]] * T(M.v2c_kite[k]) / A;
+    pv_c[c] = s;
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -310,32 +509,34 @@ __global__ void __launch_bounds__(kMaxBlock) k_v2c(DevMesh M, const T* pv_v, T* 
 // ---------------------------------------------------------------------------
 template <class T>
 __global__ void __launch_bounds__(kMaxBlock) k_edge_pv(DevMesh M, ModelOpt O, StageIO<T> S) {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= M.ne) return;
-  const int v1 = M.verticesOnEdge[e], v2 = M.verticesOnEdge[M.ne + e];
-  const T p1 = S.pv_v[v1], p2 = S.pv_v[v2];
-  T pe = T(0.5) * (p1 + p2);
   const bool need_v = (O.pv_scheme == 3) || (O.pv_scheme == 1 && O.apvm_weight != 0.0);
-  T ve = T(0);
-  if (need_v) {
-    const int n = M.nEdgesOnEdge[e];
-    for (int i = 0; i < n; ++i)
-      ve = ve + S.u[M.edgesOnEdge[(size_t)i * M.ne + e]] * T(M.weightsOnEdge[(size_t)i * M.ne + e]);
-    if (S.v_e) S.v_e[e] = ve;
-  }
-  if (O.pv_scheme == 1) {
-    if (O.apvm_weight != 0.0) {
-      const int c1 = M.cellsOnEdge[e], c2 = M.cellsOnEdge[M.ne + e];
-      const T a = ve * (p2 - p1) / T(M.dvEdge[e]);
-      const T b = S.u[e] * (S.pv_c[c2] - S.pv_c[c1]) / T(M.dcEdge[e]);
-      pe = pe - T(O.apvm_weight * O.dt) * (a + b);
+  TMC_FOR_EPT(e, M.ne) {
+    const int v1 = M.verticesOnEdge[e], v2 = M.verticesOnEdge[M.ne + e];
+    const T p1 = S.pv_v[v1], p2 = S.pv_v[v2];
+    T pe = T(0.5) * (p1 + p2);
+    T ve = T(0);
+    if (need_v) {
+      const int n = M.nEdgesOnEdge[e];
+      for (int i = 0; i < n; ++i) {
+        const size_t k = (size_t)i * M.ne + e;
+        ve = ve + S.u[M.edgesOnEdge[k]] * met<T>(M.weightsOnEdge, M.weightsOnEdge_f, k);
+      }
+      if (S.v_e) S.v_e[e] = ve;
     }
-  } else if (O.pv_scheme == 3) {
-    const T* pv = S.pv_v;
-    pe = upwind_edge<T>(M.vert2, M.vert4, O.interp_pv_order, T(O.vert_coef2), T(O.vert_coef4), M.ne, e, v1, v2, pe,
-                        ve, T(M.dvEdge[e]), [pv](int i) { return pv[i]; });
+    if (O.pv_scheme == 1) {
+      if (O.apvm_weight != 0.0) {
+        const int c1 = M.cellsOnEdge[e], c2 = M.cellsOnEdge[M.ne + e];
+        const T a = ve * (p2 - p1) / met<T>(M.dvEdge, M.dvEdge_f, e);
+        const T b = S.u[e] * (S.pv_c[c2] - S.pv_c[c1]) / met<T>(M.dcEdge, M.dcEdge_f, e);
+        pe = pe - T(O.apvm_weight * O.dt) * (a + b);
+      }
+    } else if (O.pv_scheme == 3) {
+      const T* pv = S.pv_v;
+      pe = upwind_edge<T>(M.vert2, M.vert4, O.interp_pv_order, T(O.vert_coef2), T(O.vert_coef4), M.ne, e, v1, v2,
+                          pe, ve, met<T>(M.dvEdge, M.dvEdge_f, e), [pv](int i) { return pv[i]; });
+    }
+    S.pv_e[e] = pe;
   }
-  S.pv_e[e] = pe;
 }
 
 // ---------------------------------------------------------------------------
@@ -343,31 +544,60 @@ __global__ void __launch_bounds__(kMaxBlock) k_edge_pv(DevMesh M, ModelOpt O, St
 // ---------------------------------------------------------------------------
 template <class T>
 __global__ void __launch_bounds__(kMaxBlock) k_edge_flux(DevMesh M, ModelOpt O, StageIO<T> S, RKStage rk, Partials P) {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  DD rip{0.0, 0.0}, r44{0.0, 0.0};
-  if (e < M.ne) {
-    const T pe = S.pv_e[e];
-    T s = T(0);
-    const int n = M.nEdgesOnEdge[e];
-    for (int i = 0; i < n; ++i) {
-      const size_t k = (size_t)i * M.ne + e;
-      const int ep = M.edgesOnEdge[k];
-      s = s + T(M.weightsOnEdge[k]) * S.u[ep] * S.gd_e[ep] * T(0.5) * (pe + S.pv_e[ep]);
-    }
+  T rip = T(0), r44 = T(0);  // FP32 path: FP32 products and per-thread sums, FP64 across warps
+  TMC_FOR_EPT(e, M.ne) {
     const int c1 = M.cellsOnEdge[e], c2 = M.cellsOnEdge[M.ne + e];
-    const T dc = T(M.dcEdge[e]);
-    const T dEdx = (S.E[c2] - S.E[c1]) / dc;
-    const T ut = s - dEdx;
-    T tge = T(0.5) * (T(S.gd_tend[c1]) + T(S.gd_tend[c2]));
-    const T ia = S.iap_in[e];
-    if (O.adv_order >= 3) {
-      const double* gt = S.gd_tend;
-      tge = upwind_edge<T>(M.cell2, M.cell4, O.adv_order, T(O.cell_coef2), T(O.cell_coef4), M.ne, e, c1, c2, tge, ia,
-                           dc, [gt](int i) { return T(gt[i]); });
+    const T pe = S.pv_e[e];
+    T s = T(0), tge, dEdx, dc;
+    if constexpr (kF64<T>) {
+      // calc_tangent_vor_flux (operators_mod.F90:239-260), in order
+      const int n = M.nEdgesOnEdge[e];
+      for (int i = 0; i < n; ++i) {
+        const size_t k = (size_t)i * M.ne + e;
+        const int ep = M.edgesOnEdge[k];
+        s = s + M.weightsOnEdge[k] * S.u[ep] * S.gd_e[ep] * 0.5 * (pe + S.pv_e[ep]);
+      }
+      dc = M.dcEdge[e];
+      dEdx = (S.E[c2] - S.E[c1]) / dc;
+      tge = 0.5 * (S.gd_tend[c1] + S.gd_tend[c2]);
+    } else {
+      int ep[kME2];
+      float w[kME2];
+#pragma unroll
+      for (int i = 0; i < kME2; ++i) {
+        const size_t k = (size_t)i * M.ne + e;
+        ep[i] = M.edgesOnEdge[k];  // padded entries: own edge with weight 0
+        w[i] = M.weightsOnEdge_f[k];
+      }
+      const float E1 = S.E[c1], E2 = S.E[c2], t1 = S.tendf[c1], t2 = S.tendf[c2];
+      dc = M.dcEdge_f[e];
+      float Fv[kME2], pp[kME2];
+#pragma unroll
+      for (int i = 0; i < kME2; ++i) {
+        Fv[i] = S.F[ep[i]];
+        pp[i] = S.pv_e[ep[i]];
+      }
+#pragma unroll
+      for (int i = 0; i < kME2; ++i) s += w[i] * Fv[i] * (0.5f * (pe + pp[i]));
+      dEdx = (E2 - E1) / dc;
+      tge = 0.5f * (t1 + t2);
     }
+    const T ut = s - dEdx;
+    const T uu = S.u[e];
+    if (O.adv_order >= 3) {
+      if constexpr (kF64<T>) {
+        const double* gt = S.gd_tend;
+        tge = upwind_edge<T>(M.cell2, M.cell4, O.adv_order, T(O.cell_coef2), T(O.cell_coef4), M.ne, e, c1, c2, tge,
+                             S.iap_in[e], dc, [gt](int i) { return gt[i]; });
+      } else {
+        const float* gt = S.tendf;
+        tge = upwind_edge<T>(M.cell2, M.cell4, O.adv_order, T(O.cell_coef2), T(O.cell_coef4), M.ne, e, c1, c2, tge,
+                             S.iap_in[e], dc, [gt](int i) { return gt[i]; });
+      }
+    }
+    // calc_u_tend_on_edge (tmcore_swm_mod.F90:155-201)
     const T sq = sqrt(S.gd_e[e]);
-    const T it = sq * ut + T(0.5) * S.u[e] / sq * tge;
-    const double ae = M.areaEdge[e];
+    const T it = sq * ut + T(0.5) * uu / sq * tge;
     T* tb = S.iap_tend;
     switch (rk.mode) {
       case 0:
@@ -381,7 +611,7 @@ __global__ void __launch_bounds__(kMaxBlock) k_edge_flux(DevMesh M, ModelOpt O, 
       case 2:
       case 3: {
         const T tp = tb[e];
-        rip.hi = __dmul_rn(__dmul_rn((double)tp, (double)it), ae);
+        rip = rip + tp * it * met<T>(M.areaEdge, M.areaEdge_f, e);
         S.iap_acc[e] = S.iap_acc[e] + T(2) * it;
         tb[e] = it;
         S.iap_next[e] = S.iap_old[e] + T(rk.a_dt) * it;
@@ -389,37 +619,49 @@ __global__ void __launch_bounds__(kMaxBlock) k_edge_flux(DevMesh M, ModelOpt O, 
       }
       case 4: {
         const T tp = tb[e];
-        rip.hi = __dmul_rn(__dmul_rn((double)tp, (double)it), ae);
-        const T tn = (S.iap_acc[e] + it) / T(6);
+        const T ae = met<T>(M.areaEdge, M.areaEdge_f, e);
+        rip = rip + tp * it * ae;
+        T tn;
+        if constexpr (kF64<T>)
+          tn = (S.iap_acc[e] + it) / 6.0;
+        else
+          tn = (S.iap_acc[e] + it) * (1.0f / 6.0f);
         S.iap_acc[e] = tn;
-        r44.hi = __dmul_rn(__dmul_rn((double)tn, (double)tn), ae);
+        r44 = r44 + tn * tn * ae;
         tb[e] = it;
         break;
       }
     }
   }
   if (rk.mode >= 2) {
-    DD v[2] = {rip, r44};
+    const T v[2] = {rip, r44};
     const int r[2] = {R_IP_E + 2 * (rk.mode - 2), R_44_E};
-    block_reduce_store<2>(v, P, r);
+    block_store<T, 2>(v, P, r);
   }
 }
 
 // new = old + (beta dt) t_new (update_state, tmcore_swm_mod.F90:203-213)
 template <class T>
 __global__ void __launch_bounds__(kMaxBlock) k_final_update(DevMesh M, ModelOpt O, StageIO<T> S, const double* diag) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const double bdt = diag[9];
-  if (i < M.ne) {
-    T* iap = const_cast<T*>(S.iap_old);
-    iap[i] = iap[i] + T(bdt) * S.iap_acc[i];
-  }
-  if (i < M.nc) {
-    double* gd = const_cast<double*>(S.gd_old);
-    gd[i] = gd[i] + bdt * S.gd_acc[i];
-    for (int q = 0; q < O.n_tracers; ++q) {
-      double* qq = const_cast<double*>(S.q_old) + (size_t)q * M.nc;
-      qq[i] = qq[i] + bdt * S.q_acc[(size_t)q * M.nc + i];
+  const int n = M.ne > M.nc ? M.ne : M.nc;
+  TMC_FOR_EPT(i, n) {
+    if (i < M.ne) {
+      T* iap = const_cast<T*>(S.iap_old);
+      iap[i] = iap[i] + T(bdt) * S.iap_acc[i];
+    }
+    if (i < M.nc) {
+      double* gd = const_cast<double*>(S.gd_old);
+      const double g = gd[i] + bdt * S.gd_acc[i];
+      gd[i] = g;
+      if constexpr (!kF64<T>) const_cast<float*>(S.gdf_in)[i] = (float)g;
+      for (int q = 0; q < O.n_tracers; ++q) {
+        const size_t qi = (size_t)q * M.nc + i;
+        T* qq = const_cast<T*>(S.q_old);
+        const T qn = qq[qi] + T(bdt) * S.q_acc[qi];
+        qq[qi] = qn;
+        if constexpr (!kF64<T>) const_cast<float*>(S.qr_in)[qi] = qn / (float)g;
+      }
     }
   }
 }
@@ -448,34 +690,33 @@ inline int nblk(int n, int bs) { return (n + bs - 1) / bs; }
 template <class T>
 void launch_edge_prep(const DevMesh& M, const ModelOpt& O, const StageIO<T>& S, Partials P, bool diag, int bs,
                       cudaStream_t st) {
-  k_edge_prep<T><<<nblk(M.ne, bs), bs, 0, st>>>(M, O, S, P, diag ? 1 : 0);
+  k_edge_prep<T><<<grid_for(M.ne, bs), bs, 0, st>>>(M, O, S, P, diag ? 1 : 0);
 }
 template <class T>
 void launch_cell(const DevMesh& M, const ModelOpt& O, const StageIO<T>& S, RKStage rk, Partials P, bool diag, int bs,
                  cudaStream_t st) {
-  k_cell<T><<<nblk(M.nc, bs), bs, 0, st>>>(M, O, S, rk, P, diag ? 1 : 0);
+  k_cell<T><<<grid_for(M.nc, bs), bs, 0, st>>>(M, O, S, rk, P, diag ? 1 : 0);
 }
 template <class T>
 void launch_vertex(const DevMesh& M, const ModelOpt& O, const StageIO<T>& S, Partials P, bool diag, int bs,
                    cudaStream_t st) {
-  k_vertex<T><<<nblk(M.nv, bs), bs, 0, st>>>(M, O, S, P, diag ? 1 : 0);
+  k_vertex<T><<<grid_for(M.nv, bs), bs, 0, st>>>(M, O, S, P, diag ? 1 : 0);
 }
 template <class T>
 void launch_edge_pv(const DevMesh& M, const ModelOpt& O, const StageIO<T>& S, int bs, cudaStream_t st) {
-  if (O.pv_scheme == 1 && O.apvm_weight != 0.0) k_v2c<T><<<nblk(M.nc, bs), bs, 0, st>>>(M, S.pv_v, S.pv_c);
-  k_edge_pv<T><<<nblk(M.ne, bs), bs, 0, st>>>(M, O, S);
+  if (O.pv_scheme == 1 && O.apvm_weight != 0.0) k_v2c<T><<<grid_for(M.nc, bs), bs, 0, st>>>(M, S.pv_v, S.pv_c);
+  k_edge_pv<T><<<grid_for(M.ne, bs), bs, 0, st>>>(M, O, S);
 }
 template <class T>
 void launch_edge_flux(const DevMesh& M, const ModelOpt& O, const StageIO<T>& S, RKStage rk, Partials P, int bs,
                       cudaStream_t st) {
-  k_edge_flux<T><<<nblk(M.ne, bs), bs, 0, st>>>(M, O, S, rk, P);
+  k_edge_flux<T><<<grid_for(M.ne, bs), bs, 0, st>>>(M, O, S, rk, P);
 }
 template <class T>
 void launch_final_update(const DevMesh& M, const ModelOpt& O, const StageIO<T>& S, const double* diag, int bs,
                          cudaStream_t st) {
-  k_final_update<T><<<nblk(M.ne > M.nc ? M.ne : M.nc, bs), bs, 0, st>>>(M, O, S, diag);
+  k_final_update<T><<<grid_for(M.ne > M.nc ? M.ne : M.nc, bs), bs, 0, st>>>(M, O, S, diag);
 }
-
 template <class T>
 void launch_gather(int n, const double* src, const int32_t* n2o, T* dst, cudaStream_t st) {
   k_gather<T><<<nblk(n, 256), 256, 0, st>>>(n, src, n2o, dst);

@@ -506,8 +506,9 @@ bool prepare_mesh(const tmc_mesh_desc& d, const tmc_params& p, const PrepOptions
   hm.nc = nc;
   hm.ne = ne;
   hm.nv = nv;
-  hm.me = me;
-  hm.me2 = me2;
+  const int meD = std::max(me, opt.min_me), me2D = std::max(me2, opt.min_me2);  // device slot counts
+  hm.me = meD;
+  hm.me2 = me2D;
   hm.vd = vd;
   const double radius = p.radius, omega = p.omega;
   hm.radius = radius;
@@ -584,15 +585,15 @@ bool prepare_mesh(const tmc_mesh_desc& d, const tmc_params& p, const PrepOptions
 
   // ---- device layout (slot-major SoA) ----
   hm.nEdgesOnCell.assign(nc, 0);
-  hm.edgesOnCell.assign((size_t)me * nc, 0);
-  hm.nSignEdge.assign((size_t)me * nc, 0);
+  hm.edgesOnCell.assign((size_t)meD * nc, 0);
+  hm.nSignEdge.assign((size_t)meD * nc, 0);
   hm.areaCell.assign(nc, 0.0);
   for (int cn = 0; cn < nc; ++cn) {
     int co = hm.cell_n2o[cn];
     int n = d.nEdgesOnCell[co];
     hm.nEdgesOnCell[cn] = (uint8_t)n;
     hm.areaCell[cn] = aC[co];
-    for (int i = 0; i < me; ++i) {
+    for (int i = 0; i < meD; ++i) {
       int e = (i < n) ? d.edgesOnCell[(size_t)co * me + i] - 1 : -1;
       hm.edgesOnCell[(size_t)i * nc + cn] = (e >= 0) ? eo2n[e] : 0;
       hm.nSignEdge[(size_t)i * nc + cn] = (i < n) ? nsign[(size_t)co * me + i] : 0;
@@ -601,8 +602,8 @@ bool prepare_mesh(const tmc_mesh_desc& d, const tmc_params& p, const PrepOptions
   hm.cellsOnEdge.assign((size_t)2 * ne, 0);
   hm.verticesOnEdge.assign((size_t)2 * ne, 0);
   hm.nEdgesOnEdge.assign(ne, 0);
-  hm.edgesOnEdge.assign((size_t)me2 * ne, 0);
-  hm.weightsOnEdge.assign((size_t)me2 * ne, 0.0);
+  hm.edgesOnEdge.assign((size_t)me2D * ne, 0);
+  hm.weightsOnEdge.assign((size_t)me2D * ne, 0.0);
   hm.dcEdge.assign(ne, 0.0);
   hm.dvEdge.assign(ne, 0.0);
   hm.areaEdge.assign(ne, 0.0);
@@ -614,7 +615,7 @@ bool prepare_mesh(const tmc_mesh_desc& d, const tmc_params& p, const PrepOptions
     }
     int n = d.nEdgesOnEdge[eo];
     hm.nEdgesOnEdge[en] = (uint8_t)n;
-    for (int i = 0; i < me2; ++i) {
+    for (int i = 0; i < me2D; ++i) {
       if (i < n) {
         hm.edgesOnEdge[(size_t)i * ne + en] = eo2n[d.edgesOnEdge[(size_t)eo * me2 + i] - 1];
         hm.weightsOnEdge[(size_t)i * ne + en] = d.weightsOnEdge[(size_t)eo * me2 + i];

@@ -61,6 +61,8 @@ struct HostMesh {
 struct PrepOptions {
   bool renumber = true;
   bool cell_fit = false;    // deriv2/3/4OnCell tables
+  int min_me = 0;           // pad the per-cell slot arrays to at least this many slots
+  int min_me2 = 0;          // pad the per-edge edgesOnEdge/weightsOnEdge slots
   bool vertex_fit = false;  // deriv2/4OnVertex tables
 };
 
