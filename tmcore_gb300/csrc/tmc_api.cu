@@ -483,6 +483,7 @@ int tmc_create(const tmc_mesh_desc* mesh, const tmc_params* params, tmc_handle**
     M.invAreaTriangle_f = h->upload(inv32(hm.areaTriangle));
     M.fVertex_f = h->upload(f32(hm.fVertex));
     M.invAreaCell_f = h->upload(inv32(hm.areaCell));
+    M.areaCell_f = h->upload(f32(hm.areaCell));
     M.invAreaCell = h->upload(invA);
   }
   M.cell2 = upload_stencil(h.get(), hm.cell2);

@@ -76,6 +76,7 @@ struct DevMesh {
   const float* invAreaTriangle_f;
   const float* fVertex_f;
   const float* invAreaCell_f;
+  const float* areaCell_f;
   const double* invAreaCell;
 };
 

@@ -24,18 +24,23 @@ __global__ void __launch_bounds__(256) k_finalize(Partials P, FinalizeArgs a, do
   const int r = blockIdx.x;
   const bool want = (r <= R_44_E) ? a.step : a.diag;
   if (want) {
-    DD acc{0.0, 0.0};
+    // per-thread FP64 sums over a strided subset of the block partials, then
+    // double-double across lanes and warps
+    double hi = 0.0, lo = 0.0;
     const double* reg = P.region(r);
-    for (int i = threadIdx.x; i < a.counts[r]; i += blockDim.x) acc = dd_add(acc, DD{reg[2 * i], reg[2 * i + 1]});
+    for (int i = threadIdx.x; i < a.counts[r]; i += blockDim.x) {
+      hi = __dadd_rn(hi, reg[2 * i]);
+      lo = __dadd_rn(lo, reg[2 * i + 1]);
+    }
     __shared__ DD sm[8];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
-    DD w = warp_reduce_dd(acc);
+    DD w = warp_reduce_dd(DD{hi, lo});
     if (lane == 0) sm[warp] = w;
     __syncthreads();
     if (warp == 0) {
       w = (lane < nw) ? sm[lane] : DD{0.0, 0.0};
       w = warp_reduce_dd(w);
-      if (lane == 0) res[r] = w.hi;
+      if (lane == 0) res[r] = w.hi + w.lo;
     }
   }
   __shared__ bool last;

@@ -50,30 +50,35 @@ __device__ __forceinline__ DD warp_reduce_dd(DD v) {
 }
 
 // Reduce N per-thread partial sums over the block and store region[r[k]][block]
-// as (hi, lo).  Each warp sums its lanes with a shuffle tree in A (double or
-// float); warp 0 combines the warp sums in double-double.  Every thread of the
-// block must call this (it synchronises).
+// as (sum, 0).  Warps sum their lanes with a shuffle tree in A (double or
+// float), warp 0 sums the warp sums the same way; the compensated
+// (double-double) combination happens across blocks in k_finalize.  No
+// double-double arithmetic here: warp 0 of every block sits on the same SM
+// sub-partition, and GB300 issues FP64 at 1/64 of the FP32 rate, so a
+// double-double tail per block serialises behind the whole kernel.  Every
+// thread of the block must call this (it synchronises).
 template <class A, int N>
 __device__ __forceinline__ void block_store(const A (&v)[N], const Partials& P, const int (&r)[N]) {
-  __shared__ double sm[N][kMaxBlock / 32];
+  __shared__ A sm[N][kMaxBlock / 32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
 #pragma unroll
   for (int k = 0; k < N; ++k) {
     A w = v[k];
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) w += __shfl_down_sync(0xffffffffu, w, off);
-    if (lane == 0) sm[k][warp] = (double)w;
+    if (lane == 0) sm[k][warp] = w;
   }
   __syncthreads();
   if (warp == 0) {
 #pragma unroll
     for (int k = 0; k < N; ++k) {
-      DD w = (lane < nw) ? DD{sm[k][lane], 0.0} : DD{0.0, 0.0};
-      w = warp_reduce_dd(w);
+      A w = (lane < nw) ? sm[k][lane] : A(0);
+#pragma unroll
+      for (int off = kMaxBlock / 64; off > 0; off >>= 1) w += __shfl_down_sync(0xffffffffu, w, off);
       if (lane == 0) {
         double* reg = P.region(r[k]);
-        reg[2 * blockIdx.x] = w.hi;
-        reg[2 * blockIdx.x + 1] = w.lo;
+        reg[2 * blockIdx.x] = (double)w;
+        reg[2 * blockIdx.x + 1] = 0.0;
       }
     }
   }
@@ -246,6 +251,16 @@ __global__ void __launch_bounds__(kMaxBlock) k_cell(DevMesh M, ModelOpt O, Stage
     T tT, ke;
     int eidx[kME];
     const int n = M.nEdgesOnCell[c];
+    const int mode = rk.mode;
+    // RK inputs before any store (see k_edge_flux)
+    const double gold = (mode >= 1 && mode <= 3) ? S.gd_old[c] : 0.0;
+    const double gacc = (mode >= 2) ? S.gd_acc[c] : 0.0;
+    T tprev = T(0);
+    if constexpr (kF64<T>)
+      tprev = (mode >= 2) ? S.gd_tend[c] : 0.0;
+    else
+      tprev = (mode >= 2) ? S.tendf[c] : 0.f;
+    const double gdin = diag ? S.gd_in[c] : 0.0, ghsd = diag ? S.ghs[c] : 0.0;
     if constexpr (kF64<T>) {
       // operators_mod.F90:40-55 (div_operator of u*gd_edge) and :206-221, in order
       double s = 0.0, k = 0.0;
@@ -293,30 +308,28 @@ __global__ void __launch_bounds__(kMaxBlock) k_cell(DevMesh M, ModelOpt O, Stage
     double gnext = 0.0;
     if constexpr (kF64<T>) {
       double* tb = S.gd_tend;
-      switch (rk.mode) {
+      switch (mode) {
         case 0:
           tb[c] = t;
           break;
         case 1:
           S.gd_acc[c] = t;
           tb[c] = t;
-          gnext = S.gd_old[c] + rk.a_dt * t;
+          gnext = gold + rk.a_dt * t;
           S.gd_next[c] = gnext;
           break;
         case 2:
         case 3: {
-          const double tp = tb[c];
-          rip = rip + tp * t * Ad;
-          S.gd_acc[c] = S.gd_acc[c] + 2.0 * t;
+          rip = rip + tprev * t * Ad;
+          S.gd_acc[c] = gacc + 2.0 * t;
           tb[c] = t;
-          gnext = S.gd_old[c] + rk.a_dt * t;
+          gnext = gold + rk.a_dt * t;
           S.gd_next[c] = gnext;
           break;
         }
         case 4: {
-          const double tp = tb[c];
-          rip = rip + tp * t * Ad;
-          const double tn = (S.gd_acc[c] + t) / 6.0;
+          rip = rip + tprev * t * Ad;
+          const double tn = (gacc + t) / 6.0;
           S.gd_acc[c] = tn;
           r44 = r44 + tn * tn * Ad;
           tb[c] = t;
@@ -325,8 +338,8 @@ __global__ void __launch_bounds__(kMaxBlock) k_cell(DevMesh M, ModelOpt O, Stage
       }
     } else {
       float* tb = S.tendf;
-      const float Af = (float)Ad;
-      switch (rk.mode) {
+      const float Af = M.areaCell_f[c];
+      switch (mode) {
         case 0:
           S.gd_tend[c] = t;
           tb[c] = tT;
@@ -334,25 +347,23 @@ __global__ void __launch_bounds__(kMaxBlock) k_cell(DevMesh M, ModelOpt O, Stage
         case 1:
           S.gd_acc[c] = t;
           tb[c] = tT;
-          gnext = S.gd_old[c] + rk.a_dt * t;
+          gnext = gold + rk.a_dt * t;
           S.gd_next[c] = gnext;
           S.gdf_next[c] = (float)gnext;
           break;
         case 2:
         case 3: {
-          const float tp = tb[c];
-          rip += tp * tT * Af;
-          S.gd_acc[c] = S.gd_acc[c] + 2.0 * t;
+          rip += tprev * tT * Af;
+          S.gd_acc[c] = gacc + 2.0 * t;
           tb[c] = tT;
-          gnext = S.gd_old[c] + rk.a_dt * t;
+          gnext = gold + rk.a_dt * t;
           S.gd_next[c] = gnext;
           S.gdf_next[c] = (float)gnext;
           break;
         }
         case 4: {
-          const float tp = tb[c];
-          rip += tp * tT * Af;
-          const double tn = (S.gd_acc[c] + t) * (1.0 / 6.0);
+          rip += tprev * tT * Af;
+          const double tn = (gacc + t) * (1.0 / 6.0);
           S.gd_acc[c] = tn;
           const float tnf = (float)tn;
           r44 += tnf * tnf * Af;
@@ -361,54 +372,69 @@ __global__ void __launch_bounds__(kMaxBlock) k_cell(DevMesh M, ModelOpt O, Stage
         }
       }
     }
-    for (int q = 0; q < O.n_tracers; ++q) {
-      T tq;
-      if constexpr (kF64<T>) {
-        double sq = 0.0;
-        for (int i = 0; i < n; ++i) {
-          const int e = M.edgesOnCell[(size_t)i * M.nc + c];
-          sq = sq + (double)M.nSign[(size_t)i * M.nc + c] * S.Fq[(size_t)q * M.ne + e] * M.dvEdge[e];
-        }
-        tq = (-sq) / M.areaCell[c];
-      } else {
-        float sq = 0.f;
+    // tracers, kTr at a time: loads and divergences first, then the stores
+    constexpr int kTr = 4;
+    for (int q0 = 0; q0 < O.n_tracers; q0 += kTr) {
+      T tq[kTr], qo[kTr], qa[kTr];
 #pragma unroll
-        for (int i = 0; i < kME; ++i)
-          sq += (float)M.nSign[(size_t)i * M.nc + c] * S.Fq[(size_t)q * M.ne + eidx[i]] * M.dvEdge_f[eidx[i]];
-        tq = -sq * M.invAreaCell_f[c];
+      for (int j = 0; j < kTr; ++j) {
+        const int q = q0 + j;
+        tq[j] = qo[j] = qa[j] = T(0);
+        if (q >= O.n_tracers) continue;
+        const size_t qi = (size_t)q * M.nc + c;
+        qo[j] = (mode >= 1 && mode <= 3) ? S.q_old[qi] : T(0);
+        qa[j] = (mode >= 2) ? S.q_acc[qi] : T(0);
+        if constexpr (kF64<T>) {
+          double sq = 0.0;
+          for (int i = 0; i < n; ++i) {
+            const int e = M.edgesOnCell[(size_t)i * M.nc + c];
+            sq = sq + (double)M.nSign[(size_t)i * M.nc + c] * S.Fq[(size_t)q * M.ne + e] * M.dvEdge[e];
+          }
+          tq[j] = (-sq) / M.areaCell[c];
+        } else {
+          float sq = 0.f;
+#pragma unroll
+          for (int i = 0; i < kME; ++i)
+            sq += (float)M.nSign[(size_t)i * M.nc + c] * S.Fq[(size_t)q * M.ne + eidx[i]] * M.dvEdge_f[eidx[i]];
+          tq[j] = -sq * M.invAreaCell_f[c];
+        }
       }
-      const size_t qi = (size_t)q * M.nc + c;
-      T qnext = T(0);
-      const T adt = T(rk.a_dt);
-      switch (rk.mode) {
-        case 1:
-          S.q_acc[qi] = tq;
-          qnext = S.q_old[qi] + adt * tq;
-          S.q_next[qi] = qnext;
-          break;
-        case 2:
-        case 3:
-          S.q_acc[qi] = S.q_acc[qi] + T(2) * tq;
-          qnext = S.q_old[qi] + adt * tq;
-          S.q_next[qi] = qnext;
-          break;
-        case 4:
-          if constexpr (kF64<T>)
-            S.q_acc[qi] = (S.q_acc[qi] + tq) / 6.0;
-          else
-            S.q_acc[qi] = (S.q_acc[qi] + tq) * (1.0f / 6.0f);
-          break;
-        default:
-          S.q_acc[qi] = tq;
-      }
-      if constexpr (!kF64<T>) {
-        if (rk.mode >= 1 && rk.mode <= 3) S.qr_next[qi] = qnext / (float)gnext;
+#pragma unroll
+      for (int j = 0; j < kTr; ++j) {
+        const int q = q0 + j;
+        if (q >= O.n_tracers) continue;
+        const size_t qi = (size_t)q * M.nc + c;
+        T qnext = T(0);
+        const T adt = T(rk.a_dt);
+        switch (mode) {
+          case 1:
+            S.q_acc[qi] = tq[j];
+            qnext = qo[j] + adt * tq[j];
+            S.q_next[qi] = qnext;
+            break;
+          case 2:
+          case 3:
+            S.q_acc[qi] = qa[j] + T(2) * tq[j];
+            qnext = qo[j] + adt * tq[j];
+            S.q_next[qi] = qnext;
+            break;
+          case 4:
+            if constexpr (kF64<T>)
+              S.q_acc[qi] = (qa[j] + tq[j]) / 6.0;
+            else
+              S.q_acc[qi] = (qa[j] + tq[j]) * (1.0f / 6.0f);
+            break;
+          default:
+            S.q_acc[qi] = tq[j];
+        }
+        if constexpr (!kF64<T>) {
+          if (mode >= 1 && mode <= 3) S.qr_next[qi] = qnext / (float)gnext;
+        }
       }
     }
     if (diag) {
-      const double gd = S.gd_in[c], gh = S.ghs[c];
-      mass = mass + gd * Ad;
-      enc = enc + (gd * gd + 2.0 * gd * gh) * Ad;
+      mass = mass + gdin * Ad;
+      enc = enc + (gdin * gdin + 2.0 * gdin * ghsd) * Ad;
     }
   }
   if (rk.mode >= 2) {
@@ -545,9 +571,19 @@ __global__ void __launch_bounds__(kMaxBlock) k_edge_pv(DevMesh M, ModelOpt O, St
 template <class T>
 __global__ void __launch_bounds__(kMaxBlock) k_edge_flux(DevMesh M, ModelOpt O, StageIO<T> S, RKStage rk, Partials P) {
   T rip = T(0), r44 = T(0);  // FP32 path: FP32 products and per-thread sums, FP64 across warps
+  const int mode = rk.mode;
   TMC_FOR_EPT(e, M.ne) {
+    // Loads that depend on no other load come first, before any store: a load
+    // issued after a store through a pointer the compiler must assume aliases
+    // would wait a full memory round trip.
     const int c1 = M.cellsOnEdge[e], c2 = M.cellsOnEdge[M.ne + e];
     const T pe = S.pv_e[e];
+    const T uu = S.u[e];
+    const T ge = S.gd_e[e];
+    const T tp = (mode >= 2) ? S.iap_tend[e] : T(0);
+    const T accv = (mode >= 2) ? S.iap_acc[e] : T(0);
+    const T oldv = (mode >= 1 && mode <= 3) ? S.iap_old[e] : T(0);
+    const T ae = (mode >= 2) ? met<T>(M.areaEdge, M.areaEdge_f, e) : T(0);
     T s = T(0), tge, dEdx, dc;
     if constexpr (kF64<T>) {
       // calc_tangent_vor_flux (operators_mod.F90:239-260), in order
@@ -583,7 +619,6 @@ __global__ void __launch_bounds__(kMaxBlock) k_edge_flux(DevMesh M, ModelOpt O, 
       tge = 0.5f * (t1 + t2);
     }
     const T ut = s - dEdx;
-    const T uu = S.u[e];
     if (O.adv_order >= 3) {
       if constexpr (kF64<T>) {
         const double* gt = S.gd_tend;
@@ -596,36 +631,33 @@ __global__ void __launch_bounds__(kMaxBlock) k_edge_flux(DevMesh M, ModelOpt O, 
       }
     }
     // calc_u_tend_on_edge (tmcore_swm_mod.F90:155-201)
-    const T sq = sqrt(S.gd_e[e]);
+    const T sq = sqrt(ge);
     const T it = sq * ut + T(0.5) * uu / sq * tge;
     T* tb = S.iap_tend;
-    switch (rk.mode) {
+    switch (mode) {
       case 0:
         tb[e] = it;
         break;
       case 1:
         S.iap_acc[e] = it;
         tb[e] = it;
-        S.iap_next[e] = S.iap_old[e] + T(rk.a_dt) * it;
+        S.iap_next[e] = oldv + T(rk.a_dt) * it;
         break;
       case 2:
       case 3: {
-        const T tp = tb[e];
-        rip = rip + tp * it * met<T>(M.areaEdge, M.areaEdge_f, e);
-        S.iap_acc[e] = S.iap_acc[e] + T(2) * it;
+        rip = rip + tp * it * ae;
+        S.iap_acc[e] = accv + T(2) * it;
         tb[e] = it;
-        S.iap_next[e] = S.iap_old[e] + T(rk.a_dt) * it;
+        S.iap_next[e] = oldv + T(rk.a_dt) * it;
         break;
       }
       case 4: {
-        const T tp = tb[e];
-        const T ae = met<T>(M.areaEdge, M.areaEdge_f, e);
         rip = rip + tp * it * ae;
         T tn;
         if constexpr (kF64<T>)
-          tn = (S.iap_acc[e] + it) / 6.0;
+          tn = (accv + it) / 6.0;
         else
-          tn = (S.iap_acc[e] + it) * (1.0f / 6.0f);
+          tn = (accv + it) * (1.0f / 6.0f);
         S.iap_acc[e] = tn;
         r44 = r44 + tn * tn * ae;
         tb[e] = it;
