@@ -150,6 +150,29 @@ int tmc_time_steps(tmc_handle* h, int32_t nsteps, double* ms_total, double* ms_f
 /* Number of elements after load, and bytes of device memory held. */
 int tmc_sizes(const tmc_handle* h, int64_t* nCells, int64_t* nEdges, int64_t* nVertices, int64_t* device_bytes);
 
+/* Largest nCells / nEdges tmc_mass_energy_noalloc accepts. */
+#define TMC_NOALLOC_MAX_ELEMENTS 8388608
+
+/* No counterpart in the reference.  Total mass and total energy (the sums of
+ * tmcore_swm_mod.F90:215-231, the values tmc_get_diag returns in out[0] and
+ * out[1]) of a state held in DEVICE arrays, for callers that cannot call
+ * cudaMalloc: a host that shares the GPU with a framework whose allocator
+ * owns all device memory, or one whose policy forbids device allocations
+ * while it runs.  It needs no handle and allocates nothing: its partial sums
+ * live in a fixed 384 KiB array inside the library image, which every GPU
+ * that loads the library keeps until the process exits.  Inputs: gd, ghs,
+ * areaCell (m^2) for nCells cells and iap_u, areaEdge (m^2) for nEdges edges,
+ * all device pointers, any element order.  Output: out[0] = mass,
+ * out[1] = energy, a device pointer, written asynchronously on `stream`
+ * (a cudaStream_t, NULL for the default stream).  Returns TMC_E_ARG when
+ * nCells or nEdges is not in 1..TMC_NOALLOC_MAX_ELEMENTS.  The first call on
+ * a device looks up the array's device address with that device current;
+ * make that first call before any stream capture.  Calls that overlap on the
+ * GPU (other streams, other host threads on the same device) race on the
+ * shared array. */
+int tmc_mass_energy_noalloc(const double* gd, const double* ghs, const double* areaCell, int64_t nCells,
+                            const double* iap_u, const double* areaEdge, int64_t nEdges, double* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

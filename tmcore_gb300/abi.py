@@ -75,7 +75,9 @@ SYMBOLS = {
     "tmc_op_upwind_correction": (ctypes.c_int, [vp, vp, vp, vp, i32, i32]),
     "tmc_time_steps": (ctypes.c_int, [vp, i32, dp, dp, ctypes.POINTER(i32), ctypes.POINTER(i32)]),
     "tmc_sizes": (ctypes.c_int, [vp, i64p, i64p, i64p, i64p]),
+    "tmc_mass_energy_noalloc": (ctypes.c_int, [vp, vp, vp, ctypes.c_int64, vp, vp, ctypes.c_int64, vp, vp]),
 }
+TMC_NOALLOC_MAX_ELEMENTS = 8388608
 
 
 def declare(lib: ctypes.CDLL) -> ctypes.CDLL:
