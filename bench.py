@@ -144,23 +144,68 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def flux_kernel_bytes(nc: int, ne: int, S: int, me2: int = 10) -> float:
-    """Compulsory bytes of one edge_flux launch (averaged over the 4 CRK4 stages).
+# ---------------------------------------------------------------------------
+# Algorithmic (compulsory) bytes of the device kernels: every array read once
+# per launch, gathered neighbour values counted once (perfect reuse), writes
+# once.  S: bytes of an edge/vertex/tracer state value (4 FP32 path, 8 FP64
+# path); Mw: bytes of a metric in the arithmetic (FP32 copies in the FP32
+# path, FP64 otherwise); gd is FP64 in both paths.  The layouts are those of
+# tmcore_gb300/csrc (structure of arrays, int32 indices, int8 signs).
+# ---------------------------------------------------------------------------
+def flux_kernel_bytes(nc: int, ne: int, S: int, mode: int | None = None) -> float:
+    """k_edge_flux: edgesOnEdge 40, weightsOnEdge 10 Mw, cellsOnEdge 8, dcEdge Mw;
+    pv_e, u, F (FP32) or gd_edge (FP64) and own gd_edge: 4 S; RK traffic by
+    stage (1: old r, acc/tend/next w; 2,3: areaEdge, tend r+w, acc r+w, old r,
+    next w; 4: areaEdge, tend r+w, acc r+w); per cell E (S) and the gd
+    tendency (S in the FP32 path's shadow, 8 in FP64)."""
+    Mw = S
+    rk = {1: 4 * S, 2: Mw + 6 * S, 3: Mw + 6 * S, 4: Mw + 4 * S}
+    modes = [mode] if mode else [1, 2, 3, 4]
+    tot = 0.0
+    for md in modes:
+        tot += ne * (40 + 10 * Mw + 8 + Mw + 4 * S + rk[md]) + nc * (S + S)
+    return tot / len(modes)
 
-    Per edge: edgesOnEdge 4*me2, weightsOnEdge 8*me2, nEdgesOnEdge 1,
-    cellsOnEdge 8, dcEdge 8, areaEdge 8; pv_e, u, gd_edge, iap_u of the stage
-    (own and neighbours, read once: 4S); RK traffic per stage mode
-    (1: old r, tend/acc/next w = 4S; 2,3: tend r+w, acc r+w, old r, next w
-    = 6S; 4: tend r+w, acc r+w = 4S).  Per cell: E (S) and the FP64 gd
-    tendency (8).
-    """
-    mesh = 4 * me2 + 8 * me2 + 1 + 8 + 8 + 8
-    rk = (4 + 6 + 6 + 4) / 4.0
-    return ne * (mesh + (4 + rk) * S) + nc * (S + 8)
+
+def step_bytes(nc: int, ne: int, nv: int, S: int, ntr: int, diag: bool = True) -> float:
+    """All kernels of one CRK4 step, second-order tracers, invariants on stage 1:
+    4 stages of cell, vertex, edge_pv, edge_flux (stages 1-3 also prepare the
+    next stage's gd_edge, u, F), then the final update of cells and of edges
+    (which prepares the next step's first stage)."""
+    Mw = S
+    sh = 4 if S == 4 else 0  # FP32 shadows
+    tot = 0.0
+    for k in (1, 2, 3, 4):
+        dg = diag and k == 1
+        # cell: nEdgesOnCell, edgesOnCell, nSign, cellsOnCell (tracers), 1/areaCell (f64) [+ f32 copies],
+        # gd, ghs, E out; per edge u, F, dvEdge, areaEdge; tracer values of the neighbours;
+        # RK of gd (f64) and tracers (S)
+        rk_gd = {1: 8 + 8 + sh + 8 + sh, 2: Mw + 2 * sh + 16 + 8 + 8 + sh,
+                 3: Mw + 2 * sh + 16 + 8 + 8 + sh, 4: Mw + 2 * sh + 16}[k]
+        if S == 8:
+            rk_gd = {1: 8 * 4, 2: 8 * 6, 3: 8 * 6, 4: 8 * 4}[k]
+        rk_q = {1: 4 * S, 2: 5 * S, 3: 5 * S, 4: 2 * S}[k] + (sh if k <= 3 else 0)
+        tot += nc * (1 + 24 + 6 + (24 if ntr else 0) + 8 + 2 * sh + S + S + S + rk_gd + ntr * (S + rk_q)
+                     + (24 if dg else 0)) + ne * (2 * S + 2 * Mw)
+        # vertex: cellsOnVertex, edgesOnVertex, kite, tSign, 1/areaTriangle, fVertex; pv out;
+        # gd and u, dcEdge gathered
+        tot += nv * (12 + 12 + 3 * Mw + 3 + Mw + Mw + S + (16 if dg else 0)) + nc * S + ne * (S + Mw)
+        # edge_pv: verticesOnEdge; pv_e out; pv gathered
+        tot += ne * (8 + S) + nv * S
+        # edge_flux; stages 1-3 prepare the next stage instead of storing iap_u:
+        # next gd gathered, gd_edge/u/F written
+        tot += flux_kernel_bytes(nc, ne, S, k)
+        if k <= 3:
+            tot += nc * S + ne * (3 * S - S)
+    # final cells: gd r+w, acc r, shadow w; tracers r+w, acc r, shadow w
+    tot += nc * (24 + sh + ntr * (3 * S + sh))
+    # final edges: iap_u r+w, acc r, cellsOnEdge, gd gathered, gd_edge/u/F written, areaEdge (energy)
+    tot += ne * (3 * S + 8 + 3 * S + Mw) + nc * S
+    return tot
 
 
 def step_model_bytes(nc: int, ne: int, nv: int, S: int, ntr: int) -> float:
-    """Compulsory bytes per CRK4 step of the whole path (the per-step model:
+    """The hot-path scope's per-step compulsory-traffic model (FP64 metrics,
     each mesh array read once per stage, state read/written once per stage;
     4 stages + the final update), plus the coupled tracers in FP64."""
     per_stage = 39 * nc + 153 * ne + 67 * nv + 8 * S * nc + 7 * S * ne
@@ -302,7 +347,8 @@ def main():
     peak, peak_kind = measured_peaks()
     traffic = ncu_traffic("edge_flux_level9_fp32.json")
 
-    step_bytes = step_model_bytes(m.nCells, m.nEdges, m.nVertices, S, args.tracers)
+    sbytes = step_bytes(m.nCells, m.nEdges, m.nVertices, S, args.tracers)
+    scope_bytes = step_model_bytes(m.nCells, m.nEdges, m.nVertices, S, args.tracers)
     step_s = ms_total / args.steps / 1e3
 
     # ---- FP32 h error against the plain FP64 path after the same warmup + K steps ----
@@ -322,8 +368,8 @@ def main():
         extra["fp64"] = {
             "value": args.steps * args.dt / DAY / (ms64 / 1e3), "unit": "simulated days/wall-s",
             "ms_per_step": ms64 / args.steps,
-            "step_model_gbs": step_model_bytes(m.nCells, m.nEdges, m.nVertices, 8, args.tracers)
-            / (ms64 / args.steps / 1e3) / 1e9}
+            "step_gbs": step_bytes(m.nCells, m.nEdges, m.nVertices, 8, args.tracers) / (ms64 / args.steps / 1e3) / 1e9,
+            "bound": "fp64 pipe (GB300 FP64 issue rate is 1/64 of FP32)"}
         extra["h_error_fp32_vs_fp64"] = {
             "rel_max": float(np.max(np.abs(h32 - h64)) / np.max(np.abs(h64))),
             "rel_l2": float(np.sqrt(np.sum(area * (h32 - h64) ** 2) / np.sum(area * h64 ** 2))),
@@ -384,8 +430,10 @@ def main():
         "roofline": {"bound": "hbm", "kernel": "k_edge_flux<float>", "achieved": achieved, "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                      "algorithmic_bytes_per_launch": fb, "launch_ms": t_launch * 1e3, "launches_timed": n_flux},
-        "step_roofline": {"model_bytes_per_step": step_bytes, "achieved_gbs": step_bytes / step_s / 1e9,
-                          "frac": step_bytes / step_s / 1e9 / peak},
+        "step_roofline": {"algorithmic_bytes_per_step": sbytes, "achieved_gbs": sbytes / step_s / 1e9,
+                          "frac": sbytes / step_s / 1e9 / peak,
+                          "scope_model_bytes_per_step": scope_bytes,
+                          "scope_model_frac": scope_bytes / step_s / 1e9 / peak},
         "e2e": e2e,
         "cpu_baseline": cpu,
         "setup_s": t_setup,

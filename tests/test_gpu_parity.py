@@ -149,10 +149,12 @@ def test_one_day_level5_parity_and_invariants(mesh5):
     g.close()
 
 
-def test_tracers_match_oracle(mesh4):
+@pytest.mark.parametrize("tracer_order", [0, 3, 5])
+def test_tracers_match_oracle(mesh4, tracer_order):
     from tmcore_gb300 import cases
 
-    kw = dict(dt=600.0, pv_scheme=1, apvm_weight=0.0, n_tracers=3)
+    kw = dict(dt=600.0, pv_scheme=1, apvm_weight=0.0, n_tracers=3, tracer_adv_order=tracer_order,
+              tracer_adv_mono=1)
     g, o = _models(mesh4, **kw)
     gd, u, ghs = _ic(mesh4, seed=2)
     q = cases.smooth_tracers(mesh4, 3, seed=2)

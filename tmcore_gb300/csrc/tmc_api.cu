@@ -32,6 +32,7 @@ struct EngineBase {
   virtual int alloc() = 0;
   virtual void launch_step(bool diag, std::vector<cudaEvent_t>* flux_ev, size_t* ev_pos) = 0;
   virtual void launch_diag_pass(bool finalize) = 0;
+  virtual void launch_prep() = 0;
   virtual void launch_spatial_only() = 0;
   virtual void set_state_dev(const double* raw_gd, const double* raw_iap) = 0;  // from raw (original order)
   virtual void get_field(int which, double* raw_out) = 0;                       // scatter to raw
@@ -65,6 +66,7 @@ struct tmc_handle {
   double* h_diag = nullptr;
   int bs = 256;
   bool have_state = false;
+  bool prep_valid = false;  // edge set 0 holds the preparation of state(old)
   std::unique_ptr<EngineBase> eng;
   cudaGraphExec_t g_step = nullptr, g_step_diag = nullptr;
   long step_count = 0;
@@ -109,10 +111,15 @@ struct Engine : EngineBase {
   float* ghsf = nullptr;
   float* gdf[3] = {};  // FP32 path: shadows of gd and tracer mixing ratios per slot
   float* qr[3] = {};
-  T* F = nullptr;
+  // edge quantities of a stage, double-buffered by stage parity: stage k reads
+  // set (k-1)%2 while its flux pass prepares the next stage's set
+  T* F[2] = {};
+  T* gd_e[2] = {};
+  T* u[2] = {};
+  T* Fq[2] = {};
   double *gd_acc = nullptr, *gd_tend = nullptr, *ghs = nullptr;
   T* q_acc = nullptr;
-  T *iap_acc = nullptr, *iap_tend = nullptr, *gd_e = nullptr, *u = nullptr, *Fq = nullptr, *E = nullptr;
+  T *iap_acc = nullptr, *iap_tend = nullptr, *E = nullptr;
   T *pv_v = nullptr, *vor = nullptr, *gd_v = nullptr, *pv_c = nullptr, *v_e = nullptr, *pv_e = nullptr;
   explicit Engine(tmc_handle* hh) : h(hh) {}
 
@@ -129,9 +136,13 @@ struct Engine : EngineBase {
     ghs = h->dalloc<double>(nc);
     iap_acc = h->dalloc<T>(ne);
     iap_tend = h->dalloc<T>(ne);
-    gd_e = h->dalloc<T>(ne);
-    u = h->dalloc<T>(ne);
-    Fq = h->dalloc<T>((size_t)ne * (nt > 0 ? nt : 1));
+    const bool edge_fluxes = nt > 0 && h->O.tr_order >= 3;
+    for (int i = 0; i < 2; ++i) {
+      gd_e[i] = h->dalloc<T>(ne);
+      u[i] = h->dalloc<T>(ne);
+      F[i] = h->dalloc<T>(ne);
+      Fq[i] = h->dalloc<T>(edge_fluxes ? (size_t)ne * nt : 1);
+    }
     E = h->dalloc<T>(nc);
     pv_v = h->dalloc<T>(nv);
     vor = h->dalloc<T>(nv);
@@ -139,14 +150,13 @@ struct Engine : EngineBase {
     pv_c = h->dalloc<T>(nc);
     v_e = h->dalloc<T>(ne);
     pv_e = h->dalloc<T>(ne);
-    F = h->dalloc<T>(ne);
     if (!std::is_same<T, double>::value) {
       for (int i = 0; i < 3; ++i) {
         gdf[i] = h->dalloc<float>(nc);
         qr[i] = h->dalloc<float>((size_t)nc * (nt > 0 ? nt : 1));
       }
     }
-    if (!pv_e || !F) return TMC_E_CUDA;
+    if (!pv_e || !F[1] || !Fq[1]) return TMC_E_CUDA;
     cudaMemset(ghs, 0, sizeof(double) * nc);
     if (!std::is_same<T, double>::value) {
       tendf = h->dalloc<float>(nc);
@@ -158,9 +168,15 @@ struct Engine : EngineBase {
     return TMC_OK;
   }
 
+  // Buffers of CRK4 stage k (1..4; 0 for the stand-alone passes on slot 0).
+  // State slots: stage inputs old, A, B, A; stage k writes the next stage's gd
+  // (and tracers) into next_slot.  Edge quantities: set (k-1)%2, and stages
+  // 1-3 prepare the next stage's set in their flux pass.
   StageIO<T> io(int k) const {
     StageIO<T> s{};
     static const int in_slot[5] = {0, 0, 1, 2, 1}, next_slot[5] = {-1, 1, 2, 1, -1};
+    const int set = (k >= 1) ? (k - 1) % 2 : 0;
+    const bool fuse = (k >= 1 && k <= 3);
     s.gd_in = gd[in_slot[k]];
     s.gd_old = gd[0];
     s.gd_next = next_slot[k] >= 0 ? gd[next_slot[k]] : nullptr;
@@ -175,9 +191,14 @@ struct Engine : EngineBase {
     s.q_old = q[0];
     s.q_next = next_slot[k] >= 0 ? q[next_slot[k]] : nullptr;
     s.q_acc = q_acc;
-    s.gd_e = gd_e;
-    s.u = u;
-    s.Fq = Fq;
+    s.gd_e = gd_e[set];
+    s.u = u[set];
+    s.F = F[set];
+    s.Fq = Fq[set];
+    s.gd_e_nx = fuse ? gd_e[1 - set] : nullptr;
+    s.u_nx = fuse ? u[1 - set] : nullptr;
+    s.F_nx = fuse ? F[1 - set] : nullptr;
+    s.Fq_nx = fuse ? Fq[1 - set] : nullptr;
     s.E = E;
     s.pv_v = pv_v;
     s.vor = vor;
@@ -186,7 +207,6 @@ struct Engine : EngineBase {
     s.v_e = v_e;
     s.pv_e = pv_e;
     s.ghs = ghs;
-    s.F = F;
     s.gdf_in = gdf[in_slot[k]];
     s.gdf_next = next_slot[k] >= 0 ? gdf[next_slot[k]] : nullptr;
     s.qr_in = qr[in_slot[k]];
@@ -197,11 +217,20 @@ struct Engine : EngineBase {
   }
 
   int launches_per_step() const override {
-    int per_stage = 5 + ((h->O.pv_scheme == 1 && h->O.apvm_weight != 0.0) ? 1 : 0);
-    return 4 * per_stage + 2;
+    int per_stage = 4 + ((h->O.pv_scheme == 1 && h->O.apvm_weight != 0.0) ? 1 : 0);
+    return 4 * per_stage + 3;
   }
 
-  // one CRK4 step (time_scheme_mod.F90:109-154); state(old) updated in place
+  // Edge preparation of state(old) into set 0 (+ the energy partials); needed
+  // once after the state was set from outside, afterwards each step's final
+  // pass keeps it current.
+  void launch_prep() override {
+    StageIO<T> s = io(0);
+    launch_edge_prep<T>(h->M, h->O, s, h->P, true, h->bs, h->st);
+  }
+
+  // one CRK4 step (time_scheme_mod.F90:109-154); state(old) updated in place.
+  // Requires set 0 prepared from state(old) (launch_prep or the previous step).
   void launch_step(bool diag, std::vector<cudaEvent_t>* flux_ev, size_t* ev_pos) override {
     const DevMesh& M = h->M;
     const ModelOpt& O = h->O;
@@ -209,9 +238,10 @@ struct Engine : EngineBase {
     const double adt[5] = {0.0, 0.5 * dt, 0.5 * dt, dt, 0.0};
     for (int k = 1; k <= 4; ++k) {
       StageIO<T> s = io(k);
+      s.vor = nullptr;  // vorticity and gd on vertices are kept only by the diagnostic pass
+      s.gd_v = nullptr;
       const bool dg = diag && k == 1;
       RKStage rk{k, adt[k]};
-      launch_edge_prep<T>(M, O, s, h->P, dg, h->bs, h->st);
       launch_cell<T>(M, O, s, rk, h->P, dg, h->bs, h->st);
       launch_vertex<T>(M, O, s, h->P, dg, h->bs, h->st);
       launch_edge_pv<T>(M, O, s, h->bs, h->st);
@@ -221,12 +251,12 @@ struct Engine : EngineBase {
     }
     launch_finalize(h->P, h->counts, h->hm.totalArea, h->hm.sumAreaTriangle, dt, true, diag,
                     h->p.conserve_energy != 0, h->d_diag, h->st);
-    launch_final_update<T>(M, O, io(1), h->d_diag, h->bs, h->st);
+    launch_final_update<T>(M, O, io(0), h->d_diag, h->P, h->bs, h->st);
   }
 
   // diagnostics of state(old): gd_edge, u, gd/pv/vor on vertices, invariants
   void launch_diag_pass(bool finalize) override {
-    StageIO<T> s = io(1);
+    StageIO<T> s = io(0);
     RKStage rk{0, 0.0};
     launch_edge_prep<T>(h->M, h->O, s, h->P, true, h->bs, h->st);
     launch_cell<T>(h->M, h->O, s, rk, h->P, true, h->bs, h->st);
@@ -236,9 +266,14 @@ struct Engine : EngineBase {
                       h->p.conserve_energy != 0, h->d_diag, h->st);
   }
 
-  // spatial_operators on the state in slot 1 -> gd_tend, iap_tend
+  // spatial_operators on the state in slot 1 -> gd_tend, iap_tend (uses edge set 0)
   void launch_spatial_only() override {
-    StageIO<T> s = io(2);
+    StageIO<T> s = io(0);
+    s.gd_in = gd[1];
+    s.iap_in = iap[1];
+    s.q_in = q[1];
+    s.gdf_in = gdf[1];
+    s.qr_in = qr[1];
     RKStage rk{0, 0.0};
     launch_edge_prep<T>(h->M, h->O, s, h->P, false, h->bs, h->st);
     launch_cell<T>(h->M, h->O, s, rk, h->P, false, h->bs, h->st);
@@ -260,7 +295,7 @@ struct Engine : EngineBase {
     switch (which) {
       case F_GD: launch_scatter<double>(h->M.nc, gd[0], h->d_cell_n2o, raw, h->st); break;
       case F_IAP: launch_scatter<T>(h->M.ne, iap[0], h->d_edge_n2o, raw, h->st); break;
-      case F_U: launch_scatter<T>(h->M.ne, u, h->d_edge_n2o, raw, h->st); break;
+      case F_U: launch_scatter<T>(h->M.ne, u[0], h->d_edge_n2o, raw, h->st); break;
       case F_PV_V: launch_scatter<T>(h->M.nv, pv_v, h->d_vert_n2o, raw, h->st); break;
       case F_VOR: launch_scatter<T>(h->M.nv, vor, h->d_vert_n2o, raw, h->st); break;
       case F_TEND_GD: launch_scatter<double>(h->M.nc, gd_tend, h->d_cell_n2o, raw, h->st); break;
@@ -312,7 +347,15 @@ int build_graph(tmc_handle* h, bool diag, cudaGraphExec_t* out) {
   return TMC_OK;
 }
 
+void ensure_prep(tmc_handle* h) {
+  if (!h->prep_valid) {
+    h->eng->launch_prep();
+    h->prep_valid = true;
+  }
+}
+
 int launch_one_step(tmc_handle* h) {
+  ensure_prep(h);
   const bool diag = h->p.diag_every > 0 && (h->step_count % h->p.diag_every) == 0;
   if (h->p.use_graph) {
     cudaGraphExec_t* g = diag ? &h->g_step_diag : &h->g_step;
@@ -447,6 +490,7 @@ int tmc_create(const tmc_mesh_desc* mesh, const tmc_params* params, tmc_handle**
   M.me2 = hm.me2;
   M.nEdgesOnCell = h->upload(hm.nEdgesOnCell);
   M.edgesOnCell = h->upload(hm.edgesOnCell);
+  M.cellsOnCell = h->upload(hm.cellsOnCell);
   M.nSign = h->upload(hm.nSignEdge);
   M.areaCell = h->upload(hm.areaCell);
   M.cellsOnEdge = h->upload(hm.cellsOnEdge);
@@ -594,6 +638,7 @@ int tmc_set_initial(tmc_handle* h, const double* gd, const double* u, const doub
   if ((rc = h2d(h, h->raw_c, ghs, nc))) return rc;
   h->eng->set_ghs_dev(h->raw_c);
   h->have_state = true;
+  h->prep_valid = false;
   h->step_count = 0;
   if ((rc = sync(h, "tmc_set_initial"))) return rc;
   return h->cuda_check("tmc_set_initial");
@@ -607,6 +652,7 @@ int tmc_set_state(tmc_handle* h, const double* gd, const double* iap_u) {
   if ((rc = h2d(h, h->raw_e, iap_u, h->M.ne))) return rc;
   h->eng->set_state_dev(h->raw_c, h->raw_e);
   h->have_state = true;
+  h->prep_valid = false;
   if ((rc = sync(h, "tmc_set_state"))) return rc;
   return h->cuda_check("tmc_set_state");
 }
@@ -659,6 +705,7 @@ int tmc_set_tracers(tmc_handle* h, const double* qgd) {
   int rc;
   if ((rc = h2d(h, h->raw_q, qgd, (size_t)h->M.nc * h->O.n_tracers))) return rc;
   h->eng->set_tracers_dev(h->raw_q);
+  h->prep_valid = false;
   if ((rc = sync(h, "tmc_set_tracers"))) return rc;
   return h->cuda_check("tmc_set_tracers");
 }
@@ -721,6 +768,7 @@ int tmc_time_integrate(tmc_handle* h, const double* gd_old, const double* iap_u_
     h->eng->set_tracers_dev(h->raw_q);
   }
   h->have_state = true;
+  h->prep_valid = false;
   if ((rc = launch_one_step(h))) return rc;
   h->eng->get_field(F_GD, h->raw_c);
   if ((rc = d2h(h, gd_new, h->raw_c, h->M.nc))) return rc;
@@ -756,6 +804,7 @@ int tmc_spatial_operators(tmc_handle* h, const double* gd, const double* iap_u, 
     e32->refresh_shadows(1);
   }
   h->eng->launch_spatial_only();
+  h->prep_valid = false;
   h->eng->get_field(F_TEND_GD, h->raw_c);
   if ((rc = d2h(h, tend_gd, h->raw_c, h->M.nc))) return rc;
   h->eng->get_field(F_TEND_IAP, h->raw_e);
@@ -863,6 +912,7 @@ int tmc_time_steps(tmc_handle* h, int32_t nsteps, double* ms_total, double* ms_f
     size_t pos = 0;
     for (int i = 0; i < nsteps; ++i) {
       const bool diag = h->p.diag_every > 0 && (h->step_count % h->p.diag_every) == 0;
+      ensure_prep(h);
       h->eng->launch_step(diag, &evs, &pos);
       h->step_count++;
     }

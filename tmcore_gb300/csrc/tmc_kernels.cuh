@@ -46,6 +46,7 @@ struct DevMesh {
   int nc, ne, nv, me, me2;
   const uint8_t* nEdgesOnCell;
   const int32_t* edgesOnCell;  // [me][nc]
+  const int32_t* cellsOnCell;  // [me][nc], the cell across edgesOnCell (derived)
   const int8_t* nSign;         // [me][nc]
   const double* areaCell;
   const int32_t* cellsOnEdge;     // [2][ne]
@@ -157,6 +158,13 @@ struct StageIO {
   T* u;
   T* F;   // u * gd_e
   T* Fq;  // [ntr][ne]
+  // the next stage's gd_e, u, F, Fq, written by k_edge_flux (stages 1-3) and
+  // k_final_edges (next step): the edge preparation of the next stage fused
+  // into the pass that produces its iap_u (null: not fused)
+  T* gd_e_nx;
+  T* u_nx;
+  T* F_nx;
+  T* Fq_nx;
   T* E;
   T* pv_v;
   T* vor;
@@ -182,9 +190,11 @@ void launch_edge_pv(const DevMesh& M, const ModelOpt& O, const StageIO<T>& S, in
 template <class T>
 void launch_edge_flux(const DevMesh& M, const ModelOpt& O, const StageIO<T>& S, RKStage rk, Partials P, int bs,
                       cudaStream_t st);
+// final update (beta-scaled) of cells, then of edges together with the edge
+// preparation of the next step's first stage and its energy partials
 template <class T>
-void launch_final_update(const DevMesh& M, const ModelOpt& O, const StageIO<T>& S, const double* diag, int bs,
-                         cudaStream_t st);
+void launch_final_update(const DevMesh& M, const ModelOpt& O, const StageIO<T>& S, const double* diag, Partials P,
+                         int bs, cudaStream_t st);
 // number of blocks a launcher uses for n elements
 inline int grid_for(int n, int bs) { return (n + bs * kEPT - 1) / (bs * kEPT); }
 

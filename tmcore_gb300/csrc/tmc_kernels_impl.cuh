@@ -174,9 +174,76 @@ __device__ __forceinline__ T upwind_edge(const DStencil& S2, const DStencil& S4,
 // ---------------------------------------------------------------------------
 // edge_prep: gd_edge, u, mass flux F, tracer fluxes
 // ---------------------------------------------------------------------------
+// The cell-side values an edge preparation reads: gd (FP64, or the FP32
+// shadow) and the tracer mass (FP64) or mixing-ratio shadow (FP32) of one
+// state slot.
+template <class T>
+struct CellSrc {
+  const double* gd;
+  const float* gdf;
+  const T* q;
+  const float* qr;
+};
+
+// Edge preparation of one edge (operators_mod.F90:93-104 c2e, :423-472 upwind
+// correction with the sign of iap_u, :168-176 inverse IAP; the mass flux
+// u*gd_edge of tmcore_swm_mod.F90:135; for tracers of order >= 3 the sg11
+// edge value of adv_scheme_sg11_mod.F90:42-45 times the mass flux).
+// g1, g2 are the two cells' gd in T, already loaded by the caller.
+template <class T>
+__device__ __forceinline__ void prep_edge(const DevMesh& M, const ModelOpt& O, int e, int c1, int c2, T ia, T g1,
+                                          T g2, const CellSrc<T>& C, T* gd_e, T* u, T* F, T* Fq) {
+  T ge = T(0.5) * (g1 + g2);
+  if (O.adv_order >= 3) {
+    if constexpr (kF64<T>) {
+      const double* gd = C.gd;
+      ge = upwind_edge<T>(M.cell2, M.cell4, O.adv_order, T(O.cell_coef2), T(O.cell_coef4), M.ne, e, c1, c2, ge, ia,
+                          M.dcEdge[e], [gd](int i) { return gd[i]; });
+    } else {
+      const float* gd = C.gdf;
+      ge = upwind_edge<T>(M.cell2, M.cell4, O.adv_order, T(O.cell_coef2), T(O.cell_coef4), M.ne, e, c1, c2, ge, ia,
+                          M.dcEdge_f[e], [gd](int i) { return gd[i]; });
+    }
+  }
+  const T sq = sqrt(ge);
+  const T uu = ia / sq;
+  const T Fv = uu * ge;
+  gd_e[e] = ge;
+  u[e] = uu;
+  F[e] = Fv;
+  // second-order tracers are fluxed by k_cell directly (no per-edge flux stored)
+  for (int k = 0; k < (O.tr_order >= 3 ? O.n_tracers : 0); ++k) {
+    T qe;
+    if constexpr (kF64<T>) {
+      const double* q = C.q + (size_t)k * M.nc;
+      const double* gd = C.gd;
+      qe = 0.5 * (q[c1] / g1 + q[c2] / g2);
+      qe = upwind_edge<T>(M.cell2, M.cell4, O.tr_order, T(O.tr_coef2), T(O.tr_coef4), M.ne, e, c1, c2, qe, ia,
+                          M.dcEdge[e], [q, gd](int i) { return q[i] / gd[i]; });
+    } else {
+      const float* qr = C.qr + (size_t)k * M.nc;
+      qe = 0.5f * (qr[c1] + qr[c2]);
+      qe = upwind_edge<T>(M.cell2, M.cell4, O.tr_order, T(O.tr_coef2), T(O.tr_coef4), M.ne, e, c1, c2, qe, ia,
+                          M.dcEdge_f[e], [qr](int i) { return qr[i]; });
+    }
+    Fq[(size_t)k * M.ne + e] = Fv * qe;
+  }
+}
+
+template <class T>
+__device__ __forceinline__ T energy_term(const DevMesh& M, int e, T ia) {
+  if constexpr (kF64<T>)
+    return ia * ia * M.areaEdge[e];  // tmcore_swm_mod.F90:229
+  else
+    return ia * ia * M.areaEdge_f[e];
+}
+
+// Stand-alone edge preparation of a state slot (the first stage after the
+// state was set, the diagnostic pass, spatial_operators).
 template <class T>
 __global__ void __launch_bounds__(kMaxBlock) k_edge_prep(DevMesh M, ModelOpt O, StageIO<T> S, Partials P, int diag) {
   double en = 0.0;
+  const CellSrc<T> C{S.gd_in, S.gdf_in, S.q_in, S.qr_in};
   TMC_FOR_EPT(e, M.ne) {
     const int c1 = M.cellsOnEdge[e], c2 = M.cellsOnEdge[M.ne + e];
     const T ia = S.iap_in[e];
@@ -188,47 +255,12 @@ __global__ void __launch_bounds__(kMaxBlock) k_edge_prep(DevMesh M, ModelOpt O, 
       g1 = S.gdf_in[c1];
       g2 = S.gdf_in[c2];
     }
-    T ge = T(0.5) * (g1 + g2);
-    if (O.adv_order >= 3) {
-      if constexpr (kF64<T>) {
-        const double* gd = S.gd_in;
-        ge = upwind_edge<T>(M.cell2, M.cell4, O.adv_order, T(O.cell_coef2), T(O.cell_coef4), M.ne, e, c1, c2, ge,
-                            ia, M.dcEdge[e], [gd](int i) { return gd[i]; });
-      } else {
-        const float* gd = S.gdf_in;
-        ge = upwind_edge<T>(M.cell2, M.cell4, O.adv_order, T(O.cell_coef2), T(O.cell_coef4), M.ne, e, c1, c2, ge,
-                            ia, M.dcEdge_f[e], [gd](int i) { return gd[i]; });
-      }
-    }
-    const T sq = sqrt(ge);
-    const T uu = ia / sq;
-    const T F = uu * ge;
-    S.gd_e[e] = ge;
-    S.u[e] = uu;
-    S.F[e] = F;
-    for (int k = 0; k < O.n_tracers; ++k) {
-      T qe;
-      if constexpr (kF64<T>) {
-        const double* q = S.q_in + (size_t)k * M.nc;
-        const double* gd = S.gd_in;
-        qe = 0.5 * (q[c1] / g1 + q[c2] / g2);
-        if (O.tr_order >= 3)
-          qe = upwind_edge<T>(M.cell2, M.cell4, O.tr_order, T(O.tr_coef2), T(O.tr_coef4), M.ne, e, c1, c2, qe, ia,
-                              M.dcEdge[e], [q, gd](int i) { return q[i] / gd[i]; });
-      } else {
-        const float* qr = S.qr_in + (size_t)k * M.nc;
-        qe = 0.5f * (qr[c1] + qr[c2]);
-        if (O.tr_order >= 3)
-          qe = upwind_edge<T>(M.cell2, M.cell4, O.tr_order, T(O.tr_coef2), T(O.tr_coef4), M.ne, e, c1, c2, qe, ia,
-                              M.dcEdge_f[e], [qr](int i) { return qr[i]; });
-      }
-      S.Fq[(size_t)k * M.ne + e] = F * qe;
-    }
+    prep_edge<T>(M, O, e, c1, c2, ia, g1, g2, C, S.gd_e, S.u, S.F, S.Fq);
     if (diag) {
       if constexpr (kF64<T>)
-        en = en + ia * ia * M.areaEdge[e];
+        en = en + energy_term<T>(M, e, ia);
       else
-        en += (double)(ia * ia * M.areaEdge_f[e]);
+        en += (double)energy_term<T>(M, e, ia);
     }
   }
   if (diag) {
@@ -249,7 +281,8 @@ __global__ void __launch_bounds__(kMaxBlock) k_cell(DevMesh M, ModelOpt O, Stage
   TMC_FOR_EPT(c, M.nc) {
     double t;  // gd tendency, FP64 in both modes
     T tT, ke;
-    int eidx[kME];
+    int eidx[kME], cidx[kME];
+    float nsg[kME];
     const int n = M.nEdgesOnCell[c];
     const int mode = rk.mode;
     // RK inputs before any store (see k_edge_flux)
@@ -276,12 +309,16 @@ __global__ void __launch_bounds__(kMaxBlock) k_cell(DevMesh M, ModelOpt O, Stage
       ke = (k * 0.25) / A;
       S.E[c] = ke + S.gd_in[c] + S.ghs[c];
       (void)eidx;
+      (void)cidx;
+      (void)nsg;
     } else {
-      float nsg[kME], uu[kME], Fv[kME], dv[kME], ae[kME];
+      float uu[kME], Fv[kME], dv[kME], ae[kME];
+      const bool tr_direct = O.n_tracers > 0 && O.tr_order == 2;
 #pragma unroll
       for (int i = 0; i < kME; ++i) {
         eidx[i] = M.edgesOnCell[(size_t)i * M.nc + c];  // padded slots: index 0, sign 0
         nsg[i] = (float)M.nSign[(size_t)i * M.nc + c];
+        cidx[i] = tr_direct ? M.cellsOnCell[(size_t)i * M.nc + c] : 0;
       }
 #pragma unroll
       for (int i = 0; i < kME; ++i) {
@@ -384,18 +421,41 @@ __global__ void __launch_bounds__(kMaxBlock) k_cell(DevMesh M, ModelOpt O, Stage
         const size_t qi = (size_t)q * M.nc + c;
         qo[j] = (mode >= 1 && mode <= 3) ? S.q_old[qi] : T(0);
         qa[j] = (mode >= 2) ? S.q_acc[qi] : T(0);
+        // Second-order tracers take the edge value from the two cells directly,
+        // q_edge = (q(c1) + q(c2))/2, so no per-edge tracer flux is stored;
+        // higher orders read the fluxes k_edge_prep wrote with the upwind
+        // correction.
+        const bool direct = (O.tr_order == 2);
         if constexpr (kF64<T>) {
           double sq = 0.0;
+          const double qs = direct ? S.q_in[qi] / S.gd_in[c] : 0.0;
           for (int i = 0; i < n; ++i) {
             const int e = M.edgesOnCell[(size_t)i * M.nc + c];
-            sq = sq + (double)M.nSign[(size_t)i * M.nc + c] * S.Fq[(size_t)q * M.ne + e] * M.dvEdge[e];
+            double flux;
+            if (direct) {
+              const int nb = M.cellsOnCell[(size_t)i * M.nc + c];
+              const double qn = S.q_in[(size_t)q * M.nc + nb] / S.gd_in[nb];
+              flux = S.F[e] * (0.5 * (qs + qn));
+            } else {
+              flux = S.Fq[(size_t)q * M.ne + e];
+            }
+            sq = sq + (double)M.nSign[(size_t)i * M.nc + c] * flux * M.dvEdge[e];
           }
           tq[j] = (-sq) / M.areaCell[c];
         } else {
           float sq = 0.f;
+          if (direct) {
+            const float qs = S.qr_in[qi];
 #pragma unroll
-          for (int i = 0; i < kME; ++i)
-            sq += (float)M.nSign[(size_t)i * M.nc + c] * S.Fq[(size_t)q * M.ne + eidx[i]] * M.dvEdge_f[eidx[i]];
+            for (int i = 0; i < kME; ++i) {
+              const float qn = S.qr_in[(size_t)q * M.nc + cidx[i]];
+              sq += nsg[i] * S.F[eidx[i]] * (0.5f * (qs + qn)) * M.dvEdge_f[eidx[i]];
+            }
+          } else {
+#pragma unroll
+            for (int i = 0; i < kME; ++i)
+              sq += nsg[i] * S.Fq[(size_t)q * M.ne + eidx[i]] * M.dvEdge_f[eidx[i]];
+          }
           tq[j] = -sq * M.invAreaCell_f[c];
         }
       }
@@ -584,6 +644,18 @@ __global__ void __launch_bounds__(kMaxBlock) k_edge_flux(DevMesh M, ModelOpt O, 
     const T accv = (mode >= 2) ? S.iap_acc[e] : T(0);
     const T oldv = (mode >= 1 && mode <= 3) ? S.iap_old[e] : T(0);
     const T ae = (mode >= 2) ? met<T>(M.areaEdge, M.areaEdge_f, e) : T(0);
+    // the next stage's gd on the two cells (written by this stage's k_cell)
+    const bool fuse = (S.u_nx != nullptr);
+    T gn1 = T(0), gn2 = T(0);
+    if (fuse) {
+      if constexpr (kF64<T>) {
+        gn1 = S.gd_next[c1];
+        gn2 = S.gd_next[c2];
+      } else {
+        gn1 = S.gdf_next[c1];
+        gn2 = S.gdf_next[c2];
+      }
+    }
     T s = T(0), tge, dEdx, dc;
     if constexpr (kF64<T>) {
       // calc_tangent_vor_flux (operators_mod.F90:239-260), in order
@@ -634,6 +706,7 @@ __global__ void __launch_bounds__(kMaxBlock) k_edge_flux(DevMesh M, ModelOpt O, 
     const T sq = sqrt(ge);
     const T it = sq * ut + T(0.5) * uu / sq * tge;
     T* tb = S.iap_tend;
+    T inext = T(0);  // iap_u of the next stage (update_state, tmcore_swm_mod.F90:210)
     switch (mode) {
       case 0:
         tb[e] = it;
@@ -641,14 +714,14 @@ __global__ void __launch_bounds__(kMaxBlock) k_edge_flux(DevMesh M, ModelOpt O, 
       case 1:
         S.iap_acc[e] = it;
         tb[e] = it;
-        S.iap_next[e] = oldv + T(rk.a_dt) * it;
+        inext = oldv + T(rk.a_dt) * it;
         break;
       case 2:
       case 3: {
         rip = rip + tp * it * ae;
         S.iap_acc[e] = accv + T(2) * it;
         tb[e] = it;
-        S.iap_next[e] = oldv + T(rk.a_dt) * it;
+        inext = oldv + T(rk.a_dt) * it;
         break;
       }
       case 4: {
@@ -664,6 +737,13 @@ __global__ void __launch_bounds__(kMaxBlock) k_edge_flux(DevMesh M, ModelOpt O, 
         break;
       }
     }
+    if (fuse) {
+      // edge preparation of the next stage from its gd and iap_u
+      const CellSrc<T> C{S.gd_next, S.gdf_next, S.q_next, S.qr_next};
+      prep_edge<T>(M, O, e, c1, c2, inext, gn1, gn2, C, S.gd_e_nx, S.u_nx, S.F_nx, S.Fq_nx);
+    } else if (mode >= 1 && mode <= 3) {
+      S.iap_next[e] = inext;
+    }
   }
   if (rk.mode >= 2) {
     const T v[2] = {rip, r44};
@@ -673,29 +753,58 @@ __global__ void __launch_bounds__(kMaxBlock) k_edge_flux(DevMesh M, ModelOpt O, 
 }
 
 // new = old + (beta dt) t_new (update_state, tmcore_swm_mod.F90:203-213)
+// Cells: gd and tracer mass of state(old) in place, and their FP32 shadows.
 template <class T>
-__global__ void __launch_bounds__(kMaxBlock) k_final_update(DevMesh M, ModelOpt O, StageIO<T> S, const double* diag) {
+__global__ void __launch_bounds__(kMaxBlock) k_final_cells(DevMesh M, ModelOpt O, StageIO<T> S, const double* diag) {
   const double bdt = diag[9];
-  const int n = M.ne > M.nc ? M.ne : M.nc;
-  TMC_FOR_EPT(i, n) {
-    if (i < M.ne) {
-      T* iap = const_cast<T*>(S.iap_old);
-      iap[i] = iap[i] + T(bdt) * S.iap_acc[i];
-    }
-    if (i < M.nc) {
-      double* gd = const_cast<double*>(S.gd_old);
-      const double g = gd[i] + bdt * S.gd_acc[i];
-      gd[i] = g;
-      if constexpr (!kF64<T>) const_cast<float*>(S.gdf_in)[i] = (float)g;
-      for (int q = 0; q < O.n_tracers; ++q) {
-        const size_t qi = (size_t)q * M.nc + i;
-        T* qq = const_cast<T*>(S.q_old);
-        const T qn = qq[qi] + T(bdt) * S.q_acc[qi];
-        qq[qi] = qn;
-        if constexpr (!kF64<T>) const_cast<float*>(S.qr_in)[qi] = qn / (float)g;
-      }
+  TMC_FOR_EPT(i, M.nc) {
+    double* gd = const_cast<double*>(S.gd_old);
+    const double g = gd[i] + bdt * S.gd_acc[i];
+    gd[i] = g;
+    if constexpr (!kF64<T>) const_cast<float*>(S.gdf_in)[i] = (float)g;
+    for (int q = 0; q < O.n_tracers; ++q) {
+      const size_t qi = (size_t)q * M.nc + i;
+      T* qq = const_cast<T*>(S.q_old);
+      const T qn = qq[qi] + T(bdt) * S.q_acc[qi];
+      qq[qi] = qn;
+      if constexpr (!kF64<T>) const_cast<float*>(S.qr_in)[qi] = qn / (float)g;
     }
   }
+}
+
+// Edges: iap_u of state(old) in place, then the edge preparation of the next
+// step's first stage (into S.gd_e/u/F/Fq) and the edge part of the total
+// energy of the new state (tmcore_swm_mod.F90:229) for the next step's
+// invariants.
+template <class T>
+__global__ void __launch_bounds__(kMaxBlock) k_final_edges(DevMesh M, ModelOpt O, StageIO<T> S, const double* diag,
+                                                           Partials P) {
+  const double bdt = diag[9];
+  double en = 0.0;
+  const CellSrc<T> C{S.gd_old, S.gdf_in, S.q_old, S.qr_in};
+  TMC_FOR_EPT(e, M.ne) {
+    const int c1 = M.cellsOnEdge[e], c2 = M.cellsOnEdge[M.ne + e];
+    T* iap = const_cast<T*>(S.iap_old);
+    const T a0 = iap[e], acc = S.iap_acc[e];
+    T g1, g2;
+    if constexpr (kF64<T>) {
+      g1 = S.gd_old[c1];
+      g2 = S.gd_old[c2];
+    } else {
+      g1 = S.gdf_in[c1];
+      g2 = S.gdf_in[c2];
+    }
+    const T ia = a0 + T(bdt) * acc;
+    iap[e] = ia;
+    prep_edge<T>(M, O, e, c1, c2, ia, g1, g2, C, S.gd_e, S.u, S.F, S.Fq);
+    if constexpr (kF64<T>)
+      en = en + energy_term<T>(M, e, ia);
+    else
+      en += (double)energy_term<T>(M, e, ia);
+  }
+  const double v[1] = {en};
+  const int r[1] = {R_EN_E};
+  block_store<double, 1>(v, P, r);
 }
 
 template <class T>
@@ -745,9 +854,10 @@ void launch_edge_flux(const DevMesh& M, const ModelOpt& O, const StageIO<T>& S, 
   k_edge_flux<T><<<grid_for(M.ne, bs), bs, 0, st>>>(M, O, S, rk, P);
 }
 template <class T>
-void launch_final_update(const DevMesh& M, const ModelOpt& O, const StageIO<T>& S, const double* diag, int bs,
-                         cudaStream_t st) {
-  k_final_update<T><<<grid_for(M.ne > M.nc ? M.ne : M.nc, bs), bs, 0, st>>>(M, O, S, diag);
+void launch_final_update(const DevMesh& M, const ModelOpt& O, const StageIO<T>& S, const double* diag, Partials P,
+                         int bs, cudaStream_t st) {
+  k_final_cells<T><<<grid_for(M.nc, bs), bs, 0, st>>>(M, O, S, diag);
+  k_final_edges<T><<<grid_for(M.ne, bs), bs, 0, st>>>(M, O, S, diag, P);
 }
 template <class T>
 void launch_gather(int n, const double* src, const int32_t* n2o, T* dst, cudaStream_t st) {
@@ -775,7 +885,7 @@ void launch_iap_from_u(int ne, const double* gd_e, const double* u, T* iap, cuda
   template void launch_edge_pv<T>(const DevMesh&, const ModelOpt&, const StageIO<T>&, int, cudaStream_t);        \
   template void launch_edge_flux<T>(const DevMesh&, const ModelOpt&, const StageIO<T>&, RKStage, Partials, int,  \
                                     cudaStream_t);                                                                \
-  template void launch_final_update<T>(const DevMesh&, const ModelOpt&, const StageIO<T>&, const double*, int,   \
-                                       cudaStream_t);
+  template void launch_final_update<T>(const DevMesh&, const ModelOpt&, const StageIO<T>&, const double*,         \
+                                       Partials, int, cudaStream_t);
 
 }  // namespace tmc

@@ -587,6 +587,7 @@ bool prepare_mesh(const tmc_mesh_desc& d, const tmc_params& p, const PrepOptions
   hm.nEdgesOnCell.assign(nc, 0);
   hm.edgesOnCell.assign((size_t)meD * nc, 0);
   hm.nSignEdge.assign((size_t)meD * nc, 0);
+  hm.cellsOnCell.assign((size_t)meD * nc, 0);
   hm.areaCell.assign(nc, 0.0);
   for (int cn = 0; cn < nc; ++cn) {
     int co = hm.cell_n2o[cn];
@@ -597,6 +598,12 @@ bool prepare_mesh(const tmc_mesh_desc& d, const tmc_params& p, const PrepOptions
       int e = (i < n) ? d.edgesOnCell[(size_t)co * me + i] - 1 : -1;
       hm.edgesOnCell[(size_t)i * nc + cn] = (e >= 0) ? eo2n[e] : 0;
       hm.nSignEdge[(size_t)i * nc + cn] = (i < n) ? nsign[(size_t)co * me + i] : 0;
+      int other = 0;
+      if (e >= 0) {
+        const int a = d.cellsOnEdge[(size_t)e * 2] - 1, b = d.cellsOnEdge[(size_t)e * 2 + 1] - 1;
+        other = co2n[(a == co) ? b : a];
+      }
+      hm.cellsOnCell[(size_t)i * nc + cn] = other;
     }
   }
   hm.cellsOnEdge.assign((size_t)2 * ne, 0);

@@ -35,6 +35,7 @@ struct HostMesh {
   // cells (new numbering, slot-major [slot][nc])
   std::vector<uint8_t> nEdgesOnCell;
   std::vector<int32_t> edgesOnCell;
+  std::vector<int32_t> cellsOnCell;  // the other cell of edgesOnCell(i), derived from cellsOnEdge
   std::vector<int8_t> nSignEdge;
   std::vector<double> areaCell;
   // edges
