@@ -833,9 +833,156 @@ void launch_edge_prep(const DevMesh& M, const ModelOpt& O, const StageIO<T>& S, 
                       cudaStream_t st) {
   k_edge_prep<T><<<grid_for(M.ne, bs), bs, 0, st>>>(M, O, S, P, diag ? 1 : 0);
 }
+// FP32 cell pass of the CRK4 stages (modes 1-4) with NTR second-order
+// tracers: every load is issued before the first store, in two waves
+// (indices and the cell's own values, then the gathers of the edges' u, F,
+// dvEdge, areaEdge and of the neighbours' tracer mixing ratios), so one cell
+// costs two memory round trips.  Same arithmetic as the FP32 branch of k_cell.
+template <int NTR>
+__global__ void __launch_bounds__(kMaxBlock) k_cell_fast(DevMesh M, StageIO<float> S, RKStage rk, Partials P,
+                                                         int diag) {
+  constexpr int NQ = NTR > 0 ? NTR : 1;
+  float rip = 0.f, r44 = 0.f;
+  double mass = 0.0, enc = 0.0;
+  const int mode = rk.mode;
+  TMC_FOR_EPT(c, M.nc) {
+    int ei[kME], ci[kME];
+    float ns[kME];
+#pragma unroll
+    for (int i = 0; i < kME; ++i) {
+      ei[i] = M.edgesOnCell[(size_t)i * M.nc + c];
+      ns[i] = (float)M.nSign[(size_t)i * M.nc + c];
+      ci[i] = NTR > 0 ? M.cellsOnCell[(size_t)i * M.nc + c] : 0;
+    }
+    const double gold = (mode <= 3) ? S.gd_old[c] : 0.0;
+    const double gacc = (mode >= 2) ? S.gd_acc[c] : 0.0;
+    const float tprev = (mode >= 2) ? S.tendf[c] : 0.f;
+    const float gdf = S.gdf_in[c], ghf = S.ghsf[c];
+    const double invA = M.invAreaCell[c];
+    const float invAf = M.invAreaCell_f[c];
+    const float Af = (mode >= 2) ? M.areaCell_f[c] : 0.f;
+    float qs[NQ], qo[NQ], qa[NQ];
+#pragma unroll
+    for (int j = 0; j < NTR; ++j) {
+      const size_t qi = (size_t)j * M.nc + c;
+      qs[j] = S.qr_in[qi];
+      qo[j] = (mode <= 3) ? S.q_old[qi] : 0.f;
+      qa[j] = (mode >= 2) ? S.q_acc[qi] : 0.f;
+    }
+    double gdin = 0.0, ghsd = 0.0, Ad = 0.0;
+    if (diag) {
+      gdin = S.gd_in[c];
+      ghsd = S.ghs[c];
+      Ad = M.areaCell[c];
+    }
+    float uu[kME], Fv[kME], dv[kME], ae[kME], qn[NQ][kME];
+#pragma unroll
+    for (int i = 0; i < kME; ++i) {
+      uu[i] = S.u[ei[i]];
+      Fv[i] = S.F[ei[i]];
+      dv[i] = M.dvEdge_f[ei[i]];
+      ae[i] = M.areaEdge_f[ei[i]];
+    }
+#pragma unroll
+    for (int j = 0; j < NTR; ++j)
+#pragma unroll
+      for (int i = 0; i < kME; ++i) qn[j][i] = S.qr_in[(size_t)j * M.nc + ci[i]];
+    // divergence of the mass flux (two-sum), kinetic energy, E
+    float hi = 0.f, lo = 0.f, k = 0.f;
+#pragma unroll
+    for (int i = 0; i < kME; ++i) {
+      two_sum_acc(hi, lo, __fmul_rn(__fmul_rn(ns[i], Fv[i]), dv[i]));
+      k += fabsf(ns[i]) * uu[i] * uu[i] * ae[i];
+    }
+    const double t = -((double)hi + (double)lo) * invA;
+    const float tT = (float)t;
+    S.E[c] = k * 0.25f * invAf + gdf + ghf;
+    float tq[NQ];
+#pragma unroll
+    for (int j = 0; j < NTR; ++j) {
+      float sq = 0.f;
+#pragma unroll
+      for (int i = 0; i < kME; ++i) sq += ns[i] * Fv[i] * (0.5f * (qs[j] + qn[j][i])) * dv[i];
+      tq[j] = -sq * invAf;
+    }
+    double gnext = 0.0;
+    switch (mode) {
+      case 1:
+        S.gd_acc[c] = t;
+        S.tendf[c] = tT;
+        gnext = gold + rk.a_dt * t;
+        break;
+      case 2:
+      case 3:
+        rip += tprev * tT * Af;
+        S.gd_acc[c] = gacc + 2.0 * t;
+        S.tendf[c] = tT;
+        gnext = gold + rk.a_dt * t;
+        break;
+      default: {
+        rip += tprev * tT * Af;
+        const double tn = (gacc + t) * (1.0 / 6.0);
+        S.gd_acc[c] = tn;
+        const float tnf = (float)tn;
+        r44 += tnf * tnf * Af;
+        S.tendf[c] = tT;
+      }
+    }
+    const float gnf = (float)gnext;
+    if (mode <= 3) {
+      S.gd_next[c] = gnext;
+      S.gdf_next[c] = gnf;
+    }
+    const float adt = (float)rk.a_dt;
+#pragma unroll
+    for (int j = 0; j < NTR; ++j) {
+      const size_t qi = (size_t)j * M.nc + c;
+      if (mode == 1) {
+        S.q_acc[qi] = tq[j];
+      } else if (mode <= 3) {
+        S.q_acc[qi] = qa[j] + 2.f * tq[j];
+      } else {
+        S.q_acc[qi] = (qa[j] + tq[j]) * (1.0f / 6.0f);
+      }
+      if (mode <= 3) {
+        const float qnext = qo[j] + adt * tq[j];
+        S.q_next[qi] = qnext;
+        S.qr_next[qi] = qnext / gnf;
+      }
+    }
+    if (diag) {
+      mass = mass + gdin * Ad;
+      enc = enc + (gdin * gdin + 2.0 * gdin * ghsd) * Ad;
+    }
+  }
+  if (mode >= 2) {
+    const float v[2] = {rip, r44};
+    const int r[2] = {R_IP_C + 2 * (mode - 2), R_44_C};
+    block_store<float, 2>(v, P, r);
+  }
+  if (diag) {
+    const double v[2] = {mass, enc};
+    const int r[2] = {R_MASS, R_EN_C};
+    block_store<double, 2>(v, P, r);
+  }
+}
+
 template <class T>
 void launch_cell(const DevMesh& M, const ModelOpt& O, const StageIO<T>& S, RKStage rk, Partials P, bool diag, int bs,
                  cudaStream_t st) {
+  if constexpr (!kF64<T>) {
+    const bool fast = rk.mode >= 1 && rk.mode <= 4 && (O.n_tracers == 0 || O.tr_order == 2);
+    if (fast) {
+      const int g = grid_for(M.nc, bs), dg = diag ? 1 : 0;
+      switch (O.n_tracers) {
+        case 0: k_cell_fast<0><<<g, bs, 0, st>>>(M, S, rk, P, dg); return;
+        case 1: k_cell_fast<1><<<g, bs, 0, st>>>(M, S, rk, P, dg); return;
+        case 2: k_cell_fast<2><<<g, bs, 0, st>>>(M, S, rk, P, dg); return;
+        case 4: k_cell_fast<4><<<g, bs, 0, st>>>(M, S, rk, P, dg); return;
+        default: break;
+      }
+    }
+  }
   k_cell<T><<<grid_for(M.nc, bs), bs, 0, st>>>(M, O, S, rk, P, diag ? 1 : 0);
 }
 template <class T>
