@@ -164,6 +164,10 @@ def flux_kernel_bytes(nc: int, ne: int, S: int, mode: int | None = None) -> floa
     tot = 0.0
     for md in modes:
         tot += ne * (40 + 10 * Mw + 8 + Mw + 4 * S + rk[md]) + nc * (S + S)
+        if md <= 3:
+            # fused preparation of the next stage: next gd gathered, gd_edge/u/F
+            # written instead of the next stage's iap_u
+            tot += nc * S + ne * 2 * S
     return tot / len(modes)
 
 
@@ -195,8 +199,6 @@ def step_bytes(nc: int, ne: int, nv: int, S: int, ntr: int, diag: bool = True) -
         # edge_flux; stages 1-3 prepare the next stage instead of storing iap_u:
         # next gd gathered, gd_edge/u/F written
         tot += flux_kernel_bytes(nc, ne, S, k)
-        if k <= 3:
-            tot += nc * S + ne * (3 * S - S)
     # final cells: gd r+w, acc r, shadow w; tracers r+w, acc r, shadow w
     tot += nc * (24 + sh + ntr * (3 * S + sh))
     # final edges: iap_u r+w, acc r, cellsOnEdge, gd gathered, gd_edge/u/F written, areaEdge (energy)
