@@ -51,15 +51,16 @@ typedef struct tmc_mesh_desc {
   const double *dvEdge, *dcEdge, *areaCell, *areaTriangle;
   const double *kiteAreasOnVertex; /* (vertexDegree, nVertices) */
   const double *weightsOnEdge;     /* (maxEdges2, nEdges) */
+  const double *lonCell, *lonVertex; /* radians; lonVertex is required by the adv model only */
 } tmc_mesh_desc;
 
 /* namelist &tmcore (src/core/params_mod.F90:35-55), const_mod constants,
  * plus device options. */
 typedef struct tmc_params {
   double dt;
-  int32_t time_scheme;            /* 2 = CRK4 (time_scheme_mod.F90:109-154) */
-  int32_t pv_scheme;              /* 1 APVM, 3 high-order upwind */
-  int32_t conserve_energy;        /* CRK4 beta (time_scheme_mod.F90:144-150) */
+  int32_t time_scheme;            /* 1 CRK3, 2 CRK4, 3 PC2 (time_scheme_mod.F90:47-184) */
+  int32_t pv_scheme;              /* 1 APVM, 2 conservative APVM, 3 high-order upwind */
+  int32_t conserve_energy;        /* energy-conserving beta (time_scheme_mod.F90:94-100,144-150,174-180) */
   int32_t flux_4th_order_correct; /* must be 0 on the device */
   double apvm_weight;
   int32_t adv_order;              /* 2..6, upwind correction of gd on edges */
@@ -76,7 +77,9 @@ typedef struct tmc_params {
   int32_t device;                 /* CUDA device ordinal */
   int32_t block_size;             /* threads per block, 0 = tuned default */
   int32_t stencils;               /* 1: always build the poly-fit stencil tables (else only when used) */
-  int32_t reserved[6];
+  int32_t adv_wind;               /* 0: shallow-water model; adv model (tmcore_adv_mod.F90) with the
+                                     prescribed wind 1 cosine-bell rotation, 2 deformation flow case 4 */
+  int32_t reserved[5];
 } tmc_params;
 
 typedef struct tmc_handle tmc_handle;
@@ -124,6 +127,17 @@ int tmc_time_integrate(tmc_handle* h, const double* gd_old, const double* iap_u_
 /* One call of spatial_operators (tmcore_swm_mod.F90:92-125). */
 int tmc_spatial_operators(tmc_handle* h, const double* gd, const double* iap_u, double* tend_gd,
                           double* tend_iap_u);
+
+/* The adv model (tmcore_adv_mod.F90, adv_wind = 1 or 2, FP64): one
+ * advected scalar in place of gd, transported by the prescribed wind that
+ * update_state re-sets at elapsed + the stage's dt (tmcore_adv_mod.F90:87-97);
+ * tmc_step runs time_integrate with the adv spatial operator
+ * (adv_scheme_sg11_mod.F90:33-48) and time_advance; tmc_get_diag gives the
+ * total mass in out[0] (others 0).  tmc_adv_set_initial sets the scalar and
+ * the wind at elapsed = 0 (test_cases_mod.F90:18-55). */
+int tmc_adv_set_initial(tmc_handle* h, const double* q);
+int tmc_adv_get(tmc_handle* h, double* q, double* u);
+int tmc_adv_elapsed(tmc_handle* h, double* seconds);
 
 /* Single operators of operators_mod.F90 (fine-grained parity, host arrays). */
 int tmc_op_div(tmc_handle* h, const double* f_edge, double* div_cell);                 /* :40-55 */

@@ -960,6 +960,8 @@ static void crk4(orc_model* m, spatial_fn so, update_fn up) {
 static void crk3(orc_model* m, spatial_fn so, update_fn up) {
   const int one = -1, two = -2, three = -3, old = m->old, new_ = m->new_;
   const double dt = m->p.dt;
+  /* :78-79 copy gd and iap_u only: state(one)%edge%u is never set, so the adv
+   * model's first CRK3 stage sees that array's initial content (zero here) */
   memcpy(ST(one)->c_gd, ST(old)->c_gd, sizeof(double) * m->nc);
   memcpy(ST(one)->e_iap_u, ST(old)->e_iap_u, sizeof(double) * m->ne);
   memcpy(ST(one)->qgd, ST(old)->qgd, sizeof(double) * m->nc * (size_t)m->p.n_tracers);

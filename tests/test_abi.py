@@ -23,8 +23,8 @@ def test_library_exports_header_symbols():
 def test_struct_layout_matches_header():
     from tmcore_gb300 import abi
 
-    # 6 int32 dims + 27 pointers; params: fixed layout checked by size
-    assert ctypes.sizeof(abi.MeshDesc) == 6 * 4 + 27 * ctypes.sizeof(ctypes.c_void_p)
+    # 6 int32 dims + 29 pointers; params: fixed layout checked by size
+    assert ctypes.sizeof(abi.MeshDesc) == 6 * 4 + 29 * ctypes.sizeof(ctypes.c_void_p)
     # dt, 4 int32, apvm_weight, 3 int32 + 4 bytes padding, radius/g/omega, 16 int32
     assert ctypes.sizeof(abi.Params) == 8 + 16 + 8 + 12 + 4 + 24 + 64
 

@@ -68,6 +68,27 @@ def test_conservation(pv_scheme, adv_order):
     assert 0.9 < d1[4] < 1.1  # beta near 1
 
 
+@pytest.mark.parametrize("time_scheme", [1, 3])
+@pytest.mark.parametrize("pv_scheme", [1, 2])
+def test_conservation_crk3_pc2(time_scheme, pv_scheme):
+    """CRK3 and PC2 with their energy-conserving beta (time_scheme_mod.F90:94-100,
+    :174-180) and the conservative APVM keep mass, energy and absolute vorticity."""
+    from tmcore_gb300 import cases
+
+    m = icos(3)
+    gd, u, ghs = cases.jet_bumps(m, seed=12)
+    o = make(m, dt=900.0, time_scheme=time_scheme, pv_scheme=pv_scheme, apvm_weight=0.0)
+    o.set_initial(gd, u, ghs)
+    d0 = o.diag()
+    o.step(12)
+    d1 = o.diag()
+    assert abs(d1[0] - d0[0]) / d0[0] < 1e-13
+    assert abs(d1[1] - d0[1]) / d0[1] < 1e-13
+    _, vor = o.vertex()
+    assert abs(d1[3] - d0[3]) < 1e-12 * np.max(np.abs(vor))
+    assert 0.9 < d1[4] < 1.1
+
+
 def test_energy_not_conserved_without_beta():
     from tmcore_gb300 import cases
 

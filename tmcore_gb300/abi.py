@@ -31,7 +31,7 @@ class MeshDesc(ctypes.Structure):
                                   "xCell", "yCell", "zCell", "latCell", "xEdge", "yEdge", "zEdge",
                                   "xVertex", "yVertex", "zVertex", "latVertex",
                                   "dvEdge", "dcEdge", "areaCell", "areaTriangle", "kiteAreasOnVertex",
-                                  "weightsOnEdge")]
+                                  "weightsOnEdge", "lonCell", "lonVertex")]
 
 
 class Params(ctypes.Structure):
@@ -43,7 +43,7 @@ class Params(ctypes.Structure):
                 ("omega", ctypes.c_double), ("n_tracers", i32), ("tracer_adv_order", i32),
                 ("tracer_adv_mono", i32), ("precision", i32), ("renumber", i32), ("use_graph", i32),
                 ("diag_every", i32), ("device", i32), ("block_size", i32), ("stencils", i32),
-                ("reserved", i32 * 6)]
+                ("adv_wind", i32), ("reserved", i32 * 5)]
 
 
 # name -> (restype, argtypes)
@@ -75,6 +75,9 @@ SYMBOLS = {
     "tmc_op_upwind_correction": (ctypes.c_int, [vp, vp, vp, vp, i32, i32]),
     "tmc_time_steps": (ctypes.c_int, [vp, i32, dp, dp, ctypes.POINTER(i32), ctypes.POINTER(i32)]),
     "tmc_sizes": (ctypes.c_int, [vp, i64p, i64p, i64p, i64p]),
+    "tmc_adv_set_initial": (ctypes.c_int, [vp, vp]),
+    "tmc_adv_get": (ctypes.c_int, [vp, vp, vp]),
+    "tmc_adv_elapsed": (ctypes.c_int, [vp, dp]),
     "tmc_mass_energy_noalloc": (ctypes.c_int, [vp, vp, vp, ctypes.c_int64, vp, vp, ctypes.c_int64, vp, vp]),
 }
 TMC_NOALLOC_MAX_ELEMENTS = 8388608

@@ -42,6 +42,8 @@ struct EngineBase {
   virtual void get_tracers_dev(double* raw_q) = 0;
   virtual void set_ghs_dev(const double* raw) = 0;
   virtual int launches_per_step() const = 0;
+  virtual void adv_set_initial_dev(const double* raw_q) = 0;  // adv model: gd <- q, wind at t = 0
+  virtual void adv_get_dev(double* raw_q, double* raw_u) = 0;
 };
 
 enum Field { F_GD = 0, F_IAP, F_U, F_PV_V, F_VOR, F_TEND_GD, F_TEND_IAP, F_GD_STAGE };
@@ -71,6 +73,12 @@ struct tmc_handle {
   cudaGraphExec_t g_step = nullptr, g_step_diag = nullptr;
   long step_count = 0;
   double cell_coef4 = 0.25, vert_coef4 = 0.25;  // SAVE'd coef4 of the upwind routines
+  // generic integrator program: CRK3, PC2, or the adv model (any scheme)
+  bool generic = false;
+  bool adv = false;
+  int gen_counts[R_COUNT] = {};  // partial counts of the generic step's finaliser
+  const double* d_latV = nullptr;
+  const double* d_lonV = nullptr;
   std::vector<cudaEvent_t> ev_pool;
 
   template <class X>
@@ -121,6 +129,15 @@ struct Engine : EngineBase {
   T* q_acc = nullptr;
   T *iap_acc = nullptr, *iap_tend = nullptr, *E = nullptr;
   T *pv_v = nullptr, *vor = nullptr, *gd_v = nullptr, *pv_c = nullptr, *v_e = nullptr, *pv_e = nullptr;
+  T *dpv = nullptr, *pvf = nullptr, *dpvf = nullptr;  // conservative APVM
+  // generic integrators: tendency slots (gd FP64; iap_u and tracer mass in T)
+  double* tgd[4] = {};
+  T* tiap[4] = {};
+  T* tq[4] = {};
+  double* psi = nullptr;  // adv model: stream function on vertices
+  // adv model, CRK3: the wind of state(one), which time_integrate_CRK3 never
+  // sets (it copies gd and iap_u only, time_scheme_mod.F90:78-79): zero
+  T* u_one = nullptr;
   explicit Engine(tmc_handle* hh) : h(hh) {}
 
   int alloc() override {
@@ -157,6 +174,27 @@ struct Engine : EngineBase {
       }
     }
     if (!pv_e || !F[1] || !Fq[1]) return TMC_E_CUDA;
+    if (h->O.pv_scheme == 2) {
+      dpv = h->dalloc<T>(ne);
+      pvf = h->dalloc<T>(ne);
+      dpvf = h->dalloc<T>(ne);
+      if (!dpvf) return TMC_E_CUDA;
+    }
+    if (h->generic) {
+      const int ns = h->p.time_scheme == 1 ? 3 : (h->p.time_scheme == 3 ? 2 : 4);
+      for (int i = 0; i < ns; ++i) {
+        tgd[i] = h->dalloc<double>(nc);
+        tiap[i] = h->adv ? nullptr : h->dalloc<T>(ne);
+        tq[i] = h->dalloc<T>((size_t)nc * (nt > 0 ? nt : 1));
+        if (!tgd[i] || !tq[i] || (!h->adv && !tiap[i])) return TMC_E_CUDA;
+      }
+    }
+    if (h->adv) {
+      psi = h->dalloc<double>(nv);
+      u_one = h->dalloc<T>(ne);
+      if (!psi || !u_one) return TMC_E_CUDA;
+      cudaMemset(u_one, 0, sizeof(T) * ne);
+    }
     cudaMemset(ghs, 0, sizeof(double) * nc);
     if (!std::is_same<T, double>::value) {
       tendf = h->dalloc<float>(nc);
@@ -207,6 +245,9 @@ struct Engine : EngineBase {
     s.v_e = v_e;
     s.pv_e = pv_e;
     s.ghs = ghs;
+    s.dpv = dpv;
+    s.pvf = pvf;
+    s.dpvf = dpvf;
     s.gdf_in = gdf[in_slot[k]];
     s.gdf_next = next_slot[k] >= 0 ? gdf[next_slot[k]] : nullptr;
     s.qr_in = qr[in_slot[k]];
@@ -216,9 +257,20 @@ struct Engine : EngineBase {
     return s;
   }
 
+  int launches_per_stage_passes() const {
+    const bool v2c = (h->O.pv_scheme == 1 && h->O.apvm_weight != 0.0) || h->O.pv_scheme == 2;
+    return 4 + (v2c ? 1 : 0) + (h->O.pv_scheme == 2 ? 4 : 0);
+  }
   int launches_per_step() const override {
-    int per_stage = 4 + ((h->O.pv_scheme == 1 && h->O.apvm_weight != 0.0) ? 1 : 0);
-    return 4 * per_stage + 3;
+    if (!h->generic) return 4 * launches_per_stage_passes() + 3;
+    // generic: spatial passes per evaluation (+ the edge preparation), state
+    // updates (adv: + 2 wind kernels each), combination, finaliser, final update
+    const int ts = h->p.time_scheme;
+    const int evals = ts == 1 ? 3 : (ts == 3 ? 3 : 4);
+    const int updates = ts == 1 ? 4 : (ts == 3 ? 3 : 4);
+    const int per_eval = h->adv ? 2 : 1 + launches_per_stage_passes();
+    const int per_update = h->adv ? 3 : 1;
+    return evals * per_eval + updates * per_update + 2 + (h->adv ? 1 : 0);
   }
 
   // Edge preparation of state(old) into set 0 (+ the energy partials); needed
@@ -232,6 +284,10 @@ struct Engine : EngineBase {
   // one CRK4 step (time_scheme_mod.F90:109-154); state(old) updated in place.
   // Requires set 0 prepared from state(old) (launch_prep or the previous step).
   void launch_step(bool diag, std::vector<cudaEvent_t>* flux_ev, size_t* ev_pos) override {
+    if (h->generic) {
+      launch_generic_step(diag);
+      return;
+    }
     const DevMesh& M = h->M;
     const ModelOpt& O = h->O;
     const double dt = O.dt;
@@ -245,6 +301,7 @@ struct Engine : EngineBase {
       launch_cell<T>(M, O, s, rk, h->P, dg, h->bs, h->st);
       launch_vertex<T>(M, O, s, h->P, dg, h->bs, h->st);
       launch_edge_pv<T>(M, O, s, h->bs, h->st);
+      if (O.pv_scheme == 2) launch_cons_apvm<T>(M, O, s, h->P, h->d_diag, h->bs, h->st);
       if (flux_ev) cudaEventRecord((*flux_ev)[(*ev_pos)++], h->st);
       launch_edge_flux<T>(M, O, s, rk, h->P, h->bs, h->st);
       if (flux_ev) cudaEventRecord((*flux_ev)[(*ev_pos)++], h->st);
@@ -254,8 +311,138 @@ struct Engine : EngineBase {
     launch_final_update<T>(M, O, io(0), h->d_diag, h->P, h->bs, h->st);
   }
 
+  // ---- generic integrator program (time_scheme_mod.F90:65-107 CRK3,
+  // :109-154 CRK4, :156-184 PC2; the adv model's spatial_operators and
+  // update_state, tmcore_adv_mod.F90:78-97).  State slots: old = 0 (also the
+  // stage state "one", which the schemes only read), scratch 1 and 2.
+
+  // spatial_operators of state slot xs into tendency slot ts (unfused passes,
+  // edge set 0); the adv model takes the wind of slot xs unless `wind` is given
+  void gen_spatial(int xs, int ts, const T* wind = nullptr) {
+    const DevMesh& M = h->M;
+    const ModelOpt& O = h->O;
+    if constexpr (std::is_same<T, double>::value) {
+      if (h->adv) {
+        launch_adv_spatial(M, O, gd[xs], wind ? wind : iap[xs], gd_e[0], F[0], tgd[ts], h->bs, h->st);
+        return;
+      }
+    }
+    StageIO<T> s = io(0);
+    s.gd_in = gd[xs];
+    s.iap_in = iap[xs];
+    s.q_in = q[xs];
+    s.gdf_in = gdf[xs];
+    s.qr_in = qr[xs];
+    s.gd_tend = tgd[ts];
+    s.iap_tend = tiap[ts];
+    s.q_acc = tq[ts];  // mode 0 writes the tracer tendency here
+    s.vor = nullptr;
+    s.gd_v = nullptr;
+    RKStage rk{0, 0.0};
+    launch_edge_prep<T>(M, O, s, h->P, false, h->bs, h->st);
+    launch_cell<T>(M, O, s, rk, h->P, false, h->bs, h->st);
+    launch_vertex<T>(M, O, s, h->P, false, h->bs, h->st);
+    launch_edge_pv<T>(M, O, s, h->bs, h->st);
+    if (O.pv_scheme == 2) launch_cons_apvm<T>(M, O, s, h->P, h->d_diag, h->bs, h->st);
+    launch_edge_flux<T>(M, O, s, rk, h->P, h->bs, h->st);
+  }
+
+  // update_state: slot `to` = slot `from` + coef * tendency slot ts, coef the
+  // host value a_dt or *coef_dev; the adv model then re-sets the wind of the
+  // new state at elapsed + coef (tmcore_adv_mod.F90:87-97)
+  void gen_update(int ts, int from, int to, double a_dt, const double* coef_dev) {
+    UpdateArgs<T> a{};
+    a.gd_o = gd[from];
+    a.gd_n = gd[to];
+    a.tgd = tgd[ts];
+    if (!h->adv) {
+      a.iap_o = iap[from];
+      a.iap_n = iap[to];
+      a.tiap = tiap[ts];
+    }
+    a.q_o = q[from];
+    a.q_n = q[to];
+    a.tq = tq[ts];
+    a.gdf_n = gdf[to];
+    a.qr_n = qr[to];
+    a.a_dt = a_dt;
+    a.coef_dev = coef_dev;
+    launch_update<T>(h->M, h->O.n_tracers, a, h->bs, h->st);
+    if constexpr (std::is_same<T, double>::value) {
+      if (h->adv)
+        launch_adv_wind(h->M, h->p.adv_wind, h->p.radius, h->d_latV, h->d_lonV, h->d_diag + 11, a_dt, coef_dev, psi,
+                        iap[to], h->st);
+    }
+  }
+
+  void launch_generic_step(bool diag) {
+    const double dt = h->O.dt;
+    const int ts = h->p.time_scheme;
+    if (diag) {
+      // invariants of state(old), reduced together with beta below
+      if (h->adv)
+        launch_mass_only(h->M, gd[0], h->P, h->bs, h->st);
+      else
+        launch_diag_pass(false);
+    }
+    CombineArgs<T> c{};
+    if (ts == 2) {  // CRK4: two -> 1, three -> 2, four -> 1
+      gen_spatial(0, 0);
+      gen_update(0, 0, 1, 0.5 * dt, nullptr);
+      gen_spatial(1, 1);
+      gen_update(1, 0, 2, 0.5 * dt, nullptr);
+      gen_spatial(2, 2);
+      gen_update(2, 0, 1, dt, nullptr);
+      gen_spatial(1, 3);
+    } else if (ts == 1) {  // CRK3: two -> 1, three -> 2
+      gen_spatial(0, 0, u_one);
+      gen_update(0, 0, 1, 0.5 * dt, nullptr);
+      gen_spatial(1, 1);
+      gen_update(0, 0, 2, -dt, nullptr);
+      gen_update(1, 2, 2, 2.0 * dt, nullptr);
+      gen_spatial(2, 2);
+    } else {  // PC2: new -> 1; tend(old) -> 0, tend(new) -> 1
+      gen_spatial(0, 0);
+      gen_update(0, 0, 1, 0.5 * dt, nullptr);
+      gen_spatial(1, 0);
+      gen_update(0, 0, 1, 0.5 * dt, nullptr);
+      gen_spatial(1, 1);
+    }
+    for (int k = 0; k < 4; ++k) {
+      c.tgd[k] = tgd[k];
+      c.tiap[k] = tiap[k];
+      c.tq[k] = tq[k];
+    }
+    launch_combine<T>(h->M, h->O.n_tracers, ts, c, h->P, h->bs, h->st);
+    launch_finalize(h->P, h->gen_counts, h->hm.totalArea, h->hm.sumAreaTriangle, dt, true, diag,
+                    h->p.conserve_energy != 0, h->d_diag, h->st, ts);
+    // new = old + beta dt t_new, in place (t_new: slot 0, PC2 slot 1)
+    gen_update(ts == 3 ? 1 : 0, 0, 0, 0.0, h->d_diag + 9);
+    if (h->adv) launch_adv_advance(h->d_diag + 11, dt, h->st);
+  }
+
+  void adv_set_initial_dev(const double* raw_q) override {
+    if constexpr (std::is_same<T, double>::value) {
+      launch_gather<double>(h->M.nc, raw_q, h->d_cell_n2o, gd[0], h->st);
+      cudaMemsetAsync(h->d_diag + 11, 0, sizeof(double), h->st);
+      launch_adv_wind(h->M, h->p.adv_wind, h->p.radius, h->d_latV, h->d_lonV, h->d_diag + 11, 0.0, nullptr, psi,
+                      iap[0], h->st);
+    }
+  }
+  void adv_get_dev(double* raw_q, double* raw_u) override {
+    if (raw_q) launch_scatter<double>(h->M.nc, gd[0], h->d_cell_n2o, raw_q, h->st);
+    if (raw_u) launch_scatter<T>(h->M.ne, iap[0], h->d_edge_n2o, raw_u, h->st);
+  }
+
   // diagnostics of state(old): gd_edge, u, gd/pv/vor on vertices, invariants
   void launch_diag_pass(bool finalize) override {
+    if (h->adv) {
+      launch_mass_only(h->M, gd[0], h->P, h->bs, h->st);
+      if (finalize)
+        launch_finalize(h->P, h->gen_counts, h->hm.totalArea, h->hm.sumAreaTriangle, h->O.dt, false, true, false,
+                        h->d_diag, h->st);
+      return;
+    }
     StageIO<T> s = io(0);
     RKStage rk{0, 0.0};
     launch_edge_prep<T>(h->M, h->O, s, h->P, true, h->bs, h->st);
@@ -279,6 +466,7 @@ struct Engine : EngineBase {
     launch_cell<T>(h->M, h->O, s, rk, h->P, false, h->bs, h->st);
     launch_vertex<T>(h->M, h->O, s, h->P, false, h->bs, h->st);
     launch_edge_pv<T>(h->M, h->O, s, h->bs, h->st);
+    if (h->O.pv_scheme == 2) launch_cons_apvm<T>(h->M, h->O, s, h->P, h->d_diag, h->bs, h->st);
     launch_edge_flux<T>(h->M, h->O, s, rk, h->P, h->bs, h->st);
   }
 
@@ -348,6 +536,7 @@ int build_graph(tmc_handle* h, bool diag, cudaGraphExec_t* out) {
 }
 
 void ensure_prep(tmc_handle* h) {
+  if (h->generic) return;  // the generic program prepares every evaluation itself
   if (!h->prep_valid) {
     h->eng->launch_prep();
     h->prep_valid = true;
@@ -426,16 +615,20 @@ int tmc_create(const tmc_mesh_desc* mesh, const tmc_params* params, tmc_handle**
     *out = h.release();
     return TMC_E_ARG;
   };
-  if (p.time_scheme != 2) {
-    h->err = "only time_scheme = 2 (CRK4) runs on the device";
-    *out = h.release();
-    return TMC_E_UNSUP;
+  if (p.time_scheme < 1 || p.time_scheme > 3) return bad("time_scheme must be 1 (CRK3), 2 (CRK4) or 3 (PC2)");
+  if (p.pv_scheme < 1 || p.pv_scheme > 3) return bad("pv_scheme must be 1 (APVM), 2 (conservative APVM) or 3 (upwind)");
+  if (p.adv_wind < 0 || p.adv_wind > 2) return bad("adv_wind must be 0 (shallow water), 1 or 2 (adv model)");
+  if (p.adv_wind != 0) {
+    if (p.precision != TMC_FP64) {
+      h->err = "the adv model runs in FP64 only";
+      *out = h.release();
+      return TMC_E_UNSUP;
+    }
+    if (!mesh || !mesh->lonVertex) return bad("the adv model needs lonVertex in tmc_mesh_desc");
+    if (p.n_tracers != 0) return bad("the adv model advects gd only (n_tracers must be 0)");
   }
-  if (p.pv_scheme != 1 && p.pv_scheme != 3) {
-    h->err = "pv_scheme must be 1 (APVM) or 3 (high-order upwind) on the device";
-    *out = h.release();
-    return TMC_E_UNSUP;
-  }
+  h->adv = p.adv_wind != 0;
+  h->generic = h->adv || p.time_scheme != 2;
   if (p.flux_4th_order_correct) {
     h->err = "flux_4th_order_correct is not supported on the device";
     *out = h.release();
@@ -510,6 +703,10 @@ int tmc_create(const tmc_mesh_desc* mesh, const tmc_params* params, tmc_handle**
   M.v2c_start = h->upload(hm.v2c_start);
   M.v2c_vertex = h->upload(hm.v2c_vertex);
   M.v2c_kite = h->upload(hm.v2c_kite);
+  if (h->adv) {
+    h->d_latV = h->upload(hm.latVertex);
+    h->d_lonV = h->upload(hm.lonVertex);
+  }
   if (p.precision == TMC_FP32) {
     auto f32 = [](const std::vector<double>& v) { return std::vector<float>(v.begin(), v.end()); };
     auto inv32 = [](const std::vector<double>& v) {
@@ -574,6 +771,10 @@ int tmc_create(const tmc_mesh_desc* mesh, const tmc_params* params, tmc_handle**
   for (int r : rc_edges) h->counts[r] = be;
   h->counts[R_PE] = bv;
   h->counts[R_AV] = bv;
+  for (int r = R_C1; r <= R_C3; ++r) h->counts[r] = bv;
+  for (int r = 0; r < R_COUNT; ++r) h->gen_counts[r] = h->counts[r];
+  if (h->adv)  // the invariant pass of the adv model is the mass alone, over cells
+    for (int r = R_MASS; r <= R_AV; ++r) h->gen_counts[r] = bc;
   h->d_diag = h->dalloc<double>(kDiagLen + R_COUNT + 2);  // outputs, region sums, finaliser counter
   if (cudaMallocHost(&h->h_diag, sizeof(double) * kDiagLen) != cudaSuccess) h->h_diag = nullptr;
   if (!h->d_diag || !h->h_diag || !h->P.base) {
@@ -618,9 +819,13 @@ const char* tmc_last_error(const tmc_handle* h) { return h ? h->err.c_str() : "n
 
 #define TMC_REQUIRE_HANDLE(h) \
   if (!(h) || !(h)->eng) return TMC_E_ARG;
+// entry points of the shallow-water model only
+#define TMC_REQUIRE_SWM(h)   \
+  TMC_REQUIRE_HANDLE(h);     \
+  if ((h)->adv) return (h)->fail(TMC_E_UNSUP, "not available in the adv model (adv_wind != 0)");
 
 int tmc_set_initial(tmc_handle* h, const double* gd, const double* u, const double* ghs) {
-  TMC_REQUIRE_HANDLE(h);
+  TMC_REQUIRE_SWM(h);
   if (!gd || !u || !ghs) return h->fail(TMC_E_ARG, "tmc_set_initial: NULL array");
   const int nc = h->M.nc, ne = h->M.ne;
   int rc;
@@ -645,7 +850,7 @@ int tmc_set_initial(tmc_handle* h, const double* gd, const double* u, const doub
 }
 
 int tmc_set_state(tmc_handle* h, const double* gd, const double* iap_u) {
-  TMC_REQUIRE_HANDLE(h);
+  TMC_REQUIRE_SWM(h);
   if (!gd || !iap_u) return h->fail(TMC_E_ARG, "tmc_set_state: NULL array");
   int rc;
   if ((rc = h2d(h, h->raw_c, gd, h->M.nc))) return rc;
@@ -658,7 +863,7 @@ int tmc_set_state(tmc_handle* h, const double* gd, const double* iap_u) {
 }
 
 int tmc_get_state(tmc_handle* h, double* gd, double* iap_u, double* u) {
-  TMC_REQUIRE_HANDLE(h);
+  TMC_REQUIRE_SWM(h);
   if (!h->have_state) return h->fail(TMC_E_STATE, "no state set");
   int rc;
   if (u) h->eng->launch_diag_pass(false);
@@ -681,7 +886,7 @@ int tmc_get_state(tmc_handle* h, double* gd, double* iap_u, double* u) {
 }
 
 int tmc_get_vertex(tmc_handle* h, double* pv, double* vor) {
-  TMC_REQUIRE_HANDLE(h);
+  TMC_REQUIRE_SWM(h);
   if (!h->have_state) return h->fail(TMC_E_STATE, "no state set");
   int rc;
   h->eng->launch_diag_pass(false);
@@ -699,7 +904,7 @@ int tmc_get_vertex(tmc_handle* h, double* pv, double* vor) {
 }
 
 int tmc_set_tracers(tmc_handle* h, const double* qgd) {
-  TMC_REQUIRE_HANDLE(h);
+  TMC_REQUIRE_SWM(h);
   if (h->O.n_tracers == 0) return TMC_OK;
   if (!qgd) return h->fail(TMC_E_ARG, "tmc_set_tracers: NULL array");
   int rc;
@@ -711,7 +916,7 @@ int tmc_set_tracers(tmc_handle* h, const double* qgd) {
 }
 
 int tmc_get_tracers(tmc_handle* h, double* qgd) {
-  TMC_REQUIRE_HANDLE(h);
+  TMC_REQUIRE_SWM(h);
   if (h->O.n_tracers == 0) return TMC_OK;
   if (!qgd) return h->fail(TMC_E_ARG, "tmc_get_tracers: NULL array");
   h->eng->get_tracers_dev(h->raw_q);
@@ -754,7 +959,7 @@ int tmc_get_diag(tmc_handle* h, double out[5]) {
 
 int tmc_time_integrate(tmc_handle* h, const double* gd_old, const double* iap_u_old, const double* qgd_old,
                        double* gd_new, double* iap_u_new, double* qgd_new) {
-  TMC_REQUIRE_HANDLE(h);
+  TMC_REQUIRE_SWM(h);
   if (!gd_old || !iap_u_old || !gd_new || !iap_u_new) return h->fail(TMC_E_ARG, "tmc_time_integrate: NULL array");
   const bool trc = h->O.n_tracers > 0;
   if (trc && (!qgd_old || !qgd_new)) return h->fail(TMC_E_ARG, "tmc_time_integrate: tracers need qgd arrays");
@@ -784,7 +989,7 @@ int tmc_time_integrate(tmc_handle* h, const double* gd_old, const double* iap_u_
 
 int tmc_spatial_operators(tmc_handle* h, const double* gd, const double* iap_u, double* tend_gd,
                           double* tend_iap_u) {
-  TMC_REQUIRE_HANDLE(h);
+  TMC_REQUIRE_SWM(h);
   if (!gd || !iap_u || !tend_gd || !tend_iap_u) return h->fail(TMC_E_ARG, "tmc_spatial_operators: NULL array");
   // uses state slot 1 as scratch; state(old) is untouched
   int rc;
@@ -928,6 +1133,41 @@ int tmc_time_steps(tmc_handle* h, int32_t nsteps, double* ms_total, double* ms_f
   }
   if (total_launches) *total_launches = nsteps * h->eng->launches_per_step();
   return h->cuda_check("tmc_time_steps");
+}
+
+int tmc_adv_set_initial(tmc_handle* h, const double* q) {
+  TMC_REQUIRE_HANDLE(h);
+  if (!h->adv) return h->fail(TMC_E_UNSUP, "tmc_adv_set_initial needs adv_wind = 1 or 2");
+  if (!q) return h->fail(TMC_E_ARG, "tmc_adv_set_initial: NULL array");
+  int rc;
+  if ((rc = h2d(h, h->raw_c, q, h->M.nc))) return rc;
+  h->eng->adv_set_initial_dev(h->raw_c);
+  h->have_state = true;
+  h->step_count = 0;
+  if ((rc = sync(h, "tmc_adv_set_initial"))) return rc;
+  return h->cuda_check("tmc_adv_set_initial");
+}
+
+int tmc_adv_get(tmc_handle* h, double* q, double* u) {
+  TMC_REQUIRE_HANDLE(h);
+  if (!h->adv) return h->fail(TMC_E_UNSUP, "tmc_adv_get needs adv_wind = 1 or 2");
+  if (!h->have_state) return h->fail(TMC_E_STATE, "no state set");
+  h->eng->adv_get_dev(q ? h->raw_c : nullptr, u ? h->raw_e : nullptr);
+  int rc;
+  if (q && (rc = d2h(h, q, h->raw_c, h->M.nc))) return rc;
+  if (u && (rc = d2h(h, u, h->raw_e, h->M.ne))) return rc;
+  if ((rc = sync(h, "tmc_adv_get"))) return rc;
+  return h->cuda_check("tmc_adv_get");
+}
+
+int tmc_adv_elapsed(tmc_handle* h, double* seconds) {
+  TMC_REQUIRE_HANDLE(h);
+  if (!seconds) return h->fail(TMC_E_ARG, "NULL pointer");
+  int rc;
+  if ((rc = d2h(h, h->h_diag, h->d_diag, kDiagLen))) return rc;
+  if ((rc = sync(h, "tmc_adv_elapsed"))) return rc;
+  *seconds = h->h_diag[11];
+  return TMC_OK;
 }
 
 int tmc_sizes(const tmc_handle* h, int64_t* nc, int64_t* ne, int64_t* nv, int64_t* bytes) {

@@ -115,8 +115,12 @@ enum Region {
   R_EN_C = 10,
   R_PE = 11,
   R_AV = 12,
-  R_COUNT = 13
+  R_C1 = 13,  // conservative APVM sums (operators_mod.F90:349-353)
+  R_C2 = 14,
+  R_C3 = 15,
+  R_COUNT = 16
 };
+constexpr int kFinalizeRegions = R_C1;  // regions k_finalize reduces
 
 struct Partials {
   double* base;  // [R_COUNT][cap][2]
@@ -126,6 +130,7 @@ struct Partials {
 
 // device results: [0] mass [1] energy [2] enstrophy [3] abs vort [4] beta
 //                 [5] R12 [6] R23 [7] R34 [8] R44 [9] beta*dt
+//                 [10] epsilon of the conservative APVM [11] elapsed seconds (adv model)
 constexpr int kDiagLen = 12;
 
 template <class T>
@@ -173,6 +178,11 @@ struct StageIO {
   T* v_e;
   T* pv_e;
   const double* ghs;
+  // conservative APVM (pv_scheme 2): correction direction and the two
+  // tangent fluxes of pv_edge and of the correction
+  T* dpv;
+  T* pvf;
+  T* dpvf;
 };
 
 // ---- launchers (instantiated in tmc_kernels_f64.cu / _f32.cu) ----
@@ -196,11 +206,72 @@ template <class T>
 void launch_final_update(const DevMesh& M, const ModelOpt& O, const StageIO<T>& S, const double* diag, Partials P,
                          int bs, cudaStream_t st);
 // number of blocks a launcher uses for n elements
-inline int grid_for(int n, int bs) { return (n + bs * kEPT - 1) / (bs * kEPT); }
+__host__ __device__ inline int grid_for(int n, int bs) { return (n + bs * kEPT - 1) / (bs * kEPT); }
 
-// reduction of partial regions into diag[]; counts per region
+// reduction of partial regions into diag[]; counts per region.  scheme: the
+// beta formula (1 CRK3, 2 CRK4, 3 PC2; time_scheme_mod.F90:94-100,144-150,174-180)
 void launch_finalize(Partials P, const int* counts_host, double totalArea, double sumAreaTriangle, double dt,
-                     bool step, bool diag, bool conserve, double* diag_out, cudaStream_t st);
+                     bool step, bool diag, bool conserve, double* diag_out, cudaStream_t st, int scheme = 2);
+
+// conservative APVM (pv_scheme 2) after k_edge_pv: both tangent fluxes, their
+// curls and the three global sums, epsilon, and the correction of pv_edge
+template <class T>
+void launch_cons_apvm(const DevMesh& M, const ModelOpt& O, const StageIO<T>& S, Partials P, double* diag_out, int bs,
+                      cudaStream_t st);
+void launch_cons_eps(Partials P, int count, double dt, double* diag_out, cudaStream_t st);
+
+// Generic integrators (CRK3, PC2, and CRK4 of the adv model): state update
+// new = old + coef t (update_state, tmcore_swm_mod.F90:203-213), coef from the
+// host or from device memory (beta*dt); FP32 shadows of the new state.
+template <class T>
+struct UpdateArgs {
+  const double* gd_o;
+  double* gd_n;
+  const double* tgd;
+  const T* iap_o;
+  T* iap_n;
+  const T* tiap;  // null: no edge update (adv model)
+  const T* q_o;
+  T* q_n;
+  const T* tq;
+  float* gdf_n;
+  float* qr_n;
+  double a_dt;
+  const double* coef_dev;  // non-null: coef = *coef_dev
+};
+template <class T>
+void launch_update(const DevMesh& M, int ntr, const UpdateArgs<T>& a, int bs, cudaStream_t st);
+
+// Combination of the stage tendencies into t_new (written over t[0]) and the
+// inner products of the beta formula (operators_mod.F90:187-194), into the
+// partial regions R_IP_*(k) and R_44_*:  CRK4 (scheme 2): t_new = (t1 + 2 t2 +
+// 2 t3 + t4)/6, <t1,t2>, <t2,t3>, <t3,t4>, <tn,tn>; CRK3 (1): (t1 + 4 t2 +
+// t3)/6, <t1,t2>, <t1,t3>, <t2,t3>, <tn,tn>; PC2 (3): no combination, <t0,t1>
+// and <t1,t1>.  Partial counts: grid_for(nc) for cells, grid_for(ne) for edges.
+template <class T>
+struct CombineArgs {
+  double* tgd[4];
+  T* tiap[4];  // null: no edge tendency (adv model; the edge products are zero)
+  T* tq[4];
+};
+template <class T>
+void launch_combine(const DevMesh& M, int ntr, int scheme, const CombineArgs<T>& a, Partials P, int bs,
+                    cudaStream_t st);
+
+// adv model (tmcore_adv_mod.F90:78-97): gd_edge = c2e(gd) + upwind correction
+// with the sign of u, tend = div_operator(u gd_edge) (adv_scheme_sg11_mod.F90:33-48)
+void launch_adv_spatial(const DevMesh& M, const ModelOpt& O, const double* gd, const double* u, double* gd_e,
+                        double* F, double* tend, int bs, cudaStream_t st);
+// prescribed wind at t0 + offset seconds (offset from the host, or *offset_dev
+// when non-null), u = -(psi(v2) - psi(v1))/dvEdge (cosine_bell_rotation_test_mod.F90:45-68,
+// deformation_flow_test_mod.F90:74-105)
+void launch_adv_wind(const DevMesh& M, int wind_case, double radius, const double* latV, const double* lonV,
+                     const double* t0_dev, double offset, const double* offset_dev, double* psi, double* u,
+                     cudaStream_t st);
+void launch_adv_advance(double* elapsed_dev, double dt, cudaStream_t st);
+// mass of gd into R_MASS and zero partials for the other invariant regions;
+// returns the partial count used
+int launch_mass_only(const DevMesh& M, const double* gd, Partials P, int bs, cudaStream_t st);
 
 // state transfer in the caller's element order: dst[i] = src[n2o[i]] / dst[n2o[i]] = src[i]
 template <class T>

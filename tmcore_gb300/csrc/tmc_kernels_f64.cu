@@ -11,8 +11,30 @@ TMC_INSTANTIATE(double)
 struct FinalizeArgs {
   int counts[R_COUNT];
   double totalArea, sumAreaTriangle, dt;
-  int step, diag, conserve;
+  int step, diag, conserve, scheme;
 };
+
+// Fixed-order double-double sum of one region's per-block partials, by one
+// block; lane 0 of warp 0 returns it.
+__device__ double region_sum_dd(const double* reg, int count) {
+  double hi = 0.0, lo = 0.0;
+  for (int i = threadIdx.x; i < count; i += blockDim.x) {
+    hi = __dadd_rn(hi, reg[2 * i]);
+    lo = __dadd_rn(lo, reg[2 * i + 1]);
+  }
+  __shared__ DD sm[32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  DD w = warp_reduce_dd(DD{hi, lo});
+  if (lane == 0) sm[warp] = w;
+  __syncthreads();
+  double r = 0.0;
+  if (warp == 0) {
+    w = (lane < nw) ? sm[lane] : DD{0.0, 0.0};
+    w = warp_reduce_dd(w);
+    r = w.hi + w.lo;
+  }
+  return r;
+}
 
 // One block per partial region: a fixed-order double-double reduction of the
 // region's per-block partials; the last block to finish (atomic counter, no
@@ -24,24 +46,8 @@ __global__ void __launch_bounds__(256) k_finalize(Partials P, FinalizeArgs a, do
   const int r = blockIdx.x;
   const bool want = (r <= R_44_E) ? a.step : a.diag;
   if (want) {
-    // per-thread FP64 sums over a strided subset of the block partials, then
-    // double-double across lanes and warps
-    double hi = 0.0, lo = 0.0;
-    const double* reg = P.region(r);
-    for (int i = threadIdx.x; i < a.counts[r]; i += blockDim.x) {
-      hi = __dadd_rn(hi, reg[2 * i]);
-      lo = __dadd_rn(lo, reg[2 * i + 1]);
-    }
-    __shared__ DD sm[8];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
-    DD w = warp_reduce_dd(DD{hi, lo});
-    if (lane == 0) sm[warp] = w;
-    __syncthreads();
-    if (warp == 0) {
-      w = (lane < nw) ? sm[lane] : DD{0.0, 0.0};
-      w = warp_reduce_dd(w);
-      if (lane == 0) res[r] = w.hi + w.lo;
-    }
+    const double v = region_sum_dd(P.region(r), a.counts[r]);
+    if (threadIdx.x == 0) res[r] = v;
   }
   __shared__ bool last;
   if (threadIdx.x == 0) {
@@ -57,7 +63,14 @@ __global__ void __launch_bounds__(256) k_finalize(Partials P, FinalizeArgs a, do
     for (int k = 0; k < 3; ++k) R[k] = (rv[R_IP_E + 2 * k] + rv[R_IP_C + 2 * k]) / a.totalArea;
     R[3] = (rv[R_44_E] + rv[R_44_C]) / a.totalArea;
     double beta = 1.0;
-    if (a.conserve) beta = (R[0] + R[1] + R[2]) / (3.0 * R[3]);
+    if (a.conserve) {
+      if (a.scheme == 1)  // CRK3: R[0] = <t1,t2>, R[1] = <t1,t3>, R[2] = <t2,t3>
+        beta = (2.0 * R[0] - R[1] + 2.0 * R[2]) / (3.0 * R[3]);
+      else if (a.scheme == 3)  // PC2: R[0] = <t_old,t_new>, R[3] = <t_new,t_new>
+        beta = (R[0] != 0.0 && R[3] != 0.0) ? R[0] / R[3] : 1.0;
+      else
+        beta = (R[0] + R[1] + R[2]) / (3.0 * R[3]);
+    }
     out[4] = beta;
     out[5] = R[0];
     out[6] = R[1];
@@ -75,7 +88,7 @@ __global__ void __launch_bounds__(256) k_finalize(Partials P, FinalizeArgs a, do
 }
 
 void launch_finalize(Partials P, const int* counts_host, double totalArea, double sumAreaTriangle, double dt,
-                     bool step, bool diag, bool conserve, double* diag_out, cudaStream_t st) {
+                     bool step, bool diag, bool conserve, double* diag_out, cudaStream_t st, int scheme) {
   FinalizeArgs a;
   for (int r = 0; r < R_COUNT; ++r) a.counts[r] = counts_host[r];
   a.totalArea = totalArea;
@@ -84,10 +97,132 @@ void launch_finalize(Partials P, const int* counts_host, double totalArea, doubl
   a.step = step ? 1 : 0;
   a.diag = diag ? 1 : 0;
   a.conserve = conserve ? 1 : 0;
+  a.scheme = scheme;
   // scratch after the kDiagLen outputs: R_COUNT region sums, then the counter
   double* res = diag_out + kDiagLen;
   unsigned int* counter = reinterpret_cast<unsigned int*>(diag_out + kDiagLen + R_COUNT);
-  k_finalize<<<R_COUNT, 256, 0, st>>>(P, a, diag_out, res, counter);
+  k_finalize<<<kFinalizeRegions, 256, 0, st>>>(P, a, diag_out, res, counter);
+}
+
+// Conservative APVM epsilon (operators_mod.F90:349-354): one block per sum
+// region R_C1..R_C3, the last block to finish computes
+// eps = -(s1 - 2 s2) / (2 dt s3) into out[10] and re-arms its counter.
+__global__ void __launch_bounds__(256) k_cons_eps(Partials P, int count, double dt, double* out, double* res,
+                                                  unsigned int* counter) {
+  const int r = R_C1 + blockIdx.x;
+  const double v = region_sum_dd(P.region(r), count);
+  if (threadIdx.x == 0) res[r] = v;
+  __shared__ bool last;
+  if (threadIdx.x == 0) {
+    __threadfence();
+    last = (atomicAdd(counter, 1u) == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last || threadIdx.x != 0) return;
+  __threadfence();
+  volatile const double* rv = res;
+  const double s1 = rv[R_C1], s2 = rv[R_C2], s3 = rv[R_C3];
+  out[10] = -(s1 - s2 * 2.0) / (2.0 * dt * s3);
+  *counter = 0u;
+}
+
+void launch_cons_eps(Partials P, int count, double dt, double* diag_out, cudaStream_t st) {
+  double* res = diag_out + kDiagLen;
+  unsigned int* counter = reinterpret_cast<unsigned int*>(diag_out + kDiagLen + R_COUNT + 1);
+  k_cons_eps<<<3, 256, 0, st>>>(P, count, dt, diag_out, res, counter);
+}
+
+// adv model spatial operator, edges: c2e + upwind correction with the sign of
+// u (operators_mod.F90:93-104, :423-472), mass flux u*gd_edge
+// (adv_scheme_sg11_mod.F90:42-46)
+__global__ void __launch_bounds__(kMaxBlock) k_adv_edge(DevMesh M, ModelOpt O, const double* gd, const double* u,
+                                                        double* gd_e, double* F) {
+  TMC_FOR_EPT(e, M.ne) {
+    const int c1 = M.cellsOnEdge[e], c2 = M.cellsOnEdge[M.ne + e];
+    const double ue = u[e];
+    double ge = 0.5 * (gd[c1] + gd[c2]);
+    if (O.adv_order >= 3)
+      ge = upwind_edge<double>(M.cell2, M.cell4, O.adv_order, O.cell_coef2, O.cell_coef4, M.ne, e, c1, c2, ge, ue,
+                               M.dcEdge[e], [gd](int i) { return gd[i]; });
+    gd_e[e] = ge;
+    F[e] = ue * ge;
+  }
+}
+
+// div_operator (operators_mod.F90:40-55) of the mass flux
+__global__ void __launch_bounds__(kMaxBlock) k_adv_div(DevMesh M, const double* F, double* tend) {
+  TMC_FOR_EPT(c, M.nc) {
+    double s = 0.0;
+    for (int i = 0; i < M.nEdgesOnCell[c]; ++i) {
+      const int e = M.edgesOnCell[(size_t)i * M.nc + c];
+      s = s + (double)M.nSign[(size_t)i * M.nc + c] * F[e] * M.dvEdge[e];
+    }
+    tend[c] = (-s) / M.areaCell[c];
+  }
+}
+
+void launch_adv_spatial(const DevMesh& M, const ModelOpt& O, const double* gd, const double* u, double* gd_e,
+                        double* F, double* tend, int bs, cudaStream_t st) {
+  k_adv_edge<<<grid_for(M.ne, bs), bs, 0, st>>>(M, O, gd, u, gd_e, F);
+  k_adv_div<<<grid_for(M.nc, bs), bs, 0, st>>>(M, F, tend);
+}
+
+// stream function of the prescribed wind on vertices
+__global__ void k_adv_psi(int nv, int wind_case, double radius, const double* latV, const double* lonV,
+                          const double* t0, double offset, const double* offset_dev, double* psi) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nv) return;
+  const double pi = 4.0 * atan(1.0);
+  const double lat = latV[v], lon = lonV[v];
+  if (wind_case == 1) {
+    // cosine_bell_rotation_test_mod.F90:45-68 (alpha = pi/2, one revolution in 12 days)
+    const double u0 = 2.0 * pi * radius / 12.0 / 86400.0, alpha = 0.5 * pi;
+    const double ca = cos(alpha), sa = sin(alpha);
+    psi[v] = -radius * u0 * (sin(lat) * ca - cos(lon) * cos(lat) * sa);
+  } else {
+    // deformation_flow_test_mod.F90:74-105 (case 4: deformation plus solid-body rotation)
+    const double seconds = *t0 + (offset_dev ? *offset_dev : offset);
+    const double T0 = 12.0 * 86400.0, u0 = 2.0 * pi * radius / T0;
+    const double c = pi * 2.0 * seconds / T0, k = 10.0 * radius / T0, cosT = cos(pi * seconds / T0);
+    const double sn = sin(lon - c), cl = cos(lat);
+    const double p = k * (sn * sn) * (cl * cl) * cosT - u0 * sin(lat);
+    psi[v] = p * radius;
+  }
+}
+
+__global__ void k_adv_u(int ne, const int32_t* verticesOnEdge, const double* dvEdge, const double* psi, double* u) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  u[e] = -(psi[verticesOnEdge[ne + e]] - psi[verticesOnEdge[e]]) / dvEdge[e];
+}
+
+void launch_adv_wind(const DevMesh& M, int wind_case, double radius, const double* latV, const double* lonV,
+                     const double* t0_dev, double offset, const double* offset_dev, double* psi, double* u,
+                     cudaStream_t st) {
+  k_adv_psi<<<nblk(M.nv, 256), 256, 0, st>>>(M.nv, wind_case, radius, latV, lonV, t0_dev, offset, offset_dev, psi);
+  k_adv_u<<<nblk(M.ne, 256), 256, 0, st>>>(M.ne, M.verticesOnEdge, M.dvEdge, psi, u);
+}
+
+__global__ void k_adv_advance(double* elapsed, double dt) { *elapsed = *elapsed + dt; }
+
+void launch_adv_advance(double* elapsed_dev, double dt, cudaStream_t st) {
+  k_adv_advance<<<1, 1, 0, st>>>(elapsed_dev, dt);
+}
+
+// total mass (tmcore_swm_mod.F90:215-220) alone; the other invariant regions
+// get zero partials so that the finaliser reports 0 for them
+__global__ void __launch_bounds__(kMaxBlock) k_mass_only(DevMesh M, const double* gd, Partials P) {
+  double mass = 0.0;
+  TMC_FOR_EPT(c, M.nc) mass = mass + gd[c] * M.areaCell[c];
+  const double v[5] = {mass, 0.0, 0.0, 0.0, 0.0};
+  const int r[5] = {R_MASS, R_EN_E, R_EN_C, R_PE, R_AV};
+  block_store<double, 5>(v, P, r);
+}
+
+int launch_mass_only(const DevMesh& M, const double* gd, Partials P, int bs, cudaStream_t st) {
+  const int g = grid_for(M.nc, bs);
+  k_mass_only<<<g, bs, 0, st>>>(M, gd, P);
+  return g;
 }
 
 __global__ void k_shadows(int nc, int ntr, const double* gd, const float* q, float* gdf, float* qr) {

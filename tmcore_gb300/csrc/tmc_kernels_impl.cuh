@@ -58,7 +58,8 @@ __device__ __forceinline__ DD warp_reduce_dd(DD v) {
 // double-double tail per block serialises behind the whole kernel.  Every
 // thread of the block must call this (it synchronises).
 template <class A, int N>
-__device__ __forceinline__ void block_store(const A (&v)[N], const Partials& P, const int (&r)[N]) {
+__device__ __forceinline__ void block_store(const A (&v)[N], const Partials& P, const int (&r)[N], int slot = -1) {
+  if (slot < 0) slot = blockIdx.x;
   __shared__ A sm[N][kMaxBlock / 32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
 #pragma unroll
@@ -77,8 +78,8 @@ __device__ __forceinline__ void block_store(const A (&v)[N], const Partials& P, 
       for (int off = kMaxBlock / 64; off > 0; off >>= 1) w += __shfl_down_sync(0xffffffffu, w, off);
       if (lane == 0) {
         double* reg = P.region(r[k]);
-        reg[2 * blockIdx.x] = (double)w;
-        reg[2 * blockIdx.x + 1] = 0.0;
+        reg[2 * slot] = (double)w;
+        reg[2 * slot + 1] = 0.0;
       }
     }
   }
@@ -595,7 +596,7 @@ __global__ void __launch_bounds__(kMaxBlock) k_v2c(DevMesh M, const T* pv_v, T* 
 // ---------------------------------------------------------------------------
 template <class T>
 __global__ void __launch_bounds__(kMaxBlock) k_edge_pv(DevMesh M, ModelOpt O, StageIO<T> S) {
-  const bool need_v = (O.pv_scheme == 3) || (O.pv_scheme == 1 && O.apvm_weight != 0.0);
+  const bool need_v = (O.pv_scheme >= 2) || (O.pv_scheme == 1 && O.apvm_weight != 0.0);
   TMC_FOR_EPT(e, M.ne) {
     const int v1 = M.verticesOnEdge[e], v2 = M.verticesOnEdge[M.ne + e];
     const T p1 = S.pv_v[v1], p2 = S.pv_v[v2];
@@ -616,6 +617,13 @@ __global__ void __launch_bounds__(kMaxBlock) k_edge_pv(DevMesh M, ModelOpt O, St
         const T b = S.u[e] * (S.pv_c[c2] - S.pv_c[c1]) / met<T>(M.dcEdge, M.dcEdge_f, e);
         pe = pe - T(O.apvm_weight * O.dt) * (a + b);
       }
+    } else if (O.pv_scheme == 2) {
+      // correction direction of the conservative APVM (operators_mod.F90:336-341);
+      // pv_edge stays the centred average until k_cons_apply
+      const int c1 = M.cellsOnEdge[e], c2 = M.cellsOnEdge[M.ne + e];
+      const T a = ve * (p2 - p1) / met<T>(M.dvEdge, M.dvEdge_f, e);
+      const T b = S.u[e] * (S.pv_c[c2] - S.pv_c[c1]) / met<T>(M.dcEdge, M.dcEdge_f, e);
+      S.dpv[e] = a + b;
     } else if (O.pv_scheme == 3) {
       const T* pv = S.pv_v;
       pe = upwind_edge<T>(M.vert2, M.vert4, O.interp_pv_order, T(O.vert_coef2), T(O.vert_coef4), M.ne, e, v1, v2,
@@ -623,6 +631,199 @@ __global__ void __launch_bounds__(kMaxBlock) k_edge_pv(DevMesh M, ModelOpt O, St
     }
     S.pv_e[e] = pe;
   }
+}
+
+// ---------------------------------------------------------------------------
+// conservative APVM (calc_pv_on_edge, pv_scheme 2, operators_mod.F90:318-357)
+// ---------------------------------------------------------------------------
+// calc_tangent_vor_flux (:239-260) of pv_edge and of the correction dpv; the
+// factor w u gd_edge / 2 of a neighbour is shared by both sums
+template <class T>
+__global__ void __launch_bounds__(kMaxBlock) k_cons_tvf(DevMesh M, StageIO<T> S) {
+  TMC_FOR_EPT(e, M.ne) {
+    const int n = M.nEdgesOnEdge[e];
+    const T pe = S.pv_e[e], dp = S.dpv[e];
+    T a = T(0), b = T(0);
+    for (int i = 0; i < n; ++i) {
+      const size_t k = (size_t)i * M.ne + e;
+      const int ep = M.edgesOnEdge[k];
+      const T f = met<T>(M.weightsOnEdge, M.weightsOnEdge_f, k) * S.u[ep] * S.gd_e[ep] * T(0.5);
+      a = a + f * (pe + S.pv_e[ep]);
+      b = b + f * (dp + S.dpv[ep]);
+    }
+    S.pvf[e] = a;
+    S.dpvf[e] = b;
+  }
+}
+
+// per vertex: c2v of the gd tendency (:106-123), the curls of both tangent
+// fluxes (calc_vor_tend_on_vertex :414-421), and the partial sums
+// s1 = sum pv^2 tend_gd_v A, s2 = sum pv curl(pvf) A, s3 = sum pv curl(dpvf) A
+template <class T>
+__global__ void __launch_bounds__(kMaxBlock) k_cons_vertex(DevMesh M, StageIO<T> S, Partials P) {
+  double s1 = 0.0, s2 = 0.0, s3 = 0.0;
+  TMC_FOR_EPT(v, M.nv) {
+    if constexpr (kF64<T>) {
+      const double At = M.areaTriangle[v];
+      double g = 0.0, a = 0.0, b = 0.0;
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+        g = g + S.gd_tend[M.cellsOnVertex[(size_t)i * M.nv + v]] * M.kite[(size_t)i * M.nv + v];
+      g = g / At;
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        const int e = M.edgesOnVertex[(size_t)i * M.nv + v];
+        const double ts = (double)M.tSign[(size_t)i * M.nv + v];
+        a = a + ts * S.pvf[e] * M.dcEdge[e];
+        b = b + ts * S.dpvf[e] * M.dcEdge[e];
+      }
+      const double vt = (-a) / At, dvt = (-b) / At, pv = S.pv_v[v];
+      s1 = s1 + pv * pv * g * At;
+      s2 = s2 + pv * vt * At;
+      s3 = s3 + pv * dvt * At;
+    } else {
+      const float iA = M.invAreaTriangle_f[v];
+      float g = 0.f, a = 0.f, b = 0.f;
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        g += S.tendf[M.cellsOnVertex[(size_t)i * M.nv + v]] * M.kite_f[(size_t)i * M.nv + v];
+        const int e = M.edgesOnVertex[(size_t)i * M.nv + v];
+        const float ts = (float)M.tSign[(size_t)i * M.nv + v];
+        a += ts * S.pvf[e] * M.dcEdge_f[e];
+        b += ts * S.dpvf[e] * M.dcEdge_f[e];
+      }
+      const double At = M.areaTriangle[v];
+      const float pv = S.pv_v[v];
+      s1 += (double)(pv * pv * (g * iA)) * At;
+      s2 += (double)(pv * (-a * iA)) * At;
+      s3 += (double)(pv * (-b * iA)) * At;
+    }
+  }
+  const double vals[3] = {s1, s2, s3};
+  const int r[3] = {R_C1, R_C2, R_C3};
+  block_store<double, 3>(vals, P, r);
+}
+
+// pv_edge = pv_edge - eps dt dpv (:355)
+template <class T>
+__global__ void __launch_bounds__(kMaxBlock) k_cons_apply(DevMesh M, ModelOpt O, StageIO<T> S, const double* eps) {
+  const double ed = *eps * O.dt;
+  TMC_FOR_EPT(e, M.ne) S.pv_e[e] = S.pv_e[e] - T(ed) * S.dpv[e];
+}
+
+// ---------------------------------------------------------------------------
+// generic integrators: state update, combination of tendencies, inner products
+// ---------------------------------------------------------------------------
+// cells [0, nc) then edges [nc, nc + ne) in one index space
+template <class T>
+__global__ void __launch_bounds__(kMaxBlock) k_update(DevMesh M, int ntr, UpdateArgs<T> a) {
+  const double coef = a.coef_dev ? *a.coef_dev : a.a_dt;
+  const int n = M.nc + (a.tiap ? M.ne : 0);
+  TMC_FOR_EPT(i, n) {
+    if (i < M.nc) {
+      const int c = i;
+      const double g = a.gd_o[c] + coef * a.tgd[c];  // tmcore_swm_mod.F90:211
+      a.gd_n[c] = g;
+      if constexpr (!kF64<T>) a.gdf_n[c] = (float)g;
+      for (int k = 0; k < ntr; ++k) {
+        const size_t qi = (size_t)k * M.nc + c;
+        const T q = a.q_o[qi] + T(coef) * a.tq[qi];
+        a.q_n[qi] = q;
+        if constexpr (!kF64<T>) a.qr_n[qi] = q / (float)g;
+      }
+    } else {
+      const int e = i - M.nc;
+      a.iap_n[e] = a.iap_o[e] + T(coef) * a.tiap[e];  // :210
+    }
+  }
+}
+
+template <class T>
+__global__ void __launch_bounds__(kMaxBlock) k_combine(DevMesh M, int ntr, int scheme, CombineArgs<T> a,
+                                                       Partials P) {
+  // inner products of operators_mod.F90:187-194 per region, FP64 accumulation
+  double ip[4] = {0.0, 0.0, 0.0, 0.0};
+  const int ncb = grid_for(M.nc, blockDim.x);  // blocks [0, ncb) do cells, the rest edges
+  const bool cells = (int)blockIdx.x < ncb;
+  const int n = cells ? M.nc : M.ne;
+  const int b0 = cells ? 0 : ncb;
+  for (int j = 0; j < kEPT; ++j) {
+    const int i = ((int)blockIdx.x - b0) * blockDim.x * kEPT + j * blockDim.x + threadIdx.x;
+    if (i >= n) break;
+    double t[4], w;
+    if (cells) {
+      for (int k = 0; k < 4; ++k) t[k] = a.tgd[k] ? a.tgd[k][i] : 0.0;
+      w = M.areaCell[i];
+    } else {
+      for (int k = 0; k < 4; ++k) t[k] = a.tiap[k] ? (double)a.tiap[k][i] : 0.0;
+      w = M.areaEdge[i];
+    }
+    if (scheme == 3) {  // PC2: <t0,t1>, <t1,t1>
+      ip[0] = ip[0] + t[0] * t[1] * w;
+      ip[3] = ip[3] + t[1] * t[1] * w;
+      continue;
+    }
+    double tn;
+    if (scheme == 1) {  // CRK3 (time_scheme_mod.F90:90-100)
+      tn = (t[0] + 4.0 * t[1] + t[2]) / 6.0;
+      ip[0] = ip[0] + t[0] * t[1] * w;
+      ip[1] = ip[1] + t[0] * t[2] * w;
+      ip[2] = ip[2] + t[1] * t[2] * w;
+    } else {  // CRK4 (:140-150)
+      tn = (t[0] + 2.0 * t[1] + 2.0 * t[2] + t[3]) / 6.0;
+      ip[0] = ip[0] + t[0] * t[1] * w;
+      ip[1] = ip[1] + t[1] * t[2] * w;
+      ip[2] = ip[2] + t[2] * t[3] * w;
+    }
+    if (cells) {
+      a.tgd[0][i] = tn;
+      for (int q = 0; q < ntr; ++q) {
+        const size_t qi = (size_t)q * M.nc + i;
+        const T q0 = a.tq[0][qi], q1 = a.tq[1][qi], q2 = a.tq[2][qi];
+        if (scheme == 1) {
+          a.tq[0][qi] = (q0 + T(4) * q1 + q2) / T(6);
+        } else {
+          const T q3 = a.tq[3][qi];
+          a.tq[0][qi] = (q0 + T(2) * q1 + T(2) * q2 + q3) / T(6);
+        }
+      }
+    } else if (a.tiap[0]) {
+      if constexpr (kF64<T>) {
+        a.tiap[0][i] = tn;
+      } else {
+        tn = (double)(T)tn;
+        a.tiap[0][i] = (T)tn;
+      }
+    }
+    if (cells || a.tiap[0]) ip[3] = ip[3] + tn * tn * w;
+  }
+  const int base = cells ? R_IP_C : R_IP_E;
+  const int r4 = cells ? R_44_C : R_44_E;
+  const int r[4] = {base, base + 2, base + 4, r4};
+  // partial slot: the block index within its half, cells [0, ncb), edges [0, neb)
+  block_store<double, 4>(ip, P, r, (int)blockIdx.x - b0);
+}
+
+template <class T>
+void launch_cons_apvm(const DevMesh& M, const ModelOpt& O, const StageIO<T>& S, Partials P, double* diag_out, int bs,
+                      cudaStream_t st) {
+  k_cons_tvf<T><<<grid_for(M.ne, bs), bs, 0, st>>>(M, S);
+  k_cons_vertex<T><<<grid_for(M.nv, bs), bs, 0, st>>>(M, S, P);
+  launch_cons_eps(P, grid_for(M.nv, bs), O.dt, diag_out, st);
+  k_cons_apply<T><<<grid_for(M.ne, bs), bs, 0, st>>>(M, O, S, diag_out + 10);
+}
+
+template <class T>
+void launch_update(const DevMesh& M, int ntr, const UpdateArgs<T>& a, int bs, cudaStream_t st) {
+  const int n = M.nc + (a.tiap ? M.ne : 0);
+  k_update<T><<<grid_for(n, bs), bs, 0, st>>>(M, ntr, a);
+}
+
+template <class T>
+void launch_combine(const DevMesh& M, int ntr, int scheme, const CombineArgs<T>& a, Partials P, int bs,
+                    cudaStream_t st) {
+  const int g = grid_for(M.nc, bs) + grid_for(M.ne, bs);
+  k_combine<T><<<g, bs, 0, st>>>(M, ntr, scheme, a, P);
 }
 
 // ---------------------------------------------------------------------------
@@ -992,7 +1193,8 @@ void launch_vertex(const DevMesh& M, const ModelOpt& O, const StageIO<T>& S, Par
 }
 template <class T>
 void launch_edge_pv(const DevMesh& M, const ModelOpt& O, const StageIO<T>& S, int bs, cudaStream_t st) {
-  if (O.pv_scheme == 1 && O.apvm_weight != 0.0) k_v2c<T><<<grid_for(M.nc, bs), bs, 0, st>>>(M, S.pv_v, S.pv_c);
+  if ((O.pv_scheme == 1 && O.apvm_weight != 0.0) || O.pv_scheme == 2)
+    k_v2c<T><<<grid_for(M.nc, bs), bs, 0, st>>>(M, S.pv_v, S.pv_c);
   k_edge_pv<T><<<grid_for(M.ne, bs), bs, 0, st>>>(M, O, S);
 }
 template <class T>
@@ -1033,6 +1235,10 @@ void launch_iap_from_u(int ne, const double* gd_e, const double* u, T* iap, cuda
   template void launch_edge_flux<T>(const DevMesh&, const ModelOpt&, const StageIO<T>&, RKStage, Partials, int,  \
                                     cudaStream_t);                                                                \
   template void launch_final_update<T>(const DevMesh&, const ModelOpt&, const StageIO<T>&, const double*,         \
-                                       Partials, int, cudaStream_t);
+                                       Partials, int, cudaStream_t);                                             \
+  template void launch_cons_apvm<T>(const DevMesh&, const ModelOpt&, const StageIO<T>&, Partials, double*, int,   \
+                                    cudaStream_t);                                                                \
+  template void launch_update<T>(const DevMesh&, int, const UpdateArgs<T>&, int, cudaStream_t);                 \
+  template void launch_combine<T>(const DevMesh&, int, int, const CombineArgs<T>&, Partials, int, cudaStream_t);
 
 }  // namespace tmc

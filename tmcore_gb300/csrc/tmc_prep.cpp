@@ -641,8 +641,12 @@ bool prepare_mesh(const tmc_mesh_desc& d, const tmc_params& p, const PrepOptions
   hm.kite.assign((size_t)vd * nv, 0.0);
   hm.areaTriangle.assign(nv, 0.0);
   hm.fVertex.assign(nv, 0.0);
+  hm.latVertex.assign(nv, 0.0);
+  if (d.lonVertex) hm.lonVertex.assign(nv, 0.0);
   for (int vn = 0; vn < nv; ++vn) {
     int vo = hm.vert_n2o[vn];
+    hm.latVertex[vn] = d.latVertex[vo];
+    if (d.lonVertex) hm.lonVertex[vn] = d.lonVertex[vo];
     for (int i = 0; i < vd; ++i) {
       hm.cellsOnVertex[(size_t)i * nv + vn] = co2n[d.cellsOnVertex[(size_t)vo * vd + i] - 1];
       hm.edgesOnVertex[(size_t)i * nv + vn] = eo2n[d.edgesOnVertex[(size_t)vo * vd + i] - 1];

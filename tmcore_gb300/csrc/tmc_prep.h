@@ -49,6 +49,7 @@ struct HostMesh {
   std::vector<int8_t> tSignEdge;
   std::vector<double> kite;  // [vd][nv]
   std::vector<double> areaTriangle, fVertex;
+  std::vector<double> latVertex, lonVertex;  // radians (lonVertex empty when not given)
   // v2c gather table (scalar_v2c_interp_operator, operators_mod.F90:125-141):
   // per cell, contributions in ascending ORIGINAL vertex order.
   std::vector<int32_t> v2c_start, v2c_vertex;

@@ -57,6 +57,8 @@ class TMCoreGPU:
             setattr(d, k, int(mesh.dims[k]))
         self._keep = []
         for name, _ in abi.MeshDesc._fields_[6:]:
+            if name not in mesh.vars and name in ("lonCell", "lonVertex"):
+                continue  # optional: NULL
             a = mesh.vars[name]
             a = np.ascontiguousarray(a, dtype=np.int32 if a.dtype.kind == "i" else np.float64)
             self._keep.append(a)
@@ -117,6 +119,21 @@ class TMCoreGPU:
         q = np.empty((self.n_tracers, self.nc))
         self._chk(self.lib.tmc_get_tracers(self.h, _ptr(q)))
         return q
+
+    # ------------------------------------------------------------------ adv model
+    def adv_set_initial(self, q):
+        """adv model (adv_wind 1 or 2): the advected scalar; the wind at elapsed = 0."""
+        self._chk(self.lib.tmc_adv_set_initial(self.h, _ptr(_f64(q))))
+
+    def adv_state(self):
+        q, u = np.empty(self.nc), np.empty(self.ne)
+        self._chk(self.lib.tmc_adv_get(self.h, _ptr(q), _ptr(u)))
+        return q, u
+
+    def adv_elapsed(self) -> float:
+        t = ctypes.c_double()
+        self._chk(self.lib.tmc_adv_elapsed(self.h, ctypes.byref(t)))
+        return t.value
 
     # ------------------------------------------------------------------ stepping
     def step(self, n: int = 1):
