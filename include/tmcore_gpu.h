@@ -61,7 +61,7 @@ typedef struct tmc_params {
   int32_t time_scheme;            /* 1 CRK3, 2 CRK4, 3 PC2 (time_scheme_mod.F90:47-184) */
   int32_t pv_scheme;              /* 1 APVM, 2 conservative APVM, 3 high-order upwind */
   int32_t conserve_energy;        /* energy-conserving beta (time_scheme_mod.F90:94-100,144-150,174-180) */
-  int32_t flux_4th_order_correct; /* must be 0 on the device */
+  int32_t flux_4th_order_correct; /* E-gradient correction with deriv3OnCell (tmcore_swm_mod.F90:183-195) */
   double apvm_weight;
   int32_t adv_order;              /* 2..6, upwind correction of gd on edges */
   int32_t adv_mono;

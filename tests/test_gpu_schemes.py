@@ -158,3 +158,23 @@ def test_adv_model_rejects_swm_entry_points(mesh3):
     g.step(2)
     assert np.all(np.isfinite(g.adv_state()[0]))
     g.close()
+
+
+@pytest.mark.parametrize("cfg", [dict(pv_scheme=1, apvm_weight=0.0), dict(pv_scheme=3, adv_order=3, adv_mono=1)])
+def test_flux_4th_order_correct(mesh4, cfg):
+    """E-gradient correction with the reference's deriv3OnCell (tmcore_swm_mod.F90:183-195)."""
+    g, o = _models(mesh4, dt=600.0, flux_4th_order_correct=1, **cfg)
+    gd, u, ghs = _ic(mesh4, seed=9)
+    o.set_initial(gd, u, ghs)
+    g.set_initial(gd, u, ghs)
+    gd0, iap0, _ = o.state()
+    tg_o, tu_o = o.spatial_operators(gd0, iap0)
+    tg_g, tu_g = g.spatial_operators(gd0, iap0)
+    assert np.array_equal(tg_g, tg_o)
+    assert np.array_equal(tu_g, tu_o)
+    o.step(5)
+    g.step(5)
+    go, _, uo = o.state()
+    gg, _, ug = g.get_state()
+    assert rel_max(gg, go) < 1e-12 and rel_max(ug, uo) < 1e-11
+    g.close()

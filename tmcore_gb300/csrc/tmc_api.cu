@@ -629,11 +629,6 @@ int tmc_create(const tmc_mesh_desc* mesh, const tmc_params* params, tmc_handle**
   }
   h->adv = p.adv_wind != 0;
   h->generic = h->adv || p.time_scheme != 2;
-  if (p.flux_4th_order_correct) {
-    h->err = "flux_4th_order_correct is not supported on the device";
-    *out = h.release();
-    return TMC_E_UNSUP;
-  }
   if (!(p.dt > 0.0) || !(p.radius > 0.0)) return bad("dt and radius must be positive");
   if (p.adv_order < 2 || p.adv_order > 6) return bad("adv_order must be 2..6");
   if (p.pv_scheme == 3 && (p.interp_pv_order < 3 || p.interp_pv_order > 6)) return bad("interp_pv_order must be 3..6");
@@ -662,7 +657,7 @@ int tmc_create(const tmc_mesh_desc* mesh, const tmc_params* params, tmc_handle**
     opt.min_me = 6;
     opt.min_me2 = 10;
   }
-  opt.cell_fit = p.stencils || p.adv_order >= 3 || (p.n_tracers > 0 && tro >= 3);
+  opt.cell_fit = p.stencils || p.adv_order >= 3 || (p.n_tracers > 0 && tro >= 3) || p.flux_4th_order_correct;
   opt.vertex_fit = p.stencils || p.pv_scheme == 3;
   if (!prepare_mesh(*mesh, p, opt, h->hm)) {
     h->err = h->hm.err;
@@ -728,6 +723,7 @@ int tmc_create(const tmc_mesh_desc* mesh, const tmc_params* params, tmc_handle**
     M.invAreaCell = h->upload(invA);
   }
   M.cell2 = upload_stencil(h.get(), hm.cell2);
+  M.cell3 = upload_stencil(h.get(), hm.cell3);
   M.cell4 = upload_stencil(h.get(), hm.cell4);
   M.vert2 = upload_stencil(h.get(), hm.vert2);
   M.vert4 = upload_stencil(h.get(), hm.vert4);
@@ -751,6 +747,7 @@ int tmc_create(const tmc_mesh_desc* mesh, const tmc_params* params, tmc_handle**
   O.tr_order = tro;
   O.tr_coef2 = coef2_cell(tro, p.tracer_adv_order ? p.tracer_adv_mono : p.adv_mono);
   O.tr_coef4 = h->cell_coef4;
+  O.flux4 = p.flux_4th_order_correct ? 1 : 0;
 
   const int nmax = std::max(hm.nc, std::max(hm.ne, hm.nv));
   h->raw_c = h->dalloc<double>(hm.nc);

@@ -66,7 +66,7 @@ struct DevMesh {
   const int32_t* v2c_start;
   const int32_t* v2c_vertex;
   const double* v2c_kite;
-  DStencil cell2, cell4, vert2, vert4;
+  DStencil cell2, cell3, cell4, vert2, vert4;  // cell3: deriv3OnCell on the fit3 (= fit4) stencils
   // FP32 path: FP32-rounded copies of the metrics used in FP32 arithmetic
   // and FP64 reciprocals of the areas used in FP64 arithmetic (null in FP64 mode)
   const float* weightsOnEdge_f;
@@ -92,6 +92,7 @@ struct ModelOpt {
   int n_tracers;
   int tr_order;
   double tr_coef2, tr_coef4;
+  int flux4;  // flux_4th_order_correct (tmcore_swm_mod.F90:183-195)
 };
 
 // CRK4 stage program (time_scheme_mod.F90:109-154):

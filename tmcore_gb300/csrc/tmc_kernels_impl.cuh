@@ -172,6 +172,18 @@ __device__ __forceinline__ T upwind_edge(const DStencil& S2, const DStencil& S4,
   return fe;
 }
 
+// sum_j deriv(j, side, e) (f(fit_j) - f(centre)) of one stencil side, in stencil order
+template <class T, class F>
+__device__ __forceinline__ T stencil_side(const DStencil& S, int ne, int e, int side, T fc, F f) {
+  T acc = T(0);
+  const int n = S.count[(size_t)side * ne + e];
+  for (int j = 0; j < n; ++j) {
+    const size_t k = ((size_t)j * 2 + side) * ne + e;
+    acc = acc + T(S.w[k]) * (f(S.idx[k]) - fc);
+  }
+  return acc;
+}
+
 // ---------------------------------------------------------------------------
 // edge_prep: gd_edge, u, mass flux F, tracer fluxes
 // ---------------------------------------------------------------------------
@@ -891,16 +903,28 @@ __global__ void __launch_bounds__(kMaxBlock) k_edge_flux(DevMesh M, ModelOpt O, 
       dEdx = (E2 - E1) / dc;
       tge = 0.5f * (t1 + t2);
     }
+    if (O.flux4) {
+      // flux_4th_order_correct (tmcore_swm_mod.F90:183-195): third derivatives
+      // of E on the two cells' fit3 stencils
+      const T* Ev = S.E;
+      auto fE = [Ev](int i) { return Ev[i]; };
+      const T d1 = stencil_side<T>(M.cell3, M.ne, e, 0, Ev[c1], fE);
+      const T d2 = stencil_side<T>(M.cell3, M.ne, e, 1, Ev[c2], fE);
+      dEdx = dEdx - (d2 - d1) * dc / T(24);
+    }
     const T ut = s - dEdx;
     if (O.adv_order >= 3) {
+      // the upwind side is the sign of the stage's iap_u (tmcore_swm_mod.F90:107-108);
+      // u = iap_u / sqrt(gd_edge) carries the same sign bit, and unlike iap_u it
+      // is always stored (the fused stages keep the next iap_u in registers)
       if constexpr (kF64<T>) {
         const double* gt = S.gd_tend;
         tge = upwind_edge<T>(M.cell2, M.cell4, O.adv_order, T(O.cell_coef2), T(O.cell_coef4), M.ne, e, c1, c2, tge,
-                             S.iap_in[e], dc, [gt](int i) { return gt[i]; });
+                             uu, dc, [gt](int i) { return gt[i]; });
       } else {
         const float* gt = S.tendf;
         tge = upwind_edge<T>(M.cell2, M.cell4, O.adv_order, T(O.cell_coef2), T(O.cell_coef4), M.ne, e, c1, c2, tge,
-                             S.iap_in[e], dc, [gt](int i) { return gt[i]; });
+                             uu, dc, [gt](int i) { return gt[i]; });
       }
     }
     // calc_u_tend_on_edge (tmcore_swm_mod.F90:155-201)
