@@ -79,7 +79,8 @@ typedef struct tmc_params {
   int32_t stencils;               /* 1: always build the poly-fit stencil tables (else only when used) */
   int32_t adv_wind;               /* 0: shallow-water model; adv model (tmcore_adv_mod.F90) with the
                                      prescribed wind 1 cosine-bell rotation, 2 deformation flow case 4 */
-  int32_t reserved[5];
+  int32_t members;                /* ensemble members sharing the mesh (FP32 shallow water, CRK4); 0 or 1: one */
+  int32_t reserved[4];
 } tmc_params;
 
 typedef struct tmc_handle tmc_handle;
@@ -127,6 +128,15 @@ int tmc_time_integrate(tmc_handle* h, const double* gd_old, const double* iap_u_
 /* One call of spatial_operators (tmcore_swm_mod.F90:92-125). */
 int tmc_spatial_operators(tmc_handle* h, const double* gd, const double* iap_u, double* tend_gd,
                           double* tend_iap_u);
+
+/* Ensembles (tmc_params.members > 1): every member is an independent model on
+ * the same mesh, with its own state, topography, beta and invariants; the
+ * members' arrays lie one after another and each kernel launch covers all of
+ * them.  tmc_set_initial, tmc_set_state, tmc_get_state, tmc_get_vertex,
+ * tmc_set_tracers, tmc_get_tracers and tmc_get_diag address the selected
+ * member (initially 0); tmc_step advances all members.  tmc_time_integrate and
+ * tmc_spatial_operators need members <= 1. */
+int tmc_select_member(tmc_handle* h, int32_t member);
 
 /* The adv model (tmcore_adv_mod.F90, adv_wind = 1 or 2, FP64): one
  * advected scalar in place of gd, transported by the prescribed wind that

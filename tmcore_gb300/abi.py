@@ -43,7 +43,7 @@ class Params(ctypes.Structure):
                 ("omega", ctypes.c_double), ("n_tracers", i32), ("tracer_adv_order", i32),
                 ("tracer_adv_mono", i32), ("precision", i32), ("renumber", i32), ("use_graph", i32),
                 ("diag_every", i32), ("device", i32), ("block_size", i32), ("stencils", i32),
-                ("adv_wind", i32), ("reserved", i32 * 5)]
+                ("adv_wind", i32), ("members", i32), ("reserved", i32 * 4)]
 
 
 # name -> (restype, argtypes)
@@ -75,6 +75,7 @@ SYMBOLS = {
     "tmc_op_upwind_correction": (ctypes.c_int, [vp, vp, vp, vp, i32, i32]),
     "tmc_time_steps": (ctypes.c_int, [vp, i32, dp, dp, ctypes.POINTER(i32), ctypes.POINTER(i32)]),
     "tmc_sizes": (ctypes.c_int, [vp, i64p, i64p, i64p, i64p]),
+    "tmc_select_member": (ctypes.c_int, [vp, i32]),
     "tmc_adv_set_initial": (ctypes.c_int, [vp, vp]),
     "tmc_adv_get": (ctypes.c_int, [vp, vp, vp]),
     "tmc_adv_elapsed": (ctypes.c_int, [vp, dp]),

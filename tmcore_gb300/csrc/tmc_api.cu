@@ -73,6 +73,10 @@ struct tmc_handle {
   cudaGraphExec_t g_step = nullptr, g_step_diag = nullptr;
   long step_count = 0;
   double cell_coef4 = 0.25, vert_coef4 = 0.25;  // SAVE'd coef4 of the upwind routines
+  // ensemble members of this mesh (member-outermost arrays) and the member the
+  // state-transfer calls address (tmc_select_member)
+  int members = 1;
+  int cur = 0;
   // generic integrator program: CRK3, PC2, or the adv model (any scheme)
   bool generic = false;
   bool adv = false;
@@ -140,25 +144,33 @@ struct Engine : EngineBase {
   T* u_one = nullptr;
   explicit Engine(tmc_handle* hh) : h(hh) {}
 
+  // per-member sizes (members are stored one after another)
+  size_t qsz() const { return (size_t)h->M.nc * (h->O.n_tracers > 0 ? h->O.n_tracers : 1); }
+  size_t fqsz() const {
+    return (h->O.n_tracers > 0 && h->O.tr_order >= 3) ? (size_t)h->M.ne * h->O.n_tracers : 1;
+  }
+
   int alloc() override {
-    const int nc = h->M.nc, ne = h->M.ne, nv = h->M.nv, nt = h->O.n_tracers;
+    const size_t M_ = (size_t)h->members;
+    const size_t nc = h->M.nc * M_, ne = h->M.ne * M_, nv = h->M.nv * M_;
+    const int nt = h->O.n_tracers;
+    const size_t nq = qsz() * M_, nfq = fqsz() * M_;
     for (int i = 0; i < 3; ++i) {
       gd[i] = h->dalloc<double>(nc);
       iap[i] = h->dalloc<T>(ne);
-      q[i] = h->dalloc<T>((size_t)nc * (nt > 0 ? nt : 1));
+      q[i] = h->dalloc<T>(nq);
     }
     gd_acc = h->dalloc<double>(nc);
     gd_tend = h->dalloc<double>(nc);
-    q_acc = h->dalloc<T>((size_t)nc * (nt > 0 ? nt : 1));
+    q_acc = h->dalloc<T>(nq);
     ghs = h->dalloc<double>(nc);
     iap_acc = h->dalloc<T>(ne);
     iap_tend = h->dalloc<T>(ne);
-    const bool edge_fluxes = nt > 0 && h->O.tr_order >= 3;
     for (int i = 0; i < 2; ++i) {
       gd_e[i] = h->dalloc<T>(ne);
       u[i] = h->dalloc<T>(ne);
       F[i] = h->dalloc<T>(ne);
-      Fq[i] = h->dalloc<T>(edge_fluxes ? (size_t)ne * nt : 1);
+      Fq[i] = h->dalloc<T>(nfq);
     }
     E = h->dalloc<T>(nc);
     pv_v = h->dalloc<T>(nv);
@@ -170,7 +182,7 @@ struct Engine : EngineBase {
     if (!std::is_same<T, double>::value) {
       for (int i = 0; i < 3; ++i) {
         gdf[i] = h->dalloc<float>(nc);
-        qr[i] = h->dalloc<float>((size_t)nc * (nt > 0 ? nt : 1));
+        qr[i] = h->dalloc<float>(nq);
       }
     }
     if (!pv_e || !F[1] || !Fq[1]) return TMC_E_CUDA;
@@ -185,7 +197,7 @@ struct Engine : EngineBase {
       for (int i = 0; i < ns; ++i) {
         tgd[i] = h->dalloc<double>(nc);
         tiap[i] = h->adv ? nullptr : h->dalloc<T>(ne);
-        tq[i] = h->dalloc<T>((size_t)nc * (nt > 0 ? nt : 1));
+        tq[i] = h->dalloc<T>(nq);
         if (!tgd[i] || !tq[i] || (!h->adv && !tiap[i])) return TMC_E_CUDA;
       }
     }
@@ -202,7 +214,8 @@ struct Engine : EngineBase {
       if (!tendf || !ghsf) return TMC_E_CUDA;
       cudaMemset(ghsf, 0, sizeof(float) * nc);
     }
-    cudaMemset(q[0], 0, sizeof(T) * nc * (nt > 0 ? nt : 1));
+    cudaMemset(q[0], 0, sizeof(T) * nq);
+    (void)nt;
     return TMC_OK;
   }
 
@@ -254,6 +267,12 @@ struct Engine : EngineBase {
     s.qr_next = next_slot[k] >= 0 ? qr[next_slot[k]] : nullptr;
     s.tendf = tendf;
     s.ghsf = ghsf;
+    s.members = h->members;
+    s.msc = h->M.nc;
+    s.mse = h->M.ne;
+    s.msv = h->M.nv;
+    s.msq = (long long)qsz();
+    s.msqe = (long long)fqsz();
     return s;
   }
 
@@ -307,7 +326,7 @@ struct Engine : EngineBase {
       if (flux_ev) cudaEventRecord((*flux_ev)[(*ev_pos)++], h->st);
     }
     launch_finalize(h->P, h->counts, h->hm.totalArea, h->hm.sumAreaTriangle, dt, true, diag,
-                    h->p.conserve_energy != 0, h->d_diag, h->st);
+                    h->p.conserve_energy != 0, h->d_diag, h->st, 2, h->members);
     launch_final_update<T>(M, O, io(0), h->d_diag, h->P, h->bs, h->st);
   }
 
@@ -450,7 +469,7 @@ struct Engine : EngineBase {
     launch_vertex<T>(h->M, h->O, s, h->P, true, h->bs, h->st);
     if (finalize)
       launch_finalize(h->P, h->counts, h->hm.totalArea, h->hm.sumAreaTriangle, h->O.dt, false, true,
-                      h->p.conserve_energy != 0, h->d_diag, h->st);
+                      h->p.conserve_energy != 0, h->d_diag, h->st, 2, h->members);
   }
 
   // spatial_operators on the state in slot 1 -> gd_tend, iap_tend (uses edge set 0)
@@ -470,41 +489,50 @@ struct Engine : EngineBase {
     launch_edge_flux<T>(h->M, h->O, s, rk, h->P, h->bs, h->st);
   }
 
+  // offsets of the selected member's arrays
+  size_t oc() const { return (size_t)h->cur * h->M.nc; }
+  size_t oe() const { return (size_t)h->cur * h->M.ne; }
+  size_t ov() const { return (size_t)h->cur * h->M.nv; }
+  size_t oq() const { return (size_t)h->cur * qsz(); }
+
   void set_state_dev(const double* raw_gd, const double* raw_iap) override {
-    launch_gather<double>(h->M.nc, raw_gd, h->d_cell_n2o, gd[0], h->st);
-    launch_gather<T>(h->M.ne, raw_iap, h->d_edge_n2o, iap[0], h->st);
+    launch_gather<double>(h->M.nc, raw_gd, h->d_cell_n2o, gd[0] + oc(), h->st);
+    launch_gather<T>(h->M.ne, raw_iap, h->d_edge_n2o, iap[0] + oe(), h->st);
     refresh_shadows(0);
   }
   void refresh_shadows(int slot) override {
     if constexpr (!std::is_same<T, double>::value)
-      launch_shadows(h->M.nc, h->O.n_tracers, gd[slot], q[slot], gdf[slot], qr[slot], h->st);
+      launch_shadows(h->M.nc, h->O.n_tracers, gd[slot] + oc(), q[slot] + oq(), gdf[slot] + oc(), qr[slot] + oq(),
+                     h->st);
   }
   void get_field(int which, double* raw) override {
     switch (which) {
-      case F_GD: launch_scatter<double>(h->M.nc, gd[0], h->d_cell_n2o, raw, h->st); break;
-      case F_IAP: launch_scatter<T>(h->M.ne, iap[0], h->d_edge_n2o, raw, h->st); break;
-      case F_U: launch_scatter<T>(h->M.ne, u[0], h->d_edge_n2o, raw, h->st); break;
-      case F_PV_V: launch_scatter<T>(h->M.nv, pv_v, h->d_vert_n2o, raw, h->st); break;
-      case F_VOR: launch_scatter<T>(h->M.nv, vor, h->d_vert_n2o, raw, h->st); break;
-      case F_TEND_GD: launch_scatter<double>(h->M.nc, gd_tend, h->d_cell_n2o, raw, h->st); break;
-      case F_TEND_IAP: launch_scatter<T>(h->M.ne, iap_tend, h->d_edge_n2o, raw, h->st); break;
+      case F_GD: launch_scatter<double>(h->M.nc, gd[0] + oc(), h->d_cell_n2o, raw, h->st); break;
+      case F_IAP: launch_scatter<T>(h->M.ne, iap[0] + oe(), h->d_edge_n2o, raw, h->st); break;
+      case F_U: launch_scatter<T>(h->M.ne, u[0] + oe(), h->d_edge_n2o, raw, h->st); break;
+      case F_PV_V: launch_scatter<T>(h->M.nv, pv_v + ov(), h->d_vert_n2o, raw, h->st); break;
+      case F_VOR: launch_scatter<T>(h->M.nv, vor + ov(), h->d_vert_n2o, raw, h->st); break;
+      case F_TEND_GD: launch_scatter<double>(h->M.nc, gd_tend + oc(), h->d_cell_n2o, raw, h->st); break;
+      case F_TEND_IAP: launch_scatter<T>(h->M.ne, iap_tend + oe(), h->d_edge_n2o, raw, h->st); break;
     }
   }
   void set_iap_from_u(const double* ge_new, const double* u_new) override {
-    launch_iap_from_u<T>(h->M.ne, ge_new, u_new, iap[0], h->st);
+    launch_iap_from_u<T>(h->M.ne, ge_new, u_new, iap[0] + oe(), h->st);
   }
   void set_tracers_dev(const double* raw_q) override {
     for (int k = 0; k < h->O.n_tracers; ++k)
-      launch_gather<T>(h->M.nc, raw_q + (size_t)k * h->M.nc, h->d_cell_n2o, q[0] + (size_t)k * h->M.nc, h->st);
+      launch_gather<T>(h->M.nc, raw_q + (size_t)k * h->M.nc, h->d_cell_n2o, q[0] + oq() + (size_t)k * h->M.nc,
+                       h->st);
     refresh_shadows(0);
   }
   void get_tracers_dev(double* raw_q) override {
     for (int k = 0; k < h->O.n_tracers; ++k)
-      launch_scatter<T>(h->M.nc, q[0] + (size_t)k * h->M.nc, h->d_cell_n2o, raw_q + (size_t)k * h->M.nc, h->st);
+      launch_scatter<T>(h->M.nc, q[0] + oq() + (size_t)k * h->M.nc, h->d_cell_n2o, raw_q + (size_t)k * h->M.nc,
+                        h->st);
   }
   void set_ghs_dev(const double* raw) override {
-    launch_gather<double>(h->M.nc, raw, h->d_cell_n2o, ghs, h->st);
-    if (ghsf) launch_to_f32((size_t)h->M.nc, ghs, ghsf, h->st);
+    launch_gather<double>(h->M.nc, raw, h->d_cell_n2o, ghs + oc(), h->st);
+    if (ghsf) launch_to_f32((size_t)h->M.nc, ghs + oc(), ghsf + oc(), h->st);
   }
   void copy_tracers_to_slot1() {
     cudaMemcpyAsync(q[1], q[0], sizeof(T) * h->M.nc * (h->O.n_tracers > 0 ? h->O.n_tracers : 1),
@@ -629,6 +657,15 @@ int tmc_create(const tmc_mesh_desc* mesh, const tmc_params* params, tmc_handle**
   }
   h->adv = p.adv_wind != 0;
   h->generic = h->adv || p.time_scheme != 2;
+  h->members = p.members > 0 ? p.members : 1;
+  if (h->members > 1) {
+    if (p.precision != TMC_FP32 || h->generic) {
+      h->err = "ensembles (members > 1) run the FP32 shallow-water model with CRK4";
+      *out = h.release();
+      return TMC_E_UNSUP;
+    }
+    if (h->members > 65535) return bad("members must be at most 65535");
+  }
   if (!(p.dt > 0.0) || !(p.radius > 0.0)) return bad("dt and radius must be positive");
   if (p.adv_order < 2 || p.adv_order > 6) return bad("adv_order must be 2..6");
   if (p.pv_scheme == 3 && (p.interp_pv_order < 3 || p.interp_pv_order > 6)) return bad("interp_pv_order must be 3..6");
@@ -638,6 +675,7 @@ int tmc_create(const tmc_mesh_desc* mesh, const tmc_params* params, tmc_handle**
   if (p.precision != TMC_FP64 && p.precision != TMC_FP32) return bad("precision must be TMC_FP64 or TMC_FP32");
   h->bs = p.block_size > 0 ? p.block_size : 256;
   if (h->bs % 32 != 0 || h->bs > 512) return bad("block_size must be a multiple of 32 up to 512");
+  if (p.members > 1 && h->bs > 256) return bad("block_size must be at most 256 for ensembles");
 
   if (cudaSetDevice(p.device) != cudaSuccess) {
     h->err = "cudaSetDevice failed (no CUDA device?)";
@@ -760,7 +798,7 @@ int tmc_create(const tmc_mesh_desc* mesh, const tmc_params* params, tmc_handle**
   h->op_out = h->dalloc<double>(nmax);
   const int minbs = 32;
   h->P.cap = (nmax + minbs - 1) / minbs;
-  h->P.base = h->dalloc<double>((size_t)R_COUNT * h->P.cap * 2);
+  h->P.base = h->dalloc<double>(h->P.member_stride() * h->members);
   const int bc = grid_for(hm.nc, h->bs), be = grid_for(hm.ne, h->bs), bv = grid_for(hm.nv, h->bs);
   const int rc_cells[6] = {R_IP_C, R_IP_C + 2, R_IP_C + 4, R_44_C, R_MASS, R_EN_C};
   const int rc_edges[5] = {R_IP_E, R_IP_E + 2, R_IP_E + 4, R_44_E, R_EN_E};
@@ -772,7 +810,7 @@ int tmc_create(const tmc_mesh_desc* mesh, const tmc_params* params, tmc_handle**
   for (int r = 0; r < R_COUNT; ++r) h->gen_counts[r] = h->counts[r];
   if (h->adv)  // the invariant pass of the adv model is the mass alone, over cells
     for (int r = R_MASS; r <= R_AV; ++r) h->gen_counts[r] = bc;
-  h->d_diag = h->dalloc<double>(kDiagLen + R_COUNT + 2);  // outputs, region sums, finaliser counter
+  h->d_diag = h->dalloc<double>((size_t)kDiagStride * h->members);  // per member: outputs, region sums, counters
   if (cudaMallocHost(&h->h_diag, sizeof(double) * kDiagLen) != cudaSuccess) h->h_diag = nullptr;
   if (!h->d_diag || !h->h_diag || !h->P.base) {
     h->err = "device allocation failed";
@@ -780,8 +818,8 @@ int tmc_create(const tmc_mesh_desc* mesh, const tmc_params* params, tmc_handle**
     *out = h.release();
     return TMC_E_CUDA;
   }
-  cudaMemset(h->d_diag, 0, sizeof(double) * (kDiagLen + R_COUNT + 2));
-  cudaMemset(h->P.base, 0, sizeof(double) * R_COUNT * h->P.cap * 2);
+  cudaMemset(h->d_diag, 0, sizeof(double) * kDiagStride * h->members);
+  cudaMemset(h->P.base, 0, sizeof(double) * h->P.member_stride() * h->members);
   if (p.precision == TMC_FP32)
     h->eng = std::make_unique<Engine<float>>(h.get());
   else
@@ -946,7 +984,8 @@ int tmc_get_diag(tmc_handle* h, double out[5]) {
   if (!out) return TMC_E_ARG;
   if (!h->have_state) return h->fail(TMC_E_STATE, "no state set");
   h->eng->launch_diag_pass(true);
-  cudaMemcpyAsync(h->h_diag, h->d_diag, sizeof(double) * kDiagLen, cudaMemcpyDeviceToHost, h->st);
+  cudaMemcpyAsync(h->h_diag, h->d_diag + (size_t)h->cur * kDiagStride, sizeof(double) * kDiagLen,
+                  cudaMemcpyDeviceToHost, h->st);
   int rc = sync(h, "tmc_get_diag");
   if (rc) return rc;
   for (int i = 0; i < 4; ++i) out[i] = h->h_diag[i];
@@ -957,6 +996,7 @@ int tmc_get_diag(tmc_handle* h, double out[5]) {
 int tmc_time_integrate(tmc_handle* h, const double* gd_old, const double* iap_u_old, const double* qgd_old,
                        double* gd_new, double* iap_u_new, double* qgd_new) {
   TMC_REQUIRE_SWM(h);
+  if (h->members > 1) return h->fail(TMC_E_UNSUP, "tmc_time_integrate needs members <= 1");
   if (!gd_old || !iap_u_old || !gd_new || !iap_u_new) return h->fail(TMC_E_ARG, "tmc_time_integrate: NULL array");
   const bool trc = h->O.n_tracers > 0;
   if (trc && (!qgd_old || !qgd_new)) return h->fail(TMC_E_ARG, "tmc_time_integrate: tracers need qgd arrays");
@@ -987,6 +1027,7 @@ int tmc_time_integrate(tmc_handle* h, const double* gd_old, const double* iap_u_
 int tmc_spatial_operators(tmc_handle* h, const double* gd, const double* iap_u, double* tend_gd,
                           double* tend_iap_u) {
   TMC_REQUIRE_SWM(h);
+  if (h->members > 1) return h->fail(TMC_E_UNSUP, "tmc_spatial_operators needs members <= 1");
   if (!gd || !iap_u || !tend_gd || !tend_iap_u) return h->fail(TMC_E_ARG, "tmc_spatial_operators: NULL array");
   // uses state slot 1 as scratch; state(old) is untouched
   int rc;
@@ -1130,6 +1171,13 @@ int tmc_time_steps(tmc_handle* h, int32_t nsteps, double* ms_total, double* ms_f
   }
   if (total_launches) *total_launches = nsteps * h->eng->launches_per_step();
   return h->cuda_check("tmc_time_steps");
+}
+
+int tmc_select_member(tmc_handle* h, int32_t member) {
+  TMC_REQUIRE_HANDLE(h);
+  if (member < 0 || member >= h->members) return h->fail(TMC_E_ARG, "member out of range");
+  h->cur = member;
+  return TMC_OK;
 }
 
 int tmc_adv_set_initial(tmc_handle* h, const double* q) {

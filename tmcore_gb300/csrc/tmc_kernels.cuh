@@ -124,15 +124,20 @@ enum Region {
 constexpr int kFinalizeRegions = R_C1;  // regions k_finalize reduces
 
 struct Partials {
-  double* base;  // [R_COUNT][cap][2]
+  double* base;  // [member][R_COUNT][cap][2]
   int cap;
   __host__ __device__ double* region(int r) const { return base + (size_t)r * cap * 2; }
+  __host__ __device__ size_t member_stride() const { return (size_t)R_COUNT * cap * 2; }
+  __host__ __device__ Partials at(int m) const { return Partials{base + (size_t)m * member_stride(), cap}; }
 };
 
 // device results: [0] mass [1] energy [2] enstrophy [3] abs vort [4] beta
 //                 [5] R12 [6] R23 [7] R34 [8] R44 [9] beta*dt
 //                 [10] epsilon of the conservative APVM [11] elapsed seconds (adv model)
 constexpr int kDiagLen = 12;
+// per-member block of the device diag array: outputs, region sums, counters
+constexpr int kDiagStride = 32;
+static_assert(kDiagLen + R_COUNT + 2 <= kDiagStride, "diag block too small");
 
 template <class T>
 struct StageIO {
@@ -184,7 +189,66 @@ struct StageIO {
   T* dpv;
   T* pvf;
   T* dpvf;
+  // Ensemble members of one mesh, member-outermost: the kernels run member
+  // blockIdx.y, whose arrays start `members strides` further on.
+  int members;
+  long long msc, mse, msv, msq, msqe;  // cells, edges, vertices, [ntr][nc], [ntr][ne]
+  template <class P>
+  __host__ __device__ static P* off(P* p, long long o) {
+    return p ? p + o : p;
+  }
+  __host__ __device__ StageIO at(int m) const {
+    if (m == 0) return *this;
+    StageIO s = *this;
+    const long long c = m * msc, e = m * mse, v = m * msv, q = m * msq, qe = m * msqe;
+    s.gd_in = off(gd_in, c);
+    s.gd_old = off(gd_old, c);
+    s.gd_next = off(gd_next, c);
+    s.gd_acc = off(gd_acc, c);
+    s.gd_tend = off(gd_tend, c);
+    s.iap_in = off(iap_in, e);
+    s.iap_old = off(iap_old, e);
+    s.iap_next = off(iap_next, e);
+    s.iap_acc = off(iap_acc, e);
+    s.iap_tend = off(iap_tend, e);
+    s.q_in = off(q_in, q);
+    s.q_old = off(q_old, q);
+    s.q_next = off(q_next, q);
+    s.q_acc = off(q_acc, q);
+    s.gdf_in = off(gdf_in, c);
+    s.gdf_next = off(gdf_next, c);
+    s.qr_in = off(qr_in, q);
+    s.qr_next = off(qr_next, q);
+    s.tendf = off(tendf, c);
+    s.ghsf = off(ghsf, c);
+    s.gd_e = off(gd_e, e);
+    s.u = off(u, e);
+    s.F = off(F, e);
+    s.Fq = off(Fq, qe);
+    s.gd_e_nx = off(gd_e_nx, e);
+    s.u_nx = off(u_nx, e);
+    s.F_nx = off(F_nx, e);
+    s.Fq_nx = off(Fq_nx, qe);
+    s.E = off(E, c);
+    s.pv_v = off(pv_v, v);
+    s.vor = off(vor, v);
+    s.gd_v = off(gd_v, v);
+    s.pv_c = off(pv_c, c);
+    s.v_e = off(v_e, e);
+    s.pv_e = off(pv_e, e);
+    s.ghs = off(ghs, c);
+    s.dpv = off(dpv, e);
+    s.pvf = off(pvf, e);
+    s.dpvf = off(dpvf, e);
+    return s;
+  }
 };
+
+// ensemble members a launch covers (gridDim.y)
+template <class T>
+inline unsigned nmem(const StageIO<T>& S) {
+  return S.members > 1 ? (unsigned)S.members : 1u;
+}
 
 // ---- launchers (instantiated in tmc_kernels_f64.cu / _f32.cu) ----
 template <class T>
@@ -212,14 +276,15 @@ __host__ __device__ inline int grid_for(int n, int bs) { return (n + bs * kEPT -
 // reduction of partial regions into diag[]; counts per region.  scheme: the
 // beta formula (1 CRK3, 2 CRK4, 3 PC2; time_scheme_mod.F90:94-100,144-150,174-180)
 void launch_finalize(Partials P, const int* counts_host, double totalArea, double sumAreaTriangle, double dt,
-                     bool step, bool diag, bool conserve, double* diag_out, cudaStream_t st, int scheme = 2);
+                     bool step, bool diag, bool conserve, double* diag_out, cudaStream_t st, int scheme = 2,
+                     int members = 1);
 
 // conservative APVM (pv_scheme 2) after k_edge_pv: both tangent fluxes, their
 // curls and the three global sums, epsilon, and the correction of pv_edge
 template <class T>
 void launch_cons_apvm(const DevMesh& M, const ModelOpt& O, const StageIO<T>& S, Partials P, double* diag_out, int bs,
                       cudaStream_t st);
-void launch_cons_eps(Partials P, int count, double dt, double* diag_out, cudaStream_t st);
+void launch_cons_eps(Partials P, int count, double dt, double* diag_out, cudaStream_t st, int members = 1);
 
 // Generic integrators (CRK3, PC2, and CRK4 of the adv model): state update
 // new = old + coef t (update_state, tmcore_swm_mod.F90:203-213), coef from the

@@ -41,8 +41,14 @@ __device__ double region_sum_dd(const double* reg, int count) {
 // waiting) combines the region sums into beta and the invariants
 // (time_scheme_mod.F90:144-150; tmcore_swm_mod.F90:215-255) and re-arms the
 // counter.
-__global__ void __launch_bounds__(256) k_finalize(Partials P, FinalizeArgs a, double* out, double* res,
-                                                  unsigned int* counter) {
+__global__ void __launch_bounds__(256) k_finalize(Partials P0, FinalizeArgs a, double* out0, double* res0,
+                                                  unsigned int* counter0) {
+  // one member per blockIdx.y: its partials, outputs, region sums and counter
+  const Partials P = P0.at(blockIdx.y);
+  double* out = out0 + (size_t)blockIdx.y * kDiagStride;
+  double* res = res0 + (size_t)blockIdx.y * kDiagStride;
+  unsigned int* counter = reinterpret_cast<unsigned int*>(reinterpret_cast<double*>(counter0) +
+                                                          (size_t)blockIdx.y * kDiagStride);
   const int r = blockIdx.x;
   const bool want = (r <= R_44_E) ? a.step : a.diag;
   if (want) {
@@ -88,7 +94,8 @@ __global__ void __launch_bounds__(256) k_finalize(Partials P, FinalizeArgs a, do
 }
 
 void launch_finalize(Partials P, const int* counts_host, double totalArea, double sumAreaTriangle, double dt,
-                     bool step, bool diag, bool conserve, double* diag_out, cudaStream_t st, int scheme) {
+                     bool step, bool diag, bool conserve, double* diag_out, cudaStream_t st, int scheme,
+                     int members) {
   FinalizeArgs a;
   for (int r = 0; r < R_COUNT; ++r) a.counts[r] = counts_host[r];
   a.totalArea = totalArea;
@@ -101,14 +108,19 @@ void launch_finalize(Partials P, const int* counts_host, double totalArea, doubl
   // scratch after the kDiagLen outputs: R_COUNT region sums, then the counter
   double* res = diag_out + kDiagLen;
   unsigned int* counter = reinterpret_cast<unsigned int*>(diag_out + kDiagLen + R_COUNT);
-  k_finalize<<<kFinalizeRegions, 256, 0, st>>>(P, a, diag_out, res, counter);
+  k_finalize<<<dim3(kFinalizeRegions, members > 1 ? members : 1), 256, 0, st>>>(P, a, diag_out, res, counter);
 }
 
 // Conservative APVM epsilon (operators_mod.F90:349-354): one block per sum
 // region R_C1..R_C3, the last block to finish computes
 // eps = -(s1 - 2 s2) / (2 dt s3) into out[10] and re-arms its counter.
-__global__ void __launch_bounds__(256) k_cons_eps(Partials P, int count, double dt, double* out, double* res,
-                                                  unsigned int* counter) {
+__global__ void __launch_bounds__(256) k_cons_eps(Partials P0, int count, double dt, double* out0, double* res0,
+                                                  unsigned int* counter0) {
+  const Partials P = P0.at(blockIdx.y);
+  double* out = out0 + (size_t)blockIdx.y * kDiagStride;
+  double* res = res0 + (size_t)blockIdx.y * kDiagStride;
+  unsigned int* counter = reinterpret_cast<unsigned int*>(reinterpret_cast<double*>(counter0) +
+                                                          (size_t)blockIdx.y * kDiagStride);
   const int r = R_C1 + blockIdx.x;
   const double v = region_sum_dd(P.region(r), count);
   if (threadIdx.x == 0) res[r] = v;
@@ -126,10 +138,10 @@ __global__ void __launch_bounds__(256) k_cons_eps(Partials P, int count, double 
   *counter = 0u;
 }
 
-void launch_cons_eps(Partials P, int count, double dt, double* diag_out, cudaStream_t st) {
+void launch_cons_eps(Partials P, int count, double dt, double* diag_out, cudaStream_t st, int members) {
   double* res = diag_out + kDiagLen;
   unsigned int* counter = reinterpret_cast<unsigned int*>(diag_out + kDiagLen + R_COUNT + 1);
-  k_cons_eps<<<3, 256, 0, st>>>(P, count, dt, diag_out, res, counter);
+  k_cons_eps<<<dim3(3, members > 1 ? members : 1), 256, 0, st>>>(P, count, dt, diag_out, res, counter);
 }
 
 // adv model spatial operator, edges: c2e + upwind correction with the sign of

@@ -20,6 +20,7 @@
 namespace tmc {
 
 constexpr int kMaxBlock = 512;
+constexpr int kMemberBlock = 256;  // block size limit of the ensemble (member-batched) kernels
 constexpr int kME = 6;    // unrolled maxEdges of the FP32 path
 constexpr int kME2 = 10;  // unrolled maxEdges2 of the FP32 path
 
@@ -253,8 +254,10 @@ __device__ __forceinline__ T energy_term(const DevMesh& M, int e, T ia) {
 
 // Stand-alone edge preparation of a state slot (the first stage after the
 // state was set, the diagnostic pass, spatial_operators).
-template <class T>
-__global__ void __launch_bounds__(kMaxBlock) k_edge_prep(DevMesh M, ModelOpt O, StageIO<T> S, Partials P, int diag) {
+template <class T, bool kB>
+__global__ void __launch_bounds__(kMaxBlock) k_edge_prep(DevMesh M, ModelOpt O, StageIO<T> S0, Partials P0, int diag) {
+  const StageIO<T> S = kB ? S0.at(blockIdx.y) : S0;
+  const Partials P = kB ? P0.at(blockIdx.y) : P0;
   double en = 0.0;
   const CellSrc<T> C{S.gd_in, S.gdf_in, S.q_in, S.qr_in};
   TMC_FOR_EPT(e, M.ne) {
@@ -286,9 +289,11 @@ __global__ void __launch_bounds__(kMaxBlock) k_edge_prep(DevMesh M, ModelOpt O, 
 // ---------------------------------------------------------------------------
 // cell: div of mass flux, kinetic energy, E, RK update of gd and tracers
 // ---------------------------------------------------------------------------
-template <class T>
-__global__ void __launch_bounds__(kMaxBlock) k_cell(DevMesh M, ModelOpt O, StageIO<T> S, RKStage rk, Partials P,
+template <class T, bool kB>
+__global__ void __launch_bounds__(kMaxBlock) k_cell(DevMesh M, ModelOpt O, StageIO<T> S0, RKStage rk, Partials P0,
                                                     int diag) {
+  const StageIO<T> S = kB ? S0.at(blockIdx.y) : S0;
+  const Partials P = kB ? P0.at(blockIdx.y) : P0;
   T rip = T(0), r44 = T(0);
   double mass = 0.0, enc = 0.0;
   TMC_FOR_EPT(c, M.nc) {
@@ -525,8 +530,10 @@ __global__ void __launch_bounds__(kMaxBlock) k_cell(DevMesh M, ModelOpt O, Stage
 // ---------------------------------------------------------------------------
 // vertex: gd on vertices, vorticity, potential vorticity
 // ---------------------------------------------------------------------------
-template <class T>
-__global__ void __launch_bounds__(kMaxBlock) k_vertex(DevMesh M, ModelOpt O, StageIO<T> S, Partials P, int diag) {
+template <class T, bool kB>
+__global__ void __launch_bounds__(kMaxBlock) k_vertex(DevMesh M, ModelOpt O, StageIO<T> S0, Partials P0, int diag) {
+  const StageIO<T> S = kB ? S0.at(blockIdx.y) : S0;
+  const Partials P = kB ? P0.at(blockIdx.y) : P0;
   double pe = 0.0, av = 0.0;
   TMC_FOR_EPT(v, M.nv) {
     T gv, vo, pv;
@@ -594,7 +601,9 @@ __global__ void __launch_bounds__(kMaxBlock) k_vertex(DevMesh M, ModelOpt O, Sta
 
 // pv on cells: scalar_v2c_interp_operator as a gather (operators_mod.F90:125-141)
 template <class T>
-__global__ void __launch_bounds__(kMaxBlock) k_v2c(DevMesh M, const T* pv_v, T* pv_c) {
+__global__ void __launch_bounds__(kMaxBlock) k_v2c(DevMesh M, const T* pv_v0, T* pv_c0, long long msv, long long msc) {
+  const T* pv_v = pv_v0 + blockIdx.y * msv;
+  T* pv_c = pv_c0 + blockIdx.y * msc;
   TMC_FOR_EPT(c, M.nc) {
     const T A = T(M.areaCell[c]);
     T s = T(0);
@@ -606,8 +615,9 @@ __global__ void __launch_bounds__(kMaxBlock) k_v2c(DevMesh M, const T* pv_v, T* 
 // ---------------------------------------------------------------------------
 // edge_pv: PV on edges (calc_pv_on_edge, operators_mod.F90:273-412)
 // ---------------------------------------------------------------------------
-template <class T>
-__global__ void __launch_bounds__(kMaxBlock) k_edge_pv(DevMesh M, ModelOpt O, StageIO<T> S) {
+template <class T, bool kB>
+__global__ void __launch_bounds__(kMaxBlock) k_edge_pv(DevMesh M, ModelOpt O, StageIO<T> S0) {
+  const StageIO<T> S = kB ? S0.at(blockIdx.y) : S0;
   const bool need_v = (O.pv_scheme >= 2) || (O.pv_scheme == 1 && O.apvm_weight != 0.0);
   TMC_FOR_EPT(e, M.ne) {
     const int v1 = M.verticesOnEdge[e], v2 = M.verticesOnEdge[M.ne + e];
@@ -650,8 +660,9 @@ __global__ void __launch_bounds__(kMaxBlock) k_edge_pv(DevMesh M, ModelOpt O, St
 // ---------------------------------------------------------------------------
 // calc_tangent_vor_flux (:239-260) of pv_edge and of the correction dpv; the
 // factor w u gd_edge / 2 of a neighbour is shared by both sums
-template <class T>
-__global__ void __launch_bounds__(kMaxBlock) k_cons_tvf(DevMesh M, StageIO<T> S) {
+template <class T, bool kB>
+__global__ void __launch_bounds__(kMaxBlock) k_cons_tvf(DevMesh M, StageIO<T> S0) {
+  const StageIO<T> S = kB ? S0.at(blockIdx.y) : S0;
   TMC_FOR_EPT(e, M.ne) {
     const int n = M.nEdgesOnEdge[e];
     const T pe = S.pv_e[e], dp = S.dpv[e];
@@ -671,8 +682,10 @@ __global__ void __launch_bounds__(kMaxBlock) k_cons_tvf(DevMesh M, StageIO<T> S)
 // per vertex: c2v of the gd tendency (:106-123), the curls of both tangent
 // fluxes (calc_vor_tend_on_vertex :414-421), and the partial sums
 // s1 = sum pv^2 tend_gd_v A, s2 = sum pv curl(pvf) A, s3 = sum pv curl(dpvf) A
-template <class T>
-__global__ void __launch_bounds__(kMaxBlock) k_cons_vertex(DevMesh M, StageIO<T> S, Partials P) {
+template <class T, bool kB>
+__global__ void __launch_bounds__(kMaxBlock) k_cons_vertex(DevMesh M, StageIO<T> S0, Partials P0) {
+  const StageIO<T> S = kB ? S0.at(blockIdx.y) : S0;
+  const Partials P = kB ? P0.at(blockIdx.y) : P0;
   double s1 = 0.0, s2 = 0.0, s3 = 0.0;
   TMC_FOR_EPT(v, M.nv) {
     if constexpr (kF64<T>) {
@@ -717,8 +730,10 @@ __global__ void __launch_bounds__(kMaxBlock) k_cons_vertex(DevMesh M, StageIO<T>
 }
 
 // pv_edge = pv_edge - eps dt dpv (:355)
-template <class T>
-__global__ void __launch_bounds__(kMaxBlock) k_cons_apply(DevMesh M, ModelOpt O, StageIO<T> S, const double* eps) {
+template <class T, bool kB>
+__global__ void __launch_bounds__(kMaxBlock) k_cons_apply(DevMesh M, ModelOpt O, StageIO<T> S0, const double* eps0) {
+  const StageIO<T> S = kB ? S0.at(blockIdx.y) : S0;
+  const double* eps = kB ? eps0 + (size_t)blockIdx.y * kDiagStride : eps0;
   const double ed = *eps * O.dt;
   TMC_FOR_EPT(e, M.ne) S.pv_e[e] = S.pv_e[e] - T(ed) * S.dpv[e];
 }
@@ -816,13 +831,28 @@ __global__ void __launch_bounds__(kMaxBlock) k_combine(DevMesh M, int ntr, int s
   block_store<double, 4>(ip, P, r, (int)blockIdx.x - b0);
 }
 
+// Launch KERNEL<T, kB> over (GRIDX, members): the member-batched variant
+// (kB = true, FP32 only) when the stage has several ensemble members, else the
+// single-member code, which addresses its arrays straight from the kernel
+// parameters.
+#define TMC_LAUNCH(KERNEL, GRIDX, ...)                                     \
+  do {                                                                     \
+    if constexpr (!kF64<T>) {                                              \
+      if (S.members > 1) {                                                 \
+        KERNEL<T, true><<<dim3(GRIDX, nmem(S)), bs, 0, st>>>(__VA_ARGS__); \
+        break;                                                             \
+      }                                                                    \
+    }                                                                      \
+    KERNEL<T, false><<<dim3(GRIDX, 1), bs, 0, st>>>(__VA_ARGS__);          \
+  } while (0)
+
 template <class T>
 void launch_cons_apvm(const DevMesh& M, const ModelOpt& O, const StageIO<T>& S, Partials P, double* diag_out, int bs,
                       cudaStream_t st) {
-  k_cons_tvf<T><<<grid_for(M.ne, bs), bs, 0, st>>>(M, S);
-  k_cons_vertex<T><<<grid_for(M.nv, bs), bs, 0, st>>>(M, S, P);
-  launch_cons_eps(P, grid_for(M.nv, bs), O.dt, diag_out, st);
-  k_cons_apply<T><<<grid_for(M.ne, bs), bs, 0, st>>>(M, O, S, diag_out + 10);
+  TMC_LAUNCH(k_cons_tvf, grid_for(M.ne, bs), M, S);
+  TMC_LAUNCH(k_cons_vertex, grid_for(M.nv, bs), M, S, P);
+  launch_cons_eps(P, grid_for(M.nv, bs), O.dt, diag_out, st, (int)nmem(S));
+  TMC_LAUNCH(k_cons_apply, grid_for(M.ne, bs), M, O, S, diag_out + 10);
 }
 
 template <class T>
@@ -841,8 +871,11 @@ void launch_combine(const DevMesh& M, int ntr, int scheme, const CombineArgs<T>&
 // ---------------------------------------------------------------------------
 // edge_flux: q.F_perp, gradient of E, iap_u tendency, RK update, inner products
 // ---------------------------------------------------------------------------
-template <class T>
-__global__ void __launch_bounds__(kMaxBlock) k_edge_flux(DevMesh M, ModelOpt O, StageIO<T> S, RKStage rk, Partials P) {
+template <class T, bool kB>
+__device__ __forceinline__ void edge_flux_body(const DevMesh& M, const ModelOpt& O, const StageIO<T>& S0, RKStage rk,
+                                               const Partials& P0) {
+  const StageIO<T> S = kB ? S0.at(blockIdx.y) : S0;
+  const Partials P = kB ? P0.at(blockIdx.y) : P0;
   T rip = T(0), r44 = T(0);  // FP32 path: FP32 products and per-thread sums, FP64 across warps
   const int mode = rk.mode;
   TMC_FOR_EPT(e, M.ne) {
@@ -977,10 +1010,24 @@ __global__ void __launch_bounds__(kMaxBlock) k_edge_flux(DevMesh M, ModelOpt O, 
   }
 }
 
+// the single-model kernel, and the ensemble kernel (member = blockIdx.y) with
+// its register budget capped so that member pointers do not halve occupancy
+template <class T>
+__global__ void __launch_bounds__(kMaxBlock) k_edge_flux(DevMesh M, ModelOpt O, StageIO<T> S0, RKStage rk, Partials P0) {
+  edge_flux_body<T, false>(M, O, S0, rk, P0);
+}
+template <class T>
+__global__ void __launch_bounds__(kMemberBlock, 3) k_edge_flux_members(DevMesh M, ModelOpt O, StageIO<T> S0, RKStage rk,
+                                                                    Partials P0) {
+  edge_flux_body<T, true>(M, O, S0, rk, P0);
+}
+
 // new = old + (beta dt) t_new (update_state, tmcore_swm_mod.F90:203-213)
 // Cells: gd and tracer mass of state(old) in place, and their FP32 shadows.
-template <class T>
-__global__ void __launch_bounds__(kMaxBlock) k_final_cells(DevMesh M, ModelOpt O, StageIO<T> S, const double* diag) {
+template <class T, bool kB>
+__global__ void __launch_bounds__(kMaxBlock) k_final_cells(DevMesh M, ModelOpt O, StageIO<T> S0, const double* diag0) {
+  const StageIO<T> S = kB ? S0.at(blockIdx.y) : S0;
+  const double* diag = kB ? diag0 + (size_t)blockIdx.y * kDiagStride : diag0;
   const double bdt = diag[9];
   TMC_FOR_EPT(i, M.nc) {
     double* gd = const_cast<double*>(S.gd_old);
@@ -1001,9 +1048,12 @@ __global__ void __launch_bounds__(kMaxBlock) k_final_cells(DevMesh M, ModelOpt O
 // step's first stage (into S.gd_e/u/F/Fq) and the edge part of the total
 // energy of the new state (tmcore_swm_mod.F90:229) for the next step's
 // invariants.
-template <class T>
-__global__ void __launch_bounds__(kMaxBlock) k_final_edges(DevMesh M, ModelOpt O, StageIO<T> S, const double* diag,
-                                                           Partials P) {
+template <class T, bool kB>
+__global__ void __launch_bounds__(kMaxBlock) k_final_edges(DevMesh M, ModelOpt O, StageIO<T> S0, const double* diag0,
+                                                           Partials P0) {
+  const StageIO<T> S = kB ? S0.at(blockIdx.y) : S0;
+  const Partials P = kB ? P0.at(blockIdx.y) : P0;
+  const double* diag = kB ? diag0 + (size_t)blockIdx.y * kDiagStride : diag0;
   const double bdt = diag[9];
   double en = 0.0;
   const CellSrc<T> C{S.gd_old, S.gdf_in, S.q_old, S.qr_in};
@@ -1053,19 +1103,22 @@ __global__ void k_iap_from_u(int ne, const double* gd_e, const double* u, T* iap
 // ---------------------------------------------------------------------------
 inline int nblk(int n, int bs) { return (n + bs - 1) / bs; }
 
+
 template <class T>
 void launch_edge_prep(const DevMesh& M, const ModelOpt& O, const StageIO<T>& S, Partials P, bool diag, int bs,
                       cudaStream_t st) {
-  k_edge_prep<T><<<grid_for(M.ne, bs), bs, 0, st>>>(M, O, S, P, diag ? 1 : 0);
+  TMC_LAUNCH(k_edge_prep, grid_for(M.ne, bs), M, O, S, P, diag ? 1 : 0);
 }
 // FP32 cell pass of the CRK4 stages (modes 1-4) with NTR second-order
 // tracers: every load is issued before the first store, in two waves
 // (indices and the cell's own values, then the gathers of the edges' u, F,
 // dvEdge, areaEdge and of the neighbours' tracer mixing ratios), so one cell
 // costs two memory round trips.  Same arithmetic as the FP32 branch of k_cell.
-template <int NTR>
-__global__ void __launch_bounds__(kMaxBlock) k_cell_fast(DevMesh M, StageIO<float> S, RKStage rk, Partials P,
-                                                         int diag) {
+template <int NTR, bool kB>
+__device__ __forceinline__ void cell_fast_body(const DevMesh& M, const StageIO<float>& S0, RKStage rk,
+                                               const Partials& P0, int diag) {
+  const StageIO<float> S = kB ? S0.at(blockIdx.y) : S0;
+  const Partials P = kB ? P0.at(blockIdx.y) : P0;
   constexpr int NQ = NTR > 0 ? NTR : 1;
   float rip = 0.f, r44 = 0.f;
   double mass = 0.0, enc = 0.0;
@@ -1192,6 +1245,17 @@ __global__ void __launch_bounds__(kMaxBlock) k_cell_fast(DevMesh M, StageIO<floa
   }
 }
 
+template <int NTR>
+__global__ void __launch_bounds__(kMaxBlock) k_cell_fast(DevMesh M, StageIO<float> S0, RKStage rk, Partials P0,
+                                                         int diag) {
+  cell_fast_body<NTR, false>(M, S0, rk, P0, diag);
+}
+template <int NTR>
+__global__ void __launch_bounds__(kMemberBlock, 3) k_cell_fast_members(DevMesh M, StageIO<float> S0, RKStage rk,
+                                                                    Partials P0, int diag) {
+  cell_fast_body<NTR, true>(M, S0, rk, P0, diag);
+}
+
 template <class T>
 void launch_cell(const DevMesh& M, const ModelOpt& O, const StageIO<T>& S, RKStage rk, Partials P, bool diag, int bs,
                  cudaStream_t st) {
@@ -1200,37 +1264,63 @@ void launch_cell(const DevMesh& M, const ModelOpt& O, const StageIO<T>& S, RKSta
     if (fast) {
       const int g = grid_for(M.nc, bs), dg = diag ? 1 : 0;
       switch (O.n_tracers) {
-        case 0: k_cell_fast<0><<<g, bs, 0, st>>>(M, S, rk, P, dg); return;
-        case 1: k_cell_fast<1><<<g, bs, 0, st>>>(M, S, rk, P, dg); return;
-        case 2: k_cell_fast<2><<<g, bs, 0, st>>>(M, S, rk, P, dg); return;
-        case 4: k_cell_fast<4><<<g, bs, 0, st>>>(M, S, rk, P, dg); return;
+        case 0:
+          if (S.members > 1)
+            k_cell_fast_members<0><<<dim3(g, nmem(S)), bs, 0, st>>>(M, S, rk, P, dg);
+          else
+            k_cell_fast<0><<<g, bs, 0, st>>>(M, S, rk, P, dg);
+          return;
+        case 1:
+          if (S.members > 1)
+            k_cell_fast_members<1><<<dim3(g, nmem(S)), bs, 0, st>>>(M, S, rk, P, dg);
+          else
+            k_cell_fast<1><<<g, bs, 0, st>>>(M, S, rk, P, dg);
+          return;
+        case 2:
+          if (S.members > 1)
+            k_cell_fast_members<2><<<dim3(g, nmem(S)), bs, 0, st>>>(M, S, rk, P, dg);
+          else
+            k_cell_fast<2><<<g, bs, 0, st>>>(M, S, rk, P, dg);
+          return;
+        case 4:
+          if (S.members > 1)
+            k_cell_fast_members<4><<<dim3(g, nmem(S)), bs, 0, st>>>(M, S, rk, P, dg);
+          else
+            k_cell_fast<4><<<g, bs, 0, st>>>(M, S, rk, P, dg);
+          return;
         default: break;
       }
     }
   }
-  k_cell<T><<<grid_for(M.nc, bs), bs, 0, st>>>(M, O, S, rk, P, diag ? 1 : 0);
+  TMC_LAUNCH(k_cell, grid_for(M.nc, bs), M, O, S, rk, P, diag ? 1 : 0);
 }
 template <class T>
 void launch_vertex(const DevMesh& M, const ModelOpt& O, const StageIO<T>& S, Partials P, bool diag, int bs,
                    cudaStream_t st) {
-  k_vertex<T><<<grid_for(M.nv, bs), bs, 0, st>>>(M, O, S, P, diag ? 1 : 0);
+  TMC_LAUNCH(k_vertex, grid_for(M.nv, bs), M, O, S, P, diag ? 1 : 0);
 }
 template <class T>
 void launch_edge_pv(const DevMesh& M, const ModelOpt& O, const StageIO<T>& S, int bs, cudaStream_t st) {
   if ((O.pv_scheme == 1 && O.apvm_weight != 0.0) || O.pv_scheme == 2)
-    k_v2c<T><<<grid_for(M.nc, bs), bs, 0, st>>>(M, S.pv_v, S.pv_c);
-  k_edge_pv<T><<<grid_for(M.ne, bs), bs, 0, st>>>(M, O, S);
+    k_v2c<T><<<dim3(grid_for(M.nc, bs), nmem(S)), bs, 0, st>>>(M, S.pv_v, S.pv_c, S.msv, S.msc);
+  TMC_LAUNCH(k_edge_pv, grid_for(M.ne, bs), M, O, S);
 }
 template <class T>
 void launch_edge_flux(const DevMesh& M, const ModelOpt& O, const StageIO<T>& S, RKStage rk, Partials P, int bs,
                       cudaStream_t st) {
+  if constexpr (!kF64<T>) {
+    if (S.members > 1) {
+      k_edge_flux_members<T><<<dim3(grid_for(M.ne, bs), nmem(S)), bs, 0, st>>>(M, O, S, rk, P);
+      return;
+    }
+  }
   k_edge_flux<T><<<grid_for(M.ne, bs), bs, 0, st>>>(M, O, S, rk, P);
 }
 template <class T>
 void launch_final_update(const DevMesh& M, const ModelOpt& O, const StageIO<T>& S, const double* diag, Partials P,
                          int bs, cudaStream_t st) {
-  k_final_cells<T><<<grid_for(M.nc, bs), bs, 0, st>>>(M, O, S, diag);
-  k_final_edges<T><<<grid_for(M.ne, bs), bs, 0, st>>>(M, O, S, diag, P);
+  TMC_LAUNCH(k_final_cells, grid_for(M.nc, bs), M, O, S, diag);
+  TMC_LAUNCH(k_final_edges, grid_for(M.ne, bs), M, O, S, diag, P);
 }
 template <class T>
 void launch_gather(int n, const double* src, const int32_t* n2o, T* dst, cudaStream_t st) {

@@ -120,6 +120,11 @@ class TMCoreGPU:
         self._chk(self.lib.tmc_get_tracers(self.h, _ptr(q)))
         return q
 
+    # ------------------------------------------------------------------ ensembles
+    def select_member(self, m: int):
+        """State-transfer calls address member m of an ensemble (members > 1)."""
+        self._chk(self.lib.tmc_select_member(self.h, int(m)))
+
     # ------------------------------------------------------------------ adv model
     def adv_set_initial(self, q):
         """adv model (adv_wind 1 or 2): the advected scalar; the wind at elapsed = 0."""
