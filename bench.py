@@ -48,6 +48,11 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-steps", type=int, default=1)
+    ap.add_argument("--no-autotune", action="store_true", help="keep 256-thread blocks")
+    ap.add_argument("--ensemble-members", type=int, default=512,
+                    help="FP32 ensemble on --ensemble-level (0: skip)")
+    ap.add_argument("--ensemble-level", type=int, default=6)
+    ap.add_argument("--ensemble-steps", type=int, default=20)
     return ap.parse_args()
 
 
@@ -215,6 +220,57 @@ def step_model_bytes(nc: int, ne: int, nv: int, S: int, ntr: int) -> float:
     return 4 * (per_stage + tracer_stage) + 3 * S * (nc + ne) + ntr * 3 * 8 * nc
 
 
+def ensemble_model_bytes(nc: int, ne: int, nv: int, S: int, members: int) -> float:
+    """The hot-path scope's per-step model with `members` models sharing one
+    mesh: mesh arrays once per stage, state per member."""
+    return 4 * (39 * nc + 153 * ne + 67 * nv + members * (8 * S * nc + 7 * S * ne)) + 3 * S * members * (nc + ne)
+
+
+def _ensemble_ic(job):
+    """Initial state of one ensemble member (runs in a spawned worker)."""
+    level, seed = job
+    from tmcore_gb300 import cases, mesh
+
+    return cases.jet_bumps(mesh.icos_mesh(level), seed=seed)
+
+
+def ensemble_ics(level: int, members: int):
+    """Seeds 0..members-1, generated by a spawn pool (started before any CUDA work)."""
+    import multiprocessing as mp
+
+    with mp.get_context("spawn").Pool(min(16, os.cpu_count() or 1)) as pool:
+        return pool.map(_ensemble_ic, [(level, s) for s in range(members)], chunksize=8)
+
+
+def run_ensemble(args, local, ics, peak):
+    """Config 3: FP32 members of one mesh stepped together (member = blockIdx.y of
+    every launch), CUDA graph per CRK4 step; dt = 1200 / 2^(level-4) s."""
+    from tmcore_gb300 import abi, mesh
+    from tmcore_gb300.gpu import TMCoreGPU
+
+    L, M = args.ensemble_level, len(ics)
+    m = mesh.icos_mesh(L)
+    dt = 1200.0 / 2 ** (L - 4)
+    ens = TMCoreGPU(m, members=M, dt=dt, pv_scheme=1, apvm_weight=0.0, adv_order=2, conserve_energy=1,
+                    precision=abi.TMC_FP32, diag_every=1, use_graph=1, renumber=1, device=local)
+    for k, (gd, u, ghs) in enumerate(ics):
+        ens.select_member(k)
+        ens.set_initial(gd, u, ghs)
+    tuned = ens.autotune(steps=2) if not args.no_autotune else None
+    ens.step(args.warmup)
+    ens.synchronize()
+    ms, _, _, launches = ens.time_steps(args.ensemble_steps, total=True, flux=False)
+    step_s = ms / args.ensemble_steps / 1e3
+    d = ens.diag()
+    ens.close()
+    mb = ensemble_model_bytes(m.nCells, m.nEdges, m.nVertices, 4, M)
+    return {"workload": f"{M} FP32 members on level {L} ({m.nCells} cells), seeds 0..{M - 1}, CRK4 dt={dt:g}s",
+            "members": M, "level": L, "dt_s": dt, "steps": args.ensemble_steps, "ms_per_step": step_s * 1e3,
+            "member_days_per_s": M * dt / DAY / step_s, "sim_days_per_s": dt / DAY / step_s,
+            "scope_model_bytes_per_step": mb, "achieved_gbs": mb / step_s / 1e9, "frac": mb / step_s / 1e9 / peak,
+            "gpu_launches": launches, "member0_beta": float(d[4]), "block_sizes": tuned}
+
+
 def ncu_traffic(name: str):
     """dram bytes per launch from the committed ncu summary, if present."""
     p = os.path.join(ROOT, "profiles", name)
@@ -313,6 +369,8 @@ def main():
     from tmcore_gb300 import abi
     from tmcore_gb300.gpu import TMCoreGPU
 
+    # ensemble initial states from a spawn pool, before any CUDA work
+    ens_ics = ensemble_ics(args.ensemble_level, args.ensemble_members) if args.ensemble_members > 0 else None
     dist = Dist(world)
     m, gd, u, ghs, q, t_setup = setup(args)
     args.seed += rank  # independent replicas
@@ -322,6 +380,7 @@ def main():
     gpu.set_initial(gd, u, ghs)
     if args.tracers:
         gpu.set_tracers(qgd)
+    tuned = gpu.autotune(steps=3) if not args.no_autotune else None
     gpu.step(args.warmup)
     gpu.synchronize()
 
@@ -410,6 +469,10 @@ def main():
                "d2h_bytes_per_step": bytes_io, "ms_per_step": el / args.steps * 1e3,
                "call": "tmc_time_integrate (host state in, host state out, every step)"}
 
+    if ens_ics is not None:
+        extra["ensemble"] = run_ensemble(args, local, ens_ics, peak)
+        ens_ics = None
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
@@ -426,7 +489,8 @@ def main():
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded initial state on a generated mesh)",
-        "config": config_dict(args, m, "FP32 state + FP64 metrics/gd/sums, CUDA graph per CRK4 step"),
+        "config": {**config_dict(args, m, "FP32 state + FP64 metrics/gd/sums, CUDA graph per CRK4 step"),
+                   "block_sizes": tuned},
         "clocks": clk,
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "kernel": "k_edge_flux<float>", "achieved": achieved, "peak": peak,

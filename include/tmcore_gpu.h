@@ -129,6 +129,13 @@ int tmc_time_integrate(tmc_handle* h, const double* gd_old, const double* iap_u_
 int tmc_spatial_operators(tmc_handle* h, const double* gd, const double* iap_u, double* tend_gd,
                           double* tend_iap_u);
 
+/* Autotuner: times `steps` eager steps of the current state for each block
+ * size in {64, 128, 192, 256, 384, 512} (256 at most for ensembles), one pass
+ * of the fused step at a time (edge_flux, cell, vertex, edge_pv, final), keeps
+ * the fastest per pass, restores the state and re-captures the step graphs.
+ * block_sizes (may be NULL) receives {cell, vertex, edge_pv, edge_flux, final}. */
+int tmc_autotune(tmc_handle* h, int32_t steps, int32_t block_sizes[5]);
+
 /* Ensembles (tmc_params.members > 1): every member is an independent model on
  * the same mesh, with its own state, topography, beta and invariants; the
  * members' arrays lie one after another and each kernel launch covers all of

@@ -65,3 +65,35 @@ def test_member_selection_bounds(mesh3):
     ens.close()
     with pytest.raises(TMCError):  # FP64 ensembles are not built
         TMCoreGPU(mesh3, dt=600.0, precision=0, members=3)
+
+
+@pytest.mark.parametrize("members", [1, 6])
+def test_autotune_keeps_state_and_results(mesh5, members):
+    from tmcore_gb300.gpu import TMCoreGPU
+
+    kw = dict(dt=300.0, precision=1, pv_scheme=1, apvm_weight=0.0, members=members)
+    a, b = TMCoreGPU(mesh5, **kw), TMCoreGPU(mesh5, **kw)
+    for m in range(members):
+        gd, u, ghs = _ic(mesh5, seed=40 + m)
+        for x in (a, b):
+            x.select_member(m)
+            x.set_initial(gd, u, ghs)
+    before = a.get_state()
+    sizes = a.autotune(steps=2)
+    assert all(s in (64, 128, 192, 256, 384, 512) for s in sizes.values())
+    if members > 1:
+        assert max(sizes.values()) <= 256
+    after = a.get_state()
+    assert all(np.array_equal(x, y) for x, y in zip(before, after))
+    a.step(10)
+    b.step(10)
+    for m in range(members):
+        a.select_member(m)
+        b.select_member(m)
+        ga, _, ua = a.get_state()
+        gb, _, ub = b.get_state()
+        # only beta's block partition changes with the block sizes
+        assert np.max(np.abs(ga - gb)) / np.max(np.abs(gb)) < 1e-6
+        assert np.all(np.isfinite(ua))
+    a.close()
+    b.close()

@@ -76,6 +76,7 @@ SYMBOLS = {
     "tmc_time_steps": (ctypes.c_int, [vp, i32, dp, dp, ctypes.POINTER(i32), ctypes.POINTER(i32)]),
     "tmc_sizes": (ctypes.c_int, [vp, i64p, i64p, i64p, i64p]),
     "tmc_select_member": (ctypes.c_int, [vp, i32]),
+    "tmc_autotune": (ctypes.c_int, [vp, i32, ctypes.POINTER(i32)]),
     "tmc_adv_set_initial": (ctypes.c_int, [vp, vp]),
     "tmc_adv_get": (ctypes.c_int, [vp, vp, vp]),
     "tmc_adv_elapsed": (ctypes.c_int, [vp, dp]),

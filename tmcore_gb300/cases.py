@@ -78,10 +78,26 @@ def _legendre_all(lmax, x):
     return P
 
 
+_BASIS_CACHE: list = []
+
+
+def _basis(lat, lon, lmax):
+    """Legendre table and cos/sin(m lon) of one set of points (cached per array pair)."""
+    for la, lo, lm, val in _BASIS_CACHE:
+        if la is lat and lo is lon and lm >= lmax:
+            return val
+    P = _legendre_all(lmax, np.sin(lat))
+    cm = [np.cos(m * lon) for m in range(lmax + 1)]
+    sm = [np.sin(m * lon) for m in range(lmax + 1)]
+    val = (P, cm, sm)
+    _BASIS_CACHE.append((lat, lon, lmax, val))
+    del _BASIS_CACHE[:-4]
+    return val
+
+
 def harmonic_field(lat, lon, lmin, lmax, rng):
     """Sum of real spherical harmonics of degrees lmin..lmax with N(0,1) coefficients."""
-    x = np.sin(lat)
-    P = _legendre_all(lmax, x)
+    P, cm, sm = _basis(lat, lon, lmax)
     f = np.zeros_like(lat)
     for l in range(lmin, lmax + 1):
         for m in range(0, l + 1):
@@ -89,7 +105,7 @@ def harmonic_field(lat, lon, lmin, lmax, rng):
             if m == 0:
                 f += a * P[(l, 0)]
             else:
-                f += P[(l, m)] * (a * np.cos(m * lon) + b * np.sin(m * lon))
+                f += P[(l, m)] * (a * cm[m] + b * sm[m])
     return f
 
 

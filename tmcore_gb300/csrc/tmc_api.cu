@@ -44,9 +44,13 @@ struct EngineBase {
   virtual int launches_per_step() const = 0;
   virtual void adv_set_initial_dev(const double* raw_q) = 0;  // adv model: gd <- q, wind at t = 0
   virtual void adv_get_dev(double* raw_q, double* raw_u) = 0;
+  virtual void state_slot0(void** gd, void** iap, void** q, void** ghs) = 0;  // all members
+  virtual void refresh_all_shadows() = 0;
 };
 
 enum Field { F_GD = 0, F_IAP, F_U, F_PV_V, F_VOR, F_TEND_GD, F_TEND_IAP, F_GD_STAGE };
+// passes of the fused step (block sizes, timing)
+enum Pass { P_CELL = 0, P_VERTEX, P_PV, P_FLUX, P_FINAL, P_COUNT };
 
 }  // namespace
 
@@ -84,6 +88,10 @@ struct tmc_handle {
   const double* d_latV = nullptr;
   const double* d_lonV = nullptr;
   std::vector<cudaEvent_t> ev_pool;
+  // block size per pass of the fused step (cell, vertex, edge_pv, edge_flux,
+  // final), chosen by tmc_autotune; the partial-sum counts follow them
+  int bsp[5] = {256, 256, 256, 256, 256};
+  int timed_pass = 3;  // the pass tmc_time_steps brackets with events
 
   template <class X>
   X* dalloc(size_t n) {
@@ -297,7 +305,7 @@ struct Engine : EngineBase {
   // pass keeps it current.
   void launch_prep() override {
     StageIO<T> s = io(0);
-    launch_edge_prep<T>(h->M, h->O, s, h->P, true, h->bs, h->st);
+    launch_edge_prep<T>(h->M, h->O, s, h->P, true, h->bsp[P_FINAL], h->st);
   }
 
   // one CRK4 step (time_scheme_mod.F90:109-154); state(old) updated in place.
@@ -317,17 +325,29 @@ struct Engine : EngineBase {
       s.gd_v = nullptr;
       const bool dg = diag && k == 1;
       RKStage rk{k, adt[k]};
-      launch_cell<T>(M, O, s, rk, h->P, dg, h->bs, h->st);
-      launch_vertex<T>(M, O, s, h->P, dg, h->bs, h->st);
-      launch_edge_pv<T>(M, O, s, h->bs, h->st);
-      if (O.pv_scheme == 2) launch_cons_apvm<T>(M, O, s, h->P, h->d_diag, h->bs, h->st);
-      if (flux_ev) cudaEventRecord((*flux_ev)[(*ev_pos)++], h->st);
-      launch_edge_flux<T>(M, O, s, rk, h->P, h->bs, h->st);
-      if (flux_ev) cudaEventRecord((*flux_ev)[(*ev_pos)++], h->st);
+      const int* b = h->bsp;
+      auto mark = [&](int pass) {
+        if (flux_ev && h->timed_pass == pass) cudaEventRecord((*flux_ev)[(*ev_pos)++], h->st);
+      };
+      mark(P_CELL);
+      launch_cell<T>(M, O, s, rk, h->P, dg, b[P_CELL], h->st);
+      mark(P_CELL);
+      mark(P_VERTEX);
+      launch_vertex<T>(M, O, s, h->P, dg, b[P_VERTEX], h->st);
+      mark(P_VERTEX);
+      mark(P_PV);
+      launch_edge_pv<T>(M, O, s, b[P_PV], h->st);
+      if (O.pv_scheme == 2) launch_cons_apvm<T>(M, O, s, h->P, h->d_diag, b[P_VERTEX], h->st);
+      mark(P_PV);
+      mark(P_FLUX);
+      launch_edge_flux<T>(M, O, s, rk, h->P, b[P_FLUX], h->st);
+      mark(P_FLUX);
     }
     launch_finalize(h->P, h->counts, h->hm.totalArea, h->hm.sumAreaTriangle, dt, true, diag,
                     h->p.conserve_energy != 0, h->d_diag, h->st, 2, h->members);
-    launch_final_update<T>(M, O, io(0), h->d_diag, h->P, h->bs, h->st);
+    if (flux_ev && h->timed_pass == P_FINAL) cudaEventRecord((*flux_ev)[(*ev_pos)++], h->st);
+    launch_final_update<T>(M, O, io(0), h->d_diag, h->P, h->bsp[P_FINAL], h->st);
+    if (flux_ev && h->timed_pass == P_FINAL) cudaEventRecord((*flux_ev)[(*ev_pos)++], h->st);
   }
 
   // ---- generic integrator program (time_scheme_mod.F90:65-107 CRK3,
@@ -464,9 +484,9 @@ struct Engine : EngineBase {
     }
     StageIO<T> s = io(0);
     RKStage rk{0, 0.0};
-    launch_edge_prep<T>(h->M, h->O, s, h->P, true, h->bs, h->st);
-    launch_cell<T>(h->M, h->O, s, rk, h->P, true, h->bs, h->st);
-    launch_vertex<T>(h->M, h->O, s, h->P, true, h->bs, h->st);
+    launch_edge_prep<T>(h->M, h->O, s, h->P, true, h->bsp[P_FINAL], h->st);
+    launch_cell<T>(h->M, h->O, s, rk, h->P, true, h->bsp[P_CELL], h->st);
+    launch_vertex<T>(h->M, h->O, s, h->P, true, h->bsp[P_VERTEX], h->st);
     if (finalize)
       launch_finalize(h->P, h->counts, h->hm.totalArea, h->hm.sumAreaTriangle, h->O.dt, false, true,
                       h->p.conserve_energy != 0, h->d_diag, h->st, 2, h->members);
@@ -487,6 +507,23 @@ struct Engine : EngineBase {
     launch_edge_pv<T>(h->M, h->O, s, h->bs, h->st);
     if (h->O.pv_scheme == 2) launch_cons_apvm<T>(h->M, h->O, s, h->P, h->d_diag, h->bs, h->st);
     launch_edge_flux<T>(h->M, h->O, s, rk, h->P, h->bs, h->st);
+  }
+
+  void state_slot0(void** g, void** i, void** qq, void** gh) override {
+    *g = gd[0];
+    *i = iap[0];
+    *qq = q[0];
+    *gh = ghs;
+  }
+  void refresh_all_shadows() override {
+    if constexpr (!std::is_same<T, double>::value) {
+      const int save = h->cur;
+      for (int m = 0; m < h->members; ++m) {
+        h->cur = m;
+        refresh_shadows(0);
+      }
+      h->cur = save;
+    }
   }
 
   // offsets of the selected member's arrays
@@ -561,6 +598,19 @@ int build_graph(tmc_handle* h, bool diag, cudaGraphExec_t* out) {
   cudaGraphDestroy(g);
   if (e != cudaSuccess) return h->fail(TMC_E_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
   return TMC_OK;
+}
+
+// partial counts per region: the grid of the passes that write it
+void set_counts(tmc_handle* h) {
+  const int bc = grid_for(h->M.nc, h->bsp[P_CELL]), bf = grid_for(h->M.ne, h->bsp[P_FLUX]),
+            bfin = grid_for(h->M.ne, h->bsp[P_FINAL]), bv = grid_for(h->M.nv, h->bsp[P_VERTEX]);
+  static const int cells[6] = {R_IP_C, R_IP_C + 2, R_IP_C + 4, R_44_C, R_MASS, R_EN_C};
+  static const int edges[4] = {R_IP_E, R_IP_E + 2, R_IP_E + 4, R_44_E};
+  static const int verts[5] = {R_PE, R_AV, R_C1, R_C2, R_C3};
+  for (int r : cells) h->counts[r] = bc;
+  for (int r : edges) h->counts[r] = bf;
+  h->counts[R_EN_E] = bfin;
+  for (int r : verts) h->counts[r] = bv;
 }
 
 void ensure_prep(tmc_handle* h) {
@@ -799,14 +849,9 @@ int tmc_create(const tmc_mesh_desc* mesh, const tmc_params* params, tmc_handle**
   const int minbs = 32;
   h->P.cap = (nmax + minbs - 1) / minbs;
   h->P.base = h->dalloc<double>(h->P.member_stride() * h->members);
-  const int bc = grid_for(hm.nc, h->bs), be = grid_for(hm.ne, h->bs), bv = grid_for(hm.nv, h->bs);
-  const int rc_cells[6] = {R_IP_C, R_IP_C + 2, R_IP_C + 4, R_44_C, R_MASS, R_EN_C};
-  const int rc_edges[5] = {R_IP_E, R_IP_E + 2, R_IP_E + 4, R_44_E, R_EN_E};
-  for (int r : rc_cells) h->counts[r] = bc;
-  for (int r : rc_edges) h->counts[r] = be;
-  h->counts[R_PE] = bv;
-  h->counts[R_AV] = bv;
-  for (int r = R_C1; r <= R_C3; ++r) h->counts[r] = bv;
+  for (int k = 0; k < P_COUNT; ++k) h->bsp[k] = h->bs;
+  set_counts(h.get());
+  const int bc = grid_for(hm.nc, h->bs);
   for (int r = 0; r < R_COUNT; ++r) h->gen_counts[r] = h->counts[r];
   if (h->adv)  // the invariant pass of the adv model is the mass alone, over cells
     for (int r = R_MASS; r <= R_AV; ++r) h->gen_counts[r] = bc;
@@ -1213,6 +1258,95 @@ int tmc_adv_elapsed(tmc_handle* h, double* seconds) {
   if ((rc = sync(h, "tmc_adv_elapsed"))) return rc;
   *seconds = h->h_diag[11];
   return TMC_OK;
+}
+
+int tmc_autotune(tmc_handle* h, int32_t steps, int32_t block_sizes[5]) {
+  TMC_REQUIRE_HANDLE(h);
+  if (!h->have_state) return h->fail(TMC_E_STATE, "tmc_autotune needs a state (tmc_set_initial)");
+  if (h->generic) return h->fail(TMC_E_UNSUP, "tmc_autotune tunes the fused CRK4 shallow-water step");
+  if (steps <= 0) steps = 3;
+  int rc;
+  if ((rc = sync(h, "tmc_autotune"))) return rc;
+  // save state(old) of every member; the timing steps advance it
+  const size_t M_ = (size_t)h->members;
+  const bool f32 = h->p.precision == TMC_FP32;
+  const size_t es = f32 ? sizeof(float) : sizeof(double);
+  const size_t nq = (size_t)h->M.nc * (h->O.n_tracers > 0 ? h->O.n_tracers : 1);
+  void *sv_gd = nullptr, *sv_iap = nullptr, *sv_q = nullptr;
+  void *gd0, *iap0, *q0, *ghs0;
+  h->eng->state_slot0(&gd0, &iap0, &q0, &ghs0);
+  const size_t b_gd = 8 * h->M.nc * M_, b_iap = es * h->M.ne * M_, b_q = es * nq * M_;
+  if (cudaMalloc(&sv_gd, b_gd) != cudaSuccess || cudaMalloc(&sv_iap, b_iap) != cudaSuccess ||
+      cudaMalloc(&sv_q, b_q) != cudaSuccess) {
+    cudaFree(sv_gd);
+    cudaFree(sv_iap);
+    cudaFree(sv_q);
+    return h->cuda_check("tmc_autotune: scratch allocation");
+  }
+  cudaMemcpyAsync(sv_gd, gd0, b_gd, cudaMemcpyDeviceToDevice, h->st);
+  cudaMemcpyAsync(sv_iap, iap0, b_iap, cudaMemcpyDeviceToDevice, h->st);
+  cudaMemcpyAsync(sv_q, q0, b_q, cudaMemcpyDeviceToDevice, h->st);
+  const size_t nev = (size_t)steps * 8 + 2;
+  while (h->ev_pool.size() < nev) {
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) return h->cuda_check("cudaEventCreate");
+    h->ev_pool.push_back(e);
+  }
+  const int cand_all[6] = {64, 128, 192, 256, 384, 512};
+  const int limit = h->members > 1 ? 256 : 512;
+  const int order[P_COUNT] = {P_FLUX, P_CELL, P_VERTEX, P_PV, P_FINAL};
+  const int saved_timed = h->timed_pass;
+  for (int pi = 0; pi < P_COUNT; ++pi) {
+    const int pass = order[pi];
+    h->timed_pass = pass;
+    double best = 1e300;
+    int best_bs = h->bsp[pass];
+    for (int c : cand_all) {
+      if (c > limit) continue;
+      h->bsp[pass] = c;
+      set_counts(h);
+      // one untimed step with this block size, then `steps` timed ones
+      h->prep_valid = false;
+      ensure_prep(h);
+      h->eng->launch_step(false, nullptr, nullptr);
+      std::vector<cudaEvent_t> evs(h->ev_pool.begin(), h->ev_pool.begin() + nev);
+      size_t pos = 0;
+      for (int i = 0; i < steps; ++i) h->eng->launch_step(false, &evs, &pos);
+      if ((rc = sync(h, "tmc_autotune"))) break;
+      double sum = 0.0;
+      for (size_t k = 0; k + 1 < pos; k += 2) {
+        float dt = 0.f;
+        cudaEventElapsedTime(&dt, evs[k], evs[k + 1]);
+        sum += dt;
+      }
+      if (sum < best) {
+        best = sum;
+        best_bs = c;
+      }
+    }
+    if (rc) break;
+    h->bsp[pass] = best_bs;
+  }
+  h->timed_pass = saved_timed;
+  set_counts(h);
+  // restore the state and drop the graphs captured with the old block sizes
+  cudaMemcpyAsync(gd0, sv_gd, b_gd, cudaMemcpyDeviceToDevice, h->st);
+  cudaMemcpyAsync(iap0, sv_iap, b_iap, cudaMemcpyDeviceToDevice, h->st);
+  cudaMemcpyAsync(q0, sv_q, b_q, cudaMemcpyDeviceToDevice, h->st);
+  h->eng->refresh_all_shadows();
+  h->prep_valid = false;
+  int rc2 = sync(h, "tmc_autotune");
+  cudaFree(sv_gd);
+  cudaFree(sv_iap);
+  cudaFree(sv_q);
+  if (h->g_step) cudaGraphExecDestroy(h->g_step);
+  if (h->g_step_diag) cudaGraphExecDestroy(h->g_step_diag);
+  h->g_step = h->g_step_diag = nullptr;
+  if (rc) return rc;
+  if (rc2) return rc2;
+  if (block_sizes)
+    for (int k = 0; k < P_COUNT; ++k) block_sizes[k] = h->bsp[k];
+  return h->cuda_check("tmc_autotune");
 }
 
 int tmc_sizes(const tmc_handle* h, int64_t* nc, int64_t* ne, int64_t* nv, int64_t* bytes) {

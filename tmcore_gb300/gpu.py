@@ -120,6 +120,13 @@ class TMCoreGPU:
         self._chk(self.lib.tmc_get_tracers(self.h, _ptr(q)))
         return q
 
+    def autotune(self, steps: int = 3):
+        """Per-pass block sizes by timing (tmc_autotune); returns
+        {cell, vertex, edge_pv, edge_flux, final}."""
+        out = (ctypes.c_int32 * 5)()
+        self._chk(self.lib.tmc_autotune(self.h, int(steps), out))
+        return dict(zip(("cell", "vertex", "edge_pv", "edge_flux", "final"), list(out)))
+
     # ------------------------------------------------------------------ ensembles
     def select_member(self, m: int):
         """State-transfer calls address member m of an ensemble (members > 1)."""
