@@ -53,6 +53,8 @@ def parse():
                     help="FP32 ensemble on --ensemble-level (0: skip)")
     ap.add_argument("--ensemble-level", type=int, default=6)
     ap.add_argument("--ensemble-steps", type=int, default=20)
+    ap.add_argument("--mixed-members", type=int, default=16, help="members per level of the mixed batch (0: skip)")
+    ap.add_argument("--mixed-cycles", type=int, default=5)
     return ap.parse_args()
 
 
@@ -234,12 +236,57 @@ def _ensemble_ic(job):
     return cases.jet_bumps(mesh.icos_mesh(level), seed=seed)
 
 
-def ensemble_ics(level: int, members: int):
-    """Seeds 0..members-1, generated by a spawn pool (started before any CUDA work)."""
+def ensemble_ics(level: int, members: int, mixed_levels=(), mixed_members: int = 0):
+    """Seeds 0..members-1 on `level`, and seeds 0..mixed_members-1 on each of
+    `mixed_levels`, generated by a spawn pool (started before any CUDA work)."""
     import multiprocessing as mp
 
+    jobs = [(level, s) for s in range(members)] + [(L, s) for L in mixed_levels for s in range(mixed_members)]
     with mp.get_context("spawn").Pool(min(16, os.cpu_count() or 1)) as pool:
-        return pool.map(_ensemble_ic, [(level, s) for s in range(members)], chunksize=8)
+        out = pool.map(_ensemble_ic, jobs, chunksize=4)
+    mixed = {L: out[members + i * mixed_members: members + (i + 1) * mixed_members]
+             for i, L in enumerate(mixed_levels)}
+    return out[:members], mixed
+
+
+def run_mixed(args, local, ics_by_level, peak):
+    """Config 3, mixed batch: ensembles on mesh levels 4-7 with dt = 1200 / 2^(L-4) s,
+    advanced together as one CUDA graph per 1200-s cycle (tmc_group)."""
+    from tmcore_gb300 import abi, mesh
+    from tmcore_gb300.gpu import TMCoreGPU, TMCoreGroup
+
+    models, bytes_cycle, members, desc = [], 0.0, 0, []
+    for L, ics in sorted(ics_by_level.items()):
+        m = mesh.icos_mesh(L)
+        dt = 1200.0 / 2 ** (L - 4)
+        e = TMCoreGPU(m, members=len(ics), dt=dt, pv_scheme=1, apvm_weight=0.0, adv_order=2, conserve_energy=1,
+                      precision=abi.TMC_FP32, diag_every=0, use_graph=1, renumber=1, device=local)
+        for k, (gd, u, ghs) in enumerate(ics):
+            e.select_member(k)
+            e.set_initial(gd, u, ghs)
+        if not args.no_autotune:
+            e.autotune(steps=2)
+        models.append(e)
+        members += len(ics)
+        bytes_cycle += (1200.0 / dt) * ensemble_model_bytes(m.nCells, m.nEdges, m.nVertices, 4, len(ics))
+        desc.append(f"L{L}x{len(ics)} dt={dt:g}s")
+    grp = TMCoreGroup(models, cycle_seconds=1200.0)
+    grp.run(1)
+    grp.synchronize()
+    cycles = args.mixed_cycles
+    t = time.perf_counter()
+    grp.run(cycles)
+    grp.synchronize()
+    el = time.perf_counter() - t
+    grp.close()
+    for e in models:
+        e.close()
+    cyc_s = el / cycles
+    return {"workload": "mixed batch " + ", ".join(desc) + ", one CUDA graph per 1200-s cycle",
+            "members": members, "cycles": cycles, "ms_per_cycle": cyc_s * 1e3,
+            "member_days_per_s": members * 1200.0 / DAY / cyc_s, "sim_days_per_s": 1200.0 / DAY / cyc_s,
+            "scope_model_bytes_per_cycle": bytes_cycle, "achieved_gbs": bytes_cycle / cyc_s / 1e9,
+            "frac": bytes_cycle / cyc_s / 1e9 / peak, "timing": "host wall clock around tmc_group_run + sync"}
 
 
 def run_ensemble(args, local, ics, peak):
@@ -370,7 +417,12 @@ def main():
     from tmcore_gb300.gpu import TMCoreGPU
 
     # ensemble initial states from a spawn pool, before any CUDA work
-    ens_ics = ensemble_ics(args.ensemble_level, args.ensemble_members) if args.ensemble_members > 0 else None
+    ens_ics, mixed_ics = None, None
+    if args.ensemble_members > 0 or args.mixed_members > 0:
+        ens_ics, mixed_ics = ensemble_ics(args.ensemble_level, max(args.ensemble_members, 0),
+                                          (4, 5, 6, 7) if args.mixed_members > 0 else (), args.mixed_members)
+        if args.ensemble_members <= 0:
+            ens_ics = None
     dist = Dist(world)
     m, gd, u, ghs, q, t_setup = setup(args)
     args.seed += rank  # independent replicas
@@ -472,6 +524,9 @@ def main():
     if ens_ics is not None:
         extra["ensemble"] = run_ensemble(args, local, ens_ics, peak)
         ens_ics = None
+    if mixed_ics:
+        extra["mixed_batch"] = run_mixed(args, local, mixed_ics, peak)
+        mixed_ics = None
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:

@@ -145,6 +145,20 @@ int tmc_autotune(tmc_handle* h, int32_t steps, int32_t block_sizes[5]);
  * tmc_spatial_operators need members <= 1. */
 int tmc_select_member(tmc_handle* h, int32_t member);
 
+/* Groups: several handles (different meshes and dt, each possibly an
+ * ensemble) advanced together, e.g. a mixed batch of mesh levels with
+ * dt = 1200 / 2^(level-4) s.  One CUDA graph per cycle of cycle_seconds holds
+ * one independent branch per handle with cycle_seconds / dt steps (which must
+ * be whole), so the handles' kernels run concurrently.  tmc_group_run is
+ * asynchronous; later calls on a member handle are ordered after it.  The
+ * handles must outlive the group and must not change their state size. */
+typedef struct tmc_group tmc_group;
+int tmc_group_create(tmc_handle* const* handles, int32_t n, double cycle_seconds, tmc_group** out);
+int tmc_group_run(tmc_group* g, int32_t cycles);
+int tmc_group_synchronize(tmc_group* g);
+const char* tmc_group_last_error(const tmc_group* g);
+int tmc_group_destroy(tmc_group* g);
+
 /* The adv model (tmcore_adv_mod.F90, adv_wind = 1 or 2, FP64): one
  * advected scalar in place of gd, transported by the prescribed wind that
  * update_state re-sets at elapsed + the stage's dt (tmcore_adv_mod.F90:87-97);

@@ -97,3 +97,34 @@ def test_autotune_keeps_state_and_results(mesh5, members):
         assert np.all(np.isfinite(ua))
     a.close()
     b.close()
+
+
+def test_group_of_levels_matches_separate_runs(mesh3, mesh4):
+    """A mixed batch (two mesh levels, dt = 600 / 300 s, ensembles of 2):
+    one graph per 600-s cycle equals stepping each model on its own."""
+    from tmcore_gb300.gpu import TMCoreGPU, TMCoreGroup
+
+    spec = [(mesh3, 600.0), (mesh4, 300.0)]
+    grouped, alone = [], []
+    for mesh, dt in spec:
+        kw = dict(dt=dt, precision=1, pv_scheme=1, apvm_weight=0.0, members=2)
+        g, a = TMCoreGPU(mesh, **kw), TMCoreGPU(mesh, **kw)
+        for m in range(2):
+            gd, u, ghs = _ic(mesh, seed=60 + m)
+            for x in (g, a):
+                x.select_member(m)
+                x.set_initial(gd, u, ghs)
+        grouped.append(g)
+        alone.append(a)
+    grp = TMCoreGroup(grouped, cycle_seconds=600.0)
+    grp.run(3)
+    for (mesh, dt), g, a in zip(spec, grouped, alone):
+        a.step(int(3 * 600.0 / dt))
+        for m in range(2):
+            g.select_member(m)
+            a.select_member(m)
+            sg, sa = g.get_state(), a.get_state()
+            assert all(np.array_equal(x, y) for x, y in zip(sg, sa))
+    grp.close()
+    for x in grouped + alone:
+        x.close()

@@ -77,6 +77,11 @@ SYMBOLS = {
     "tmc_sizes": (ctypes.c_int, [vp, i64p, i64p, i64p, i64p]),
     "tmc_select_member": (ctypes.c_int, [vp, i32]),
     "tmc_autotune": (ctypes.c_int, [vp, i32, ctypes.POINTER(i32)]),
+    "tmc_group_create": (ctypes.c_int, [ctypes.POINTER(vp), i32, ctypes.c_double, ctypes.POINTER(vp)]),
+    "tmc_group_run": (ctypes.c_int, [vp, i32]),
+    "tmc_group_synchronize": (ctypes.c_int, [vp]),
+    "tmc_group_last_error": (ctypes.c_char_p, [vp]),
+    "tmc_group_destroy": (ctypes.c_int, [vp]),
     "tmc_adv_set_initial": (ctypes.c_int, [vp, vp]),
     "tmc_adv_get": (ctypes.c_int, [vp, vp, vp]),
     "tmc_adv_elapsed": (ctypes.c_int, [vp, dp]),

@@ -3,6 +3,7 @@
 // caller's element order, timing.
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <memory>
@@ -1347,6 +1348,136 @@ int tmc_autotune(tmc_handle* h, int32_t steps, int32_t block_sizes[5]) {
   if (block_sizes)
     for (int k = 0; k < P_COUNT; ++k) block_sizes[k] = h->bsp[k];
   return h->cuda_check("tmc_autotune");
+}
+
+}  // extern "C"
+
+// A group of handles (different meshes, each possibly an ensemble) advanced
+// together: one CUDA graph per cycle of `cycle_seconds`, with one branch per
+// handle that runs cycle_seconds / dt steps of that handle; the branches are
+// independent, so the levels' kernels overlap on the GPU.
+struct tmc_group {
+  std::vector<tmc_handle*> hs;
+  std::vector<int> steps;  // per handle and cycle
+  cudaStream_t st = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_done = nullptr;
+  std::vector<cudaEvent_t> ev_join;
+  cudaGraphExec_t graph = nullptr;
+  std::string err;
+};
+
+extern "C" {
+
+int tmc_group_create(tmc_handle* const* handles, int32_t n, double cycle_seconds, tmc_group** out) {
+  if (!out || !handles || n <= 0 || !(cycle_seconds > 0.0)) return TMC_E_ARG;
+  *out = nullptr;
+  auto g = std::make_unique<tmc_group>();
+  for (int i = 0; i < n; ++i) {
+    tmc_handle* h = handles[i];
+    if (!h || !h->eng) return TMC_E_ARG;
+    if (h->generic) {
+      h->err = "tmc_group_create: groups run the fused CRK4 shallow-water step";
+      return TMC_E_UNSUP;
+    }
+    if (!h->have_state) {
+      h->err = "tmc_group_create: set the state first";
+      return TMC_E_STATE;
+    }
+    const double k = cycle_seconds / h->O.dt;
+    const int ki = (int)(k + 0.5);
+    if (ki < 1 || std::fabs(k - ki) > 1e-9 * k) {
+      h->err = "tmc_group_create: cycle_seconds must be a whole number of this handle's dt";
+      return TMC_E_ARG;
+    }
+    for (tmc_handle* o : g->hs)
+      if (o == h) return TMC_E_ARG;
+    g->hs.push_back(h);
+    g->steps.push_back(ki);
+  }
+  auto cerr = [&](const char* where) {
+    cudaError_t e = cudaGetLastError();
+    g->err = std::string(where) + ": " + cudaGetErrorString(e);
+    *out = g.release();
+    return TMC_E_CUDA;
+  };
+  if (cudaStreamCreateWithFlags(&g->st, cudaStreamNonBlocking) != cudaSuccess) return cerr("cudaStreamCreate");
+  if (cudaEventCreateWithFlags(&g->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&g->ev_done, cudaEventDisableTiming) != cudaSuccess)
+    return cerr("cudaEventCreate");
+  g->ev_join.resize(n);
+  for (auto& e : g->ev_join)
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return cerr("cudaEventCreate");
+  // every handle's edge preparation is current before capture
+  for (tmc_handle* h : g->hs) {
+    ensure_prep(h);
+    if (cudaStreamSynchronize(h->st) != cudaSuccess) return cerr("cudaStreamSynchronize");
+  }
+  cudaGraph_t graph = nullptr;
+  if (cudaStreamBeginCapture(g->st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return cerr("BeginCapture");
+  cudaEventRecord(g->ev_fork, g->st);
+  for (int i = 0; i < n; ++i) {
+    tmc_handle* h = g->hs[i];
+    cudaStreamWaitEvent(h->st, g->ev_fork, 0);
+    for (int k = 0; k < g->steps[i]; ++k) h->eng->launch_step(false, nullptr, nullptr);
+    cudaEventRecord(g->ev_join[i], h->st);
+    cudaStreamWaitEvent(g->st, g->ev_join[i], 0);
+  }
+  if (cudaStreamEndCapture(g->st, &graph) != cudaSuccess) return cerr("EndCapture");
+  cudaError_t e = cudaGraphInstantiate(&g->graph, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return cerr("cudaGraphInstantiate");
+  *out = g.release();
+  return TMC_OK;
+}
+
+int tmc_group_run(tmc_group* g, int32_t cycles) {
+  if (!g || !g->graph || cycles < 0) return TMC_E_ARG;
+  // the group's stream starts after all work already queued on the handles
+  for (size_t i = 0; i < g->hs.size(); ++i) {
+    cudaEventRecord(g->ev_join[i], g->hs[i]->st);
+    cudaStreamWaitEvent(g->st, g->ev_join[i], 0);
+  }
+  for (int c = 0; c < cycles; ++c)
+    if (cudaGraphLaunch(g->graph, g->st) != cudaSuccess) {
+      g->err = std::string("cudaGraphLaunch: ") + cudaGetErrorString(cudaGetLastError());
+      return TMC_E_CUDA;
+    }
+  // later calls on each handle are ordered after the group's work
+  cudaEventRecord(g->ev_done, g->st);
+  for (size_t i = 0; i < g->hs.size(); ++i) {
+    cudaStreamWaitEvent(g->hs[i]->st, g->ev_done, 0);
+    g->hs[i]->step_count += (long)g->steps[i] * cycles;
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    g->err = cudaGetErrorString(e);
+    return TMC_E_CUDA;
+  }
+  return TMC_OK;
+}
+
+int tmc_group_synchronize(tmc_group* g) {
+  if (!g) return TMC_E_ARG;
+  cudaError_t e = cudaStreamSynchronize(g->st);
+  if (e != cudaSuccess) {
+    g->err = cudaGetErrorString(e);
+    return TMC_E_CUDA;
+  }
+  return TMC_OK;
+}
+
+const char* tmc_group_last_error(const tmc_group* g) { return g ? g->err.c_str() : "null group"; }
+
+int tmc_group_destroy(tmc_group* g) {
+  if (!g) return TMC_OK;
+  if (g->st) cudaStreamSynchronize(g->st);
+  if (g->graph) cudaGraphExecDestroy(g->graph);
+  for (cudaEvent_t e : g->ev_join) cudaEventDestroy(e);
+  if (g->ev_fork) cudaEventDestroy(g->ev_fork);
+  if (g->ev_done) cudaEventDestroy(g->ev_done);
+  if (g->st) cudaStreamDestroy(g->st);
+  delete g;
+  return TMC_OK;
 }
 
 int tmc_sizes(const tmc_handle* h, int64_t* nc, int64_t* ne, int64_t* nv, int64_t* bytes) {

@@ -209,3 +209,43 @@ class TMCoreGPU:
         self._chk(self.lib.tmc_op_upwind_correction(self.h, _ptr(_f64(f_cell)), _ptr(_f64(u_edge)), _ptr(fe),
                                                     int(order), int(mono)))
         return fe
+
+
+class TMCoreGroup:
+    """Several models (different meshes and dt) advanced together: one CUDA
+    graph per cycle of ``cycle_seconds`` with one branch per model
+    (tmc_group_*)."""
+
+    def __init__(self, models, cycle_seconds: float):
+        self.lib = _lib.gpu()
+        self.models = list(models)
+        arr = (ctypes.c_void_p * len(self.models))(*[m.h.value for m in self.models])
+        g = ctypes.c_void_p()
+        rc = self.lib.tmc_group_create(arr, len(self.models), float(cycle_seconds), ctypes.byref(g))
+        self.g = g
+        if rc != 0:
+            msg = self.lib.tmc_group_last_error(g).decode() if g.value else \
+                "; ".join(m.lib.tmc_last_error(m.h).decode() for m in self.models)
+            self.close()
+            raise TMCError(rc, msg)
+
+    def run(self, cycles: int = 1):
+        rc = self.lib.tmc_group_run(self.g, int(cycles))
+        if rc != 0:
+            raise TMCError(rc, self.lib.tmc_group_last_error(self.g).decode())
+
+    def synchronize(self):
+        rc = self.lib.tmc_group_synchronize(self.g)
+        if rc != 0:
+            raise TMCError(rc, self.lib.tmc_group_last_error(self.g).decode())
+
+    def close(self):
+        if getattr(self, "g", None) is not None and self.g.value:
+            self.lib.tmc_group_destroy(self.g)
+        self.g = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
