@@ -145,6 +145,31 @@ int tmc_autotune(tmc_handle* h, int32_t steps, int32_t block_sizes[5]);
  * tmc_spatial_operators need members <= 1. */
 int tmc_select_member(tmc_handle* h, int32_t member);
 
+/* The learned PV-on-edge closure network: 24 -> 64 -> 64 -> 64 -> 1 with
+ * GELU (tanh form) between hidden layers; TMC_MLP_PARAMS FP32 master
+ * parameters in the order W1[64][24], b1[64], W2[64][64], b2[64],
+ * W3[64][64], b3[64], W4[64], b4, used as BF16 weights (FP32 biases) with
+ * FP32 accumulation.  Inputs are normalised as (x - x_mean) * x_inv_std and
+ * the output is scaled by y_scale.  tmc_mlp_forward runs on the tensor cores
+ * (tensor_cores = 1) or the CUDA cores (0); training is Adam (lr, beta1 0.9,
+ * beta2 0.999, eps 1e-8) on the mean squared error over consecutive batches
+ * of the stored dataset.  Arrays are host pointers. */
+#define TMC_MLP_PARAMS 9985
+#define TMC_MLP_FEATURES 24
+typedef struct tmc_mlp tmc_mlp;
+int tmc_mlp_create(int32_t device, uint64_t seed, tmc_mlp** out);
+int tmc_mlp_destroy(tmc_mlp* n);
+const char* tmc_mlp_last_error(const tmc_mlp* n);
+int tmc_mlp_get_params(tmc_mlp* n, float* params);
+int tmc_mlp_set_params(tmc_mlp* n, const float* params);
+int tmc_mlp_set_scaling(tmc_mlp* n, const float* x_mean, const float* x_inv_std, float y_scale);
+int tmc_mlp_forward(tmc_mlp* n, const float* x, int64_t rows, float* y, int32_t tensor_cores);
+int tmc_mlp_set_dataset(tmc_mlp* n, const float* x, const float* y, int64_t rows);
+int tmc_mlp_train(tmc_mlp* n, int32_t batch, int32_t steps, float lr, float* losses);
+/* gradient of the mean squared error over rows (a multiple of 128) w.r.t.
+ * the parameters, without updating them */
+int tmc_mlp_gradient(tmc_mlp* n, const float* x, const float* y, int64_t rows, float* grad, double* loss);
+
 /* Groups: several handles (different meshes and dt, each possibly an
  * ensemble) advanced together, e.g. a mixed batch of mesh levels with
  * dt = 1200 / 2^(level-4) s.  One CUDA graph per cycle of cycle_seconds holds

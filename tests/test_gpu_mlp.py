@@ -1,0 +1,113 @@
+"""The closure network (tmc_mlp_*): tensor-core forward against a numpy
+model of the same arithmetic (BF16 weights and layer inputs, FP32
+accumulation, tanh-form GELU), CUDA-core forward and gradient against numpy
+in FP64, and Adam training that fits a smooth target."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+NIN, NH = 24, 64
+
+
+def bf16(a):
+    a = np.ascontiguousarray(a, np.float32)
+    u = a.view(np.uint32).astype(np.uint64)
+    u = (u + 0x7FFF + ((u >> 16) & 1)) >> 16 << 16
+    return u.astype(np.uint32).view(np.float32)
+
+
+def unpack(p):
+    o = 0
+    out = {}
+    for name, shape in (("W1", (NH, NIN)), ("b1", (NH,)), ("W2", (NH, NH)), ("b2", (NH,)), ("W3", (NH, NH)),
+                        ("b3", (NH,)), ("W4", (NH,)), ("b4", (1,))):
+        n = int(np.prod(shape))
+        out[name] = p[o:o + n].reshape(shape)
+        o += n
+    assert o == p.size
+    return out
+
+
+def gelu(z):
+    return 0.5 * z * (1.0 + np.tanh(0.7978845608028654 * (z + 0.044715 * z ** 3)))
+
+
+def gelu_grad(z):
+    t = np.tanh(0.7978845608028654 * (z + 0.044715 * z ** 3))
+    return 0.5 * (1 + t) + 0.5 * z * (1 - t * t) * 0.7978845608028654 * (1 + 3 * 0.044715 * z * z)
+
+
+def forward_np(p, x, round_act):
+    P = unpack(p)
+    W = {k: bf16(P[k]).astype(np.float64) for k in ("W1", "W2", "W3", "W4")}
+    r = (lambda a: bf16(a).astype(np.float64)) if round_act else (lambda a: a)
+    h = r(x.astype(np.float64))
+    zs = []
+    for i, (Wk, bk) in enumerate((("W1", "b1"), ("W2", "b2"), ("W3", "b3"))):
+        z = h @ W[Wk].T + P[bk].astype(np.float64)
+        zs.append(z)
+        h = gelu(z)
+        if i < 2:
+            h = r(h)
+    return h @ W["W4"] + float(P["b4"][0]), zs, W
+
+
+def test_tensor_core_forward_matches_model():
+    from tmcore_gb300.gpu import ClosureMLP
+
+    net = ClosureMLP(seed=3)
+    rng = np.random.default_rng(0)
+    x = rng.standard_normal((1000, NIN)).astype(np.float32)  # a partial last tile
+    p = net.params
+    y_tc = net.forward(x, tensor_cores=True)
+    y_ref, _, _ = forward_np(p, x, round_act=True)
+    scale = np.max(np.abs(y_ref))
+    assert np.max(np.abs(y_tc - y_ref)) < 1e-2 * scale
+    y_simt = net.forward(x, tensor_cores=False)
+    y_fp, _, _ = forward_np(p, x, round_act=False)
+    assert np.max(np.abs(y_simt - y_fp)) < 1e-4 * np.max(np.abs(y_fp))
+    net.close()
+
+
+def test_gradient_matches_numpy():
+    from tmcore_gb300.gpu import ClosureMLP
+
+    net = ClosureMLP(seed=5)
+    rng = np.random.default_rng(1)
+    x = rng.standard_normal((256, NIN)).astype(np.float32)
+    t = rng.standard_normal(256).astype(np.float32)
+    g, loss = net.gradient(x, t)
+    p = net.params
+    y, zs, W = forward_np(p, x, round_act=False)
+    e = y - t
+    assert abs(loss - np.mean(e ** 2)) < 1e-4 * np.mean(e ** 2)
+    dy = 2 * e / len(t)
+    h = [x.astype(np.float64), gelu(zs[0]), gelu(zs[1]), gelu(zs[2])]
+    ref = {"W4": dy @ h[3], "b4": np.array([dy.sum()])}
+    dz = np.outer(dy, W["W4"]) * gelu_grad(zs[2])
+    for layer in (3, 2, 1):
+        ref[f"W{layer}"] = dz.T @ h[layer - 1]
+        ref[f"b{layer}"] = dz.sum(0)
+        if layer > 1:
+            dz = (dz @ W[f"W{layer}"]) * gelu_grad(zs[layer - 2])
+    G = unpack(g)
+    for k, v in ref.items():
+        assert np.max(np.abs(G[k] - v)) < 2e-3 * np.max(np.abs(v)) + 1e-7, k
+    net.close()
+
+
+def test_adam_training_fits_a_smooth_target():
+    from tmcore_gb300.gpu import ClosureMLP
+
+    net = ClosureMLP(seed=7)
+    rng = np.random.default_rng(2)
+    x = rng.standard_normal((65536, NIN)).astype(np.float32)
+    y = (np.sin(x[:, 0]) + 0.5 * x[:, 1] * x[:, 2] - 0.3 * x[:, 3]).astype(np.float32)
+    net.set_dataset(x, y)
+    losses = net.train(steps=400, batch=8192, lr=3e-3)
+    assert np.all(np.isfinite(losses))
+    assert losses[-20:].mean() < 0.05 * losses[:5].mean()
+    pred = net.forward(x[:4096], tensor_cores=True)
+    assert np.mean((pred - y[:4096]) ** 2) < 0.1 * np.var(y)
+    net.close()

@@ -82,12 +82,24 @@ SYMBOLS = {
     "tmc_group_synchronize": (ctypes.c_int, [vp]),
     "tmc_group_last_error": (ctypes.c_char_p, [vp]),
     "tmc_group_destroy": (ctypes.c_int, [vp]),
+    "tmc_mlp_create": (ctypes.c_int, [i32, ctypes.c_uint64, ctypes.POINTER(vp)]),
+    "tmc_mlp_destroy": (ctypes.c_int, [vp]),
+    "tmc_mlp_last_error": (ctypes.c_char_p, [vp]),
+    "tmc_mlp_get_params": (ctypes.c_int, [vp, vp]),
+    "tmc_mlp_set_params": (ctypes.c_int, [vp, vp]),
+    "tmc_mlp_set_scaling": (ctypes.c_int, [vp, vp, vp, ctypes.c_float]),
+    "tmc_mlp_forward": (ctypes.c_int, [vp, vp, ctypes.c_int64, vp, i32]),
+    "tmc_mlp_set_dataset": (ctypes.c_int, [vp, vp, vp, ctypes.c_int64]),
+    "tmc_mlp_train": (ctypes.c_int, [vp, i32, i32, ctypes.c_float, vp]),
+    "tmc_mlp_gradient": (ctypes.c_int, [vp, vp, vp, ctypes.c_int64, vp, dp]),
     "tmc_adv_set_initial": (ctypes.c_int, [vp, vp]),
     "tmc_adv_get": (ctypes.c_int, [vp, vp, vp]),
     "tmc_adv_elapsed": (ctypes.c_int, [vp, dp]),
     "tmc_mass_energy_noalloc": (ctypes.c_int, [vp, vp, vp, ctypes.c_int64, vp, vp, ctypes.c_int64, vp, vp]),
 }
 TMC_NOALLOC_MAX_ELEMENTS = 8388608
+TMC_MLP_PARAMS = 9985
+TMC_MLP_FEATURES = 24
 
 
 def declare(lib: ctypes.CDLL) -> ctypes.CDLL:

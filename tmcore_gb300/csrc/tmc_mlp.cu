@@ -1,0 +1,478 @@
+// The learned PV-on-edge closure network: tensor-core forward (tcgen05),
+// CUDA-core training (forward with stored pre-activations, backward, Adam),
+// and its C ABI (include/tmcore_gpu.h, tmc_mlp_*).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "tmc_mlp_tc.cuh"
+#include "tmcore_gpu.h"
+
+using namespace tmc::mlp;
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// forward on the tensor cores, features from a [rows][24] FP32 buffer
+// ---------------------------------------------------------------------------
+struct BufSrc {
+  const float* x;
+  float* y;
+  long long rows;
+  __device__ bool features(long long i, float (&f)[kIn]) const {
+    if (i >= rows) return false;
+#pragma unroll
+    for (int k = 0; k < kIn; ++k) f[k] = x[i * kIn + k];
+    return true;
+  }
+  __device__ void output(long long i, float v) const { y[i] = v; }
+};
+
+__global__ void __launch_bounds__(kTile) k_mlp_fwd_tc(Net net, BufSrc src, long long ntiles, int* err) {
+  extern __shared__ __align__(128) uint8_t smem[];
+  if (!forward_tiles(net, src, ntiles, smem) && threadIdx.x == 0) atomicExch(err, 1);
+}
+
+// ---------------------------------------------------------------------------
+// CUDA-core forward (FP32 activations, BF16-rounded weights): the reference
+// the tensor-core path is checked against
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float gelu_ref(float z) { return gelu_tanh(z, tanhf(gelu_arg(z))); }
+__device__ __forceinline__ float gelu_grad(float z) {
+  const float c = 0.7978845608028654f;
+  const float th = tanhf(gelu_arg(z));
+  return 0.5f * (1.f + th) + 0.5f * z * (1.f - th * th) * c * (1.f + 3.f * 0.044715f * z * z);
+}
+
+struct SimtW {
+  float W1[kH][kIn], W2[kH][kH], W3[kH][kH], b[3][kH], w4[kH], b4;
+  float xm[kIn], xi[kIn];
+};
+
+__device__ void load_simt_weights(const Net& net, SimtW& w) {
+  for (int i = threadIdx.x; i < kH * kIn; i += blockDim.x) w.W1[i / kIn][i % kIn] = __bfloat162float(net.pb[kOffW1 + i]);
+  for (int i = threadIdx.x; i < kH * kH; i += blockDim.x) {
+    w.W2[i / kH][i % kH] = __bfloat162float(net.pb[kOffW2 + i]);
+    w.W3[i / kH][i % kH] = __bfloat162float(net.pb[kOffW3 + i]);
+  }
+  for (int i = threadIdx.x; i < kH; i += blockDim.x) {
+    w.b[0][i] = net.p[kOffB1 + i];
+    w.b[1][i] = net.p[kOffB2 + i];
+    w.b[2][i] = net.p[kOffB3 + i];
+    w.w4[i] = __bfloat162float(net.pb[kOffW4 + i]);
+  }
+  for (int i = threadIdx.x; i < kIn; i += blockDim.x) {
+    w.xm[i] = net.xmean[i];
+    w.xi[i] = net.xinv[i];
+  }
+  if (threadIdx.x == 0) w.b4 = net.p[kOffB4];
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(128) k_mlp_fwd_simt(Net net, const float* x, float* y, long long rows) {
+  extern __shared__ __align__(128) uint8_t smem[];
+  SimtW& w = *reinterpret_cast<SimtW*>(smem);
+  load_simt_weights(net, w);
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < rows; i += (long long)gridDim.x * blockDim.x) {
+    float a[kH], b[kH];
+    float xs[kIn];
+    for (int k = 0; k < kIn; ++k) xs[k] = (x[i * kIn + k] - w.xm[k]) * w.xi[k];
+    for (int j = 0; j < kH; ++j) {
+      float z = w.b[0][j];
+      for (int k = 0; k < kIn; ++k) z += w.W1[j][k] * xs[k];
+      a[j] = gelu_ref(z);
+    }
+    for (int j = 0; j < kH; ++j) {
+      float z = w.b[1][j];
+      for (int k = 0; k < kH; ++k) z += w.W2[j][k] * a[k];
+      b[j] = gelu_ref(z);
+    }
+    float out = w.b4;
+    for (int j = 0; j < kH; ++j) {
+      float z = w.b[2][j];
+      for (int k = 0; k < kH; ++k) z += w.W3[j][k] * b[k];
+      out += w.w4[j] * gelu_ref(z);
+    }
+    y[i] = out * net.yscale;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// training: one block = 128 samples of the batch; forward keeping the
+// pre-activations, MSE loss, backward, block-level weight-gradient GEMMs
+// accumulated into the global FP32 gradient with atomics
+// ---------------------------------------------------------------------------
+constexpr int kLd = kH + 1;  // padded row length (bank conflicts)
+struct TrainSmem {
+  SimtW w;
+  float x[kTile][kIn + 1];
+  float z[3][kTile][kLd];  // pre-activations, overwritten by their gradients
+  float h[kTile][kLd];     // the activations of one layer at a time
+  float dy[kTile];
+};
+
+__device__ void block_dw(const float (*dz)[kLd], const float (*hin)[kLd], int kin, float* gW, float* gb) {
+  // gW[j][k] += sum_s dz[s][j] hin[s][k]; gb[j] += sum_s dz[s][j]
+  const int t = threadIdx.x, j = t >> 1, k0 = (t & 1) * 32;
+  float acc[32];
+#pragma unroll
+  for (int i = 0; i < 32; ++i) acc[i] = 0.f;
+  float accb = 0.f;
+  for (int s = 0; s < kTile; ++s) {
+    const float d = dz[s][j];
+    accb += d;
+#pragma unroll
+    for (int i = 0; i < 32; ++i) acc[i] += d * hin[s][k0 + i];
+  }
+#pragma unroll
+  for (int i = 0; i < 32; ++i)
+    if (k0 + i < kin) atomicAdd(&gW[j * kin + k0 + i], acc[i]);
+  if ((t & 1) == 0) atomicAdd(&gb[j], accb);
+}
+
+__global__ void __launch_bounds__(kTile) k_mlp_train(Net net, const float* X, const float* Y, long long rows,
+                                                     long long offset, float inv_batch, float* grad, double* loss) {
+  extern __shared__ __align__(128) uint8_t smem[];
+  TrainSmem& S = *reinterpret_cast<TrainSmem*>(smem);
+  load_simt_weights(net, S.w);
+  const int t = threadIdx.x;
+  const long long i = (offset + (long long)blockIdx.x * kTile + t) % rows;
+  // forward
+  for (int k = 0; k < kIn; ++k) S.x[t][k] = (X[i * kIn + k] - S.w.xm[k]) * S.w.xi[k];
+  float a[kH];
+  for (int j = 0; j < kH; ++j) {
+    float z = S.w.b[0][j];
+    for (int k = 0; k < kIn; ++k) z += S.w.W1[j][k] * S.x[t][k];
+    S.z[0][t][j] = z;
+    a[j] = gelu_ref(z);
+  }
+  float b[kH];
+  for (int j = 0; j < kH; ++j) {
+    float z = S.w.b[1][j];
+    for (int k = 0; k < kH; ++k) z += S.w.W2[j][k] * a[k];
+    S.z[1][t][j] = z;
+    b[j] = gelu_ref(z);
+  }
+  float out = S.w.b4;
+  for (int j = 0; j < kH; ++j) {
+    float z = S.w.b[2][j];
+    for (int k = 0; k < kH; ++k) z += S.w.W3[j][k] * b[k];
+    S.z[2][t][j] = z;
+    const float h3 = gelu_ref(z);
+    S.h[t][j] = h3;
+    out += S.w.w4[j] * h3;
+  }
+  const float e = out - Y[i] / net.yscale;
+  const float dy = 2.f * e * inv_batch;
+  S.dy[t] = dy;
+  // loss: block sum of e^2
+  {
+    float l = e * e;
+    for (int off = 16; off > 0; off >>= 1) l += __shfl_down_sync(0xffffffffu, l, off);
+    if ((t & 31) == 0) atomicAdd(loss, (double)l * inv_batch);
+  }
+  __syncthreads();
+  // output layer
+  if (t < kH) {
+    float acc = 0.f;
+    for (int s = 0; s < kTile; ++s) acc += S.dy[s] * S.h[s][t];
+    atomicAdd(&grad[kOffW4 + t], acc);
+  }
+  if (t == kH) {
+    float acc = 0.f;
+    for (int s = 0; s < kTile; ++s) acc += S.dy[s];
+    atomicAdd(&grad[kOffB4], acc);
+  }
+  // dz3 = dy w4 gelu'(z3), in place of z3
+  for (int j = 0; j < kH; ++j) S.z[2][t][j] = dy * S.w.w4[j] * gelu_grad(S.z[2][t][j]);
+  __syncthreads();
+  // layer 3: h = h2
+  for (int j = 0; j < kH; ++j) S.h[t][j] = gelu_ref(S.z[1][t][j]);
+  __syncthreads();
+  block_dw(S.z[2], S.h, kH, grad + kOffW3, grad + kOffB3);
+  // dz2 = (dz3 W3) gelu'(z2)
+  {
+    float d[kH];
+    for (int k = 0; k < kH; ++k) d[k] = 0.f;
+    for (int j = 0; j < kH; ++j) {
+      const float g = S.z[2][t][j];
+      for (int k = 0; k < kH; ++k) d[k] += g * S.w.W3[j][k];
+    }
+    for (int k = 0; k < kH; ++k) S.z[1][t][k] = d[k] * gelu_grad(S.z[1][t][k]);
+  }
+  __syncthreads();
+  // layer 2: h = h1
+  for (int j = 0; j < kH; ++j) S.h[t][j] = gelu_ref(S.z[0][t][j]);
+  __syncthreads();
+  block_dw(S.z[1], S.h, kH, grad + kOffW2, grad + kOffB2);
+  // dz1 = (dz2 W2) gelu'(z1)
+  {
+    float d[kH];
+    for (int k = 0; k < kH; ++k) d[k] = 0.f;
+    for (int j = 0; j < kH; ++j) {
+      const float g = S.z[1][t][j];
+      for (int k = 0; k < kH; ++k) d[k] += g * S.w.W2[j][k];
+    }
+    for (int k = 0; k < kH; ++k) S.z[0][t][k] = d[k] * gelu_grad(S.z[0][t][k]);
+  }
+  __syncthreads();
+  // layer 1: h = normalised input
+  for (int k = 0; k < kIn; ++k) S.h[t][k] = S.x[t][k];
+  __syncthreads();
+  block_dw(S.z[0], S.h, kIn, grad + kOffW1, grad + kOffB1);
+}
+
+// Adam (Kingma & Ba 2015) on the FP32 master parameters; BF16 copy refreshed,
+// gradient cleared
+__global__ void k_adam(float* p, __nv_bfloat16* pb, float* g, float* m, float* v, int n, float lr, float b1c,
+                       float b2c) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+  const float gi = g[i];
+  const float mi = b1 * m[i] + (1.f - b1) * gi;
+  const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+  m[i] = mi;
+  v[i] = vi;
+  const float mh = mi / b1c, vh = vi / b2c;
+  const float pi = p[i] - lr * mh / (sqrtf(vh) + eps);
+  p[i] = pi;
+  pb[i] = __float2bfloat16_rn(pi);
+  g[i] = 0.f;
+}
+
+__global__ void k_to_bf16(const float* p, __nv_bfloat16* pb, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) pb[i] = __float2bfloat16_rn(p[i]);
+}
+
+}  // namespace
+
+struct tmc_mlp {
+  int device = 0;
+  cudaStream_t st = nullptr;
+  float* p = nullptr;  // master FP32
+  __nv_bfloat16* pb = nullptr;
+  float *g = nullptr, *m = nullptr, *v = nullptr;
+  float *xmean = nullptr, *xinv = nullptr;
+  float yscale = 1.f;
+  float *dx = nullptr, *dy = nullptr;  // dataset
+  long long rows = 0;
+  long long cursor = 0;
+  int adam_t = 0;
+  float *io_x = nullptr, *io_y = nullptr;
+  long long io_cap = 0;
+  int* d_err = nullptr;
+  double* d_loss = nullptr;
+  int sms = 148;
+  std::string err;
+  int fail(int code, const std::string& s) {
+    err = s;
+    return code;
+  }
+  int check(const char* where) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(TMC_E_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+    return TMC_OK;
+  }
+  Net net() const { return Net{p, pb, xmean, xinv, yscale}; }
+};
+
+tmc::mlp::Net tmc_mlp_net(const tmc_mlp* n) { return n->net(); }
+
+extern "C" {
+
+int tmc_mlp_create(int32_t device, uint64_t seed, tmc_mlp** out) {
+  if (!out) return TMC_E_ARG;
+  *out = nullptr;
+  auto n = new tmc_mlp();
+  n->device = device;
+  if (cudaSetDevice(device) != cudaSuccess) {
+    cudaGetLastError();
+    n->err = "cudaSetDevice failed (no CUDA device?)";
+    *out = n;
+    return TMC_E_CUDA;
+  }
+  cudaDeviceGetAttribute(&n->sms, cudaDevAttrMultiProcessorCount, device);
+  bool okc = cudaStreamCreateWithFlags(&n->st, cudaStreamNonBlocking) == cudaSuccess;
+  okc = okc && cudaMalloc(&n->p, sizeof(float) * kParams) == cudaSuccess;
+  okc = okc && cudaMalloc(&n->pb, sizeof(__nv_bfloat16) * kParams) == cudaSuccess;
+  okc = okc && cudaMalloc(&n->g, sizeof(float) * kParams) == cudaSuccess;
+  okc = okc && cudaMalloc(&n->m, sizeof(float) * kParams) == cudaSuccess;
+  okc = okc && cudaMalloc(&n->v, sizeof(float) * kParams) == cudaSuccess;
+  okc = okc && cudaMalloc(&n->xmean, sizeof(float) * kIn) == cudaSuccess;
+  okc = okc && cudaMalloc(&n->xinv, sizeof(float) * kIn) == cudaSuccess;
+  okc = okc && cudaMalloc(&n->d_err, sizeof(int)) == cudaSuccess;
+  okc = okc && cudaMalloc(&n->d_loss, sizeof(double)) == cudaSuccess;
+  *out = n;
+  if (!okc) return n->check("tmc_mlp_create");
+  // PyTorch-style Linear initialisation: U(-1/sqrt(fan_in), 1/sqrt(fan_in))
+  std::vector<float> h(kParams);
+  std::mt19937_64 rng(seed);
+  auto fill = [&](int off, int count, int fan_in) {
+    std::uniform_real_distribution<float> d(-1.f / std::sqrt((float)fan_in), 1.f / std::sqrt((float)fan_in));
+    for (int i = 0; i < count; ++i) h[off + i] = d(rng);
+  };
+  fill(kOffW1, kH * kIn, kIn);
+  fill(kOffB1, kH, kIn);
+  fill(kOffW2, kH * kH, kH);
+  fill(kOffB2, kH, kH);
+  fill(kOffW3, kH * kH, kH);
+  fill(kOffB3, kH, kH);
+  fill(kOffW4, kH, kH);
+  fill(kOffB4, 1, kH);
+  std::vector<float> zero(kIn, 0.f), one(kIn, 1.f);
+  cudaMemcpy(n->xmean, zero.data(), sizeof(float) * kIn, cudaMemcpyHostToDevice);
+  cudaMemcpy(n->xinv, one.data(), sizeof(float) * kIn, cudaMemcpyHostToDevice);
+  cudaMemset(n->g, 0, sizeof(float) * kParams);
+  cudaMemset(n->m, 0, sizeof(float) * kParams);
+  cudaMemset(n->v, 0, sizeof(float) * kParams);
+  cudaMemset(n->d_err, 0, sizeof(int));
+  int rc = tmc_mlp_set_params(n, h.data());
+  if (rc) return rc;
+  cudaFuncSetAttribute(k_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TrainSmem));
+  cudaFuncSetAttribute(k_mlp_fwd_simt, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SimtW));
+  cudaFuncSetAttribute(k_mlp_fwd_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemTc);
+  return n->check("tmc_mlp_create");
+}
+
+int tmc_mlp_destroy(tmc_mlp* n) {
+  if (!n) return TMC_OK;
+  if (n->st) cudaStreamSynchronize(n->st);
+  void* ptrs[] = {n->p, n->pb, n->g, n->m, n->v, n->xmean, n->xinv, n->dx, n->dy, n->io_x, n->io_y, n->d_err, n->d_loss};
+  for (void* q : ptrs) cudaFree(q);
+  if (n->st) cudaStreamDestroy(n->st);
+  delete n;
+  return TMC_OK;
+}
+
+const char* tmc_mlp_last_error(const tmc_mlp* n) { return n ? n->err.c_str() : "null network"; }
+
+int tmc_mlp_get_params(tmc_mlp* n, float* params) {
+  if (!n || !params) return TMC_E_ARG;
+  if (cudaMemcpyAsync(params, n->p, sizeof(float) * kParams, cudaMemcpyDeviceToHost, n->st) != cudaSuccess)
+    return n->check("tmc_mlp_get_params");
+  cudaStreamSynchronize(n->st);
+  return n->check("tmc_mlp_get_params");
+}
+
+int tmc_mlp_set_params(tmc_mlp* n, const float* params) {
+  if (!n || !params) return TMC_E_ARG;
+  cudaMemcpyAsync(n->p, params, sizeof(float) * kParams, cudaMemcpyHostToDevice, n->st);
+  k_to_bf16<<<(kParams + 255) / 256, 256, 0, n->st>>>(n->p, n->pb, kParams);
+  cudaMemsetAsync(n->m, 0, sizeof(float) * kParams, n->st);
+  cudaMemsetAsync(n->v, 0, sizeof(float) * kParams, n->st);
+  n->adam_t = 0;
+  cudaStreamSynchronize(n->st);
+  return n->check("tmc_mlp_set_params");
+}
+
+int tmc_mlp_set_scaling(tmc_mlp* n, const float* x_mean, const float* x_inv_std, float y_scale) {
+  if (!n || !x_mean || !x_inv_std || !(y_scale > 0.f)) return TMC_E_ARG;
+  cudaMemcpyAsync(n->xmean, x_mean, sizeof(float) * kIn, cudaMemcpyHostToDevice, n->st);
+  cudaMemcpyAsync(n->xinv, x_inv_std, sizeof(float) * kIn, cudaMemcpyHostToDevice, n->st);
+  n->yscale = y_scale;
+  cudaStreamSynchronize(n->st);
+  return n->check("tmc_mlp_set_scaling");
+}
+
+static int ensure_io(tmc_mlp* n, long long rows) {
+  if (rows <= n->io_cap) return TMC_OK;
+  cudaFree(n->io_x);
+  cudaFree(n->io_y);
+  n->io_x = n->io_y = nullptr;
+  n->io_cap = 0;
+  if (cudaMalloc(&n->io_x, sizeof(float) * kIn * rows) != cudaSuccess ||
+      cudaMalloc(&n->io_y, sizeof(float) * rows) != cudaSuccess)
+    return n->check("tmc_mlp io buffers");
+  n->io_cap = rows;
+  return TMC_OK;
+}
+
+int tmc_mlp_forward(tmc_mlp* n, const float* x, int64_t rows, float* y, int32_t tensor_cores) {
+  if (!n || !x || !y || rows < 0) return TMC_E_ARG;
+  if (rows == 0) return TMC_OK;
+  int rc = ensure_io(n, rows);
+  if (rc) return rc;
+  cudaMemcpyAsync(n->io_x, x, sizeof(float) * kIn * rows, cudaMemcpyHostToDevice, n->st);
+  if (tensor_cores) {
+    const long long ntiles = (rows + kTile - 1) / kTile;
+    const int grid = (int)std::min<long long>(ntiles, (long long)n->sms * 4);
+    cudaMemsetAsync(n->d_err, 0, sizeof(int), n->st);
+    k_mlp_fwd_tc<<<grid, kTile, kSmemTc, n->st>>>(n->net(), BufSrc{n->io_x, n->io_y, rows}, ntiles, n->d_err);
+  } else {
+    const int grid = (int)std::min<long long>((rows + 127) / 128, (long long)n->sms * 8);
+    k_mlp_fwd_simt<<<grid, 128, sizeof(SimtW), n->st>>>(n->net(), n->io_x, n->io_y, rows);
+  }
+  cudaMemcpyAsync(y, n->io_y, sizeof(float) * rows, cudaMemcpyDeviceToHost, n->st);
+  int herr = 0;
+  if (tensor_cores) cudaMemcpyAsync(&herr, n->d_err, sizeof(int), cudaMemcpyDeviceToHost, n->st);
+  if (cudaStreamSynchronize(n->st) != cudaSuccess) return n->check("tmc_mlp_forward");
+  if (herr) return n->fail(TMC_E_HEALTH, "tmc_mlp_forward: a tensor-core completion wait timed out");
+  return n->check("tmc_mlp_forward");
+}
+
+int tmc_mlp_set_dataset(tmc_mlp* n, const float* x, const float* y, int64_t rows) {
+  if (!n || !x || !y || rows <= 0) return TMC_E_ARG;
+  cudaFree(n->dx);
+  cudaFree(n->dy);
+  n->dx = n->dy = nullptr;
+  n->rows = 0;
+  if (cudaMalloc(&n->dx, sizeof(float) * kIn * rows) != cudaSuccess ||
+      cudaMalloc(&n->dy, sizeof(float) * rows) != cudaSuccess)
+    return n->check("tmc_mlp_set_dataset");
+  cudaMemcpyAsync(n->dx, x, sizeof(float) * kIn * rows, cudaMemcpyHostToDevice, n->st);
+  cudaMemcpyAsync(n->dy, y, sizeof(float) * rows, cudaMemcpyHostToDevice, n->st);
+  n->rows = rows;
+  n->cursor = 0;
+  cudaStreamSynchronize(n->st);
+  return n->check("tmc_mlp_set_dataset");
+}
+
+int tmc_mlp_train(tmc_mlp* n, int32_t batch, int32_t steps, float lr, float* losses) {
+  if (!n || batch <= 0 || batch % kTile != 0 || steps < 0) return n ? n->fail(TMC_E_ARG, "batch must be a positive multiple of 128") : TMC_E_ARG;
+  if (!n->dx) return n->fail(TMC_E_STATE, "tmc_mlp_train: no dataset");
+  for (int s = 0; s < steps; ++s) {
+    cudaMemsetAsync(n->d_loss, 0, sizeof(double), n->st);
+    k_mlp_train<<<batch / kTile, kTile, sizeof(TrainSmem), n->st>>>(n->net(), n->dx, n->dy, n->rows, n->cursor,
+                                                                    1.f / batch, n->g, n->d_loss);
+    n->cursor = (n->cursor + batch) % n->rows;
+    n->adam_t += 1;
+    const float b1c = 1.f - std::pow(0.9f, (float)n->adam_t), b2c = 1.f - std::pow(0.999f, (float)n->adam_t);
+    k_adam<<<(kParams + 255) / 256, 256, 0, n->st>>>(n->p, n->pb, n->g, n->m, n->v, kParams, lr, b1c, b2c);
+    if (losses) {
+      double l = 0.0;
+      cudaMemcpyAsync(&l, n->d_loss, sizeof(double), cudaMemcpyDeviceToHost, n->st);
+      if (cudaStreamSynchronize(n->st) != cudaSuccess) return n->check("tmc_mlp_train");
+      losses[s] = (float)l;
+    }
+  }
+  if (cudaStreamSynchronize(n->st) != cudaSuccess) return n->check("tmc_mlp_train");
+  return n->check("tmc_mlp_train");
+}
+
+int tmc_mlp_gradient(tmc_mlp* n, const float* x, const float* y, int64_t rows, float* grad, double* loss) {
+  if (!n || !x || !y || !grad || rows <= 0 || rows % kTile != 0)
+    return n ? n->fail(TMC_E_ARG, "rows must be a positive multiple of 128") : TMC_E_ARG;
+  int rc = ensure_io(n, rows);
+  if (rc) return rc;
+  cudaMemcpyAsync(n->io_x, x, sizeof(float) * kIn * rows, cudaMemcpyHostToDevice, n->st);
+  cudaMemcpyAsync(n->io_y, y, sizeof(float) * rows, cudaMemcpyHostToDevice, n->st);
+  cudaMemsetAsync(n->g, 0, sizeof(float) * kParams, n->st);
+  cudaMemsetAsync(n->d_loss, 0, sizeof(double), n->st);
+  k_mlp_train<<<(unsigned)(rows / kTile), kTile, sizeof(TrainSmem), n->st>>>(n->net(), n->io_x, n->io_y, rows, 0,
+                                                                             1.f / (float)rows, n->g, n->d_loss);
+  cudaMemcpyAsync(grad, n->g, sizeof(float) * kParams, cudaMemcpyDeviceToHost, n->st);
+  double l = 0.0;
+  cudaMemcpyAsync(&l, n->d_loss, sizeof(double), cudaMemcpyDeviceToHost, n->st);
+  cudaMemsetAsync(n->g, 0, sizeof(float) * kParams, n->st);
+  if (cudaStreamSynchronize(n->st) != cudaSuccess) return n->check("tmc_mlp_gradient");
+  if (loss) *loss = l;
+  return n->check("tmc_mlp_gradient");
+}
+
+}  // extern "C"

@@ -1,0 +1,59 @@
+// The learned PV-on-edge closure: a 24 -> 64 -> 64 -> 64 -> 1 MLP with GELU
+// (tanh form, Hendrycks & Gimpel 2016) between the hidden layers, BF16
+// weights and FP32 accumulation.
+//
+// Inference runs on the 5th-generation tensor cores: tiles of 128 edges, one
+// tcgen05.mma (M = 128, N = 64, K = 16, BF16 x BF16 -> FP32 in tensor memory)
+// per 16 inputs of a layer, issued by one thread; the weights and the
+// activations sit in shared memory in the canonical no-swizzle K-major
+// layout (8-row x 16-byte core matrices); the epilogue (bias, GELU, BF16
+// rounding) reads the accumulator back with tcgen05.ld and writes the next
+// layer's operand.  Training (forward with stored pre-activations, backward,
+// Adam) runs on the CUDA cores in FP32 from the BF16 weights.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace tmc {
+namespace mlp {
+
+constexpr int kIn = 24;     // features per edge
+constexpr int kInPad = 32;  // first-layer K padded to two MMA K-steps
+constexpr int kH = 64;      // hidden width
+constexpr int kTile = 128;  // edges per tensor-core tile (MMA M)
+
+// parameter vector layout (FP32 master copy; the BF16 copy has the same layout)
+constexpr int kOffW1 = 0;
+constexpr int kOffB1 = kOffW1 + kH * kIn;
+constexpr int kOffW2 = kOffB1 + kH;
+constexpr int kOffB2 = kOffW2 + kH * kH;
+constexpr int kOffW3 = kOffB2 + kH;
+constexpr int kOffB3 = kOffW3 + kH * kH;
+constexpr int kOffW4 = kOffB3 + kH;
+constexpr int kOffB4 = kOffW4 + kH;
+constexpr int kParams = kOffB4 + 1;  // 9985
+static_assert(kParams == 9985, "24-64-64-64-1 MLP has 9985 parameters");
+
+// device view of the network for the forward kernels
+struct Net {
+  const float* p;             // FP32 master parameters (biases are read from here)
+  const __nv_bfloat16* pb;    // BF16 parameters (weights are read from here)
+  const float* xmean;         // [kIn] feature normalisation
+  const float* xinv;          // [kIn]
+  float yscale;               // output scale
+};
+
+__device__ __forceinline__ float gelu_tanh(float x, float t) { return 0.5f * x * (1.f + t); }
+__device__ __forceinline__ float gelu_arg(float x) { return 0.7978845608028654f * (x + 0.044715f * x * x * x); }
+
+// shared-memory size of the tensor-core forward kernel
+constexpr int kSmemW1 = kH * kInPad * 2;  // 4 KB
+constexpr int kSmemW = kH * kH * 2;       // 8 KB
+constexpr int kSmemA = kTile * kH * 2;    // 16 KB
+constexpr int kSmemTc = kSmemW1 + 2 * kSmemW + kSmemA + 64;
+
+}  // namespace mlp
+}  // namespace tmc

@@ -249,3 +249,76 @@ class TMCoreGroup:
             self.close()
         except Exception:
             pass
+
+
+class ClosureMLP:
+    """The 24-64-64-64-1 GELU network of the learned PV-on-edge closure
+    (tmc_mlp_*): BF16 weights, FP32 accumulation, tensor-core forward,
+    Adam training on the device."""
+
+    def __init__(self, device: int = 0, seed: int = 0):
+        self.lib = _lib.gpu()
+        n = ctypes.c_void_p()
+        rc = self.lib.tmc_mlp_create(int(device), int(seed), ctypes.byref(n))
+        self.n = n
+        if rc != 0:
+            msg = self.lib.tmc_mlp_last_error(n).decode() if n.value else "tmc_mlp_create failed"
+            self.close()
+            raise TMCError(rc, msg)
+
+    def _chk(self, rc):
+        if rc != 0:
+            raise TMCError(rc, self.lib.tmc_mlp_last_error(self.n).decode())
+
+    def close(self):
+        if getattr(self, "n", None) is not None and self.n.value:
+            self.lib.tmc_mlp_destroy(self.n)
+        self.n = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def params(self) -> np.ndarray:
+        p = np.empty(abi.TMC_MLP_PARAMS, np.float32)
+        self._chk(self.lib.tmc_mlp_get_params(self.n, _ptr(p)))
+        return p
+
+    @params.setter
+    def params(self, p):
+        p = np.ascontiguousarray(p, np.float32)
+        assert p.size == abi.TMC_MLP_PARAMS
+        self._chk(self.lib.tmc_mlp_set_params(self.n, _ptr(p)))
+
+    def set_scaling(self, x_mean, x_inv_std, y_scale: float):
+        xm = np.ascontiguousarray(x_mean, np.float32)
+        xi = np.ascontiguousarray(x_inv_std, np.float32)
+        self._chk(self.lib.tmc_mlp_set_scaling(self.n, _ptr(xm), _ptr(xi), float(y_scale)))
+
+    def forward(self, x, tensor_cores: bool = True) -> np.ndarray:
+        x = np.ascontiguousarray(x, np.float32).reshape(-1, abi.TMC_MLP_FEATURES)
+        y = np.empty(x.shape[0], np.float32)
+        self._chk(self.lib.tmc_mlp_forward(self.n, _ptr(x), x.shape[0], _ptr(y), 1 if tensor_cores else 0))
+        return y
+
+    def set_dataset(self, x, y):
+        x = np.ascontiguousarray(x, np.float32).reshape(-1, abi.TMC_MLP_FEATURES)
+        y = np.ascontiguousarray(y, np.float32).reshape(-1)
+        self._keep = (x, y)
+        self._chk(self.lib.tmc_mlp_set_dataset(self.n, _ptr(x), _ptr(y), x.shape[0]))
+
+    def train(self, steps: int, batch: int = 65536, lr: float = 1e-3) -> np.ndarray:
+        losses = np.empty(max(int(steps), 1), np.float32)
+        self._chk(self.lib.tmc_mlp_train(self.n, int(batch), int(steps), float(lr), _ptr(losses)))
+        return losses[:steps]
+
+    def gradient(self, x, y):
+        x = np.ascontiguousarray(x, np.float32).reshape(-1, abi.TMC_MLP_FEATURES)
+        y = np.ascontiguousarray(y, np.float32).reshape(-1)
+        g = np.empty(abi.TMC_MLP_PARAMS, np.float32)
+        loss = ctypes.c_double()
+        self._chk(self.lib.tmc_mlp_gradient(self.n, _ptr(x), _ptr(y), x.shape[0], _ptr(g), ctypes.byref(loss)))
+        return g, loss.value
