@@ -170,6 +170,21 @@ int tmc_mlp_train(tmc_mlp* n, int32_t batch, int32_t steps, float lr, float* los
  * the parameters, without updating them */
 int tmc_mlp_gradient(tmc_mlp* n, const float* x, const float* y, int64_t rows, float* grad, double* loss);
 
+/* The learned closure in the FP32 CRK4 step: after the pv-on-edge pass of
+ * every stage, the network's output for each edge (features: the stage's
+ * u, tangential velocity, gd_edge, pv_edge, pv and gd on the two vertices /
+ * cells, E, ghs and f on them, dvEdge, dcEdge, u on four neighbour edges, the
+ * two pv gradients) is added to pv_edge before q.F_perp.  net = NULL turns it
+ * off; the network must outlive its use.  tmc_set_member_closure switches it
+ * per ensemble member (the invariant-drift fallback).  tmc_closure_status
+ * reports a tensor-core wait that ran out.  tmc_closure_features returns the
+ * [nEdges][TMC_MLP_FEATURES] features and pv_edge of state(old) of the
+ * selected member (caller's edge order), for training. */
+int tmc_set_closure(tmc_handle* h, const tmc_mlp* net);
+int tmc_set_member_closure(tmc_handle* h, int32_t member, int32_t on);
+int tmc_closure_status(tmc_handle* h, int32_t* timed_out);
+int tmc_closure_features(tmc_handle* h, float* features, double* pv_edge);
+
 /* Groups: several handles (different meshes and dt, each possibly an
  * ensemble) advanced together, e.g. a mixed batch of mesh levels with
  * dt = 1200 / 2^(level-4) s.  One CUDA graph per cycle of cycle_seconds holds

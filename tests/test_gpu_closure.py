@@ -1,0 +1,95 @@
+"""The learned closure inside the FP32 step: features, a zero network that
+changes nothing, and the per-member switch of an ensemble."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _ic(mesh, seed):
+    from tmcore_gb300 import cases
+
+    return cases.jet_bumps(mesh, seed=seed)
+
+
+KW = dict(dt=600.0, precision=1, pv_scheme=1, apvm_weight=0.0)
+
+
+def test_features_match_state(mesh4):
+    from tmcore_gb300.gpu import TMCoreGPU
+
+    m = mesh4
+    g = TMCoreGPU(m, **KW)
+    gd, u, ghs = _ic(m, 80)
+    g.set_initial(gd, u, ghs)
+    g.step(2)
+    f, pv = g.closure_features()
+    gd1, _, u1 = g.get_state()
+    pvv, _ = g.get_vertex()
+    c1, c2 = m.cellsOnEdge[:, 0] - 1, m.cellsOnEdge[:, 1] - 1
+    v1, v2 = m.verticesOnEdge[:, 0] - 1, m.verticesOnEdge[:, 1] - 1
+    r = 6371220.0
+    assert np.allclose(f[:, 0], u1, rtol=1e-5, atol=1e-5 * np.max(np.abs(u1)))
+    assert np.allclose(f[:, 2], 0.5 * (gd1[c1] + gd1[c2]), rtol=1e-5)
+    assert np.allclose(f[:, 8], gd1[c1], rtol=1e-6) and np.allclose(f[:, 9], gd1[c2], rtol=1e-6)
+    assert np.allclose(f[:, 4], pvv[v1], rtol=1e-4, atol=1e-6 * np.max(np.abs(pvv)))
+    assert np.allclose(f[:, 16], m.dvEdge * r, rtol=1e-6) and np.allclose(f[:, 17], m.dcEdge * r, rtol=1e-6)
+    assert np.allclose(f[:, 14], 2 * 7.292e-5 * np.sin(m.latVertex[v1]), rtol=1e-6, atol=1e-12)
+    # centred pv on edges (pv_scheme 1 without APVM)
+    assert np.allclose(pv, 0.5 * (pvv[v1] + pvv[v2]), rtol=1e-4, atol=1e-6 * np.max(np.abs(pvv)))
+    g.close()
+
+
+def test_zero_network_changes_nothing(mesh4):
+    from tmcore_gb300.gpu import ClosureMLP, TMCoreGPU
+
+    net = ClosureMLP(seed=1)
+    net.params = np.zeros(9985, np.float32)
+    a, b = TMCoreGPU(mesh4, **KW), TMCoreGPU(mesh4, **KW)
+    gd, u, ghs = _ic(mesh4, 81)
+    for x in (a, b):
+        x.set_initial(gd, u, ghs)
+    a.set_closure(net)
+    a.step(6)
+    b.step(6)
+    assert not a.closure_status()
+    sa, sb = a.get_state(), b.get_state()
+    assert all(np.array_equal(x, y) for x, y in zip(sa, sb))
+    a.close()
+    b.close()
+    net.close()
+
+
+def test_member_switch(mesh4):
+    """Member 1 with the closure switched off evolves exactly as the plain
+    model; member 0 with it on does not."""
+    from tmcore_gb300.gpu import ClosureMLP, TMCoreGPU
+
+    net = ClosureMLP(seed=2)
+    p = net.params
+    p *= 0.5
+    net.params = p
+    net.set_scaling(np.zeros(24), np.ones(24), 1e-9)  # corrections of order 1e-9 (pv ~ 1e-8)
+    ens = TMCoreGPU(mesh4, members=2, **KW)
+    plain = TMCoreGPU(mesh4, **KW)
+    gd, u, ghs = _ic(mesh4, 82)
+    for k in range(2):
+        ens.select_member(k)
+        ens.set_initial(gd, u, ghs)
+    plain.set_initial(gd, u, ghs)
+    ens.set_closure(net)
+    ens.set_member_closure(1, False)
+    ens.step(6)
+    plain.step(6)
+    ens.select_member(1)
+    s1, sp = ens.get_state(), plain.get_state()
+    assert all(np.array_equal(x, y) for x, y in zip(s1, sp))
+    ens.select_member(0)
+    s0 = ens.get_state()
+    assert not np.array_equal(s0[0], sp[0])
+    assert np.all(np.isfinite(s0[0])) and np.all(np.isfinite(s0[2]))
+    with pytest.raises(Exception):
+        TMCoreGPU(mesh4, dt=600.0, precision=0).set_closure(net)
+    ens.close()
+    plain.close()
+    net.close()

@@ -92,6 +92,10 @@ SYMBOLS = {
     "tmc_mlp_set_dataset": (ctypes.c_int, [vp, vp, vp, ctypes.c_int64]),
     "tmc_mlp_train": (ctypes.c_int, [vp, i32, i32, ctypes.c_float, vp]),
     "tmc_mlp_gradient": (ctypes.c_int, [vp, vp, vp, ctypes.c_int64, vp, dp]),
+    "tmc_set_closure": (ctypes.c_int, [vp, vp]),
+    "tmc_set_member_closure": (ctypes.c_int, [vp, i32, i32]),
+    "tmc_closure_status": (ctypes.c_int, [vp, ctypes.POINTER(i32)]),
+    "tmc_closure_features": (ctypes.c_int, [vp, vp, vp]),
     "tmc_adv_set_initial": (ctypes.c_int, [vp, vp]),
     "tmc_adv_get": (ctypes.c_int, [vp, vp, vp]),
     "tmc_adv_elapsed": (ctypes.c_int, [vp, dp]),

@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "tmc_kernels.cuh"
+#include "tmc_mlp.cuh"
 #include "tmc_prep.h"
 #include "tmcore_gpu.h"
 
@@ -47,6 +48,7 @@ struct EngineBase {
   virtual void adv_get_dev(double* raw_q, double* raw_u) = 0;
   virtual void state_slot0(void** gd, void** iap, void** q, void** ghs) = 0;  // all members
   virtual void refresh_all_shadows() = 0;
+  virtual void closure_features(float* feat, float* pv) = 0;
 };
 
 enum Field { F_GD = 0, F_IAP, F_U, F_PV_V, F_VOR, F_TEND_GD, F_TEND_IAP, F_GD_STAGE };
@@ -92,6 +94,12 @@ struct tmc_handle {
   // block size per pass of the fused step (cell, vertex, edge_pv, edge_flux,
   // final), chosen by tmc_autotune; the partial-sum counts follow them
   int bsp[5] = {256, 256, 256, 256, 256};
+  // learned PV-on-edge closure (FP32 path): network, per-member switch, wait status
+  const tmc_mlp* closure = nullptr;
+  tmc::mlp::Net closure_net{};
+  int* d_member_on = nullptr;
+  int* d_closure_err = nullptr;
+  int sms = 148;
   int timed_pass = 3;  // the pass tmc_time_steps brackets with events
 
   template <class X>
@@ -339,6 +347,7 @@ struct Engine : EngineBase {
       mark(P_PV);
       launch_edge_pv<T>(M, O, s, b[P_PV], h->st);
       if (O.pv_scheme == 2) launch_cons_apvm<T>(M, O, s, h->P, h->d_diag, b[P_VERTEX], h->st);
+      launch_closure_pass(s);
       mark(P_PV);
       mark(P_FLUX);
       launch_edge_flux<T>(M, O, s, rk, h->P, b[P_FLUX], h->st);
@@ -349,6 +358,28 @@ struct Engine : EngineBase {
     if (flux_ev && h->timed_pass == P_FINAL) cudaEventRecord((*flux_ev)[(*ev_pos)++], h->st);
     launch_final_update<T>(M, O, io(0), h->d_diag, h->P, h->bsp[P_FINAL], h->st);
     if (flux_ev && h->timed_pass == P_FINAL) cudaEventRecord((*flux_ev)[(*ev_pos)++], h->st);
+  }
+
+  // the learned closure on this stage's pv_edge (FP32 path)
+  void launch_closure_pass(const StageIO<T>& s) {
+    if constexpr (std::is_same<T, float>::value) {
+      if (h->closure) {
+        ClosureArgs a{&h->closure_net, h->d_member_on, h->d_closure_err, h->sms};
+        launch_closure(h->M, s, a, h->st);
+      }
+    }
+  }
+
+  // features of state(old) of the selected member (after a diagnostic pass and
+  // the pv-on-edge pass), internal edge order
+  void closure_features(float* feat, float* pv) {
+    if constexpr (std::is_same<T, float>::value) {
+      launch_diag_pass(false);
+      StageIO<T> s = io(0);
+      launch_edge_pv<T>(h->M, h->O, s, h->bsp[P_PV], h->st);
+      if (h->O.pv_scheme == 2) launch_cons_apvm<T>(h->M, h->O, s, h->P, h->d_diag, h->bsp[P_VERTEX], h->st);
+      launch_closure_features(h->M, s, h->cur, feat, pv, h->st);
+    }
   }
 
   // ---- generic integrator program (time_scheme_mod.F90:65-107 CRK3,
@@ -865,6 +896,14 @@ int tmc_create(const tmc_mesh_desc* mesh, const tmc_params* params, tmc_handle**
     return TMC_E_CUDA;
   }
   cudaMemset(h->d_diag, 0, sizeof(double) * kDiagStride * h->members);
+  cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, p.device);
+  h->d_member_on = h->dalloc<int>(h->members);
+  h->d_closure_err = h->dalloc<int>(1);
+  if (h->d_member_on) {
+    std::vector<int> on(h->members, 1);
+    cudaMemcpy(h->d_member_on, on.data(), sizeof(int) * h->members, cudaMemcpyHostToDevice);
+  }
+  if (h->d_closure_err) cudaMemset(h->d_closure_err, 0, sizeof(int));
   cudaMemset(h->P.base, 0, sizeof(double) * h->P.member_stride() * h->members);
   if (p.precision == TMC_FP32)
     h->eng = std::make_unique<Engine<float>>(h.get());
@@ -1224,6 +1263,73 @@ int tmc_select_member(tmc_handle* h, int32_t member) {
   if (member < 0 || member >= h->members) return h->fail(TMC_E_ARG, "member out of range");
   h->cur = member;
   return TMC_OK;
+}
+
+int tmc_set_closure(tmc_handle* h, const tmc_mlp* net) {
+  TMC_REQUIRE_SWM(h);
+  if (net && (h->p.precision != TMC_FP32 || h->generic))
+    return h->fail(TMC_E_UNSUP, "the learned closure runs in the FP32 CRK4 shallow-water step");
+  if (sync(h, "tmc_set_closure")) return TMC_E_CUDA;
+  h->closure = net;
+  if (net) h->closure_net = tmc_mlp_net(net);
+  h->O.need_pv_c = net ? 1 : 0;
+  if (h->g_step) cudaGraphExecDestroy(h->g_step);
+  if (h->g_step_diag) cudaGraphExecDestroy(h->g_step_diag);
+  h->g_step = h->g_step_diag = nullptr;
+  return TMC_OK;
+}
+
+int tmc_set_member_closure(tmc_handle* h, int32_t member, int32_t on) {
+  TMC_REQUIRE_SWM(h);
+  if (member < 0 || member >= h->members) return h->fail(TMC_E_ARG, "member out of range");
+  const int v = on ? 1 : 0;
+  if (cudaMemcpyAsync(h->d_member_on + member, &v, sizeof(int), cudaMemcpyHostToDevice, h->st) != cudaSuccess)
+    return h->cuda_check("tmc_set_member_closure");
+  return sync(h, "tmc_set_member_closure");
+}
+
+int tmc_closure_status(tmc_handle* h, int32_t* timed_out) {
+  TMC_REQUIRE_SWM(h);
+  int v = 0;
+  cudaMemcpyAsync(&v, h->d_closure_err, sizeof(int), cudaMemcpyDeviceToHost, h->st);
+  int rc = sync(h, "tmc_closure_status");
+  if (rc) return rc;
+  if (timed_out) *timed_out = v;
+  return TMC_OK;
+}
+
+int tmc_closure_features(tmc_handle* h, float* features, double* pv_edge) {
+  TMC_REQUIRE_SWM(h);
+  if (!features) return h->fail(TMC_E_ARG, "NULL array");
+  if (h->p.precision != TMC_FP32 || h->generic)
+    return h->fail(TMC_E_UNSUP, "closure features come from the FP32 CRK4 shallow-water step");
+  if (!h->have_state) return h->fail(TMC_E_STATE, "no state set");
+  const int ne = h->M.ne;
+  float *d_feat = nullptr, *d_pv = nullptr;
+  if (cudaMalloc(&d_feat, sizeof(float) * (size_t)ne * mlp::kIn) != cudaSuccess ||
+      cudaMalloc(&d_pv, sizeof(float) * ne) != cudaSuccess) {
+    cudaFree(d_feat);
+    return h->cuda_check("tmc_closure_features: allocation");
+  }
+  const int saved = h->O.need_pv_c;
+  h->O.need_pv_c = 1;
+  h->eng->closure_features(d_feat, d_pv);
+  h->O.need_pv_c = saved;
+  h->prep_valid = false;
+  std::vector<float> f((size_t)ne * mlp::kIn), pv(ne);
+  cudaMemcpyAsync(f.data(), d_feat, sizeof(float) * f.size(), cudaMemcpyDeviceToHost, h->st);
+  cudaMemcpyAsync(pv.data(), d_pv, sizeof(float) * ne, cudaMemcpyDeviceToHost, h->st);
+  int rc = sync(h, "tmc_closure_features");
+  cudaFree(d_feat);
+  cudaFree(d_pv);
+  if (rc) return rc;
+  // caller's edge order
+  for (int i = 0; i < ne; ++i) {
+    const int o = h->hm.edge_n2o[i];
+    std::memcpy(features + (size_t)o * mlp::kIn, f.data() + (size_t)i * mlp::kIn, sizeof(float) * mlp::kIn);
+    if (pv_edge) pv_edge[o] = pv[i];
+  }
+  return h->cuda_check("tmc_closure_features");
 }
 
 int tmc_adv_set_initial(tmc_handle* h, const double* q) {

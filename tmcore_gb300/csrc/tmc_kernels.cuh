@@ -93,6 +93,7 @@ struct ModelOpt {
   int tr_order;
   double tr_coef2, tr_coef4;
   int flux4;  // flux_4th_order_correct (tmcore_swm_mod.F90:183-195)
+  int need_pv_c;  // pv on cells every stage (the learned closure reads it)
 };
 
 // CRK4 stage program (time_scheme_mod.F90:109-154):
@@ -350,6 +351,21 @@ void launch_iap_from_u(int ne, const double* gd_e, const double* u, T* iap, cuda
 // FP32 shadows of gd and tracer mixing ratios of a state slot (FP32 path)
 void launch_shadows(int nc, int ntr, const double* gd, const float* q, float* gdf, float* qr, cudaStream_t st);
 void launch_to_f32(size_t n, const double* src, float* dst, cudaStream_t st);
+
+// Learned PV-on-edge closure (FP32 path, after k_edge_pv): 24 features per
+// edge from the stage state, the MLP on the tensor cores, pv_edge += the
+// output for every member whose flag is set.  `net` is a tmc::mlp::Net.
+// Needs pv_c (k_v2c) of the stage.  *err is set when a completion wait ran out.
+struct ClosureArgs {
+  const void* net;         // const tmc::mlp::Net*
+  const int* member_on;    // [members] 1: apply
+  int* err;
+  int sms;
+};
+void launch_closure(const DevMesh& M, const StageIO<float>& S, const ClosureArgs& a, cudaStream_t st);
+// the features (and pv_edge) of every edge of member m, into feat[ne][24] / pv[ne]
+void launch_closure_features(const DevMesh& M, const StageIO<float>& S, int member, float* feat, float* pv,
+                             cudaStream_t st);
 
 // single operators for parity (FP64 only)
 void launch_op(int op, const DevMesh& M, const ModelOpt& O, const double* a, const double* b, const double* c,

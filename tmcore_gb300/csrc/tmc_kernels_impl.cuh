@@ -1301,7 +1301,7 @@ void launch_vertex(const DevMesh& M, const ModelOpt& O, const StageIO<T>& S, Par
 }
 template <class T>
 void launch_edge_pv(const DevMesh& M, const ModelOpt& O, const StageIO<T>& S, int bs, cudaStream_t st) {
-  if ((O.pv_scheme == 1 && O.apvm_weight != 0.0) || O.pv_scheme == 2)
+  if ((O.pv_scheme == 1 && O.apvm_weight != 0.0) || O.pv_scheme == 2 || O.need_pv_c)
     k_v2c<T><<<dim3(grid_for(M.nc, bs), nmem(S)), bs, 0, st>>>(M, S.pv_v, S.pv_c, S.msv, S.msc);
   TMC_LAUNCH(k_edge_pv, grid_for(M.ne, bs), M, O, S);
 }

@@ -9,10 +9,13 @@
 #include <string>
 #include <vector>
 
+#include "tmc_kernels.cuh"
 #include "tmc_mlp_tc.cuh"
 #include "tmcore_gpu.h"
 
 using namespace tmc::mlp;
+using tmc::DevMesh;
+using tmc::StageIO;
 
 namespace {
 
@@ -35,6 +38,87 @@ struct BufSrc {
 __global__ void __launch_bounds__(kTile) k_mlp_fwd_tc(Net net, BufSrc src, long long ntiles, int* err) {
   extern __shared__ __align__(128) uint8_t smem[];
   if (!forward_tiles(net, src, ntiles, smem) && threadIdx.x == 0) atomicExch(err, 1);
+}
+
+// ---------------------------------------------------------------------------
+// the closure: features of an edge of one member from the stage state
+// ---------------------------------------------------------------------------
+// 0 u, 1 tangential velocity, 2 gd_edge, 3 pv_edge, 4-5 pv on the two
+// vertices, 6-7 pv on the two cells, 8-9 gd, 10-11 E = ke + gd + ghs,
+// 12-13 ghs on the two cells, 14-15 Coriolis on the two vertices, 16 dvEdge,
+// 17 dcEdge, 18-21 u on the first four edgesOnEdge, 22 pv gradient along the
+// edge, 23 pv gradient across it
+__device__ __forceinline__ void closure_features(const DevMesh& M, const StageIO<float>& S, int m, int e,
+                                                 float (&x)[kIn]) {
+  const long long oc = (long long)m * S.msc, oe = (long long)m * S.mse, ov = (long long)m * S.msv;
+  const float* u = S.u + oe;
+  const int c1 = M.cellsOnEdge[e], c2 = M.cellsOnEdge[M.ne + e];
+  const int v1 = M.verticesOnEdge[e], v2 = M.verticesOnEdge[M.ne + e];
+  float ve = 0.f;
+#pragma unroll
+  for (int i = 0; i < 10; ++i) {
+    const size_t k = (size_t)i * M.ne + e;
+    ve += u[M.edgesOnEdge[k]] * M.weightsOnEdge_f[k];  // padded entries carry weight 0
+  }
+  const float dv = M.dvEdge_f[e], dc = M.dcEdge_f[e];
+  const float pv1 = S.pv_v[ov + v1], pv2 = S.pv_v[ov + v2];
+  const float pc1 = S.pv_c[oc + c1], pc2 = S.pv_c[oc + c2];
+  x[0] = u[e];
+  x[1] = ve;
+  x[2] = S.gd_e[oe + e];
+  x[3] = S.pv_e[oe + e];
+  x[4] = pv1;
+  x[5] = pv2;
+  x[6] = pc1;
+  x[7] = pc2;
+  x[8] = S.gdf_in[oc + c1];
+  x[9] = S.gdf_in[oc + c2];
+  x[10] = S.E[oc + c1];
+  x[11] = S.E[oc + c2];
+  x[12] = S.ghsf[oc + c1];
+  x[13] = S.ghsf[oc + c2];
+  x[14] = M.fVertex_f[v1];
+  x[15] = M.fVertex_f[v2];
+  x[16] = dv;
+  x[17] = dc;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) x[18 + i] = u[M.edgesOnEdge[(size_t)i * M.ne + e]];
+  x[22] = (pv2 - pv1) / dv;
+  x[23] = (pc2 - pc1) / dc;
+}
+
+struct ClosureSrc {
+  DevMesh M;
+  StageIO<float> S;
+  const int* on;
+  long long ne, rows;
+  __device__ bool features(long long i, float (&x)[kIn]) const {
+    if (i >= rows) return false;
+    const int m = (int)(i / ne), e = (int)(i - (long long)m * ne);
+    closure_features(M, S, m, e, x);
+    return true;
+  }
+  __device__ void output(long long i, float r) const {
+    const int m = (int)(i / ne), e = (int)(i - (long long)m * ne);
+    if (on[m]) {
+      float* pe = S.pv_e + (long long)m * S.mse + e;
+      *pe = *pe + r;
+    }
+  }
+};
+
+__global__ void __launch_bounds__(kTile) k_closure(Net net, ClosureSrc src, long long ntiles, int* err) {
+  extern __shared__ __align__(128) uint8_t smem[];
+  if (!forward_tiles(net, src, ntiles, smem) && threadIdx.x == 0) atomicExch(err, 1);
+}
+
+__global__ void k_closure_features(DevMesh M, StageIO<float> S, int m, float* feat, float* pv) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= M.ne) return;
+  float x[kIn];
+  closure_features(M, S, m, e, x);
+  for (int k = 0; k < kIn; ++k) feat[(size_t)e * kIn + k] = x[k];
+  pv[e] = x[3];
 }
 
 // ---------------------------------------------------------------------------
@@ -251,6 +335,25 @@ __global__ void k_to_bf16(const float* p, __nv_bfloat16* pb, int n) {
 }
 
 }  // namespace
+
+namespace tmc {
+void launch_closure(const DevMesh& M, const StageIO<float>& S, const ClosureArgs& a, cudaStream_t st) {
+  const int members = S.members > 1 ? S.members : 1;
+  ClosureSrc src{M, S, a.member_on, M.ne, (long long)M.ne * members};
+  const long long ntiles = (src.rows + kTile - 1) / kTile;
+  const int grid = (int)std::min<long long>(ntiles, (long long)a.sms * 4);
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_closure, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemTc);
+    attr = true;
+  }
+  k_closure<<<grid, kTile, kSmemTc, st>>>(*static_cast<const Net*>(a.net), src, ntiles, a.err);
+}
+void launch_closure_features(const DevMesh& M, const StageIO<float>& S, int member, float* feat, float* pv,
+                             cudaStream_t st) {
+  k_closure_features<<<(M.ne + 255) / 256, 256, 0, st>>>(M, S, member, feat, pv);
+}
+}  // namespace tmc
 
 struct tmc_mlp {
   int device = 0;

@@ -57,3 +57,7 @@ constexpr int kSmemTc = kSmemW1 + 2 * kSmemW + kSmemA + 64;
 
 }  // namespace mlp
 }  // namespace tmc
+
+struct tmc_mlp;
+// the device view of a network handle (tmc_mlp.cu)
+tmc::mlp::Net tmc_mlp_net(const tmc_mlp* n);

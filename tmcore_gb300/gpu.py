@@ -127,6 +127,27 @@ class TMCoreGPU:
         self._chk(self.lib.tmc_autotune(self.h, int(steps), out))
         return dict(zip(("cell", "vertex", "edge_pv", "edge_flux", "final"), list(out)))
 
+    # ------------------------------------------------------------------ learned closure
+    def set_closure(self, net):
+        """Apply `net` (a ClosureMLP, or None) to pv_edge in every stage."""
+        self._closure = net
+        self._chk(self.lib.tmc_set_closure(self.h, None if net is None else net.n))
+
+    def set_member_closure(self, member: int, on: bool):
+        self._chk(self.lib.tmc_set_member_closure(self.h, int(member), 1 if on else 0))
+
+    def closure_status(self) -> bool:
+        v = ctypes.c_int32()
+        self._chk(self.lib.tmc_closure_status(self.h, ctypes.byref(v)))
+        return bool(v.value)
+
+    def closure_features(self):
+        """[nEdges, 24] features and pv_edge of state(old) of the selected member."""
+        f = np.empty((self.ne, abi.TMC_MLP_FEATURES), np.float32)
+        pv = np.empty(self.ne)
+        self._chk(self.lib.tmc_closure_features(self.h, _ptr(f), _ptr(pv)))
+        return f, pv
+
     # ------------------------------------------------------------------ ensembles
     def select_member(self, m: int):
         """State-transfer calls address member m of an ensemble (members > 1)."""
