@@ -185,6 +185,25 @@ int tmc_set_member_closure(tmc_handle* h, int32_t member, int32_t on);
 int tmc_closure_status(tmc_handle* h, int32_t* timed_out);
 int tmc_closure_features(tmc_handle* h, float* features, double* pv_edge);
 
+/* Coarse-graining of a fine-mesh state onto a coarser mesh (the closure's
+ * training data): cells are area-weighted means over the fine cells whose
+ * centres lie in the coarse cell (nearest coarse generator); the coarse
+ * normal velocity is the sum of the fine normal fluxes u dvEdge across the
+ * boundary between two coarse cells' aggregates divided by the coarse dvEdge
+ * (edge-flux averaging); edge scalars (pv on edges) are dvEdge-weighted means
+ * over the same fine edges.  Host arrays in both meshes' own order; any
+ * output pointer may be NULL.  tmc_coarsen_unmatched counts coarse edges
+ * without fine edges (their outputs are 0). */
+typedef struct tmc_coarsen tmc_coarsen;
+int tmc_coarsen_create(const tmc_mesh_desc* fine, const tmc_mesh_desc* coarse, int32_t device, tmc_coarsen** out);
+int tmc_coarsen_apply(tmc_coarsen* c, const double* fine_gd, const double* fine_u, const double* fine_pv_edge,
+                      double* coarse_gd, double* coarse_u, double* coarse_pv_edge);
+int tmc_coarsen_unmatched(const tmc_coarsen* c, int64_t* edges);
+/* the coarse cell (1-based) each fine cell is aggregated into */
+int tmc_coarsen_cell_map(const tmc_coarsen* c, int32_t* coarse_cell_of_fine);
+const char* tmc_coarsen_last_error(const tmc_coarsen* c);
+int tmc_coarsen_destroy(tmc_coarsen* c);
+
 /* Groups: several handles (different meshes and dt, each possibly an
  * ensemble) advanced together, e.g. a mixed batch of mesh levels with
  * dt = 1200 / 2^(level-4) s.  One CUDA graph per cycle of cycle_seconds holds

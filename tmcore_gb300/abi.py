@@ -96,6 +96,13 @@ SYMBOLS = {
     "tmc_set_member_closure": (ctypes.c_int, [vp, i32, i32]),
     "tmc_closure_status": (ctypes.c_int, [vp, ctypes.POINTER(i32)]),
     "tmc_closure_features": (ctypes.c_int, [vp, vp, vp]),
+    "tmc_coarsen_create": (ctypes.c_int, [ctypes.POINTER(MeshDesc), ctypes.POINTER(MeshDesc), i32,
+                                           ctypes.POINTER(vp)]),
+    "tmc_coarsen_apply": (ctypes.c_int, [vp, vp, vp, vp, vp, vp, vp]),
+    "tmc_coarsen_unmatched": (ctypes.c_int, [vp, i64p]),
+    "tmc_coarsen_cell_map": (ctypes.c_int, [vp, vp]),
+    "tmc_coarsen_last_error": (ctypes.c_char_p, [vp]),
+    "tmc_coarsen_destroy": (ctypes.c_int, [vp]),
     "tmc_adv_set_initial": (ctypes.c_int, [vp, vp]),
     "tmc_adv_get": (ctypes.c_int, [vp, vp, vp]),
     "tmc_adv_elapsed": (ctypes.c_int, [vp, dp]),

@@ -44,6 +44,22 @@ def _ptr(a):
     return None if a is None else a.ctypes.data
 
 
+def mesh_desc(mesh):
+    """tmc_mesh_desc of an MPASMesh; returns (desc, arrays to keep alive)."""
+    d = abi.MeshDesc()
+    for k in ("nCells", "nEdges", "nVertices", "maxEdges", "maxEdges2", "vertexDegree"):
+        setattr(d, k, int(mesh.dims[k]))
+    keep = []
+    for name, _ in abi.MeshDesc._fields_[6:]:
+        if name not in mesh.vars and name in ("lonCell", "lonVertex"):
+            continue  # optional: NULL
+        a = mesh.vars[name]
+        a = np.ascontiguousarray(a, dtype=np.int32 if a.dtype.kind == "i" else np.float64)
+        keep.append(a)
+        setattr(d, name, a.ctypes.data)
+    return d, keep
+
+
 class TMCoreGPU:
     """A device-resident shallow-water model (handle of the C ABI)."""
 
@@ -52,17 +68,7 @@ class TMCoreGPU:
         self.params = params if params is not None else default_params(**kw)
         self.mesh = mesh
         self.nc, self.ne, self.nv = mesh.nCells, mesh.nEdges, mesh.nVertices
-        d = abi.MeshDesc()
-        for k in ("nCells", "nEdges", "nVertices", "maxEdges", "maxEdges2", "vertexDegree"):
-            setattr(d, k, int(mesh.dims[k]))
-        self._keep = []
-        for name, _ in abi.MeshDesc._fields_[6:]:
-            if name not in mesh.vars and name in ("lonCell", "lonVertex"):
-                continue  # optional: NULL
-            a = mesh.vars[name]
-            a = np.ascontiguousarray(a, dtype=np.int32 if a.dtype.kind == "i" else np.float64)
-            self._keep.append(a)
-            setattr(d, name, a.ctypes.data)
+        d, self._keep = mesh_desc(mesh)
         h = ctypes.c_void_p()
         rc = self.lib.tmc_create(ctypes.byref(d), ctypes.byref(self.params), ctypes.byref(h))
         self.h = h
@@ -343,3 +349,53 @@ class ClosureMLP:
         loss = ctypes.c_double()
         self._chk(self.lib.tmc_mlp_gradient(self.n, _ptr(x), _ptr(y), x.shape[0], _ptr(g), ctypes.byref(loss)))
         return g, loss.value
+
+
+class Coarsener:
+    """Coarse-graining of fine-mesh fields onto a coarser mesh (tmc_coarsen_*)."""
+
+    def __init__(self, fine, coarse, device: int = 0):
+        self.lib = _lib.gpu()
+        self.fine, self.coarse = fine, coarse
+        df, kf = mesh_desc(fine)
+        dc, kc = mesh_desc(coarse)
+        c = ctypes.c_void_p()
+        rc = self.lib.tmc_coarsen_create(ctypes.byref(df), ctypes.byref(dc), int(device), ctypes.byref(c))
+        self.c = c
+        if rc != 0:
+            msg = self.lib.tmc_coarsen_last_error(c).decode() if c.value else "tmc_coarsen_create failed"
+            self.close()
+            raise TMCError(rc, msg)
+
+    def unmatched(self) -> int:
+        n = ctypes.c_int64()
+        self.lib.tmc_coarsen_unmatched(self.c, ctypes.byref(n))
+        return n.value
+
+    def cell_map(self) -> np.ndarray:
+        """0-based coarse cell of every fine cell."""
+        m = np.empty(self.fine.nCells, np.int32)
+        self.lib.tmc_coarsen_cell_map(self.c, _ptr(m))
+        return m - 1
+
+    def __call__(self, gd=None, u=None, pv_edge=None):
+        nc, ne = self.coarse.nCells, self.coarse.nEdges
+        og = np.empty(nc) if gd is not None else None
+        ou = np.empty(ne) if u is not None else None
+        op = np.empty(ne) if pv_edge is not None else None
+        a = [None if v is None else _f64(v) for v in (gd, u, pv_edge)]
+        rc = self.lib.tmc_coarsen_apply(self.c, _ptr(a[0]), _ptr(a[1]), _ptr(a[2]), _ptr(og), _ptr(ou), _ptr(op))
+        if rc != 0:
+            raise TMCError(rc, self.lib.tmc_coarsen_last_error(self.c).decode())
+        return og, ou, op
+
+    def close(self):
+        if getattr(self, "c", None) is not None and self.c.value:
+            self.lib.tmc_coarsen_destroy(self.c)
+        self.c = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
