@@ -116,6 +116,8 @@ int tmc_step(tmc_handle* h, int32_t nsteps);
  *  total_absolute_vorticity, beta} of state(old) (tmcore_swm_mod.F90:215-255,
  *  diag_mod.F90:76-91); synchronises. */
 int tmc_get_diag(tmc_handle* h, double out[5]);
+/* the same for every ensemble member: out[members][5] */
+int tmc_get_diag_all(tmc_handle* h, double* out);
 int tmc_synchronize(tmc_handle* h);
 
 /* time_integrate with host arrays: state(old) in, state(new) out, one step

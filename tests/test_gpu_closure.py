@@ -93,3 +93,42 @@ def test_member_switch(mesh4):
     ens.close()
     plain.close()
     net.close()
+
+
+def test_training_data_and_training_small():
+    """Level-4 FP64 runs coarse-grained to level 3: finite features, a
+    non-zero PV-on-edge residual, and a loss that falls."""
+    from tmcore_gb300 import closure
+
+    X, Y = closure.training_data(fine_level=4, coarse_level=3, runs=1, days=0.25, samples_per_run=2)
+    assert X.shape == (2 * 1920, 24) and Y.shape == (2 * 1920,)
+    assert np.all(np.isfinite(X)) and np.all(np.isfinite(Y)) and np.std(Y) > 0
+    net, losses, sc = closure.train(X, Y, steps=150, batch=1920, lr=3e-3)
+    assert losses[-10:].mean() < 0.7 * losses[:3].mean()
+    net.close()
+
+
+def test_fallback_switches_off_a_drifting_member(mesh4):
+    from tmcore_gb300.closure import FallbackMonitor
+    from tmcore_gb300.gpu import ClosureMLP, TMCoreGPU
+
+    good = ClosureMLP(seed=3)
+    good.params = np.zeros(9985, np.float32)
+    bad = ClosureMLP(seed=4)
+    bad.set_scaling(np.zeros(24), np.ones(24), 1e-6)  # pv corrections 100x the pv itself
+    for net, expect in ((good, 0), (bad, 3)):
+        ens = TMCoreGPU(mesh4, members=3, diag_every=0, **KW)
+        for k in range(3):
+            gd, u, ghs = _ic(mesh4, 90 + k)
+            ens.select_member(k)
+            ens.set_initial(gd, u, ghs)
+        ens.set_closure(net)
+        mon = FallbackMonitor(ens, 3, tol=1e-4, every=4)
+        mon.step(12)
+        assert len({m for m, _ in mon.fallbacks}) == expect
+        for k in range(3):
+            ens.select_member(k)
+            assert np.all(np.isfinite(ens.get_state()[0]))
+        ens.close()
+    good.close()
+    bad.close()

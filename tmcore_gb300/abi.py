@@ -60,6 +60,7 @@ SYMBOLS = {
     "tmc_get_tracers": (ctypes.c_int, [vp, vp]),
     "tmc_step": (ctypes.c_int, [vp, i32]),
     "tmc_get_diag": (ctypes.c_int, [vp, vp]),
+    "tmc_get_diag_all": (ctypes.c_int, [vp, vp]),
     "tmc_synchronize": (ctypes.c_int, [vp]),
     "tmc_time_integrate": (ctypes.c_int, [vp, vp, vp, vp, vp, vp, vp]),
     "tmc_spatial_operators": (ctypes.c_int, [vp, vp, vp, vp, vp]),

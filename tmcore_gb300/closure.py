@@ -1,0 +1,193 @@
+"""The learned PV-on-edge closure: training data, training, and ensembles
+with a per-member invariant-drift fallback.
+
+Training data: FP64 runs of the fine mesh (seeded jet + mountains), sampled
+at intervals and coarse-grained on the device (``Coarsener``); the coarse FP32
+model is set to each coarse-grained state and exports its closure features
+and its own pv on edges; the target is the coarse-grained fine pv on edges
+minus the coarse model's (the PV-on-edge residual).  Training is Adam on the
+device (``ClosureMLP``).  Inference runs inside the FP32 step of an ensemble
+(``TMCoreGPU.set_closure``); ``FallbackMonitor`` switches the closure off for
+a member whose total energy or mass drifts beyond a bound and restores that
+member's last checkpoint.
+
+Run ``python -m tmcore_gb300.closure --help`` for the end-to-end pipeline.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import time
+
+import numpy as np
+
+from . import abi, cases
+from .gpu import ClosureMLP, Coarsener, TMCoreGPU
+from .mesh import icos_mesh
+
+DAY = 86400.0
+
+
+def level_dt(level: int) -> float:
+    """dt = 1200 / 2^(level - 4) s."""
+    return 1200.0 / 2 ** (level - 4)
+
+
+def _edge_pv(mesh, pv_vertex):
+    v1, v2 = mesh.verticesOnEdge[:, 0] - 1, mesh.verticesOnEdge[:, 1] - 1
+    return 0.5 * (pv_vertex[v1] + pv_vertex[v2])
+
+
+def training_data(fine_level=8, coarse_level=6, runs=4, days=1.0, samples_per_run=8, seed0=0, device=0,
+                  log=None):
+    """(features [N, 24] float32, targets [N] float32) from FP64 fine runs."""
+    fine, coarse = icos_mesh(fine_level), icos_mesh(coarse_level)
+    cg = Coarsener(fine, coarse, device=device)
+    dt_f = level_dt(fine_level)
+    steps = max(1, int(round(days * DAY / dt_f / samples_per_run)))
+    kw = dict(pv_scheme=1, apvm_weight=0.0, adv_order=2, conserve_energy=1, renumber=1, device=device)
+    cm = TMCoreGPU(coarse, dt=level_dt(coarse_level), precision=abi.TMC_FP32, **kw)
+    X, Y = [], []
+    for r in range(runs):
+        gd, u, ghs = cases.jet_bumps(fine, seed=seed0 + r)
+        fm = TMCoreGPU(fine, dt=dt_f, precision=abi.TMC_FP64, diag_every=0, **kw)
+        fm.set_initial(gd, u, ghs)
+        ghs_c, _, _ = cg(gd=ghs)
+        for s in range(samples_per_run):
+            fm.step(steps)
+            gdf, _, uf = fm.get_state()
+            pvv, _ = fm.get_vertex()
+            gd_c, u_c, pv_true = cg(gd=gdf, u=uf, pv_edge=_edge_pv(fine, pvv))
+            cm.set_initial(gd_c, u_c, ghs_c)
+            x, pv_c = cm.closure_features()
+            X.append(x)
+            Y.append((pv_true - pv_c).astype(np.float32))
+            if log:
+                log(f"run {r} sample {s}: |residual| {np.sqrt(np.mean(Y[-1] ** 2)):.3e}")
+        fm.close()
+    cm.close()
+    cg.close()
+    return np.concatenate(X), np.concatenate(Y)
+
+
+def train(X, Y, steps=2000, batch=65536, lr=1e-3, seed=0, device=0):
+    """A ClosureMLP fitted to (X, Y); returns (net, losses, scaling)."""
+    rng = np.random.default_rng(seed)
+    perm = rng.permutation(len(Y))
+    X, Y = X[perm], Y[perm]
+    xm = X.mean(0).astype(np.float64)
+    xs = X.std(0).astype(np.float64)
+    xs[xs == 0] = 1.0
+    ys = float(np.std(Y)) or 1.0
+    net = ClosureMLP(device=device, seed=seed)
+    net.set_scaling(xm, 1.0 / xs, ys)
+    net.set_dataset(X, Y)
+    b = min(batch, (len(Y) // 128) * 128)
+    losses = net.train(steps=steps, batch=b, lr=lr)
+    return net, losses, {"x_mean": xm, "x_inv_std": 1.0 / xs, "y_scale": ys}
+
+
+def save(path, net, scaling):
+    np.savez(path, params=net.params, **scaling)
+
+
+def load(path, device=0):
+    z = np.load(path)
+    net = ClosureMLP(device=device)
+    net.params = z["params"]
+    net.set_scaling(z["x_mean"], z["x_inv_std"], float(z["y_scale"]))
+    return net
+
+
+class FallbackMonitor:
+    """Per-member invariant-drift fallback: every `every` steps, a member whose
+    relative drift of total energy (or mass) since its start exceeds `tol`
+    gets the closure switched off and its state rolled back to its last
+    checkpoint (taken at the previous check)."""
+
+    def __init__(self, model: TMCoreGPU, members: int, tol: float = 1e-3, every: int = 24):
+        self.model, self.members, self.tol, self.every = model, members, tol, every
+        d = model.diag_all()
+        self.ref = d[:, :2].copy()
+        self.on = np.ones(members, bool)
+        self.fallbacks: list[tuple[int, int]] = []
+        self.steps = 0
+        self.ckpt = [self._save(m) for m in range(members)]
+
+    def _save(self, m):
+        self.model.select_member(m)
+        return self.model.get_state(with_u=False)
+
+    def step(self, n: int):
+        """Advance all members n steps, checking every `every` steps."""
+        while n > 0:
+            k = min(n, self.every - self.steps % self.every)
+            self.model.step(k)
+            self.steps += k
+            n -= k
+            if self.steps % self.every == 0:
+                self.check()
+
+    def check(self):
+        d = self.model.diag_all()
+        drift = np.abs(d[:, :2] - self.ref) / np.abs(self.ref)
+        bad = np.flatnonzero(self.on & ((drift.max(1) > self.tol) | ~np.all(np.isfinite(d[:, :2]), 1)))
+        for m in bad:
+            self.model.set_member_closure(int(m), False)
+            self.on[m] = False
+            self.model.select_member(int(m))
+            gd, iap = self.ckpt[m]
+            self.model.set_state(gd, iap)
+            self.fallbacks.append((int(m), self.steps))
+        for m in np.flatnonzero(self.on):
+            self.ckpt[m] = self._save(int(m))
+        return bad
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
+    ap.add_argument("--fine-level", type=int, default=8)
+    ap.add_argument("--coarse-level", type=int, default=6)
+    ap.add_argument("--runs", type=int, default=4)
+    ap.add_argument("--days", type=float, default=1.0)
+    ap.add_argument("--samples", type=int, default=8)
+    ap.add_argument("--steps", type=int, default=1500)
+    ap.add_argument("--members", type=int, default=256)
+    ap.add_argument("--ens-days", type=float, default=1.0)
+    ap.add_argument("--out", default=None, help="save the trained network (.npz)")
+    a = ap.parse_args()
+    t0 = time.time()
+    X, Y = training_data(a.fine_level, a.coarse_level, a.runs, a.days, a.samples)
+    t_data = time.time() - t0
+    t0 = time.time()
+    net, losses, sc = train(X, Y, steps=a.steps)
+    t_train = time.time() - t0
+    if a.out:
+        save(a.out, net, sc)
+    # held-out ensemble on the coarse mesh with the closure and the fallback
+    coarse = icos_mesh(a.coarse_level)
+    dt = level_dt(a.coarse_level)
+    ens = TMCoreGPU(coarse, members=a.members, dt=dt, precision=abi.TMC_FP32, pv_scheme=1, apvm_weight=0.0,
+                    diag_every=0)
+    for m in range(a.members):
+        gd, u, ghs = cases.jet_bumps(coarse, seed=10_000 + m)
+        ens.select_member(m)
+        ens.set_initial(gd, u, ghs)
+    ens.set_closure(net)
+    mon = FallbackMonitor(ens, a.members)
+    nsteps = int(round(a.ens_days * DAY / dt))
+    t0 = time.time()
+    mon.step(nsteps)
+    ens.synchronize()
+    t_ens = time.time() - t0
+    print(json.dumps({
+        "training_samples": int(len(Y)), "data_s": t_data, "train_s": t_train,
+        "loss_first": float(losses[0]), "loss_last": float(np.mean(losses[-20:])),
+        "ensemble": {"members": a.members, "level": a.coarse_level, "steps": nsteps, "wall_s": t_ens,
+                     "member_days_per_s": a.members * nsteps * dt / DAY / t_ens,
+                     "fallbacks": len(mon.fallbacks), "closure_timed_out": ens.closure_status()},
+    }))
+
+
+if __name__ == "__main__":
+    main()

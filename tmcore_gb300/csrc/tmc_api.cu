@@ -1078,6 +1078,23 @@ int tmc_get_diag(tmc_handle* h, double out[5]) {
   return h->cuda_check("tmc_get_diag");
 }
 
+int tmc_get_diag_all(tmc_handle* h, double* out) {
+  TMC_REQUIRE_HANDLE(h);
+  if (!out) return TMC_E_ARG;
+  if (!h->have_state) return h->fail(TMC_E_STATE, "no state set");
+  h->eng->launch_diag_pass(true);
+  std::vector<double> all((size_t)kDiagStride * h->members);
+  cudaMemcpyAsync(all.data(), h->d_diag, sizeof(double) * all.size(), cudaMemcpyDeviceToHost, h->st);
+  int rc = sync(h, "tmc_get_diag_all");
+  if (rc) return rc;
+  for (int m = 0; m < h->members; ++m) {
+    const double* d = all.data() + (size_t)m * kDiagStride;
+    for (int i = 0; i < 4; ++i) out[(size_t)m * 5 + i] = d[i];
+    out[(size_t)m * 5 + 4] = h->step_count > 0 ? d[4] : 1.0;
+  }
+  return h->cuda_check("tmc_get_diag_all");
+}
+
 int tmc_time_integrate(tmc_handle* h, const double* gd_old, const double* iap_u_old, const double* qgd_old,
                        double* gd_new, double* iap_u_new, double* qgd_new) {
   TMC_REQUIRE_SWM(h);

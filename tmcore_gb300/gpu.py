@@ -187,6 +187,13 @@ class TMCoreGPU:
         self._chk(self.lib.tmc_get_diag(self.h, _ptr(out)))
         return out
 
+    def diag_all(self):
+        """[members, 5] invariants and beta of every ensemble member."""
+        m = int(self.params.members) if self.params.members > 1 else 1
+        out = np.empty((m, 5))
+        self._chk(self.lib.tmc_get_diag_all(self.h, _ptr(out)))
+        return out
+
     def time_integrate(self, gd_old, iap_old, q_old=None, out=None):
         """One step with host arrays in and out (tmc_time_integrate)."""
         if out is None:
