@@ -54,6 +54,7 @@ def parse():
     ap.add_argument("--ensemble-level", type=int, default=6)
     ap.add_argument("--ensemble-steps", type=int, default=20)
     ap.add_argument("--mixed-members", type=int, default=16, help="members per level of the mixed batch (0: skip)")
+    ap.add_argument("--closure-members", type=int, default=256, help="ensemble with the learned closure (0: skip)")
     ap.add_argument("--mixed-cycles", type=int, default=5)
     return ap.parse_args()
 
@@ -318,6 +319,47 @@ def run_ensemble(args, local, ics, peak):
             "gpu_launches": launches, "member0_beta": float(d[4]), "block_sizes": tuned}
 
 
+def run_closure_leg(args, local, ics, peak):
+    """Config 5's step: the FP32 ensemble with the learned closure on (a
+    network of the trained shape; the cost does not depend on its weights),
+    against the same ensemble without it."""
+    import numpy as np
+
+    from tmcore_gb300 import abi, mesh
+    from tmcore_gb300.gpu import ClosureMLP, TMCoreGPU
+
+    L, M = args.ensemble_level, len(ics)
+    m = mesh.icos_mesh(L)
+    dt = 1200.0 / 2 ** (L - 4)
+    net = ClosureMLP(device=local, seed=1)
+    net.set_scaling(np.zeros(24), np.ones(24), 1e-12)
+    ens = TMCoreGPU(m, members=M, dt=dt, pv_scheme=1, apvm_weight=0.0, adv_order=2, conserve_energy=1,
+                    precision=abi.TMC_FP32, diag_every=1, use_graph=1, renumber=1, device=local)
+    for k, (gd, u, ghs) in enumerate(ics):
+        ens.select_member(k)
+        ens.set_initial(gd, u, ghs)
+    if not args.no_autotune:
+        ens.autotune(steps=2)
+    ens.step(args.warmup)
+    ens.synchronize()
+    ms_plain, _, _, _ = ens.time_steps(args.ensemble_steps, total=True, flux=False)
+    ens.set_closure(net)
+    ens.step(args.warmup)
+    ens.synchronize()
+    ms, _, _, launches = ens.time_steps(args.ensemble_steps, total=True, flux=False)
+    timed_out = ens.closure_status()
+    ens.close()
+    net.close()
+    step_s = ms / args.ensemble_steps / 1e3
+    flops = 4 * M * m.nEdges * 2.0 * (32 * 64 + 2 * 64 * 64)  # tensor-core MMA flops per step (K padded to 32)
+    return {"workload": f"{M} FP32 members on level {L} with the learned PV-on-edge closure every stage",
+            "members": M, "ms_per_step": step_s * 1e3, "member_days_per_s": M * dt / DAY / step_s,
+            "plain_ms_per_step": ms_plain / args.ensemble_steps,
+            "closure_tflops": flops / 1e12 / (step_s - ms_plain / args.ensemble_steps / 1e3)
+            if step_s * 1e3 > ms_plain / args.ensemble_steps else None,
+            "closure_mma_tflops_per_step": flops / 1e12, "gpu_launches": launches, "timed_out": timed_out}
+
+
 def ncu_traffic(name: str):
     """dram bytes per launch from the committed ncu summary, if present."""
     p = os.path.join(ROOT, "profiles", name)
@@ -523,6 +565,8 @@ def main():
 
     if ens_ics is not None:
         extra["ensemble"] = run_ensemble(args, local, ens_ics, peak)
+        if args.closure_members > 0:
+            extra["closure"] = run_closure_leg(args, local, ens_ics[:args.closure_members], peak)
         ens_ics = None
     if mixed_ics:
         extra["mixed_batch"] = run_mixed(args, local, mixed_ics, peak)
