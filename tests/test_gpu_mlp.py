@@ -62,8 +62,10 @@ def test_tensor_core_forward_matches_model():
     p = net.params
     y_tc = net.forward(x, tensor_cores=True)
     y_ref, _, _ = forward_np(p, x, round_act=True)
+    # the tensor-core epilogue evaluates bias and GELU in packed BF16 arithmetic
     scale = np.max(np.abs(y_ref))
-    assert np.max(np.abs(y_tc - y_ref)) < 1e-2 * scale
+    assert np.max(np.abs(y_tc - y_ref)) < 3e-2 * scale
+    assert np.sqrt(np.mean((y_tc - y_ref) ** 2)) < 1e-2 * np.sqrt(np.mean(y_ref ** 2))
     y_simt = net.forward(x, tensor_cores=False)
     y_fp, _, _ = forward_np(p, x, round_act=False)
     assert np.max(np.abs(y_simt - y_fp)) < 1e-4 * np.max(np.abs(y_fp))

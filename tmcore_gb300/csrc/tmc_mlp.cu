@@ -35,7 +35,7 @@ struct BufSrc {
   __device__ void output(long long i, float v) const { y[i] = v; }
 };
 
-__global__ void __launch_bounds__(kTile) k_mlp_fwd_tc(Net net, BufSrc src, long long ntiles, int* err) {
+__global__ void __launch_bounds__(kTcThreads) k_mlp_fwd_tc(Net net, BufSrc src, long long ntiles, int* err) {
   extern __shared__ __align__(128) uint8_t smem[];
   if (!forward_tiles(net, src, ntiles, smem) && threadIdx.x == 0) atomicExch(err, 1);
 }
@@ -87,27 +87,36 @@ __device__ __forceinline__ void closure_features(const DevMesh& M, const StageIO
   x[23] = (pc2 - pc1) / dc;
 }
 
+// rows: tile-major per member (tiles_per_member tiles of 128 edges each), so
+// the member and the edge of a row come from the tile index without a 64-bit
+// division; rows past a member's last edge are empty
 struct ClosureSrc {
   DevMesh M;
   StageIO<float> S;
   const int* on;
-  long long ne, rows;
+  int members, tpm;
+  __device__ bool where(long long i, int& m, int& e) const {
+    const int tile = (int)(i >> 7), t = (int)(i & (kTile - 1));
+    m = tile / tpm;
+    e = (tile - m * tpm) * kTile + t;
+    return m < members && e < M.ne;
+  }
   __device__ bool features(long long i, float (&x)[kIn]) const {
-    if (i >= rows) return false;
-    const int m = (int)(i / ne), e = (int)(i - (long long)m * ne);
+    int m, e;
+    if (!where(i, m, e)) return false;
     closure_features(M, S, m, e, x);
     return true;
   }
   __device__ void output(long long i, float r) const {
-    const int m = (int)(i / ne), e = (int)(i - (long long)m * ne);
-    if (on[m]) {
+    int m, e;
+    if (where(i, m, e) && on[m]) {
       float* pe = S.pv_e + (long long)m * S.mse + e;
       *pe = *pe + r;
     }
   }
 };
 
-__global__ void __launch_bounds__(kTile) k_closure(Net net, ClosureSrc src, long long ntiles, int* err) {
+__global__ void __launch_bounds__(kTcThreads) k_closure(Net net, ClosureSrc src, long long ntiles, int* err) {
   extern __shared__ __align__(128) uint8_t smem[];
   if (!forward_tiles(net, src, ntiles, smem) && threadIdx.x == 0) atomicExch(err, 1);
 }
@@ -339,15 +348,16 @@ __global__ void k_to_bf16(const float* p, __nv_bfloat16* pb, int n) {
 namespace tmc {
 void launch_closure(const DevMesh& M, const StageIO<float>& S, const ClosureArgs& a, cudaStream_t st) {
   const int members = S.members > 1 ? S.members : 1;
-  ClosureSrc src{M, S, a.member_on, M.ne, (long long)M.ne * members};
-  const long long ntiles = (src.rows + kTile - 1) / kTile;
-  const int grid = (int)std::min<long long>(ntiles, (long long)a.sms * 4);
+  const int tpm = (M.ne + kTile - 1) / kTile;
+  ClosureSrc src{M, S, a.member_on, members, tpm};
+  const long long ntiles = (long long)tpm * members;
+  const int grid = (int)std::min<long long>(ntiles, (long long)a.sms * 8);
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(k_closure, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemTc);
     attr = true;
   }
-  k_closure<<<grid, kTile, kSmemTc, st>>>(*static_cast<const Net*>(a.net), src, ntiles, a.err);
+  k_closure<<<grid, kTcThreads, kSmemTc, st>>>(*static_cast<const Net*>(a.net), src, ntiles, a.err);
 }
 void launch_closure_features(const DevMesh& M, const StageIO<float>& S, int member, float* feat, float* pv,
                              cudaStream_t st) {
@@ -504,9 +514,9 @@ int tmc_mlp_forward(tmc_mlp* n, const float* x, int64_t rows, float* y, int32_t 
   cudaMemcpyAsync(n->io_x, x, sizeof(float) * kIn * rows, cudaMemcpyHostToDevice, n->st);
   if (tensor_cores) {
     const long long ntiles = (rows + kTile - 1) / kTile;
-    const int grid = (int)std::min<long long>(ntiles, (long long)n->sms * 4);
+    const int grid = (int)std::min<long long>(ntiles, (long long)n->sms * 8);
     cudaMemsetAsync(n->d_err, 0, sizeof(int), n->st);
-    k_mlp_fwd_tc<<<grid, kTile, kSmemTc, n->st>>>(n->net(), BufSrc{n->io_x, n->io_y, rows}, ntiles, n->d_err);
+    k_mlp_fwd_tc<<<grid, kTcThreads, kSmemTc, n->st>>>(n->net(), BufSrc{n->io_x, n->io_y, rows}, ntiles, n->d_err);
   } else {
     const int grid = (int)std::min<long long>((rows + 127) / 128, (long long)n->sms * 8);
     k_mlp_fwd_simt<<<grid, 128, sizeof(SimtW), n->st>>>(n->net(), n->io_x, n->io_y, rows);

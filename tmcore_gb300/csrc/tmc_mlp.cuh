@@ -24,6 +24,7 @@ constexpr int kIn = 24;     // features per edge
 constexpr int kInPad = 32;  // first-layer K padded to two MMA K-steps
 constexpr int kH = 64;      // hidden width
 constexpr int kTile = 128;  // edges per tensor-core tile (MMA M)
+constexpr int kTcThreads = 128;  // threads per block of the tensor-core forward (one per row)
 
 // parameter vector layout (FP32 master copy; the BF16 copy has the same layout)
 constexpr int kOffW1 = 0;

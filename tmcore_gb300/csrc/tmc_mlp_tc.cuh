@@ -102,6 +102,34 @@ __device__ __forceinline__ float tanh_fast(float x) {
   return y;
 }
 
+// GELU (tanh form) on a pair of BF16 values with packed BF16 arithmetic:
+// 0.5 z (1 + tanh(c (z + 0.044715 z^3))), tanh.approx on the pair
+__device__ __forceinline__ __nv_bfloat162 tanh_bf16x2(__nv_bfloat162 x) {
+  uint32_t in = *reinterpret_cast<uint32_t*>(&x), out;
+  asm("tanh.approx.bf16x2 %0, %1;" : "=r"(out) : "r"(in));
+  return *reinterpret_cast<__nv_bfloat162*>(&out);
+}
+// 2 gelu(z) = z (1 + tanh(c (z + 0.044715 z^3))); the factor 1/2 is folded
+// into the next layer's weights (exact in BF16)
+__device__ __forceinline__ __nv_bfloat162 gelu2_bf16x2(__nv_bfloat162 z) {
+  const __nv_bfloat162 k0 = __float2bfloat162_rn(0.7978845608028654f);
+  const __nv_bfloat162 k1 = __float2bfloat162_rn(0.7978845608028654f * 0.044715f);
+  const __nv_bfloat162 a = __hmul2(z, __hfma2(__hmul2(z, z), k1, k0));
+  return __hfma2(z, tanh_bf16x2(a), z);
+}
+
+// (bias and) GELU of 16 accumulator columns into 8 BF16 pairs; without a bias
+// the bias came through the MMA (layer 1: two input columns of ones)
+template <bool kBias>
+__device__ __forceinline__ void bias_gelu16(const float (&d)[16], const float* b, __nv_bfloat162 (&h)[8]) {
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const float z0 = kBias ? d[2 * j] + b[2 * j] : d[2 * j];
+    const float z1 = kBias ? d[2 * j + 1] + b[2 * j + 1] : d[2 * j + 1];
+    h[j] = gelu2_bf16x2(__floats2bfloat162_rn(z0, z1));
+  }
+}
+
 // store 8 consecutive K values of one row (16 bytes) of a K-major operand
 __device__ __forceinline__ void store8_bf16(uint8_t* base, int row, int k0, int K, const float* v) {
   __nv_bfloat162 h[4];
@@ -110,11 +138,28 @@ __device__ __forceinline__ void store8_bf16(uint8_t* base, int row, int k0, int 
   *reinterpret_cast<uint4*>(base + core_off(row, k0, K)) = *reinterpret_cast<uint4*>(h);
 }
 
+// Named barrier of the 128 threads of one tile group (ids 1, 2, ...).
+__device__ __forceinline__ void group_sync(int id) { asm volatile("bar.sync %0, 128;" ::"r"(id) : "memory"); }
+__device__ __forceinline__ bool group_sync_and(int id, bool v) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\t"
+      "setp.ne.u32 p, %1, 0;\n\t"
+      "bar.red.and.pred q, %2, 128, p;\n\t"
+      "selp.u32 %0, 1, 0, q;\n\t}\n"
+      : "=r"(r)
+      : "r"((uint32_t)v), "r"(id)
+      : "memory");
+  return r != 0;
+}
+
 // Forward of the MLP over tiles of 128 rows on the tensor cores.  Src
-// provides, for row index i of the current tile, `bool features(long long i,
-// float (&x)[kIn])` (false: no row) and `void output(long long i, float y)`.
-// 128 threads; thread t owns row t of every tile (TMEM lane t).  Returns
-// false (uniformly) when an mbarrier wait ran out.
+// provides, for row index i, `bool features(long long i, float (&x)[kIn])`
+// (false: no row) and `void output(long long i, float y)`.  128 threads per
+// block; thread t owns row t of every tile (TMEM lane t).  The features of
+// the block's next tile are loaded while the current tile runs through the
+// three layers.  Returns false when an mbarrier wait ran out (uniformly over
+// the block).
 template <class Src>
 __device__ bool forward_tiles(const Net& net, Src& src, long long ntiles, uint8_t* smem) {
   uint8_t* sW1 = smem;
@@ -122,28 +167,38 @@ __device__ bool forward_tiles(const Net& net, Src& src, long long ntiles, uint8_
   uint8_t* sW3 = sW2 + kSmemW;
   uint8_t* sA = sW3 + kSmemW;
   uint64_t* mbar = reinterpret_cast<uint64_t*>(sA + kSmemA);
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(sA + kSmemA + 8);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 1);
   __shared__ float sb[3][kH];
   __shared__ float sw4[kH];
   __shared__ float sxm[kIn], sxi[kIn];
   const int t = threadIdx.x, warp = t >> 5;
 
-  // weights (BF16, K-major: row = output unit, K = input) and biases
+  // weights (BF16, K-major: row = output unit, K = input).  Layer 1: its
+  // bias as two BF16 columns (high and low part) against input columns 24-25
+  // of ones.  Layers 2-4: weights halved (exact), since the epilogue returns
+  // 2 gelu(z).
   for (int i = t; i < kH * kInPad; i += blockDim.x) {
     const int n = i / kInPad, k = i % kInPad;
-    const __nv_bfloat16 w = k < kIn ? net.pb[kOffW1 + n * kIn + k] : __float2bfloat16_rn(0.f);
+    __nv_bfloat16 w = __float2bfloat16_rn(0.f);
+    if (k < kIn) {
+      w = net.pb[kOffW1 + n * kIn + k];
+    } else if (k == kIn || k == kIn + 1) {
+      const float b = net.p[kOffB1 + n];
+      const __nv_bfloat16 hi = __float2bfloat16_rn(b);
+      w = k == kIn ? hi : __float2bfloat16_rn(b - __bfloat162float(hi));
+    }
     *reinterpret_cast<__nv_bfloat16*>(sW1 + core_off(n, k, kInPad)) = w;
   }
   for (int i = t; i < kH * kH; i += blockDim.x) {
     const int n = i / kH, k = i % kH;
-    *reinterpret_cast<__nv_bfloat16*>(sW2 + core_off(n, k, kH)) = net.pb[kOffW2 + i];
-    *reinterpret_cast<__nv_bfloat16*>(sW3 + core_off(n, k, kH)) = net.pb[kOffW3 + i];
+    *reinterpret_cast<__nv_bfloat16*>(sW2 + core_off(n, k, kH)) = __hmul(net.pb[kOffW2 + i], __float2bfloat16_rn(0.5f));
+    *reinterpret_cast<__nv_bfloat16*>(sW3 + core_off(n, k, kH)) = __hmul(net.pb[kOffW3 + i], __float2bfloat16_rn(0.5f));
   }
   for (int i = t; i < kH; i += blockDim.x) {
     sb[0][i] = net.p[kOffB1 + i];
     sb[1][i] = net.p[kOffB2 + i];
     sb[2][i] = net.p[kOffB3 + i];
-    sw4[i] = __bfloat162float(net.pb[kOffW4 + i]);
+    sw4[i] = 0.5f * __bfloat162float(net.pb[kOffW4 + i]);
   }
   for (int i = t; i < kIn; i += blockDim.x) {
     sxm[i] = net.xmean[i];
@@ -172,22 +227,31 @@ __device__ bool forward_tiles(const Net& net, Src& src, long long ntiles, uint8_
   uint32_t phase = 0;
   bool ok = true;
 
-  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+  long long tile = blockIdx.x;
+  float xn[kIn];
+  bool vn = tile < ntiles ? src.features(tile * kTile + t, xn) : false;
+  for (; tile < ntiles; tile += gridDim.x) {
     const long long row = tile * kTile + t;
-    float x[kIn];
-    const bool valid = src.features(row, x);
+    const bool valid = vn;
     {
       float xs[kInPad];
 #pragma unroll
-      for (int k = 0; k < kIn; ++k) xs[k] = valid ? (x[k] - sxm[k]) * sxi[k] : 0.f;
+      for (int k = 0; k < kIn; ++k) xs[k] = valid ? (xn[k] - sxm[k]) * sxi[k] : 0.f;
+      xs[kIn] = 1.f;  // the two columns of ones that carry layer 1's bias
+      xs[kIn + 1] = 1.f;
 #pragma unroll
-      for (int k = kIn; k < kInPad; ++k) xs[k] = 0.f;
+      for (int k = kIn + 2; k < kInPad; ++k) xs[k] = 0.f;
 #pragma unroll
       for (int k0 = 0; k0 < kInPad; k0 += 8) store8_bf16(sA, t, k0, kInPad, xs + k0);
     }
     fence_async_smem();
     fence_before_sync();
     __syncthreads();
+    // the next tile's features, in flight during this tile's layers
+    {
+      const long long nt = tile + gridDim.x;
+      vn = nt < ntiles ? src.features(nt * kTile + t, xn) : false;
+    }
     float y = b4;
 #pragma unroll 1
     for (int l = 0; l < 3; ++l) {
@@ -207,22 +271,35 @@ __device__ bool forward_tiles(const Net& net, Src& src, long long ntiles, uint8_
       if (!ok) break;
       fence_after_sync();
 #pragma unroll
-      for (int c = 0; c < kH; c += 16) {
-        float d[16];
-        tmem_ld16(tl + c, d);
+      for (int half = 0; half < 2; ++half) {
+        // 32 accumulator columns of this row: two loads, one wait
+        const int c0 = 32 * half;
+        float d0[16], d1[16];
+        tmem_ld16(tl + c0, d0);
+        tmem_ld16(tl + c0 + 16, d1);
         tmem_wait_ld();
-        float h[16];
-#pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          const float z = d[j] + sb[l][c + j];
-          h[j] = gelu_tanh(z, tanh_fast(gelu_arg(z)));
+        __nv_bfloat162 h[2][8];
+        if (l == 0) {
+          bias_gelu16<false>(d0, nullptr, h[0]);
+          bias_gelu16<false>(d1, nullptr, h[1]);
+        } else {
+          bias_gelu16<true>(d0, sb[l] + c0, h[0]);
+          bias_gelu16<true>(d1, sb[l] + c0 + 16, h[1]);
         }
         if (l < 2) {
-          store8_bf16(sA, t, c, kH, h);
-          store8_bf16(sA, t, c + 8, kH, h + 8);
+#pragma unroll
+          for (int q = 0; q < 2; ++q) {
+            *reinterpret_cast<uint4*>(sA + core_off(t, c0 + 16 * q, kH)) = *reinterpret_cast<uint4*>(&h[q][0]);
+            *reinterpret_cast<uint4*>(sA + core_off(t, c0 + 16 * q + 8, kH)) = *reinterpret_cast<uint4*>(&h[q][4]);
+          }
         } else {
 #pragma unroll
-          for (int j = 0; j < 16; ++j) y += h[j] * sw4[c + j];
+          for (int q = 0; q < 2; ++q)
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+              const float2 f = __bfloat1622float2(h[q][j]);
+              y += f.x * sw4[c0 + 16 * q + 2 * j] + f.y * sw4[c0 + 16 * q + 2 * j + 1];
+            }
         }
       }
       if (l < 2) fence_async_smem();
