@@ -138,6 +138,19 @@ int tmc_spatial_operators(tmc_handle* h, const double* gd, const double* iap_u, 
  * block_sizes (may be NULL) receives {cell, vertex, edge_pv, edge_flux, final}. */
 int tmc_autotune(tmc_handle* h, int32_t steps, int32_t block_sizes[5]);
 
+/* History diagnostics on the device (history_mod.F90:124-174 with
+ * mpas_reconstruct, tmcore_swm_mod.F90:78-86): for state(old) of the selected
+ * member, u on edges, the zonal and meridional wind on cells
+ * (mpas_reconstruct_1d, mpas_vector_reconstruction.F90:207-261), h = (gd +
+ * ghs)/g, div = div_operator(u) on cells, pv and vorticity on vertices.  Any
+ * output pointer may be NULL.  The wind needs lonCell, latCell and
+ * x/y/zEdge in tmc_mesh_desc.  tmc_reconstruct applies mpas_reconstruct_1d
+ * to a given edge field (uX, uY, uZ: Cartesian components). */
+int tmc_history_fields(tmc_handle* h, double* u, double* zonal, double* meridional, double* h_cell, double* div,
+                       double* pv, double* vor);
+int tmc_reconstruct(tmc_handle* h, const double* u, double* uX, double* uY, double* uZ, double* zonal,
+                    double* meridional);
+
 /* Ensembles (tmc_params.members > 1): every member is an independent model on
  * the same mesh, with its own state, topography, beta and invariants; the
  * members' arrays lie one after another and each kernel launch covers all of

@@ -97,6 +97,7 @@ def lib() -> ctypes.CDLL:
         L.orc_adv_set_initial.argtypes = [vp, vp, ip]
         L.orc_adv_step.argtypes = [vp, ip]
         L.orc_adv_get.argtypes = [vp, vp, vp]
+        L.orc_reconstruct.argtypes = [vp, vp, vp, vp, vp, vp, vp]
         L.orc_adv_elapsed.restype = ctypes.c_double
         L.orc_adv_elapsed.argtypes = [vp]
     return _lib
@@ -220,6 +221,12 @@ class Oracle:
         return q
 
     # adv
+    def reconstruct(self, u):
+        """(uX, uY, uZ, zonal, meridional) on cells from u on edges (mpas_reconstruct_1d)."""
+        out = [np.empty(self.nc) for _ in range(5)]
+        self.L.orc_reconstruct(self.h, _p(np.ascontiguousarray(u, np.float64)), *[_p(a) for a in out])
+        return tuple(out)
+
     def adv_set_initial(self, q, wind_case: int):
         self.L.orc_adv_set_initial(self.h, _p(np.ascontiguousarray(q, np.float64)), int(wind_case))
 

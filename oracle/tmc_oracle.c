@@ -42,6 +42,8 @@ struct orc_model {
   int32_t *nSignEdge, *tSignEdge;
   /* geometry (radius-scaled after derive) */
   double *xCell, *yCell, *zCell, *latCell, *lonCell, *xVertex, *yVertex, *zVertex, *latVertex, *lonVertex;
+  double *xEdge, *yEdge, *zEdge;
+  double* coeffs_reconstruct; /* (3, maxEdges, nCells), built on first use */
   double *dvEdge, *dcEdge, *areaCell, *areaTriangle, *areaEdge, *kiteAreasOnVertex, *weightsOnEdge;
   double *fCell, *fVertex;
   double totalArea;
@@ -249,6 +251,11 @@ static void mesh_derive(orc_model* m) {
     m->xVertex[v] *= radius;
     m->yVertex[v] *= radius;
     m->zVertex[v] *= radius;
+  }
+  for (int e = 0; e < m->ne; ++e) {
+    m->xEdge[e] *= radius;
+    m->yEdge[e] *= radius;
+    m->zEdge[e] *= radius;
   }
   for (int e = 0; e < m->ne; ++e) {
     m->dvEdge[e] *= radius;
@@ -1063,6 +1070,174 @@ static void adv_update(orc_model* m, double dt, const orc_tend* t, const orc_sta
   adv_update_wind(m, m->elapsed + dt, n);
 }
 
+/* ================= vector reconstruction (history diagnostics) ================= */
+
+/* mpas_vector_operations.F90:93-99 */
+static void unit_vec_in_r3(double x[3]) {
+  double mag = sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
+  for (int i = 0; i < 3; ++i) x[i] = x[i] / mag;
+}
+
+/* mpas_rbf_interpolation.F90:1366-1373: inverse multiquadric */
+static double evaluate_rbf(double r2) { return 1.0 / sqrt(1.0 + r2); }
+
+/* mpas_rbf_interpolation.F90:1779-1843 elgs: Gaussian elimination with scaled
+ * partial pivoting (Pang 1997); a is (n, n) column-major 0-based */
+#define AM(i, j) a[(size_t)(j) * n + (i)]
+static void elgs(double* a, int n, int* indx) {
+  double c[16];
+  int k = 0;
+  for (int i = 0; i < n; ++i) indx[i] = i;
+  for (int i = 0; i < n; ++i) {
+    double c1 = 0.0;
+    for (int j = 0; j < n; ++j) c1 = fmax(c1, fabs(AM(i, j)));
+    c[i] = c1;
+  }
+  for (int j = 0; j < n - 1; ++j) {
+    double pi1 = 0.0;
+    for (int i = j; i < n; ++i) {
+      double pi = fabs(AM(indx[i], j)) / c[indx[i]];
+      if (pi > pi1) {
+        pi1 = pi;
+        k = i;
+      }
+    }
+    int itmp = indx[j];
+    indx[j] = indx[k];
+    indx[k] = itmp;
+    for (int i = j + 1; i < n; ++i) {
+      double pj = AM(indx[i], j) / AM(indx[j], j);
+      AM(indx[i], j) = pj;
+      for (int kk = j + 1; kk < n; ++kk) AM(indx[i], kk) = AM(indx[i], kk) - pj * AM(indx[j], kk);
+    }
+  }
+}
+
+/* :1667-1695 mpas_legs */
+static void legs(double* a, int n, double* b, double* x, int* indx) {
+  elgs(a, n, indx);
+  for (int i = 0; i < n - 1; ++i)
+    for (int j = i + 1; j < n; ++j) b[indx[j]] = b[indx[j]] - AM(indx[j], i) * b[indx[i]];
+  x[n - 1] = b[indx[n - 1]] / AM(indx[n - 1], n - 1);
+  for (int i = n - 2; i >= 0; --i) {
+    x[i] = b[indx[i]];
+    for (int j = i + 1; j < n; ++j) x[i] = x[i] - AM(indx[i], j) * x[j];
+    x[i] = x[i] / AM(indx[i], i);
+  }
+}
+#undef AM
+
+/* mpas_vector_operations.F90:493-560 (edge normals and the cell tangent
+ * planes) and mpas_vector_reconstruction.F90:52-127 with
+ * mpas_rbf_interpolation.F90:1076-1142, :1524-1556 (the coefficients) */
+static void reconstruct_init(orc_model* m) {
+  const int nc = m->nc, ne = m->ne, me = m->me;
+  double* en = dalloc((size_t)3 * ne);
+  for (int e = 1; e <= ne; ++e) {
+    int c1 = COE(1, e) - 1, c2 = COE(2, e) - 1;
+    double* v = en + (size_t)3 * (e - 1);
+    v[0] = m->xCell[c2] - m->xCell[c1];
+    v[1] = m->yCell[c2] - m->yCell[c1];
+    v[2] = m->zCell[c2] - m->zCell[c1];
+    unit_vec_in_r3(v);
+  }
+  m->coeffs_reconstruct = dalloc((size_t)3 * me * nc);
+  for (int iCell = 1; iCell <= nc; ++iCell) {
+    const int c = iCell - 1, n = A1(m->nEdgesOnCell, iCell), N = n + 2;
+    double cc[3] = {m->xCell[c], m->yCell[c], m->zCell[c]};
+    double loc[16][3], nrm[16][3];
+    for (int i = 1; i <= n; ++i) {
+      int e = EOC(i, iCell) - 1;
+      loc[i - 1][0] = m->xEdge[e];
+      loc[i - 1][1] = m->yEdge[e];
+      loc[i - 1][2] = m->zEdge[e];
+      for (int d = 0; d < 3; ++d) nrm[i - 1][d] = en[(size_t)3 * e + d];
+    }
+    double alpha = 0.0;
+    for (int i = 0; i < n; ++i) {
+      double d0 = cc[0] - loc[i][0], d1 = cc[1] - loc[i][1], d2 = cc[2] - loc[i][2];
+      alpha = alpha + sqrt(d0 * d0 + d1 * d1 + d2 * d2);
+    }
+    alpha = alpha / n;
+    /* tangent plane: rHat, xHat toward the first edge's normal, yHat = rHat x xHat */
+    double rh[3] = {cc[0], cc[1], cc[2]};
+    unit_vec_in_r3(rh);
+    const double* n1 = en + (size_t)3 * (EOC(1, iCell) - 1);
+    double ndr = n1[0] * rh[0] + n1[1] * rh[1] + n1[2] * rh[2];
+    double xh[3] = {n1[0] - ndr * rh[0], n1[1] - ndr * rh[1], n1[2] - ndr * rh[2]};
+    unit_vec_in_r3(xh);
+    double yh[3] = {rh[1] * xh[2] - rh[2] * xh[1], rh[2] * xh[0] - rh[0] * xh[2], rh[0] * xh[1] - rh[1] * xh[0]};
+    unit_vec_in_r3(yh);
+    const double* pb[2] = {xh, yh};
+    double ps[16][2], pu[16][2], pd[2];
+    for (int i = 0; i < n; ++i)
+      for (int k = 0; k < 2; ++k) {
+        ps[i][k] = loc[i][0] * pb[k][0] + loc[i][1] * pb[k][1] + loc[i][2] * pb[k][2];
+        pu[i][k] = nrm[i][0] * pb[k][0] + nrm[i][1] * pb[k][1] + nrm[i][2] * pb[k][2];
+      }
+    for (int k = 0; k < 2; ++k) pd[k] = cc[0] * pb[k][0] + cc[1] * pb[k][1] + cc[2] * pb[k][2];
+    double mat[16 * 16], mat2[16 * 16], rhs[2][16], x[2][16];
+    int indx[16];
+    memset(mat, 0, sizeof(mat));
+    memset(rhs, 0, sizeof(rhs));
+    const double a2 = alpha * alpha;
+    for (int j = 0; j < n; ++j)
+      for (int i = j; i < n; ++i) {
+        double d0 = ps[i][0] - ps[j][0], d1 = ps[i][1] - ps[j][1];
+        double r2 = (d0 * d0 + d1 * d1) / a2;
+        double v = evaluate_rbf(r2) * (pu[i][0] * pu[j][0] + pu[i][1] * pu[j][1]);
+        mat[(size_t)j * N + i] = v;
+        mat[(size_t)i * N + j] = v;
+      }
+    for (int j = 0; j < n; ++j) {
+      double d0 = pd[0] - ps[j][0], d1 = pd[1] - ps[j][1];
+      double rbf = evaluate_rbf((d0 * d0 + d1 * d1) / a2);
+      rhs[0][j] = rbf * pu[j][0];
+      rhs[1][j] = rbf * pu[j][1];
+    }
+    for (int i = 0; i < n; ++i)
+      for (int k = 0; k < 2; ++k) {
+        mat[(size_t)(n + k) * N + i] = pu[i][k];
+        mat[(size_t)i * N + (n + k)] = pu[i][k];
+      }
+    rhs[0][n] = 1.0;
+    rhs[1][n + 1] = 1.0;
+    memcpy(mat2, mat, sizeof(double) * N * N);
+    legs(mat, N, rhs[0], x[0], indx);
+    legs(mat2, N, rhs[1], x[1], indx);
+    for (int i = 0; i < n; ++i)
+      for (int d = 0; d < 3; ++d)
+        m->coeffs_reconstruct[((size_t)c * me + i) * 3 + d] = pb[0][d] * x[0][i] + pb[1][d] * x[1][i];
+  }
+  free(en);
+}
+
+/* mpas_vector_reconstruction.F90:207-261 mpas_reconstruct_1d */
+void orc_reconstruct(orc_model* m, const double* u, double* uX, double* uY, double* uZ, double* uzon,
+                     double* umer) {
+  if (!m->coeffs_reconstruct) reconstruct_init(m);
+  for (int iCell = 1; iCell <= m->nc; ++iCell) {
+    const int c = iCell - 1;
+    double x = 0.0, y = 0.0, z = 0.0;
+    for (int i = 1; i <= A1(m->nEdgesOnCell, iCell); ++i) {
+      const double ue = A1(u, EOC(i, iCell));
+      const double* k = m->coeffs_reconstruct + ((size_t)c * m->me + (i - 1)) * 3;
+      x = x + k[0] * ue;
+      y = y + k[1] * ue;
+      z = z + k[2] * ue;
+    }
+    uX[c] = x;
+    uY[c] = y;
+    uZ[c] = z;
+  }
+  for (int c = 0; c < m->nc; ++c) {
+    double clat = cos(m->latCell[c]), slat = sin(m->latCell[c]);
+    double clon = cos(m->lonCell[c]), slon = sin(m->lonCell[c]);
+    uzon[c] = -uX[c] * slon + uY[c] * clon;
+    umer[c] = -(uX[c] * clon + uY[c] * slon) * slat + uZ[c] * clat;
+  }
+}
+
 /* ======================= lifetime and public API ======================= */
 
 static void alloc_state(orc_model* m, orc_state* s) {
@@ -1130,6 +1305,9 @@ orc_model* orc_create(const orc_mesh_in* in, const orc_params* p) {
   m->latCell = dup(in->latCell, nc * 8);
   m->lonCell = dup(in->lonCell, nc * 8);
   m->xVertex = dup(in->xVertex, nv * 8);
+  m->xEdge = dup(in->xEdge, ne * 8);
+  m->yEdge = dup(in->yEdge, ne * 8);
+  m->zEdge = dup(in->zEdge, ne * 8);
   m->yVertex = dup(in->yVertex, nv * 8);
   m->zVertex = dup(in->zVertex, nv * 8);
   m->latVertex = dup(in->latVertex, nv * 8);
@@ -1201,7 +1379,7 @@ void orc_destroy(orc_model* m) {
                   m->verticesOnCell, m->cellsOnEdge, m->verticesOnEdge, m->edgesOnEdge, m->cellsOnVertex,
                   m->edgesOnVertex, m->verticesOnVertex, m->nSignEdge, m->tSignEdge, m->xCell, m->yCell,
                   m->zCell, m->latCell, m->lonCell, m->xVertex, m->yVertex, m->zVertex, m->latVertex,
-                  m->lonVertex, m->dvEdge, m->dcEdge, m->areaCell, m->areaTriangle, m->areaEdge,
+                  m->lonVertex, m->xEdge, m->yEdge, m->zEdge, m->coeffs_reconstruct, m->dvEdge, m->dcEdge, m->areaCell, m->areaTriangle, m->areaEdge,
                   m->kiteAreasOnVertex, m->weightsOnEdge, m->fCell, m->fVertex, m->nFit2Cells, m->nFit3Cells,
                   m->nFit4Cells, m->nFit2Vertices, m->nFit3Vertices, m->nFit4Vertices, m->fit2Cells,
                   m->fit3Cells, m->fit4Cells, m->fit2Vertices, m->fit3Vertices, m->fit4Vertices,

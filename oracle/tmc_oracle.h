@@ -123,6 +123,11 @@ void orc_adv_step(orc_model* m, int nsteps);
 void orc_adv_get(const orc_model* m, double* q, double* u);
 double orc_adv_elapsed(const orc_model* m);
 
+/* cell-centre wind from edge normal velocity (mpas_reconstruct_1d):
+ * Cartesian components and the zonal / meridional winds */
+void orc_reconstruct(orc_model* m, const double* u, double* uX, double* uY, double* uZ, double* uzon,
+                     double* umer);
+
 #ifdef __cplusplus
 }
 #endif

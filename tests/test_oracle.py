@@ -211,3 +211,21 @@ def test_poly_fit_tables_shape():
     # second-derivative weights of a centre-relative stencil sum to a finite number
     d2 = o.poly_table("deriv2OnCell").reshape(m.nEdges, 2, 31)
     assert np.all(np.isfinite(d2))
+
+
+def test_reconstruct_solid_body_rotation():
+    """mpas_reconstruct_1d of a zonal solid-body rotation gives u0 cos(lat)
+    zonally and nothing meridionally (to the RBF reconstruction's accuracy)."""
+    from tmcore_gb300 import cases
+
+    m = icos(4)
+    r, u0 = 6371220.0, 30.0
+    u = cases._uv_from_psi(m, -r * u0 * np.sin(m.latVertex), r)
+    o = make(m)
+    uX, uY, uZ, zon, mer = o.reconstruct(u)
+    ref = u0 * np.cos(m.latCell)
+    assert np.max(np.abs(zon - ref)) < 2e-2 * u0
+    assert np.max(np.abs(mer)) < 2e-2 * u0
+    # the Cartesian wind is tangent to the sphere
+    radial = uX * m.xCell + uY * m.yCell + uZ * m.zCell
+    assert np.max(np.abs(radial)) < 1e-6 * u0

@@ -77,6 +77,8 @@ SYMBOLS = {
     "tmc_time_steps": (ctypes.c_int, [vp, i32, dp, dp, ctypes.POINTER(i32), ctypes.POINTER(i32)]),
     "tmc_sizes": (ctypes.c_int, [vp, i64p, i64p, i64p, i64p]),
     "tmc_select_member": (ctypes.c_int, [vp, i32]),
+    "tmc_history_fields": (ctypes.c_int, [vp, vp, vp, vp, vp, vp, vp, vp]),
+    "tmc_reconstruct": (ctypes.c_int, [vp, vp, vp, vp, vp, vp, vp]),
     "tmc_autotune": (ctypes.c_int, [vp, i32, ctypes.POINTER(i32)]),
     "tmc_group_create": (ctypes.c_int, [ctypes.POINTER(vp), i32, ctypes.c_double, ctypes.POINTER(vp)]),
     "tmc_group_run": (ctypes.c_int, [vp, i32]),

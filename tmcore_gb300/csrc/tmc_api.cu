@@ -49,6 +49,10 @@ struct EngineBase {
   virtual void state_slot0(void** gd, void** iap, void** q, void** ghs) = 0;  // all members
   virtual void refresh_all_shadows() = 0;
   virtual void closure_features(float* feat, float* pv) = 0;
+  // history fields of the selected member into device arrays (null: skip):
+  // u [ne], zonal, meridional, h, div [nc], pv, vor [nv]
+  virtual void history_dev(double* u, double* zon, double* mer, double* hc, double* div, double* pv, double* vor,
+                           double* scratch_e) = 0;
 };
 
 enum Field { F_GD = 0, F_IAP, F_U, F_PV_V, F_VOR, F_TEND_GD, F_TEND_IAP, F_GD_STAGE };
@@ -100,6 +104,8 @@ struct tmc_handle {
   int* d_member_on = nullptr;
   int* d_closure_err = nullptr;
   int sms = 148;
+  double* d_hist = nullptr;    // history outputs on cells (5 x nCells)
+  double* d_hist_e = nullptr;  // history outputs on edges and vertices
   int timed_pass = 3;  // the pass tmc_time_steps brackets with events
 
   template <class X>
@@ -380,6 +386,21 @@ struct Engine : EngineBase {
       if (h->O.pv_scheme == 2) launch_cons_apvm<T>(h->M, h->O, s, h->P, h->d_diag, h->bsp[P_VERTEX], h->st);
       launch_closure_features(h->M, s, h->cur, feat, pv, h->st);
     }
+  }
+
+  void history_dev(double* uo, double* zon, double* mer, double* hc, double* div, double* pv, double* vor,
+                   double* scratch_e) override {
+    launch_diag_pass(false);  // gd_edge, u, pv and vorticity of state(old)
+    const T* ue = u[0] + oe();
+    if (uo) launch_to_f64<T>((size_t)h->M.ne, ue, uo, h->st);
+    if (zon || mer) launch_reconstruct<T>(h->M, ue, nullptr, nullptr, nullptr, zon, mer, h->st);
+    if (hc) launch_h_field(h->M.nc, gd[0] + oc(), ghs + oc(), h->p.g, hc, h->st);
+    if (div) {
+      launch_to_f64<T>((size_t)h->M.ne, ue, scratch_e, h->st);
+      launch_op(OP_DIV, h->M, h->O, scratch_e, nullptr, nullptr, div, 0, 0, 0.0, 0.0, h->bs, h->st);
+    }
+    if (pv) launch_to_f64<T>((size_t)h->M.nv, pv_v + ov(), pv, h->st);
+    if (vor) launch_to_f64<T>((size_t)h->M.nv, this->vor + ov(), vor, h->st);
   }
 
   // ---- generic integrator program (time_scheme_mod.F90:65-107 CRK3,
@@ -818,6 +839,10 @@ int tmc_create(const tmc_mesh_desc* mesh, const tmc_params* params, tmc_handle**
   M.v2c_start = h->upload(hm.v2c_start);
   M.v2c_vertex = h->upload(hm.v2c_vertex);
   M.v2c_kite = h->upload(hm.v2c_kite);
+  if (!hm.recon.empty()) {
+    M.recon = h->upload(hm.recon);
+    M.cell_trig = h->upload(hm.cell_trig);
+  }
   if (h->adv) {
     h->d_latV = h->upload(hm.latVertex);
     h->d_lonV = h->upload(hm.lonVertex);
@@ -1347,6 +1372,64 @@ int tmc_closure_features(tmc_handle* h, float* features, double* pv_edge) {
     if (pv_edge) pv_edge[o] = pv[i];
   }
   return h->cuda_check("tmc_closure_features");
+}
+
+int tmc_reconstruct(tmc_handle* h, const double* u, double* uX, double* uY, double* uZ, double* zonal,
+                    double* meridional) {
+  TMC_REQUIRE_HANDLE(h);
+  if (!u) return h->fail(TMC_E_ARG, "NULL array");
+  if (!h->M.recon) return h->fail(TMC_E_STATE, "tmc_reconstruct needs lonCell, latCell and x/y/zEdge in the mesh");
+  const int nc = h->M.nc;
+  if (!h->d_hist && !(h->d_hist = h->dalloc<double>((size_t)5 * nc))) return h->cuda_check("tmc_reconstruct");
+  int rc;
+  if ((rc = h2d(h, h->raw_e, u, h->M.ne))) return rc;
+  launch_gather<double>(h->M.ne, h->raw_e, h->d_edge_n2o, h->op_b, h->st);
+  double* d[5] = {h->d_hist, h->d_hist + nc, h->d_hist + 2 * (size_t)nc, h->d_hist + 3 * (size_t)nc,
+                  h->d_hist + 4 * (size_t)nc};
+  launch_reconstruct<double>(h->M, h->op_b, d[0], d[1], d[2], d[3], d[4], h->st);
+  double* outs[5] = {uX, uY, uZ, zonal, meridional};
+  for (int k = 0; k < 5; ++k) {
+    if (!outs[k]) continue;
+    launch_scatter<double>(nc, d[k], h->d_cell_n2o, h->raw_c, h->st);
+    if ((rc = d2h(h, outs[k], h->raw_c, nc))) return rc;
+    if ((rc = sync(h, "tmc_reconstruct"))) return rc;
+  }
+  return h->cuda_check("tmc_reconstruct");
+}
+
+int tmc_history_fields(tmc_handle* h, double* u, double* zonal, double* meridional, double* h_cell, double* div,
+                       double* pv, double* vor) {
+  TMC_REQUIRE_SWM(h);
+  if (!h->have_state) return h->fail(TMC_E_STATE, "no state set");
+  if ((zonal || meridional) && !h->M.recon)
+    return h->fail(TMC_E_STATE, "the zonal/meridional wind needs lonCell, latCell and x/y/zEdge in the mesh");
+  const int nc = h->M.nc, ne = h->M.ne, nv = h->M.nv;
+  if (!h->d_hist && !(h->d_hist = h->dalloc<double>((size_t)5 * nc))) return h->cuda_check("tmc_history_fields");
+  if (!h->d_hist_e && !(h->d_hist_e = h->dalloc<double>((size_t)2 * ne + 2 * (size_t)nv)))
+    return h->cuda_check("tmc_history_fields");
+  double *c0 = h->d_hist, *c1 = c0 + nc, *c2 = c1 + nc, *c3 = c2 + nc;
+  double *e0 = h->d_hist_e, *e1 = e0 + ne, *v0 = e1 + ne, *v1 = v0 + nv;
+  h->eng->history_dev(u ? e0 : nullptr, zonal ? c0 : nullptr, meridional ? c1 : nullptr, h_cell ? c2 : nullptr,
+                      div ? c3 : nullptr, pv ? v0 : nullptr, vor ? v1 : nullptr, e1);
+  h->prep_valid = false;
+  struct Out {
+    double* host;
+    double* dev;
+    int n;
+    const int32_t* n2o;
+    double* raw;
+  } outs[7] = {{u, e0, ne, h->d_edge_n2o, h->raw_e},       {zonal, c0, nc, h->d_cell_n2o, h->raw_c},
+               {meridional, c1, nc, h->d_cell_n2o, h->raw_c}, {h_cell, c2, nc, h->d_cell_n2o, h->raw_c},
+               {div, c3, nc, h->d_cell_n2o, h->raw_c},       {pv, v0, nv, h->d_vert_n2o, h->raw_v},
+               {vor, v1, nv, h->d_vert_n2o, h->raw_v}};
+  int rc;
+  for (auto& o : outs) {
+    if (!o.host) continue;
+    launch_scatter<double>(o.n, o.dev, o.n2o, o.raw, h->st);
+    if ((rc = d2h(h, o.host, o.raw, o.n))) return rc;
+    if ((rc = sync(h, "tmc_history_fields"))) return rc;
+  }
+  return h->cuda_check("tmc_history_fields");
 }
 
 int tmc_adv_set_initial(tmc_handle* h, const double* q) {

@@ -79,6 +79,9 @@ struct DevMesh {
   const float* invAreaCell_f;
   const float* areaCell_f;
   const double* invAreaCell;
+  // vector reconstruction (history): coefficients [3][me][nc], cos/sin lat, lon [4][nc]
+  const double* recon;
+  const double* cell_trig;
 };
 
 struct ModelOpt {
@@ -366,6 +369,16 @@ void launch_closure(const DevMesh& M, const StageIO<float>& S, const ClosureArgs
 // the features (and pv_edge) of every edge of member m, into feat[ne][24] / pv[ne]
 void launch_closure_features(const DevMesh& M, const StageIO<float>& S, int member, float* feat, float* pv,
                              cudaStream_t st);
+
+// History diagnostics (history_mod.F90:124-174): the cell-centre wind of
+// mpas_reconstruct_1d (mpas_vector_reconstruction.F90:207-261), h = (gd + ghs)/g,
+// and a copy of an edge field in FP64.  Outputs may be null.
+template <class T>
+void launch_reconstruct(const DevMesh& M, const T* u, double* uX, double* uY, double* uZ, double* zonal,
+                        double* meridional, cudaStream_t st);
+void launch_h_field(int nc, const double* gd, const double* ghs, double g, double* h, cudaStream_t st);
+template <class T>
+void launch_to_f64(size_t n, const T* src, double* dst, cudaStream_t st);
 
 // single operators for parity (FP64 only)
 void launch_op(int op, const DevMesh& M, const ModelOpt& O, const double* a, const double* b, const double* c,

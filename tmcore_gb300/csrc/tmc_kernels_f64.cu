@@ -237,6 +237,16 @@ int launch_mass_only(const DevMesh& M, const double* gd, Partials P, int bs, cud
   return g;
 }
 
+// h = (gd + ghs) / g (history_mod.F90:166)
+__global__ void k_h_field(int nc, const double* gd, const double* ghs, double g, double* h) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < nc) h[c] = (gd[c] + ghs[c]) / g;
+}
+
+void launch_h_field(int nc, const double* gd, const double* ghs, double g, double* h, cudaStream_t st) {
+  k_h_field<<<nblk(nc, 256), 256, 0, st>>>(nc, gd, ghs, g, h);
+}
+
 __global__ void k_shadows(int nc, int ntr, const double* gd, const float* q, float* gdf, float* qr) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nc) return;

@@ -1335,6 +1335,43 @@ void launch_iap_from_u(int ne, const double* gd_e, const double* u, T* iap, cuda
   k_iap_from_u<T><<<nblk(ne, 256), 256, 0, st>>>(ne, gd_e, u, iap);
 }
 
+// mpas_reconstruct_1d (mpas_vector_reconstruction.F90:207-261), reference order
+template <class T>
+__global__ void k_reconstruct(DevMesh M, const T* u, double* uX, double* uY, double* uZ, double* zon, double* mer) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= M.nc) return;
+  double x = 0.0, y = 0.0, z = 0.0;
+  for (int i = 0; i < M.nEdgesOnCell[c]; ++i) {
+    const double ue = (double)u[M.edgesOnCell[(size_t)i * M.nc + c]];
+    x = x + M.recon[((size_t)0 * M.me + i) * M.nc + c] * ue;
+    y = y + M.recon[((size_t)1 * M.me + i) * M.nc + c] * ue;
+    z = z + M.recon[((size_t)2 * M.me + i) * M.nc + c] * ue;
+  }
+  if (uX) uX[c] = x;
+  if (uY) uY[c] = y;
+  if (uZ) uZ[c] = z;
+  const double clat = M.cell_trig[c], slat = M.cell_trig[(size_t)M.nc + c];
+  const double clon = M.cell_trig[(size_t)2 * M.nc + c], slon = M.cell_trig[(size_t)3 * M.nc + c];
+  if (zon) zon[c] = -x * slon + y * clon;
+  if (mer) mer[c] = -(x * clon + y * slon) * slat + z * clat;
+}
+
+template <class T>
+__global__ void k_to_f64(size_t n, const T* src, double* dst) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = (double)src[i];
+}
+
+template <class T>
+void launch_reconstruct(const DevMesh& M, const T* u, double* uX, double* uY, double* uZ, double* zonal,
+                        double* meridional, cudaStream_t st) {
+  k_reconstruct<T><<<nblk(M.nc, 256), 256, 0, st>>>(M, u, uX, uY, uZ, zonal, meridional);
+}
+template <class T>
+void launch_to_f64(size_t n, const T* src, double* dst, cudaStream_t st) {
+  k_to_f64<T><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, src, dst);
+}
+
 #define TMC_INSTANTIATE(T)                                                                                        \
   template void launch_gather<T>(int, const double*, const int32_t*, T*, cudaStream_t);                          \
   template void launch_scatter<T>(int, const T*, const int32_t*, double*, cudaStream_t);                         \
@@ -1353,6 +1390,9 @@ void launch_iap_from_u(int ne, const double* gd_e, const double* u, T* iap, cuda
   template void launch_cons_apvm<T>(const DevMesh&, const ModelOpt&, const StageIO<T>&, Partials, double*, int,   \
                                     cudaStream_t);                                                                \
   template void launch_update<T>(const DevMesh&, int, const UpdateArgs<T>&, int, cudaStream_t);                 \
+  template void launch_reconstruct<T>(const DevMesh&, const T*, double*, double*, double*, double*, double*,   \
+                                      cudaStream_t);                                                            \
+  template void launch_to_f64<T>(size_t, const T*, double*, cudaStream_t);                                       \
   template void launch_combine<T>(const DevMesh&, int, int, const CombineArgs<T>&, Partials, int, cudaStream_t);
 
 }  // namespace tmc

@@ -422,6 +422,145 @@ void compact(const std::vector<int32_t>& nfit, const std::vector<int32_t>& fit, 
   }
 }
 
+// Vector reconstruction coefficients of one cell (mpas_vector_reconstruction.F90:52-127;
+// mpas_rbf_interpolation.F90:1076-1142, :1524-1556 with the inverse multiquadric
+// :1366-1373 and scaled partial pivoting :1667-1695, :1779-1843, the method of
+// Pang 1997), in the reference's operation order; positions radius-scaled.
+void unit3(double v[3]) {
+  const double mag = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+  for (int i = 0; i < 3; ++i) v[i] = v[i] / mag;
+}
+double rbf_imq(double r2) { return 1.0 / std::sqrt(1.0 + r2); }
+
+// Gaussian elimination with scaled partial pivoting and the solve: column-major n x n
+void pivot_solve(double* a, int n, double* b, double* x) {
+  int idx[16];
+  double sc[16];
+  int k = 0;
+  auto A = [&](int i, int j) -> double& { return a[(size_t)j * n + i]; };
+  for (int i = 0; i < n; ++i) idx[i] = i;
+  for (int i = 0; i < n; ++i) {
+    double c1 = 0.0;
+    for (int j = 0; j < n; ++j) c1 = std::fmax(c1, std::fabs(A(i, j)));
+    sc[i] = c1;
+  }
+  for (int j = 0; j < n - 1; ++j) {
+    double best = 0.0;
+    for (int i = j; i < n; ++i) {
+      const double r = std::fabs(A(idx[i], j)) / sc[idx[i]];
+      if (r > best) {
+        best = r;
+        k = i;
+      }
+    }
+    std::swap(idx[j], idx[k]);
+    for (int i = j + 1; i < n; ++i) {
+      const double f = A(idx[i], j) / A(idx[j], j);
+      A(idx[i], j) = f;
+      for (int kk = j + 1; kk < n; ++kk) A(idx[i], kk) = A(idx[i], kk) - f * A(idx[j], kk);
+    }
+  }
+  for (int i = 0; i < n - 1; ++i)
+    for (int j = i + 1; j < n; ++j) b[idx[j]] = b[idx[j]] - A(idx[j], i) * b[idx[i]];
+  x[n - 1] = b[idx[n - 1]] / A(idx[n - 1], n - 1);
+  for (int i = n - 2; i >= 0; --i) {
+    double v = b[idx[i]];
+    for (int j = i + 1; j < n; ++j) v = v - A(idx[i], j) * x[j];
+    x[i] = v / A(idx[i], i);
+  }
+}
+
+// coefficients[slot][xyz] of cell c (original numbering, 0-based)
+void reconstruct_cell(const tmc_mesh_desc& d, double radius, int c, const std::vector<double>& en, double out[][3]) {
+  const int n = d.nEdgesOnCell[c], N = n + 2;
+  const double cc[3] = {d.xCell[c] * radius, d.yCell[c] * radius, d.zCell[c] * radius};
+  double loc[16][3], nrm[16][3];
+  for (int i = 0; i < n; ++i) {
+    const int e = d.edgesOnCell[(size_t)c * d.maxEdges + i] - 1;
+    loc[i][0] = d.xEdge[e] * radius;
+    loc[i][1] = d.yEdge[e] * radius;
+    loc[i][2] = d.zEdge[e] * radius;
+    for (int k = 0; k < 3; ++k) nrm[i][k] = en[(size_t)3 * e + k];
+  }
+  double alpha = 0.0;
+  for (int i = 0; i < n; ++i) {
+    const double d0 = cc[0] - loc[i][0], d1 = cc[1] - loc[i][1], d2 = cc[2] - loc[i][2];
+    alpha = alpha + std::sqrt(d0 * d0 + d1 * d1 + d2 * d2);
+  }
+  alpha = alpha / n;
+  double rh[3] = {cc[0], cc[1], cc[2]};
+  unit3(rh);
+  const double* n1 = &en[(size_t)3 * (d.edgesOnCell[(size_t)c * d.maxEdges] - 1)];
+  const double ndr = n1[0] * rh[0] + n1[1] * rh[1] + n1[2] * rh[2];
+  double xh[3] = {n1[0] - ndr * rh[0], n1[1] - ndr * rh[1], n1[2] - ndr * rh[2]};
+  unit3(xh);
+  double yh[3] = {rh[1] * xh[2] - rh[2] * xh[1], rh[2] * xh[0] - rh[0] * xh[2], rh[0] * xh[1] - rh[1] * xh[0]};
+  unit3(yh);
+  const double* pb[2] = {xh, yh};
+  double ps[16][2], pu[16][2], pd[2];
+  for (int i = 0; i < n; ++i)
+    for (int k = 0; k < 2; ++k) {
+      ps[i][k] = loc[i][0] * pb[k][0] + loc[i][1] * pb[k][1] + loc[i][2] * pb[k][2];
+      pu[i][k] = nrm[i][0] * pb[k][0] + nrm[i][1] * pb[k][1] + nrm[i][2] * pb[k][2];
+    }
+  for (int k = 0; k < 2; ++k) pd[k] = cc[0] * pb[k][0] + cc[1] * pb[k][1] + cc[2] * pb[k][2];
+  double m1[16 * 16] = {}, m2[16 * 16], rhs[2][16] = {}, x[2][16];
+  const double a2 = alpha * alpha;
+  for (int j = 0; j < n; ++j)
+    for (int i = j; i < n; ++i) {
+      const double d0 = ps[i][0] - ps[j][0], d1 = ps[i][1] - ps[j][1];
+      const double v = rbf_imq((d0 * d0 + d1 * d1) / a2) * (pu[i][0] * pu[j][0] + pu[i][1] * pu[j][1]);
+      m1[(size_t)j * N + i] = v;
+      m1[(size_t)i * N + j] = v;
+    }
+  for (int j = 0; j < n; ++j) {
+    const double d0 = pd[0] - ps[j][0], d1 = pd[1] - ps[j][1];
+    const double r = rbf_imq((d0 * d0 + d1 * d1) / a2);
+    rhs[0][j] = r * pu[j][0];
+    rhs[1][j] = r * pu[j][1];
+  }
+  for (int i = 0; i < n; ++i)
+    for (int k = 0; k < 2; ++k) {
+      m1[(size_t)(n + k) * N + i] = pu[i][k];
+      m1[(size_t)i * N + (n + k)] = pu[i][k];
+    }
+  rhs[0][n] = 1.0;
+  rhs[1][n + 1] = 1.0;
+  std::memcpy(m2, m1, sizeof(double) * N * N);
+  pivot_solve(m1, N, rhs[0], x[0]);
+  pivot_solve(m2, N, rhs[1], x[1]);
+  for (int i = 0; i < n; ++i)
+    for (int k = 0; k < 3; ++k) out[i][k] = pb[0][k] * x[0][i] + pb[1][k] * x[1][i];
+}
+
+void build_reconstruct(const tmc_mesh_desc& d, double radius, HostMesh& hm) {
+  const int nc = d.nCells, ne = d.nEdges, me = hm.me;
+  // edge normals, cell 1 -> cell 2 (mpas_vector_operations.F90:515-540)
+  std::vector<double> en((size_t)3 * ne);
+  for (int e = 0; e < ne; ++e) {
+    const int c1 = d.cellsOnEdge[(size_t)e * 2] - 1, c2 = d.cellsOnEdge[(size_t)e * 2 + 1] - 1;
+    double* v = &en[(size_t)3 * e];
+    v[0] = d.xCell[c2] * radius - d.xCell[c1] * radius;
+    v[1] = d.yCell[c2] * radius - d.yCell[c1] * radius;
+    v[2] = d.zCell[c2] * radius - d.zCell[c1] * radius;
+    unit3(v);
+  }
+  hm.recon.assign((size_t)3 * me * nc, 0.0);
+  hm.cell_trig.assign((size_t)4 * nc, 0.0);
+#pragma omp parallel for schedule(dynamic, 256)
+  for (int co = 0; co < nc; ++co) {
+    double out[16][3];
+    reconstruct_cell(d, radius, co, en, out);
+    const int cn = hm.cell_o2n[co];
+    for (int i = 0; i < d.nEdgesOnCell[co]; ++i)
+      for (int k = 0; k < 3; ++k) hm.recon[((size_t)k * me + i) * nc + cn] = out[i][k];
+    hm.cell_trig[cn] = std::cos(d.latCell[co]);
+    hm.cell_trig[(size_t)nc + cn] = std::sin(d.latCell[co]);
+    hm.cell_trig[(size_t)2 * nc + cn] = std::cos(d.lonCell[co]);
+    hm.cell_trig[(size_t)3 * nc + cn] = std::sin(d.lonCell[co]);
+  }
+}
+
 }  // namespace
 
 bool prepare_mesh(const tmc_mesh_desc& d, const tmc_params& p, const PrepOptions& opt, HostMesh& hm) {
@@ -690,6 +829,9 @@ bool prepare_mesh(const tmc_mesh_desc& d, const tmc_params& p, const PrepOptions
     compact(F.nfit2v, F.fit2v, F.d2v, ctr, vo2n, hm.edge_n2o, ne, hm.vert2);
     compact(F.nfit4v, F.fit4v, F.d4v, ctr, vo2n, hm.edge_n2o, ne, hm.vert4);
   }
+  // the cell-centre wind of the history output (needs lonCell and the edge positions)
+  if (d.lonCell && d.latCell && d.xEdge && d.yEdge && d.zEdge && d.maxEdges <= 14)
+    build_reconstruct(d, p.radius, hm);
   return true;
 }
 

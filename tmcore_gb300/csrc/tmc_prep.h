@@ -50,6 +50,10 @@ struct HostMesh {
   std::vector<double> kite;  // [vd][nv]
   std::vector<double> areaTriangle, fVertex;
   std::vector<double> latVertex, lonVertex;  // radians (lonVertex empty when not given)
+  // vector reconstruction to cell centres (mpas_init_reconstruct): coefficients
+  // [3][me][nc] (x, y, z per edge slot) and cos/sin of lat and lon [4][nc]
+  // (empty when lonCell is not given)
+  std::vector<double> recon, cell_trig;
   // v2c gather table (scalar_v2c_interp_operator, operators_mod.F90:125-141):
   // per cell, contributions in ascending ORIGINAL vertex order.
   std::vector<int32_t> v2c_start, v2c_vertex;

@@ -133,6 +133,21 @@ class TMCoreGPU:
         self._chk(self.lib.tmc_autotune(self.h, int(steps), out))
         return dict(zip(("cell", "vertex", "edge_pv", "edge_flux", "final"), list(out)))
 
+    # ------------------------------------------------------------------ history diagnostics
+    def history_fields(self):
+        """dict of the history fields of state(old): u, zonal, meridional, h, div, pv, vor."""
+        out = {"u": np.empty(self.ne), "zonal": np.empty(self.nc), "meridional": np.empty(self.nc),
+               "h": np.empty(self.nc), "div": np.empty(self.nc), "pv": np.empty(self.nv), "vor": np.empty(self.nv)}
+        self._chk(self.lib.tmc_history_fields(self.h, *[_ptr(out[k]) for k in
+                                                        ("u", "zonal", "meridional", "h", "div", "pv", "vor")]))
+        return out
+
+    def reconstruct(self, u):
+        """(uX, uY, uZ, zonal, meridional) on cells from u on edges (mpas_reconstruct_1d)."""
+        out = [np.empty(self.nc) for _ in range(5)]
+        self._chk(self.lib.tmc_reconstruct(self.h, _ptr(_f64(u)), *[_ptr(a) for a in out]))
+        return tuple(out)
+
     # ------------------------------------------------------------------ learned closure
     def set_closure(self, net):
         """Apply `net` (a ClosureMLP, or None) to pv_edge in every stage."""
