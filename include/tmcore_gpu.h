@@ -219,6 +219,26 @@ int tmc_coarsen_cell_map(const tmc_coarsen* c, int32_t* coarse_cell_of_fine);
 const char* tmc_coarsen_last_error(const tmc_coarsen* c);
 int tmc_coarsen_destroy(tmc_coarsen* c);
 
+/* MPAS grid files and history files in NetCDF classic format (CDF-1 and
+ * 64-bit-offset CDF-2), read and written without the NetCDF library.
+ * tmc_mesh_file_open reads the dimensions and arrays mesh_mod.F90:79-167
+ * reads (the other variables are skipped) and fills *desc with pointers into
+ * the file object, valid until tmc_mesh_file_close; arrays absent from the
+ * file are NULL.  tmc_mesh_file_write writes the non-NULL arrays of a
+ * tmc_mesh_desc as an MPAS grid file.  The history file holds the mesh
+ * coordinates and, per tmc_history_write, one record of the fields of
+ * history_mod.F90:124-174 (u, zonalWind, merdionalWind, h, pv, vor, div, tm,
+ * te) of the handle's selected member at the given time. */
+typedef struct tmc_mesh_file tmc_mesh_file;
+int tmc_mesh_file_open(const char* path, tmc_mesh_file** out, tmc_mesh_desc* desc);
+const char* tmc_mesh_file_error(const tmc_mesh_file* f);
+int tmc_mesh_file_close(tmc_mesh_file* f);
+int tmc_mesh_file_write(const char* path, const tmc_mesh_desc* desc);
+typedef struct tmc_history tmc_history;
+int tmc_history_create(const char* path, const tmc_mesh_desc* mesh, tmc_history** out);
+int tmc_history_write(tmc_history* hw, tmc_handle* h, double seconds);
+int tmc_history_close(tmc_history* hw);
+
 /* Groups: several handles (different meshes and dt, each possibly an
  * ensemble) advanced together, e.g. a mixed batch of mesh levels with
  * dt = 1200 / 2^(level-4) s.  One CUDA graph per cycle of cycle_seconds holds

@@ -46,3 +46,34 @@ def test_history_fields(mesh4, precision):
     assert rel_max(f["pv"], pvo) < (1e-12 if precision == 0 else 1e-4)
     assert rel_max(f["vor"], voro) < (1e-10 if precision == 0 else 1e-2)
     g.close()
+
+
+def test_history_file(mesh4, tmp_path):
+    """Two records of the history file (history_mod.F90 fields), read back with scipy."""
+    import os
+
+    from scipy.io import netcdf_file
+
+    from tmcore_gb300 import cases
+    from tmcore_gb300.gpu import HistoryWriter, TMCoreGPU
+
+    g = TMCoreGPU(mesh4, dt=600.0, pv_scheme=1, apvm_weight=0.0)
+    gd, u, ghs = cases.jet_bumps(mesh4, seed=33)
+    g.set_initial(gd, u, ghs)
+    p = os.path.join(tmp_path, "h0.nc")
+    hw = HistoryWriter(p, mesh4)
+    hw.write(g, 0.0)
+    f0 = g.history_fields()
+    g.step(6)
+    hw.write(g, 3600.0)
+    f1 = g.history_fields()
+    d1 = g.diag()
+    hw.close()
+    with netcdf_file(p, "r", mmap=False) as nc:
+        assert nc.variables["time"][:].tolist() == [0.0, 3600.0]
+        assert np.array_equal(nc.variables["u"][0], f0["u"]) and np.array_equal(nc.variables["u"][1], f1["u"])
+        assert np.array_equal(nc.variables["h"][1], f1["h"]) and np.array_equal(nc.variables["vor"][1], f1["vor"])
+        assert np.array_equal(nc.variables["zonalWind"][1], f1["zonal"])
+        assert nc.variables["tm"][1] == d1[0] and nc.variables["te"][1] == d1[1]
+        assert np.array_equal(nc.variables["xCell"][:], mesh4.xCell)
+    g.close()

@@ -63,6 +63,7 @@ GPU_SOURCES = [
     ("tmc_mlp.cu", "nvcc", []),
     ("tmc_coarsen.cu", "nvcc", []),
     ("tmc_prep.cpp", "g++", ["-ffp-contract=off"]),
+    ("tmc_netcdf.cpp", "g++", []),
 ]
 
 

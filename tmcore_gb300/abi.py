@@ -106,6 +106,13 @@ SYMBOLS = {
     "tmc_coarsen_cell_map": (ctypes.c_int, [vp, vp]),
     "tmc_coarsen_last_error": (ctypes.c_char_p, [vp]),
     "tmc_coarsen_destroy": (ctypes.c_int, [vp]),
+    "tmc_mesh_file_open": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(vp), ctypes.POINTER(MeshDesc)]),
+    "tmc_mesh_file_error": (ctypes.c_char_p, [vp]),
+    "tmc_mesh_file_close": (ctypes.c_int, [vp]),
+    "tmc_mesh_file_write": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(MeshDesc)]),
+    "tmc_history_create": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(MeshDesc), ctypes.POINTER(vp)]),
+    "tmc_history_write": (ctypes.c_int, [vp, vp, ctypes.c_double]),
+    "tmc_history_close": (ctypes.c_int, [vp]),
     "tmc_adv_set_initial": (ctypes.c_int, [vp, vp]),
     "tmc_adv_get": (ctypes.c_int, [vp, vp, vp]),
     "tmc_adv_elapsed": (ctypes.c_int, [vp, dp]),

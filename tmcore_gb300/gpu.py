@@ -421,3 +421,88 @@ class Coarsener:
             self.close()
         except Exception:
             pass
+
+
+def read_mesh_file(path: str):
+    """An MPAS grid file read by the library's NetCDF-classic reader
+    (tmc_mesh_file_open), as an MPASMesh (arrays copied)."""
+    from .mesh import MPASMesh
+
+    lib = _lib.gpu()
+    d = abi.MeshDesc()
+    f = ctypes.c_void_p()
+    rc = lib.tmc_mesh_file_open(str(path).encode(), ctypes.byref(f), ctypes.byref(d))
+    try:
+        if rc != 0:
+            raise TMCError(rc, lib.tmc_mesh_file_error(f).decode() if f.value else "tmc_mesh_file_open failed")
+        dims = {k: int(getattr(d, k)) for k in ("nCells", "nEdges", "nVertices", "maxEdges", "maxEdges2",
+                                                 "vertexDegree")}
+        n = {"Cell": dims["nCells"], "Edge": dims["nEdges"], "Vertex": dims["nVertices"]}
+        shapes = {"nEdgesOnCell": (n["Cell"],), "nEdgesOnEdge": (n["Edge"],),
+                  "cellsOnCell": (n["Cell"], dims["maxEdges"]), "edgesOnCell": (n["Cell"], dims["maxEdges"]),
+                  "verticesOnCell": (n["Cell"], dims["maxEdges"]), "cellsOnEdge": (n["Edge"], 2),
+                  "verticesOnEdge": (n["Edge"], 2), "edgesOnEdge": (n["Edge"], dims["maxEdges2"]),
+                  "cellsOnVertex": (n["Vertex"], dims["vertexDegree"]),
+                  "edgesOnVertex": (n["Vertex"], dims["vertexDegree"]),
+                  "kiteAreasOnVertex": (n["Vertex"], dims["vertexDegree"]),
+                  "weightsOnEdge": (n["Edge"], dims["maxEdges2"])}
+        vars_ = {}
+        for name, ctype in abi.MeshDesc._fields_[6:]:
+            ptr = getattr(d, name)
+            if not ptr:
+                continue
+            if name in shapes:
+                shape = shapes[name]
+            else:
+                kind = "Vertex" if name == "areaTriangle" else [k for k in ("Cell", "Edge", "Vertex")
+                                                                   if name.endswith(k)][0]
+                shape = (n[kind],)
+            size = int(np.prod(shape))
+            is_int = name.startswith("n") or name.endswith(("OnCell", "OnEdge", "OnVertex")) and name not in (
+                "kiteAreasOnVertex", "weightsOnEdge")
+            ct = ctypes.c_int32 if is_int else ctypes.c_double
+            arr = np.ctypeslib.as_array(ctypes.cast(ptr, ctypes.POINTER(ct)), shape=(size,)).copy()
+            vars_[name] = arr.reshape(shape)
+        return MPASMesh(dims, vars_, {})
+    finally:
+        if f.value:
+            lib.tmc_mesh_file_close(f)
+
+
+def write_mesh_file(path: str, mesh):
+    """Write an MPASMesh with the library's NetCDF-classic writer (tmc_mesh_file_write)."""
+    lib = _lib.gpu()
+    d, keep = mesh_desc(mesh)
+    rc = lib.tmc_mesh_file_write(str(path).encode(), ctypes.byref(d))
+    del keep
+    if rc != 0:
+        raise TMCError(rc, f"tmc_mesh_file_write({path}) failed")
+
+
+class HistoryWriter:
+    """History file of history_mod.F90 written by the library (tmc_history_*)."""
+
+    def __init__(self, path: str, mesh):
+        self.lib = _lib.gpu()
+        d, self._keep = mesh_desc(mesh)
+        hw = ctypes.c_void_p()
+        rc = self.lib.tmc_history_create(str(path).encode(), ctypes.byref(d), ctypes.byref(hw))
+        if rc != 0:
+            raise TMCError(rc, f"tmc_history_create({path}) failed")
+        self.hw = hw
+
+    def write(self, model: TMCoreGPU, seconds: float):
+        rc = self.lib.tmc_history_write(self.hw, model.h, float(seconds))
+        if rc != 0:
+            raise TMCError(rc, model.lib.tmc_last_error(model.h).decode())
+
+    def close(self):
+        if getattr(self, "hw", None) is not None and self.hw.value:
+            self.lib.tmc_history_close(self.hw)
+        self.hw = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
