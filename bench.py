@@ -179,14 +179,15 @@ def flux_kernel_bytes(nc: int, ne: int, S: int, mode: int | None = None) -> floa
     return tot / len(modes)
 
 
-def step_bytes(nc: int, ne: int, nv: int, S: int, ntr: int, diag: bool = True) -> float:
-    """All kernels of one CRK4 step, second-order tracers, invariants on stage 1:
-    4 stages of cell, vertex, edge_pv, edge_flux (stages 1-3 also prepare the
-    next stage's gd_edge, u, F), then the final update of cells and of edges
-    (which prepares the next step's first stage)."""
+def pass_bytes(nc: int, ne: int, nv: int, S: int, ntr: int, diag: bool = True) -> dict:
+    """Algorithmic bytes of each pass of one CRK4 step (4 stages of cell,
+    vertex, edge_pv, edge_flux with the invariants on stage 1; stages 1-3 of
+    the flux pass also prepare the next stage's gd_edge, u, F), then the final
+    update of cells and of edges (which prepares the next step's first stage),
+    as mean bytes per launch."""
     Mw = S
     sh = 4 if S == 4 else 0  # FP32 shadows
-    tot = 0.0
+    cell = vert = epv = flux = 0.0
     for k in (1, 2, 3, 4):
         dg = diag and k == 1
         # cell: nEdgesOnCell, edgesOnCell, nSign, cellsOnCell (tracers), 1/areaCell (f64) [+ f32 copies],
@@ -197,21 +198,25 @@ def step_bytes(nc: int, ne: int, nv: int, S: int, ntr: int, diag: bool = True) -
         if S == 8:
             rk_gd = {1: 8 * 4, 2: 8 * 6, 3: 8 * 6, 4: 8 * 4}[k]
         rk_q = {1: 4 * S, 2: 5 * S, 3: 5 * S, 4: 2 * S}[k] + (sh if k <= 3 else 0)
-        tot += nc * (1 + 24 + 6 + (24 if ntr else 0) + 8 + 2 * sh + S + S + S + rk_gd + ntr * (S + rk_q)
-                     + (24 if dg else 0)) + ne * (2 * S + 2 * Mw)
+        cell += nc * (1 + 24 + 6 + (24 if ntr else 0) + 8 + 2 * sh + S + S + S + rk_gd + ntr * (S + rk_q)
+                      + (24 if dg else 0)) + ne * (2 * S + 2 * Mw)
         # vertex: cellsOnVertex, edgesOnVertex, kite, tSign, 1/areaTriangle, fVertex; pv out;
         # gd and u, dcEdge gathered
-        tot += nv * (12 + 12 + 3 * Mw + 3 + Mw + Mw + S + (16 if dg else 0)) + nc * S + ne * (S + Mw)
+        vert += nv * (12 + 12 + 3 * Mw + 3 + Mw + Mw + S + (16 if dg else 0)) + nc * S + ne * (S + Mw)
         # edge_pv: verticesOnEdge; pv_e out; pv gathered
-        tot += ne * (8 + S) + nv * S
-        # edge_flux; stages 1-3 prepare the next stage instead of storing iap_u:
-        # next gd gathered, gd_edge/u/F written
-        tot += flux_kernel_bytes(nc, ne, S, k)
+        epv += ne * (8 + S) + nv * S
+        flux += flux_kernel_bytes(nc, ne, S, k)
     # final cells: gd r+w, acc r, shadow w; tracers r+w, acc r, shadow w
-    tot += nc * (24 + sh + ntr * (3 * S + sh))
     # final edges: iap_u r+w, acc r, cellsOnEdge, gd gathered, gd_edge/u/F written, areaEdge (energy)
-    tot += ne * (3 * S + 8 + 3 * S + Mw) + nc * S
-    return tot
+    final = nc * (24 + sh + ntr * (3 * S + sh)) + ne * (3 * S + 8 + 3 * S + Mw) + nc * S
+    return {"cell": cell / 4, "vertex": vert / 4, "edge_pv": epv / 4, "edge_flux": flux / 4, "final": final}
+
+
+def step_bytes(nc: int, ne: int, nv: int, S: int, ntr: int, diag: bool = True) -> float:
+    """All kernels of one CRK4 step (pass_bytes: four launches of each stage
+    pass and one final update)."""
+    b = pass_bytes(nc, ne, nv, S, ntr, diag)
+    return 4 * (b["cell"] + b["vertex"] + b["edge_pv"] + b["edge_flux"]) + b["final"]
 
 
 def step_model_bytes(nc: int, ne: int, nv: int, S: int, ntr: int) -> float:
@@ -503,6 +508,12 @@ def main():
     traffic = ncu_traffic("edge_flux_level9_fp32.json")
 
     sbytes = step_bytes(m.nCells, m.nEdges, m.nVertices, S, args.tracers)
+    # every pass of the step, launch by launch (CUDA events around the pass)
+    pt = gpu.pass_times(max(2, min(args.steps, 6)))
+    pb = pass_bytes(m.nCells, m.nEdges, m.nVertices, S, args.tracers)
+    passes = {k: {"ms_per_launch": pt[k], "algorithmic_bytes_per_launch": pb[k],
+                  "achieved_gbs": pb[k] / (pt[k] / 1e3) / 1e9, "frac": pb[k] / (pt[k] / 1e3) / 1e9 / peak}
+              for k in pt if pt[k] > 0}
     scope_bytes = step_model_bytes(m.nCells, m.nEdges, m.nVertices, S, args.tracers)
     step_s = ms_total / args.steps / 1e3
 
@@ -595,6 +606,7 @@ def main():
         "roofline": {"bound": "hbm", "kernel": "k_edge_flux<float>", "achieved": achieved, "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                      "algorithmic_bytes_per_launch": fb, "launch_ms": t_launch * 1e3, "launches_timed": n_flux},
+        "passes": passes,
         "step_roofline": {"algorithmic_bytes_per_step": sbytes, "achieved_gbs": sbytes / step_s / 1e9,
                           "frac": sbytes / step_s / 1e9 / peak,
                           "scope_model_bytes_per_step": scope_bytes,

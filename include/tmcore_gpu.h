@@ -137,6 +137,11 @@ int tmc_spatial_operators(tmc_handle* h, const double* gd, const double* iap_u, 
  * the fastest per pass, restores the state and re-captures the step graphs.
  * block_sizes (may be NULL) receives {cell, vertex, edge_pv, edge_flux, final}. */
 int tmc_autotune(tmc_handle* h, int32_t steps, int32_t block_sizes[5]);
+/* Mean device time of one launch of each pass of the fused step over
+ * `steps` eager steps (CUDA events around the pass; the steps advance the
+ * state): ms = {cell, vertex, edge_pv (with the closure and conservative APVM
+ * kernels), edge_flux, final update}. */
+int tmc_pass_times(tmc_handle* h, int32_t steps, double ms[5]);
 
 /* History diagnostics on the device (history_mod.F90:124-174 with
  * mpas_reconstruct, tmcore_swm_mod.F90:78-86): for state(old) of the selected

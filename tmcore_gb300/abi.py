@@ -80,6 +80,7 @@ SYMBOLS = {
     "tmc_history_fields": (ctypes.c_int, [vp, vp, vp, vp, vp, vp, vp, vp]),
     "tmc_reconstruct": (ctypes.c_int, [vp, vp, vp, vp, vp, vp, vp]),
     "tmc_autotune": (ctypes.c_int, [vp, i32, ctypes.POINTER(i32)]),
+    "tmc_pass_times": (ctypes.c_int, [vp, i32, vp]),
     "tmc_group_create": (ctypes.c_int, [ctypes.POINTER(vp), i32, ctypes.c_double, ctypes.POINTER(vp)]),
     "tmc_group_run": (ctypes.c_int, [vp, i32]),
     "tmc_group_synchronize": (ctypes.c_int, [vp]),

@@ -3,6 +3,7 @@
 // caller's element order, timing.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -907,6 +908,9 @@ int tmc_create(const tmc_mesh_desc* mesh, const tmc_params* params, tmc_handle**
   h->P.cap = (nmax + minbs - 1) / minbs;
   h->P.base = h->dalloc<double>(h->P.member_stride() * h->members);
   for (int k = 0; k < P_COUNT; ++k) h->bsp[k] = h->bs;
+  // the FP32 cell pass is compiled for at most 256 threads per block (its
+  // register budget leaves room for 3 blocks per SM)
+  if (p.precision == TMC_FP32) h->bsp[P_CELL] = std::min(h->bsp[P_CELL], 256);
   set_counts(h.get());
   const int bc = grid_for(hm.nc, h->bs);
   for (int r = 0; r < R_COUNT; ++r) h->gen_counts[r] = h->counts[r];
@@ -1467,6 +1471,46 @@ int tmc_adv_elapsed(tmc_handle* h, double* seconds) {
   return TMC_OK;
 }
 
+int tmc_pass_times(tmc_handle* h, int32_t steps, double ms[5]) {
+  TMC_REQUIRE_HANDLE(h);
+  if (!ms) return TMC_E_ARG;
+  if (!h->have_state) return h->fail(TMC_E_STATE, "no state set");
+  if (h->generic) return h->fail(TMC_E_UNSUP, "tmc_pass_times times the fused CRK4 shallow-water step");
+  if (steps <= 0) steps = 3;
+  const size_t nev = (size_t)steps * 8 + 2;
+  while (h->ev_pool.size() < nev) {
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) return h->cuda_check("cudaEventCreate");
+    h->ev_pool.push_back(e);
+  }
+  int rc;
+  const int saved = h->timed_pass;
+  for (int pass = 0; pass < P_COUNT; ++pass) {
+    h->timed_pass = pass;
+    std::vector<cudaEvent_t> evs(h->ev_pool.begin(), h->ev_pool.begin() + nev);
+    size_t pos = 0;
+    for (int i = 0; i < steps; ++i) {
+      const bool diag = h->p.diag_every > 0 && (h->step_count % h->p.diag_every) == 0;
+      ensure_prep(h);
+      h->eng->launch_step(diag, &evs, &pos);
+      h->step_count++;
+    }
+    if ((rc = sync(h, "tmc_pass_times"))) {
+      h->timed_pass = saved;
+      return rc;
+    }
+    double sum = 0.0;
+    for (size_t k = 0; k + 1 < pos; k += 2) {
+      float dt = 0.f;
+      cudaEventElapsedTime(&dt, evs[k], evs[k + 1]);
+      sum += dt;
+    }
+    ms[pass] = pos ? sum / (double)(pos / 2) : 0.0;
+  }
+  h->timed_pass = saved;
+  return h->cuda_check("tmc_pass_times");
+}
+
 int tmc_autotune(tmc_handle* h, int32_t steps, int32_t block_sizes[5]) {
   TMC_REQUIRE_HANDLE(h);
   if (!h->have_state) return h->fail(TMC_E_STATE, "tmc_autotune needs a state (tmc_set_initial)");
@@ -1509,7 +1553,7 @@ int tmc_autotune(tmc_handle* h, int32_t steps, int32_t block_sizes[5]) {
     double best = 1e300;
     int best_bs = h->bsp[pass];
     for (int c : cand_all) {
-      if (c > limit) continue;
+      if (c > limit || (pass == P_CELL && f32 && c > 256)) continue;
       h->bsp[pass] = c;
       set_counts(h);
       // one untimed step with this block size, then `steps` timed ones

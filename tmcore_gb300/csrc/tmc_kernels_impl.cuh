@@ -21,6 +21,7 @@ namespace tmc {
 
 constexpr int kMaxBlock = 512;
 constexpr int kMemberBlock = 256;  // block size limit of the ensemble (member-batched) kernels
+constexpr int kCellBlock = 256;    // block size limit of the FP32 cell pass (register budget for 3 blocks/SM)
 constexpr int kME = 6;    // unrolled maxEdges of the FP32 path
 constexpr int kME2 = 10;  // unrolled maxEdges2 of the FP32 path
 
@@ -535,12 +536,10 @@ __global__ void __launch_bounds__(kMaxBlock) k_vertex(DevMesh M, ModelOpt O, Sta
   const StageIO<T> S = kB ? S0.at(blockIdx.y) : S0;
   const Partials P = kB ? P0.at(blockIdx.y) : P0;
   double pe = 0.0, av = 0.0;
-  TMC_FOR_EPT(v, M.nv) {
-    T gv, vo, pv;
-    if constexpr (kF64<T>) {
+  if constexpr (kF64<T>) {
+    TMC_FOR_EPT(v, M.nv) {
       // operators_mod.F90:106-123 (c2v), :76-91 (curl), :262-270 (pv)
-      double s = 0.0;
-      gv = 0.0;
+      double s = 0.0, gv = 0.0;
 #pragma unroll
       for (int i = 0; i < 3; ++i)
         gv = gv + S.gd_in[M.cellsOnVertex[(size_t)i * M.nv + v]] * M.kite[(size_t)i * M.nv + v];
@@ -551,9 +550,20 @@ __global__ void __launch_bounds__(kMaxBlock) k_vertex(DevMesh M, ModelOpt O, Sta
         const int e = M.edgesOnVertex[(size_t)i * M.nv + v];
         s = s + (double)M.tSign[(size_t)i * M.nv + v] * S.u[e] * M.dcEdge[e];
       }
-      vo = (-s) / At;
-      pv = (M.fVertex[v] + vo) / gv;
-    } else {
+      const double vo = (-s) / At;
+      const double pv = (M.fVertex[v] + vo) / gv;
+      S.pv_v[v] = pv;
+      if (S.vor) S.vor[v] = vo;
+      if (S.gd_v) S.gd_v[v] = gv;
+      if (diag) {
+        pe = pe + gv * (pv * pv) * At;
+        av = av + (vo + M.fVertex[v]) * At;
+      }
+    }
+  } else {
+    // one vertex at a time: measured faster than batching the loads of the
+    // thread's vertices (which costs occupancy for a pass with three gathers)
+    TMC_FOR_EPT(v, M.nv) {
       int ci[3], ei[3];
       float kt[3], ts[3];
 #pragma unroll
@@ -571,20 +581,14 @@ __global__ void __launch_bounds__(kMaxBlock) k_vertex(DevMesh M, ModelOpt O, Sta
         dc[i] = M.dcEdge_f[ei[i]];
       }
       const float iA = M.invAreaTriangle_f[v];
-      gv = (g[0] * kt[0] + g[1] * kt[1] + g[2] * kt[2]) * iA;
-      const float s = ts[0] * uu[0] * dc[0] + ts[1] * uu[1] * dc[1] + ts[2] * uu[2] * dc[2];
-      vo = -s * iA;
-      pv = (M.fVertex_f[v] + vo) / gv;
-    }
-    S.pv_v[v] = pv;
-    if (S.vor) S.vor[v] = vo;
-    if (S.gd_v) S.gd_v[v] = gv;
-    if (diag) {
-      if constexpr (kF64<T>) {
-        const double At = M.areaTriangle[v];
-        pe = pe + gv * (pv * pv) * At;
-        av = av + (vo + M.fVertex[v]) * At;
-      } else {
+      const float gv = (g[0] * kt[0] + g[1] * kt[1] + g[2] * kt[2]) * iA;
+      const float sv = ts[0] * uu[0] * dc[0] + ts[1] * uu[1] * dc[1] + ts[2] * uu[2] * dc[2];
+      const float vo = -sv * iA;
+      const float pv = (M.fVertex_f[v] + vo) / gv;
+      S.pv_v[v] = pv;
+      if (S.vor) S.vor[v] = vo;
+      if (S.gd_v) S.gd_v[v] = gv;
+      if (diag) {
         const double At = M.areaTriangle[v];
         pe += (double)(gv * (pv * pv)) * At;
         av += ((double)vo + M.fVertex[v]) * At;
@@ -619,6 +623,26 @@ template <class T, bool kB>
 __global__ void __launch_bounds__(kMaxBlock) k_edge_pv(DevMesh M, ModelOpt O, StageIO<T> S0) {
   const StageIO<T> S = kB ? S0.at(blockIdx.y) : S0;
   const bool need_v = (O.pv_scheme >= 2) || (O.pv_scheme == 1 && O.apvm_weight != 0.0);
+  if (!need_v) {
+    // centred pv (APVM weight 0): all loads of the thread's kEPT edges first
+    const int e0 = blockIdx.x * (kEPT * blockDim.x) + threadIdx.x;
+    int v1[kEPT], v2[kEPT];
+    T pe[kEPT];
+#pragma unroll
+    for (int j = 0; j < kEPT; ++j) {
+      const int e = e0 + j * blockDim.x;
+      v1[j] = e < M.ne ? M.verticesOnEdge[e] : 0;
+      v2[j] = e < M.ne ? M.verticesOnEdge[M.ne + e] : 0;
+    }
+#pragma unroll
+    for (int j = 0; j < kEPT; ++j) pe[j] = T(0.5) * (S.pv_v[v1[j]] + S.pv_v[v2[j]]);
+#pragma unroll
+    for (int j = 0; j < kEPT; ++j) {
+      const int e = e0 + j * blockDim.x;
+      if (e < M.ne) S.pv_e[e] = pe[j];
+    }
+    return;
+  }
   TMC_FOR_EPT(e, M.ne) {
     const int v1 = M.verticesOnEdge[e], v2 = M.verticesOnEdge[M.ne + e];
     const T p1 = S.pv_v[v1], p2 = S.pv_v[v2];
@@ -1029,17 +1053,39 @@ __global__ void __launch_bounds__(kMaxBlock) k_final_cells(DevMesh M, ModelOpt O
   const StageIO<T> S = kB ? S0.at(blockIdx.y) : S0;
   const double* diag = kB ? diag0 + (size_t)blockIdx.y * kDiagStride : diag0;
   const double bdt = diag[9];
-  TMC_FOR_EPT(i, M.nc) {
-    double* gd = const_cast<double*>(S.gd_old);
-    const double g = gd[i] + bdt * S.gd_acc[i];
-    gd[i] = g;
-    if constexpr (!kF64<T>) const_cast<float*>(S.gdf_in)[i] = (float)g;
-    for (int q = 0; q < O.n_tracers; ++q) {
+  // all loads of the thread's kEPT cells before any store (a load after a
+  // store through a possibly aliasing pointer waits a full round trip)
+  const int i0 = blockIdx.x * (kEPT * blockDim.x) + threadIdx.x;
+  double* gd = const_cast<double*>(S.gd_old);
+  double g[kEPT];
+#pragma unroll
+  for (int j = 0; j < kEPT; ++j) {
+    const int i = i0 + j * blockDim.x;
+    g[j] = i < M.nc ? gd[i] + bdt * S.gd_acc[i] : 0.0;
+  }
+#pragma unroll
+  for (int j = 0; j < kEPT; ++j) {
+    const int i = i0 + j * blockDim.x;
+    if (i >= M.nc) continue;
+    gd[i] = g[j];
+    if constexpr (!kF64<T>) const_cast<float*>(S.gdf_in)[i] = (float)g[j];
+  }
+  T* qq = const_cast<T*>(S.q_old);
+  for (int q = 0; q < O.n_tracers; ++q) {
+    T qn[kEPT];
+#pragma unroll
+    for (int j = 0; j < kEPT; ++j) {
+      const int i = i0 + j * blockDim.x;
       const size_t qi = (size_t)q * M.nc + i;
-      T* qq = const_cast<T*>(S.q_old);
-      const T qn = qq[qi] + T(bdt) * S.q_acc[qi];
-      qq[qi] = qn;
-      if constexpr (!kF64<T>) const_cast<float*>(S.qr_in)[qi] = qn / (float)g;
+      qn[j] = i < M.nc ? qq[qi] + T(bdt) * S.q_acc[qi] : T(0);
+    }
+#pragma unroll
+    for (int j = 0; j < kEPT; ++j) {
+      const int i = i0 + j * blockDim.x;
+      if (i >= M.nc) continue;
+      const size_t qi = (size_t)q * M.nc + i;
+      qq[qi] = qn[j];
+      if constexpr (!kF64<T>) const_cast<float*>(S.qr_in)[qi] = qn[j] / (float)g[j];
     }
   }
 }
@@ -1057,25 +1103,39 @@ __global__ void __launch_bounds__(kMaxBlock) k_final_edges(DevMesh M, ModelOpt O
   const double bdt = diag[9];
   double en = 0.0;
   const CellSrc<T> C{S.gd_old, S.gdf_in, S.q_old, S.qr_in};
-  TMC_FOR_EPT(e, M.ne) {
-    const int c1 = M.cellsOnEdge[e], c2 = M.cellsOnEdge[M.ne + e];
-    T* iap = const_cast<T*>(S.iap_old);
-    const T a0 = iap[e], acc = S.iap_acc[e];
-    T g1, g2;
+  // loads of all kEPT edges first (see k_final_cells)
+  const int e0 = blockIdx.x * (kEPT * blockDim.x) + threadIdx.x;
+  T* iap = const_cast<T*>(S.iap_old);
+  int c1[kEPT], c2[kEPT];
+  T ia[kEPT], g1[kEPT], g2[kEPT];
+#pragma unroll
+  for (int j = 0; j < kEPT; ++j) {
+    const int e = e0 + j * blockDim.x;
+    const bool in = e < M.ne;
+    c1[j] = in ? M.cellsOnEdge[e] : 0;
+    c2[j] = in ? M.cellsOnEdge[M.ne + e] : 0;
+    ia[j] = in ? iap[e] + T(bdt) * S.iap_acc[e] : T(0);
+  }
+#pragma unroll
+  for (int j = 0; j < kEPT; ++j) {
     if constexpr (kF64<T>) {
-      g1 = S.gd_old[c1];
-      g2 = S.gd_old[c2];
+      g1[j] = S.gd_old[c1[j]];
+      g2[j] = S.gd_old[c2[j]];
     } else {
-      g1 = S.gdf_in[c1];
-      g2 = S.gdf_in[c2];
+      g1[j] = S.gdf_in[c1[j]];
+      g2[j] = S.gdf_in[c2[j]];
     }
-    const T ia = a0 + T(bdt) * acc;
-    iap[e] = ia;
-    prep_edge<T>(M, O, e, c1, c2, ia, g1, g2, C, S.gd_e, S.u, S.F, S.Fq);
+  }
+#pragma unroll
+  for (int j = 0; j < kEPT; ++j) {
+    const int e = e0 + j * blockDim.x;
+    if (e >= M.ne) continue;
+    iap[e] = ia[j];
+    prep_edge<T>(M, O, e, c1[j], c2[j], ia[j], g1[j], g2[j], C, S.gd_e, S.u, S.F, S.Fq);
     if constexpr (kF64<T>)
-      en = en + energy_term<T>(M, e, ia);
+      en = en + energy_term<T>(M, e, ia[j]);
     else
-      en += (double)energy_term<T>(M, e, ia);
+      en += (double)energy_term<T>(M, e, ia[j]);
   }
   const double v[1] = {en};
   const int r[1] = {R_EN_E};
@@ -1246,7 +1306,7 @@ __device__ __forceinline__ void cell_fast_body(const DevMesh& M, const StageIO<f
 }
 
 template <int NTR>
-__global__ void __launch_bounds__(kMaxBlock) k_cell_fast(DevMesh M, StageIO<float> S0, RKStage rk, Partials P0,
+__global__ void __launch_bounds__(kCellBlock, 3) k_cell_fast(DevMesh M, StageIO<float> S0, RKStage rk, Partials P0,
                                                          int diag) {
   cell_fast_body<NTR, false>(M, S0, rk, P0, diag);
 }

@@ -169,6 +169,12 @@ class TMCoreGPU:
         self._chk(self.lib.tmc_closure_features(self.h, _ptr(f), _ptr(pv)))
         return f, pv
 
+    def pass_times(self, steps: int = 3) -> dict:
+        """Mean device ms per launch of each pass of the fused step (tmc_pass_times)."""
+        out = np.empty(5)
+        self._chk(self.lib.tmc_pass_times(self.h, int(steps), _ptr(out)))
+        return dict(zip(("cell", "vertex", "edge_pv", "edge_flux", "final"), out.tolist()))
+
     # ------------------------------------------------------------------ ensembles
     def select_member(self, m: int):
         """State-transfer calls address member m of an ensemble (members > 1)."""
