@@ -1126,6 +1126,7 @@ __global__ void __launch_bounds__(kMaxBlock) k_final_edges(DevMesh M, ModelOpt O
       g2[j] = S.gdf_in[c2[j]];
     }
   }
+  T enT = T(0);  // FP32 path: the thread's few terms in FP32, FP64 from the block sum on
 #pragma unroll
   for (int j = 0; j < kEPT; ++j) {
     const int e = e0 + j * blockDim.x;
@@ -1135,8 +1136,9 @@ __global__ void __launch_bounds__(kMaxBlock) k_final_edges(DevMesh M, ModelOpt O
     if constexpr (kF64<T>)
       en = en + energy_term<T>(M, e, ia[j]);
     else
-      en += (double)energy_term<T>(M, e, ia[j]);
+      enT += energy_term<T>(M, e, ia[j]);
   }
+  if constexpr (!kF64<T>) en = (double)enT;
   const double v[1] = {en};
   const int r[1] = {R_EN_E};
   block_store<double, 1>(v, P, r);
