@@ -38,6 +38,7 @@ struct EngineBase {
   virtual void launch_prep() = 0;
   virtual void launch_spatial_only() = 0;
   virtual void set_state_dev(const double* raw_gd, const double* raw_iap) = 0;  // from raw (original order)
+  virtual void gather_field(int which, const double* raw) = 0;                  // F_GD, F_IAP or tracers (-1), no shadows
   virtual void get_field(int which, double* raw_out) = 0;                       // scatter to raw
   virtual void set_iap_from_u(const double* ge_new, const double* u_new) = 0;
   virtual void set_tracers_dev(const double* raw_q) = 0;
@@ -106,6 +107,8 @@ struct tmc_handle {
   int* d_closure_err = nullptr;
   int sms = 148;
   double* d_hist = nullptr;    // history outputs on cells (5 x nCells)
+  cudaStream_t cst = nullptr;  // host-copy stream of tmc_time_integrate
+  cudaEvent_t cev[8] = {};
   double* d_hist_e = nullptr;  // history outputs on edges and vertices
   int timed_pass = 3;  // the pass tmc_time_steps brackets with events
 
@@ -586,6 +589,16 @@ struct Engine : EngineBase {
   size_t ov() const { return (size_t)h->cur * h->M.nv; }
   size_t oq() const { return (size_t)h->cur * qsz(); }
 
+  void gather_field(int which, const double* raw) override {
+    if (which == F_GD)
+      launch_gather<double>(h->M.nc, raw, h->d_cell_n2o, gd[0] + oc(), h->st);
+    else if (which == F_IAP)
+      launch_gather<T>(h->M.ne, raw, h->d_edge_n2o, iap[0] + oe(), h->st);
+    else
+      for (int k = 0; k < h->O.n_tracers; ++k)
+        launch_gather<T>(h->M.nc, raw + (size_t)k * h->M.nc, h->d_cell_n2o, q[0] + oq() + (size_t)k * h->M.nc,
+                         h->st);
+  }
   void set_state_dev(const double* raw_gd, const double* raw_iap) override {
     launch_gather<double>(h->M.nc, raw_gd, h->d_cell_n2o, gd[0] + oc(), h->st);
     launch_gather<T>(h->M.ne, raw_iap, h->d_edge_n2o, iap[0] + oe(), h->st);
@@ -953,6 +966,12 @@ int tmc_create(const tmc_mesh_desc* mesh, const tmc_params* params, tmc_handle**
 int tmc_destroy(tmc_handle* h) {
   if (!h) return TMC_OK;
   if (h->st) cudaStreamSynchronize(h->st);
+  if (h->cst) {
+    cudaStreamSynchronize(h->cst);
+    for (cudaEvent_t e : h->cev)
+      if (e) cudaEventDestroy(e);
+    cudaStreamDestroy(h->cst);
+  }
   if (h->g_step) cudaGraphExecDestroy(h->g_step);
   if (h->g_step_diag) cudaGraphExecDestroy(h->g_step_diag);
   for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
@@ -1132,25 +1151,54 @@ int tmc_time_integrate(tmc_handle* h, const double* gd_old, const double* iap_u_
   const bool trc = h->O.n_tracers > 0;
   if (trc && (!qgd_old || !qgd_new)) return h->fail(TMC_E_ARG, "tmc_time_integrate: tracers need qgd arrays");
   const size_t nq = (size_t)h->M.nc * h->O.n_tracers;
-  int rc;
-  if ((rc = h2d(h, h->raw_c, gd_old, h->M.nc))) return rc;
-  if ((rc = h2d(h, h->raw_e, iap_u_old, h->M.ne))) return rc;
-  h->eng->set_state_dev(h->raw_c, h->raw_e);
-  if (trc) {
-    if ((rc = h2d(h, h->raw_q, qgd_old, nq))) return rc;
-    h->eng->set_tracers_dev(h->raw_q);
+  // The host copies run on a second stream, overlapped with the permutation
+  // gathers and scatters on the compute stream: each field's gather waits for
+  // its own copy only, each field's copy back waits for its own scatter only.
+  if (!h->cst) {
+    if (cudaStreamCreateWithFlags(&h->cst, cudaStreamNonBlocking) != cudaSuccess)
+      return h->cuda_check("tmc_time_integrate: copy stream");
+    for (auto& e : h->cev)
+      if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
+        return h->cuda_check("tmc_time_integrate: events");
   }
+  cudaStream_t cs = h->cst;
+  cudaEventRecord(h->cev[0], h->st);  // earlier work on the raw buffers is done
+  cudaStreamWaitEvent(cs, h->cev[0], 0);
+  struct Io {
+    const double* in;
+    double* out;
+    double* raw;
+    size_t n;
+    int field;
+  } io[3] = {{gd_old, gd_new, h->raw_c, (size_t)h->M.nc, F_GD},
+             {iap_u_old, iap_u_new, h->raw_e, (size_t)h->M.ne, F_IAP},
+             {qgd_old, qgd_new, h->raw_q, nq, -1}};
+  const int nio = trc ? 3 : 2;
+  for (int i = 0; i < nio; ++i) {
+    if (cudaMemcpyAsync(io[i].raw, io[i].in, io[i].n * sizeof(double), cudaMemcpyHostToDevice, cs) != cudaSuccess)
+      return h->cuda_check("H2D");
+    cudaEventRecord(h->cev[1 + i], cs);
+  }
+  for (int i = 0; i < nio; ++i) {
+    cudaStreamWaitEvent(h->st, h->cev[1 + i], 0);
+    h->eng->gather_field(io[i].field, io[i].raw);
+  }
+  h->eng->refresh_shadows(0);
   h->have_state = true;
   h->prep_valid = false;
+  int rc;
   if ((rc = launch_one_step(h))) return rc;
-  h->eng->get_field(F_GD, h->raw_c);
-  if ((rc = d2h(h, gd_new, h->raw_c, h->M.nc))) return rc;
-  h->eng->get_field(F_IAP, h->raw_e);
-  if ((rc = d2h(h, iap_u_new, h->raw_e, h->M.ne))) return rc;
-  if (trc) {
-    h->eng->get_tracers_dev(h->raw_q);
-    if ((rc = d2h(h, qgd_new, h->raw_q, nq))) return rc;
+  for (int i = 0; i < nio; ++i) {
+    if (io[i].field == F_GD || io[i].field == F_IAP)
+      h->eng->get_field(io[i].field, io[i].raw);
+    else
+      h->eng->get_tracers_dev(io[i].raw);
+    cudaEventRecord(h->cev[4 + i], h->st);
+    cudaStreamWaitEvent(cs, h->cev[4 + i], 0);
+    if (cudaMemcpyAsync(io[i].out, io[i].raw, io[i].n * sizeof(double), cudaMemcpyDeviceToHost, cs) != cudaSuccess)
+      return h->cuda_check("D2H");
   }
+  if (cudaStreamSynchronize(cs) != cudaSuccess) return h->cuda_check("tmc_time_integrate");
   if ((rc = sync(h, "tmc_time_integrate"))) return rc;
   return h->cuda_check("tmc_time_integrate");
 }
