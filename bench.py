@@ -326,8 +326,9 @@ def run_ensemble(args, local, ics, peak):
 
 def run_closure_leg(args, local, ics, peak):
     """Config 5's step: the FP32 ensemble with the learned closure on (a
-    network of the trained shape; the cost does not depend on its weights),
-    against the same ensemble without it."""
+    network of the trained shape; the cost does not depend on its weights) in
+    every stage and in stage 1 only (held for stages 2-4), against the same
+    ensemble without it."""
     import numpy as np
 
     from tmcore_gb300 import abi, mesh
@@ -352,6 +353,10 @@ def run_closure_leg(args, local, ics, peak):
     ens.step(args.warmup)
     ens.synchronize()
     ms, _, _, launches = ens.time_steps(args.ensemble_steps, total=True, flux=False)
+    ens.set_closure_stages(False)  # the network in stage 1, its output held for stages 2-4
+    ens.step(args.warmup)
+    ens.synchronize()
+    ms_s1, _, _, _ = ens.time_steps(args.ensemble_steps, total=True, flux=False)
     timed_out = ens.closure_status()
     ens.close()
     net.close()
@@ -360,6 +365,8 @@ def run_closure_leg(args, local, ics, peak):
     return {"workload": f"{M} FP32 members on level {L} with the learned PV-on-edge closure every stage",
             "members": M, "ms_per_step": step_s * 1e3, "member_days_per_s": M * dt / DAY / step_s,
             "plain_ms_per_step": ms_plain / args.ensemble_steps,
+            "stage1_ms_per_step": ms_s1 / args.ensemble_steps,
+            "stage1_member_days_per_s": M * dt / DAY / (ms_s1 / args.ensemble_steps / 1e3),
             "closure_tflops": flops / 1e12 / (step_s - ms_plain / args.ensemble_steps / 1e3)
             if step_s * 1e3 > ms_plain / args.ensemble_steps else None,
             "closure_mma_tflops_per_step": flops / 1e12, "gpu_launches": launches, "timed_out": timed_out}

@@ -201,23 +201,32 @@ int tmc_mlp_gradient(tmc_mlp* n, const float* x, const float* y, int64_t rows, f
  * [nEdges][TMC_MLP_FEATURES] features and pv_edge of state(old) of the
  * selected member (caller's edge order), for training. */
 int tmc_set_closure(tmc_handle* h, const tmc_mlp* net);
+/* every_stage 1 (the default): the network runs on every stage's pv_edge;
+ * 0: it runs in stage 1 and its output is held and added in stages 2-4. */
+int tmc_set_closure_stages(tmc_handle* h, int32_t every_stage);
 int tmc_set_member_closure(tmc_handle* h, int32_t member, int32_t on);
 int tmc_closure_status(tmc_handle* h, int32_t* timed_out);
 int tmc_closure_features(tmc_handle* h, float* features, double* pv_edge);
 
 /* Coarse-graining of a fine-mesh state onto a coarser mesh (the closure's
- * training data): cells are area-weighted means over the fine cells whose
- * centres lie in the coarse cell (nearest coarse generator); the coarse
- * normal velocity is the sum of the fine normal fluxes u dvEdge across the
- * boundary between two coarse cells' aggregates divided by the coarse dvEdge
- * (edge-flux averaging); edge scalars (pv on edges) are dvEdge-weighted means
- * over the same fine edges.  Host arrays in both meshes' own order; any
- * output pointer may be NULL.  tmc_coarsen_unmatched counts coarse edges
- * without fine edges (their outputs are 0). */
+ * training data and held-out truth).  Cells: kite-area-weighted means (each
+ * fine kite goes to the coarse generator nearest its centre point; kites in
+ * a tie band of 0.1 fine dcEdge between two generators are split equally).
+ * Edges: the mean, over the fine edges within 0.75 fine dcEdge of the coarse
+ * Voronoi edge and between its vertices, of the fine velocity u n + v t (v
+ * the TRiSK tangential velocity) along the coarse normal; edge scalars (pv
+ * on edges) are plain means over the same fine edges.  Host arrays in both
+ * meshes' own order; any output pointer may be NULL.  device < 0 builds the
+ * maps only (no CUDA; tmc_coarsen_apply then returns TMC_E_UNSUP).
+ * tmc_coarsen_rows returns map `which` (0 cells, 1 normal velocity, 2 edge
+ * scalars) as CSR rows over the fine array (start has a row count + 1
+ * entries; NULL pointers return nnz only).  tmc_coarsen_unmatched counts
+ * coarse edges without fine edges (their outputs are 0). */
 typedef struct tmc_coarsen tmc_coarsen;
 int tmc_coarsen_create(const tmc_mesh_desc* fine, const tmc_mesh_desc* coarse, int32_t device, tmc_coarsen** out);
 int tmc_coarsen_apply(tmc_coarsen* c, const double* fine_gd, const double* fine_u, const double* fine_pv_edge,
                       double* coarse_gd, double* coarse_u, double* coarse_pv_edge);
+int tmc_coarsen_rows(const tmc_coarsen* c, int32_t which, int64_t* nnz, int32_t* start, int32_t* idx, double* w);
 int tmc_coarsen_unmatched(const tmc_coarsen* c, int64_t* edges);
 /* the coarse cell (1-based) each fine cell is aggregated into */
 int tmc_coarsen_cell_map(const tmc_coarsen* c, int32_t* coarse_cell_of_fine);

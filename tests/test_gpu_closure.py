@@ -1,5 +1,6 @@
 """The learned closure inside the FP32 step: features, a zero network that
-changes nothing, and the per-member switch of an ensemble."""
+changes nothing, the per-member switch of an ensemble, the training pipeline
+and what the trained network gains over the plain method on held-out seeds."""
 import numpy as np
 import pytest
 
@@ -60,9 +61,11 @@ def test_zero_network_changes_nothing(mesh4):
     net.close()
 
 
-def test_member_switch(mesh4):
+@pytest.mark.parametrize("every_stage", [True, False])
+def test_member_switch(mesh4, every_stage):
     """Member 1 with the closure switched off evolves exactly as the plain
-    model; member 0 with it on does not."""
+    model; member 0 with it on does not (network in every stage, or in stage
+    1 with its output held for stages 2-4)."""
     from tmcore_gb300.gpu import ClosureMLP, TMCoreGPU
 
     net = ClosureMLP(seed=2)
@@ -78,6 +81,7 @@ def test_member_switch(mesh4):
         ens.set_initial(gd, u, ghs)
     plain.set_initial(gd, u, ghs)
     ens.set_closure(net)
+    ens.set_closure_stages(every_stage)
     ens.set_member_closure(1, False)
     ens.step(6)
     plain.step(6)
@@ -132,3 +136,25 @@ def test_fallback_switches_off_a_drifting_member(mesh4):
         ens.close()
     good.close()
     bad.close()
+
+
+def test_trained_closure_gains_on_held_out_seeds():
+    """Level-6 FP64 runs coarse-grained to level 4 train the network; on 8
+    held-out seeds, one day on level 4 with the closure (in every stage, and
+    in stage 1 held for the others) has a lower u error against the
+    coarse-grained level-6 truth than level 4 without it, and no higher h
+    error; the plain level-5 run, scored the same way, is more accurate than
+    plain level 4 (the comparison itself is sound)."""
+    from tmcore_gb300 import closure
+
+    X, Y = closure.training_data(fine_level=6, coarse_level=4, runs=8, days=2.0, samples_per_run=16)
+    net, losses, _ = closure.train(X, Y, steps=1500)
+    assert np.mean(losses[-20:]) < 0.5 * losses[0]
+    r = closure.evaluate(net, fine_level=6, coarse_level=4, members=8, days=1.0, samples=1)
+    e = {k: (v["h"][0], v["u"][0]) for k, v in r["error"].items()}
+    assert not r["closure_timed_out"]
+    for k in ("closure", "closure_stage1"):
+        assert e[k][1] < 0.99 * e["plain"][1], e
+        assert e[k][0] < 1.002 * e["plain"][0], e
+    assert e["plain_finer"][0] < e["plain"][0] and e["plain_finer"][1] < e["plain"][1]
+    net.close()

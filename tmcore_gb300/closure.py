@@ -99,6 +99,101 @@ def load(path, device=0):
     return net
 
 
+def _rel_l2(a, b, w):
+    return float(np.sqrt(np.sum(w * (a - b) ** 2) / np.sum(w * b * b)))
+
+
+def _member_states(model, members):
+    out = []
+    for k in range(members):
+        model.select_member(k)
+        gd, _, u = model.get_state()
+        out.append((gd, u))
+    return out
+
+
+def evaluate(net, fine_level=7, coarse_level=5, members=8, days=5.0, samples=5, seed0=10_000, device=0,
+             log=None):
+    """Held-out comparison of the learned coarse run with the plain method.
+
+    For `members` seeds not used in training, the FP64 run on the fine mesh,
+    coarse-grained onto the coarse mesh, is the truth.  Four FP32 ensembles
+    start from the coarse-grained initial state: the coarse mesh with the
+    closure in every stage ("closure"), the same with the closure run in stage
+    1 and its output held for the other stages ("closure_stage1"), the coarse
+    mesh without it ("plain"), and the plain method one level finer
+    ("plain_finer", coarse-grained onto the coarse mesh for scoring).  At `samples` evenly
+    spaced times each gets the member-mean relative L2 error of h (area
+    weighted) and of u (dvEdge dcEdge weighted); each gets its device time per
+    simulated day (CUDA events around its steps, all members).
+    """
+    fine, coarse, mid = icos_mesh(fine_level), icos_mesh(coarse_level), icos_mesh(coarse_level + 1)
+    kw = dict(pv_scheme=1, apvm_weight=0.0, adv_order=2, conserve_energy=1, renumber=1, device=device)
+    cg_c, cg_m = Coarsener(fine, coarse, device=device), Coarsener(fine, mid, device=device)
+    cg_mc = Coarsener(mid, coarse, device=device)
+    dt_f, dt_c, dt_m = level_dt(fine_level), level_dt(coarse_level), level_dt(coarse_level + 1)
+    total = days * DAY
+    n_f = int(round(total / samples / dt_f))
+    n_c, n_m = int(round(total / samples / dt_c)), int(round(total / samples / dt_m))
+    runs = {
+        "closure": TMCoreGPU(coarse, members=members, dt=dt_c, precision=abi.TMC_FP32, diag_every=0, **kw),
+        "closure_stage1": TMCoreGPU(coarse, members=members, dt=dt_c, precision=abi.TMC_FP32, diag_every=0, **kw),
+        "plain": TMCoreGPU(coarse, members=members, dt=dt_c, precision=abi.TMC_FP32, diag_every=0, **kw),
+        "plain_finer": TMCoreGPU(mid, members=members, dt=dt_m, precision=abi.TMC_FP32, diag_every=0, **kw),
+    }
+    truth = []  # per member: list of (gd, u) on the coarse mesh at the sample times
+    for k in range(members):
+        gd, u, ghs = cases.jet_bumps(fine, seed=seed0 + k)
+        for name, cg in (("closure", cg_c), ("closure_stage1", cg_c), ("plain", cg_c), ("plain_finer", cg_m)):
+            gd0, u0, _ = cg(gd=gd, u=u)
+            ghs0, _, _ = cg(gd=ghs)
+            runs[name].select_member(k)
+            runs[name].set_initial(gd0, u0, ghs0)
+        fm = TMCoreGPU(fine, dt=dt_f, precision=abi.TMC_FP64, diag_every=0, **kw)
+        fm.set_initial(gd, u, ghs)
+        tk = []
+        for s in range(samples):
+            fm.step(n_f)
+            gdf, _, uf = fm.get_state()
+            g_c, u_c, _ = cg_c(gd=gdf, u=uf)
+            tk.append((g_c, u_c))
+        fm.close()
+        truth.append(tk)
+    runs["closure"].set_closure(net)
+    runs["closure_stage1"].set_closure(net)
+    runs["closure_stage1"].set_closure_stages(False)
+    wa = coarse.vars["areaCell"]
+    we = coarse.vars["dvEdge"] * coarse.vars["dcEdge"]
+    err = {name: {"h": [], "u": []} for name in runs}
+    ms = {name: 0.0 for name in runs}
+    for s in range(samples):
+        for name, r in runs.items():
+            t, _, _, _ = r.time_steps(n_m if name == "plain_finer" else n_c, total=True, flux=False)
+            ms[name] += t
+            st = _member_states(r, members)
+            if name == "plain_finer":
+                st = [cg_mc(gd=gd, u=u)[:2] for gd, u in st]
+            eh = np.mean([_rel_l2(st[k][0], truth[k][s][0], wa) for k in range(members)])
+            eu = np.mean([_rel_l2(st[k][1], truth[k][s][1], we) for k in range(members)])
+            err[name]["h"].append(float(eh))
+            err[name]["u"].append(float(eu))
+        if log:
+            log(f"day {(s + 1) * total / samples / DAY:.2f}: " +
+                ", ".join(f"{n} h {err[n]['h'][-1]:.3e} u {err[n]['u'][-1]:.3e}" for n in runs))
+    timed_out = runs["closure"].closure_status() or runs["closure_stage1"].closure_status()
+    for r in runs.values():
+        r.close()
+    for c in (cg_c, cg_m, cg_mc):
+        c.close()
+    return {
+        "fine_level": fine_level, "coarse_level": coarse_level, "members": members, "days": days,
+        "times_days": [(s + 1) * total / samples / DAY for s in range(samples)],
+        "error": err,
+        "device_s_per_day": {n: ms[n] / 1e3 / days for n in runs},
+        "closure_timed_out": timed_out,
+    }
+
+
 class FallbackMonitor:
     """Per-member invariant-drift fallback: every `every` steps, a member whose
     relative drift of total energy (or mass) since its start exceeds `tol`
@@ -154,6 +249,10 @@ def main():
     ap.add_argument("--steps", type=int, default=1500)
     ap.add_argument("--members", type=int, default=256)
     ap.add_argument("--ens-days", type=float, default=1.0)
+    ap.add_argument("--every-stage", action="store_true",
+                    help="run the network in every stage (default: stage 1, its output held for stages 2-4)")
+    ap.add_argument("--eval-members", type=int, default=16, help="held-out seeds of the comparison (0: skip)")
+    ap.add_argument("--eval-days", type=float, default=5.0)
     ap.add_argument("--out", default=None, help="save the trained network (.npz)")
     a = ap.parse_args()
     t0 = time.time()
@@ -174,18 +273,24 @@ def main():
         ens.select_member(m)
         ens.set_initial(gd, u, ghs)
     ens.set_closure(net)
+    ens.set_closure_stages(a.every_stage)
     mon = FallbackMonitor(ens, a.members)
     nsteps = int(round(a.ens_days * DAY / dt))
     t0 = time.time()
     mon.step(nsteps)
     ens.synchronize()
     t_ens = time.time() - t0
+    fallbacks, timed_out = len(mon.fallbacks), ens.closure_status()
+    ens.close()
+    comparison = (evaluate(net, a.fine_level, a.coarse_level, members=a.eval_members, days=a.eval_days)
+                  if a.eval_members > 0 else None)
     print(json.dumps({
         "training_samples": int(len(Y)), "data_s": t_data, "train_s": t_train,
         "loss_first": float(losses[0]), "loss_last": float(np.mean(losses[-20:])),
         "ensemble": {"members": a.members, "level": a.coarse_level, "steps": nsteps, "wall_s": t_ens,
                      "member_days_per_s": a.members * nsteps * dt / DAY / t_ens,
-                     "fallbacks": len(mon.fallbacks), "closure_timed_out": ens.closure_status()},
+                     "every_stage": a.every_stage, "fallbacks": fallbacks, "closure_timed_out": timed_out},
+        "comparison": comparison,
     }))
 
 

@@ -105,6 +105,8 @@ struct tmc_handle {
   tmc::mlp::Net closure_net{};
   int* d_member_on = nullptr;
   int* d_closure_err = nullptr;
+  bool closure_every_stage = true;
+  float* d_closure_dq = nullptr;  // the held correction (closure in stage 1 only)
   int sms = 148;
   double* d_hist = nullptr;    // history outputs on cells (5 x nCells)
   cudaStream_t cst = nullptr;  // host-copy stream of tmc_time_integrate
@@ -357,7 +359,7 @@ struct Engine : EngineBase {
       mark(P_PV);
       launch_edge_pv<T>(M, O, s, b[P_PV], h->st);
       if (O.pv_scheme == 2) launch_cons_apvm<T>(M, O, s, h->P, h->d_diag, b[P_VERTEX], h->st);
-      launch_closure_pass(s);
+      launch_closure_pass(s, k);
       mark(P_PV);
       mark(P_FLUX);
       launch_edge_flux<T>(M, O, s, rk, h->P, b[P_FLUX], h->st);
@@ -371,10 +373,12 @@ struct Engine : EngineBase {
   }
 
   // the learned closure on this stage's pv_edge (FP32 path)
-  void launch_closure_pass(const StageIO<T>& s) {
+  // (in every stage, or in stage 1 with its output held for stages 2-4)
+  void launch_closure_pass(const StageIO<T>& s, int stage) {
     if constexpr (std::is_same<T, float>::value) {
       if (h->closure) {
-        ClosureArgs a{&h->closure_net, h->d_member_on, h->d_closure_err, h->sms};
+        const int mode = h->closure_every_stage ? 0 : (stage == 1 ? 1 : 2);
+        ClosureArgs a{&h->closure_net, h->d_member_on, h->d_closure_err, h->sms, h->d_closure_dq, mode};
         launch_closure(h->M, s, a, h->st);
       }
     }
@@ -1367,6 +1371,22 @@ int tmc_set_closure(tmc_handle* h, const tmc_mlp* net) {
   h->closure = net;
   if (net) h->closure_net = tmc_mlp_net(net);
   h->O.need_pv_c = net ? 1 : 0;
+  if (h->g_step) cudaGraphExecDestroy(h->g_step);
+  if (h->g_step_diag) cudaGraphExecDestroy(h->g_step_diag);
+  h->g_step = h->g_step_diag = nullptr;
+  return TMC_OK;
+}
+
+int tmc_set_closure_stages(tmc_handle* h, int32_t every_stage) {
+  TMC_REQUIRE_SWM(h);
+  if (h->p.precision != TMC_FP32 || h->generic)
+    return h->fail(TMC_E_UNSUP, "the learned closure runs in the FP32 CRK4 shallow-water step");
+  if (sync(h, "tmc_set_closure_stages")) return TMC_E_CUDA;
+  h->closure_every_stage = every_stage != 0;
+  if (!h->closure_every_stage && !h->d_closure_dq) {
+    h->d_closure_dq = h->dalloc<float>((size_t)h->members * h->M.ne);
+    if (!h->d_closure_dq) return h->cuda_check("tmc_set_closure_stages: allocation");
+  }
   if (h->g_step) cudaGraphExecDestroy(h->g_step);
   if (h->g_step_diag) cudaGraphExecDestroy(h->g_step_diag);
   h->g_step = h->g_step_diag = nullptr;

@@ -1,17 +1,33 @@
 // Coarse-graining of a fine-mesh state onto a coarser mesh (training data
-// of the learned closure): area-weighted aggregation of cell values over the
-// fine cells whose centres lie in each coarse Voronoi cell, and edge-flux
-// averaging of the normal velocity (the fine normal fluxes u dvEdge across
-// the boundary between two aggregates, divided by the coarse dvEdge); edge
-// scalars (pv on edges) are dvEdge-weighted means over the same fine edges.
+// and the truth of the learned closure's held-out comparison).
 //
-// The maps are built on the host (nearest coarse generator by a greedy walk
-// over the coarse cellsOnCell graph, which ends at the nearest generator on a
-// Voronoi mesh) and applied by gather kernels in CSR form.
+// Cells: area-weighted aggregation over kites.  Each fine cell is cut into
+// its kites (cell centre, one vertex and the two half-edges between them;
+// kiteAreasOnVertex), and each kite goes to the coarse cell whose generator
+// is nearest the kite's centre point (the midpoint of the fine cell centre
+// and the vertex).  A kite within a small tie band of two coarse generators
+// (refined icosahedral meshes put many on coarse Voronoi boundaries) is split
+// equally between them.  The coarse value is the kite-area-weighted mean.
+//
+// Edges: strip averaging of the fine velocity's component along the coarse
+// normal.  For a coarse edge, the fine edges whose midpoints lie within
+// 0.75 fine dcEdge of the coarse Voronoi edge's great circle, between its two
+// vertices, each give the full velocity u n + v t (v the TRiSK tangential
+// velocity, sum of weightsOnEdge u over edgesOnEdge) dotted with the coarse
+// normal; the coarse u is their mean.  Edge scalars (pv on edges) are means
+// over the same fine edges.  Both maps are linear and stored as CSR rows over
+// the fine arrays; gather kernels apply them.
+//
+// The fine edges that can lie in a coarse edge's strip are found through the
+// cell map (each fine cell's nearest coarse generator, by a greedy walk over
+// the coarse cellsOnCell graph, which ends at the nearest generator on a
+// Voronoi mesh): the fine edges touching either coarse cell's fine cells.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "tmcore_gpu.h"
@@ -30,7 +46,70 @@ __global__ void k_gather_csr(int n, const int32_t* start, const int32_t* idx, co
 struct Csr {
   std::vector<int32_t> start, idx;
   std::vector<double> w;
+  // append one row from (column, weight) pairs, merging repeated columns
+  void add_row(std::vector<std::pair<int, double>>& row) {
+    if (start.empty()) start.push_back(0);
+    std::sort(row.begin(), row.end(), [](const std::pair<int, double>& a, const std::pair<int, double>& b) {
+      return a.first < b.first;
+    });
+    for (size_t i = 0; i < row.size();) {
+      double s = 0.0;
+      size_t j = i;
+      for (; j < row.size() && row[j].first == row[i].first; ++j) s += row[j].second;
+      idx.push_back(row[i].first);
+      w.push_back(s);
+      i = j;
+    }
+    start.push_back((int32_t)idx.size());
+  }
 };
+
+struct V3 {
+  double x, y, z;
+};
+inline V3 operator+(V3 a, V3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+inline V3 operator-(V3 a, V3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline V3 operator*(double s, V3 a) { return {s * a.x, s * a.y, s * a.z}; }
+inline double dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline V3 cross(V3 a, V3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+inline V3 unit(V3 a) { return (1.0 / std::sqrt(dot(a, a))) * a; }
+
+inline V3 cell_pt(const tmc_mesh_desc& m, int i) { return unit({m.xCell[i], m.yCell[i], m.zCell[i]}); }
+inline V3 edge_pt(const tmc_mesh_desc& m, int e) { return unit({m.xEdge[e], m.yEdge[e], m.zEdge[e]}); }
+inline V3 vert_pt(const tmc_mesh_desc& m, int v) { return unit({m.xVertex[v], m.yVertex[v], m.zVertex[v]}); }
+
+// unit normal of edge e (from cellsOnEdge 1 to 2) in the tangent plane at the edge
+V3 edge_normal(const tmc_mesh_desc& m, int e) {
+  const V3 r = edge_pt(m, e);
+  V3 d = cell_pt(m, m.cellsOnEdge[(size_t)e * 2 + 1] - 1) - cell_pt(m, m.cellsOnEdge[(size_t)e * 2] - 1);
+  d = d - dot(d, r) * r;
+  return unit(d);
+}
+
+// nearest coarse generator of the unit vector p, by a greedy walk from g
+int walk_nearest(const tmc_mesh_desc& c, const V3& p, int g) {
+  double best = dot(p, cell_pt(c, g));
+  for (int it = 0; it < 4 * c.nCells; ++it) {
+    int nb = -1;
+    double nbv = best;
+    for (int j = 0; j < c.nEdgesOnCell[g]; ++j) {
+      const int k = c.cellsOnCell[(size_t)g * c.maxEdges + j] - 1;
+      if (k < 0) continue;
+      const double v = dot(p, cell_pt(c, k));
+      if (v > nbv) {
+        nbv = v;
+        nb = k;
+      }
+    }
+    if (nb < 0) break;
+    g = nb;
+    best = nbv;
+  }
+  return g;
+}
+
+constexpr double kTieBand = 0.1;     // kites within 0.1 fine dcEdge of two generators are split
+constexpr double kStripHalf = 0.75;  // strip half-width in fine dcEdge
 
 }  // namespace
 
@@ -43,6 +122,7 @@ struct tmc_coarsen {
           *p_idx = nullptr;
   double *c_w = nullptr, *e_w = nullptr, *p_w = nullptr;
   double *fin = nullptr, *fout = nullptr;
+  Csr host[3];  // cells, u, edge scalars
   std::string err;
 };
 
@@ -56,34 +136,119 @@ X* upload(const std::vector<X>& v) {
   return d;
 }
 
-// nearest coarse generator of each fine cell
-std::vector<int> nearest_cells(const tmc_mesh_desc& f, const tmc_mesh_desc& c) {
-  std::vector<int> map(f.nCells, 0);
-  int g = 0;
-  for (int i = 0; i < f.nCells; ++i) {
-    const double px = f.xCell[i], py = f.yCell[i], pz = f.zCell[i];
-    auto dot = [&](int k) { return px * c.xCell[k] + py * c.yCell[k] + pz * c.zCell[k]; };
-    double best = dot(g);
-    for (int it = 0; it < 4 * c.nCells; ++it) {
-      int nb = -1;
-      double nbv = best;
-      const int n = c.nEdgesOnCell[g];
-      for (int j = 0; j < n; ++j) {
-        const int k = c.cellsOnCell[(size_t)g * c.maxEdges + j] - 1;
+// kite-area-weighted cell aggregation
+Csr cell_rows(const tmc_mesh_desc& f, const tmc_mesh_desc& c, const std::vector<int>& map, double R) {
+  std::vector<std::vector<std::pair<int, double>>> rows(c.nCells);
+  const int deg = f.vertexDegree;
+  for (int v = 0; v < f.nVertices; ++v) {
+    const V3 pv = vert_pt(f, v);
+    for (int j = 0; j < deg; ++j) {
+      const int i = f.cellsOnVertex[(size_t)v * deg + j] - 1;
+      if (i < 0) continue;
+      const double a = f.kiteAreasOnVertex[(size_t)v * deg + j];
+      const V3 p = unit(cell_pt(f, i) + pv);
+      const int g = walk_nearest(c, p, map[i]);
+      // the nearest neighbouring generator, for the tie band
+      const double ag = std::acos(std::min(1.0, dot(p, cell_pt(c, g))));
+      int g2 = -1;
+      double a2 = 1e300;
+      for (int q = 0; q < c.nEdgesOnCell[g]; ++q) {
+        const int k = c.cellsOnCell[(size_t)g * c.maxEdges + q] - 1;
         if (k < 0) continue;
-        const double v = dot(k);
-        if (v > nbv) {
-          nbv = v;
-          nb = k;
+        const double ak = std::acos(std::min(1.0, dot(p, cell_pt(c, k))));
+        if (ak < a2) {
+          a2 = ak;
+          g2 = k;
         }
       }
-      if (nb < 0) break;
-      g = nb;
-      best = nbv;
+      int ce = -1;  // the fine edge between this kite's cell and the next, for its dcEdge
+      for (int q = 0; q < f.nEdgesOnCell[i] && ce < 0; ++q) {
+        const int e = f.edgesOnCell[(size_t)i * f.maxEdges + q] - 1;
+        if (e >= 0 && (f.verticesOnEdge[(size_t)e * 2] - 1 == v || f.verticesOnEdge[(size_t)e * 2 + 1] - 1 == v))
+          ce = e;
+      }
+      const double band = kTieBand * (ce >= 0 ? f.dcEdge[ce] / R : 0.0);
+      if (g2 >= 0 && a2 - ag <= band) {
+        rows[g].push_back({i, 0.5 * a});
+        rows[g2].push_back({i, 0.5 * a});
+      } else {
+        rows[g].push_back({i, a});
+      }
     }
-    map[i] = g;
   }
-  return map;
+  Csr out;
+  for (auto& r : rows) {
+    double s = 0.0;
+    for (auto& pr : r) s += pr.second;
+    for (auto& pr : r) pr.second /= s;
+    out.add_row(r);
+  }
+  return out;
+}
+
+// strip averaging of the velocity's component along each coarse normal (ce),
+// and the plain mean over the same fine edges (cp)
+long long edge_rows(const tmc_mesh_desc& f, const tmc_mesh_desc& c, const std::vector<int>& map, double R, Csr& ce,
+                    Csr& cp) {
+  std::vector<std::vector<int>> by_cell(c.nCells);  // fine edges touching each aggregate
+  for (int e = 0; e < f.nEdges; ++e) {
+    const int a = map[f.cellsOnEdge[(size_t)e * 2] - 1];
+    const int b = f.cellsOnEdge[(size_t)e * 2 + 1] > 0 ? map[f.cellsOnEdge[(size_t)e * 2 + 1] - 1] : a;
+    by_cell[a].push_back(e);
+    if (b != a) by_cell[b].push_back(e);
+  }
+  std::vector<V3> nf(f.nEdges), tf(f.nEdges), xf(f.nEdges);
+  for (int e = 0; e < f.nEdges; ++e) {
+    xf[e] = edge_pt(f, e);
+    nf[e] = edge_normal(f, e);
+    tf[e] = cross(xf[e], nf[e]);
+  }
+  std::vector<int> stamp(f.nEdges, -1);
+  long long unmatched = 0;
+  std::vector<std::pair<int, double>> ru, rp;
+  std::vector<int> sel;
+  for (int k = 0; k < c.nEdges; ++k) {
+    const int A = c.cellsOnEdge[(size_t)k * 2] - 1, B = c.cellsOnEdge[(size_t)k * 2 + 1] - 1;
+    const V3 P = vert_pt(c, c.verticesOnEdge[(size_t)k * 2] - 1), Q = vert_pt(c, c.verticesOnEdge[(size_t)k * 2 + 1] - 1);
+    const V3 gc = unit(cross(P, Q));
+    const double arc = std::atan2(std::sqrt(dot(cross(P, Q), cross(P, Q))), dot(P, Q));
+    const V3 nk = edge_normal(c, k);
+    sel.clear();
+    for (double widen = 1.0; sel.empty() && widen <= 4.0; widen *= 2.0) {
+      for (int side = 0; side < 2; ++side) {
+        const int agg = side == 0 ? A : B;
+        if (agg < 0) continue;
+        for (int e : by_cell[agg]) {
+          if (stamp[e] == k * 4 + (int)widen) continue;
+          stamp[e] = k * 4 + (int)widen;
+          const V3& X = xf[e];
+          if (std::fabs(dot(X, gc)) >= kStripHalf * widen * f.dcEdge[e] / R) continue;
+          const double s = std::atan2(dot(cross(P, X), gc), dot(P, X)) / arc;
+          if (s < 0.0 || s > 1.0) continue;
+          sel.push_back(e);
+        }
+      }
+    }
+    ru.clear();
+    rp.clear();
+    if (sel.empty()) {
+      ++unmatched;
+    } else {
+      const double inv = 1.0 / (double)sel.size();
+      for (int e : sel) {
+        ru.push_back({e, inv * dot(nf[e], nk)});
+        const double wt = inv * dot(tf[e], nk);
+        for (int j = 0; j < f.nEdgesOnEdge[e]; ++j) {
+          const int e2 = f.edgesOnEdge[(size_t)e * f.maxEdges2 + j] - 1;
+          if (e2 >= 0) ru.push_back({e2, wt * f.weightsOnEdge[(size_t)e * f.maxEdges2 + j]});
+        }
+        rp.push_back({e, inv});
+      }
+    }
+    ce.add_row(ru);
+    cp.add_row(rp);
+  }
+  return unmatched;
 }
 
 }  // namespace
@@ -96,80 +261,33 @@ int tmc_coarsen_create(const tmc_mesh_desc* fine, const tmc_mesh_desc* coarse, i
   auto* C = new tmc_coarsen();
   *out = C;
   const tmc_mesh_desc &f = *fine, &c = *coarse;
-  if (!f.xCell || !f.yCell || !f.zCell || !f.areaCell || !f.cellsOnEdge || !f.dvEdge || !c.xCell || !c.yCell ||
-      !c.zCell || !c.nEdgesOnCell || !c.cellsOnCell || !c.edgesOnCell || !c.cellsOnEdge || !c.dvEdge) {
+  if (!f.xCell || !f.yCell || !f.zCell || !f.cellsOnEdge || !f.dcEdge || !f.xEdge || !f.yEdge || !f.zEdge ||
+      !f.xVertex || !f.yVertex || !f.zVertex || !f.cellsOnVertex || !f.kiteAreasOnVertex || !f.nEdgesOnCell ||
+      !f.edgesOnCell || !f.verticesOnEdge || !f.nEdgesOnEdge || !f.edgesOnEdge || !f.weightsOnEdge || !c.xCell ||
+      !c.yCell || !c.zCell || !c.xVertex || !c.yVertex || !c.zVertex || !c.xEdge || !c.yEdge || !c.zEdge ||
+      !c.nEdgesOnCell || !c.cellsOnCell || !c.cellsOnEdge || !c.verticesOnEdge) {
     C->err = "tmc_coarsen_create: missing mesh arrays";
     return TMC_E_ARG;
-  }
-  if (cudaSetDevice(device) != cudaSuccess) {
-    cudaGetLastError();
-    C->err = "cudaSetDevice failed (no CUDA device?)";
-    return TMC_E_CUDA;
   }
   C->ncf = f.nCells;
   C->nef = f.nEdges;
   C->ncc = c.nCells;
   C->nec = c.nEdges;
-  C->cell_map = nearest_cells(f, c);
-  const std::vector<int>& map = C->cell_map;
-  // cells: area-weighted mean over the fine cells of each coarse cell
-  Csr cc;
-  {
-    std::vector<double> asum(c.nCells, 0.0);
-    std::vector<int> cnt(c.nCells, 0);
-    for (int i = 0; i < f.nCells; ++i) {
-      asum[map[i]] += f.areaCell[i];
-      cnt[map[i]]++;
-    }
-    cc.start.assign(c.nCells + 1, 0);
-    for (int k = 0; k < c.nCells; ++k) cc.start[k + 1] = cc.start[k] + cnt[k];
-    cc.idx.resize(f.nCells);
-    cc.w.resize(f.nCells);
-    std::vector<int> fill(c.nCells, 0);
-    for (int i = 0; i < f.nCells; ++i) {
-      const int k = map[i], pos = cc.start[k] + fill[k]++;
-      cc.idx[pos] = i;
-      cc.w[pos] = f.areaCell[i] / asum[k];
-    }
-  }
-  // edges: fine edges whose two cells fall in two neighbouring coarse cells
+  const double R = std::sqrt(f.xCell[0] * f.xCell[0] + f.yCell[0] * f.yCell[0] + f.zCell[0] * f.zCell[0]);
+  std::vector<int>& map = C->cell_map;
+  map.assign(f.nCells, 0);
+  for (int i = 0, g = 0; i < f.nCells; ++i) g = map[i] = walk_nearest(c, cell_pt(f, i), g);
+  const Csr cc = cell_rows(f, c, map, R);
   Csr ce, cp;
-  {
-    std::vector<std::vector<std::pair<int, double>>> lu(c.nEdges), lp(c.nEdges);
-    for (int e = 0; e < f.nEdges; ++e) {
-      const int a = map[f.cellsOnEdge[(size_t)e * 2] - 1], b = map[f.cellsOnEdge[(size_t)e * 2 + 1] - 1];
-      if (a == b) continue;
-      int hit = -1;
-      for (int j = 0; j < c.nEdgesOnCell[a]; ++j) {
-        const int k = c.edgesOnCell[(size_t)a * c.maxEdges + j] - 1;
-        const int k1 = c.cellsOnEdge[(size_t)k * 2] - 1, k2 = c.cellsOnEdge[(size_t)k * 2 + 1] - 1;
-        if ((k1 == a && k2 == b) || (k1 == b && k2 == a)) {
-          hit = k;
-          break;
-        }
-      }
-      if (hit < 0) continue;
-      const double s = (c.cellsOnEdge[(size_t)hit * 2] - 1 == a) ? 1.0 : -1.0;
-      lu[hit].push_back({e, s * f.dvEdge[e] / c.dvEdge[hit]});
-      lp[hit].push_back({e, f.dvEdge[e]});
-    }
-    ce.start.assign(c.nEdges + 1, 0);
-    cp.start.assign(c.nEdges + 1, 0);
-    for (int k = 0; k < c.nEdges; ++k) {
-      if (lu[k].empty()) C->unmatched++;
-      ce.start[k + 1] = ce.start[k] + (int)lu[k].size();
-      cp.start[k + 1] = cp.start[k] + (int)lp[k].size();
-      double wsum = 0.0;
-      for (auto& pr : lp[k]) wsum += pr.second;
-      for (auto& pr : lu[k]) {
-        ce.idx.push_back(pr.first);
-        ce.w.push_back(pr.second);
-      }
-      for (auto& pr : lp[k]) {
-        cp.idx.push_back(pr.first);
-        cp.w.push_back(pr.second / wsum);
-      }
-    }
+  C->unmatched = edge_rows(f, c, map, R, ce, cp);
+  C->host[0] = cc;
+  C->host[1] = ce;
+  C->host[2] = cp;
+  if (device < 0) return TMC_OK;  // maps only
+  if (cudaSetDevice(device) != cudaSuccess) {
+    cudaGetLastError();
+    C->err = "cudaSetDevice failed (no CUDA device?)";
+    return TMC_E_CUDA;
   }
   cudaStreamCreateWithFlags(&C->st, cudaStreamNonBlocking);
   C->c_start = upload(cc.start);
@@ -204,7 +322,11 @@ static int coarsen_one(tmc_coarsen* C, const double* src, int nsrc, double* dst,
 
 int tmc_coarsen_apply(tmc_coarsen* C, const double* fine_gd, const double* fine_u, const double* fine_pv_edge,
                       double* coarse_gd, double* coarse_u, double* coarse_pv_edge) {
-  if (!C || !C->c_w) return TMC_E_ARG;
+  if (!C) return TMC_E_ARG;
+  if (!C->c_w) {
+    C->err = "tmc_coarsen_apply: a coarsener created with device < 0 holds the maps only";
+    return TMC_E_UNSUP;
+  }
   int rc;
   if (fine_gd && coarse_gd &&
       (rc = coarsen_one(C, fine_gd, C->ncf, coarse_gd, C->ncc, C->c_start, C->c_idx, C->c_w)))
@@ -214,6 +336,16 @@ int tmc_coarsen_apply(tmc_coarsen* C, const double* fine_gd, const double* fine_
   if (fine_pv_edge && coarse_pv_edge &&
       (rc = coarsen_one(C, fine_pv_edge, C->nef, coarse_pv_edge, C->nec, C->p_start, C->p_idx, C->p_w)))
     return rc;
+  return TMC_OK;
+}
+
+int tmc_coarsen_rows(const tmc_coarsen* C, int32_t which, int64_t* nnz, int32_t* start, int32_t* idx, double* w) {
+  if (!C || !nnz || which < 0 || which > 2) return TMC_E_ARG;
+  const Csr& r = C->host[which];
+  *nnz = (int64_t)r.idx.size();
+  if (start) std::copy(r.start.begin(), r.start.end(), start);
+  if (idx) std::copy(r.idx.begin(), r.idx.end(), idx);
+  if (w) std::copy(r.w.begin(), r.w.end(), w);
   return TMC_OK;
 }
 
@@ -235,7 +367,8 @@ int tmc_coarsen_destroy(tmc_coarsen* C) {
   if (!C) return TMC_OK;
   if (C->st) cudaStreamSynchronize(C->st);
   void* p[] = {C->c_start, C->c_idx, C->c_w, C->e_start, C->e_idx, C->e_w, C->p_start, C->p_idx, C->p_w, C->fin, C->fout};
-  for (void* q : p) cudaFree(q);
+  for (void* q : p)
+    if (q) cudaFree(q);
   if (C->st) cudaStreamDestroy(C->st);
   delete C;
   return TMC_OK;

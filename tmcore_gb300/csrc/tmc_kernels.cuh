@@ -364,6 +364,8 @@ struct ClosureArgs {
   const int* member_on;    // [members] 1: apply
   int* err;
   int sms;
+  float* dq;               // held correction [members][edge stride] (modes 1 and 2)
+  int mode;                // 0: run the network; 1: run it and hold its output in dq; 2: add dq only
 };
 void launch_closure(const DevMesh& M, const StageIO<float>& S, const ClosureArgs& a, cudaStream_t st);
 // the features (and pv_edge) of every edge of member m, into feat[ne][24] / pv[ne]

@@ -94,6 +94,7 @@ struct ClosureSrc {
   DevMesh M;
   StageIO<float> S;
   const int* on;
+  float* dq;  // non-null: the correction is also held here (0 for members switched off)
   int members, tpm;
   __device__ bool where(long long i, int& m, int& e) const {
     const int tile = (int)(i >> 7), t = (int)(i & (kTile - 1));
@@ -109,12 +110,21 @@ struct ClosureSrc {
   }
   __device__ void output(long long i, float r) const {
     int m, e;
-    if (where(i, m, e) && on[m]) {
-      float* pe = S.pv_e + (long long)m * S.mse + e;
-      *pe = *pe + r;
-    }
+    if (!where(i, m, e)) return;
+    const long long k = (long long)m * S.mse + e;
+    const float v = on[m] ? r : 0.f;
+    if (dq) dq[k] = v;
+    if (on[m]) S.pv_e[k] = S.pv_e[k] + v;
   }
 };
+
+// the held correction of stage 1 added to pv_edge in the later stages
+__global__ void k_closure_hold(float* pv_e, const float* dq, int ne, long long mse) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  const long long k = (long long)blockIdx.y * mse + e;  // member blockIdx.y
+  pv_e[k] += dq[k];
+}
 
 __global__ void __launch_bounds__(kTcThreads) k_closure(Net net, ClosureSrc src, long long ntiles, int* err) {
   extern __shared__ __align__(128) uint8_t smem[];
@@ -349,7 +359,11 @@ namespace tmc {
 void launch_closure(const DevMesh& M, const StageIO<float>& S, const ClosureArgs& a, cudaStream_t st) {
   const int members = S.members > 1 ? S.members : 1;
   const int tpm = (M.ne + kTile - 1) / kTile;
-  ClosureSrc src{M, S, a.member_on, members, tpm};
+  if (a.mode == 2) {
+    k_closure_hold<<<dim3((M.ne + 255) / 256, members), 256, 0, st>>>(S.pv_e, a.dq, M.ne, S.mse);
+    return;
+  }
+  ClosureSrc src{M, S, a.member_on, a.mode == 1 ? a.dq : nullptr, members, tpm};
   const long long ntiles = (long long)tpm * members;
   const int grid = (int)std::min<long long>(ntiles, (long long)a.sms * 8);
   static bool attr = false;

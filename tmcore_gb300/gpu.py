@@ -154,6 +154,11 @@ class TMCoreGPU:
         self._closure = net
         self._chk(self.lib.tmc_set_closure(self.h, None if net is None else net.n))
 
+    def set_closure_stages(self, every_stage: bool):
+        """True: the network runs in every stage; False: in stage 1, its output
+        held for stages 2-4."""
+        self._chk(self.lib.tmc_set_closure_stages(self.h, 1 if every_stage else 0))
+
     def set_member_closure(self, member: int, on: bool):
         self._chk(self.lib.tmc_set_member_closure(self.h, int(member), 1 if on else 0))
 
@@ -380,7 +385,8 @@ class ClosureMLP:
 
 
 class Coarsener:
-    """Coarse-graining of fine-mesh fields onto a coarser mesh (tmc_coarsen_*)."""
+    """Coarse-graining of fine-mesh fields onto a coarser mesh (tmc_coarsen_*);
+    device < 0 builds the maps only (``rows``), without CUDA."""
 
     def __init__(self, fine, coarse, device: int = 0):
         self.lib = _lib.gpu()
@@ -394,6 +400,18 @@ class Coarsener:
             msg = self.lib.tmc_coarsen_last_error(c).decode() if c.value else "tmc_coarsen_create failed"
             self.close()
             raise TMCError(rc, msg)
+
+    def rows(self, which: int):
+        """Map `which` (0 cells, 1 normal velocity, 2 edge scalars) as CSR
+        arrays (start, idx, w) over the fine array."""
+        n = ctypes.c_int64()
+        self.lib.tmc_coarsen_rows(self.c, int(which), ctypes.byref(n), None, None, None)
+        rows = self.coarse.nCells if which == 0 else self.coarse.nEdges
+        start, idx, w = np.empty(rows + 1, np.int32), np.empty(n.value, np.int32), np.empty(n.value)
+        rc = self.lib.tmc_coarsen_rows(self.c, int(which), ctypes.byref(n), _ptr(start), _ptr(idx), _ptr(w))
+        if rc != 0:
+            raise TMCError(rc, "tmc_coarsen_rows")
+        return start, idx, w
 
     def unmatched(self) -> int:
         n = ctypes.c_int64()
