@@ -45,6 +45,8 @@ def parse():
     ap.add_argument("--tracers", type=int, default=4)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison run")
+    ap.add_argument("--error-days", type=float, default=1.0,
+                    help="simulated days of the FP32-vs-FP64 per-field error comparison (0: skip)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-steps", type=int, default=1)
@@ -486,6 +488,7 @@ def main():
     gpu.set_initial(gd, u, ghs)
     if args.tracers:
         gpu.set_tracers(qgd)
+    d0_mass = gpu.diag()[0]
     tuned = gpu.autotune(steps=3) if not args.no_autotune else None
     gpu.step(args.warmup)
     gpu.synchronize()
@@ -548,6 +551,31 @@ def main():
             "rel_l2": float(np.sqrt(np.sum(area * (h32 - h64) ** 2) / np.sum(area * h64 ** 2))),
             "u_rel_max": float(np.max(np.abs(u32 - u64)) / np.max(np.abs(u64))),
             "after_steps": args.warmup + args.steps}
+        if args.error_days > 0:
+            # the FP32 path against the FP64 path after whole simulated days, per field
+            n = int(round(args.error_days * DAY / args.dt))
+            g64.step(max(0, n - args.warmup - args.steps))
+            g32 = TMCoreGPU(m, **gpu_params(args, abi.TMC_FP32), device=local)
+            g32.set_initial(gd, u, ghs)
+            if args.tracers:
+                g32.set_tracers(qgd)
+            g32.step(n)
+            a32, _, v32 = g32.get_state()
+            a64, _, v64 = g64.get_state()
+            h32, h64 = a32 / 9.80616, a64 / 9.80616
+            el = m.dvEdge * m.dcEdge
+            err = {"steps": n, "days": n * args.dt / DAY,
+                   "h_rel_max": float(np.max(np.abs(h32 - h64)) / np.max(np.abs(h64))),
+                   "h_rel_l2": float(np.sqrt(np.sum(area * (h32 - h64) ** 2) / np.sum(area * h64 ** 2))),
+                   "u_rel_max": float(np.max(np.abs(v32 - v64)) / np.max(np.abs(v64))),
+                   "u_rel_l2": float(np.sqrt(np.sum(el * (v32 - v64) ** 2) / np.sum(el * v64 ** 2)))}
+            if args.tracers:
+                q32, q64 = g32.get_tracers() / a32[None, :], g64.get_tracers() / a64[None, :]
+                err["tracer_rel_max"] = [float(np.max(np.abs(q32[k] - q64[k])) / np.max(np.abs(q64[k])))
+                                         for k in range(args.tracers)]
+            err["mass_drift_fp32"] = float((g32.diag()[0] - d0_mass) / d0_mass)
+            extra["error_fp32_vs_fp64"] = err
+            g32.close()
         g64.close()
     extra["invariants_fp32"] = {"mass": d32[0], "energy": d32[1], "enstrophy": d32[2], "abs_vorticity": d32[3],
                                 "beta": d32[4]}
