@@ -27,6 +27,17 @@
 #ifndef TMC_FINAL_MIN_BLOCKS
 #define TMC_FINAL_MIN_BLOCKS 4
 #endif
+// The same for the single-model cell pass (blocks of kCellBlock) and final
+// edge update (blocks of up to kMaxBlock).  Level 9: the cell pass takes 139 us
+// at 3 (80 registers) and 165 us at 4; the final pass 122 us at 2 (64
+// registers, no spill), 129 us with no minimum (64 registers, 4 bytes
+// spilled) and 176 us at 1 (120 registers).
+#ifndef TMC_CELL_SINGLE_MIN_BLOCKS
+#define TMC_CELL_SINGLE_MIN_BLOCKS 3
+#endif
+#ifndef TMC_FINAL_SINGLE_MIN_BLOCKS
+#define TMC_FINAL_SINGLE_MIN_BLOCKS 2
+#endif
 
 #include <type_traits>
 
@@ -1110,7 +1121,7 @@ __global__ void __launch_bounds__(kMaxBlock) k_final_cells(DevMesh M, ModelOpt O
 // energy of the new state (tmcore_swm_mod.F90:229) for the next step's
 // invariants.
 template <class T, bool kB>
-__global__ void __launch_bounds__(kB ? kMemberBlock : kMaxBlock, kB ? TMC_FINAL_MIN_BLOCKS : 0)
+__global__ void __launch_bounds__(kB ? kMemberBlock : kMaxBlock, kB ? TMC_FINAL_MIN_BLOCKS : TMC_FINAL_SINGLE_MIN_BLOCKS)
     k_final_edges(DevMesh M, ModelOpt O, StageIO<T> S0, const double* diag0, Partials P0) {
   const StageIO<T> S = kB ? S0.at(blockIdx.y) : S0;
   const Partials P = kB ? P0.at(blockIdx.y) : P0;
@@ -1323,7 +1334,7 @@ __device__ __forceinline__ void cell_fast_body(const DevMesh& M, const StageIO<f
 }
 
 template <int NTR>
-__global__ void __launch_bounds__(kCellBlock, 3) k_cell_fast(DevMesh M, StageIO<float> S0, RKStage rk, Partials P0,
+__global__ void __launch_bounds__(kCellBlock, TMC_CELL_SINGLE_MIN_BLOCKS) k_cell_fast(DevMesh M, StageIO<float> S0, RKStage rk, Partials P0,
                                                          int diag) {
   cell_fast_body<NTR, false>(M, S0, rk, P0, diag);
 }
