@@ -259,7 +259,10 @@ int tmc_history_close(tmc_history* hw);
  * one independent branch per handle with cycle_seconds / dt steps (which must
  * be whole), so the handles' kernels run concurrently.  tmc_group_run is
  * asynchronous; later calls on a member handle are ordered after it.  The
- * handles must outlive the group and must not change their state size. */
+ * handles must outlive the group and must not change their state size.  The
+ * graph holds each handle's step as configured when the group was created
+ * (closure, closure stages, block sizes): after changing those, create the
+ * group again. */
 typedef struct tmc_group tmc_group;
 int tmc_group_create(tmc_handle* const* handles, int32_t n, double cycle_seconds, tmc_group** out);
 int tmc_group_run(tmc_group* g, int32_t cycles);
