@@ -80,7 +80,10 @@ typedef struct tmc_params {
   int32_t adv_wind;               /* 0: shallow-water model; adv model (tmcore_adv_mod.F90) with the
                                      prescribed wind 1 cosine-bell rotation, 2 deformation flow case 4 */
   int32_t members;                /* ensemble members sharing the mesh (FP32 shallow water, CRK4); 0 or 1: one */
-  int32_t reserved[4];
+  int32_t member_layout;          /* ensembles: 0 member-outermost arrays (every option), 1 member-innermost
+                                     (members a multiple of 32; pv_scheme 1 with apvm_weight 0, adv_order 2,
+                                     no tracers, no closure): one 128-byte line per neighbour gather of 32 members */
+  int32_t reserved[3];
 } tmc_params;
 
 typedef struct tmc_handle tmc_handle;

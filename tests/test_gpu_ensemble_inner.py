@@ -1,0 +1,169 @@
+"""Member-innermost ensembles (tmc_params.member_layout = 1): arrays
+[element][member], one warp per 32 members of an element.
+
+The kernels repeat the FP32 single-model expressions, but the compiler
+contracts multiplies and adds into FMAs differently in the two kernels, so
+FP32 fields differ in the last bit here and there; the gd tendency is a
+cancellation of large flux terms, which turns those bits into relative
+differences of about 1e-8 in gd after a few steps.  A member that read a
+wrong neighbour or another member's data would be off by 1e-3 or more.  The
+invariants come from compensated sums over another partition (FP32 terms for
+energy, enstrophy and absolute vorticity; FP64 gd for mass)."""
+import numpy as np
+import pytest
+
+from conftest import rel_max
+
+pytestmark = pytest.mark.gpu
+
+M = 32
+KW = dict(precision=1, pv_scheme=1, apvm_weight=0.0, adv_order=2)
+
+
+def _ics(mesh, n, seed0):
+    from tmcore_gb300 import cases
+
+    return [cases.jet_bumps(mesh, seed=seed0 + m) for m in range(n)]
+
+
+def _ensemble(mesh, ics, layout, **kw):
+    from tmcore_gb300.gpu import TMCoreGPU
+
+    ens = TMCoreGPU(mesh, members=len(ics), member_layout=layout, **KW, **kw)
+    for m, (gd, u, ghs) in enumerate(ics):
+        ens.select_member(m)
+        ens.set_initial(gd, u, ghs)
+    return ens
+
+
+def _single(mesh, ic, **kw):
+    from tmcore_gb300.gpu import TMCoreGPU
+
+    one = TMCoreGPU(mesh, **KW, **kw)
+    one.set_initial(*ic)
+    return one
+
+
+def test_members_match_single_runs_without_beta(mesh4):
+    kw = dict(dt=600.0, conserve_energy=0, diag_every=1)
+    ics = _ics(mesh4, M, 100)
+    ens = _ensemble(mesh4, ics, 1, **kw)
+    outer = _ensemble(mesh4, ics, 0, **kw)
+    ens.step(7)
+    outer.step(7)
+    for m in (0, 13, M - 1):
+        one = _single(mesh4, ics[m], **kw)
+        one.step(7)
+        ens.select_member(m)
+        outer.select_member(m)
+        ge, ie, ue = ens.get_state()
+        g1, i1, u1 = one.get_state()
+        go, io, _ = outer.get_state()
+        errs = (rel_max(ge, g1), rel_max(ie, i1), rel_max(ue, u1), rel_max(ge, go), rel_max(ie, io))
+        assert max(errs[0], errs[3]) < 1e-6 and max(errs[1], errs[2], errs[4]) < 1e-5, (m, errs)
+        pe, ve = ens.get_vertex()
+        p1, v1 = one.get_vertex()
+        assert rel_max(pe, p1) < 1e-5 and rel_max(ve, v1) < 1e-5, m
+        de, d1 = ens.diag(), one.diag()
+        assert abs(de[0] - d1[0]) <= 1e-13 * abs(d1[0]), (de[0], d1[0])  # mass: FP64 gd, conserved by both
+        assert abs(de[1] - d1[1]) <= 1e-8 * abs(d1[1]), (de[1], d1[1])   # energy
+        assert abs(de[2] - d1[2]) <= 1e-6 * abs(d1[2]), (de[2], d1[2])   # potential enstrophy
+        assert abs(de[3] - d1[3]) <= 1e-9 * 2 * 7.292e-5, (de[3], d1[3])  # absolute vorticity (mean of f + vor)
+        assert de[4] == 1.0
+        one.close()
+    ens.close()
+    outer.close()
+
+
+def test_members_match_single_runs_with_beta(mesh4):
+    kw = dict(dt=600.0, conserve_energy=1, diag_every=1)
+    ics = _ics(mesh4, M, 200)
+    ens = _ensemble(mesh4, ics, 1, **kw)
+    ens.step(10)
+    all_diag = ens.diag_all()
+    for m in (0, 7, M - 1):
+        one = _single(mesh4, ics[m], **kw)
+        one.step(10)
+        ens.select_member(m)
+        ge, ie, _ = ens.get_state()
+        g1, i1, _ = one.get_state()
+        assert rel_max(ge, g1) < 1e-6, (m, rel_max(ge, g1))
+        assert rel_max(ie, i1) < 1e-5, (m, rel_max(ie, i1))
+        d1 = one.diag()
+        assert abs(all_diag[m, 4] - d1[4]) < 1e-6, (m, all_diag[m, 4], d1[4])  # beta
+        assert abs(all_diag[m, 0] - d1[0]) <= 1e-12 * abs(d1[0])
+        one.close()
+    ens.close()
+
+
+def test_mass_conserved_and_energy_steady(mesh4):
+    kw = dict(dt=600.0, conserve_energy=1, diag_every=1)
+    ens = _ensemble(mesh4, _ics(mesh4, M, 300), 1, **kw)
+    d0 = ens.diag_all()
+    ens.step(24)
+    d1 = ens.diag_all()
+    assert np.all(np.isfinite(d1))
+    assert np.max(np.abs(d1[:, 0] - d0[:, 0]) / d0[:, 0]) < 1e-13
+    assert np.max(np.abs(d1[:, 1] - d0[:, 1]) / d0[:, 1]) < 1e-6
+    ens.close()
+
+
+def test_history_fields_of_a_member(mesh4):
+    kw = dict(dt=600.0, conserve_energy=0)
+    ics = _ics(mesh4, M, 400)
+    ens = _ensemble(mesh4, ics, 1, **kw)
+    one = _single(mesh4, ics[5], **kw)
+    ens.step(3)
+    one.step(3)
+    ens.select_member(5)
+    he, h1 = ens.history_fields(), one.history_fields()
+    for k in h1:
+        assert rel_max(he[k], h1[k]) < (1e-4 if k == "div" else 1e-5), (k, rel_max(he[k], h1[k]))
+    ens.close()
+    one.close()
+
+
+def test_autotune_and_group(mesh3, mesh4):
+    from tmcore_gb300.gpu import TMCoreGroup
+
+    kw = dict(conserve_energy=1, diag_every=0)
+    a = _ensemble(mesh4, _ics(mesh4, 64, 500), 1, dt=300.0, **kw)
+    before = a.get_state()
+    sizes = a.autotune(steps=2)
+    assert max(sizes.values()) <= 256
+    assert all(np.array_equal(x, y) for x, y in zip(before, a.get_state()))
+    # a group of two member-innermost ensembles (levels 3 and 4) equals separate stepping
+    g3 = _ensemble(mesh3, _ics(mesh3, M, 600), 1, dt=600.0, **kw)
+    s3 = _ensemble(mesh3, _ics(mesh3, M, 600), 1, dt=600.0, **kw)
+    s4 = _ensemble(mesh4, _ics(mesh4, 64, 500), 1, dt=300.0, **kw)
+    grp = TMCoreGroup([g3, a], cycle_seconds=600.0)
+    grp.run(2)
+    s3.step(2)
+    s4.step(4)
+    for x, y in ((g3, s3), (a, s4)):
+        for m in (0, 31):
+            x.select_member(m)
+            y.select_member(m)
+            assert all(np.array_equal(p, q) for p, q in zip(x.get_state(), y.get_state()))
+    grp.close()
+    for x in (a, g3, s3, s4):
+        x.close()
+
+
+def test_member_layout_refusals(mesh3):
+    from tmcore_gb300 import abi
+    from tmcore_gb300.gpu import ClosureMLP, TMCError, TMCoreGPU
+
+    with pytest.raises(TMCError) as e:
+        TMCoreGPU(mesh3, dt=600.0, members=48, member_layout=1, **KW)
+    assert e.value.code == abi.TMC_E_ARG
+    with pytest.raises(TMCError) as e:
+        TMCoreGPU(mesh3, dt=600.0, members=32, member_layout=1, precision=1, pv_scheme=3, interp_pv_order=3)
+    assert e.value.code == abi.TMC_E_UNSUP
+    ens = TMCoreGPU(mesh3, dt=600.0, members=32, member_layout=1, **KW)
+    net = ClosureMLP(seed=0)
+    with pytest.raises(TMCError) as e:
+        ens.set_closure(net)
+    assert e.value.code == abi.TMC_E_UNSUP
+    net.close()
+    ens.close()

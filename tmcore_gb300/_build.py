@@ -60,6 +60,7 @@ GPU_SOURCES = [
     ("tmc_kernels_f64.cu", "nvcc", ["-fmad=false"]),
     ("tmc_kernels_f32.cu", "nvcc", []),
     ("tmc_noalloc.cu", "nvcc", []),
+    ("tmc_ensemble.cu", "nvcc", []),
     ("tmc_mlp.cu", "nvcc", []),
     ("tmc_coarsen.cu", "nvcc", []),
     ("tmc_prep.cpp", "g++", ["-ffp-contract=off"]),

@@ -43,7 +43,8 @@ class Params(ctypes.Structure):
                 ("omega", ctypes.c_double), ("n_tracers", i32), ("tracer_adv_order", i32),
                 ("tracer_adv_mono", i32), ("precision", i32), ("renumber", i32), ("use_graph", i32),
                 ("diag_every", i32), ("device", i32), ("block_size", i32), ("stencils", i32),
-                ("adv_wind", i32), ("members", i32), ("reserved", i32 * 4)]
+                ("adv_wind", i32), ("members", i32), ("member_layout", i32),
+                ("reserved", i32 * 3)]
 
 
 # name -> (restype, argtypes)

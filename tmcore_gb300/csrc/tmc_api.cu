@@ -12,6 +12,7 @@
 #include <string>
 #include <vector>
 
+#include "tmc_ensemble.cuh"
 #include "tmc_kernels.cuh"
 #include "tmc_mlp.cuh"
 #include "tmc_prep.h"
@@ -648,6 +649,213 @@ struct Engine : EngineBase {
   }
 };
 
+// Member-innermost ensemble engine (tmc_params.member_layout = 1): the
+// same CRK4 stage program as Engine<float> on arrays [element][member]
+// (tmc_ensemble.cuh).  State slots old, A, B for gd and its FP32 shadow;
+// iap_u lives in slot old only (the fused stages keep the next stage's iap_u
+// in registers and store its edge preparation instead).
+struct EnsEngine : EngineBase {
+  tmc_handle* h;
+  ens::Dims D{};
+  ens::Partials EP{};
+  double* gd[3] = {};
+  float* gdf[3] = {};
+  float* iap0 = nullptr;
+  double *gd_acc = nullptr, *ghs = nullptr;
+  float *iap_acc = nullptr, *iap_tend = nullptr, *tendf = nullptr, *ghsf = nullptr;
+  float* gd_e[2] = {};
+  float* u[2] = {};
+  float* F[2] = {};
+  float *E = nullptr, *pv_v = nullptr, *vor = nullptr, *gd_v = nullptr, *pv_e = nullptr;
+  explicit EnsEngine(tmc_handle* hh) : h(hh) {}
+
+  int alloc() override {
+    const size_t M_ = (size_t)h->members;
+    const size_t nc = h->M.nc * M_, ne = h->M.ne * M_, nv = h->M.nv * M_;
+    D.M = h->members;
+    D.G = h->members / 32;
+    D.slots_c = ens::slots_for(h->M.nc);
+    D.slots_e = ens::slots_for(h->M.ne);
+    D.slots_v = ens::slots_for(h->M.nv);
+    EP.cap = std::max(D.slots_c, std::max(D.slots_e, D.slots_v));
+    EP.M = D.M;
+    EP.sf = h->dalloc<float>((size_t)(R_44_E + 1) * EP.cap * M_);
+    EP.sd = h->dalloc<double>((size_t)(R_AV - R_MASS + 1) * EP.cap * M_);
+    for (int i = 0; i < 3; ++i) {
+      gd[i] = h->dalloc<double>(nc);
+      gdf[i] = h->dalloc<float>(nc);
+    }
+    iap0 = h->dalloc<float>(ne);
+    gd_acc = h->dalloc<double>(nc);
+    ghs = h->dalloc<double>(nc);
+    ghsf = h->dalloc<float>(nc);
+    tendf = h->dalloc<float>(nc);
+    iap_acc = h->dalloc<float>(ne);
+    iap_tend = h->dalloc<float>(ne);
+    for (int i = 0; i < 2; ++i) {
+      gd_e[i] = h->dalloc<float>(ne);
+      u[i] = h->dalloc<float>(ne);
+      F[i] = h->dalloc<float>(ne);
+    }
+    E = h->dalloc<float>(nc);
+    pv_v = h->dalloc<float>(nv);
+    vor = h->dalloc<float>(nv);
+    gd_v = h->dalloc<float>(nv);
+    pv_e = h->dalloc<float>(ne);
+    if (!EP.sf || !EP.sd || !pv_e || !F[1] || !gd_v) return TMC_E_CUDA;
+    cudaMemset(ghs, 0, sizeof(double) * nc);
+    cudaMemset(ghsf, 0, sizeof(float) * nc);
+    return TMC_OK;
+  }
+
+  // buffers of CRK4 stage k (1..4; 0: the stand-alone passes on state(old)),
+  // the slot program of Engine::io
+  ens::IO io(int k) const {
+    static const int in_slot[5] = {0, 0, 1, 2, 1}, next_slot[5] = {-1, 1, 2, 1, -1};
+    const int set = (k >= 1) ? (k - 1) % 2 : 0;
+    const bool fuse = (k >= 1 && k <= 3);
+    ens::IO s{};
+    s.gd_in = gd[in_slot[k]];
+    s.gd_old = gd[0];
+    s.gd_next = next_slot[k] >= 0 ? gd[next_slot[k]] : nullptr;
+    s.gd_acc = gd_acc;
+    s.iap_in = iap0;
+    s.iap_old = iap0;
+    s.iap_next = nullptr;
+    s.iap_acc = iap_acc;
+    s.iap_tend = iap_tend;
+    s.gdf_in = gdf[in_slot[k]];
+    s.gdf_next = next_slot[k] >= 0 ? gdf[next_slot[k]] : nullptr;
+    s.tendf = tendf;
+    s.ghsf = ghsf;
+    s.ghs = ghs;
+    s.gd_e = gd_e[set];
+    s.u = u[set];
+    s.F = F[set];
+    s.gd_e_nx = fuse ? gd_e[1 - set] : nullptr;
+    s.u_nx = fuse ? u[1 - set] : nullptr;
+    s.F_nx = fuse ? F[1 - set] : nullptr;
+    s.E = E;
+    s.pv_v = pv_v;
+    s.vor = vor;
+    s.gd_v = gd_v;
+    s.pv_e = pv_e;
+    return s;
+  }
+
+  int launches_per_step() const override { return 4 * 4 + 2 + 2; }
+
+  void launch_prep() override { ens::launch_edge_prep(h->M, D, io(0), EP, true, h->bsp[P_FINAL], h->st); }
+
+  void launch_step(bool diag, std::vector<cudaEvent_t>* ev, size_t* pos) override {
+    const DevMesh& M = h->M;
+    const double dt = h->O.dt;
+    const double adt[5] = {0.0, 0.5 * dt, 0.5 * dt, dt, 0.0};
+    const int* b = h->bsp;
+    auto mark = [&](int pass) {
+      if (ev && h->timed_pass == pass) cudaEventRecord((*ev)[(*pos)++], h->st);
+    };
+    for (int k = 1; k <= 4; ++k) {
+      ens::IO s = io(k);
+      s.vor = nullptr;  // kept only by the diagnostic pass
+      s.gd_v = nullptr;
+      const bool dg = diag && k == 1;
+      const RKStage rk{k, adt[k]};
+      mark(P_CELL);
+      ens::launch_cell(M, D, s, rk, EP, dg, b[P_CELL], h->st);
+      mark(P_CELL);
+      mark(P_VERTEX);
+      ens::launch_vertex(M, D, s, EP, dg, b[P_VERTEX], h->st);
+      mark(P_VERTEX);
+      mark(P_PV);
+      ens::launch_edge_pv(M, D, s, b[P_PV], h->st);
+      mark(P_PV);
+      mark(P_FLUX);
+      ens::launch_edge_flux(M, D, s, rk, EP, b[P_FLUX], h->st);
+      mark(P_FLUX);
+    }
+    ens::launch_finalize(D, EP, true, diag, h->p.conserve_energy != 0, h->hm.totalArea, h->hm.sumAreaTriangle, dt,
+                         h->d_diag, h->st);
+    mark(P_FINAL);
+    ens::launch_final(M, D, io(0), h->d_diag, EP, b[P_FINAL], h->st);
+    mark(P_FINAL);
+  }
+
+  // gd_edge, u, pv, vorticity and invariants of state(old)
+  void launch_diag_pass(bool finalize) override {
+    const ens::IO s = io(0);
+    ens::launch_edge_prep(h->M, D, s, EP, true, h->bsp[P_FINAL], h->st);
+    ens::launch_cell_diag(h->M, D, s, EP, h->bsp[P_CELL], h->st);
+    ens::launch_vertex(h->M, D, s, EP, true, h->bsp[P_VERTEX], h->st);
+    if (finalize)
+      ens::launch_finalize(D, EP, false, true, false, h->hm.totalArea, h->hm.sumAreaTriangle, h->O.dt, h->d_diag,
+                           h->st);
+  }
+  void launch_spatial_only() override {}  // tmc_spatial_operators needs members <= 1
+
+  void set_state_dev(const double* raw_gd, const double* raw_iap) override {
+    ens::launch_gather_f64(h->M.nc, D.M, h->cur, raw_gd, h->d_cell_n2o, gd[0], h->st);
+    ens::launch_gather_f32(h->M.ne, D.M, h->cur, raw_iap, h->d_edge_n2o, iap0, h->st);
+    refresh_shadows(0);
+  }
+  void gather_field(int which, const double* raw) override {
+    if (which == F_GD)
+      ens::launch_gather_f64(h->M.nc, D.M, h->cur, raw, h->d_cell_n2o, gd[0], h->st);
+    else if (which == F_IAP)
+      ens::launch_gather_f32(h->M.ne, D.M, h->cur, raw, h->d_edge_n2o, iap0, h->st);
+  }
+  void get_field(int which, double* raw) override {
+    const int m = h->cur, Mm = D.M;
+    switch (which) {
+      case F_GD: ens::launch_scatter_f64(h->M.nc, Mm, m, gd[0], h->d_cell_n2o, raw, h->st); break;
+      case F_IAP: ens::launch_scatter_f32(h->M.ne, Mm, m, iap0, h->d_edge_n2o, raw, h->st); break;
+      case F_U: ens::launch_scatter_f32(h->M.ne, Mm, m, u[0], h->d_edge_n2o, raw, h->st); break;
+      case F_PV_V: ens::launch_scatter_f32(h->M.nv, Mm, m, pv_v, h->d_vert_n2o, raw, h->st); break;
+      case F_VOR: ens::launch_scatter_f32(h->M.nv, Mm, m, vor, h->d_vert_n2o, raw, h->st); break;
+      default: break;  // tendencies: tmc_spatial_operators needs members <= 1
+    }
+  }
+  void set_iap_from_u(const double* ge_new, const double* u_new) override {
+    ens::launch_iap_from_u(h->M.ne, D.M, h->cur, ge_new, u_new, iap0, h->st);
+  }
+  void set_tracers_dev(const double*) override {}  // member_layout 1 has no tracers
+  void get_tracers_dev(double*) override {}
+  void refresh_shadows(int slot) override { ens::launch_shadow(h->M.nc, D.M, h->cur, gd[slot], gdf[slot], h->st); }
+  void set_ghs_dev(const double* raw) override {
+    ens::launch_gather_f64(h->M.nc, D.M, h->cur, raw, h->d_cell_n2o, ghs, h->st);
+    ens::launch_shadow(h->M.nc, D.M, h->cur, ghs, ghsf, h->st);
+  }
+  void adv_set_initial_dev(const double*) override {}
+  void adv_get_dev(double*, double*) override {}
+  void state_slot0(void** g, void** i, void** q, void** gh) override {
+    *g = gd[0];
+    *i = iap0;
+    *q = nullptr;  // no tracers
+    *gh = ghs;
+  }
+  void refresh_all_shadows() override { ens::launch_shadow(h->M.nc, D.M, -1, gd[0], gdf[0], h->st); }
+  void closure_features(float*, float*) override {}  // tmc_closure_features refuses member_layout 1
+
+  // history fields of the selected member: its u, gd and ghs copied out of
+  // the member-innermost arrays, then the single-model kernels
+  void history_dev(double* uo, double* zon, double* mer, double* hc, double* div, double* pv, double* vo,
+                   double* scratch_e) override {
+    launch_diag_pass(false);
+    const int m = h->cur, Mm = D.M, nc = h->M.nc, ne = h->M.ne, nv = h->M.nv;
+    ens::launch_extract_f32(ne, Mm, m, u[0], scratch_e, h->st);
+    if (uo) cudaMemcpyAsync(uo, scratch_e, sizeof(double) * ne, cudaMemcpyDeviceToDevice, h->st);
+    if (zon || mer) launch_reconstruct<double>(h->M, scratch_e, nullptr, nullptr, nullptr, zon, mer, h->st);
+    if (hc) {
+      ens::launch_extract_f64(nc, Mm, m, gd[0], h->op_a, h->st);
+      ens::launch_extract_f64(nc, Mm, m, ghs, h->op_b, h->st);
+      launch_h_field(nc, h->op_a, h->op_b, h->p.g, hc, h->st);
+    }
+    if (div) launch_op(OP_DIV, h->M, h->O, scratch_e, nullptr, nullptr, div, 0, 0, 0.0, 0.0, h->bs, h->st);
+    if (pv) ens::launch_extract_f32(nv, Mm, m, pv_v, pv, h->st);
+    if (vo) ens::launch_extract_f32(nv, Mm, m, vor, vo, h->st);
+  }
+};
+
 DStencil upload_stencil(tmc_handle* h, const Stencil& S) {
   DStencil d{};
   d.width = S.width;
@@ -786,6 +994,16 @@ int tmc_create(const tmc_mesh_desc* mesh, const tmc_params* params, tmc_handle**
       return TMC_E_UNSUP;
     }
     if (h->members > 65535) return bad("members must be at most 65535");
+  }
+  if (p.member_layout != 0) {
+    if (p.member_layout != 1) return bad("member_layout must be 0 (member-outermost) or 1 (member-innermost)");
+    if (h->members < 32 || h->members % 32 != 0) return bad("member_layout 1 needs members a multiple of 32");
+    if (p.pv_scheme != 1 || p.apvm_weight != 0.0 || p.adv_order != 2 || p.n_tracers != 0 ||
+        p.flux_4th_order_correct) {
+      h->err = "member_layout 1 runs centred pv (pv_scheme 1, apvm_weight 0), adv_order 2, no tracers";
+      *out = h.release();
+      return TMC_E_UNSUP;
+    }
   }
   if (!(p.dt > 0.0) || !(p.radius > 0.0)) return bad("dt and radius must be positive");
   if (p.adv_order < 2 || p.adv_order > 6) return bad("adv_order must be 2..6");
@@ -951,7 +1169,9 @@ int tmc_create(const tmc_mesh_desc* mesh, const tmc_params* params, tmc_handle**
   }
   if (h->d_closure_err) cudaMemset(h->d_closure_err, 0, sizeof(int));
   cudaMemset(h->P.base, 0, sizeof(double) * h->P.member_stride() * h->members);
-  if (p.precision == TMC_FP32)
+  if (p.member_layout == 1)
+    h->eng = std::make_unique<EnsEngine>(h.get());
+  else if (p.precision == TMC_FP32)
     h->eng = std::make_unique<Engine<float>>(h.get());
   else
     h->eng = std::make_unique<Engine<double>>(h.get());
@@ -1367,6 +1587,7 @@ int tmc_set_closure(tmc_handle* h, const tmc_mlp* net) {
   TMC_REQUIRE_SWM(h);
   if (net && (h->p.precision != TMC_FP32 || h->generic))
     return h->fail(TMC_E_UNSUP, "the learned closure runs in the FP32 CRK4 shallow-water step");
+  if (net && h->p.member_layout == 1) return h->fail(TMC_E_UNSUP, "the learned closure needs member_layout 0");
   if (sync(h, "tmc_set_closure")) return TMC_E_CUDA;
   h->closure = net;
   if (net) h->closure_net = tmc_mlp_net(net);
@@ -1415,8 +1636,8 @@ int tmc_closure_status(tmc_handle* h, int32_t* timed_out) {
 int tmc_closure_features(tmc_handle* h, float* features, double* pv_edge) {
   TMC_REQUIRE_SWM(h);
   if (!features) return h->fail(TMC_E_ARG, "NULL array");
-  if (h->p.precision != TMC_FP32 || h->generic)
-    return h->fail(TMC_E_UNSUP, "closure features come from the FP32 CRK4 shallow-water step");
+  if (h->p.precision != TMC_FP32 || h->generic || h->p.member_layout == 1)
+    return h->fail(TMC_E_UNSUP, "closure features come from the FP32 CRK4 shallow-water step (member_layout 0)");
   if (!h->have_state) return h->fail(TMC_E_STATE, "no state set");
   const int ne = h->M.ne;
   float *d_feat = nullptr, *d_pv = nullptr;
@@ -1596,7 +1817,7 @@ int tmc_autotune(tmc_handle* h, int32_t steps, int32_t block_sizes[5]) {
   h->eng->state_slot0(&gd0, &iap0, &q0, &ghs0);
   const size_t b_gd = 8 * h->M.nc * M_, b_iap = es * h->M.ne * M_, b_q = es * nq * M_;
   if (cudaMalloc(&sv_gd, b_gd) != cudaSuccess || cudaMalloc(&sv_iap, b_iap) != cudaSuccess ||
-      cudaMalloc(&sv_q, b_q) != cudaSuccess) {
+      (q0 && cudaMalloc(&sv_q, b_q) != cudaSuccess)) {
     cudaFree(sv_gd);
     cudaFree(sv_iap);
     cudaFree(sv_q);
@@ -1604,7 +1825,7 @@ int tmc_autotune(tmc_handle* h, int32_t steps, int32_t block_sizes[5]) {
   }
   cudaMemcpyAsync(sv_gd, gd0, b_gd, cudaMemcpyDeviceToDevice, h->st);
   cudaMemcpyAsync(sv_iap, iap0, b_iap, cudaMemcpyDeviceToDevice, h->st);
-  cudaMemcpyAsync(sv_q, q0, b_q, cudaMemcpyDeviceToDevice, h->st);
+  if (q0) cudaMemcpyAsync(sv_q, q0, b_q, cudaMemcpyDeviceToDevice, h->st);
   const size_t nev = (size_t)steps * 8 + 2;
   while (h->ev_pool.size() < nev) {
     cudaEvent_t e;
@@ -1651,7 +1872,7 @@ int tmc_autotune(tmc_handle* h, int32_t steps, int32_t block_sizes[5]) {
   // restore the state and drop the graphs captured with the old block sizes
   cudaMemcpyAsync(gd0, sv_gd, b_gd, cudaMemcpyDeviceToDevice, h->st);
   cudaMemcpyAsync(iap0, sv_iap, b_iap, cudaMemcpyDeviceToDevice, h->st);
-  cudaMemcpyAsync(q0, sv_q, b_q, cudaMemcpyDeviceToDevice, h->st);
+  if (q0) cudaMemcpyAsync(q0, sv_q, b_q, cudaMemcpyDeviceToDevice, h->st);
   h->eng->refresh_all_shadows();
   h->prep_valid = false;
   int rc2 = sync(h, "tmc_autotune");

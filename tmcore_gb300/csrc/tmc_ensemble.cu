@@ -1,0 +1,749 @@
+// Member-innermost ensemble kernels (see tmc_ensemble.cuh).  FP32 path,
+// CRK4 (time_scheme_mod.F90:109-154), centred pv on edges (APVM weight 0,
+// operators_mod.F90:296-316), second-order gd on edges, no tracers.
+//
+// Thread layout of every pass: blockIdx.x = a range of kEnsEPB consecutive
+// elements (space-filling-curve order), warp w of the block = member group
+// blockIdx.y * W + w, lane = member within the group.  The block stages the
+// stencils of its elements in shared memory; each warp then walks the
+// elements, and each neighbour gather of a warp reads one 128-byte line
+// (32 FP32 members) or two (FP64 gd).
+#include <cuda_runtime.h>
+
+#include "tmc_ensemble.cuh"
+
+namespace tmc {
+namespace ens {
+
+namespace {
+
+constexpr int kME = 6;    // edges per cell (padded slots: sign 0)
+constexpr int kME2 = 10;  // edges per edge (padded slots: weight 0)
+constexpr int kMaxBS = 256;
+
+// FP32 error-free addition (Knuth TwoSum): hi + lo accumulates p exactly
+__device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float p) {
+  const float t = __fadd_rn(hi, p);
+  const float bp = __fsub_rn(t, hi);
+  const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(t, bp)), __fsub_rn(p, bp));
+  hi = t;
+  lo = __fadd_rn(lo, err);
+}
+
+struct DD {
+  double hi, lo;
+};
+__device__ __forceinline__ DD dd_add(DD a, DD b) {
+  const double s = __dadd_rn(a.hi, b.hi);
+  const double bb = __dsub_rn(s, a.hi);
+  double e = __dadd_rn(__dsub_rn(a.hi, __dsub_rn(s, bb)), __dsub_rn(b.hi, bb));
+  e = __dadd_rn(e, __dadd_rn(a.lo, b.lo));
+  const double hi = __dadd_rn(s, e);
+  return {hi, __dsub_rn(e, __dsub_rn(hi, s))};
+}
+
+// One block = one member group of 32 (blockIdx.y) and kEnsEPB consecutive
+// elements (blockIdx.x); its W warps take elements w, w + W, ... so that at
+// any time they work on W neighbouring elements and share the neighbours'
+// lines in L1.
+struct Lane {
+  int m;     // member
+  size_t M;  // member stride
+  int w, W;  // warp, warps
+  int lane;
+};
+__device__ __forceinline__ Lane lane_of(const Dims& D) {
+  return Lane{(int)(blockIdx.y * 32 + (threadIdx.x & 31)), (size_t)D.M, (int)(threadIdx.x >> 5),
+              (int)(blockDim.x >> 5), (int)(threadIdx.x & 31)};
+}
+
+inline dim3 grid_of(int n, const Dims& D, int bs, int* threads) {
+  int W = bs / 32;
+  if (W < 1) W = 1;
+  if (W > kMaxBS / 32) W = kMaxBS / 32;
+  *threads = W * 32;
+  return dim3((unsigned)slots_for(n), (unsigned)D.G);
+}
+
+// Per-member partial sums of one block: the warps' values of each lane are
+// combined in a fixed order (FP32 TwoSum, or FP64) and lane m of warp 0
+// stores them.  Every thread of the block calls these (they synchronise).
+template <int N>
+__device__ __forceinline__ void block_partials_f(const Lane& L, const float (&v)[N], float* const (&dst)[N]) {
+  __shared__ float sh[N][kMaxBS / 32][32];
+#pragma unroll
+  for (int k = 0; k < N; ++k) sh[k][L.w][L.lane] = v[k];
+  __syncthreads();
+  if (L.w == 0) {
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+      if (!dst[k]) continue;
+      float hi = 0.f, lo = 0.f;
+      for (int q = 0; q < L.W; ++q) two_sum_acc(hi, lo, sh[k][q][L.lane]);
+      dst[k][L.m] = hi + lo;
+    }
+  }
+  __syncthreads();
+}
+template <int N>
+__device__ __forceinline__ void block_partials_d(const Lane& L, const double (&v)[N], double* const (&dst)[N]) {
+  __shared__ double sh[N][kMaxBS / 32][32];
+#pragma unroll
+  for (int k = 0; k < N; ++k) sh[k][L.w][L.lane] = v[k];
+  __syncthreads();
+  if (L.w == 0) {
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+      double a = 0.0;
+      for (int q = 0; q < L.W; ++q) a += sh[k][q][L.lane];
+      dst[k][L.m] = a;
+    }
+  }
+  __syncthreads();
+}
+
+// Edge preparation of one edge (operators_mod.F90:93-104 c2e, :168-176
+// inverse IAP; mass flux u gd_edge, tmcore_swm_mod.F90:135), the FP32
+// single-model arithmetic.
+__device__ __forceinline__ void prep(float ia, float g1, float g2, float* gd_e, float* u, float* F, size_t em) {
+  const float ge = 0.5f * (g1 + g2);
+  const float sq = sqrtf(ge);
+  const float uu = ia / sq;
+  gd_e[em] = ge;
+  u[em] = uu;
+  F[em] = uu * ge;
+}
+
+// ---------------------------------------------------------------------------
+// cell: div of the mass flux (FP32 two-sum -> FP64 tendency), kinetic energy,
+// E = ke + gd + ghs, RK update of gd (div_operator operators_mod.F90:40-55,
+// calc_kinetic_energy :206-221, calc_gd_tend_on_cell tmcore_swm_mod.F90:127-139)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kMaxBS) k_ens_cell(DevMesh Mh, Dims D, IO S, RKStage rk, Partials P, int diag) {
+  __shared__ int s_e[kME][kEnsEPB];
+  __shared__ float s_ns[kME][kEnsEPB];
+  __shared__ float s_dv[kME][kEnsEPB];
+  __shared__ float s_ae[kME][kEnsEPB];
+  __shared__ double s_invA[kEnsEPB];
+  __shared__ double s_A[kEnsEPB];
+  __shared__ float s_invAf[kEnsEPB];
+  __shared__ float s_Af[kEnsEPB];
+  const int nc = Mh.nc, c0 = blockIdx.x * kEnsEPB, nel = min(kEnsEPB, nc - c0);
+  for (int t = threadIdx.x; t < kME * kEnsEPB; t += blockDim.x) {
+    const int i = t / kEnsEPB, j = t - i * kEnsEPB;
+    if (j < nel) {
+      const size_t k = (size_t)i * nc + c0 + j;
+      const int e = Mh.edgesOnCell[k];
+      s_e[i][j] = e;
+      s_ns[i][j] = (float)Mh.nSign[k];
+      s_dv[i][j] = Mh.dvEdge_f[e];
+      s_ae[i][j] = Mh.areaEdge_f[e];
+    }
+  }
+  for (int j = threadIdx.x; j < nel; j += blockDim.x) {
+    s_invA[j] = Mh.invAreaCell[c0 + j];
+    s_A[j] = Mh.areaCell[c0 + j];
+    s_invAf[j] = Mh.invAreaCell_f[c0 + j];
+    s_Af[j] = Mh.areaCell_f[c0 + j];
+  }
+  __syncthreads();
+  const Lane L = lane_of(D);
+  const size_t Mm = L.M;
+  const int m = L.m;
+  const int mode = rk.mode;
+  float rip = 0.f, r44 = 0.f, eh = 0.f, el = 0.f;
+  double mass = 0.0;
+  for (int j = L.w; j < nel; j += L.W) {
+    const size_t cm = (size_t)(c0 + j) * Mm + m;
+    const double gold = (mode <= 3) ? S.gd_old[cm] : 0.0;
+    const double gacc = (mode >= 2) ? S.gd_acc[cm] : 0.0;
+    const float tprev = (mode >= 2) ? S.tendf[cm] : 0.f;
+    const float gdf = S.gdf_in[cm], ghf = S.ghsf[cm];
+    const double gdin = diag ? S.gd_in[cm] : 0.0;
+    float uu[kME], Fv[kME];
+#pragma unroll
+    for (int i = 0; i < kME; ++i) {
+      const size_t k = (size_t)s_e[i][j] * Mm + m;
+      uu[i] = S.u[k];
+      Fv[i] = S.F[k];
+    }
+    float hi = 0.f, lo = 0.f, k = 0.f;
+#pragma unroll
+    for (int i = 0; i < kME; ++i) {
+      const float ns = s_ns[i][j];
+      two_sum_acc(hi, lo, __fmul_rn(__fmul_rn(ns, Fv[i]), s_dv[i][j]));
+      k += fabsf(ns) * uu[i] * uu[i] * s_ae[i][j];
+    }
+    const double t = -((double)hi + (double)lo) * s_invA[j];
+    const float tT = (float)t;
+    S.E[cm] = k * 0.25f * s_invAf[j] + gdf + ghf;
+    const float Af = s_Af[j];
+    double gnext = 0.0;
+    switch (mode) {
+      case 1:
+        S.gd_acc[cm] = t;
+        S.tendf[cm] = tT;
+        gnext = gold + rk.a_dt * t;
+        break;
+      case 2:
+      case 3:
+        rip += tprev * tT * Af;
+        S.gd_acc[cm] = gacc + 2.0 * t;
+        S.tendf[cm] = tT;
+        gnext = gold + rk.a_dt * t;
+        break;
+      default: {
+        rip += tprev * tT * Af;
+        const double tn = (gacc + t) * (1.0 / 6.0);
+        S.gd_acc[cm] = tn;
+        const float tnf = (float)tn;
+        r44 += tnf * tnf * Af;
+        S.tendf[cm] = tT;
+      }
+    }
+    if (mode <= 3) {
+      S.gd_next[cm] = gnext;
+      S.gdf_next[cm] = (float)gnext;
+    }
+    if (diag) {
+      // total mass (FP64 gd), and the cell part of the total energy
+      // (gd^2 + 2 gd ghs) areaCell from FP32 terms, compensated
+      // (tmcore_swm_mod.F90:215-231)
+      mass = mass + gdin * s_A[j];
+      two_sum_acc(eh, el, gdf * (gdf + 2.f * ghf) * Af);
+    }
+  }
+  const int slot = blockIdx.x;
+  if (mode >= 2) {
+    const float v[2] = {rip, r44};
+    float* const dst[2] = {P.f(R_IP_C + 2 * (mode - 2), slot), mode == 4 ? P.f(R_44_C, slot) : nullptr};
+    block_partials_f<2>(L, v, dst);
+  }
+  if (diag) {
+    const double v[2] = {mass, (double)eh + (double)el};
+    double* const dst[2] = {P.d(R_MASS, slot), P.d(R_EN_C, slot)};
+    block_partials_d<2>(L, v, dst);
+  }
+}
+
+// invariants of a state only (the diagnostic pass): mass and cell energy
+__global__ void __launch_bounds__(kMaxBS) k_ens_cell_diag(DevMesh Mh, Dims D, IO S, Partials P) {
+  __shared__ double s_A[kEnsEPB];
+  __shared__ float s_Af[kEnsEPB];
+  const int nc = Mh.nc, c0 = blockIdx.x * kEnsEPB, nel = min(kEnsEPB, nc - c0);
+  for (int j = threadIdx.x; j < nel; j += blockDim.x) {
+    s_A[j] = Mh.areaCell[c0 + j];
+    s_Af[j] = Mh.areaCell_f[c0 + j];
+  }
+  __syncthreads();
+  const Lane L = lane_of(D);
+  float eh = 0.f, el = 0.f;
+  double mass = 0.0;
+  for (int j = L.w; j < nel; j += L.W) {
+    const size_t cm = (size_t)(c0 + j) * L.M + L.m;
+    const double gdin = S.gd_in[cm];
+    const float gdf = S.gdf_in[cm], ghf = S.ghsf[cm];
+    mass = mass + gdin * s_A[j];
+    two_sum_acc(eh, el, gdf * (gdf + 2.f * ghf) * s_Af[j]);
+  }
+  const double v[2] = {mass, (double)eh + (double)el};
+  double* const dst[2] = {P.d(R_MASS, blockIdx.x), P.d(R_EN_C, blockIdx.x)};
+  block_partials_d<2>(L, v, dst);
+}
+
+// ---------------------------------------------------------------------------
+// vertex: gd on vertices, vorticity, pv (operators_mod.F90:106-123, :76-91,
+// :262-270); potential enstrophy and absolute vorticity on diag stages
+// ---------------------------------------------------------------------------
+constexpr int kVU = 2;  // vertices per warp iteration (loads of all first)
+
+__global__ void __launch_bounds__(kMaxBS) k_ens_vertex(DevMesh Mh, Dims D, IO S, Partials P, int diag) {
+  __shared__ int s_c[3][kEnsEPB];
+  __shared__ int s_e[3][kEnsEPB];
+  __shared__ float s_kt[3][kEnsEPB];
+  __shared__ float s_ts[3][kEnsEPB];  // tSign
+  __shared__ float s_dc[3][kEnsEPB];  // dcEdge of the vertex's edges
+  __shared__ float s_iA[kEnsEPB];
+  __shared__ float s_f[kEnsEPB];
+  __shared__ float s_At[kEnsEPB];
+  const int nv = Mh.nv, v0 = blockIdx.x * kEnsEPB, nel = min(kEnsEPB, nv - v0);
+  for (int t = threadIdx.x; t < 3 * kEnsEPB; t += blockDim.x) {
+    const int i = t / kEnsEPB, j = t - i * kEnsEPB;
+    if (j < nel) {
+      const size_t k = (size_t)i * nv + v0 + j;
+      const int e = Mh.edgesOnVertex[k];
+      s_c[i][j] = Mh.cellsOnVertex[k];
+      s_e[i][j] = e;
+      s_kt[i][j] = Mh.kite_f[k];
+      s_ts[i][j] = (float)Mh.tSign[k];
+      s_dc[i][j] = Mh.dcEdge_f[e];
+    }
+  }
+  for (int j = threadIdx.x; j < nel; j += blockDim.x) {
+    s_iA[j] = Mh.invAreaTriangle_f[v0 + j];
+    s_f[j] = Mh.fVertex_f[v0 + j];
+    s_At[j] = (float)Mh.areaTriangle[v0 + j];
+  }
+  __syncthreads();
+  const Lane L = lane_of(D);
+  const size_t Mm = L.M;
+  const int m = L.m;
+  float ph = 0.f, pl = 0.f, ah = 0.f, al = 0.f;
+  for (int base = L.w; base < nel; base += L.W * kVU) {
+    float g[kVU][3], uu[kVU][3];
+#pragma unroll
+    for (int q = 0; q < kVU; ++q) {
+      const int j = min(base + q * L.W, nel - 1);
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        g[q][i] = S.gdf_in[(size_t)s_c[i][j] * Mm + m];
+        uu[q][i] = S.u[(size_t)s_e[i][j] * Mm + m];
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < kVU; ++q) {
+      const int j = base + q * L.W;
+      if (j >= nel) break;
+      const float iA = s_iA[j];
+      const float gv = (g[q][0] * s_kt[0][j] + g[q][1] * s_kt[1][j] + g[q][2] * s_kt[2][j]) * iA;
+      const float sv = s_ts[0][j] * uu[q][0] * s_dc[0][j] + s_ts[1][j] * uu[q][1] * s_dc[1][j] +
+                       s_ts[2][j] * uu[q][2] * s_dc[2][j];
+      const float vo = -sv * iA;
+      const float pv = (s_f[j] + vo) / gv;
+      const size_t vm = (size_t)(v0 + j) * Mm + m;
+      S.pv_v[vm] = pv;
+      if (S.vor) S.vor[vm] = vo;
+      if (S.gd_v) S.gd_v[vm] = gv;
+      if (diag) {
+        // potential enstrophy and absolute vorticity (tmcore_swm_mod.F90:233-255),
+        // FP32 terms, compensated; vorticity and f as separate terms
+        two_sum_acc(ph, pl, gv * (pv * pv) * s_At[j]);
+        two_sum_acc(ah, al, vo * s_At[j]);
+        two_sum_acc(ah, al, s_f[j] * s_At[j]);
+      }
+    }
+  }
+  if (diag) {
+    const double v[2] = {(double)ph + (double)pl, (double)ah + (double)al};
+    double* const dst[2] = {P.d(R_PE, blockIdx.x), P.d(R_AV, blockIdx.x)};
+    block_partials_d<2>(L, v, dst);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// edge_pv: centred pv on edges (APVM weight 0, operators_mod.F90:296-316)
+// ---------------------------------------------------------------------------
+constexpr int kPU = 4;
+
+__global__ void __launch_bounds__(kMaxBS) k_ens_edge_pv(DevMesh Mh, Dims D, IO S) {
+  __shared__ int s_v[2][kEnsEPB];
+  const int ne = Mh.ne, e0 = blockIdx.x * kEnsEPB, nel = min(kEnsEPB, ne - e0);
+  for (int t = threadIdx.x; t < 2 * kEnsEPB; t += blockDim.x) {
+    const int i = t / kEnsEPB, j = t - i * kEnsEPB;
+    if (j < nel) s_v[i][j] = Mh.verticesOnEdge[(size_t)i * ne + e0 + j];
+  }
+  __syncthreads();
+  const Lane L = lane_of(D);
+  const size_t Mm = L.M;
+  const int m = L.m;
+  for (int base = L.w; base < nel; base += L.W * kPU) {
+    float p1[kPU], p2[kPU];
+#pragma unroll
+    for (int q = 0; q < kPU; ++q) {
+      const int j = min(base + q * L.W, nel - 1);
+      p1[q] = S.pv_v[(size_t)s_v[0][j] * Mm + m];
+      p2[q] = S.pv_v[(size_t)s_v[1][j] * Mm + m];
+    }
+#pragma unroll
+    for (int q = 0; q < kPU; ++q) {
+      const int j = base + q * L.W;
+      if (j >= nel) break;
+      S.pv_e[(size_t)(e0 + j) * Mm + m] = 0.5f * (p1[q] + p2[q]);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// edge_flux: q.F_perp over the 10 neighbours (calc_tangent_vor_flux,
+// operators_mod.F90:239-260), the gradient of E and the iap_u tendency
+// (calc_u_tend_on_edge, tmcore_swm_mod.F90:155-201), the RK update of iap_u
+// and the CRK4 inner products (time_scheme_mod.F90:109-154); stages 1-3 also
+// prepare the next stage's gd_edge, u and F from its gd and iap_u.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kMaxBS) k_ens_edge_flux(DevMesh Mh, Dims D, IO S, RKStage rk, Partials P) {
+  __shared__ int s_ep[kME2][kEnsEPB];
+  __shared__ float s_w[kME2][kEnsEPB];
+  __shared__ int s_c[2][kEnsEPB];
+  __shared__ float s_dc[kEnsEPB];
+  __shared__ float s_ae[kEnsEPB];
+  const int ne = Mh.ne, e0 = blockIdx.x * kEnsEPB, nel = min(kEnsEPB, ne - e0);
+  for (int t = threadIdx.x; t < kME2 * kEnsEPB; t += blockDim.x) {
+    const int i = t / kEnsEPB, j = t - i * kEnsEPB;
+    if (j < nel) {
+      const size_t k = (size_t)i * ne + e0 + j;
+      s_ep[i][j] = Mh.edgesOnEdge[k];  // padded entries: the edge itself, weight 0
+      s_w[i][j] = Mh.weightsOnEdge_f[k];
+    }
+  }
+  for (int t = threadIdx.x; t < 2 * kEnsEPB; t += blockDim.x) {
+    const int i = t / kEnsEPB, j = t - i * kEnsEPB;
+    if (j < nel) s_c[i][j] = Mh.cellsOnEdge[(size_t)i * ne + e0 + j];
+  }
+  for (int j = threadIdx.x; j < nel; j += blockDim.x) {
+    s_dc[j] = Mh.dcEdge_f[e0 + j];
+    s_ae[j] = Mh.areaEdge_f[e0 + j];
+  }
+  __syncthreads();
+  const Lane L = lane_of(D);
+  const size_t Mm = L.M;
+  const int m = L.m;
+  const int mode = rk.mode;
+  const bool fuse = S.u_nx != nullptr;
+  const float adt = (float)rk.a_dt;
+  float rip = 0.f, r44 = 0.f;
+  for (int j = L.w; j < nel; j += L.W) {
+    const size_t em = (size_t)(e0 + j) * Mm + m;
+    const size_t c1m = (size_t)s_c[0][j] * Mm + m, c2m = (size_t)s_c[1][j] * Mm + m;
+    const float pe = S.pv_e[em];
+    const float uu = S.u[em];
+    const float ge = S.gd_e[em];
+    const float tp = (mode >= 2) ? S.iap_tend[em] : 0.f;
+    const float accv = (mode >= 2) ? S.iap_acc[em] : 0.f;
+    const float oldv = (mode >= 1 && mode <= 3) ? S.iap_old[em] : 0.f;
+    float gn1 = 0.f, gn2 = 0.f;
+    if (fuse) {
+      gn1 = S.gdf_next[c1m];
+      gn2 = S.gdf_next[c2m];
+    }
+    const float E1 = S.E[c1m], E2 = S.E[c2m], t1 = S.tendf[c1m], t2 = S.tendf[c2m];
+    float Fv[kME2], pp[kME2];
+#pragma unroll
+    for (int i = 0; i < kME2; ++i) {
+      const size_t k = (size_t)s_ep[i][j] * Mm + m;
+      Fv[i] = S.F[k];
+      pp[i] = S.pv_e[k];
+    }
+    float s = 0.f;
+#pragma unroll
+    for (int i = 0; i < kME2; ++i) s += s_w[i][j] * Fv[i] * (0.5f * (pe + pp[i]));
+    const float dc = s_dc[j];
+    const float dEdx = (E2 - E1) / dc;
+    const float tge = 0.5f * (t1 + t2);
+    const float ut = s - dEdx;
+    const float sq = sqrtf(ge);
+    const float it = sq * ut + 0.5f * uu / sq * tge;
+    const float ae = s_ae[j];
+    float inext = 0.f;
+    switch (mode) {
+      case 1:
+        S.iap_acc[em] = it;
+        S.iap_tend[em] = it;
+        inext = oldv + adt * it;
+        break;
+      case 2:
+      case 3:
+        rip = rip + tp * it * ae;
+        S.iap_acc[em] = accv + 2.f * it;
+        S.iap_tend[em] = it;
+        inext = oldv + adt * it;
+        break;
+      default: {
+        rip = rip + tp * it * ae;
+        const float tn = (accv + it) * (1.0f / 6.0f);
+        S.iap_acc[em] = tn;
+        r44 = r44 + tn * tn * ae;
+        S.iap_tend[em] = it;
+      }
+    }
+    if (fuse)
+      prep(inext, gn1, gn2, S.gd_e_nx, S.u_nx, S.F_nx, em);
+    else if (mode <= 3)
+      S.iap_next[em] = inext;
+  }
+  if (mode >= 2) {
+    const int slot = blockIdx.x;
+    const float v[2] = {rip, r44};
+    float* const dst[2] = {P.f(R_IP_E + 2 * (mode - 2), slot), mode == 4 ? P.f(R_44_E, slot) : nullptr};
+    block_partials_f<2>(L, v, dst);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// final update new = old + (beta dt) t_new (update_state, tmcore_swm_mod.F90:203-213),
+// in place in state(old), with beta per member
+// ---------------------------------------------------------------------------
+constexpr int kFU = 4;
+
+__global__ void __launch_bounds__(kMaxBS) k_ens_final_cells(DevMesh Mh, Dims D, IO S, const double* diag) {
+  const Lane L = lane_of(D);
+  const size_t Mm = L.M;
+  const int m = L.m;
+  const double bdt = diag[(size_t)m * kDiagStride + 9];
+  const int nc = Mh.nc, c0 = blockIdx.x * kEnsEPB, nel = min(kEnsEPB, nc - c0);
+  double* gd = const_cast<double*>(S.gd_old);
+  float* gdf = const_cast<float*>(S.gdf_in);
+  for (int base = L.w; base < nel; base += L.W * kFU) {
+    double g[kFU];
+#pragma unroll
+    for (int q = 0; q < kFU; ++q) {
+      const size_t cm = (size_t)(c0 + min(base + q * L.W, nel - 1)) * Mm + m;
+      g[q] = gd[cm] + bdt * S.gd_acc[cm];
+    }
+#pragma unroll
+    for (int q = 0; q < kFU; ++q) {
+      const int j = base + q * L.W;
+      if (j >= nel) break;
+      const size_t cm = (size_t)(c0 + j) * Mm + m;
+      gd[cm] = g[q];
+      gdf[cm] = (float)g[q];
+    }
+  }
+}
+
+// Edges: iap_u of state(old) in place, then the edge preparation of the next
+// step's first stage and the edge energy iap_u^2 areaEdge of the new state
+// (tmcore_swm_mod.F90:229), FP32 terms, compensated.  `update` false: the
+// stand-alone edge preparation of S.iap_in (energy only when `diag`).
+template <bool kUpdate>
+__global__ void __launch_bounds__(kMaxBS) k_ens_edges(DevMesh Mh, Dims D, IO S, const double* diag, Partials P,
+                                                      int want_energy) {
+  __shared__ int s_c[2][kEnsEPB];
+  __shared__ float s_ae[kEnsEPB];
+  const int ne = Mh.ne, e0 = blockIdx.x * kEnsEPB, nel = min(kEnsEPB, ne - e0);
+  for (int t = threadIdx.x; t < 2 * kEnsEPB; t += blockDim.x) {
+    const int i = t / kEnsEPB, j = t - i * kEnsEPB;
+    if (j < nel) s_c[i][j] = Mh.cellsOnEdge[(size_t)i * ne + e0 + j];
+  }
+  for (int j = threadIdx.x; j < nel; j += blockDim.x) s_ae[j] = Mh.areaEdge_f[e0 + j];
+  __syncthreads();
+  const Lane L = lane_of(D);
+  const size_t Mm = L.M;
+  const int m = L.m;
+  const float bdt = kUpdate ? (float)diag[(size_t)m * kDiagStride + 9] : 0.f;
+  float* iap = const_cast<float*>(kUpdate ? S.iap_old : S.iap_in);
+  float eh = 0.f, el = 0.f;
+  for (int base = L.w; base < nel; base += L.W * kFU) {
+    float ia[kFU], g1[kFU], g2[kFU];
+#pragma unroll
+    for (int q = 0; q < kFU; ++q) {
+      const int j = min(base + q * L.W, nel - 1);
+      const size_t em = (size_t)(e0 + j) * Mm + m;
+      ia[q] = kUpdate ? iap[em] + bdt * S.iap_acc[em] : iap[em];
+      g1[q] = S.gdf_in[(size_t)s_c[0][j] * Mm + m];
+      g2[q] = S.gdf_in[(size_t)s_c[1][j] * Mm + m];
+    }
+#pragma unroll
+    for (int q = 0; q < kFU; ++q) {
+      const int j = base + q * L.W;
+      if (j >= nel) break;
+      const size_t em = (size_t)(e0 + j) * Mm + m;
+      if (kUpdate) iap[em] = ia[q];
+      prep(ia[q], g1[q], g2[q], const_cast<float*>(S.gd_e), const_cast<float*>(S.u), const_cast<float*>(S.F), em);
+      if (want_energy) two_sum_acc(eh, el, ia[q] * ia[q] * s_ae[j]);
+    }
+  }
+  if (want_energy) {
+    const double v[1] = {(double)eh + (double)el};
+    double* const dst[1] = {P.d(R_EN_E, blockIdx.x)};
+    block_partials_d<1>(L, v, dst);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// reduction of the per-thread partials: block = (region, group of 32
+// members), warp w sums slots w, w + W, ... for its 32 members (FP32 TwoSum
+// for the step products, FP64 for the invariants), warp 0 combines the warps
+// in double-double and stores the region sum after the member's kDiagLen
+// outputs.
+// ---------------------------------------------------------------------------
+struct RegionList {
+  int n;
+  int r[R_COUNT];
+  int count[R_COUNT];
+};
+
+__global__ void __launch_bounds__(256) k_ens_reduce(Partials P, RegionList RL, double* diag_out) {
+  const int r = RL.r[blockIdx.x], count = RL.count[blockIdx.x];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int m = blockIdx.y * 32 + lane;
+  double hi = 0.0, lo = 0.0;
+  if (r <= R_44_E) {
+    float fh = 0.f, fl = 0.f;
+    for (int s = w; s < count; s += nw) two_sum_acc(fh, fl, P.f(r, s)[m]);
+    hi = (double)fh;
+    lo = (double)fl;
+  } else {
+    for (int s = w; s < count; s += nw) hi += P.d(r, s)[m];
+  }
+  __shared__ double sh[8][32], sl[8][32];
+  sh[w][lane] = hi;
+  sl[w][lane] = lo;
+  __syncthreads();
+  if (w != 0) return;
+  DD acc{0.0, 0.0};
+  for (int k = 0; k < nw; ++k) acc = dd_add(acc, DD{sh[k][lane], sl[k][lane]});
+  diag_out[(size_t)m * kDiagStride + kDiagLen + r] = acc.hi + acc.lo;
+}
+
+// beta (time_scheme_mod.F90:144-150) and the invariants (tmcore_swm_mod.F90:215-255)
+// of every member from its region sums
+__global__ void k_ens_beta(int M, int step, int diag, int conserve, double totalArea, double sumAreaTriangle,
+                           double dt, double* diag_out) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= M) return;
+  double* out = diag_out + (size_t)m * kDiagStride;
+  const double* rv = out + kDiagLen;
+  if (step) {
+    double R[4];
+    for (int k = 0; k < 3; ++k) R[k] = (rv[R_IP_E + 2 * k] + rv[R_IP_C + 2 * k]) / totalArea;
+    R[3] = (rv[R_44_E] + rv[R_44_C]) / totalArea;
+    const double beta = conserve ? (R[0] + R[1] + R[2]) / (3.0 * R[3]) : 1.0;
+    out[4] = beta;
+    out[5] = R[0];
+    out[6] = R[1];
+    out[7] = R[2];
+    out[8] = R[3];
+    out[9] = beta * dt;
+  }
+  if (diag) {
+    out[0] = rv[R_MASS];
+    out[1] = rv[R_EN_E] + rv[R_EN_C];
+    out[2] = rv[R_PE];
+    out[3] = rv[R_AV] / sumAreaTriangle;
+  }
+}
+
+// ---- state transfer ----
+__global__ void k_ens_gather_f64(int n, int M, int m, const double* raw, const int32_t* n2o, double* dst) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[(size_t)i * M + m] = raw[n2o[i]];
+}
+__global__ void k_ens_gather_f32(int n, int M, int m, const double* raw, const int32_t* n2o, float* dst) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[(size_t)i * M + m] = (float)raw[n2o[i]];
+}
+template <class T>
+__global__ void k_ens_scatter(int n, int M, int m, const T* src, const int32_t* n2o, double* raw) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) raw[n2o[i]] = (double)src[(size_t)i * M + m];
+}
+template <class T>
+__global__ void k_ens_extract(int n, int M, int m, const T* src, double* dst) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = (double)src[(size_t)i * M + m];
+}
+__global__ void k_ens_iap_from_u(int ne, int M, int m, const double* gd_e, const double* u, float* iap) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < ne) iap[(size_t)i * M + m] = (float)(sqrt(gd_e[i]) * u[i]);
+}
+__global__ void k_ens_shadow(size_t n, int M, int m, const double* gd, float* gdf) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const size_t k = m < 0 ? i : i * M + m;
+  gdf[k] = (float)gd[k];
+}
+
+inline unsigned nb(size_t n) { return (unsigned)((n + 255) / 256); }
+
+}  // namespace
+
+// ---- launchers ----
+void launch_cell(const DevMesh& Mh, const Dims& D, const IO& S, RKStage rk, const Partials& P, bool diag, int bs,
+                 cudaStream_t st) {
+  int th;
+  const dim3 g = grid_of(Mh.nc, D, bs, &th);
+  k_ens_cell<<<g, th, 0, st>>>(Mh, D, S, rk, P, diag ? 1 : 0);
+}
+void launch_cell_diag(const DevMesh& Mh, const Dims& D, const IO& S, const Partials& P, int bs, cudaStream_t st) {
+  int th;
+  const dim3 g = grid_of(Mh.nc, D, bs, &th);
+  k_ens_cell_diag<<<g, th, 0, st>>>(Mh, D, S, P);
+}
+void launch_vertex(const DevMesh& Mh, const Dims& D, const IO& S, const Partials& P, bool diag, int bs,
+                   cudaStream_t st) {
+  int th;
+  const dim3 g = grid_of(Mh.nv, D, bs, &th);
+  k_ens_vertex<<<g, th, 0, st>>>(Mh, D, S, P, diag ? 1 : 0);
+}
+void launch_edge_pv(const DevMesh& Mh, const Dims& D, const IO& S, int bs, cudaStream_t st) {
+  int th;
+  const dim3 g = grid_of(Mh.ne, D, bs, &th);
+  k_ens_edge_pv<<<g, th, 0, st>>>(Mh, D, S);
+}
+void launch_edge_flux(const DevMesh& Mh, const Dims& D, const IO& S, RKStage rk, const Partials& P, int bs,
+                      cudaStream_t st) {
+  int th;
+  const dim3 g = grid_of(Mh.ne, D, bs, &th);
+  k_ens_edge_flux<<<g, th, 0, st>>>(Mh, D, S, rk, P);
+}
+void launch_final(const DevMesh& Mh, const Dims& D, const IO& S, const double* diag, const Partials& P, int bs,
+                  cudaStream_t st) {
+  int th;
+  const dim3 gc = grid_of(Mh.nc, D, bs, &th);
+  k_ens_final_cells<<<gc, th, 0, st>>>(Mh, D, S, diag);
+  const dim3 ge = grid_of(Mh.ne, D, bs, &th);
+  k_ens_edges<true><<<ge, th, 0, st>>>(Mh, D, S, diag, P, 1);
+}
+void launch_edge_prep(const DevMesh& Mh, const Dims& D, const IO& S, const Partials& P, bool diag, int bs,
+                      cudaStream_t st) {
+  int th;
+  const dim3 g = grid_of(Mh.ne, D, bs, &th);
+  k_ens_edges<false><<<g, th, 0, st>>>(Mh, D, S, nullptr, P, diag ? 1 : 0);
+}
+void launch_finalize(const Dims& D, const Partials& P, bool step, bool diag, bool conserve, double totalArea,
+                     double sumAreaTriangle, double dt, double* diag_out, cudaStream_t st) {
+  RegionList RL{};
+  auto add = [&](int r, int count) {
+    RL.r[RL.n] = r;
+    RL.count[RL.n] = count;
+    RL.n++;
+  };
+  if (step) {
+    for (int k = 0; k < 3; ++k) {
+      add(R_IP_C + 2 * k, D.slots_c);
+      add(R_IP_E + 2 * k, D.slots_e);
+    }
+    add(R_44_C, D.slots_c);
+    add(R_44_E, D.slots_e);
+  }
+  if (diag) {
+    add(R_MASS, D.slots_c);
+    add(R_EN_C, D.slots_c);
+    add(R_EN_E, D.slots_e);
+    add(R_PE, D.slots_v);
+    add(R_AV, D.slots_v);
+  }
+  if (RL.n == 0) return;
+  k_ens_reduce<<<dim3(RL.n, D.G), 256, 0, st>>>(P, RL, diag_out);
+  k_ens_beta<<<nb(D.M), 256, 0, st>>>(D.M, step ? 1 : 0, diag ? 1 : 0, conserve ? 1 : 0, totalArea,
+                                      sumAreaTriangle, dt, diag_out);
+}
+
+void launch_gather_f64(int n, int M, int m, const double* raw, const int32_t* n2o, double* dst, cudaStream_t st) {
+  k_ens_gather_f64<<<nb(n), 256, 0, st>>>(n, M, m, raw, n2o, dst);
+}
+void launch_gather_f32(int n, int M, int m, const double* raw, const int32_t* n2o, float* dst, cudaStream_t st) {
+  k_ens_gather_f32<<<nb(n), 256, 0, st>>>(n, M, m, raw, n2o, dst);
+}
+void launch_scatter_f64(int n, int M, int m, const double* src, const int32_t* n2o, double* raw, cudaStream_t st) {
+  k_ens_scatter<double><<<nb(n), 256, 0, st>>>(n, M, m, src, n2o, raw);
+}
+void launch_scatter_f32(int n, int M, int m, const float* src, const int32_t* n2o, double* raw, cudaStream_t st) {
+  k_ens_scatter<float><<<nb(n), 256, 0, st>>>(n, M, m, src, n2o, raw);
+}
+void launch_extract_f64(int n, int M, int m, const double* src, double* dst, cudaStream_t st) {
+  k_ens_extract<double><<<nb(n), 256, 0, st>>>(n, M, m, src, dst);
+}
+void launch_extract_f32(int n, int M, int m, const float* src, double* dst, cudaStream_t st) {
+  k_ens_extract<float><<<nb(n), 256, 0, st>>>(n, M, m, src, dst);
+}
+void launch_iap_from_u(int ne, int M, int m, const double* gd_e, const double* u, float* iap, cudaStream_t st) {
+  k_ens_iap_from_u<<<nb(ne), 256, 0, st>>>(ne, M, m, gd_e, u, iap);
+}
+void launch_shadow(int nc, int M, int m, const double* gd, float* gdf, cudaStream_t st) {
+  const size_t n = m < 0 ? (size_t)nc * M : (size_t)nc;
+  k_ens_shadow<<<nb(n), 256, 0, st>>>(n, M, m, gd, gdf);
+}
+
+}  // namespace ens
+}  // namespace tmc

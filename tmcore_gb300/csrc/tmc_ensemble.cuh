@@ -1,0 +1,118 @@
+// Member-innermost ensembles (tmc_params.member_layout = 1).
+//
+// M members of one mesh (M a multiple of 32) are stored member-innermost:
+// element i of member m sits at [i * M + m].  A warp owns 32 consecutive
+// members of one element at a time, so every neighbour gather of a warp is
+// one 128-byte line (FP32) and every mesh index or metric it needs is the
+// same for all its lanes.  A block covers one member group and kEnsEPB
+// consecutive elements; it first stages those elements' stencils (indices,
+// signs, weights, metrics) in shared memory, then its W warps take elements
+// w, w + W, ..., so that they work on neighbouring elements together and
+// share the neighbours' lines in L1.  The arithmetic is that of the FP32
+// single-model kernels (tmc_kernels_impl.cuh) in the same expression order:
+// FP32 edge and vertex state, FP64 gd, its tendency from an FP32 two-sum
+// flux divergence and its RK accumulation.
+//
+// Global sums: the warps of a block combine their lanes' sums in shared
+// memory, and lane m of warp 0 stores member m's partial sum of the block,
+// [region][slot][M] (coalesced across the warp).  The CRK4 inner products are FP32 partials
+// combined with FP32 two-sum arithmetic; the invariants are FP64 partials.
+// k_ens_reduce sums the slots of one region for 32 members per block and
+// k_ens_beta forms beta and the invariants per member into the per-member
+// diag block that the member-outermost path also uses.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "tmc_kernels.cuh"
+
+namespace tmc {
+namespace ens {
+
+constexpr int kEnsEPB = 64;  // elements per block (and per partial-sum slot)
+
+struct Dims {
+  int M;  // members (a multiple of 32)
+  int G;  // member groups of 32
+  int slots_c, slots_e, slots_v;  // partial slots: blocks along cells, edges, vertices
+};
+
+__host__ __device__ inline int slots_for(int n) { return (n + kEnsEPB - 1) / kEnsEPB; }
+
+// Per-thread partial sums: step regions R_IP_C..R_44_E (FP32) and invariant
+// regions R_MASS..R_AV (FP64), each [slots][M].
+struct Partials {
+  float* sf;   // [R_44_E + 1][cap][M]
+  double* sd;  // [R_AV - R_MASS + 1][cap][M]
+  int cap;     // slots per region
+  int M;
+  __host__ __device__ float* f(int r, int slot) const { return sf + ((size_t)r * cap + slot) * M; }
+  __host__ __device__ double* d(int r, int slot) const { return sd + ((size_t)(r - R_MASS) * cap + slot) * M; }
+};
+
+// Buffers of one CRK4 stage, all member-innermost.
+struct IO {
+  const double* gd_in;
+  const double* gd_old;
+  double* gd_next;
+  double* gd_acc;
+  const float* iap_in;
+  const float* iap_old;
+  float* iap_next;
+  float* iap_acc;
+  float* iap_tend;
+  const float* gdf_in;
+  float* gdf_next;
+  float* tendf;
+  const float* ghsf;
+  const double* ghs;
+  const float* gd_e;
+  const float* u;
+  const float* F;
+  float* gd_e_nx;  // the next stage's edge set (stages 1-3), null: not fused
+  float* u_nx;
+  float* F_nx;
+  float* E;
+  float* pv_v;
+  float* vor;   // null: not kept
+  float* gd_v;  // null: not kept
+  float* pv_e;
+};
+
+// passes of the fused CRK4 step (bs: threads per block, a multiple of 32)
+void launch_cell(const DevMesh& Mh, const Dims& D, const IO& S, RKStage rk, const Partials& P, bool diag, int bs,
+                 cudaStream_t st);
+void launch_vertex(const DevMesh& Mh, const Dims& D, const IO& S, const Partials& P, bool diag, int bs,
+                   cudaStream_t st);
+void launch_edge_pv(const DevMesh& Mh, const Dims& D, const IO& S, int bs, cudaStream_t st);
+void launch_edge_flux(const DevMesh& Mh, const Dims& D, const IO& S, RKStage rk, const Partials& P, int bs,
+                      cudaStream_t st);
+// new = old + beta dt t_new for cells, then edges with the edge preparation
+// of the next step's first stage and the edge energy of the new state
+void launch_final(const DevMesh& Mh, const Dims& D, const IO& S, const double* diag, const Partials& P, int bs,
+                  cudaStream_t st);
+// edge preparation of slot S.gd_in / S.iap_in into S.gd_e/u/F (+ edge energy)
+void launch_edge_prep(const DevMesh& Mh, const Dims& D, const IO& S, const Partials& P, bool diag, int bs,
+                      cudaStream_t st);
+// mass and the cell part of the energy of S.gd_in (the diagnostic pass)
+void launch_cell_diag(const DevMesh& Mh, const Dims& D, const IO& S, const Partials& P, int bs, cudaStream_t st);
+// region sums, beta (CRK4) and invariants into diag[m * kDiagStride + ...]
+void launch_finalize(const Dims& D, const Partials& P, bool step, bool diag, bool conserve, double totalArea,
+                     double sumAreaTriangle, double dt, double* diag_out, cudaStream_t st);
+
+// state transfer of member m (caller's element order <-> member-innermost)
+void launch_gather_f64(int n, int M, int m, const double* raw, const int32_t* n2o, double* dst, cudaStream_t st);
+void launch_gather_f32(int n, int M, int m, const double* raw, const int32_t* n2o, float* dst, cudaStream_t st);
+void launch_scatter_f64(int n, int M, int m, const double* src, const int32_t* n2o, double* raw, cudaStream_t st);
+void launch_scatter_f32(int n, int M, int m, const float* src, const int32_t* n2o, double* raw, cudaStream_t st);
+// member m of a member-innermost array into a contiguous FP64 array (internal order)
+void launch_extract_f64(int n, int M, int m, const double* src, double* dst, cudaStream_t st);
+void launch_extract_f32(int n, int M, int m, const float* src, double* dst, cudaStream_t st);
+// iap_u of member m = sqrt(gd_edge) u (internal order inputs)
+void launch_iap_from_u(int ne, int M, int m, const double* gd_e, const double* u, float* iap, cudaStream_t st);
+// FP32 shadow of member m's gd (m < 0: every member)
+void launch_shadow(int nc, int M, int m, const double* gd, float* gdf, cudaStream_t st);
+
+}  // namespace ens
+}  // namespace tmc

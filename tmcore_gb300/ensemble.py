@@ -25,11 +25,12 @@ def main():
     ap.add_argument("--closure", action="store_true", help="a closure network of the trained shape on every stage")
     ap.add_argument("--autotune", action="store_true")
     ap.add_argument("--distinct-seeds", action="store_true", help="seed m for member m (else one seed for all)")
+    ap.add_argument("--layout", type=int, default=0, help="member_layout: 0 member-outermost, 1 member-innermost")
     a = ap.parse_args()
     m = icos_mesh(a.level)
     dt = 1200.0 / 2 ** (a.level - 4)
     ens = TMCoreGPU(m, members=a.members, dt=dt, precision=abi.TMC_FP32, pv_scheme=1, apvm_weight=0.0,
-                    diag_every=1)
+                    adv_order=2, diag_every=1, member_layout=a.layout)
     ic = None if a.distinct_seeds else cases.jet_bumps(m, seed=0)
     for k in range(a.members):
         gd, u, ghs = cases.jet_bumps(m, seed=k) if a.distinct_seeds else ic
@@ -44,7 +45,8 @@ def main():
     ens.step(a.warmup)
     ens.synchronize()
     ms, _, _, launches = ens.time_steps(a.steps, total=True, flux=False)
-    print(json.dumps({"members": a.members, "level": a.level, "closure": a.closure, "ms_per_step": ms / a.steps,
+    print(json.dumps({"members": a.members, "level": a.level, "layout": a.layout, "closure": a.closure,
+                      "ms_per_step": ms / a.steps,
                       "member_days_per_s": a.members * a.steps * dt / 86400.0 / (ms / 1e3),
                       "gpu_launches": launches, "block_sizes": sizes,
                       "closure_timed_out": ens.closure_status() if a.closure else None}))
