@@ -44,14 +44,15 @@ def _single(mesh, ic, **kw):
     return one
 
 
-def test_members_match_single_runs_without_beta(mesh4):
+@pytest.mark.parametrize("members", [M, 2 * M])  # one or two members per lane
+def test_members_match_single_runs_without_beta(mesh4, members):
     kw = dict(dt=600.0, conserve_energy=0, diag_every=1)
-    ics = _ics(mesh4, M, 100)
+    ics = _ics(mesh4, members, 100)
     ens = _ensemble(mesh4, ics, 1, **kw)
     outer = _ensemble(mesh4, ics, 0, **kw)
     ens.step(7)
     outer.step(7)
-    for m in (0, 13, M - 1):
+    for m in (0, 13, members - 1):
         one = _single(mesh4, ics[m], **kw)
         one.step(7)
         ens.select_member(m)
@@ -75,13 +76,14 @@ def test_members_match_single_runs_without_beta(mesh4):
     outer.close()
 
 
-def test_members_match_single_runs_with_beta(mesh4):
+@pytest.mark.parametrize("members", [M, 2 * M])
+def test_members_match_single_runs_with_beta(mesh4, members):
     kw = dict(dt=600.0, conserve_energy=1, diag_every=1)
-    ics = _ics(mesh4, M, 200)
+    ics = _ics(mesh4, members, 200)
     ens = _ensemble(mesh4, ics, 1, **kw)
     ens.step(10)
     all_diag = ens.diag_all()
-    for m in (0, 7, M - 1):
+    for m in (0, 7, members - 1):
         one = _single(mesh4, ics[m], **kw)
         one.step(10)
         ens.select_member(m)
@@ -98,7 +100,7 @@ def test_members_match_single_runs_with_beta(mesh4):
 
 def test_mass_conserved_and_energy_steady(mesh4):
     kw = dict(dt=600.0, conserve_energy=1, diag_every=1)
-    ens = _ensemble(mesh4, _ics(mesh4, M, 300), 1, **kw)
+    ens = _ensemble(mesh4, _ics(mesh4, 2 * M, 300), 1, **kw)
     d0 = ens.diag_all()
     ens.step(24)
     d1 = ens.diag_all()

@@ -2,12 +2,14 @@
 // CRK4 (time_scheme_mod.F90:109-154), centred pv on edges (APVM weight 0,
 // operators_mod.F90:296-316), second-order gd on edges, no tracers.
 //
-// Thread layout of every pass: blockIdx.x = a range of kEnsEPB consecutive
-// elements (space-filling-curve order), warp w of the block = member group
-// blockIdx.y * W + w, lane = member within the group.  The block stages the
-// stencils of its elements in shared memory; each warp then walks the
-// elements, and each neighbour gather of a warp reads one 128-byte line
-// (32 FP32 members) or two (FP64 gd).
+// Thread layout of every pass: blockIdx.x = kEnsEPB consecutive elements
+// (space-filling-curve order), blockIdx.y = a group of 32 V members, lane l
+// = members (32 blockIdx.y + l) V ... + V - 1 (V = 2 when the member count
+// is a multiple of 64: a lane's two members are one 8-byte load, and the
+// index, shared-memory and address work of an element is shared by both).
+// The block stages the stencils of its elements in shared memory; its W
+// warps then take elements w, w + W, ..., neighbouring elements at the same
+// time, and every neighbour gather of a warp reads whole 128-byte lines.
 #include <cuda_runtime.h>
 
 #include "tmc_ensemble.cuh"
@@ -42,18 +44,53 @@ __device__ __forceinline__ DD dd_add(DD a, DD b) {
   return {hi, __dsub_rn(e, __dsub_rn(hi, s))};
 }
 
-// One block = one member group of 32 (blockIdx.y) and kEnsEPB consecutive
-// elements (blockIdx.x); its W warps take elements w, w + W, ... so that at
-// any time they work on W neighbouring elements and share the neighbours'
-// lines in L1.
+// V consecutive members of one element: one load / store of V * 4 (or 8) bytes
+template <int V>
+__device__ __forceinline__ void ldv(const float* p, size_t i, float (&o)[V]) {
+  if constexpr (V == 2) {
+    const float2 t = *reinterpret_cast<const float2*>(p + i);
+    o[0] = t.x;
+    o[1] = t.y;
+  } else {
+    o[0] = p[i];
+  }
+}
+template <int V>
+__device__ __forceinline__ void ldv(const double* p, size_t i, double (&o)[V]) {
+  if constexpr (V == 2) {
+    const double2 t = *reinterpret_cast<const double2*>(p + i);
+    o[0] = t.x;
+    o[1] = t.y;
+  } else {
+    o[0] = p[i];
+  }
+}
+template <int V>
+__device__ __forceinline__ void stv(float* p, size_t i, const float (&v)[V]) {
+  if constexpr (V == 2)
+    *reinterpret_cast<float2*>(p + i) = make_float2(v[0], v[1]);
+  else
+    p[i] = v[0];
+}
+template <int V>
+__device__ __forceinline__ void stv(double* p, size_t i, const double (&v)[V]) {
+  if constexpr (V == 2)
+    *reinterpret_cast<double2*>(p + i) = make_double2(v[0], v[1]);
+  else
+    p[i] = v[0];
+}
+
+// This thread's members and warp: one block = one member group (blockIdx.y)
+// and kEnsEPB consecutive elements (blockIdx.x).
 struct Lane {
-  int m;     // member
+  int m0;    // first member of the lane
   size_t M;  // member stride
   int w, W;  // warp, warps
   int lane;
 };
+template <int V>
 __device__ __forceinline__ Lane lane_of(const Dims& D) {
-  return Lane{(int)(blockIdx.y * 32 + (threadIdx.x & 31)), (size_t)D.M, (int)(threadIdx.x >> 5),
+  return Lane{(int)((blockIdx.y * 32 + (threadIdx.x & 31)) * V), (size_t)D.M, (int)(threadIdx.x >> 5),
               (int)(blockDim.x >> 5), (int)(threadIdx.x & 31)};
 }
 
@@ -62,41 +99,55 @@ inline dim3 grid_of(int n, const Dims& D, int bs, int* threads) {
   if (W < 1) W = 1;
   if (W > kMaxBS / 32) W = kMaxBS / 32;
   *threads = W * 32;
-  return dim3((unsigned)slots_for(n), (unsigned)D.G);
+  return dim3((unsigned)slots_for(n), (unsigned)(D.M / (32 * D.V)));
 }
 
-// Per-member partial sums of one block: the warps' values of each lane are
-// combined in a fixed order (FP32 TwoSum, or FP64) and lane m of warp 0
-// stores them.  Every thread of the block calls these (they synchronise).
-template <int N>
-__device__ __forceinline__ void block_partials_f(const Lane& L, const float (&v)[N], float* const (&dst)[N]) {
-  __shared__ float sh[N][kMaxBS / 32][32];
+// Per-member partial sums of one block: the warps' values of each member are
+// combined in a fixed order (FP32 TwoSum, or FP64) and warp 0 stores them.
+// Every thread of the block calls these (they synchronise).
+template <int N, int V>
+__device__ __forceinline__ void block_partials_f(const Lane& L, const float (&v)[N][V], float* const (&dst)[N]) {
+  __shared__ float sh[N][V][kMaxBS / 32][32];
 #pragma unroll
-  for (int k = 0; k < N; ++k) sh[k][L.w][L.lane] = v[k];
+  for (int k = 0; k < N; ++k)
+#pragma unroll
+    for (int c = 0; c < V; ++c) sh[k][c][L.w][L.lane] = v[k][c];
   __syncthreads();
   if (L.w == 0) {
 #pragma unroll
     for (int k = 0; k < N; ++k) {
       if (!dst[k]) continue;
-      float hi = 0.f, lo = 0.f;
-      for (int q = 0; q < L.W; ++q) two_sum_acc(hi, lo, sh[k][q][L.lane]);
-      dst[k][L.m] = hi + lo;
+      float o[V];
+#pragma unroll
+      for (int c = 0; c < V; ++c) {
+        float hi = 0.f, lo = 0.f;
+        for (int q = 0; q < L.W; ++q) two_sum_acc(hi, lo, sh[k][c][q][L.lane]);
+        o[c] = hi + lo;
+      }
+      stv<V>(dst[k], (size_t)L.m0, o);
     }
   }
   __syncthreads();
 }
-template <int N>
-__device__ __forceinline__ void block_partials_d(const Lane& L, const double (&v)[N], double* const (&dst)[N]) {
-  __shared__ double sh[N][kMaxBS / 32][32];
+template <int N, int V>
+__device__ __forceinline__ void block_partials_d(const Lane& L, const double (&v)[N][V], double* const (&dst)[N]) {
+  __shared__ double sh[N][V][kMaxBS / 32][32];
 #pragma unroll
-  for (int k = 0; k < N; ++k) sh[k][L.w][L.lane] = v[k];
+  for (int k = 0; k < N; ++k)
+#pragma unroll
+    for (int c = 0; c < V; ++c) sh[k][c][L.w][L.lane] = v[k][c];
   __syncthreads();
   if (L.w == 0) {
 #pragma unroll
     for (int k = 0; k < N; ++k) {
-      double a = 0.0;
-      for (int q = 0; q < L.W; ++q) a += sh[k][q][L.lane];
-      dst[k][L.m] = a;
+      double o[V];
+#pragma unroll
+      for (int c = 0; c < V; ++c) {
+        double a = 0.0;
+        for (int q = 0; q < L.W; ++q) a += sh[k][c][q][L.lane];
+        o[c] = a;
+      }
+      stv<V>(dst[k], (size_t)L.m0, o);
     }
   }
   __syncthreads();
@@ -105,13 +156,21 @@ __device__ __forceinline__ void block_partials_d(const Lane& L, const double (&v
 // Edge preparation of one edge (operators_mod.F90:93-104 c2e, :168-176
 // inverse IAP; mass flux u gd_edge, tmcore_swm_mod.F90:135), the FP32
 // single-model arithmetic.
-__device__ __forceinline__ void prep(float ia, float g1, float g2, float* gd_e, float* u, float* F, size_t em) {
-  const float ge = 0.5f * (g1 + g2);
+__device__ __forceinline__ void prep1(float ia, float g1, float g2, float& ge, float& uu, float& Fv) {
+  ge = 0.5f * (g1 + g2);
   const float sq = sqrtf(ge);
-  const float uu = ia / sq;
-  gd_e[em] = ge;
-  u[em] = uu;
-  F[em] = uu * ge;
+  uu = ia / sq;
+  Fv = uu * ge;
+}
+template <int V>
+__device__ __forceinline__ void prep(const float (&ia)[V], const float (&g1)[V], const float (&g2)[V], float* gd_e,
+                                     float* u, float* F, size_t em) {
+  float ge[V], uu[V], Fv[V];
+#pragma unroll
+  for (int c = 0; c < V; ++c) prep1(ia[c], g1[c], g2[c], ge[c], uu[c], Fv[c]);
+  stv<V>(gd_e, em, ge);
+  stv<V>(u, em, uu);
+  stv<V>(F, em, Fv);
 }
 
 // ---------------------------------------------------------------------------
@@ -119,6 +178,7 @@ __device__ __forceinline__ void prep(float ia, float g1, float g2, float* gd_e, 
 // E = ke + gd + ghs, RK update of gd (div_operator operators_mod.F90:40-55,
 // calc_kinetic_energy :206-221, calc_gd_tend_on_cell tmcore_swm_mod.F90:127-139)
 // ---------------------------------------------------------------------------
+template <int V>
 __global__ void __launch_bounds__(kMaxBS) k_ens_cell(DevMesh Mh, Dims D, IO S, RKStage rk, Partials P, int diag) {
   __shared__ int s_e[kME][kEnsEPB];
   __shared__ float s_ns[kME][kEnsEPB];
@@ -147,86 +207,103 @@ __global__ void __launch_bounds__(kMaxBS) k_ens_cell(DevMesh Mh, Dims D, IO S, R
     s_Af[j] = Mh.areaCell_f[c0 + j];
   }
   __syncthreads();
-  const Lane L = lane_of(D);
+  const Lane L = lane_of<V>(D);
   const size_t Mm = L.M;
-  const int m = L.m;
   const int mode = rk.mode;
-  float rip = 0.f, r44 = 0.f, eh = 0.f, el = 0.f;
-  double mass = 0.0;
+  float rip[V], r44[V], eh[V], el[V];
+  double mass[V];
+#pragma unroll
+  for (int c = 0; c < V; ++c) rip[c] = r44[c] = eh[c] = el[c] = 0.f, mass[c] = 0.0;
   for (int j = L.w; j < nel; j += L.W) {
-    const size_t cm = (size_t)(c0 + j) * Mm + m;
-    const double gold = (mode <= 3) ? S.gd_old[cm] : 0.0;
-    const double gacc = (mode >= 2) ? S.gd_acc[cm] : 0.0;
-    const float tprev = (mode >= 2) ? S.tendf[cm] : 0.f;
-    const float gdf = S.gdf_in[cm], ghf = S.ghsf[cm];
-    const double gdin = diag ? S.gd_in[cm] : 0.0;
-    float uu[kME], Fv[kME];
+    const size_t cm = (size_t)(c0 + j) * Mm + L.m0;
+    double gold[V], gacc[V], gdin[V];
+    float tprev[V], gdf[V], ghf[V];
+    if (mode <= 3) ldv<V>(S.gd_old, cm, gold);
+    if (mode >= 2) {
+      ldv<V>(S.gd_acc, cm, gacc);
+      ldv<V>(S.tendf, cm, tprev);
+    }
+    ldv<V>(S.gdf_in, cm, gdf);
+    ldv<V>(S.ghsf, cm, ghf);
+    if (diag) ldv<V>(S.gd_in, cm, gdin);
+    float uu[kME][V], Fv[kME][V];
 #pragma unroll
     for (int i = 0; i < kME; ++i) {
-      const size_t k = (size_t)s_e[i][j] * Mm + m;
-      uu[i] = S.u[k];
-      Fv[i] = S.F[k];
+      const size_t k = (size_t)s_e[i][j] * Mm + L.m0;
+      ldv<V>(S.u, k, uu[i]);
+      ldv<V>(S.F, k, Fv[i]);
     }
-    float hi = 0.f, lo = 0.f, k = 0.f;
+    double tn_acc[V], gnext[V];
+    float Eo[V], tT[V], gnf[V];
 #pragma unroll
-    for (int i = 0; i < kME; ++i) {
-      const float ns = s_ns[i][j];
-      two_sum_acc(hi, lo, __fmul_rn(__fmul_rn(ns, Fv[i]), s_dv[i][j]));
-      k += fabsf(ns) * uu[i] * uu[i] * s_ae[i][j];
-    }
-    const double t = -((double)hi + (double)lo) * s_invA[j];
-    const float tT = (float)t;
-    S.E[cm] = k * 0.25f * s_invAf[j] + gdf + ghf;
-    const float Af = s_Af[j];
-    double gnext = 0.0;
-    switch (mode) {
-      case 1:
-        S.gd_acc[cm] = t;
-        S.tendf[cm] = tT;
-        gnext = gold + rk.a_dt * t;
-        break;
-      case 2:
-      case 3:
-        rip += tprev * tT * Af;
-        S.gd_acc[cm] = gacc + 2.0 * t;
-        S.tendf[cm] = tT;
-        gnext = gold + rk.a_dt * t;
-        break;
-      default: {
-        rip += tprev * tT * Af;
-        const double tn = (gacc + t) * (1.0 / 6.0);
-        S.gd_acc[cm] = tn;
-        const float tnf = (float)tn;
-        r44 += tnf * tnf * Af;
-        S.tendf[cm] = tT;
+    for (int c = 0; c < V; ++c) {
+      float hi = 0.f, lo = 0.f, k = 0.f;
+#pragma unroll
+      for (int i = 0; i < kME; ++i) {
+        const float ns = s_ns[i][j];
+        two_sum_acc(hi, lo, __fmul_rn(__fmul_rn(ns, Fv[i][c]), s_dv[i][j]));
+        k += fabsf(ns) * uu[i][c] * uu[i][c] * s_ae[i][j];
+      }
+      const double t = -((double)hi + (double)lo) * s_invA[j];
+      tT[c] = (float)t;
+      Eo[c] = k * 0.25f * s_invAf[j] + gdf[c] + ghf[c];
+      const float Af = s_Af[j];
+      gnext[c] = 0.0;
+      switch (mode) {
+        case 1:
+          tn_acc[c] = t;
+          gnext[c] = gold[c] + rk.a_dt * t;
+          break;
+        case 2:
+        case 3:
+          rip[c] += tprev[c] * tT[c] * Af;
+          tn_acc[c] = gacc[c] + 2.0 * t;
+          gnext[c] = gold[c] + rk.a_dt * t;
+          break;
+        default: {
+          rip[c] += tprev[c] * tT[c] * Af;
+          const double tn = (gacc[c] + t) * (1.0 / 6.0);
+          tn_acc[c] = tn;
+          const float tnf = (float)tn;
+          r44[c] += tnf * tnf * Af;
+        }
+      }
+      gnf[c] = (float)gnext[c];
+      if (diag) {
+        // total mass (FP64 gd), and the cell part of the total energy
+        // (gd^2 + 2 gd ghs) areaCell from FP32 terms, compensated
+        // (tmcore_swm_mod.F90:215-231)
+        mass[c] = mass[c] + gdin[c] * s_A[j];
+        two_sum_acc(eh[c], el[c], gdf[c] * (gdf[c] + 2.f * ghf[c]) * Af);
       }
     }
+    stv<V>(S.E, cm, Eo);
+    stv<V>(S.gd_acc, cm, tn_acc);
+    stv<V>(S.tendf, cm, tT);
     if (mode <= 3) {
-      S.gd_next[cm] = gnext;
-      S.gdf_next[cm] = (float)gnext;
-    }
-    if (diag) {
-      // total mass (FP64 gd), and the cell part of the total energy
-      // (gd^2 + 2 gd ghs) areaCell from FP32 terms, compensated
-      // (tmcore_swm_mod.F90:215-231)
-      mass = mass + gdin * s_A[j];
-      two_sum_acc(eh, el, gdf * (gdf + 2.f * ghf) * Af);
+      stv<V>(S.gd_next, cm, gnext);
+      stv<V>(S.gdf_next, cm, gnf);
     }
   }
   const int slot = blockIdx.x;
   if (mode >= 2) {
-    const float v[2] = {rip, r44};
+    float v[2][V];
+#pragma unroll
+    for (int c = 0; c < V; ++c) v[0][c] = rip[c], v[1][c] = r44[c];
     float* const dst[2] = {P.f(R_IP_C + 2 * (mode - 2), slot), mode == 4 ? P.f(R_44_C, slot) : nullptr};
-    block_partials_f<2>(L, v, dst);
+    block_partials_f<2, V>(L, v, dst);
   }
   if (diag) {
-    const double v[2] = {mass, (double)eh + (double)el};
+    double v[2][V];
+#pragma unroll
+    for (int c = 0; c < V; ++c) v[0][c] = mass[c], v[1][c] = (double)eh[c] + (double)el[c];
     double* const dst[2] = {P.d(R_MASS, slot), P.d(R_EN_C, slot)};
-    block_partials_d<2>(L, v, dst);
+    block_partials_d<2, V>(L, v, dst);
   }
 }
 
 // invariants of a state only (the diagnostic pass): mass and cell energy
+template <int V>
 __global__ void __launch_bounds__(kMaxBS) k_ens_cell_diag(DevMesh Mh, Dims D, IO S, Partials P) {
   __shared__ double s_A[kEnsEPB];
   __shared__ float s_Af[kEnsEPB];
@@ -236,28 +313,38 @@ __global__ void __launch_bounds__(kMaxBS) k_ens_cell_diag(DevMesh Mh, Dims D, IO
     s_Af[j] = Mh.areaCell_f[c0 + j];
   }
   __syncthreads();
-  const Lane L = lane_of(D);
-  float eh = 0.f, el = 0.f;
-  double mass = 0.0;
+  const Lane L = lane_of<V>(D);
+  float eh[V], el[V];
+  double mass[V];
+#pragma unroll
+  for (int c = 0; c < V; ++c) eh[c] = el[c] = 0.f, mass[c] = 0.0;
   for (int j = L.w; j < nel; j += L.W) {
-    const size_t cm = (size_t)(c0 + j) * L.M + L.m;
-    const double gdin = S.gd_in[cm];
-    const float gdf = S.gdf_in[cm], ghf = S.ghsf[cm];
-    mass = mass + gdin * s_A[j];
-    two_sum_acc(eh, el, gdf * (gdf + 2.f * ghf) * s_Af[j]);
+    const size_t cm = (size_t)(c0 + j) * L.M + L.m0;
+    double gdin[V];
+    float gdf[V], ghf[V];
+    ldv<V>(S.gd_in, cm, gdin);
+    ldv<V>(S.gdf_in, cm, gdf);
+    ldv<V>(S.ghsf, cm, ghf);
+#pragma unroll
+    for (int c = 0; c < V; ++c) {
+      mass[c] = mass[c] + gdin[c] * s_A[j];
+      two_sum_acc(eh[c], el[c], gdf[c] * (gdf[c] + 2.f * ghf[c]) * s_Af[j]);
+    }
   }
-  const double v[2] = {mass, (double)eh + (double)el};
+  double v[2][V];
+#pragma unroll
+  for (int c = 0; c < V; ++c) v[0][c] = mass[c], v[1][c] = (double)eh[c] + (double)el[c];
   double* const dst[2] = {P.d(R_MASS, blockIdx.x), P.d(R_EN_C, blockIdx.x)};
-  block_partials_d<2>(L, v, dst);
+  block_partials_d<2, V>(L, v, dst);
 }
 
 // ---------------------------------------------------------------------------
 // vertex: gd on vertices, vorticity, pv (operators_mod.F90:106-123, :76-91,
 // :262-270); potential enstrophy and absolute vorticity on diag stages
 // ---------------------------------------------------------------------------
-constexpr int kVU = 2;  // vertices per warp iteration (loads of all first)
-
+template <int V>
 __global__ void __launch_bounds__(kMaxBS) k_ens_vertex(DevMesh Mh, Dims D, IO S, Partials P, int diag) {
+  constexpr int kVU = 2;  // vertices per warp iteration (loads of both first)
   __shared__ int s_c[3][kEnsEPB];
   __shared__ int s_e[3][kEnsEPB];
   __shared__ float s_kt[3][kEnsEPB];
@@ -285,19 +372,20 @@ __global__ void __launch_bounds__(kMaxBS) k_ens_vertex(DevMesh Mh, Dims D, IO S,
     s_At[j] = (float)Mh.areaTriangle[v0 + j];
   }
   __syncthreads();
-  const Lane L = lane_of(D);
+  const Lane L = lane_of<V>(D);
   const size_t Mm = L.M;
-  const int m = L.m;
-  float ph = 0.f, pl = 0.f, ah = 0.f, al = 0.f;
+  float ph[V], pl[V], ah[V], al[V];
+#pragma unroll
+  for (int c = 0; c < V; ++c) ph[c] = pl[c] = ah[c] = al[c] = 0.f;
   for (int base = L.w; base < nel; base += L.W * kVU) {
-    float g[kVU][3], uu[kVU][3];
+    float g[kVU][3][V], uu[kVU][3][V];
 #pragma unroll
     for (int q = 0; q < kVU; ++q) {
       const int j = min(base + q * L.W, nel - 1);
 #pragma unroll
       for (int i = 0; i < 3; ++i) {
-        g[q][i] = S.gdf_in[(size_t)s_c[i][j] * Mm + m];
-        uu[q][i] = S.u[(size_t)s_e[i][j] * Mm + m];
+        ldv<V>(S.gdf_in, (size_t)s_c[i][j] * Mm + L.m0, g[q][i]);
+        ldv<V>(S.u, (size_t)s_e[i][j] * Mm + L.m0, uu[q][i]);
       }
     }
 #pragma unroll
@@ -305,37 +393,43 @@ __global__ void __launch_bounds__(kMaxBS) k_ens_vertex(DevMesh Mh, Dims D, IO S,
       const int j = base + q * L.W;
       if (j >= nel) break;
       const float iA = s_iA[j];
-      const float gv = (g[q][0] * s_kt[0][j] + g[q][1] * s_kt[1][j] + g[q][2] * s_kt[2][j]) * iA;
-      const float sv = s_ts[0][j] * uu[q][0] * s_dc[0][j] + s_ts[1][j] * uu[q][1] * s_dc[1][j] +
-                       s_ts[2][j] * uu[q][2] * s_dc[2][j];
-      const float vo = -sv * iA;
-      const float pv = (s_f[j] + vo) / gv;
-      const size_t vm = (size_t)(v0 + j) * Mm + m;
-      S.pv_v[vm] = pv;
-      if (S.vor) S.vor[vm] = vo;
-      if (S.gd_v) S.gd_v[vm] = gv;
-      if (diag) {
-        // potential enstrophy and absolute vorticity (tmcore_swm_mod.F90:233-255),
-        // FP32 terms, compensated; vorticity and f as separate terms
-        two_sum_acc(ph, pl, gv * (pv * pv) * s_At[j]);
-        two_sum_acc(ah, al, vo * s_At[j]);
-        two_sum_acc(ah, al, s_f[j] * s_At[j]);
+      float pv[V], vo[V], gv[V];
+#pragma unroll
+      for (int c = 0; c < V; ++c) {
+        gv[c] = (g[q][0][c] * s_kt[0][j] + g[q][1][c] * s_kt[1][j] + g[q][2][c] * s_kt[2][j]) * iA;
+        const float sv = s_ts[0][j] * uu[q][0][c] * s_dc[0][j] + s_ts[1][j] * uu[q][1][c] * s_dc[1][j] +
+                         s_ts[2][j] * uu[q][2][c] * s_dc[2][j];
+        vo[c] = -sv * iA;
+        pv[c] = (s_f[j] + vo[c]) / gv[c];
+        if (diag) {
+          // potential enstrophy and absolute vorticity (tmcore_swm_mod.F90:233-255),
+          // FP32 terms, compensated; vorticity and f as separate terms
+          two_sum_acc(ph[c], pl[c], gv[c] * (pv[c] * pv[c]) * s_At[j]);
+          two_sum_acc(ah[c], al[c], vo[c] * s_At[j]);
+          two_sum_acc(ah[c], al[c], s_f[j] * s_At[j]);
+        }
       }
+      const size_t vm = (size_t)(v0 + j) * Mm + L.m0;
+      stv<V>(S.pv_v, vm, pv);
+      if (S.vor) stv<V>(S.vor, vm, vo);
+      if (S.gd_v) stv<V>(S.gd_v, vm, gv);
     }
   }
   if (diag) {
-    const double v[2] = {(double)ph + (double)pl, (double)ah + (double)al};
+    double v[2][V];
+#pragma unroll
+    for (int c = 0; c < V; ++c) v[0][c] = (double)ph[c] + (double)pl[c], v[1][c] = (double)ah[c] + (double)al[c];
     double* const dst[2] = {P.d(R_PE, blockIdx.x), P.d(R_AV, blockIdx.x)};
-    block_partials_d<2>(L, v, dst);
+    block_partials_d<2, V>(L, v, dst);
   }
 }
 
 // ---------------------------------------------------------------------------
 // edge_pv: centred pv on edges (APVM weight 0, operators_mod.F90:296-316)
 // ---------------------------------------------------------------------------
-constexpr int kPU = 4;
-
+template <int V>
 __global__ void __launch_bounds__(kMaxBS) k_ens_edge_pv(DevMesh Mh, Dims D, IO S) {
+  constexpr int kPU = 4;
   __shared__ int s_v[2][kEnsEPB];
   const int ne = Mh.ne, e0 = blockIdx.x * kEnsEPB, nel = min(kEnsEPB, ne - e0);
   for (int t = threadIdx.x; t < 2 * kEnsEPB; t += blockDim.x) {
@@ -343,22 +437,24 @@ __global__ void __launch_bounds__(kMaxBS) k_ens_edge_pv(DevMesh Mh, Dims D, IO S
     if (j < nel) s_v[i][j] = Mh.verticesOnEdge[(size_t)i * ne + e0 + j];
   }
   __syncthreads();
-  const Lane L = lane_of(D);
+  const Lane L = lane_of<V>(D);
   const size_t Mm = L.M;
-  const int m = L.m;
   for (int base = L.w; base < nel; base += L.W * kPU) {
-    float p1[kPU], p2[kPU];
+    float p1[kPU][V], p2[kPU][V];
 #pragma unroll
     for (int q = 0; q < kPU; ++q) {
       const int j = min(base + q * L.W, nel - 1);
-      p1[q] = S.pv_v[(size_t)s_v[0][j] * Mm + m];
-      p2[q] = S.pv_v[(size_t)s_v[1][j] * Mm + m];
+      ldv<V>(S.pv_v, (size_t)s_v[0][j] * Mm + L.m0, p1[q]);
+      ldv<V>(S.pv_v, (size_t)s_v[1][j] * Mm + L.m0, p2[q]);
     }
 #pragma unroll
     for (int q = 0; q < kPU; ++q) {
       const int j = base + q * L.W;
       if (j >= nel) break;
-      S.pv_e[(size_t)(e0 + j) * Mm + m] = 0.5f * (p1[q] + p2[q]);
+      float pe[V];
+#pragma unroll
+      for (int c = 0; c < V; ++c) pe[c] = 0.5f * (p1[q][c] + p2[q][c]);
+      stv<V>(S.pv_e, (size_t)(e0 + j) * Mm + L.m0, pe);
     }
   }
 }
@@ -370,6 +466,7 @@ __global__ void __launch_bounds__(kMaxBS) k_ens_edge_pv(DevMesh Mh, Dims D, IO S
 // and the CRK4 inner products (time_scheme_mod.F90:109-154); stages 1-3 also
 // prepare the next stage's gd_edge, u and F from its gd and iap_u.
 // ---------------------------------------------------------------------------
+template <int V>
 __global__ void __launch_bounds__(kMaxBS) k_ens_edge_flux(DevMesh Mh, Dims D, IO S, RKStage rk, Partials P) {
   __shared__ int s_ep[kME2][kEnsEPB];
   __shared__ float s_w[kME2][kEnsEPB];
@@ -394,77 +491,87 @@ __global__ void __launch_bounds__(kMaxBS) k_ens_edge_flux(DevMesh Mh, Dims D, IO
     s_ae[j] = Mh.areaEdge_f[e0 + j];
   }
   __syncthreads();
-  const Lane L = lane_of(D);
+  const Lane L = lane_of<V>(D);
   const size_t Mm = L.M;
-  const int m = L.m;
   const int mode = rk.mode;
   const bool fuse = S.u_nx != nullptr;
   const float adt = (float)rk.a_dt;
-  float rip = 0.f, r44 = 0.f;
+  float rip[V], r44[V];
+#pragma unroll
+  for (int c = 0; c < V; ++c) rip[c] = r44[c] = 0.f;
   for (int j = L.w; j < nel; j += L.W) {
-    const size_t em = (size_t)(e0 + j) * Mm + m;
-    const size_t c1m = (size_t)s_c[0][j] * Mm + m, c2m = (size_t)s_c[1][j] * Mm + m;
-    const float pe = S.pv_e[em];
-    const float uu = S.u[em];
-    const float ge = S.gd_e[em];
-    const float tp = (mode >= 2) ? S.iap_tend[em] : 0.f;
-    const float accv = (mode >= 2) ? S.iap_acc[em] : 0.f;
-    const float oldv = (mode >= 1 && mode <= 3) ? S.iap_old[em] : 0.f;
-    float gn1 = 0.f, gn2 = 0.f;
-    if (fuse) {
-      gn1 = S.gdf_next[c1m];
-      gn2 = S.gdf_next[c2m];
+    const size_t em = (size_t)(e0 + j) * Mm + L.m0;
+    const size_t c1m = (size_t)s_c[0][j] * Mm + L.m0, c2m = (size_t)s_c[1][j] * Mm + L.m0;
+    float pe[V], uu[V], ge[V], tp[V], accv[V], oldv[V], gn1[V], gn2[V], E1[V], E2[V], t1[V], t2[V];
+    ldv<V>(S.pv_e, em, pe);
+    ldv<V>(S.u, em, uu);
+    ldv<V>(S.gd_e, em, ge);
+    if (mode >= 2) {
+      ldv<V>(S.iap_tend, em, tp);
+      ldv<V>(S.iap_acc, em, accv);
     }
-    const float E1 = S.E[c1m], E2 = S.E[c2m], t1 = S.tendf[c1m], t2 = S.tendf[c2m];
-    float Fv[kME2], pp[kME2];
+    if (mode >= 1 && mode <= 3) ldv<V>(S.iap_old, em, oldv);
+    if (fuse) {
+      ldv<V>(S.gdf_next, c1m, gn1);
+      ldv<V>(S.gdf_next, c2m, gn2);
+    }
+    ldv<V>(S.E, c1m, E1);
+    ldv<V>(S.E, c2m, E2);
+    ldv<V>(S.tendf, c1m, t1);
+    ldv<V>(S.tendf, c2m, t2);
+    float Fv[kME2][V], pp[kME2][V];
 #pragma unroll
     for (int i = 0; i < kME2; ++i) {
-      const size_t k = (size_t)s_ep[i][j] * Mm + m;
-      Fv[i] = S.F[k];
-      pp[i] = S.pv_e[k];
+      const size_t k = (size_t)s_ep[i][j] * Mm + L.m0;
+      ldv<V>(S.F, k, Fv[i]);
+      ldv<V>(S.pv_e, k, pp[i]);
     }
-    float s = 0.f;
+    const float dc = s_dc[j], ae = s_ae[j];
+    float acc_o[V], it_o[V], inext[V];
 #pragma unroll
-    for (int i = 0; i < kME2; ++i) s += s_w[i][j] * Fv[i] * (0.5f * (pe + pp[i]));
-    const float dc = s_dc[j];
-    const float dEdx = (E2 - E1) / dc;
-    const float tge = 0.5f * (t1 + t2);
-    const float ut = s - dEdx;
-    const float sq = sqrtf(ge);
-    const float it = sq * ut + 0.5f * uu / sq * tge;
-    const float ae = s_ae[j];
-    float inext = 0.f;
-    switch (mode) {
-      case 1:
-        S.iap_acc[em] = it;
-        S.iap_tend[em] = it;
-        inext = oldv + adt * it;
-        break;
-      case 2:
-      case 3:
-        rip = rip + tp * it * ae;
-        S.iap_acc[em] = accv + 2.f * it;
-        S.iap_tend[em] = it;
-        inext = oldv + adt * it;
-        break;
-      default: {
-        rip = rip + tp * it * ae;
-        const float tn = (accv + it) * (1.0f / 6.0f);
-        S.iap_acc[em] = tn;
-        r44 = r44 + tn * tn * ae;
-        S.iap_tend[em] = it;
+    for (int c = 0; c < V; ++c) {
+      float s = 0.f;
+#pragma unroll
+      for (int i = 0; i < kME2; ++i) s += s_w[i][j] * Fv[i][c] * (0.5f * (pe[c] + pp[i][c]));
+      const float dEdx = (E2[c] - E1[c]) / dc;
+      const float tge = 0.5f * (t1[c] + t2[c]);
+      const float ut = s - dEdx;
+      const float sq = sqrtf(ge[c]);
+      const float it = sq * ut + 0.5f * uu[c] / sq * tge;
+      it_o[c] = it;
+      inext[c] = 0.f;
+      switch (mode) {
+        case 1:
+          acc_o[c] = it;
+          inext[c] = oldv[c] + adt * it;
+          break;
+        case 2:
+        case 3:
+          rip[c] = rip[c] + tp[c] * it * ae;
+          acc_o[c] = accv[c] + 2.f * it;
+          inext[c] = oldv[c] + adt * it;
+          break;
+        default: {
+          rip[c] = rip[c] + tp[c] * it * ae;
+          const float tn = (accv[c] + it) * (1.0f / 6.0f);
+          acc_o[c] = tn;
+          r44[c] = r44[c] + tn * tn * ae;
+        }
       }
     }
+    stv<V>(S.iap_acc, em, acc_o);
+    stv<V>(S.iap_tend, em, it_o);
     if (fuse)
-      prep(inext, gn1, gn2, S.gd_e_nx, S.u_nx, S.F_nx, em);
+      prep<V>(inext, gn1, gn2, S.gd_e_nx, S.u_nx, S.F_nx, em);
     else if (mode <= 3)
-      S.iap_next[em] = inext;
+      stv<V>(S.iap_next, em, inext);
   }
   if (mode >= 2) {
-    const int slot = blockIdx.x;
-    const float v[2] = {rip, r44};
-    float* const dst[2] = {P.f(R_IP_E + 2 * (mode - 2), slot), mode == 4 ? P.f(R_44_E, slot) : nullptr};
-    block_partials_f<2>(L, v, dst);
+    float v[2][V];
+#pragma unroll
+    for (int c = 0; c < V; ++c) v[0][c] = rip[c], v[1][c] = r44[c];
+    float* const dst[2] = {P.f(R_IP_E + 2 * (mode - 2), blockIdx.x), mode == 4 ? P.f(R_44_E, blockIdx.x) : nullptr};
+    block_partials_f<2, V>(L, v, dst);
   }
 }
 
@@ -474,37 +581,47 @@ __global__ void __launch_bounds__(kMaxBS) k_ens_edge_flux(DevMesh Mh, Dims D, IO
 // ---------------------------------------------------------------------------
 constexpr int kFU = 4;
 
+template <int V>
 __global__ void __launch_bounds__(kMaxBS) k_ens_final_cells(DevMesh Mh, Dims D, IO S, const double* diag) {
-  const Lane L = lane_of(D);
+  const Lane L = lane_of<V>(D);
   const size_t Mm = L.M;
-  const int m = L.m;
-  const double bdt = diag[(size_t)m * kDiagStride + 9];
+  double bdt[V];
+#pragma unroll
+  for (int c = 0; c < V; ++c) bdt[c] = diag[(size_t)(L.m0 + c) * kDiagStride + 9];
   const int nc = Mh.nc, c0 = blockIdx.x * kEnsEPB, nel = min(kEnsEPB, nc - c0);
   double* gd = const_cast<double*>(S.gd_old);
   float* gdf = const_cast<float*>(S.gdf_in);
   for (int base = L.w; base < nel; base += L.W * kFU) {
-    double g[kFU];
+    double g[kFU][V], a[kFU][V];
 #pragma unroll
     for (int q = 0; q < kFU; ++q) {
-      const size_t cm = (size_t)(c0 + min(base + q * L.W, nel - 1)) * Mm + m;
-      g[q] = gd[cm] + bdt * S.gd_acc[cm];
+      const size_t cm = (size_t)(c0 + min(base + q * L.W, nel - 1)) * Mm + L.m0;
+      ldv<V>(gd, cm, g[q]);
+      ldv<V>(S.gd_acc, cm, a[q]);
     }
 #pragma unroll
     for (int q = 0; q < kFU; ++q) {
       const int j = base + q * L.W;
       if (j >= nel) break;
-      const size_t cm = (size_t)(c0 + j) * Mm + m;
-      gd[cm] = g[q];
-      gdf[cm] = (float)g[q];
+      const size_t cm = (size_t)(c0 + j) * Mm + L.m0;
+      double gn[V];
+      float gf[V];
+#pragma unroll
+      for (int c = 0; c < V; ++c) {
+        gn[c] = g[q][c] + bdt[c] * a[q][c];
+        gf[c] = (float)gn[c];
+      }
+      stv<V>(gd, cm, gn);
+      stv<V>(gdf, cm, gf);
     }
   }
 }
 
 // Edges: iap_u of state(old) in place, then the edge preparation of the next
 // step's first stage and the edge energy iap_u^2 areaEdge of the new state
-// (tmcore_swm_mod.F90:229), FP32 terms, compensated.  `update` false: the
-// stand-alone edge preparation of S.iap_in (energy only when `diag`).
-template <bool kUpdate>
+// (tmcore_swm_mod.F90:229), FP32 terms, compensated.  kUpdate false: the
+// stand-alone edge preparation of S.iap_in (energy only when want_energy).
+template <int V, bool kUpdate>
 __global__ void __launch_bounds__(kMaxBS) k_ens_edges(DevMesh Mh, Dims D, IO S, const double* diag, Partials P,
                                                       int want_energy) {
   __shared__ int s_c[2][kEnsEPB];
@@ -516,36 +633,49 @@ __global__ void __launch_bounds__(kMaxBS) k_ens_edges(DevMesh Mh, Dims D, IO S, 
   }
   for (int j = threadIdx.x; j < nel; j += blockDim.x) s_ae[j] = Mh.areaEdge_f[e0 + j];
   __syncthreads();
-  const Lane L = lane_of(D);
+  const Lane L = lane_of<V>(D);
   const size_t Mm = L.M;
-  const int m = L.m;
-  const float bdt = kUpdate ? (float)diag[(size_t)m * kDiagStride + 9] : 0.f;
+  float bdt[V];
+#pragma unroll
+  for (int c = 0; c < V; ++c) bdt[c] = kUpdate ? (float)diag[(size_t)(L.m0 + c) * kDiagStride + 9] : 0.f;
   float* iap = const_cast<float*>(kUpdate ? S.iap_old : S.iap_in);
-  float eh = 0.f, el = 0.f;
+  float eh[V], el[V];
+#pragma unroll
+  for (int c = 0; c < V; ++c) eh[c] = el[c] = 0.f;
   for (int base = L.w; base < nel; base += L.W * kFU) {
-    float ia[kFU], g1[kFU], g2[kFU];
+    float ia[kFU][V], ac[kFU][V], g1[kFU][V], g2[kFU][V];
 #pragma unroll
     for (int q = 0; q < kFU; ++q) {
       const int j = min(base + q * L.W, nel - 1);
-      const size_t em = (size_t)(e0 + j) * Mm + m;
-      ia[q] = kUpdate ? iap[em] + bdt * S.iap_acc[em] : iap[em];
-      g1[q] = S.gdf_in[(size_t)s_c[0][j] * Mm + m];
-      g2[q] = S.gdf_in[(size_t)s_c[1][j] * Mm + m];
+      const size_t em = (size_t)(e0 + j) * Mm + L.m0;
+      ldv<V>(iap, em, ia[q]);
+      if (kUpdate) ldv<V>(S.iap_acc, em, ac[q]);
+      ldv<V>(S.gdf_in, (size_t)s_c[0][j] * Mm + L.m0, g1[q]);
+      ldv<V>(S.gdf_in, (size_t)s_c[1][j] * Mm + L.m0, g2[q]);
     }
 #pragma unroll
     for (int q = 0; q < kFU; ++q) {
       const int j = base + q * L.W;
       if (j >= nel) break;
-      const size_t em = (size_t)(e0 + j) * Mm + m;
-      if (kUpdate) iap[em] = ia[q];
-      prep(ia[q], g1[q], g2[q], const_cast<float*>(S.gd_e), const_cast<float*>(S.u), const_cast<float*>(S.F), em);
-      if (want_energy) two_sum_acc(eh, el, ia[q] * ia[q] * s_ae[j]);
+      const size_t em = (size_t)(e0 + j) * Mm + L.m0;
+      if (kUpdate) {
+#pragma unroll
+        for (int c = 0; c < V; ++c) ia[q][c] = ia[q][c] + bdt[c] * ac[q][c];
+        stv<V>(iap, em, ia[q]);
+      }
+      prep<V>(ia[q], g1[q], g2[q], const_cast<float*>(S.gd_e), const_cast<float*>(S.u), const_cast<float*>(S.F),
+              em);
+      if (want_energy)
+#pragma unroll
+        for (int c = 0; c < V; ++c) two_sum_acc(eh[c], el[c], ia[q][c] * ia[q][c] * s_ae[j]);
     }
   }
   if (want_energy) {
-    const double v[1] = {(double)eh + (double)el};
+    double v[1][V];
+#pragma unroll
+    for (int c = 0; c < V; ++c) v[0][c] = (double)eh[c] + (double)el[c];
     double* const dst[1] = {P.d(R_EN_E, blockIdx.x)};
-    block_partials_d<1>(L, v, dst);
+    block_partials_d<1, V>(L, v, dst);
   }
 }
 
@@ -652,43 +782,67 @@ void launch_cell(const DevMesh& Mh, const Dims& D, const IO& S, RKStage rk, cons
                  cudaStream_t st) {
   int th;
   const dim3 g = grid_of(Mh.nc, D, bs, &th);
-  k_ens_cell<<<g, th, 0, st>>>(Mh, D, S, rk, P, diag ? 1 : 0);
+  if (D.V == 2)
+    k_ens_cell<2><<<g, th, 0, st>>>(Mh, D, S, rk, P, diag ? 1 : 0);
+  else
+    k_ens_cell<1><<<g, th, 0, st>>>(Mh, D, S, rk, P, diag ? 1 : 0);
 }
 void launch_cell_diag(const DevMesh& Mh, const Dims& D, const IO& S, const Partials& P, int bs, cudaStream_t st) {
   int th;
   const dim3 g = grid_of(Mh.nc, D, bs, &th);
-  k_ens_cell_diag<<<g, th, 0, st>>>(Mh, D, S, P);
+  if (D.V == 2)
+    k_ens_cell_diag<2><<<g, th, 0, st>>>(Mh, D, S, P);
+  else
+    k_ens_cell_diag<1><<<g, th, 0, st>>>(Mh, D, S, P);
 }
 void launch_vertex(const DevMesh& Mh, const Dims& D, const IO& S, const Partials& P, bool diag, int bs,
                    cudaStream_t st) {
   int th;
   const dim3 g = grid_of(Mh.nv, D, bs, &th);
-  k_ens_vertex<<<g, th, 0, st>>>(Mh, D, S, P, diag ? 1 : 0);
+  if (D.V == 2)
+    k_ens_vertex<2><<<g, th, 0, st>>>(Mh, D, S, P, diag ? 1 : 0);
+  else
+    k_ens_vertex<1><<<g, th, 0, st>>>(Mh, D, S, P, diag ? 1 : 0);
 }
 void launch_edge_pv(const DevMesh& Mh, const Dims& D, const IO& S, int bs, cudaStream_t st) {
   int th;
   const dim3 g = grid_of(Mh.ne, D, bs, &th);
-  k_ens_edge_pv<<<g, th, 0, st>>>(Mh, D, S);
+  if (D.V == 2)
+    k_ens_edge_pv<2><<<g, th, 0, st>>>(Mh, D, S);
+  else
+    k_ens_edge_pv<1><<<g, th, 0, st>>>(Mh, D, S);
 }
 void launch_edge_flux(const DevMesh& Mh, const Dims& D, const IO& S, RKStage rk, const Partials& P, int bs,
                       cudaStream_t st) {
   int th;
   const dim3 g = grid_of(Mh.ne, D, bs, &th);
-  k_ens_edge_flux<<<g, th, 0, st>>>(Mh, D, S, rk, P);
+  if (D.V == 2)
+    k_ens_edge_flux<2><<<g, th, 0, st>>>(Mh, D, S, rk, P);
+  else
+    k_ens_edge_flux<1><<<g, th, 0, st>>>(Mh, D, S, rk, P);
 }
 void launch_final(const DevMesh& Mh, const Dims& D, const IO& S, const double* diag, const Partials& P, int bs,
                   cudaStream_t st) {
   int th;
   const dim3 gc = grid_of(Mh.nc, D, bs, &th);
-  k_ens_final_cells<<<gc, th, 0, st>>>(Mh, D, S, diag);
+  if (D.V == 2)
+    k_ens_final_cells<2><<<gc, th, 0, st>>>(Mh, D, S, diag);
+  else
+    k_ens_final_cells<1><<<gc, th, 0, st>>>(Mh, D, S, diag);
   const dim3 ge = grid_of(Mh.ne, D, bs, &th);
-  k_ens_edges<true><<<ge, th, 0, st>>>(Mh, D, S, diag, P, 1);
+  if (D.V == 2)
+    k_ens_edges<2, true><<<ge, th, 0, st>>>(Mh, D, S, diag, P, 1);
+  else
+    k_ens_edges<1, true><<<ge, th, 0, st>>>(Mh, D, S, diag, P, 1);
 }
 void launch_edge_prep(const DevMesh& Mh, const Dims& D, const IO& S, const Partials& P, bool diag, int bs,
                       cudaStream_t st) {
   int th;
   const dim3 g = grid_of(Mh.ne, D, bs, &th);
-  k_ens_edges<false><<<g, th, 0, st>>>(Mh, D, S, nullptr, P, diag ? 1 : 0);
+  if (D.V == 2)
+    k_ens_edges<2, false><<<g, th, 0, st>>>(Mh, D, S, nullptr, P, diag ? 1 : 0);
+  else
+    k_ens_edges<1, false><<<g, th, 0, st>>>(Mh, D, S, nullptr, P, diag ? 1 : 0);
 }
 void launch_finalize(const Dims& D, const Partials& P, bool step, bool diag, bool conserve, double totalArea,
                      double sumAreaTriangle, double dt, double* diag_out, cudaStream_t st) {

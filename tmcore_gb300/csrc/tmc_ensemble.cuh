@@ -35,6 +35,7 @@ constexpr int kEnsEPB = 64;  // elements per block (and per partial-sum slot)
 struct Dims {
   int M;  // members (a multiple of 32)
   int G;  // member groups of 32
+  int V;  // members per lane: 2 when M is a multiple of 64, else 1
   int slots_c, slots_e, slots_v;  // partial slots: blocks along cells, edges, vertices
 };
 
