@@ -651,22 +651,24 @@ struct Engine : EngineBase {
 
 // Member-innermost ensemble engine (tmc_params.member_layout = 1): the
 // same CRK4 stage program as Engine<float> on arrays [element][member]
-// (tmc_ensemble.cuh).  State slots old, A, B for gd and its FP32 shadow;
-// iap_u lives in slot old only (the fused stages keep the next stage's iap_u
-// in registers and store its edge preparation instead).
+// (tmc_ensemble.cuh).  State slots old, A, B for gd (double-float: the FP32
+// h halves are what the stencils read); iap_u lives in slot old only (the
+// fused stages keep the next stage's iap_u in registers and store its edge
+// preparation instead).
 struct EnsEngine : EngineBase {
   tmc_handle* h;
   ens::Dims D{};
   ens::Partials EP{};
-  double* gd[3] = {};
-  float* gdf[3] = {};
+  float* gd[3] = {};  // FF: [2][nCells * M]
   float* iap0 = nullptr;
-  double *gd_acc = nullptr, *ghs = nullptr;
+  float* gd_acc = nullptr;  // FF
+  double* ghs = nullptr;
   float *iap_acc = nullptr, *iap_tend = nullptr, *tendf = nullptr, *ghsf = nullptr;
   float* gd_e[2] = {};
   float* u[2] = {};
   float* F[2] = {};
   float *E = nullptr, *pv_v = nullptr, *vor = nullptr, *gd_v = nullptr, *pv_e = nullptr;
+  float *invA_hl = nullptr, *A_hl = nullptr;
   explicit EnsEngine(tmc_handle* hh) : h(hh) {}
 
   int alloc() override {
@@ -682,12 +684,9 @@ struct EnsEngine : EngineBase {
     EP.M = D.M;
     EP.sf = h->dalloc<float>((size_t)(R_44_E + 1) * EP.cap * M_);
     EP.sd = h->dalloc<double>((size_t)(R_AV - R_MASS + 1) * EP.cap * M_);
-    for (int i = 0; i < 3; ++i) {
-      gd[i] = h->dalloc<double>(nc);
-      gdf[i] = h->dalloc<float>(nc);
-    }
+    for (int i = 0; i < 3; ++i) gd[i] = h->dalloc<float>(2 * nc);
     iap0 = h->dalloc<float>(ne);
-    gd_acc = h->dalloc<double>(nc);
+    gd_acc = h->dalloc<float>(2 * nc);
     ghs = h->dalloc<double>(nc);
     ghsf = h->dalloc<float>(nc);
     tendf = h->dalloc<float>(nc);
@@ -703,7 +702,19 @@ struct EnsEngine : EngineBase {
     vor = h->dalloc<float>(nv);
     gd_v = h->dalloc<float>(nv);
     pv_e = h->dalloc<float>(ne);
-    if (!EP.sf || !EP.sd || !pv_e || !F[1] || !gd_v) return TMC_E_CUDA;
+    // 1 / areaCell and areaCell as double-float pairs [2][nCells]
+    const int ncell = h->M.nc;
+    std::vector<float> ia(2 * (size_t)ncell), a(2 * (size_t)ncell);
+    for (int c = 0; c < ncell; ++c) {
+      const double A = h->hm.areaCell[c], iA = 1.0 / A;
+      ia[c] = (float)iA;
+      ia[ncell + c] = (float)(iA - (double)ia[c]);
+      a[c] = (float)A;
+      a[ncell + c] = (float)(A - (double)a[c]);
+    }
+    invA_hl = h->upload(ia);
+    A_hl = h->upload(a);
+    if (!EP.sf || !EP.sd || !pv_e || !F[1] || !gd_v || !invA_hl || !A_hl) return TMC_E_CUDA;
     cudaMemset(ghs, 0, sizeof(double) * nc);
     cudaMemset(ghsf, 0, sizeof(float) * nc);
     return TMC_OK;
@@ -725,11 +736,8 @@ struct EnsEngine : EngineBase {
     s.iap_next = nullptr;
     s.iap_acc = iap_acc;
     s.iap_tend = iap_tend;
-    s.gdf_in = gdf[in_slot[k]];
-    s.gdf_next = next_slot[k] >= 0 ? gdf[next_slot[k]] : nullptr;
     s.tendf = tendf;
     s.ghsf = ghsf;
-    s.ghs = ghs;
     s.gd_e = gd_e[set];
     s.u = u[set];
     s.F = F[set];
@@ -741,6 +749,9 @@ struct EnsEngine : EngineBase {
     s.vor = vor;
     s.gd_v = gd_v;
     s.pv_e = pv_e;
+    s.invA_hl = invA_hl;
+    s.A_hl = A_hl;
+    s.ffs = (size_t)h->M.nc * D.M;
     return s;
   }
 
@@ -795,20 +806,19 @@ struct EnsEngine : EngineBase {
   void launch_spatial_only() override {}  // tmc_spatial_operators needs members <= 1
 
   void set_state_dev(const double* raw_gd, const double* raw_iap) override {
-    ens::launch_gather_f64(h->M.nc, D.M, h->cur, raw_gd, h->d_cell_n2o, gd[0], h->st);
+    ens::launch_gather_ff(h->M.nc, D.M, h->cur, raw_gd, h->d_cell_n2o, gd[0], h->st);
     ens::launch_gather_f32(h->M.ne, D.M, h->cur, raw_iap, h->d_edge_n2o, iap0, h->st);
-    refresh_shadows(0);
   }
   void gather_field(int which, const double* raw) override {
     if (which == F_GD)
-      ens::launch_gather_f64(h->M.nc, D.M, h->cur, raw, h->d_cell_n2o, gd[0], h->st);
+      ens::launch_gather_ff(h->M.nc, D.M, h->cur, raw, h->d_cell_n2o, gd[0], h->st);
     else if (which == F_IAP)
       ens::launch_gather_f32(h->M.ne, D.M, h->cur, raw, h->d_edge_n2o, iap0, h->st);
   }
   void get_field(int which, double* raw) override {
     const int m = h->cur, Mm = D.M;
     switch (which) {
-      case F_GD: ens::launch_scatter_f64(h->M.nc, Mm, m, gd[0], h->d_cell_n2o, raw, h->st); break;
+      case F_GD: ens::launch_scatter_ff(h->M.nc, Mm, m, gd[0], h->d_cell_n2o, raw, h->st); break;
       case F_IAP: ens::launch_scatter_f32(h->M.ne, Mm, m, iap0, h->d_edge_n2o, raw, h->st); break;
       case F_U: ens::launch_scatter_f32(h->M.ne, Mm, m, u[0], h->d_edge_n2o, raw, h->st); break;
       case F_PV_V: ens::launch_scatter_f32(h->M.nv, Mm, m, pv_v, h->d_vert_n2o, raw, h->st); break;
@@ -821,7 +831,7 @@ struct EnsEngine : EngineBase {
   }
   void set_tracers_dev(const double*) override {}  // member_layout 1 has no tracers
   void get_tracers_dev(double*) override {}
-  void refresh_shadows(int slot) override { ens::launch_shadow(h->M.nc, D.M, h->cur, gd[slot], gdf[slot], h->st); }
+  void refresh_shadows(int) override {}  // the h halves of gd are its FP32 values
   void set_ghs_dev(const double* raw) override {
     ens::launch_gather_f64(h->M.nc, D.M, h->cur, raw, h->d_cell_n2o, ghs, h->st);
     ens::launch_shadow(h->M.nc, D.M, h->cur, ghs, ghsf, h->st);
@@ -834,7 +844,7 @@ struct EnsEngine : EngineBase {
     *q = nullptr;  // no tracers
     *gh = ghs;
   }
-  void refresh_all_shadows() override { ens::launch_shadow(h->M.nc, D.M, -1, gd[0], gdf[0], h->st); }
+  void refresh_all_shadows() override {}
   void closure_features(float*, float*) override {}  // tmc_closure_features refuses member_layout 1
 
   // history fields of the selected member: its u, gd and ghs copied out of
@@ -847,7 +857,7 @@ struct EnsEngine : EngineBase {
     if (uo) cudaMemcpyAsync(uo, scratch_e, sizeof(double) * ne, cudaMemcpyDeviceToDevice, h->st);
     if (zon || mer) launch_reconstruct<double>(h->M, scratch_e, nullptr, nullptr, nullptr, zon, mer, h->st);
     if (hc) {
-      ens::launch_extract_f64(nc, Mm, m, gd[0], h->op_a, h->st);
+      ens::launch_extract_ff(nc, Mm, m, gd[0], h->op_a, h->st);
       ens::launch_extract_f64(nc, Mm, m, ghs, h->op_b, h->st);
       launch_h_field(nc, h->op_a, h->op_b, h->p.g, hc, h->st);
     }

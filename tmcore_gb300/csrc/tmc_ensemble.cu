@@ -44,6 +44,34 @@ __device__ __forceinline__ DD dd_add(DD a, DD b) {
   return {hi, __dsub_rn(e, __dsub_rn(hi, s))};
 }
 
+// Double-float (FF) arithmetic for gd: a value h + l with |l| <= ulp(h) / 2.
+// Error-free transforms (Knuth TwoSum; the FMA product error) with explicit
+// rounding, so the compiler cannot contract them.
+struct FF {
+  float h, l;
+};
+__device__ __forceinline__ FF ff_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+  const FF s = ff_two_sum(a.h, b.h);
+  return ff_two_sum(s.h, __fadd_rn(s.l, __fadd_rn(a.l, b.l)));
+}
+__device__ __forceinline__ FF ff_mul(FF a, FF b) {
+  const float p = __fmul_rn(a.h, b.h);
+  float e = __fmaf_rn(a.h, b.h, -p);
+  e = __fmaf_rn(a.h, b.l, e);
+  e = __fmaf_rn(a.l, b.h, e);
+  return ff_two_sum(p, e);
+}
+__host__ __device__ __forceinline__ FF ff_from(double x) {
+  const float h = (float)x;
+  return {h, (float)(x - (double)h)};
+}
+__device__ __forceinline__ double ff_to_double(FF a) { return (double)a.h + (double)a.l; }
+
 // V consecutive members of one element: one load / store of V * 4 (or 8) bytes
 template <int V>
 __device__ __forceinline__ void ldv(const float* p, size_t i, float (&o)[V]) {
@@ -78,6 +106,23 @@ __device__ __forceinline__ void stv(double* p, size_t i, const double (&v)[V]) {
     *reinterpret_cast<double2*>(p + i) = make_double2(v[0], v[1]);
   else
     p[i] = v[0];
+}
+
+template <int V>
+__device__ __forceinline__ void ldff(const float* p, size_t i, size_t ffs, FF (&o)[V]) {
+  float h[V], l[V];
+  ldv<V>(p, i, h);
+  ldv<V>(p + ffs, i, l);
+#pragma unroll
+  for (int c = 0; c < V; ++c) o[c] = FF{h[c], l[c]};
+}
+template <int V>
+__device__ __forceinline__ void stff(float* p, size_t i, size_t ffs, const FF (&v)[V]) {
+  float h[V], l[V];
+#pragma unroll
+  for (int c = 0; c < V; ++c) h[c] = v[c].h, l[c] = v[c].l;
+  stv<V>(p, i, h);
+  stv<V>(p + ffs, i, l);
 }
 
 // This thread's members and warp: one block = one member group (blockIdx.y)
@@ -184,8 +229,8 @@ __global__ void __launch_bounds__(kMaxBS) k_ens_cell(DevMesh Mh, Dims D, IO S, R
   __shared__ float s_ns[kME][kEnsEPB];
   __shared__ float s_dv[kME][kEnsEPB];
   __shared__ float s_ae[kME][kEnsEPB];
-  __shared__ double s_invA[kEnsEPB];
-  __shared__ double s_A[kEnsEPB];
+  __shared__ FF s_invA[kEnsEPB];
+  __shared__ FF s_A[kEnsEPB];
   __shared__ float s_invAf[kEnsEPB];
   __shared__ float s_Af[kEnsEPB];
   const int nc = Mh.nc, c0 = blockIdx.x * kEnsEPB, nel = min(kEnsEPB, nc - c0);
@@ -201,31 +246,32 @@ __global__ void __launch_bounds__(kMaxBS) k_ens_cell(DevMesh Mh, Dims D, IO S, R
     }
   }
   for (int j = threadIdx.x; j < nel; j += blockDim.x) {
-    s_invA[j] = Mh.invAreaCell[c0 + j];
-    s_A[j] = Mh.areaCell[c0 + j];
+    s_invA[j] = FF{S.invA_hl[c0 + j], S.invA_hl[nc + c0 + j]};
+    s_A[j] = FF{S.A_hl[c0 + j], S.A_hl[nc + c0 + j]};
     s_invAf[j] = Mh.invAreaCell_f[c0 + j];
     s_Af[j] = Mh.areaCell_f[c0 + j];
   }
   __syncthreads();
   const Lane L = lane_of<V>(D);
-  const size_t Mm = L.M;
+  const size_t Mm = L.M, ffs = S.ffs;
   const int mode = rk.mode;
+  const FF adt = ff_from(rk.a_dt), sixth = ff_from(1.0 / 6.0);
   float rip[V], r44[V], eh[V], el[V];
-  double mass[V];
+  FF mass[V];
 #pragma unroll
-  for (int c = 0; c < V; ++c) rip[c] = r44[c] = eh[c] = el[c] = 0.f, mass[c] = 0.0;
+  for (int c = 0; c < V; ++c) rip[c] = r44[c] = eh[c] = el[c] = 0.f, mass[c] = FF{0.f, 0.f};
   for (int j = L.w; j < nel; j += L.W) {
     const size_t cm = (size_t)(c0 + j) * Mm + L.m0;
-    double gold[V], gacc[V], gdin[V];
-    float tprev[V], gdf[V], ghf[V];
-    if (mode <= 3) ldv<V>(S.gd_old, cm, gold);
+    FF gold[V], gacc[V];
+    float tprev[V], gdf[V], ghf[V], gdl[V];
+    if (mode <= 3) ldff<V>(S.gd_old, cm, ffs, gold);
     if (mode >= 2) {
-      ldv<V>(S.gd_acc, cm, gacc);
+      ldff<V>(S.gd_acc, cm, ffs, gacc);
       ldv<V>(S.tendf, cm, tprev);
     }
-    ldv<V>(S.gdf_in, cm, gdf);
+    ldv<V>(S.gd_in, cm, gdf);
     ldv<V>(S.ghsf, cm, ghf);
-    if (diag) ldv<V>(S.gd_in, cm, gdin);
+    if (diag) ldv<V>(S.gd_in + ffs, cm, gdl);
     float uu[kME][V], Fv[kME][V];
 #pragma unroll
     for (int i = 0; i < kME; ++i) {
@@ -233,8 +279,8 @@ __global__ void __launch_bounds__(kMaxBS) k_ens_cell(DevMesh Mh, Dims D, IO S, R
       ldv<V>(S.u, k, uu[i]);
       ldv<V>(S.F, k, Fv[i]);
     }
-    double tn_acc[V], gnext[V];
-    float Eo[V], tT[V], gnf[V];
+    FF acc_o[V], gnext[V];
+    float Eo[V], tT[V];
 #pragma unroll
     for (int c = 0; c < V; ++c) {
       float hi = 0.f, lo = 0.f, k = 0.f;
@@ -244,46 +290,43 @@ __global__ void __launch_bounds__(kMaxBS) k_ens_cell(DevMesh Mh, Dims D, IO S, R
         two_sum_acc(hi, lo, __fmul_rn(__fmul_rn(ns, Fv[i][c]), s_dv[i][j]));
         k += fabsf(ns) * uu[i][c] * uu[i][c] * s_ae[i][j];
       }
-      const double t = -((double)hi + (double)lo) * s_invA[j];
-      tT[c] = (float)t;
+      // gd tendency t = -(flux divergence) / areaCell
+      FF t = ff_mul(ff_two_sum(hi, lo), s_invA[j]);
+      t = FF{-t.h, -t.l};
+      tT[c] = t.h;
       Eo[c] = k * 0.25f * s_invAf[j] + gdf[c] + ghf[c];
       const float Af = s_Af[j];
-      gnext[c] = 0.0;
+      gnext[c] = FF{0.f, 0.f};
       switch (mode) {
         case 1:
-          tn_acc[c] = t;
-          gnext[c] = gold[c] + rk.a_dt * t;
+          acc_o[c] = t;
+          gnext[c] = ff_add(gold[c], ff_mul(adt, t));
           break;
         case 2:
         case 3:
           rip[c] += tprev[c] * tT[c] * Af;
-          tn_acc[c] = gacc[c] + 2.0 * t;
-          gnext[c] = gold[c] + rk.a_dt * t;
+          acc_o[c] = ff_add(gacc[c], FF{2.f * t.h, 2.f * t.l});
+          gnext[c] = ff_add(gold[c], ff_mul(adt, t));
           break;
         default: {
           rip[c] += tprev[c] * tT[c] * Af;
-          const double tn = (gacc[c] + t) * (1.0 / 6.0);
-          tn_acc[c] = tn;
-          const float tnf = (float)tn;
-          r44[c] += tnf * tnf * Af;
+          const FF tn = ff_mul(ff_add(gacc[c], t), sixth);
+          acc_o[c] = tn;
+          r44[c] += tn.h * tn.h * Af;
         }
       }
-      gnf[c] = (float)gnext[c];
       if (diag) {
-        // total mass (FP64 gd), and the cell part of the total energy
-        // (gd^2 + 2 gd ghs) areaCell from FP32 terms, compensated
-        // (tmcore_swm_mod.F90:215-231)
-        mass[c] = mass[c] + gdin[c] * s_A[j];
+        // total mass from the FF gd (FF products, FF sum), and the cell part
+        // of the total energy (gd^2 + 2 gd ghs) areaCell from FP32 terms,
+        // compensated (tmcore_swm_mod.F90:215-231)
+        mass[c] = ff_add(mass[c], ff_mul(FF{gdf[c], gdl[c]}, s_A[j]));
         two_sum_acc(eh[c], el[c], gdf[c] * (gdf[c] + 2.f * ghf[c]) * Af);
       }
     }
     stv<V>(S.E, cm, Eo);
-    stv<V>(S.gd_acc, cm, tn_acc);
+    stff<V>(S.gd_acc, cm, ffs, acc_o);
     stv<V>(S.tendf, cm, tT);
-    if (mode <= 3) {
-      stv<V>(S.gd_next, cm, gnext);
-      stv<V>(S.gdf_next, cm, gnf);
-    }
+    if (mode <= 3) stff<V>(S.gd_next, cm, ffs, gnext);
   }
   const int slot = blockIdx.x;
   if (mode >= 2) {
@@ -296,7 +339,7 @@ __global__ void __launch_bounds__(kMaxBS) k_ens_cell(DevMesh Mh, Dims D, IO S, R
   if (diag) {
     double v[2][V];
 #pragma unroll
-    for (int c = 0; c < V; ++c) v[0][c] = mass[c], v[1][c] = (double)eh[c] + (double)el[c];
+    for (int c = 0; c < V; ++c) v[0][c] = ff_to_double(mass[c]), v[1][c] = (double)eh[c] + (double)el[c];
     double* const dst[2] = {P.d(R_MASS, slot), P.d(R_EN_C, slot)};
     block_partials_d<2, V>(L, v, dst);
   }
@@ -305,35 +348,34 @@ __global__ void __launch_bounds__(kMaxBS) k_ens_cell(DevMesh Mh, Dims D, IO S, R
 // invariants of a state only (the diagnostic pass): mass and cell energy
 template <int V>
 __global__ void __launch_bounds__(kMaxBS) k_ens_cell_diag(DevMesh Mh, Dims D, IO S, Partials P) {
-  __shared__ double s_A[kEnsEPB];
+  __shared__ FF s_A[kEnsEPB];
   __shared__ float s_Af[kEnsEPB];
   const int nc = Mh.nc, c0 = blockIdx.x * kEnsEPB, nel = min(kEnsEPB, nc - c0);
   for (int j = threadIdx.x; j < nel; j += blockDim.x) {
-    s_A[j] = Mh.areaCell[c0 + j];
+    s_A[j] = FF{S.A_hl[c0 + j], S.A_hl[nc + c0 + j]};
     s_Af[j] = Mh.areaCell_f[c0 + j];
   }
   __syncthreads();
   const Lane L = lane_of<V>(D);
   float eh[V], el[V];
-  double mass[V];
+  FF mass[V];
 #pragma unroll
-  for (int c = 0; c < V; ++c) eh[c] = el[c] = 0.f, mass[c] = 0.0;
+  for (int c = 0; c < V; ++c) eh[c] = el[c] = 0.f, mass[c] = FF{0.f, 0.f};
   for (int j = L.w; j < nel; j += L.W) {
     const size_t cm = (size_t)(c0 + j) * L.M + L.m0;
-    double gdin[V];
-    float gdf[V], ghf[V];
-    ldv<V>(S.gd_in, cm, gdin);
-    ldv<V>(S.gdf_in, cm, gdf);
+    FF g[V];
+    float ghf[V];
+    ldff<V>(S.gd_in, cm, S.ffs, g);
     ldv<V>(S.ghsf, cm, ghf);
 #pragma unroll
     for (int c = 0; c < V; ++c) {
-      mass[c] = mass[c] + gdin[c] * s_A[j];
-      two_sum_acc(eh[c], el[c], gdf[c] * (gdf[c] + 2.f * ghf[c]) * s_Af[j]);
+      mass[c] = ff_add(mass[c], ff_mul(g[c], s_A[j]));
+      two_sum_acc(eh[c], el[c], g[c].h * (g[c].h + 2.f * ghf[c]) * s_Af[j]);
     }
   }
   double v[2][V];
 #pragma unroll
-  for (int c = 0; c < V; ++c) v[0][c] = mass[c], v[1][c] = (double)eh[c] + (double)el[c];
+  for (int c = 0; c < V; ++c) v[0][c] = ff_to_double(mass[c]), v[1][c] = (double)eh[c] + (double)el[c];
   double* const dst[2] = {P.d(R_MASS, blockIdx.x), P.d(R_EN_C, blockIdx.x)};
   block_partials_d<2, V>(L, v, dst);
 }
@@ -384,7 +426,7 @@ __global__ void __launch_bounds__(kMaxBS) k_ens_vertex(DevMesh Mh, Dims D, IO S,
       const int j = min(base + q * L.W, nel - 1);
 #pragma unroll
       for (int i = 0; i < 3; ++i) {
-        ldv<V>(S.gdf_in, (size_t)s_c[i][j] * Mm + L.m0, g[q][i]);
+        ldv<V>(S.gd_in, (size_t)s_c[i][j] * Mm + L.m0, g[q][i]);
         ldv<V>(S.u, (size_t)s_e[i][j] * Mm + L.m0, uu[q][i]);
       }
     }
@@ -512,8 +554,8 @@ __global__ void __launch_bounds__(kMaxBS) k_ens_edge_flux(DevMesh Mh, Dims D, IO
     }
     if (mode >= 1 && mode <= 3) ldv<V>(S.iap_old, em, oldv);
     if (fuse) {
-      ldv<V>(S.gdf_next, c1m, gn1);
-      ldv<V>(S.gdf_next, c2m, gn2);
+      ldv<V>(S.gd_next, c1m, gn1);  // h halves: the FP32 gd of the next stage
+      ldv<V>(S.gd_next, c2m, gn2);
     }
     ldv<V>(S.E, c1m, E1);
     ldv<V>(S.E, c2m, E2);
@@ -584,35 +626,28 @@ constexpr int kFU = 4;
 template <int V>
 __global__ void __launch_bounds__(kMaxBS) k_ens_final_cells(DevMesh Mh, Dims D, IO S, const double* diag) {
   const Lane L = lane_of<V>(D);
-  const size_t Mm = L.M;
-  double bdt[V];
+  const size_t Mm = L.M, ffs = S.ffs;
+  FF bdt[V];
 #pragma unroll
-  for (int c = 0; c < V; ++c) bdt[c] = diag[(size_t)(L.m0 + c) * kDiagStride + 9];
+  for (int c = 0; c < V; ++c) bdt[c] = ff_from(diag[(size_t)(L.m0 + c) * kDiagStride + 9]);
   const int nc = Mh.nc, c0 = blockIdx.x * kEnsEPB, nel = min(kEnsEPB, nc - c0);
-  double* gd = const_cast<double*>(S.gd_old);
-  float* gdf = const_cast<float*>(S.gdf_in);
+  float* gd = const_cast<float*>(S.gd_old);
   for (int base = L.w; base < nel; base += L.W * kFU) {
-    double g[kFU][V], a[kFU][V];
+    FF g[kFU][V], a[kFU][V];
 #pragma unroll
     for (int q = 0; q < kFU; ++q) {
       const size_t cm = (size_t)(c0 + min(base + q * L.W, nel - 1)) * Mm + L.m0;
-      ldv<V>(gd, cm, g[q]);
-      ldv<V>(S.gd_acc, cm, a[q]);
+      ldff<V>(gd, cm, ffs, g[q]);
+      ldff<V>(S.gd_acc, cm, ffs, a[q]);
     }
 #pragma unroll
     for (int q = 0; q < kFU; ++q) {
       const int j = base + q * L.W;
       if (j >= nel) break;
-      const size_t cm = (size_t)(c0 + j) * Mm + L.m0;
-      double gn[V];
-      float gf[V];
+      FF gn[V];
 #pragma unroll
-      for (int c = 0; c < V; ++c) {
-        gn[c] = g[q][c] + bdt[c] * a[q][c];
-        gf[c] = (float)gn[c];
-      }
-      stv<V>(gd, cm, gn);
-      stv<V>(gdf, cm, gf);
+      for (int c = 0; c < V; ++c) gn[c] = ff_add(g[q][c], ff_mul(bdt[c], a[q][c]));
+      stff<V>(gd, (size_t)(c0 + j) * Mm + L.m0, ffs, gn);
     }
   }
 }
@@ -650,8 +685,8 @@ __global__ void __launch_bounds__(kMaxBS) k_ens_edges(DevMesh Mh, Dims D, IO S, 
       const size_t em = (size_t)(e0 + j) * Mm + L.m0;
       ldv<V>(iap, em, ia[q]);
       if (kUpdate) ldv<V>(S.iap_acc, em, ac[q]);
-      ldv<V>(S.gdf_in, (size_t)s_c[0][j] * Mm + L.m0, g1[q]);
-      ldv<V>(S.gdf_in, (size_t)s_c[1][j] * Mm + L.m0, g2[q]);
+      ldv<V>(S.gd_in, (size_t)s_c[0][j] * Mm + L.m0, g1[q]);
+      ldv<V>(S.gd_in, (size_t)s_c[1][j] * Mm + L.m0, g2[q]);
     }
 #pragma unroll
     for (int q = 0; q < kFU; ++q) {
@@ -752,15 +787,29 @@ __global__ void k_ens_gather_f32(int n, int M, int m, const double* raw, const i
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) dst[(size_t)i * M + m] = (float)raw[n2o[i]];
 }
-template <class T>
-__global__ void k_ens_scatter(int n, int M, int m, const T* src, const int32_t* n2o, double* raw) {
+__global__ void k_ens_gather_ff(int n, int M, int m, const double* raw, const int32_t* n2o, float* dst) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const FF v = ff_from(raw[n2o[i]]);
+  dst[(size_t)i * M + m] = v.h;
+  dst[(size_t)n * M + (size_t)i * M + m] = v.l;
+}
+__global__ void k_ens_scatter_f32(int n, int M, int m, const float* src, const int32_t* n2o, double* raw) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) raw[n2o[i]] = (double)src[(size_t)i * M + m];
+}
+__global__ void k_ens_scatter_ff(int n, int M, int m, const float* src, const int32_t* n2o, double* raw) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) raw[n2o[i]] = ff_to_double(FF{src[(size_t)i * M + m], src[(size_t)n * M + (size_t)i * M + m]});
 }
 template <class T>
 __global__ void k_ens_extract(int n, int M, int m, const T* src, double* dst) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) dst[i] = (double)src[(size_t)i * M + m];
+}
+__global__ void k_ens_extract_ff(int n, int M, int m, const float* src, double* dst) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = ff_to_double(FF{src[(size_t)i * M + m], src[(size_t)n * M + (size_t)i * M + m]});
 }
 __global__ void k_ens_iap_from_u(int ne, int M, int m, const double* gd_e, const double* u, float* iap) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -879,17 +928,23 @@ void launch_gather_f64(int n, int M, int m, const double* raw, const int32_t* n2
 void launch_gather_f32(int n, int M, int m, const double* raw, const int32_t* n2o, float* dst, cudaStream_t st) {
   k_ens_gather_f32<<<nb(n), 256, 0, st>>>(n, M, m, raw, n2o, dst);
 }
-void launch_scatter_f64(int n, int M, int m, const double* src, const int32_t* n2o, double* raw, cudaStream_t st) {
-  k_ens_scatter<double><<<nb(n), 256, 0, st>>>(n, M, m, src, n2o, raw);
+void launch_gather_ff(int n, int M, int m, const double* raw, const int32_t* n2o, float* dst, cudaStream_t st) {
+  k_ens_gather_ff<<<nb(n), 256, 0, st>>>(n, M, m, raw, n2o, dst);
 }
 void launch_scatter_f32(int n, int M, int m, const float* src, const int32_t* n2o, double* raw, cudaStream_t st) {
-  k_ens_scatter<float><<<nb(n), 256, 0, st>>>(n, M, m, src, n2o, raw);
+  k_ens_scatter_f32<<<nb(n), 256, 0, st>>>(n, M, m, src, n2o, raw);
+}
+void launch_scatter_ff(int n, int M, int m, const float* src, const int32_t* n2o, double* raw, cudaStream_t st) {
+  k_ens_scatter_ff<<<nb(n), 256, 0, st>>>(n, M, m, src, n2o, raw);
 }
 void launch_extract_f64(int n, int M, int m, const double* src, double* dst, cudaStream_t st) {
   k_ens_extract<double><<<nb(n), 256, 0, st>>>(n, M, m, src, dst);
 }
 void launch_extract_f32(int n, int M, int m, const float* src, double* dst, cudaStream_t st) {
   k_ens_extract<float><<<nb(n), 256, 0, st>>>(n, M, m, src, dst);
+}
+void launch_extract_ff(int n, int M, int m, const float* src, double* dst, cudaStream_t st) {
+  k_ens_extract_ff<<<nb(n), 256, 0, st>>>(n, M, m, src, dst);
 }
 void launch_iap_from_u(int ne, int M, int m, const double* gd_e, const double* u, float* iap, cudaStream_t st) {
   k_ens_iap_from_u<<<nb(ne), 256, 0, st>>>(ne, M, m, gd_e, u, iap);

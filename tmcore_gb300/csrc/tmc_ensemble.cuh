@@ -9,9 +9,10 @@
 // signs, weights, metrics) in shared memory, then its W warps take elements
 // w, w + W, ..., so that they work on neighbouring elements together and
 // share the neighbours' lines in L1.  The arithmetic is that of the FP32
-// single-model kernels (tmc_kernels_impl.cuh) in the same expression order:
-// FP32 edge and vertex state, FP64 gd, its tendency from an FP32 two-sum
-// flux divergence and its RK accumulation.
+// single-model kernels (tmc_kernels_impl.cuh) in the same expression order
+// (FP32 edge and vertex state, the gd tendency from an FP32 two-sum flux
+// divergence), except that gd and its RK accumulation are double-float
+// (see IO) instead of FP64.
 //
 // Global sums: the warps of a block combine their lanes' sums in shared
 // memory, and lane m of warp 0 stores member m's partial sum of the block,
@@ -52,22 +53,24 @@ struct Partials {
   __host__ __device__ double* d(int r, int slot) const { return sd + ((size_t)(r - R_MASS) * cap + slot) * M; }
 };
 
-// Buffers of one CRK4 stage, all member-innermost.
+// Buffers of one CRK4 stage, all member-innermost.  gd and its RK
+// accumulator are double-float (FF) values h + l in two FP32 halves of one
+// array, h for every element first, then l at offset `ffs` (nCells * M): the
+// h half is the FP32 value of gd the stencils read, the pair keeps about 48
+// significant bits, and all gd arithmetic runs on the FP32 pipes (GB300
+// issues FP64 at 1/64 of the FP32 rate).
 struct IO {
-  const double* gd_in;
-  const double* gd_old;
-  double* gd_next;
-  double* gd_acc;
+  const float* gd_in;
+  const float* gd_old;
+  float* gd_next;
+  float* gd_acc;
   const float* iap_in;
   const float* iap_old;
   float* iap_next;
   float* iap_acc;
   float* iap_tend;
-  const float* gdf_in;
-  float* gdf_next;
   float* tendf;
   const float* ghsf;
-  const double* ghs;
   const float* gd_e;
   const float* u;
   const float* F;
@@ -79,6 +82,9 @@ struct IO {
   float* vor;   // null: not kept
   float* gd_v;  // null: not kept
   float* pv_e;
+  const float* invA_hl;  // 1 / areaCell as FF: [2][nCells]
+  const float* A_hl;     // areaCell as FF: [2][nCells]
+  size_t ffs;            // offset of the l halves (nCells * M)
 };
 
 // passes of the fused CRK4 step (bs: threads per block, a multiple of 32)
@@ -102,17 +108,20 @@ void launch_cell_diag(const DevMesh& Mh, const Dims& D, const IO& S, const Parti
 void launch_finalize(const Dims& D, const Partials& P, bool step, bool diag, bool conserve, double totalArea,
                      double sumAreaTriangle, double dt, double* diag_out, cudaStream_t st);
 
-// state transfer of member m (caller's element order <-> member-innermost)
+// state transfer of member m (caller's element order <-> member-innermost);
+// _ff: an FF array (h, then l at offset n * M)
 void launch_gather_f64(int n, int M, int m, const double* raw, const int32_t* n2o, double* dst, cudaStream_t st);
 void launch_gather_f32(int n, int M, int m, const double* raw, const int32_t* n2o, float* dst, cudaStream_t st);
-void launch_scatter_f64(int n, int M, int m, const double* src, const int32_t* n2o, double* raw, cudaStream_t st);
+void launch_gather_ff(int n, int M, int m, const double* raw, const int32_t* n2o, float* dst, cudaStream_t st);
 void launch_scatter_f32(int n, int M, int m, const float* src, const int32_t* n2o, double* raw, cudaStream_t st);
+void launch_scatter_ff(int n, int M, int m, const float* src, const int32_t* n2o, double* raw, cudaStream_t st);
 // member m of a member-innermost array into a contiguous FP64 array (internal order)
 void launch_extract_f64(int n, int M, int m, const double* src, double* dst, cudaStream_t st);
 void launch_extract_f32(int n, int M, int m, const float* src, double* dst, cudaStream_t st);
+void launch_extract_ff(int n, int M, int m, const float* src, double* dst, cudaStream_t st);
 // iap_u of member m = sqrt(gd_edge) u (internal order inputs)
 void launch_iap_from_u(int ne, int M, int m, const double* gd_e, const double* u, float* iap, cudaStream_t st);
-// FP32 shadow of member m's gd (m < 0: every member)
+// FP32 copy of member m's FP64 array (m < 0: every member)
 void launch_shadow(int nc, int M, int m, const double* gd, float* gdf, cudaStream_t st);
 
 }  // namespace ens
