@@ -236,6 +236,36 @@ def ensemble_model_bytes(nc: int, ne: int, nv: int, S: int, members: int) -> flo
     return 4 * (39 * nc + 153 * ne + 67 * nv + members * (8 * S * nc + 7 * S * ne)) + 3 * S * members * (nc + ne)
 
 
+def inner_ensemble_pass_bytes(nc: int, ne: int, nv: int, members: int) -> dict:
+    """Algorithmic bytes per launch of each pass of the member-innermost
+    ensemble step (every array once per pass, gathers at perfect reuse),
+    averaged over the four CRK4 stages: FP32 edge and vertex fields, gd and
+    its RK accumulator double-float (8 bytes), mesh tables once per pass.
+    Per member and stage (modes 1 / 2-3 / 4):
+      cell   u, F 8 Ne; gd old 8, acc 8 / 16 / 8, tend 0 / 4 / 4 in, gd h, ghs 8,
+             E 4, acc 8, tend 4, next gd 8 / 8 / 0 out  (+4 Nc gd l on the diag stage)
+      vertex gd h 4 Nc, u 4 Ne in, pv 4 Nv out
+      edge_pv pv 4 Nv in, pv_e 4 Ne out
+      flux   pv_e, u, gd_e, F 16, tend + acc 0 / 8 / 8, old 4 / 4 / 0, acc + tend 8,
+             next gd_e, u, F 12 / 12 / 0 per edge; E, tend, next gd h 12 / 12 / 8 per cell
+      final  cells gd r/w 16, acc 8; edges iap r/w 8, acc 4, gd_e, u, F 12, gd h 4 Nc."""
+    M = members
+    mesh = {"cell": 39 * nc + 8 * ne, "vertex": 67 * nv, "edge_pv": 8 * ne, "flux": 153 * ne, "final": 8 * ne}
+    per = {
+        "cell": (32 * ne + 184 * nc + 4 * nc) / 4.0,
+        "vertex": 4 * nc + 4 * ne + 4 * nv,
+        "edge_pv": 4 * nv + 4 * ne,
+        "flux": (168 * ne + 44 * nc) / 4.0,
+        "final": 28 * nc + 24 * ne,
+    }
+    return {k: mesh[k] + M * per[k] for k in per}
+
+
+def inner_ensemble_step_bytes(nc: int, ne: int, nv: int, members: int) -> float:
+    b = inner_ensemble_pass_bytes(nc, ne, nv, members)
+    return 4 * (b["cell"] + b["vertex"] + b["edge_pv"] + b["flux"]) + b["final"]
+
+
 def _ensemble_ic(job):
     """Initial state of one ensemble member (runs in a spawned worker)."""
     level, seed = job
@@ -298,32 +328,53 @@ def run_mixed(args, local, ics_by_level, peak):
 
 
 def run_ensemble(args, local, ics, peak):
-    """Config 3: FP32 members of one mesh stepped together (member = blockIdx.y of
-    every launch), CUDA graph per CRK4 step; dt = 1200 / 2^(level-4) s."""
+    """Config 3: FP32 members of one mesh stepped together, CUDA graph per CRK4
+    step; dt = 1200 / 2^(level-4) s.  Member-innermost layout (member_layout 1:
+    arrays [element][member], a warp per 32 members of an element), with the
+    member-outermost layout (member = blockIdx.y) timed beside it."""
     from tmcore_gb300 import abi, mesh
     from tmcore_gb300.gpu import TMCoreGPU
 
     L, M = args.ensemble_level, len(ics)
     m = mesh.icos_mesh(L)
     dt = 1200.0 / 2 ** (L - 4)
-    ens = TMCoreGPU(m, members=M, dt=dt, pv_scheme=1, apvm_weight=0.0, adv_order=2, conserve_energy=1,
-                    precision=abi.TMC_FP32, diag_every=1, use_graph=1, renumber=1, device=local)
-    for k, (gd, u, ghs) in enumerate(ics):
-        ens.select_member(k)
-        ens.set_initial(gd, u, ghs)
-    tuned = ens.autotune(steps=2) if not args.no_autotune else None
-    ens.step(args.warmup)
-    ens.synchronize()
-    ms, _, _, launches = ens.time_steps(args.ensemble_steps, total=True, flux=False)
-    step_s = ms / args.ensemble_steps / 1e3
-    d = ens.diag()
-    ens.close()
+    res = {}
+    for layout in ((1, 0) if M % 32 == 0 else (0,)):
+        ens = TMCoreGPU(m, members=M, dt=dt, pv_scheme=1, apvm_weight=0.0, adv_order=2, conserve_energy=1,
+                        precision=abi.TMC_FP32, diag_every=1, use_graph=1, renumber=1, device=local,
+                        member_layout=layout)
+        for k, (gd, u, ghs) in enumerate(ics):
+            ens.select_member(k)
+            ens.set_initial(gd, u, ghs)
+        tuned = ens.autotune(steps=2) if not args.no_autotune else None
+        ens.step(args.warmup)
+        ens.synchronize()
+        ms, _, _, launches = ens.time_steps(args.ensemble_steps, total=True, flux=False)
+        passes = ens.pass_times(3) if layout == 1 else None
+        d = ens.diag()
+        ens.close()
+        res[layout] = (ms / args.ensemble_steps / 1e3, launches, d, tuned, passes)
+    lay = 1 if 1 in res else 0
+    step_s, launches, d, tuned, passes = res[lay]
     mb = ensemble_model_bytes(m.nCells, m.nEdges, m.nVertices, 4, M)
-    return {"workload": f"{M} FP32 members on level {L} ({m.nCells} cells), seeds 0..{M - 1}, CRK4 dt={dt:g}s",
-            "members": M, "level": L, "dt_s": dt, "steps": args.ensemble_steps, "ms_per_step": step_s * 1e3,
-            "member_days_per_s": M * dt / DAY / step_s, "sim_days_per_s": dt / DAY / step_s,
-            "scope_model_bytes_per_step": mb, "achieved_gbs": mb / step_s / 1e9, "frac": mb / step_s / 1e9 / peak,
-            "gpu_launches": launches, "member0_beta": float(d[4]), "block_sizes": tuned}
+    out = {"workload": f"{M} FP32 members on level {L} ({m.nCells} cells), seeds 0..{M - 1}, CRK4 dt={dt:g}s",
+           "member_layout": lay, "members": M, "level": L, "dt_s": dt, "steps": args.ensemble_steps,
+           "ms_per_step": step_s * 1e3, "member_days_per_s": M * dt / DAY / step_s, "sim_days_per_s": dt / DAY / step_s,
+           "scope_model_bytes_per_step": mb, "achieved_gbs": mb / step_s / 1e9, "frac": mb / step_s / 1e9 / peak,
+           "gpu_launches": launches, "member0_beta": float(d[4]), "block_sizes": tuned}
+    if lay == 1:
+        pb = inner_ensemble_pass_bytes(m.nCells, m.nEdges, m.nVertices, M)
+        sb = inner_ensemble_step_bytes(m.nCells, m.nEdges, m.nVertices, M)
+        out["pass_model_bytes_per_step"] = sb
+        out["pass_model_frac"] = sb / step_s / 1e9 / peak
+        out["passes"] = {k: {"ms_per_launch": passes[k], "algorithmic_bytes_per_launch": pb[k],
+                             "achieved_gbs": pb[k] / (passes[k] * 1e-3) / 1e9,
+                             "frac": pb[k] / (passes[k] * 1e-3) / 1e9 / peak} for k in pb}
+    if 0 in res and lay == 1:
+        s0 = res[0][0]
+        out["member_outermost"] = {"ms_per_step": s0 * 1e3, "member_days_per_s": M * dt / DAY / s0,
+                                   "block_sizes": res[0][3]}
+    return out
 
 
 def run_closure_leg(args, local, ics, peak):

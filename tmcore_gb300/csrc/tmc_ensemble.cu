@@ -14,6 +14,28 @@
 
 #include "tmc_ensemble.cuh"
 
+// Minimum resident blocks per SM the heavy passes are compiled for (0: none
+// given).  Any minimum changes the compiler's register heuristics: on 512
+// level-6 members, 1 (flux 96, cell 110 registers with two members per
+// lane) measured 4.87 ms per step, none 5.07, 3 4.94, flux 4 (64 registers,
+// spilled) 5.50.
+#ifndef TMC_ENS_FLUX_MINB
+#define TMC_ENS_FLUX_MINB 1
+#endif
+#ifndef TMC_ENS_CELL_MINB
+#define TMC_ENS_CELL_MINB 1
+#endif
+#ifndef TMC_ENS_VERT_MINB
+#define TMC_ENS_VERT_MINB 1
+#endif
+#define TMC_ENS_LB_0 __launch_bounds__(256)
+#define TMC_ENS_LB_1 __launch_bounds__(256, 1)
+#define TMC_ENS_LB_2 __launch_bounds__(256, 2)
+#define TMC_ENS_LB_3 __launch_bounds__(256, 3)
+#define TMC_ENS_LB_4 __launch_bounds__(256, 4)
+#define TMC_ENS_LB_(n) TMC_ENS_LB_##n
+#define TMC_ENS_LB(n) TMC_ENS_LB_(n)
+
 namespace tmc {
 namespace ens {
 
@@ -224,7 +246,7 @@ __device__ __forceinline__ void prep(const float (&ia)[V], const float (&g1)[V],
 // calc_kinetic_energy :206-221, calc_gd_tend_on_cell tmcore_swm_mod.F90:127-139)
 // ---------------------------------------------------------------------------
 template <int V>
-__global__ void __launch_bounds__(kMaxBS) k_ens_cell(DevMesh Mh, Dims D, IO S, RKStage rk, Partials P, int diag) {
+__global__ void TMC_ENS_LB(TMC_ENS_CELL_MINB) k_ens_cell(DevMesh Mh, Dims D, IO S, RKStage rk, Partials P, int diag) {
   __shared__ int s_e[kME][kEnsEPB];
   __shared__ float s_ns[kME][kEnsEPB];
   __shared__ float s_dv[kME][kEnsEPB];
@@ -385,7 +407,7 @@ __global__ void __launch_bounds__(kMaxBS) k_ens_cell_diag(DevMesh Mh, Dims D, IO
 // :262-270); potential enstrophy and absolute vorticity on diag stages
 // ---------------------------------------------------------------------------
 template <int V>
-__global__ void __launch_bounds__(kMaxBS) k_ens_vertex(DevMesh Mh, Dims D, IO S, Partials P, int diag) {
+__global__ void TMC_ENS_LB(TMC_ENS_VERT_MINB) k_ens_vertex(DevMesh Mh, Dims D, IO S, Partials P, int diag) {
   constexpr int kVU = 2;  // vertices per warp iteration (loads of both first)
   __shared__ int s_c[3][kEnsEPB];
   __shared__ int s_e[3][kEnsEPB];
@@ -509,7 +531,7 @@ __global__ void __launch_bounds__(kMaxBS) k_ens_edge_pv(DevMesh Mh, Dims D, IO S
 // prepare the next stage's gd_edge, u and F from its gd and iap_u.
 // ---------------------------------------------------------------------------
 template <int V>
-__global__ void __launch_bounds__(kMaxBS) k_ens_edge_flux(DevMesh Mh, Dims D, IO S, RKStage rk, Partials P) {
+__global__ void TMC_ENS_LB(TMC_ENS_FLUX_MINB) k_ens_edge_flux(DevMesh Mh, Dims D, IO S, RKStage rk, Partials P) {
   __shared__ int s_ep[kME2][kEnsEPB];
   __shared__ float s_w[kME2][kEnsEPB];
   __shared__ int s_c[2][kEnsEPB];
