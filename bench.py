@@ -250,12 +250,12 @@ def inner_ensemble_pass_bytes(nc: int, ne: int, nv: int, members: int) -> dict:
              next gd_e, u, F 12 / 12 / 0 per edge; E, tend, next gd h 12 / 12 / 8 per cell
       final  cells gd r/w 16, acc 8; edges iap r/w 8, acc 4, gd_e, u, F 12, gd h 4 Nc."""
     M = members
-    mesh = {"cell": 39 * nc + 8 * ne, "vertex": 67 * nv, "edge_pv": 8 * ne, "flux": 153 * ne, "final": 8 * ne}
+    mesh = {"cell": 39 * nc + 8 * ne, "vertex": 67 * nv, "edge_pv": 8 * ne, "edge_flux": 153 * ne, "final": 8 * ne}
     per = {
         "cell": (32 * ne + 184 * nc + 4 * nc) / 4.0,
         "vertex": 4 * nc + 4 * ne + 4 * nv,
         "edge_pv": 4 * nv + 4 * ne,
-        "flux": (168 * ne + 44 * nc) / 4.0,
+        "edge_flux": (168 * ne + 44 * nc) / 4.0,
         "final": 28 * nc + 24 * ne,
     }
     return {k: mesh[k] + M * per[k] for k in per}
@@ -263,7 +263,7 @@ def inner_ensemble_pass_bytes(nc: int, ne: int, nv: int, members: int) -> dict:
 
 def inner_ensemble_step_bytes(nc: int, ne: int, nv: int, members: int) -> float:
     b = inner_ensemble_pass_bytes(nc, ne, nv, members)
-    return 4 * (b["cell"] + b["vertex"] + b["edge_pv"] + b["flux"]) + b["final"]
+    return 4 * (b["cell"] + b["vertex"] + b["edge_pv"] + b["edge_flux"]) + b["final"]
 
 
 def _ensemble_ic(job):

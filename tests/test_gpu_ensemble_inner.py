@@ -44,7 +44,7 @@ def _single(mesh, ic, **kw):
     return one
 
 
-@pytest.mark.parametrize("members", [M, 2 * M])  # one or two members per lane
+@pytest.mark.parametrize("members", [M, 2 * M, 4 * M])  # one, two or four members per lane
 def test_members_match_single_runs_without_beta(mesh4, members):
     kw = dict(dt=600.0, conserve_energy=0, diag_every=1)
     ics = _ics(mesh4, members, 100)

@@ -669,6 +669,7 @@ struct EnsEngine : EngineBase {
   float* F[2] = {};
   float *E = nullptr, *pv_v = nullptr, *vor = nullptr, *gd_v = nullptr, *pv_e = nullptr;
   float *invA_hl = nullptr, *A_hl = nullptr;
+  float *cdv = nullptr, *cae = nullptr, *vdc = nullptr;
   explicit EnsEngine(tmc_handle* hh) : h(hh) {}
 
   int alloc() override {
@@ -714,7 +715,22 @@ struct EnsEngine : EngineBase {
     }
     invA_hl = h->upload(ia);
     A_hl = h->upload(a);
-    if (!EP.sf || !EP.sd || !pv_e || !F[1] || !gd_v || !invA_hl || !A_hl) return TMC_E_CUDA;
+    // the edge metrics the cell and vertex passes read per slot, gathered once
+    // here (FP32, as Engine<float> reads them), so staging them is one
+    // coalesced load instead of an index load and a dependent gather
+    const HostMesh& hm = h->hm;
+    const int nvert = h->M.nv, me = hm.me;
+    std::vector<float> v_cdv((size_t)me * ncell), v_cae((size_t)me * ncell), v_vdc(3 * (size_t)nvert);
+    for (size_t k = 0; k < v_cdv.size(); ++k) {
+      const int e = hm.edgesOnCell[k];
+      v_cdv[k] = (float)hm.dvEdge[e];
+      v_cae[k] = (float)hm.areaEdge[e];
+    }
+    for (size_t k = 0; k < v_vdc.size(); ++k) v_vdc[k] = (float)hm.dcEdge[hm.edgesOnVertex[k]];
+    cdv = h->upload(v_cdv);
+    cae = h->upload(v_cae);
+    vdc = h->upload(v_vdc);
+    if (!EP.sf || !EP.sd || !pv_e || !F[1] || !gd_v || !invA_hl || !A_hl || !cdv || !cae || !vdc) return TMC_E_CUDA;
     cudaMemset(ghs, 0, sizeof(double) * nc);
     cudaMemset(ghsf, 0, sizeof(float) * nc);
     return TMC_OK;
@@ -751,6 +767,9 @@ struct EnsEngine : EngineBase {
     s.pv_e = pv_e;
     s.invA_hl = invA_hl;
     s.A_hl = A_hl;
+    s.cdv = cdv;
+    s.cae = cae;
+    s.vdc = vdc;
     s.ffs = (size_t)h->M.nc * D.M;
     return s;
   }

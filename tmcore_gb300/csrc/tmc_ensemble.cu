@@ -28,6 +28,11 @@
 #ifndef TMC_ENS_VERT_MINB
 #define TMC_ENS_VERT_MINB 1
 #endif
+// vertices per warp iteration of the vertex pass (512 level-6 members:
+// 2 -> 4.85 ms per step, 1 -> 4.86, 4 -> 4.89)
+#ifndef TMC_ENS_VU
+#define TMC_ENS_VU 2
+#endif
 #define TMC_ENS_LB_0 __launch_bounds__(256)
 #define TMC_ENS_LB_1 __launch_bounds__(256, 1)
 #define TMC_ENS_LB_2 __launch_bounds__(256, 2)
@@ -260,11 +265,10 @@ __global__ void TMC_ENS_LB(TMC_ENS_CELL_MINB) k_ens_cell(DevMesh Mh, Dims D, IO 
     const int i = t / kEnsEPB, j = t - i * kEnsEPB;
     if (j < nel) {
       const size_t k = (size_t)i * nc + c0 + j;
-      const int e = Mh.edgesOnCell[k];
-      s_e[i][j] = e;
+      s_e[i][j] = Mh.edgesOnCell[k];
       s_ns[i][j] = (float)Mh.nSign[k];
-      s_dv[i][j] = Mh.dvEdge_f[e];
-      s_ae[i][j] = Mh.areaEdge_f[e];
+      s_dv[i][j] = S.cdv[k];  // dvEdge and areaEdge of the cell's edges, gathered at set-up
+      s_ae[i][j] = S.cae[k];
     }
   }
   for (int j = threadIdx.x; j < nel; j += blockDim.x) {
@@ -408,7 +412,7 @@ __global__ void __launch_bounds__(kMaxBS) k_ens_cell_diag(DevMesh Mh, Dims D, IO
 // ---------------------------------------------------------------------------
 template <int V>
 __global__ void TMC_ENS_LB(TMC_ENS_VERT_MINB) k_ens_vertex(DevMesh Mh, Dims D, IO S, Partials P, int diag) {
-  constexpr int kVU = 2;  // vertices per warp iteration (loads of both first)
+  constexpr int kVU = TMC_ENS_VU;  // vertices per warp iteration (their loads first)
   __shared__ int s_c[3][kEnsEPB];
   __shared__ int s_e[3][kEnsEPB];
   __shared__ float s_kt[3][kEnsEPB];
@@ -422,12 +426,11 @@ __global__ void TMC_ENS_LB(TMC_ENS_VERT_MINB) k_ens_vertex(DevMesh Mh, Dims D, I
     const int i = t / kEnsEPB, j = t - i * kEnsEPB;
     if (j < nel) {
       const size_t k = (size_t)i * nv + v0 + j;
-      const int e = Mh.edgesOnVertex[k];
       s_c[i][j] = Mh.cellsOnVertex[k];
-      s_e[i][j] = e;
+      s_e[i][j] = Mh.edgesOnVertex[k];
       s_kt[i][j] = Mh.kite_f[k];
       s_ts[i][j] = (float)Mh.tSign[k];
-      s_dc[i][j] = Mh.dcEdge_f[e];
+      s_dc[i][j] = S.vdc[k];  // dcEdge of the vertex's edges, gathered at set-up
     }
   }
   for (int j = threadIdx.x; j < nel; j += blockDim.x) {

@@ -82,6 +82,9 @@ struct IO {
   float* vor;   // null: not kept
   float* gd_v;  // null: not kept
   float* pv_e;
+  const float* cdv;      // dvEdge of edgesOnCell: [6][nCells] (FP32)
+  const float* cae;      // areaEdge of edgesOnCell: [6][nCells] (FP32)
+  const float* vdc;      // dcEdge of edgesOnVertex: [3][nVertices] (FP32)
   const float* invA_hl;  // 1 / areaCell as FF: [2][nCells]
   const float* A_hl;     // areaCell as FF: [2][nCells]
   size_t ffs;            // offset of the l halves (nCells * M)
