@@ -1,5 +1,5 @@
 """Member-innermost ensembles (tmc_params.member_layout = 1): arrays
-[element][member], one warp per 32 members of an element.
+[element][member], 32 (or 16) lanes per element, one or two members per lane.
 
 The kernels repeat the FP32 single-model expressions, but the compiler
 contracts multiplies and adds into FMAs differently in the two kernels, so
@@ -44,7 +44,8 @@ def _single(mesh, ic, **kw):
     return one
 
 
-@pytest.mark.parametrize("members", [M, 2 * M, 4 * M])  # one, two or four members per lane
+# 16 and 48: a warp covers two elements of 16 members; 64: two members per lane
+@pytest.mark.parametrize("members", [16, M, 48, 2 * M])
 def test_members_match_single_runs_without_beta(mesh4, members):
     kw = dict(dt=600.0, conserve_energy=0, diag_every=1)
     ics = _ics(mesh4, members, 100)
@@ -157,7 +158,7 @@ def test_member_layout_refusals(mesh3):
     from tmcore_gb300.gpu import ClosureMLP, TMCError, TMCoreGPU
 
     with pytest.raises(TMCError) as e:
-        TMCoreGPU(mesh3, dt=600.0, members=48, member_layout=1, **KW)
+        TMCoreGPU(mesh3, dt=600.0, members=40, member_layout=1, **KW)
     assert e.value.code == abi.TMC_E_ARG
     with pytest.raises(TMCError) as e:
         TMCoreGPU(mesh3, dt=600.0, members=32, member_layout=1, precision=1, pv_scheme=3, interp_pv_order=3)

@@ -676,8 +676,9 @@ struct EnsEngine : EngineBase {
     const size_t M_ = (size_t)h->members;
     const size_t nc = h->M.nc * M_, ne = h->M.ne * M_, nv = h->M.nv * M_;
     D.M = h->members;
-    D.G = h->members / 32;
+    D.G = (h->members + 31) / 32;
     D.V = h->members % 64 == 0 ? 2 : 1;
+    D.LPE = h->members % 32 == 0 ? 32 : 16;
     D.slots_c = ens::slots_for(h->M.nc);
     D.slots_e = ens::slots_for(h->M.ne);
     D.slots_v = ens::slots_for(h->M.nv);
@@ -1027,7 +1028,7 @@ int tmc_create(const tmc_mesh_desc* mesh, const tmc_params* params, tmc_handle**
   }
   if (p.member_layout != 0) {
     if (p.member_layout != 1) return bad("member_layout must be 0 (member-outermost) or 1 (member-innermost)");
-    if (h->members < 32 || h->members % 32 != 0) return bad("member_layout 1 needs members a multiple of 32");
+    if (h->members < 16 || h->members % 16 != 0) return bad("member_layout 1 needs members a multiple of 16");
     if (p.pv_scheme != 1 || p.apvm_weight != 0.0 || p.adv_order != 2 || p.n_tracers != 0 ||
         p.flux_4th_order_correct) {
       h->err = "member_layout 1 runs centred pv (pv_scheme 1, apvm_weight 0), adv_order 2, no tracers";

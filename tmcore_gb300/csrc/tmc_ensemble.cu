@@ -152,18 +152,22 @@ __device__ __forceinline__ void stff(float* p, size_t i, size_t ffs, const FF (&
   stv<V>(p + ffs, i, l);
 }
 
-// This thread's members and warp: one block = one member group (blockIdx.y)
-// and kEnsEPB consecutive elements (blockIdx.x).
+// This thread's members and elements.  One block = one member group
+// (blockIdx.y) and kEnsEPB consecutive elements (blockIdx.x).  A warp covers
+// 32 / LPE elements at a time, LPE lanes each (LPE = 16 when the member
+// count is not a multiple of 32): its warps take elements j0, j0 + js, ...
 struct Lane {
-  int m0;    // first member of the lane
-  size_t M;  // member stride
-  int w, W;  // warp, warps
-  int lane;
+  int m0;      // first member of the lane
+  size_t M;    // member stride
+  int j0, js;  // first element and element stride of the thread
+  int slot, nslot;  // this thread's row of a block reduction, and the rows
+  int ml;      // member lane (0 .. LPE-1)
 };
 template <int V>
 __device__ __forceinline__ Lane lane_of(const Dims& D) {
-  return Lane{(int)((blockIdx.y * 32 + (threadIdx.x & 31)) * V), (size_t)D.M, (int)(threadIdx.x >> 5),
-              (int)(blockDim.x >> 5), (int)(threadIdx.x & 31)};
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, W = blockDim.x >> 5;
+  const int epw = 32 / D.LPE, sub = lane / D.LPE, ml = lane % D.LPE;
+  return Lane{(int)((blockIdx.y * D.LPE + ml) * V), (size_t)D.M, w * epw + sub, W * epw, w * epw + sub, W * epw, ml};
 }
 
 inline dim3 grid_of(int n, const Dims& D, int bs, int* threads) {
@@ -171,21 +175,23 @@ inline dim3 grid_of(int n, const Dims& D, int bs, int* threads) {
   if (W < 1) W = 1;
   if (W > kMaxBS / 32) W = kMaxBS / 32;
   *threads = W * 32;
-  return dim3((unsigned)slots_for(n), (unsigned)(D.M / (32 * D.V)));
+  return dim3((unsigned)slots_for(n), (unsigned)(D.M / (D.LPE * D.V)));
 }
 
-// Per-member partial sums of one block: the warps' values of each member are
-// combined in a fixed order (FP32 TwoSum, or FP64) and warp 0 stores them.
-// Every thread of the block calls these (they synchronise).
+// Per-member partial sums of one block: the rows (warps and the element
+// halves of a warp) of each member are combined in a fixed order (FP32
+// TwoSum, or FP64) and row 0 stores them.  Every thread of the block calls
+// these (they synchronise).
+constexpr int kRows = 2 * kMaxBS / 32;
 template <int N, int V>
 __device__ __forceinline__ void block_partials_f(const Lane& L, const float (&v)[N][V], float* const (&dst)[N]) {
-  __shared__ float sh[N][V][kMaxBS / 32][32];
+  __shared__ float sh[N][V][kRows][32];
 #pragma unroll
   for (int k = 0; k < N; ++k)
 #pragma unroll
-    for (int c = 0; c < V; ++c) sh[k][c][L.w][L.lane] = v[k][c];
+    for (int c = 0; c < V; ++c) sh[k][c][L.slot][L.ml] = v[k][c];
   __syncthreads();
-  if (L.w == 0) {
+  if (L.slot == 0) {
 #pragma unroll
     for (int k = 0; k < N; ++k) {
       if (!dst[k]) continue;
@@ -193,7 +199,7 @@ __device__ __forceinline__ void block_partials_f(const Lane& L, const float (&v)
 #pragma unroll
       for (int c = 0; c < V; ++c) {
         float hi = 0.f, lo = 0.f;
-        for (int q = 0; q < L.W; ++q) two_sum_acc(hi, lo, sh[k][c][q][L.lane]);
+        for (int q = 0; q < L.nslot; ++q) two_sum_acc(hi, lo, sh[k][c][q][L.ml]);
         o[c] = hi + lo;
       }
       stv<V>(dst[k], (size_t)L.m0, o);
@@ -203,20 +209,20 @@ __device__ __forceinline__ void block_partials_f(const Lane& L, const float (&v)
 }
 template <int N, int V>
 __device__ __forceinline__ void block_partials_d(const Lane& L, const double (&v)[N][V], double* const (&dst)[N]) {
-  __shared__ double sh[N][V][kMaxBS / 32][32];
+  __shared__ double sh[N][V][kRows][32];
 #pragma unroll
   for (int k = 0; k < N; ++k)
 #pragma unroll
-    for (int c = 0; c < V; ++c) sh[k][c][L.w][L.lane] = v[k][c];
+    for (int c = 0; c < V; ++c) sh[k][c][L.slot][L.ml] = v[k][c];
   __syncthreads();
-  if (L.w == 0) {
+  if (L.slot == 0) {
 #pragma unroll
     for (int k = 0; k < N; ++k) {
       double o[V];
 #pragma unroll
       for (int c = 0; c < V; ++c) {
         double a = 0.0;
-        for (int q = 0; q < L.W; ++q) a += sh[k][c][q][L.lane];
+        for (int q = 0; q < L.nslot; ++q) a += sh[k][c][q][L.ml];
         o[c] = a;
       }
       stv<V>(dst[k], (size_t)L.m0, o);
@@ -286,7 +292,7 @@ __global__ void TMC_ENS_LB(TMC_ENS_CELL_MINB) k_ens_cell(DevMesh Mh, Dims D, IO 
   FF mass[V];
 #pragma unroll
   for (int c = 0; c < V; ++c) rip[c] = r44[c] = eh[c] = el[c] = 0.f, mass[c] = FF{0.f, 0.f};
-  for (int j = L.w; j < nel; j += L.W) {
+  for (int j = L.j0; j < nel; j += L.js) {
     const size_t cm = (size_t)(c0 + j) * Mm + L.m0;
     FF gold[V], gacc[V];
     float tprev[V], gdf[V], ghf[V], gdl[V];
@@ -387,7 +393,7 @@ __global__ void __launch_bounds__(kMaxBS) k_ens_cell_diag(DevMesh Mh, Dims D, IO
   FF mass[V];
 #pragma unroll
   for (int c = 0; c < V; ++c) eh[c] = el[c] = 0.f, mass[c] = FF{0.f, 0.f};
-  for (int j = L.w; j < nel; j += L.W) {
+  for (int j = L.j0; j < nel; j += L.js) {
     const size_t cm = (size_t)(c0 + j) * L.M + L.m0;
     FF g[V];
     float ghf[V];
@@ -444,11 +450,11 @@ __global__ void TMC_ENS_LB(TMC_ENS_VERT_MINB) k_ens_vertex(DevMesh Mh, Dims D, I
   float ph[V], pl[V], ah[V], al[V];
 #pragma unroll
   for (int c = 0; c < V; ++c) ph[c] = pl[c] = ah[c] = al[c] = 0.f;
-  for (int base = L.w; base < nel; base += L.W * kVU) {
+  for (int base = L.j0; base < nel; base += L.js * kVU) {
     float g[kVU][3][V], uu[kVU][3][V];
 #pragma unroll
     for (int q = 0; q < kVU; ++q) {
-      const int j = min(base + q * L.W, nel - 1);
+      const int j = min(base + q * L.js, nel - 1);
 #pragma unroll
       for (int i = 0; i < 3; ++i) {
         ldv<V>(S.gd_in, (size_t)s_c[i][j] * Mm + L.m0, g[q][i]);
@@ -457,7 +463,7 @@ __global__ void TMC_ENS_LB(TMC_ENS_VERT_MINB) k_ens_vertex(DevMesh Mh, Dims D, I
     }
 #pragma unroll
     for (int q = 0; q < kVU; ++q) {
-      const int j = base + q * L.W;
+      const int j = base + q * L.js;
       if (j >= nel) break;
       const float iA = s_iA[j];
       float pv[V], vo[V], gv[V];
@@ -506,17 +512,17 @@ __global__ void __launch_bounds__(kMaxBS) k_ens_edge_pv(DevMesh Mh, Dims D, IO S
   __syncthreads();
   const Lane L = lane_of<V>(D);
   const size_t Mm = L.M;
-  for (int base = L.w; base < nel; base += L.W * kPU) {
+  for (int base = L.j0; base < nel; base += L.js * kPU) {
     float p1[kPU][V], p2[kPU][V];
 #pragma unroll
     for (int q = 0; q < kPU; ++q) {
-      const int j = min(base + q * L.W, nel - 1);
+      const int j = min(base + q * L.js, nel - 1);
       ldv<V>(S.pv_v, (size_t)s_v[0][j] * Mm + L.m0, p1[q]);
       ldv<V>(S.pv_v, (size_t)s_v[1][j] * Mm + L.m0, p2[q]);
     }
 #pragma unroll
     for (int q = 0; q < kPU; ++q) {
-      const int j = base + q * L.W;
+      const int j = base + q * L.js;
       if (j >= nel) break;
       float pe[V];
 #pragma unroll
@@ -566,7 +572,7 @@ __global__ void TMC_ENS_LB(TMC_ENS_FLUX_MINB) k_ens_edge_flux(DevMesh Mh, Dims D
   float rip[V], r44[V];
 #pragma unroll
   for (int c = 0; c < V; ++c) rip[c] = r44[c] = 0.f;
-  for (int j = L.w; j < nel; j += L.W) {
+  for (int j = L.j0; j < nel; j += L.js) {
     const size_t em = (size_t)(e0 + j) * Mm + L.m0;
     const size_t c1m = (size_t)s_c[0][j] * Mm + L.m0, c2m = (size_t)s_c[1][j] * Mm + L.m0;
     float pe[V], uu[V], ge[V], tp[V], accv[V], oldv[V], gn1[V], gn2[V], E1[V], E2[V], t1[V], t2[V];
@@ -657,17 +663,17 @@ __global__ void __launch_bounds__(kMaxBS) k_ens_final_cells(DevMesh Mh, Dims D, 
   for (int c = 0; c < V; ++c) bdt[c] = ff_from(diag[(size_t)(L.m0 + c) * kDiagStride + 9]);
   const int nc = Mh.nc, c0 = blockIdx.x * kEnsEPB, nel = min(kEnsEPB, nc - c0);
   float* gd = const_cast<float*>(S.gd_old);
-  for (int base = L.w; base < nel; base += L.W * kFU) {
+  for (int base = L.j0; base < nel; base += L.js * kFU) {
     FF g[kFU][V], a[kFU][V];
 #pragma unroll
     for (int q = 0; q < kFU; ++q) {
-      const size_t cm = (size_t)(c0 + min(base + q * L.W, nel - 1)) * Mm + L.m0;
+      const size_t cm = (size_t)(c0 + min(base + q * L.js, nel - 1)) * Mm + L.m0;
       ldff<V>(gd, cm, ffs, g[q]);
       ldff<V>(S.gd_acc, cm, ffs, a[q]);
     }
 #pragma unroll
     for (int q = 0; q < kFU; ++q) {
-      const int j = base + q * L.W;
+      const int j = base + q * L.js;
       if (j >= nel) break;
       FF gn[V];
 #pragma unroll
@@ -702,11 +708,11 @@ __global__ void __launch_bounds__(kMaxBS) k_ens_edges(DevMesh Mh, Dims D, IO S, 
   float eh[V], el[V];
 #pragma unroll
   for (int c = 0; c < V; ++c) eh[c] = el[c] = 0.f;
-  for (int base = L.w; base < nel; base += L.W * kFU) {
+  for (int base = L.j0; base < nel; base += L.js * kFU) {
     float ia[kFU][V], ac[kFU][V], g1[kFU][V], g2[kFU][V];
 #pragma unroll
     for (int q = 0; q < kFU; ++q) {
-      const int j = min(base + q * L.W, nel - 1);
+      const int j = min(base + q * L.js, nel - 1);
       const size_t em = (size_t)(e0 + j) * Mm + L.m0;
       ldv<V>(iap, em, ia[q]);
       if (kUpdate) ldv<V>(S.iap_acc, em, ac[q]);
@@ -715,7 +721,7 @@ __global__ void __launch_bounds__(kMaxBS) k_ens_edges(DevMesh Mh, Dims D, IO S, 
     }
 #pragma unroll
     for (int q = 0; q < kFU; ++q) {
-      const int j = base + q * L.W;
+      const int j = base + q * L.js;
       if (j >= nel) break;
       const size_t em = (size_t)(e0 + j) * Mm + L.m0;
       if (kUpdate) {
@@ -756,20 +762,21 @@ __global__ void __launch_bounds__(256) k_ens_reduce(Partials P, RegionList RL, d
   const int r = RL.r[blockIdx.x], count = RL.count[blockIdx.x];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const int m = blockIdx.y * 32 + lane;
+  const bool in = m < P.M;
   double hi = 0.0, lo = 0.0;
   if (r <= R_44_E) {
     float fh = 0.f, fl = 0.f;
-    for (int s = w; s < count; s += nw) two_sum_acc(fh, fl, P.f(r, s)[m]);
+    for (int s = w; in && s < count; s += nw) two_sum_acc(fh, fl, P.f(r, s)[m]);
     hi = (double)fh;
     lo = (double)fl;
   } else {
-    for (int s = w; s < count; s += nw) hi += P.d(r, s)[m];
+    for (int s = w; in && s < count; s += nw) hi += P.d(r, s)[m];
   }
   __shared__ double sh[8][32], sl[8][32];
   sh[w][lane] = hi;
   sl[w][lane] = lo;
   __syncthreads();
-  if (w != 0) return;
+  if (w != 0 || !in) return;
   DD acc{0.0, 0.0};
   for (int k = 0; k < nw; ++k) acc = dd_add(acc, DD{sh[k][lane], sl[k][lane]});
   diag_out[(size_t)m * kDiagStride + kDiagLen + r] = acc.hi + acc.lo;

@@ -1,6 +1,6 @@
 // Member-innermost ensembles (tmc_params.member_layout = 1).
 //
-// M members of one mesh (M a multiple of 32) are stored member-innermost:
+// M members of one mesh (M a multiple of 16) are stored member-innermost:
 // element i of member m sits at [i * M + m].  A warp owns 32 consecutive
 // members of one element at a time, so every neighbour gather of a warp is
 // one 128-byte line (FP32) and every mesh index or metric it needs is the
@@ -34,9 +34,10 @@ namespace ens {
 constexpr int kEnsEPB = 64;  // elements per block (and per partial-sum slot)
 
 struct Dims {
-  int M;  // members (a multiple of 32)
-  int G;  // member groups of 32
-  int V;  // members per lane: 2 when M is a multiple of 64, else 1
+  int M;    // members (a multiple of 16)
+  int G;    // groups of 32 members for the reductions (the last may be partial)
+  int V;    // members per lane: 2 when M is a multiple of 64, else 1
+  int LPE;  // lanes per element: 32, or 16 when M is not a multiple of 32
   int slots_c, slots_e, slots_v;  // partial slots: blocks along cells, edges, vertices
 };
 
