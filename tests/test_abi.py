@@ -40,3 +40,29 @@ def test_create_fails_cleanly_without_gpu_or_with_bad_args():
     p = abi.Params()
     lib.tmc_default_params(ctypes.byref(p))
     assert p.time_scheme == 2 and p.pv_scheme == 3 and p.radius == 6371220.0
+
+
+def test_member_layout_arguments_checked_before_device_set_up():
+    """member_layout 1 refuses member counts that are not a multiple of 16
+    (TMC_E_ARG) and options its kernels do not implement (TMC_E_UNSUP) before
+    any CUDA call, so these checks hold without a GPU."""
+    from conftest import icos
+    from tmcore_gb300 import _lib, abi
+    from tmcore_gb300.gpu import default_params, mesh_desc
+
+    lib = _lib.gpu()
+    d, keep = mesh_desc(icos(2))
+    cases = [
+        (dict(members=40, member_layout=1, precision=1, pv_scheme=1, apvm_weight=0.0, adv_order=2), abi.TMC_E_ARG),
+        (dict(members=32, member_layout=2, precision=1, pv_scheme=1, apvm_weight=0.0, adv_order=2), abi.TMC_E_ARG),
+        (dict(members=32, member_layout=1, precision=1, pv_scheme=3, interp_pv_order=3), abi.TMC_E_UNSUP),
+        (dict(members=32, member_layout=1, precision=1, pv_scheme=1, apvm_weight=0.0, adv_order=2, n_tracers=1),
+         abi.TMC_E_UNSUP),
+        (dict(members=32, member_layout=1, precision=0, pv_scheme=1, apvm_weight=0.0, adv_order=2), abi.TMC_E_UNSUP),
+    ]
+    for kw, code in cases:
+        p = default_params(dt=600.0, **kw)
+        h = ctypes.c_void_p()
+        assert lib.tmc_create(ctypes.byref(d), ctypes.byref(p), ctypes.byref(h)) == code, kw
+        assert h.value and lib.tmc_last_error(h)
+        lib.tmc_destroy(h)
