@@ -71,7 +71,7 @@ typedef struct tmc_params {
   int32_t tracer_adv_order;       /* 0: adv_order */
   int32_t tracer_adv_mono;
   int32_t precision;              /* TMC_FP64 or TMC_FP32 */
-  int32_t renumber;               /* 1: space-filling-curve renumbering at load */
+  int32_t renumber;               /* element order on the device: 0 as given, 1 Hilbert curve, 2 Morton curve */
   int32_t use_graph;              /* 1: one CUDA graph per RK step */
   int32_t diag_every;             /* invariants of the state every k steps (0: only on request) */
   int32_t device;                 /* CUDA device ordinal */

@@ -170,3 +170,28 @@ def test_member_layout_refusals(mesh3):
     assert e.value.code == abi.TMC_E_UNSUP
     net.close()
     ens.close()
+
+
+def test_ordering_autotuner(mesh4):
+    """The ordering autotuner times element orders x member layouts, skips
+    layouts the options do not allow, and its choice runs."""
+    from tmcore_gb300 import tune
+    from tmcore_gb300.gpu import TMCoreGPU
+
+    ics = _ics(mesh4, M, 700)
+    best, timings = tune.autotune_ordering(mesh4, ics, steps=2, dt=600.0, **KW)
+    assert len(timings) == 6 and all("ms_per_step" in t for t in timings), timings
+    assert best["renumber"] in (0, 1, 2) and best["member_layout"] in (0, 1)
+    ens = TMCoreGPU(mesh4, **best)
+    for m, (gd, u, ghs) in enumerate(ics):
+        ens.select_member(m)
+        ens.set_initial(gd, u, ghs)
+    ens.step(3)
+    assert np.all(np.isfinite(ens.diag_all()))
+    ens.close()
+    # pv_scheme 3 has no member-innermost kernels: only member_layout 0 is timed
+    kw = dict(KW, pv_scheme=3, interp_pv_order=3)
+    kw.pop("apvm_weight")
+    best, timings = tune.autotune_ordering(mesh4, ics, steps=1, orders=(1,), dt=600.0, **kw)
+    assert best["member_layout"] == 0
+    assert [t["member_layout"] for t in timings if "error" in t] == [1]

@@ -1054,7 +1054,8 @@ int tmc_create(const tmc_mesh_desc* mesh, const tmc_params* params, tmc_handle**
     return TMC_E_CUDA;
   }
   PrepOptions opt;
-  opt.renumber = p.renumber != 0;
+  if (p.renumber < 0 || p.renumber > 2) return bad("renumber must be 0 (as given), 1 (Hilbert) or 2 (Morton)");
+  opt.renumber = p.renumber;
   if (p.precision == TMC_FP32) {
     // the FP32 kernels unroll over 6 edges per cell and 10 edges per edge
     if (mesh->maxEdges > 6 || mesh->maxEdges2 > 10) {

@@ -48,17 +48,36 @@ uint64_t hilbert_key(double x, double y, double z) {
   return key;
 }
 
+// 3-D Morton (Z-order) index of a point of [-1,1]^3: the bits of the three
+// 20-bit coordinates interleaved, most significant first.
+uint64_t morton_key(double x, double y, double z) {
+  const int b = 20;
+  const double scale = (double)((1u << b) - 1);
+  const double c[3] = {x, y, z};
+  uint32_t X[3];
+  for (int i = 0; i < 3; ++i) {
+    const double t = (std::min(1.0, std::max(-1.0, c[i])) + 1.0) * 0.5;
+    X[i] = (uint32_t)std::llround(t * scale);
+  }
+  uint64_t key = 0;
+  for (int j = b - 1; j >= 0; --j)
+    for (int i = 0; i < 3; ++i) key = (key << 1) | ((X[i] >> j) & 1u);
+  return key;
+}
+
 namespace {
 
-std::vector<int32_t> sfc_order(int n, const double* x, const double* y, const double* z, bool renumber) {
+// element order: 0 the caller's, 1 Hilbert curve, 2 Morton curve of the
+// unit-sphere positions
+std::vector<int32_t> sfc_order(int n, const double* x, const double* y, const double* z, int mode) {
   std::vector<int32_t> order(n);
   std::iota(order.begin(), order.end(), 0);
-  if (!renumber) return order;
+  if (mode == 0) return order;
   std::vector<uint64_t> key(n);
 #pragma omp parallel for schedule(static)
   for (int i = 0; i < n; ++i) {
     double r = std::sqrt(x[i] * x[i] + y[i] * y[i] + z[i] * z[i]);
-    key[i] = hilbert_key(x[i] / r, y[i] / r, z[i] / r);
+    key[i] = mode == 2 ? morton_key(x[i] / r, y[i] / r, z[i] / r) : hilbert_key(x[i] / r, y[i] / r, z[i] / r);
   }
   std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) { return key[a] < key[b]; });
   return order;

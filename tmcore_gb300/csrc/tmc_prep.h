@@ -65,7 +65,7 @@ struct HostMesh {
 };
 
 struct PrepOptions {
-  bool renumber = true;
+  int renumber = 1;  // element order: 0 as given, 1 Hilbert curve, 2 Morton curve
   bool cell_fit = false;    // deriv2/3/4OnCell tables
   int min_me = 0;           // pad the per-cell slot arrays to at least this many slots
   int min_me2 = 0;          // pad the per-edge edgesOnEdge/weightsOnEdge slots
@@ -77,5 +77,7 @@ bool prepare_mesh(const tmc_mesh_desc& d, const tmc_params& p, const PrepOptions
 
 // 3-D Hilbert index of a point of the unit cube [-1,1]^3 (Skilling 2004).
 uint64_t hilbert_key(double x, double y, double z);
+// 3-D Morton (bit-interleaved) index of a point of [-1,1]^3.
+uint64_t morton_key(double x, double y, double z);
 
 }  // namespace tmc

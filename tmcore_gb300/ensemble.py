@@ -11,7 +11,7 @@ import json
 
 import numpy as np
 
-from . import abi, cases
+from . import abi, cases, tune
 from .gpu import ClosureMLP, TMCoreGPU
 from .mesh import icos_mesh
 
@@ -26,14 +26,20 @@ def main():
     ap.add_argument("--autotune", action="store_true")
     ap.add_argument("--distinct-seeds", action="store_true", help="seed m for member m (else one seed for all)")
     ap.add_argument("--layout", type=int, default=0, help="member_layout: 0 member-outermost, 1 member-innermost")
+    ap.add_argument("--tune-ordering", action="store_true",
+                    help="time element orders x member layouts first (tune.autotune_ordering) and use the fastest")
     a = ap.parse_args()
     m = icos_mesh(a.level)
     dt = 1200.0 / 2 ** (a.level - 4)
-    ens = TMCoreGPU(m, members=a.members, dt=dt, precision=abi.TMC_FP32, pv_scheme=1, apvm_weight=0.0,
-                    adv_order=2, diag_every=1, member_layout=a.layout)
     ic = None if a.distinct_seeds else cases.jet_bumps(m, seed=0)
-    for k in range(a.members):
-        gd, u, ghs = cases.jet_bumps(m, seed=k) if a.distinct_seeds else ic
+    ics = [cases.jet_bumps(m, seed=k) if a.distinct_seeds else ic for k in range(a.members)]
+    params = dict(members=a.members, dt=dt, precision=abi.TMC_FP32, pv_scheme=1, apvm_weight=0.0, adv_order=2,
+                  diag_every=1, member_layout=a.layout)
+    orderings = None
+    if a.tune_ordering:
+        params, orderings = tune.autotune_ordering(m, ics, **params)
+    ens = TMCoreGPU(m, **params)
+    for k, (gd, u, ghs) in enumerate(ics):
         ens.select_member(k)
         ens.set_initial(gd, u, ghs)
     net = None
@@ -41,11 +47,12 @@ def main():
         net = ClosureMLP(seed=1)
         net.set_scaling(np.zeros(24), np.ones(24), 1e-12)
         ens.set_closure(net)
-    sizes = ens.autotune(2) if a.autotune else None
+    sizes = ens.autotune(2) if (a.autotune or a.tune_ordering) else None
     ens.step(a.warmup)
     ens.synchronize()
     ms, _, _, launches = ens.time_steps(a.steps, total=True, flux=False)
-    print(json.dumps({"members": a.members, "level": a.level, "layout": a.layout, "closure": a.closure,
+    print(json.dumps({"members": a.members, "level": a.level, "layout": params["member_layout"],
+                      "renumber": params.get("renumber", 1), "orderings": orderings, "closure": a.closure,
                       "ms_per_step": ms / a.steps,
                       "member_days_per_s": a.members * a.steps * dt / 86400.0 / (ms / 1e3),
                       "gpu_launches": launches, "block_sizes": sizes,
