@@ -164,12 +164,50 @@ def test_member_layout_refusals(mesh3):
         TMCoreGPU(mesh3, dt=600.0, members=32, member_layout=1, precision=1, pv_scheme=3, interp_pv_order=3)
     assert e.value.code == abi.TMC_E_UNSUP
     ens = TMCoreGPU(mesh3, dt=600.0, members=32, member_layout=1, **KW)
-    net = ClosureMLP(seed=0)
-    with pytest.raises(TMCError) as e:
-        ens.set_closure(net)
+    from tmcore_gb300 import cases
+    ens.set_initial(*cases.jet_bumps(mesh3, seed=1))
+    with pytest.raises(TMCError) as e:  # training features come from member_layout 0 models
+        ens.closure_features()
     assert e.value.code == abi.TMC_E_UNSUP
-    net.close()
     ens.close()
+
+
+@pytest.mark.parametrize("every_stage", [True, False])
+def test_closure_matches_member_outermost(mesh4, every_stage):
+    """The learned closure in the member-innermost step (network on rows
+    [edge][member]) agrees with the member-outermost step to FP32 rounding;
+    a member whose switch is off evolves as the plain model."""
+    from tmcore_gb300.gpu import ClosureMLP, TMCoreGPU
+
+    net = ClosureMLP(seed=2)
+    p = net.params
+    p *= 0.5
+    net.params = p
+    net.set_scaling(np.zeros(24), np.ones(24), 1e-9)  # corrections of order 1e-9 (pv ~ 1e-8)
+    ics = _ics(mesh4, M, 800)
+    kw = dict(dt=600.0, conserve_energy=1)
+    inner, outer, plain = _ensemble(mesh4, ics, 1, **kw), _ensemble(mesh4, ics, 0, **kw), _ensemble(mesh4, ics, 1, **kw)
+    for x in (inner, outer):
+        x.set_closure(net)
+        x.set_closure_stages(every_stage)
+        x.set_member_closure(5, False)
+    for x in (inner, outer, plain):
+        x.step(6)
+    assert not inner.closure_status()
+    for m in (0, 5, M - 1):
+        for x in (inner, outer, plain):
+            x.select_member(m)
+        gi, ii, _ = inner.get_state()
+        go, io, _ = outer.get_state()
+        gp, ip, _ = plain.get_state()
+        assert rel_max(gi, go) < 1e-6 and rel_max(ii, io) < 1e-5, (m, rel_max(gi, go), rel_max(ii, io))
+        if m == 5:
+            assert rel_max(gi, gp) < 1e-6 and rel_max(ii, ip) < 1e-5, m
+        else:
+            assert rel_max(ii, ip) > 1e-4, (m, rel_max(ii, ip))  # the closure acts
+    for x in (inner, outer, plain):
+        x.close()
+    net.close()
 
 
 def test_ordering_autotuner(mesh4):

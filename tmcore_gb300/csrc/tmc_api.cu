@@ -668,6 +668,7 @@ struct EnsEngine : EngineBase {
   float* u[2] = {};
   float* F[2] = {};
   float *E = nullptr, *pv_v = nullptr, *vor = nullptr, *gd_v = nullptr, *pv_e = nullptr;
+  float* pv_c = nullptr;  // pv on cells (the learned closure's features)
   float *invA_hl = nullptr, *A_hl = nullptr;
   float *cdv = nullptr, *cae = nullptr, *vdc = nullptr;
   explicit EnsEngine(tmc_handle* hh) : h(hh) {}
@@ -704,6 +705,7 @@ struct EnsEngine : EngineBase {
     vor = h->dalloc<float>(nv);
     gd_v = h->dalloc<float>(nv);
     pv_e = h->dalloc<float>(ne);
+    pv_c = h->dalloc<float>(nc);
     // 1 / areaCell and areaCell as double-float pairs [2][nCells]
     const int ncell = h->M.nc;
     std::vector<float> ia(2 * (size_t)ncell), a(2 * (size_t)ncell);
@@ -731,7 +733,8 @@ struct EnsEngine : EngineBase {
     cdv = h->upload(v_cdv);
     cae = h->upload(v_cae);
     vdc = h->upload(v_vdc);
-    if (!EP.sf || !EP.sd || !pv_e || !F[1] || !gd_v || !invA_hl || !A_hl || !cdv || !cae || !vdc) return TMC_E_CUDA;
+    if (!EP.sf || !EP.sd || !pv_e || !pv_c || !F[1] || !gd_v || !invA_hl || !A_hl || !cdv || !cae || !vdc)
+      return TMC_E_CUDA;
     cudaMemset(ghs, 0, sizeof(double) * nc);
     cudaMemset(ghsf, 0, sizeof(float) * nc);
     return TMC_OK;
@@ -775,7 +778,10 @@ struct EnsEngine : EngineBase {
     return s;
   }
 
-  int launches_per_step() const override { return 4 * 4 + 2 + 2; }
+  int launches_per_step() const override {
+    const int closure = !h->closure ? 0 : (h->closure_every_stage ? 4 * 2 : 2 + 3);
+    return 4 * 4 + 2 + 2 + closure;
+  }
 
   void launch_prep() override { ens::launch_edge_prep(h->M, D, io(0), EP, true, h->bsp[P_FINAL], h->st); }
 
@@ -801,6 +807,14 @@ struct EnsEngine : EngineBase {
       mark(P_VERTEX);
       mark(P_PV);
       ens::launch_edge_pv(M, D, s, b[P_PV], h->st);
+      if (h->closure) {
+        // the learned closure on this stage's pv_edge: in every stage, or in
+        // stage 1 with its output held for stages 2-4
+        const int mode = h->closure_every_stage ? 0 : (k == 1 ? 1 : 2);
+        if (mode != 2) ens::launch_v2c(M, D, s, pv_c, h->st);
+        const ClosureArgs a{&h->closure_net, h->d_member_on, h->d_closure_err, h->sms, h->d_closure_dq, mode};
+        ens::launch_closure(M, D, s, pv_c, a, h->st);
+      }
       mark(P_PV);
       mark(P_FLUX);
       ens::launch_edge_flux(M, D, s, rk, EP, b[P_FLUX], h->st);
@@ -865,7 +879,8 @@ struct EnsEngine : EngineBase {
     *gh = ghs;
   }
   void refresh_all_shadows() override {}
-  void closure_features(float*, float*) override {}  // tmc_closure_features refuses member_layout 1
+  void closure_features(float*, float*) override {}  // tmc_closure_features refuses member_layout 1 (training
+                                                     // features come from member_layout 0 models)
 
   // history fields of the selected member: its u, gd and ghs copied out of
   // the member-innermost arrays, then the single-model kernels
@@ -1619,7 +1634,6 @@ int tmc_set_closure(tmc_handle* h, const tmc_mlp* net) {
   TMC_REQUIRE_SWM(h);
   if (net && (h->p.precision != TMC_FP32 || h->generic))
     return h->fail(TMC_E_UNSUP, "the learned closure runs in the FP32 CRK4 shallow-water step");
-  if (net && h->p.member_layout == 1) return h->fail(TMC_E_UNSUP, "the learned closure needs member_layout 0");
   if (sync(h, "tmc_set_closure")) return TMC_E_CUDA;
   h->closure = net;
   if (net) h->closure_net = tmc_mlp_net(net);

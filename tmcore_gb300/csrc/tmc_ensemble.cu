@@ -810,6 +810,25 @@ __global__ void k_ens_beta(int M, int step, int diag, int conserve, double total
   }
 }
 
+// pv on cells for the learned closure: scalar_v2c_interp_operator as a
+// gather over the cell's vertices (operators_mod.F90:125-141), the FP32
+// arithmetic of k_v2c; block = one cell, threads = members
+__global__ void k_ens_v2c(DevMesh Mh, int M, const float* pv_v, float* pv_c) {
+  const int c = blockIdx.x, m = blockIdx.y * blockDim.x + threadIdx.x;
+  if (m >= M) return;
+  const float A = (float)Mh.areaCell[c];
+  float s = 0.f;
+  for (int k = Mh.v2c_start[c]; k < Mh.v2c_start[c + 1]; ++k)
+    s = s + pv_v[(size_t)Mh.v2c_vertex[k] * M + m] * (float)Mh.v2c_kite[k] / A;
+  pv_c[(size_t)c * M + m] = s;
+}
+
+// the held closure correction of stage 1 added to pv_edge in stages 2-4
+__global__ void k_ens_closure_hold(size_t n, float* pv_e, const float* dq) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) pv_e[i] += dq[i];
+}
+
 // ---- state transfer ----
 __global__ void k_ens_gather_f64(int n, int M, int m, const double* raw, const int32_t* n2o, double* dst) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -952,6 +971,14 @@ void launch_finalize(const Dims& D, const Partials& P, bool step, bool diag, boo
   k_ens_reduce<<<dim3(RL.n, D.G), 256, 0, st>>>(P, RL, diag_out);
   k_ens_beta<<<nb(D.M), 256, 0, st>>>(D.M, step ? 1 : 0, diag ? 1 : 0, conserve ? 1 : 0, totalArea,
                                       sumAreaTriangle, dt, diag_out);
+}
+
+void launch_v2c(const DevMesh& Mh, const Dims& D, const IO& S, float* pv_c, cudaStream_t st) {
+  k_ens_v2c<<<dim3(Mh.nc, (D.M + 127) / 128), 128, 0, st>>>(Mh, D.M, S.pv_v, pv_c);
+}
+void launch_closure_hold(const DevMesh& Mh, const Dims& D, const IO& S, const float* dq, cudaStream_t st) {
+  const size_t n = (size_t)Mh.ne * D.M;
+  k_ens_closure_hold<<<nb(n), 256, 0, st>>>(n, S.pv_e, dq);
 }
 
 void launch_gather_f64(int n, int M, int m, const double* raw, const int32_t* n2o, double* dst, cudaStream_t st) {

@@ -112,6 +112,15 @@ void launch_cell_diag(const DevMesh& Mh, const Dims& D, const IO& S, const Parti
 void launch_finalize(const Dims& D, const Partials& P, bool step, bool diag, bool conserve, double totalArea,
                      double sumAreaTriangle, double dt, double* diag_out, cudaStream_t st);
 
+// The learned PV-on-edge closure (after the pv-on-edge pass): pv on cells
+// (the network reads it), then the network on rows [edge][member] with its
+// output added to pv_edge of members whose switch is on (a.mode 0 every stage;
+// 1 stage 1, output also held in a.dq; 2 add the held a.dq only)
+void launch_v2c(const DevMesh& Mh, const Dims& D, const IO& S, float* pv_c, cudaStream_t st);
+void launch_closure_hold(const DevMesh& Mh, const Dims& D, const IO& S, const float* dq, cudaStream_t st);
+void launch_closure(const DevMesh& Mh, const Dims& D, const IO& S, const float* pv_c, const ClosureArgs& a,
+                    cudaStream_t st);
+
 // state transfer of member m (caller's element order <-> member-innermost);
 // _ff: an FF array (h, then l at offset n * M)
 void launch_gather_f64(int n, int M, int m, const double* raw, const int32_t* n2o, double* dst, cudaStream_t st);

@@ -9,6 +9,7 @@
 #include <string>
 #include <vector>
 
+#include "tmc_ensemble.cuh"
 #include "tmc_kernels.cuh"
 #include "tmc_mlp_tc.cuh"
 #include "tmcore_gpu.h"
@@ -117,6 +118,71 @@ struct ClosureSrc {
     if (on[m]) S.pv_e[k] = S.pv_e[k] + v;
   }
 };
+
+// Rows of the member-innermost layout: row i = element i / M, member i % M,
+// the order of the arrays, so the 128 rows of a tile read whole lines.  The
+// features are those of closure_features, from [element][member] arrays.
+struct EnsClosureSrc {
+  DevMesh M;
+  tmc::ens::IO S;
+  const float* pv_c;
+  const int* on;
+  float* dq;  // non-null: the correction is also held here (0 for members switched off)
+  int mem;
+  long long rows;
+  __device__ bool features(long long i, float (&x)[kIn]) const {
+    if (i >= rows) return false;
+    const int e = (int)(i / mem), m = (int)(i - (long long)e * mem);
+    const size_t W = (size_t)mem;
+    const int c1 = M.cellsOnEdge[e], c2 = M.cellsOnEdge[M.ne + e];
+    const int v1 = M.verticesOnEdge[e], v2 = M.verticesOnEdge[M.ne + e];
+    float ve = 0.f;
+#pragma unroll
+    for (int k = 0; k < 10; ++k) {
+      const size_t s = (size_t)k * M.ne + e;
+      ve += S.u[M.edgesOnEdge[s] * W + m] * M.weightsOnEdge_f[s];  // padded entries carry weight 0
+    }
+    const float dv = M.dvEdge_f[e], dc = M.dcEdge_f[e];
+    const float pv1 = S.pv_v[v1 * W + m], pv2 = S.pv_v[v2 * W + m];
+    const float pc1 = pv_c[c1 * W + m], pc2 = pv_c[c2 * W + m];
+    x[0] = S.u[i];
+    x[1] = ve;
+    x[2] = S.gd_e[i];
+    x[3] = S.pv_e[i];
+    x[4] = pv1;
+    x[5] = pv2;
+    x[6] = pc1;
+    x[7] = pc2;
+    x[8] = S.gd_in[c1 * W + m];  // h halves: the FP32 gd
+    x[9] = S.gd_in[c2 * W + m];
+    x[10] = S.E[c1 * W + m];
+    x[11] = S.E[c2 * W + m];
+    x[12] = S.ghsf[c1 * W + m];
+    x[13] = S.ghsf[c2 * W + m];
+    x[14] = M.fVertex_f[v1];
+    x[15] = M.fVertex_f[v2];
+    x[16] = dv;
+    x[17] = dc;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) x[18 + k] = S.u[M.edgesOnEdge[(size_t)k * M.ne + e] * W + m];
+    x[22] = (pv2 - pv1) / dv;
+    x[23] = (pc2 - pc1) / dc;
+    return true;
+  }
+  __device__ void output(long long i, float r) const {
+    if (i >= rows) return;
+    const int m = (int)(i % mem);
+    const float v = on[m] ? r : 0.f;
+    if (dq) dq[i] = v;
+    if (on[m]) S.pv_e[i] = S.pv_e[i] + v;
+  }
+};
+
+__global__ void __launch_bounds__(kTcThreads) k_closure_inner(Net net, EnsClosureSrc src, long long ntiles,
+                                                               int* err) {
+  extern __shared__ __align__(128) uint8_t smem[];
+  if (!forward_tiles(net, src, ntiles, smem) && threadIdx.x == 0) atomicExch(err, 1);
+}
 
 // the held correction of stage 1 added to pv_edge in the later stages
 __global__ void k_closure_hold(float* pv_e, const float* dq, int ne, long long mse) {
@@ -373,6 +439,25 @@ void launch_closure(const DevMesh& M, const StageIO<float>& S, const ClosureArgs
   }
   k_closure<<<grid, kTcThreads, kSmemTc, st>>>(*static_cast<const Net*>(a.net), src, ntiles, a.err);
 }
+namespace ens {
+void launch_closure(const DevMesh& Mh, const Dims& D, const IO& S, const float* pv_c, const ClosureArgs& a,
+                    cudaStream_t st) {
+  if (a.mode == 2) {
+    launch_closure_hold(Mh, D, S, a.dq, st);
+    return;
+  }
+  const long long rows = (long long)Mh.ne * D.M;
+  EnsClosureSrc src{Mh, S, pv_c, a.member_on, a.mode == 1 ? a.dq : nullptr, D.M, rows};
+  const long long ntiles = (rows + kTile - 1) / kTile;
+  const int grid = (int)std::min<long long>(ntiles, (long long)a.sms * 8);
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_closure_inner, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemTc);
+    attr = true;
+  }
+  k_closure_inner<<<grid, kTcThreads, kSmemTc, st>>>(*static_cast<const Net*>(a.net), src, ntiles, a.err);
+}
+}  // namespace ens
 void launch_closure_features(const DevMesh& M, const StageIO<float>& S, int member, float* feat, float* pv,
                              cudaStream_t st) {
   k_closure_features<<<(M.ne + 255) / 256, 256, 0, st>>>(M, S, member, feat, pv);
