@@ -36,9 +36,9 @@ struct BufSrc {
   __device__ void output(long long i, float v) const { y[i] = v; }
 };
 
-__global__ void __launch_bounds__(kTcThreads) k_mlp_fwd_tc(Net net, BufSrc src, long long ntiles, int* err) {
+__global__ void __launch_bounds__(kTcThreads, kTcMinBlocks) k_mlp_fwd_tc(Net net, BufSrc src, long long ntiles, int* err) {
   extern __shared__ __align__(128) uint8_t smem[];
-  if (!forward_tiles(net, src, ntiles, smem) && threadIdx.x == 0) atomicExch(err, 1);
+  if (!forward_tiles(net, src, ntiles, smem) && threadIdx.x % kTile == 0) atomicExch(err, 1);
 }
 
 // ---------------------------------------------------------------------------
@@ -178,10 +178,10 @@ struct EnsClosureSrc {
   }
 };
 
-__global__ void __launch_bounds__(kTcThreads) k_closure_inner(Net net, EnsClosureSrc src, long long ntiles,
+__global__ void __launch_bounds__(kTcThreads, kTcMinBlocks) k_closure_inner(Net net, EnsClosureSrc src, long long ntiles,
                                                                int* err) {
   extern __shared__ __align__(128) uint8_t smem[];
-  if (!forward_tiles(net, src, ntiles, smem) && threadIdx.x == 0) atomicExch(err, 1);
+  if (!forward_tiles(net, src, ntiles, smem) && threadIdx.x % kTile == 0) atomicExch(err, 1);
 }
 
 // the held correction of stage 1 added to pv_edge in the later stages
@@ -192,9 +192,9 @@ __global__ void k_closure_hold(float* pv_e, const float* dq, int ne, long long m
   pv_e[k] += dq[k];
 }
 
-__global__ void __launch_bounds__(kTcThreads) k_closure(Net net, ClosureSrc src, long long ntiles, int* err) {
+__global__ void __launch_bounds__(kTcThreads, kTcMinBlocks) k_closure(Net net, ClosureSrc src, long long ntiles, int* err) {
   extern __shared__ __align__(128) uint8_t smem[];
-  if (!forward_tiles(net, src, ntiles, smem) && threadIdx.x == 0) atomicExch(err, 1);
+  if (!forward_tiles(net, src, ntiles, smem) && threadIdx.x % kTile == 0) atomicExch(err, 1);
 }
 
 __global__ void k_closure_features(DevMesh M, StageIO<float> S, int m, float* feat, float* pv) {
@@ -431,7 +431,7 @@ void launch_closure(const DevMesh& M, const StageIO<float>& S, const ClosureArgs
   }
   ClosureSrc src{M, S, a.member_on, a.mode == 1 ? a.dq : nullptr, members, tpm};
   const long long ntiles = (long long)tpm * members;
-  const int grid = (int)std::min<long long>(ntiles, (long long)a.sms * 8);
+  const int grid = (int)std::min<long long>((ntiles + kGroups - 1) / kGroups, (long long)a.sms * 4);
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(k_closure, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemTc);
@@ -449,7 +449,7 @@ void launch_closure(const DevMesh& Mh, const Dims& D, const IO& S, const float* 
   const long long rows = (long long)Mh.ne * D.M;
   EnsClosureSrc src{Mh, S, pv_c, a.member_on, a.mode == 1 ? a.dq : nullptr, D.M, rows};
   const long long ntiles = (rows + kTile - 1) / kTile;
-  const int grid = (int)std::min<long long>(ntiles, (long long)a.sms * 8);
+  const int grid = (int)std::min<long long>((ntiles + kGroups - 1) / kGroups, (long long)a.sms * 4);
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(k_closure_inner, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemTc);
@@ -613,7 +613,7 @@ int tmc_mlp_forward(tmc_mlp* n, const float* x, int64_t rows, float* y, int32_t 
   cudaMemcpyAsync(n->io_x, x, sizeof(float) * kIn * rows, cudaMemcpyHostToDevice, n->st);
   if (tensor_cores) {
     const long long ntiles = (rows + kTile - 1) / kTile;
-    const int grid = (int)std::min<long long>(ntiles, (long long)n->sms * 8);
+    const int grid = (int)std::min<long long>((ntiles + kGroups - 1) / kGroups, (long long)n->sms * 4);
     cudaMemsetAsync(n->d_err, 0, sizeof(int), n->st);
     k_mlp_fwd_tc<<<grid, kTcThreads, kSmemTc, n->st>>>(n->net(), BufSrc{n->io_x, n->io_y, rows}, ntiles, n->d_err);
   } else {

@@ -24,7 +24,17 @@ constexpr int kIn = 24;     // features per edge
 constexpr int kInPad = 32;  // first-layer K padded to two MMA K-steps
 constexpr int kH = 64;      // hidden width
 constexpr int kTile = 128;  // edges per tensor-core tile (MMA M)
-constexpr int kTcThreads = 128;  // threads per block of the tensor-core forward (one per row)
+constexpr int kGroups = 2;       // tiles in flight per block of the tensor-core forward
+constexpr int kTcThreads = kTile * kGroups;  // one thread per row of each tile
+// blocks per SM the tensor-core forward is compiled for: its shared memory
+// (53 KB) allows 4, whose 4 x 128 accumulator columns fill the 512 of TMEM,
+// so an allocation never waits.  4 (64 registers, ~100 bytes spilled) beats
+// 3 and 2: 256 level-6 members with the closure in every stage take 13.4 ms
+// per step against 14.9 and 14.8 (one tile group per block: 14.2)
+#ifndef TMC_TC_MIN_BLOCKS
+#define TMC_TC_MIN_BLOCKS 4
+#endif
+constexpr int kTcMinBlocks = TMC_TC_MIN_BLOCKS;
 
 // parameter vector layout (FP32 master copy; the BF16 copy has the same layout)
 constexpr int kOffW1 = 0;
@@ -54,7 +64,7 @@ __device__ __forceinline__ float gelu_arg(float x) { return 0.7978845608028654f 
 constexpr int kSmemW1 = kH * kInPad * 2;  // 4 KB
 constexpr int kSmemW = kH * kH * 2;       // 8 KB
 constexpr int kSmemA = kTile * kH * 2;    // 16 KB
-constexpr int kSmemTc = kSmemW1 + 2 * kSmemW + kSmemA + 64;
+constexpr int kSmemTc = kSmemW1 + 2 * kSmemW + kGroups * kSmemA + 64;
 
 }  // namespace mlp
 }  // namespace tmc

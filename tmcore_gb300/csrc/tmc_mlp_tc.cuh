@@ -155,23 +155,29 @@ __device__ __forceinline__ bool group_sync_and(int id, bool v) {
 
 // Forward of the MLP over tiles of 128 rows on the tensor cores.  Src
 // provides, for row index i, `bool features(long long i, float (&x)[kIn])`
-// (false: no row) and `void output(long long i, float y)`.  128 threads per
-// block; thread t owns row t of every tile (TMEM lane t).  The features of
-// the block's next tile are loaded while the current tile runs through the
-// three layers.  Returns false when an mbarrier wait ran out (uniformly over
-// the block).
+// (false: no row) and `void output(long long i, float y)`.  A block runs
+// kGroups tile groups of 128 threads that share the staged weights: group g
+// takes tiles kGroups * blockIdx.x + g, + kGroups * gridDim.x, ... with its
+// own operand buffer, mbarrier, 64 accumulator columns and named barrier, so
+// one group's epilogue overlaps the other's MMAs.  Thread r of a group owns
+// row r of its tiles (TMEM lane r).  The features of the group's next tile
+// are loaded while the current tile runs through the three layers.  Returns
+// false when an mbarrier wait ran out (uniformly over the group).
 template <class Src>
 __device__ bool forward_tiles(const Net& net, Src& src, long long ntiles, uint8_t* smem) {
   uint8_t* sW1 = smem;
   uint8_t* sW2 = sW1 + kSmemW1;
   uint8_t* sW3 = sW2 + kSmemW;
-  uint8_t* sA = sW3 + kSmemW;
-  uint64_t* mbar = reinterpret_cast<uint64_t*>(sA + kSmemA);
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 1);
+  uint8_t* sA0 = sW3 + kSmemW;  // kGroups tile operands
+  uint64_t* mbar0 = reinterpret_cast<uint64_t*>(sA0 + kGroups * kSmemA);  // one mbarrier per group
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar0 + kGroups);
   __shared__ float sb[3][kH];
   __shared__ float sw4[kH];
   __shared__ float sxm[kIn], sxi[kIn];
   const int t = threadIdx.x, warp = t >> 5;
+  // tile group of this thread (its own tiles, operand, mbarrier, accumulator
+  // columns and named barrier) and its row in the group's tiles
+  const int grp = t / kTile, r = t % kTile, bar = 1 + grp;
 
   // weights (BF16, K-major: row = output unit, K = input).  Layer 1: its
   // bias as two BF16 columns (high and low part) against input columns 24-25
@@ -205,14 +211,14 @@ __device__ bool forward_tiles(const Net& net, Src& src, long long ntiles, uint8_
     sxi[i] = net.xinv[i];
   }
   const float b4 = net.p[kOffB4];
-  const uint32_t mb = smem_u32(mbar);
-  if (t == 0) {
+  const uint32_t mb = smem_u32(mbar0 + grp);
+  if (r == 0) {
     mbar_init(mb, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
-                 "r"(kH)
+                 "r"(kH * kGroups)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -220,18 +226,20 @@ __device__ bool forward_tiles(const Net& net, Src& src, long long ntiles, uint8_
   fence_before_sync();
   __syncthreads();
   fence_after_sync();
-  const uint32_t tmem = *tslot;
-  const uint32_t tl = tmem + ((uint32_t)(warp * 32) << 16);  // this warp's lane quarter
+  const uint32_t tmem = *tslot + (uint32_t)(grp * kH);  // this group's accumulator columns
+  const uint32_t tl = tmem + ((uint32_t)((warp & 3) * 32) << 16);  // this warp's lane quarter
   constexpr uint32_t kIdesc = idesc_bf16_f32(kTile, kH);
+  uint8_t* sA = sA0 + grp * kSmemA;
   const uint32_t aA = smem_u32(sA), aW[3] = {smem_u32(sW1), smem_u32(sW2), smem_u32(sW3)};
   uint32_t phase = 0;
   bool ok = true;
 
-  long long tile = blockIdx.x;
+  const long long stride = (long long)gridDim.x * kGroups;
+  long long tile = (long long)blockIdx.x * kGroups + grp;
   float xn[kIn];
-  bool vn = tile < ntiles ? src.features(tile * kTile + t, xn) : false;
-  for (; tile < ntiles; tile += gridDim.x) {
-    const long long row = tile * kTile + t;
+  bool vn = tile < ntiles ? src.features(tile * kTile + r, xn) : false;
+  for (; tile < ntiles; tile += stride) {
+    const long long row = tile * kTile + r;
     const bool valid = vn;
     {
       float xs[kInPad];
@@ -242,21 +250,21 @@ __device__ bool forward_tiles(const Net& net, Src& src, long long ntiles, uint8_
 #pragma unroll
       for (int k = kIn + 2; k < kInPad; ++k) xs[k] = 0.f;
 #pragma unroll
-      for (int k0 = 0; k0 < kInPad; k0 += 8) store8_bf16(sA, t, k0, kInPad, xs + k0);
+      for (int k0 = 0; k0 < kInPad; k0 += 8) store8_bf16(sA, r, k0, kInPad, xs + k0);
     }
     fence_async_smem();
     fence_before_sync();
-    __syncthreads();
+    group_sync(bar);
     // the next tile's features, in flight during this tile's layers
     {
-      const long long nt = tile + gridDim.x;
-      vn = nt < ntiles ? src.features(nt * kTile + t, xn) : false;
+      const long long nt = tile + stride;
+      vn = nt < ntiles ? src.features(nt * kTile + r, xn) : false;
     }
     float y = b4;
 #pragma unroll 1
     for (int l = 0; l < 3; ++l) {
       const int K = l == 0 ? kInPad : kH;
-      if (t == 0) {
+      if (r == 0) {
         fence_after_sync();
         for (int k = 0; k < K / 16; ++k) {
           const uint64_t ad = smem_desc(aA + k * 256, 128, (uint32_t)(K / 8) * 128);
@@ -267,7 +275,7 @@ __device__ bool forward_tiles(const Net& net, Src& src, long long ntiles, uint8_
       }
       const bool got = mbar_wait(mb, phase);
       phase ^= 1u;
-      ok = __syncthreads_and(got ? 1 : 0) != 0;
+      ok = group_sync_and(bar, got);
       if (!ok) break;
       fence_after_sync();
 #pragma unroll
@@ -289,8 +297,8 @@ __device__ bool forward_tiles(const Net& net, Src& src, long long ntiles, uint8_
         if (l < 2) {
 #pragma unroll
           for (int q = 0; q < 2; ++q) {
-            *reinterpret_cast<uint4*>(sA + core_off(t, c0 + 16 * q, kH)) = *reinterpret_cast<uint4*>(&h[q][0]);
-            *reinterpret_cast<uint4*>(sA + core_off(t, c0 + 16 * q + 8, kH)) = *reinterpret_cast<uint4*>(&h[q][4]);
+            *reinterpret_cast<uint4*>(sA + core_off(r, c0 + 16 * q, kH)) = *reinterpret_cast<uint4*>(&h[q][0]);
+            *reinterpret_cast<uint4*>(sA + core_off(r, c0 + 16 * q + 8, kH)) = *reinterpret_cast<uint4*>(&h[q][4]);
           }
         } else {
 #pragma unroll
@@ -304,7 +312,7 @@ __device__ bool forward_tiles(const Net& net, Src& src, long long ntiles, uint8_
       }
       if (l < 2) fence_async_smem();
       fence_before_sync();
-      __syncthreads();
+      group_sync(bar);
     }
     if (!ok) break;
     if (valid) src.output(row, y * net.yscale);
@@ -312,7 +320,8 @@ __device__ bool forward_tiles(const Net& net, Src& src, long long ntiles, uint8_
   fence_before_sync();
   __syncthreads();
   fence_after_sync();
-  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kH) : "memory");
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(*tslot), "r"(kH * kGroups) : "memory");
   return ok;
 }
 
