@@ -868,7 +868,7 @@ struct EnsEngine : EngineBase {
   void refresh_shadows(int) override {}  // the h halves of gd are its FP32 values
   void set_ghs_dev(const double* raw) override {
     ens::launch_gather_f64(h->M.nc, D.M, h->cur, raw, h->d_cell_n2o, ghs, h->st);
-    ens::launch_shadow(h->M.nc, D.M, h->cur, ghs, ghsf, h->st);
+    ens::launch_to_f32(h->M.nc, D.M, h->cur, ghs, ghsf, h->st);
   }
   void adv_set_initial_dev(const double*) override {}
   void adv_get_dev(double*, double*) override {}

@@ -866,11 +866,11 @@ __global__ void k_ens_iap_from_u(int ne, int M, int m, const double* gd_e, const
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < ne) iap[(size_t)i * M + m] = (float)(sqrt(gd_e[i]) * u[i]);
 }
-__global__ void k_ens_shadow(size_t n, int M, int m, const double* gd, float* gdf) {
+__global__ void k_ens_to_f32(size_t n, int M, int m, const double* src, float* dst) {
   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const size_t k = m < 0 ? i : i * M + m;
-  gdf[k] = (float)gd[k];
+  dst[k] = (float)src[k];
 }
 
 inline unsigned nb(size_t n) { return (unsigned)((n + 255) / 256); }
@@ -1008,9 +1008,9 @@ void launch_extract_ff(int n, int M, int m, const float* src, double* dst, cudaS
 void launch_iap_from_u(int ne, int M, int m, const double* gd_e, const double* u, float* iap, cudaStream_t st) {
   k_ens_iap_from_u<<<nb(ne), 256, 0, st>>>(ne, M, m, gd_e, u, iap);
 }
-void launch_shadow(int nc, int M, int m, const double* gd, float* gdf, cudaStream_t st) {
-  const size_t n = m < 0 ? (size_t)nc * M : (size_t)nc;
-  k_ens_shadow<<<nb(n), 256, 0, st>>>(n, M, m, gd, gdf);
+void launch_to_f32(int n, int M, int m, const double* src, float* dst, cudaStream_t st) {
+  const size_t k = m < 0 ? (size_t)n * M : (size_t)n;
+  k_ens_to_f32<<<nb(k), 256, 0, st>>>(k, M, m, src, dst);
 }
 
 }  // namespace ens

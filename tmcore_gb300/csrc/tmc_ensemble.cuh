@@ -134,8 +134,8 @@ void launch_extract_f32(int n, int M, int m, const float* src, double* dst, cuda
 void launch_extract_ff(int n, int M, int m, const float* src, double* dst, cudaStream_t st);
 // iap_u of member m = sqrt(gd_edge) u (internal order inputs)
 void launch_iap_from_u(int ne, int M, int m, const double* gd_e, const double* u, float* iap, cudaStream_t st);
-// FP32 copy of member m's FP64 array (m < 0: every member)
-void launch_shadow(int nc, int M, int m, const double* gd, float* gdf, cudaStream_t st);
+// FP32 copy of member m's FP64 array of n elements (m < 0: every member)
+void launch_to_f32(int n, int M, int m, const double* src, float* dst, cudaStream_t st);
 
 }  // namespace ens
 }  // namespace tmc
