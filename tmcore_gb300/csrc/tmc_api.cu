@@ -1148,6 +1148,7 @@ int tmc_create(const tmc_mesh_desc* mesh, const tmc_params* params, tmc_handle**
     M.fVertex_f = h->upload(f32(hm.fVertex));
     M.invAreaCell_f = h->upload(inv32(hm.areaCell));
     M.areaCell_f = h->upload(f32(hm.areaCell));
+    M.areaTriangle_f = h->upload(f32(hm.areaTriangle));
     M.invAreaCell = h->upload(invA);
   }
   M.cell2 = upload_stencil(h.get(), hm.cell2);

@@ -78,6 +78,7 @@ struct DevMesh {
   const float* fVertex_f;
   const float* invAreaCell_f;
   const float* areaCell_f;
+  const float* areaTriangle_f;
   const double* invAreaCell;
   // vector reconstruction (history): coefficients [3][me][nc], cos/sin lat, lon [4][nc]
   const double* recon;

@@ -589,6 +589,7 @@ __global__ void __launch_bounds__(kMaxBlock) k_vertex(DevMesh M, ModelOpt O, Sta
   } else {
     // one vertex at a time: measured faster than batching the loads of the
     // thread's vertices (which costs occupancy for a pass with three gathers)
+    float ph = 0.f, pl = 0.f, ah = 0.f, al = 0.f;
     TMC_FOR_EPT(v, M.nv) {
       int ci[3], ei[3];
       float kt[3], ts[3];
@@ -615,11 +616,17 @@ __global__ void __launch_bounds__(kMaxBlock) k_vertex(DevMesh M, ModelOpt O, Sta
       if (S.vor) S.vor[v] = vo;
       if (S.gd_v) S.gd_v[v] = gv;
       if (diag) {
-        const double At = M.areaTriangle[v];
-        pe += (double)(gv * (pv * pv)) * At;
-        av += ((double)vo + M.fVertex[v]) * At;
+        // potential enstrophy and absolute vorticity (tmcore_swm_mod.F90:233-255)
+        // from FP32 terms with compensated sums: FP64 terms made this launch
+        // FP64-pipe bound
+        const float At = M.areaTriangle_f[v];
+        two_sum_acc(ph, pl, gv * (pv * pv) * At);
+        two_sum_acc(ah, al, vo * At);
+        two_sum_acc(ah, al, M.fVertex_f[v] * At);
       }
     }
+    pe = (double)ph + (double)pl;
+    av = (double)ah + (double)al;
   }
   (void)O;
   if (diag) {
@@ -1209,7 +1216,8 @@ __device__ __forceinline__ void cell_fast_body(const DevMesh& M, const StageIO<f
   const Partials P = kB ? P0.at(blockIdx.y) : P0;
   constexpr int NQ = NTR > 0 ? NTR : 1;
   float rip = 0.f, r44 = 0.f;
-  double mass = 0.0, enc = 0.0;
+  double mass = 0.0;
+  float eh = 0.f, el = 0.f;
   const int mode = rk.mode;
   TMC_FOR_EPT(c, M.nc) {
     int ei[kME], ci[kME];
@@ -1235,11 +1243,12 @@ __device__ __forceinline__ void cell_fast_body(const DevMesh& M, const StageIO<f
       qo[j] = (mode <= 3) ? S.q_old[qi] : 0.f;
       qa[j] = (mode >= 2) ? S.q_acc[qi] : 0.f;
     }
-    double gdin = 0.0, ghsd = 0.0, Ad = 0.0;
+    double gdin = 0.0, Ad = 0.0;
+    float Afd = 0.f;
     if (diag) {
       gdin = S.gd_in[c];
-      ghsd = S.ghs[c];
       Ad = M.areaCell[c];
+      Afd = M.areaCell_f[c];
     }
     float uu[kME], Fv[kME], dv[kME], ae[kME], qn[NQ][kME];
 #pragma unroll
@@ -1317,8 +1326,12 @@ __device__ __forceinline__ void cell_fast_body(const DevMesh& M, const StageIO<f
       }
     }
     if (diag) {
+      // total mass from the FP64 gd; the cell part of the total energy
+      // (gd^2 + 2 gd ghs) areaCell (tmcore_swm_mod.F90:215-231) from FP32
+      // terms with a compensated sum (an FP64 term would cost four FP64
+      // operations per cell at 1/64 of the FP32 rate)
       mass = mass + gdin * Ad;
-      enc = enc + (gdin * gdin + 2.0 * gdin * ghsd) * Ad;
+      two_sum_acc(eh, el, gdf * (gdf + 2.f * ghf) * Afd);
     }
   }
   if (mode >= 2) {
@@ -1327,7 +1340,7 @@ __device__ __forceinline__ void cell_fast_body(const DevMesh& M, const StageIO<f
     block_store<float, 2>(v, P, r);
   }
   if (diag) {
-    const double v[2] = {mass, enc};
+    const double v[2] = {mass, (double)eh + (double)el};
     const int r[2] = {R_MASS, R_EN_C};
     block_store<double, 2>(v, P, r);
   }
