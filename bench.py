@@ -452,6 +452,41 @@ def run_closure_leg(args, local, ics, peak):
     return out
 
 
+def run_training_leg(args, local):
+    """Config 4's kernels: Adam steps of the closure network on batches of
+    65536 rows (synthetic features and a smooth target of the network's
+    input width), and the tensor-core forward on the same rows.  Host wall
+    clock around the calls, which synchronise; the forward includes its
+    host copies (24 + 1 floats per row)."""
+    import numpy as np
+
+    from tmcore_gb300.gpu import ClosureMLP
+
+    rows, batch, steps = 1 << 20, 65536, 50
+    rng = np.random.default_rng(0)
+    x = rng.standard_normal((rows, 24)).astype(np.float32)
+    y = (0.3 * np.tanh(x[:, 0] * x[:, 1]) + 0.1 * x[:, 2]).astype(np.float32)
+    net = ClosureMLP(device=local, seed=3)
+    net.set_scaling(np.zeros(24), np.ones(24), 1.0)
+    net.set_dataset(x, y)
+    net.train(5, batch=batch)
+    t = time.perf_counter()
+    losses = net.train(steps, batch=batch)
+    train_s = (time.perf_counter() - t) / steps
+    net.forward(x[:batch])
+    t = time.perf_counter()
+    net.forward(x)
+    fwd_s = time.perf_counter() - t
+    net.close()
+    flops_row = 2.0 * (24 * 64 + 2 * 64 * 64 + 64)
+    return {"workload": f"closure network 24-64-64-64-1, Adam (lr 1e-3) on batches of {batch} rows, "
+                        f"{rows} synthetic rows", "batch": batch, "steps": steps,
+            "ms_per_batch": train_s * 1e3, "train_rows_per_s": batch / train_s,
+            "train_tflops": 3 * flops_row * batch / train_s / 1e12,
+            "forward_rows_per_s_with_copies": rows / fwd_s, "loss_first_last": [float(losses[0]), float(losses[-1])],
+            "timing": "host wall clock around tmc_mlp_train / tmc_mlp_forward (both synchronise)"}
+
+
 def ncu_traffic(name: str):
     """dram bytes per launch from the committed ncu summary, if present."""
     p = os.path.join(ROOT, "profiles", name)
@@ -691,6 +726,7 @@ def main():
         extra["ensemble"] = run_ensemble(args, local, ens_ics, peak)
         if args.closure_members > 0:
             extra["closure"] = run_closure_leg(args, local, ens_ics[:args.closure_members], peak)
+            extra["training"] = run_training_leg(args, local)
         ens_ics = None
     if mixed_ics:
         extra["mixed_batch"] = run_mixed(args, local, mixed_ics, peak)
