@@ -608,10 +608,12 @@ __global__ void __launch_bounds__(kMaxBlock) k_vertex(DevMesh M, ModelOpt O, Sta
         dc[i] = M.dcEdge_f[ei[i]];
       }
       const float iA = M.invAreaTriangle_f[v];
+      const float At = diag ? M.areaTriangle_f[v] : 0.f;  // loaded before the stores below
+      const float fv = M.fVertex_f[v];
       const float gv = (g[0] * kt[0] + g[1] * kt[1] + g[2] * kt[2]) * iA;
       const float sv = ts[0] * uu[0] * dc[0] + ts[1] * uu[1] * dc[1] + ts[2] * uu[2] * dc[2];
       const float vo = -sv * iA;
-      const float pv = (M.fVertex_f[v] + vo) / gv;
+      const float pv = (fv + vo) / gv;
       S.pv_v[v] = pv;
       if (S.vor) S.vor[v] = vo;
       if (S.gd_v) S.gd_v[v] = gv;
@@ -619,10 +621,9 @@ __global__ void __launch_bounds__(kMaxBlock) k_vertex(DevMesh M, ModelOpt O, Sta
         // potential enstrophy and absolute vorticity (tmcore_swm_mod.F90:233-255)
         // from FP32 terms with compensated sums: FP64 terms made this launch
         // FP64-pipe bound
-        const float At = M.areaTriangle_f[v];
         two_sum_acc(ph, pl, gv * (pv * pv) * At);
         two_sum_acc(ah, al, vo * At);
-        two_sum_acc(ah, al, M.fVertex_f[v] * At);
+        two_sum_acc(ah, al, fv * At);
       }
     }
     pe = (double)ph + (double)pl;
@@ -1140,7 +1141,7 @@ __global__ void __launch_bounds__(kB ? kMemberBlock : kMaxBlock, kB ? TMC_FINAL_
   const int e0 = blockIdx.x * (kEPT * blockDim.x) + threadIdx.x;
   T* iap = const_cast<T*>(S.iap_old);
   int c1[kEPT], c2[kEPT];
-  T ia[kEPT], g1[kEPT], g2[kEPT];
+  T ia[kEPT], g1[kEPT], g2[kEPT], ae[kEPT];
 #pragma unroll
   for (int j = 0; j < kEPT; ++j) {
     const int e = e0 + j * blockDim.x;
@@ -1148,6 +1149,7 @@ __global__ void __launch_bounds__(kB ? kMemberBlock : kMaxBlock, kB ? TMC_FINAL_
     c1[j] = in ? M.cellsOnEdge[e] : 0;
     c2[j] = in ? M.cellsOnEdge[M.ne + e] : 0;
     ia[j] = in ? iap[e] + T(bdt) * S.iap_acc[e] : T(0);
+    ae[j] = in ? met<T>(M.areaEdge, M.areaEdge_f, e) : T(0);  // for the energy, loaded before any store
   }
 #pragma unroll
   for (int j = 0; j < kEPT; ++j) {
@@ -1166,10 +1168,11 @@ __global__ void __launch_bounds__(kB ? kMemberBlock : kMaxBlock, kB ? TMC_FINAL_
     if (e >= M.ne) continue;
     iap[e] = ia[j];
     prep_edge<T>(M, O, e, c1[j], c2[j], ia[j], g1[j], g2[j], C, S.gd_e, S.u, S.F, S.Fq);
+    // energy_term (tmcore_swm_mod.F90:229) with areaEdge already loaded
     if constexpr (kF64<T>)
-      en = en + energy_term<T>(M, e, ia[j]);
+      en = en + ia[j] * ia[j] * ae[j];
     else
-      enT += energy_term<T>(M, e, ia[j]);
+      enT += ia[j] * ia[j] * ae[j];
   }
   if constexpr (!kF64<T>) en = (double)enT;
   const double v[1] = {en};
