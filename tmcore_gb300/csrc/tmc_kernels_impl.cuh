@@ -589,27 +589,30 @@ __global__ void __launch_bounds__(kMaxBlock) k_vertex(DevMesh M, ModelOpt O, Sta
   } else {
     // one vertex at a time: measured faster than batching the loads of the
     // thread's vertices (which costs occupancy for a pass with three gathers)
+    // Every load is a read-only (non-coherent) load: nothing this kernel
+    // stores aliases them, which lets the compiler issue a vertex's loads
+    // ahead of the previous vertex's stores.
     float ph = 0.f, pl = 0.f, ah = 0.f, al = 0.f;
     TMC_FOR_EPT(v, M.nv) {
       int ci[3], ei[3];
       float kt[3], ts[3];
 #pragma unroll
       for (int i = 0; i < 3; ++i) {
-        ci[i] = M.cellsOnVertex[(size_t)i * M.nv + v];
-        ei[i] = M.edgesOnVertex[(size_t)i * M.nv + v];
-        kt[i] = M.kite_f[(size_t)i * M.nv + v];
-        ts[i] = (float)M.tSign[(size_t)i * M.nv + v];
+        ci[i] = __ldg(M.cellsOnVertex + (size_t)i * M.nv + v);
+        ei[i] = __ldg(M.edgesOnVertex + (size_t)i * M.nv + v);
+        kt[i] = __ldg(M.kite_f + (size_t)i * M.nv + v);
+        ts[i] = (float)__ldg(M.tSign + (size_t)i * M.nv + v);
       }
       float g[3], uu[3], dc[3];
 #pragma unroll
       for (int i = 0; i < 3; ++i) {
-        g[i] = S.gdf_in[ci[i]];
-        uu[i] = S.u[ei[i]];
-        dc[i] = M.dcEdge_f[ei[i]];
+        g[i] = __ldg(S.gdf_in + ci[i]);
+        uu[i] = __ldg(S.u + ei[i]);
+        dc[i] = __ldg(M.dcEdge_f + ei[i]);
       }
-      const float iA = M.invAreaTriangle_f[v];
-      const float At = diag ? M.areaTriangle_f[v] : 0.f;  // loaded before the stores below
-      const float fv = M.fVertex_f[v];
+      const float iA = __ldg(M.invAreaTriangle_f + v);
+      const float At = diag ? __ldg(M.areaTriangle_f + v) : 0.f;
+      const float fv = __ldg(M.fVertex_f + v);
       const float gv = (g[0] * kt[0] + g[1] * kt[1] + g[2] * kt[2]) * iA;
       const float sv = ts[0] * uu[0] * dc[0] + ts[1] * uu[1] * dc[1] + ts[2] * uu[2] * dc[2];
       const float vo = -sv * iA;
