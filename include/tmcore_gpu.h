@@ -25,7 +25,7 @@ extern "C" {
 #define TMC_OK 0
 #define TMC_E_ARG (-1)      /* bad argument or configuration */
 #define TMC_E_CUDA (-2)     /* CUDA runtime error (message in tmc_last_error) */
-#define TMC_E_HEALTH (-3)   /* non-finite or non-positive depth detected */
+#define TMC_E_HEALTH (-3)   /* non-finite state detected (tmc_get_diag), or a tensor-core wait ran out */
 #define TMC_E_UNSUP (-4)    /* option combination not implemented on the device */
 #define TMC_E_STATE (-5)    /* call out of order (e.g. step before set_state) */
 
@@ -117,9 +117,12 @@ int tmc_get_tracers(tmc_handle* h, double* qgd);
 int tmc_step(tmc_handle* h, int32_t nsteps);
 /* {total_mass, total_energy, total_potential_enstrophy,
  *  total_absolute_vorticity, beta} of state(old) (tmcore_swm_mod.F90:215-255,
- *  diag_mod.F90:76-91); synchronises. */
+ *  diag_mod.F90:76-91); synchronises.  Returns TMC_E_HEALTH (outputs filled)
+ *  when an invariant is not finite: the state has left the physical range. */
 int tmc_get_diag(tmc_handle* h, double out[5]);
-/* the same for every ensemble member: out[members][5] */
+/* the same for every ensemble member: out[members][5]; returns TMC_OK with
+ * non-finite rows for members that blew up, so that a host can switch them
+ * off or roll them back while the others continue */
 int tmc_get_diag_all(tmc_handle* h, double* out);
 int tmc_synchronize(tmc_handle* h);
 

@@ -287,3 +287,26 @@ def test_steps_match_oracle_upwind_orders(mesh4, cfg):
     if ntr:
         assert rel_max(g.get_tracers(), o.tracers()) < 1e-12
     g.close()
+
+
+def test_health_error_on_blown_up_state(mesh4):
+    """A state outside the physical range (a negative depth) turns the step's
+    fields non-finite; tmc_get_diag reports it as TMC_E_HEALTH and the handle
+    stays usable: a valid state set afterwards steps normally."""
+    from tmcore_gb300 import abi
+    from tmcore_gb300.gpu import TMCError, TMCoreGPU
+
+    for prec in (0, 1):
+        g = TMCoreGPU(mesh4, dt=600.0, pv_scheme=1, apvm_weight=0.0, precision=prec)
+        gd, u, ghs = _ic(mesh4, seed=3)
+        bad = gd.copy()
+        bad[::7] = -bad[::7]
+        g.set_initial(bad, u, ghs)
+        g.step(2)
+        with pytest.raises(TMCError) as e:
+            g.diag()
+        assert e.value.code == abi.TMC_E_HEALTH
+        g.set_initial(gd, u, ghs)
+        g.step(2)
+        assert np.all(np.isfinite(g.diag()))
+        g.close()

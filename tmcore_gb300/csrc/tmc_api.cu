@@ -1395,7 +1395,13 @@ int tmc_get_diag(tmc_handle* h, double out[5]) {
   if (rc) return rc;
   for (int i = 0; i < 4; ++i) out[i] = h->h_diag[i];
   out[4] = h->step_count > 0 ? h->h_diag[4] : 1.0;
-  return h->cuda_check("tmc_get_diag");
+  if ((rc = h->cuda_check("tmc_get_diag"))) return rc;
+  // device health: a non-finite invariant means the state has left the
+  // physical range (a negative depth makes sqrt(gd_edge) and everything
+  // after it NaN); the outputs are filled all the same
+  for (int i = 0; i < 5; ++i)
+    if (!std::isfinite(out[i])) return h->fail(TMC_E_HEALTH, "tmc_get_diag: non-finite invariants (the state blew up)");
+  return TMC_OK;
 }
 
 int tmc_get_diag_all(tmc_handle* h, double* out) {
