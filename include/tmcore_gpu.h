@@ -10,7 +10,14 @@
  *
  * Element order at this ABI is always the caller's (the mesh file's) order;
  * the space-filling-curve renumbering used on the device is internal.
- * Unless stated otherwise, array arguments are HOST pointers.
+ * The state and field arrays of the handle calls (tmc_set_initial,
+ * tmc_set_state, tmc_get_state, tmc_get_vertex, tmc_set_tracers,
+ * tmc_get_tracers, tmc_time_integrate, tmc_spatial_operators, tmc_op_*,
+ * tmc_history_fields, tmc_reconstruct, tmc_adv_*) may be HOST or DEVICE
+ * pointers: the copies take their direction from unified addressing.  The
+ * mesh (tmc_create), diagnostics (tmc_get_diag*), network parameters and
+ * datasets (tmc_mlp_*), closure features and coarse-graining arrays are
+ * host arrays unless stated otherwise.
  */
 #ifndef TMCORE_GPU_H
 #define TMCORE_GPU_H

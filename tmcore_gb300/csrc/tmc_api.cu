@@ -970,12 +970,14 @@ int sync(tmc_handle* h, const char* where) {
 }
 
 int h2d(tmc_handle* h, double* dst, const double* src, size_t n) {
-  if (cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyHostToDevice, h->st) != cudaSuccess)
+  // cudaMemcpyDefault: the caller's array may be host or device memory
+  // (unified addressing tells the direction)
+  if (cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDefault, h->st) != cudaSuccess)
     return h->cuda_check("H2D");
   return TMC_OK;
 }
 int d2h(tmc_handle* h, double* dst, const double* src, size_t n) {
-  if (cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToHost, h->st) != cudaSuccess)
+  if (cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDefault, h->st) != cudaSuccess)
     return h->cuda_check("D2H");
   return TMC_OK;
 }
@@ -1453,7 +1455,7 @@ int tmc_time_integrate(tmc_handle* h, const double* gd_old, const double* iap_u_
              {qgd_old, qgd_new, h->raw_q, nq, -1}};
   const int nio = trc ? 3 : 2;
   for (int i = 0; i < nio; ++i) {
-    if (cudaMemcpyAsync(io[i].raw, io[i].in, io[i].n * sizeof(double), cudaMemcpyHostToDevice, cs) != cudaSuccess)
+    if (cudaMemcpyAsync(io[i].raw, io[i].in, io[i].n * sizeof(double), cudaMemcpyDefault, cs) != cudaSuccess)
       return h->cuda_check("H2D");
     cudaEventRecord(h->cev[1 + i], cs);
   }
@@ -1473,7 +1475,7 @@ int tmc_time_integrate(tmc_handle* h, const double* gd_old, const double* iap_u_
       h->eng->get_tracers_dev(io[i].raw);
     cudaEventRecord(h->cev[4 + i], h->st);
     cudaStreamWaitEvent(cs, h->cev[4 + i], 0);
-    if (cudaMemcpyAsync(io[i].out, io[i].raw, io[i].n * sizeof(double), cudaMemcpyDeviceToHost, cs) != cudaSuccess)
+    if (cudaMemcpyAsync(io[i].out, io[i].raw, io[i].n * sizeof(double), cudaMemcpyDefault, cs) != cudaSuccess)
       return h->cuda_check("D2H");
   }
   if (cudaStreamSynchronize(cs) != cudaSuccess) return h->cuda_check("tmc_time_integrate");
