@@ -353,3 +353,32 @@ def test_device_pointers_match_host_arrays(mesh4):
                                     h_gd.ctypes.data_as(f64p), h_iap.ctypes.data_as(f64p), None) == 0
     assert np.array_equal(n_gd.cpu().numpy(), h_gd) and np.array_equal(n_iap.cpu().numpy(), h_iap)
     g.close()
+
+
+def test_handles_on_concurrent_host_threads(mesh4):
+    """One handle per host thread: two threads create, step and read their own
+    handles at the same time (ctypes releases the GIL during the calls); each
+    result equals the same run made alone."""
+    import threading
+
+    from tmcore_gb300.gpu import TMCoreGPU
+
+    def run(seed, prec, out, key):
+        g = TMCoreGPU(mesh4, dt=600.0, pv_scheme=1, apvm_weight=0.0, precision=prec)
+        g.set_initial(*_ic(mesh4, seed=seed))
+        for _ in range(5):
+            g.step(4)
+            g.diag()
+        out[key] = g.get_state()
+        g.close()
+
+    jobs = [(21, 0), (22, 1), (23, 1)]
+    together, alone = {}, {}
+    threads = [threading.Thread(target=run, args=(s, p, together, k)) for k, (s, p) in enumerate(jobs)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    for k, (s, p) in enumerate(jobs):
+        run(s, p, alone, k)
+        assert all(np.array_equal(a, b) for a, b in zip(together[k], alone[k])), k
