@@ -89,7 +89,7 @@ typedef struct tmc_params {
   int32_t members;                /* ensemble members sharing the mesh (FP32 shallow water, CRK4); 0 or 1: one */
   int32_t member_layout;          /* ensembles: 0 member-outermost arrays (every option), 1 member-innermost
                                      (members a multiple of 16; pv_scheme 1 with apvm_weight 0, adv_order 2,
-                                     no tracers; tmc_closure_features needs 0): whole-line neighbour gathers */
+                                     no tracers): whole-line neighbour gathers */
   int32_t reserved[3];
 } tmc_params;
 

@@ -163,13 +163,23 @@ def test_member_layout_refusals(mesh3):
     with pytest.raises(TMCError) as e:
         TMCoreGPU(mesh3, dt=600.0, members=32, member_layout=1, precision=1, pv_scheme=3, interp_pv_order=3)
     assert e.value.code == abi.TMC_E_UNSUP
-    ens = TMCoreGPU(mesh3, dt=600.0, members=32, member_layout=1, **KW)
-    from tmcore_gb300 import cases
-    ens.set_initial(*cases.jet_bumps(mesh3, seed=1))
-    with pytest.raises(TMCError) as e:  # training features come from member_layout 0 models
-        ens.closure_features()
-    assert e.value.code == abi.TMC_E_UNSUP
-    ens.close()
+
+
+def test_closure_features_match_member_outermost(mesh4):
+    """tmc_closure_features of a member of a member-innermost ensemble equals
+    the member-outermost export of the same state (to FP32 rounding)."""
+    ics = _ics(mesh4, M, 900)
+    inner, outer = _ensemble(mesh4, ics, 1, dt=600.0), _ensemble(mesh4, ics, 0, dt=600.0)
+    for m in (0, 17):
+        inner.select_member(m)
+        outer.select_member(m)
+        fi, pi = inner.closure_features()
+        fo, po = outer.closure_features()
+        for k in range(fi.shape[1]):
+            assert rel_max(fi[:, k], fo[:, k]) < 1e-5, (m, k, rel_max(fi[:, k], fo[:, k]))
+        assert rel_max(pi, po) < 1e-5
+    inner.close()
+    outer.close()
 
 
 @pytest.mark.parametrize("every_stage", [True, False])

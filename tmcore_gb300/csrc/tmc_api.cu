@@ -879,8 +879,16 @@ struct EnsEngine : EngineBase {
     *gh = ghs;
   }
   void refresh_all_shadows() override {}
-  void closure_features(float*, float*) override {}  // tmc_closure_features refuses member_layout 1 (training
-                                                     // features come from member_layout 0 models)
+  // the closure's features of state(old) of the selected member: its edge
+  // preparation, E (a cell pass without update), pv on vertices, edges and cells
+  void closure_features(float* feat, float* pv) override {
+    launch_diag_pass(false);
+    const ens::IO s = io(0);
+    ens::launch_cell(h->M, D, s, RKStage{0, 0.0}, EP, false, h->bsp[P_CELL], h->st);
+    ens::launch_edge_pv(h->M, D, s, h->bsp[P_PV], h->st);
+    ens::launch_v2c(h->M, D, s, pv_c, h->st);
+    ens::launch_closure_features(h->M, D, s, pv_c, h->cur, feat, pv, h->st);
+  }
 
   // history fields of the selected member: its u, gd and ghs copied out of
   // the member-innermost arrays, then the single-model kernels
@@ -1691,8 +1699,8 @@ int tmc_closure_status(tmc_handle* h, int32_t* timed_out) {
 int tmc_closure_features(tmc_handle* h, float* features, double* pv_edge) {
   TMC_REQUIRE_SWM(h);
   if (!features) return h->fail(TMC_E_ARG, "NULL array");
-  if (h->p.precision != TMC_FP32 || h->generic || h->p.member_layout == 1)
-    return h->fail(TMC_E_UNSUP, "closure features come from the FP32 CRK4 shallow-water step (member_layout 0)");
+  if (h->p.precision != TMC_FP32 || h->generic)
+    return h->fail(TMC_E_UNSUP, "closure features come from the FP32 CRK4 shallow-water step");
   if (!h->have_state) return h->fail(TMC_E_STATE, "no state set");
   const int ne = h->M.ne;
   float *d_feat = nullptr, *d_pv = nullptr;

@@ -296,7 +296,7 @@ __global__ void TMC_ENS_LB(TMC_ENS_CELL_MINB) k_ens_cell(DevMesh Mh, Dims D, IO 
     const size_t cm = (size_t)(c0 + j) * Mm + L.m0;
     FF gold[V], gacc[V];
     float tprev[V], gdf[V], ghf[V], gdl[V];
-    if (mode <= 3) ldff<V>(S.gd_old, cm, ffs, gold);
+    if (mode >= 1 && mode <= 3) ldff<V>(S.gd_old, cm, ffs, gold);
     if (mode >= 2) {
       ldff<V>(S.gd_acc, cm, ffs, gacc);
       ldv<V>(S.tendf, cm, tprev);
@@ -330,6 +330,9 @@ __global__ void TMC_ENS_LB(TMC_ENS_CELL_MINB) k_ens_cell(DevMesh Mh, Dims D, IO 
       const float Af = s_Af[j];
       gnext[c] = FF{0.f, 0.f};
       switch (mode) {
+        case 0:  // E only (the closure's features of a state)
+          acc_o[c] = t;
+          break;
         case 1:
           acc_o[c] = t;
           gnext[c] = ff_add(gold[c], ff_mul(adt, t));
@@ -356,9 +359,11 @@ __global__ void TMC_ENS_LB(TMC_ENS_CELL_MINB) k_ens_cell(DevMesh Mh, Dims D, IO 
       }
     }
     stv<V>(S.E, cm, Eo);
-    stff<V>(S.gd_acc, cm, ffs, acc_o);
-    stv<V>(S.tendf, cm, tT);
-    if (mode <= 3) stff<V>(S.gd_next, cm, ffs, gnext);
+    if (mode >= 1) {
+      stff<V>(S.gd_acc, cm, ffs, acc_o);
+      stv<V>(S.tendf, cm, tT);
+    }
+    if (mode >= 1 && mode <= 3) stff<V>(S.gd_next, cm, ffs, gnext);
   }
   const int slot = blockIdx.x;
   if (mode >= 2) {

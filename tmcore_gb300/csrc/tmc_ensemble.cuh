@@ -95,7 +95,8 @@ struct IO {
   size_t ffs;            // offset of the l halves (nCells * M)
 };
 
-// passes of the fused CRK4 step (bs: threads per block, a multiple of 32)
+// passes of the fused CRK4 step (bs: threads per block, a multiple of 32);
+// launch_cell with rk.mode 0 computes E only (no RK update)
 void launch_cell(const DevMesh& Mh, const Dims& D, const IO& S, RKStage rk, const Partials& P, bool diag, int bs,
                  cudaStream_t st);
 void launch_vertex(const DevMesh& Mh, const Dims& D, const IO& S, const Partials& P, bool diag, int bs,
@@ -124,6 +125,9 @@ void launch_v2c(const DevMesh& Mh, const Dims& D, const IO& S, float* pv_c, cuda
 void launch_closure_hold(const DevMesh& Mh, const Dims& D, const IO& S, const float* dq, cudaStream_t st);
 void launch_closure(const DevMesh& Mh, const Dims& D, const IO& S, const float* pv_c, const ClosureArgs& a,
                     cudaStream_t st);
+// the closure's features and pv_edge of member m (internal edge order) into feat[ne][24], pv[ne]
+void launch_closure_features(const DevMesh& Mh, const Dims& D, const IO& S, const float* pv_c, int m, float* feat,
+                             float* pv, cudaStream_t st);
 
 // state transfer of member m (caller's element order <-> member-innermost);
 // _ff: an FF array (h, then l at offset n * M)

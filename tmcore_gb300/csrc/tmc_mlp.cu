@@ -184,6 +184,15 @@ __global__ void __launch_bounds__(kTcThreads, kTcMinBlocks) k_closure_inner(Net 
   if (!forward_tiles(net, src, ntiles, smem) && threadIdx.x % kTile == 0) atomicExch(err, 1);
 }
 
+__global__ void k_closure_features_inner(EnsClosureSrc src, int m, float* feat, float* pv) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= src.M.ne) return;
+  float x[kIn];
+  src.features((long long)e * src.mem + m, x);
+  for (int k = 0; k < kIn; ++k) feat[(size_t)e * kIn + k] = x[k];
+  pv[e] = x[3];
+}
+
 // the held correction of stage 1 added to pv_edge in the later stages
 __global__ void k_closure_hold(float* pv_e, const float* dq, int ne, long long mse) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
@@ -456,6 +465,11 @@ void launch_closure(const DevMesh& Mh, const Dims& D, const IO& S, const float* 
     attr = true;
   }
   k_closure_inner<<<grid, kTcThreads, kSmemTc, st>>>(*static_cast<const Net*>(a.net), src, ntiles, a.err);
+}
+void launch_closure_features(const DevMesh& Mh, const Dims& D, const IO& S, const float* pv_c, int m, float* feat,
+                             float* pv, cudaStream_t st) {
+  const EnsClosureSrc src{Mh, S, pv_c, nullptr, nullptr, D.M, (long long)Mh.ne * D.M};
+  k_closure_features_inner<<<(Mh.ne + 255) / 256, 256, 0, st>>>(src, m, feat, pv);
 }
 }  // namespace ens
 void launch_closure_features(const DevMesh& M, const StageIO<float>& S, int member, float* feat, float* pv,
