@@ -455,9 +455,10 @@ def run_closure_leg(args, local, ics, peak):
 def run_training_leg(args, local):
     """Config 4's kernels: Adam steps of the closure network on batches of
     65536 rows (synthetic features and a smooth target of the network's
-    input width), and the tensor-core forward on the same rows.  Host wall
-    clock around the calls, which synchronise; the forward includes its
-    host copies (24 + 1 floats per row)."""
+    input width), with the forward and backward on the tensor cores (the
+    headline) and on the CUDA cores in FP32, and the tensor-core forward on
+    the same rows.  Host wall clock around the calls, which synchronise; the
+    forward includes its host copies (24 + 1 floats per row)."""
     import numpy as np
 
     from tmcore_gb300.gpu import ClosureMLP
@@ -466,24 +467,32 @@ def run_training_leg(args, local):
     rng = np.random.default_rng(0)
     x = rng.standard_normal((rows, 24)).astype(np.float32)
     y = (0.3 * np.tanh(x[:, 0] * x[:, 1]) + 0.1 * x[:, 2]).astype(np.float32)
-    net = ClosureMLP(device=local, seed=3)
-    net.set_scaling(np.zeros(24), np.ones(24), 1.0)
-    net.set_dataset(x, y)
-    net.train(5, batch=batch)
-    t = time.perf_counter()
-    losses = net.train(steps, batch=batch)
-    train_s = (time.perf_counter() - t) / steps
-    net.forward(x[:batch])
-    t = time.perf_counter()
-    net.forward(x)
-    fwd_s = time.perf_counter() - t
-    net.close()
+    res = {}
+    for tc in (True, False):
+        net = ClosureMLP(device=local, seed=3)
+        net.set_train_mode(tc)
+        net.set_scaling(np.zeros(24), np.ones(24), 1.0)
+        net.set_dataset(x, y)
+        net.train(5, batch=batch)
+        t = time.perf_counter()
+        losses = net.train(steps, batch=batch)
+        res[tc] = ((time.perf_counter() - t) / steps, losses)
+        if tc:
+            net.forward(x[:batch])
+            t = time.perf_counter()
+            net.forward(x)
+            fwd_s = time.perf_counter() - t
+        net.close()
+    train_s, losses = res[True]
     flops_row = 2.0 * (24 * 64 + 2 * 64 * 64 + 64)
     return {"workload": f"closure network 24-64-64-64-1, Adam (lr 1e-3) on batches of {batch} rows, "
                         f"{rows} synthetic rows", "batch": batch, "steps": steps,
+            "trainer": "tensor cores (tcgen05 forward and backward, BF16 operands, FP32 accumulation)",
             "ms_per_batch": train_s * 1e3, "train_rows_per_s": batch / train_s,
             "train_tflops": 3 * flops_row * batch / train_s / 1e12,
+            "cuda_cores_fp32_ms_per_batch": res[False][0] * 1e3,
             "forward_rows_per_s_with_copies": rows / fwd_s, "loss_first_last": [float(losses[0]), float(losses[-1])],
+            "cuda_cores_loss_first_last": [float(res[False][1][0]), float(res[False][1][-1])],
             "timing": "host wall clock around tmc_mlp_train / tmc_mlp_forward (both synchronise)"}
 
 

@@ -202,6 +202,13 @@ int tmc_mlp_train(tmc_mlp* n, int32_t batch, int32_t steps, float lr, float* los
 /* gradient of the mean squared error over rows (a multiple of 128) w.r.t.
  * the parameters, without updating them */
 int tmc_mlp_gradient(tmc_mlp* n, const float* x, const float* y, int64_t rows, float* grad, double* loss);
+/* Where tmc_mlp_train and tmc_mlp_gradient run: 1 (the default) the tensor
+ * cores, forward and backward as tcgen05 MMAs of BF16 operands (weights,
+ * activations and their gradients) with FP32 accumulation, the gradient
+ * summed over blocks in a fixed order; 0 the CUDA cores, forward and
+ * backward in FP32 from the BF16 weights.  TMC_E_HEALTH: a completion wait of
+ * the tensor-core trainer timed out. */
+int tmc_mlp_set_train_mode(tmc_mlp* n, int32_t tensor_cores);
 
 /* The learned closure in the FP32 CRK4 step: after the pv-on-edge pass of
  * every stage, the network's output for each edge (features: the stage's

@@ -97,6 +97,7 @@ SYMBOLS = {
     "tmc_mlp_set_dataset": (ctypes.c_int, [vp, vp, vp, ctypes.c_int64]),
     "tmc_mlp_train": (ctypes.c_int, [vp, i32, i32, ctypes.c_float, vp]),
     "tmc_mlp_gradient": (ctypes.c_int, [vp, vp, vp, ctypes.c_int64, vp, dp]),
+    "tmc_mlp_set_train_mode": (ctypes.c_int, [vp, i32]),
     "tmc_set_closure": (ctypes.c_int, [vp, vp]),
     "tmc_set_closure_stages": (ctypes.c_int, [vp, i32]),
     "tmc_set_member_closure": (ctypes.c_int, [vp, i32, i32]),

@@ -70,8 +70,9 @@ def training_data(fine_level=8, coarse_level=6, runs=4, days=1.0, samples_per_ru
     return np.concatenate(X), np.concatenate(Y)
 
 
-def train(X, Y, steps=2000, batch=65536, lr=1e-3, seed=0, device=0):
-    """A ClosureMLP fitted to (X, Y); returns (net, losses, scaling)."""
+def train(X, Y, steps=2000, batch=65536, lr=1e-3, seed=0, device=0, tensor_cores=True):
+    """A ClosureMLP fitted to (X, Y), its gradients on the tensor cores (or
+    the CUDA cores); returns (net, losses, scaling)."""
     rng = np.random.default_rng(seed)
     perm = rng.permutation(len(Y))
     X, Y = X[perm], Y[perm]
@@ -80,6 +81,7 @@ def train(X, Y, steps=2000, batch=65536, lr=1e-3, seed=0, device=0):
     xs[xs == 0] = 1.0
     ys = float(np.std(Y)) or 1.0
     net = ClosureMLP(device=device, seed=seed)
+    net.set_train_mode(tensor_cores)
     net.set_scaling(xm, 1.0 / xs, ys)
     net.set_dataset(X, Y)
     b = min(batch, (len(Y) // 128) * 128)

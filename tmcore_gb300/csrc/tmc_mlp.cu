@@ -1,6 +1,6 @@
 // The learned PV-on-edge closure network: tensor-core forward (tcgen05),
-// CUDA-core training (forward with stored pre-activations, backward, Adam),
-// and its C ABI (include/tmcore_gpu.h, tmc_mlp_*).
+// training (forward and backward) on the tensor cores or on the CUDA cores
+// in FP32, Adam, and its C ABI (include/tmcore_gpu.h, tmc_mlp_*).
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -12,6 +12,7 @@
 #include "tmc_ensemble.cuh"
 #include "tmc_kernels.cuh"
 #include "tmc_mlp_tc.cuh"
+#include "tmc_mlp_train_tc.cuh"
 #include "tmcore_gpu.h"
 
 using namespace tmc::mlp;
@@ -428,6 +429,45 @@ __global__ void k_to_bf16(const float* p, __nv_bfloat16* pb, int n) {
   if (i < n) pb[i] = __float2bfloat16_rn(p[i]);
 }
 
+// ---------------------------------------------------------------------------
+// training on the tensor cores (tmc_mlp_train_tc.cuh): rows of the batch
+// from the dataset, wrapping at its end
+// ---------------------------------------------------------------------------
+struct TrainSrc {
+  const float* X;
+  const float* Y;
+  long long rows, offset;
+  float yscale;
+  __device__ bool sample(long long i, float (&x)[kIn], float& t) const {
+    const long long j = (offset + i) % rows;
+#pragma unroll
+    for (int k = 0; k < kIn; ++k) x[k] = X[j * kIn + k];
+    t = Y[j] / yscale;
+    return true;
+  }
+};
+
+__global__ void __launch_bounds__(kTrTile, 1) k_mlp_train_tc(Net net, TrainSrc src, long long ntiles, float inv_batch,
+                                                             float* part, double* ploss, int* err) {
+  extern __shared__ __align__(128) uint8_t smem[];
+  if (!train_tiles(net, src, ntiles, inv_batch, part, ploss, smem) && threadIdx.x == 0) atomicExch(err, 1);
+}
+
+// grad += the blocks' partial gradients, summed in block order; loss += their losses
+__global__ void k_grad_reduce(const float* part, const double* ploss, int nblk, float* grad, double* loss) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < kParams) {
+    float s = 0.f;
+    for (int b = 0; b < nblk; ++b) s += part[(size_t)b * kParams + i];
+    grad[i] += s;
+  }
+  if (i == 0) {
+    double l = 0.0;
+    for (int b = 0; b < nblk; ++b) l += ploss[b];
+    *loss += l;
+  }
+}
+
 }  // namespace
 
 namespace tmc {
@@ -494,6 +534,9 @@ struct tmc_mlp {
   long long io_cap = 0;
   int* d_err = nullptr;
   double* d_loss = nullptr;
+  int train_tc = 1;          // tmc_mlp_train / tmc_mlp_gradient on the tensor cores (0: CUDA cores)
+  float* part = nullptr;     // [sms][kParams] per-block partial gradients (tensor-core trainer)
+  double* ploss = nullptr;   // [sms]
   int sms = 148;
   std::string err;
   int fail(int code, const std::string& s) {
@@ -534,6 +577,8 @@ int tmc_mlp_create(int32_t device, uint64_t seed, tmc_mlp** out) {
   okc = okc && cudaMalloc(&n->xinv, sizeof(float) * kIn) == cudaSuccess;
   okc = okc && cudaMalloc(&n->d_err, sizeof(int)) == cudaSuccess;
   okc = okc && cudaMalloc(&n->d_loss, sizeof(double)) == cudaSuccess;
+  okc = okc && cudaMalloc(&n->part, sizeof(float) * kParams * n->sms) == cudaSuccess;
+  okc = okc && cudaMalloc(&n->ploss, sizeof(double) * n->sms) == cudaSuccess;
   *out = n;
   if (!okc) return n->check("tmc_mlp_create");
   // PyTorch-style Linear initialisation: U(-1/sqrt(fan_in), 1/sqrt(fan_in))
@@ -563,13 +608,15 @@ int tmc_mlp_create(int32_t device, uint64_t seed, tmc_mlp** out) {
   cudaFuncSetAttribute(k_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TrainSmem));
   cudaFuncSetAttribute(k_mlp_fwd_simt, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SimtW));
   cudaFuncSetAttribute(k_mlp_fwd_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemTc);
+  cudaFuncSetAttribute(k_mlp_train_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemTrain);
   return n->check("tmc_mlp_create");
 }
 
 int tmc_mlp_destroy(tmc_mlp* n) {
   if (!n) return TMC_OK;
   if (n->st) cudaStreamSynchronize(n->st);
-  void* ptrs[] = {n->p, n->pb, n->g, n->m, n->v, n->xmean, n->xinv, n->dx, n->dy, n->io_x, n->io_y, n->d_err, n->d_loss};
+  void* ptrs[] = {n->p, n->pb, n->g, n->m, n->v, n->xmean, n->xinv, n->dx, n->dy, n->io_x, n->io_y, n->d_err, n->d_loss,
+                   n->part,  n->ploss};
   for (void* q : ptrs) cudaFree(q);
   if (n->st) cudaStreamDestroy(n->st);
   delete n;
@@ -659,13 +706,45 @@ int tmc_mlp_set_dataset(tmc_mlp* n, const float* x, const float* y, int64_t rows
   return n->check("tmc_mlp_set_dataset");
 }
 
+// one gradient pass over `batch` rows of X/Y from row `offset` (wrapping at
+// `rows`), added into n->g and its loss into n->d_loss
+static void launch_gradient(tmc_mlp* n, const float* X, const float* Y, long long rows, long long offset, long long batch) {
+  const float inv_batch = 1.f / (float)batch;
+  if (n->train_tc) {
+    const long long ntiles = batch / kTile;
+    const int grid = (int)std::min<long long>(ntiles, (long long)n->sms);
+    k_mlp_train_tc<<<grid, kTrTile, kSmemTrain, n->st>>>(n->net(), TrainSrc{X, Y, rows, offset, n->yscale}, ntiles,
+                                                          inv_batch, n->part, n->ploss, n->d_err);
+    k_grad_reduce<<<(kParams + 255) / 256, 256, 0, n->st>>>(n->part, n->ploss, grid, n->g, n->d_loss);
+  } else {
+    k_mlp_train<<<(unsigned)(batch / kTile), kTile, sizeof(TrainSmem), n->st>>>(n->net(), X, Y, rows, offset,
+                                                                                inv_batch, n->g, n->d_loss);
+  }
+}
+
+// the completion-wait flag of the tensor-core trainer, read and cleared
+static int train_status(tmc_mlp* n, const char* where) {
+  int herr = 0;
+  cudaMemcpyAsync(&herr, n->d_err, sizeof(int), cudaMemcpyDeviceToHost, n->st);
+  cudaMemsetAsync(n->d_err, 0, sizeof(int), n->st);
+  if (cudaStreamSynchronize(n->st) != cudaSuccess) return n->check(where);
+  if (herr) return n->fail(TMC_E_HEALTH, std::string(where) + ": a tensor-core completion wait timed out");
+  return n->check(where);
+}
+
+int tmc_mlp_set_train_mode(tmc_mlp* n, int32_t tensor_cores) {
+  if (!n || (tensor_cores != 0 && tensor_cores != 1)) return n ? n->fail(TMC_E_ARG, "tensor_cores must be 0 or 1") : TMC_E_ARG;
+  n->train_tc = tensor_cores;
+  return TMC_OK;
+}
+
 int tmc_mlp_train(tmc_mlp* n, int32_t batch, int32_t steps, float lr, float* losses) {
   if (!n || batch <= 0 || batch % kTile != 0 || steps < 0) return n ? n->fail(TMC_E_ARG, "batch must be a positive multiple of 128") : TMC_E_ARG;
   if (!n->dx) return n->fail(TMC_E_STATE, "tmc_mlp_train: no dataset");
+  cudaMemsetAsync(n->d_err, 0, sizeof(int), n->st);
   for (int s = 0; s < steps; ++s) {
     cudaMemsetAsync(n->d_loss, 0, sizeof(double), n->st);
-    k_mlp_train<<<batch / kTile, kTile, sizeof(TrainSmem), n->st>>>(n->net(), n->dx, n->dy, n->rows, n->cursor,
-                                                                    1.f / batch, n->g, n->d_loss);
+    launch_gradient(n, n->dx, n->dy, n->rows, n->cursor, batch);
     n->cursor = (n->cursor + batch) % n->rows;
     n->adam_t += 1;
     const float b1c = 1.f - std::pow(0.9f, (float)n->adam_t), b2c = 1.f - std::pow(0.999f, (float)n->adam_t);
@@ -677,8 +756,7 @@ int tmc_mlp_train(tmc_mlp* n, int32_t batch, int32_t steps, float lr, float* los
       losses[s] = (float)l;
     }
   }
-  if (cudaStreamSynchronize(n->st) != cudaSuccess) return n->check("tmc_mlp_train");
-  return n->check("tmc_mlp_train");
+  return train_status(n, "tmc_mlp_train");
 }
 
 int tmc_mlp_gradient(tmc_mlp* n, const float* x, const float* y, int64_t rows, float* grad, double* loss) {
@@ -690,15 +768,15 @@ int tmc_mlp_gradient(tmc_mlp* n, const float* x, const float* y, int64_t rows, f
   cudaMemcpyAsync(n->io_y, y, sizeof(float) * rows, cudaMemcpyHostToDevice, n->st);
   cudaMemsetAsync(n->g, 0, sizeof(float) * kParams, n->st);
   cudaMemsetAsync(n->d_loss, 0, sizeof(double), n->st);
-  k_mlp_train<<<(unsigned)(rows / kTile), kTile, sizeof(TrainSmem), n->st>>>(n->net(), n->io_x, n->io_y, rows, 0,
-                                                                             1.f / (float)rows, n->g, n->d_loss);
+  cudaMemsetAsync(n->d_err, 0, sizeof(int), n->st);
+  launch_gradient(n, n->io_x, n->io_y, rows, 0, rows);
   cudaMemcpyAsync(grad, n->g, sizeof(float) * kParams, cudaMemcpyDeviceToHost, n->st);
   double l = 0.0;
   cudaMemcpyAsync(&l, n->d_loss, sizeof(double), cudaMemcpyDeviceToHost, n->st);
   cudaMemsetAsync(n->g, 0, sizeof(float) * kParams, n->st);
-  if (cudaStreamSynchronize(n->st) != cudaSuccess) return n->check("tmc_mlp_gradient");
-  if (loss) *loss = l;
-  return n->check("tmc_mlp_gradient");
+  rc = train_status(n, "tmc_mlp_gradient");
+  if (rc == TMC_OK && loss) *loss = l;
+  return rc;
 }
 
 }  // extern "C"

@@ -314,7 +314,8 @@ class TMCoreGroup:
 class ClosureMLP:
     """The 24-64-64-64-1 GELU network of the learned PV-on-edge closure
     (tmc_mlp_*): BF16 weights, FP32 accumulation, tensor-core forward,
-    Adam training on the device."""
+    Adam training on the device (forward and backward on the tensor cores,
+    or on the CUDA cores in FP32 after ``set_train_mode(False)``)."""
 
     def __init__(self, device: int = 0, seed: int = 0):
         self.lib = _lib.gpu()
@@ -369,6 +370,10 @@ class ClosureMLP:
         y = np.ascontiguousarray(y, np.float32).reshape(-1)
         self._keep = (x, y)
         self._chk(self.lib.tmc_mlp_set_dataset(self.n, _ptr(x), _ptr(y), x.shape[0]))
+
+    def set_train_mode(self, tensor_cores: bool):
+        """Run train() and gradient() on the tensor cores (True) or the CUDA cores."""
+        self._chk(self.lib.tmc_mlp_set_train_mode(self.n, 1 if tensor_cores else 0))
 
     def train(self, steps: int, batch: int = 65536, lr: float = 1e-3) -> np.ndarray:
         losses = np.empty(max(int(steps), 1), np.float32)
