@@ -204,23 +204,28 @@ __device__ bool train_tiles(const Net& net, const Src& src, long long ntiles, fl
     __syncthreads();
   };
 
+  // the row of the block's next tile, loaded while the current one runs
+  float xr[kIn], tr = 0.f;
+  bool vr = blockIdx.x < ntiles ? src.sample((long long)blockIdx.x * kTrTile + r, xr, tr) : false;
   for (long long tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-    float xs[kInPad], tgt;
+    const float tgt = vr ? tr : 0.f;
     {
-      float xr[kIn];
-      const bool valid = src.sample(tile * kTrTile + r, xr, tgt);
+      float xs[kInPad];
 #pragma unroll
-      for (int k = 0; k < kIn; ++k) xs[k] = valid ? (xr[k] - sxm[k]) * sxi[k] : 0.f;
+      for (int k = 0; k < kIn; ++k) xs[k] = vr ? (xr[k] - sxm[k]) * sxi[k] : 0.f;
       xs[kIn] = xs[kIn + 1] = 1.f;
 #pragma unroll
       for (int k = kIn + 2; k < kInPad; ++k) xs[k] = 0.f;
-      if (!valid) tgt = 0.f;
 #pragma unroll
       for (int k0 = 0; k0 < kInPad; k0 += 8) store8_bf16(sA, r, k0, kInPad, xs + k0);
 #pragma unroll
       for (int k = 0; k < kInPad; ++k) st_bf16(sXT, k, r, kTrK, xs[k]);
     }
     publish();
+    {
+      const long long nt = tile + gridDim.x;
+      vr = nt < ntiles ? src.sample(nt * kTrTile + r, xr, tr) : false;
+    }
     // forward
     float y = b4;
 #pragma unroll 1
