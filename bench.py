@@ -352,11 +352,10 @@ def run_ensemble(args, local, ics, peak):
     L, M = args.ensemble_level, len(ics)
     m = mesh.icos_mesh(L)
     dt = 1200.0 / 2 ** (L - 4)
-    res = {}
-    for layout in ((1, 0) if M % 32 == 0 else (0,)):
-        ens = TMCoreGPU(m, members=M, dt=dt, pv_scheme=1, apvm_weight=0.0, adv_order=2, conserve_energy=1,
-                        precision=abi.TMC_FP32, diag_every=1, use_graph=1, renumber=1, device=local,
-                        member_layout=layout)
+
+    def timed(layout, **scheme):
+        ens = TMCoreGPU(m, members=M, dt=dt, adv_order=2, conserve_energy=1, precision=abi.TMC_FP32, diag_every=1,
+                        use_graph=1, renumber=1, device=local, member_layout=layout, **scheme)
         for k, (gd, u, ghs) in enumerate(ics):
             ens.select_member(k)
             ens.set_initial(gd, u, ghs)
@@ -367,7 +366,10 @@ def run_ensemble(args, local, ics, peak):
         passes = ens.pass_times(3) if layout == 1 else None
         d = ens.diag()
         ens.close()
-        res[layout] = (ms / args.ensemble_steps / 1e3, launches, d, tuned, passes)
+        return ms / args.ensemble_steps / 1e3, launches, d, tuned, passes
+
+    centred = dict(pv_scheme=1, apvm_weight=0.0)
+    res = {layout: timed(layout, **centred) for layout in ((1, 0) if M % 32 == 0 else (0,))}
     lay = 1 if 1 in res else 0
     step_s, launches, d, tuned, passes = res[lay]
     mb = ensemble_model_bytes(m.nCells, m.nEdges, m.nVertices, 4, M)
@@ -388,6 +390,13 @@ def run_ensemble(args, local, ics, peak):
         s0 = res[0][0]
         out["member_outermost"] = {"ms_per_step": s0 * 1e3, "member_days_per_s": M * dt / DAY / s0,
                                    "block_sizes": res[0][3]}
+    if lay == 1:
+        # the reference namelist's pv scheme: upwind pv on edges, interp_pv_order 3
+        up = {k: timed(k, pv_scheme=3, interp_pv_order=3) for k in (1, 0)}
+        out["upwind_pv"] = {"pv_scheme": 3, "interp_pv_order": 3,
+                            "ms_per_step": up[1][0] * 1e3, "member_days_per_s": M * dt / DAY / up[1][0],
+                            "edge_pv_ms_per_launch": up[1][4]["edge_pv"],
+                            "member_outermost_ms_per_step": up[0][0] * 1e3}
     return out
 
 

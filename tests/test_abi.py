@@ -55,7 +55,8 @@ def test_member_layout_arguments_checked_before_device_set_up():
     cases = [
         (dict(members=40, member_layout=1, precision=1, pv_scheme=1, apvm_weight=0.0, adv_order=2), abi.TMC_E_ARG),
         (dict(members=32, member_layout=2, precision=1, pv_scheme=1, apvm_weight=0.0, adv_order=2), abi.TMC_E_ARG),
-        (dict(members=32, member_layout=1, precision=1, pv_scheme=3, interp_pv_order=3), abi.TMC_E_UNSUP),
+        (dict(members=32, member_layout=1, precision=1, pv_scheme=3, interp_pv_order=5), abi.TMC_E_UNSUP),
+        (dict(members=32, member_layout=1, precision=1, pv_scheme=2), abi.TMC_E_UNSUP),
         (dict(members=32, member_layout=1, precision=1, pv_scheme=1, apvm_weight=0.0, adv_order=2, n_tracers=1),
          abi.TMC_E_UNSUP),
         (dict(members=32, member_layout=1, precision=0, pv_scheme=1, apvm_weight=0.0, adv_order=2), abi.TMC_E_UNSUP),

@@ -99,6 +99,37 @@ def test_members_match_single_runs_with_beta(mesh4, members):
     ens.close()
 
 
+# the reference namelist's pv scheme (upwind, interp_pv_order 3; its
+# apvm_weight 0.5 applies to pv_scheme 1 only), and order 4
+@pytest.mark.parametrize("members,order", [(M, 3), (2 * M, 3), (48, 4)])
+def test_upwind_pv_members_match_single_runs(mesh4, members, order):
+    from tmcore_gb300.gpu import TMCoreGPU
+
+    kw = dict(dt=600.0, conserve_energy=1, diag_every=1, precision=1, pv_scheme=3, interp_pv_order=order,
+              apvm_weight=0.5, adv_order=2)
+    ics = _ics(mesh4, members, 1100)
+    ens = TMCoreGPU(mesh4, members=members, member_layout=1, **kw)
+    for m, (gd, u, ghs) in enumerate(ics):
+        ens.select_member(m)
+        ens.set_initial(gd, u, ghs)
+    ens.step(8)
+    all_diag = ens.diag_all()
+    for m in (0, 21, members - 1):
+        one = TMCoreGPU(mesh4, **kw)
+        one.set_initial(*ics[m])
+        one.step(8)
+        ens.select_member(m)
+        ge, ie, ue = ens.get_state()
+        g1, i1, u1 = one.get_state()
+        errs = (rel_max(ge, g1), rel_max(ie, i1), rel_max(ue, u1))
+        assert errs[0] < 1e-6 and max(errs[1:]) < 1e-5, (m, errs)
+        d1 = one.diag()
+        assert abs(all_diag[m, 4] - d1[4]) < 1e-6, (m, all_diag[m, 4], d1[4])  # beta
+        assert abs(all_diag[m, 0] - d1[0]) <= 1e-12 * abs(d1[0])
+        one.close()
+    ens.close()
+
+
 def test_mass_conserved_and_energy_steady(mesh4):
     kw = dict(dt=600.0, conserve_energy=1, diag_every=1)
     ens = _ensemble(mesh4, _ics(mesh4, 2 * M, 300), 1, **kw)
@@ -160,9 +191,10 @@ def test_member_layout_refusals(mesh3):
     with pytest.raises(TMCError) as e:
         TMCoreGPU(mesh3, dt=600.0, members=40, member_layout=1, **KW)
     assert e.value.code == abi.TMC_E_ARG
-    with pytest.raises(TMCError) as e:
-        TMCoreGPU(mesh3, dt=600.0, members=32, member_layout=1, precision=1, pv_scheme=3, interp_pv_order=3)
-    assert e.value.code == abi.TMC_E_UNSUP
+    for kw in (dict(pv_scheme=3, interp_pv_order=5), dict(pv_scheme=2, apvm_weight=0.5)):
+        with pytest.raises(TMCError) as e:
+            TMCoreGPU(mesh3, dt=600.0, members=32, member_layout=1, precision=1, **kw)
+        assert e.value.code == abi.TMC_E_UNSUP
 
 
 def test_closure_features_match_member_outermost(mesh4):
@@ -237,9 +269,8 @@ def test_ordering_autotuner(mesh4):
     ens.step(3)
     assert np.all(np.isfinite(ens.diag_all()))
     ens.close()
-    # pv_scheme 3 has no member-innermost kernels: only member_layout 0 is timed
-    kw = dict(KW, pv_scheme=3, interp_pv_order=3)
-    kw.pop("apvm_weight")
+    # pv_scheme 2 has no member-innermost kernels: only member_layout 0 is timed
+    kw = dict(KW, pv_scheme=2)
     best, timings = tune.autotune_ordering(mesh4, ics, steps=1, orders=(1,), dt=600.0, **kw)
     assert best["member_layout"] == 0
     assert [t["member_layout"] for t in timings if "error" in t] == [1]

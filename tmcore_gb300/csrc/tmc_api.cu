@@ -671,7 +671,9 @@ struct EnsEngine : EngineBase {
   float* pv_c = nullptr;  // pv on cells (the learned closure's features)
   float *invA_hl = nullptr, *A_hl = nullptr;
   float *cdv = nullptr, *cae = nullptr, *vdc = nullptr;
+  ens::Upwind up{};  // pv_scheme 3: the vertex fit stencils (width 0 otherwise)
   explicit EnsEngine(tmc_handle* hh) : h(hh) {}
+  const ens::Upwind* upwind() const { return up.width ? &up : nullptr; }
 
   int alloc() override {
     const size_t M_ = (size_t)h->members;
@@ -733,6 +735,16 @@ struct EnsEngine : EngineBase {
     cdv = h->upload(v_cdv);
     cae = h->upload(v_cae);
     vdc = h->upload(v_vdc);
+    if (h->O.pv_scheme == 3) {
+      // the weights in FP32, as the FP32 single-model kernel converts them
+      std::vector<float> wf(hm.vert2.w.begin(), hm.vert2.w.end());
+      up.count = h->M.vert2.count;
+      up.idx = h->M.vert2.idx;
+      up.w = h->upload(wf);
+      up.width = hm.vert2.width;
+      up.coef2 = (float)h->O.vert_coef2;
+      if (!up.w || !up.count || !up.idx) return TMC_E_CUDA;
+    }
     if (!EP.sf || !EP.sd || !pv_e || !pv_c || !F[1] || !gd_v || !invA_hl || !A_hl || !cdv || !cae || !vdc)
       return TMC_E_CUDA;
     cudaMemset(ghs, 0, sizeof(double) * nc);
@@ -806,7 +818,7 @@ struct EnsEngine : EngineBase {
       ens::launch_vertex(M, D, s, EP, dg, b[P_VERTEX], h->st);
       mark(P_VERTEX);
       mark(P_PV);
-      ens::launch_edge_pv(M, D, s, b[P_PV], h->st);
+      ens::launch_edge_pv(M, D, s, upwind(), b[P_PV], h->st);
       if (h->closure) {
         // the learned closure on this stage's pv_edge: in every stage, or in
         // stage 1 with its output held for stages 2-4
@@ -885,7 +897,7 @@ struct EnsEngine : EngineBase {
     launch_diag_pass(false);
     const ens::IO s = io(0);
     ens::launch_cell(h->M, D, s, RKStage{0, 0.0}, EP, false, h->bsp[P_CELL], h->st);
-    ens::launch_edge_pv(h->M, D, s, h->bsp[P_PV], h->st);
+    ens::launch_edge_pv(h->M, D, s, upwind(), h->bsp[P_PV], h->st);
     ens::launch_v2c(h->M, D, s, pv_c, h->st);
     ens::launch_closure_features(h->M, D, s, pv_c, h->cur, feat, pv, h->st);
   }
@@ -1054,9 +1066,11 @@ int tmc_create(const tmc_mesh_desc* mesh, const tmc_params* params, tmc_handle**
   if (p.member_layout != 0) {
     if (p.member_layout != 1) return bad("member_layout must be 0 (member-outermost) or 1 (member-innermost)");
     if (h->members < 16 || h->members % 16 != 0) return bad("member_layout 1 needs members a multiple of 16");
-    if (p.pv_scheme != 1 || p.apvm_weight != 0.0 || p.adv_order != 2 || p.n_tracers != 0 ||
-        p.flux_4th_order_correct) {
-      h->err = "member_layout 1 runs centred pv (pv_scheme 1, apvm_weight 0), adv_order 2, no tracers";
+    const bool centred = p.pv_scheme == 1 && p.apvm_weight == 0.0;
+    const bool upwind = p.pv_scheme == 3 && (p.interp_pv_order == 3 || p.interp_pv_order == 4);
+    if (!(centred || upwind) || p.adv_order != 2 || p.n_tracers != 0 || p.flux_4th_order_correct) {
+      h->err = "member_layout 1 runs centred pv (pv_scheme 1, apvm_weight 0) or upwind pv (pv_scheme 3, "
+               "interp_pv_order 3 or 4), adv_order 2, no tracers";
       *out = h.release();
       return TMC_E_UNSUP;
     }
@@ -1227,6 +1241,11 @@ int tmc_create(const tmc_mesh_desc* mesh, const tmc_params* params, tmc_handle**
   }
   if (h->d_closure_err) cudaMemset(h->d_closure_err, 0, sizeof(int));
   cudaMemset(h->P.base, 0, sizeof(double) * h->P.member_stride() * h->members);
+  if (p.member_layout == 1 && p.pv_scheme == 3 && h->hm.vert2.width > ens::kUpW) {
+    h->err = "member_layout 1: vertex fit stencils wider than " + std::to_string(ens::kUpW);
+    *out = h.release();
+    return TMC_E_UNSUP;
+  }
   if (p.member_layout == 1)
     h->eng = std::make_unique<EnsEngine>(h.get());
   else if (p.precision == TMC_FP32)

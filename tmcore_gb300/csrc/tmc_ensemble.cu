@@ -30,6 +30,12 @@
 #endif
 // vertices per warp iteration of the vertex pass (512 level-6 members:
 // 2 -> 4.85 ms per step, 1 -> 4.86, 4 -> 4.89)
+// shared-memory carveout (percent) of the upwind pv kernel: its stencil
+// gathers reuse lines in L1, which the carveout leaves to it (-1: the
+// driver's choice)
+#ifndef TMC_ENS_UP_CARVEOUT
+#define TMC_ENS_UP_CARVEOUT -1
+#endif
 #ifndef TMC_ENS_VU
 #define TMC_ENS_VU 2
 #endif
@@ -538,6 +544,87 @@ __global__ void __launch_bounds__(kMaxBS) k_ens_edge_pv(DevMesh Mh, Dims D, IO S
 }
 
 // ---------------------------------------------------------------------------
+// edge_pv, upwind (pv_scheme 3, orders 3 and 4; operators_mod.F90:359-412):
+// the centred value corrected by the two-sided fit-stencil second
+// derivatives, upwinded by the sign of the tangential velocity
+// (operators_mod.F90:296-316 for the tangential velocity)
+// ---------------------------------------------------------------------------
+template <int V>
+__global__ void __launch_bounds__(kMaxBS) k_ens_edge_pv_up(DevMesh Mh, Dims D, IO S, Upwind U) {
+  __shared__ int s_v[2][kEnsEPB];
+  __shared__ int s_ep[kME2][kEnsEPB];
+  __shared__ float s_we[kME2][kEnsEPB];
+  __shared__ int s_n[2][kEnsEPB];
+  __shared__ int s_i[kUpW][2][kEnsEPB];
+  __shared__ float s_w[kUpW][2][kEnsEPB];
+  __shared__ float s_dv[kEnsEPB];
+  const int ne = Mh.ne, e0 = blockIdx.x * kEnsEPB, nel = min(kEnsEPB, ne - e0);
+  for (int t = threadIdx.x; t < 2 * kEnsEPB; t += blockDim.x) {
+    const int i = t / kEnsEPB, j = t - i * kEnsEPB;
+    if (j < nel) {
+      s_v[i][j] = Mh.verticesOnEdge[(size_t)i * ne + e0 + j];
+      s_n[i][j] = U.count[(size_t)i * ne + e0 + j];
+    }
+  }
+  for (int t = threadIdx.x; t < kME2 * kEnsEPB; t += blockDim.x) {
+    const int i = t / kEnsEPB, j = t - i * kEnsEPB;
+    if (j < nel) {
+      const size_t k = (size_t)i * ne + e0 + j;
+      s_ep[i][j] = Mh.edgesOnEdge[k];  // padded entries: the edge itself, weight 0
+      s_we[i][j] = Mh.weightsOnEdge_f[k];
+    }
+  }
+  for (int t = threadIdx.x; t < U.width * 2 * kEnsEPB; t += blockDim.x) {
+    const int q = t / kEnsEPB, j = t - q * kEnsEPB;  // q = stencil point * 2 + side
+    if (j < nel) {
+      const size_t k = (size_t)q * ne + e0 + j;
+      s_i[q >> 1][q & 1][j] = U.idx[k];
+      s_w[q >> 1][q & 1][j] = U.w[k];
+    }
+  }
+  for (int j = threadIdx.x; j < nel; j += blockDim.x) s_dv[j] = Mh.dvEdge_f[e0 + j];
+  __syncthreads();
+  const Lane L = lane_of<V>(D);
+  const size_t Mm = L.M;
+  const float coef2 = U.coef2;
+  for (int j = L.j0; j < nel; j += L.js) {
+    float p[2][V], ve[V], d[2][V];
+    ldv<V>(S.pv_v, (size_t)s_v[0][j] * Mm + L.m0, p[0]);
+    ldv<V>(S.pv_v, (size_t)s_v[1][j] * Mm + L.m0, p[1]);
+#pragma unroll
+    for (int c = 0; c < V; ++c) ve[c] = 0.f;
+#pragma unroll
+    for (int i = 0; i < kME2; ++i) {
+      float uu[V];
+      ldv<V>(S.u, (size_t)s_ep[i][j] * Mm + L.m0, uu);
+#pragma unroll
+      for (int c = 0; c < V; ++c) ve[c] = ve[c] + uu[c] * s_we[i][j];
+    }
+#pragma unroll
+    for (int sd = 0; sd < 2; ++sd) {
+#pragma unroll
+      for (int c = 0; c < V; ++c) d[sd][c] = 0.f;
+      const int n = s_n[sd][j];
+      for (int q = 0; q < n; ++q) {
+        float f[V];
+        ldv<V>(S.pv_v, (size_t)s_i[q][sd][j] * Mm + L.m0, f);
+        const float w = s_w[q][sd][j];
+#pragma unroll
+        for (int c = 0; c < V; ++c) d[sd][c] = d[sd][c] + w * (f[c] - p[sd][c]);
+      }
+    }
+    const float dist = s_dv[j];
+    float pe[V];
+#pragma unroll
+    for (int c = 0; c < V; ++c) {
+      const float fe = 0.5f * (p[0][c] + p[1][c]);
+      pe[c] = fe - dist * dist * ((d[0][c] + d[1][c]) - copysignf(1.f, ve[c]) * coef2 * (d[1][c] - d[0][c])) / 12.f;
+    }
+    stv<V>(S.pv_e, (size_t)(e0 + j) * Mm + L.m0, pe);
+  }
+}
+
+// ---------------------------------------------------------------------------
 // edge_flux: q.F_perp over the 10 neighbours (calc_tangent_vor_flux,
 // operators_mod.F90:239-260), the gradient of E and the iap_u tendency
 // (calc_u_tend_on_edge, tmcore_swm_mod.F90:155-201), the RK update of iap_u
@@ -909,9 +996,24 @@ void launch_vertex(const DevMesh& Mh, const Dims& D, const IO& S, const Partials
   else
     k_ens_vertex<1><<<g, th, 0, st>>>(Mh, D, S, P, diag ? 1 : 0);
 }
-void launch_edge_pv(const DevMesh& Mh, const Dims& D, const IO& S, int bs, cudaStream_t st) {
+void launch_edge_pv(const DevMesh& Mh, const Dims& D, const IO& S, const Upwind* up, int bs, cudaStream_t st) {
   int th;
   const dim3 g = grid_of(Mh.ne, D, bs, &th);
+  if (up) {
+#if TMC_ENS_UP_CARVEOUT >= 0
+    static bool carve = false;
+    if (!carve) {
+      cudaFuncSetAttribute(k_ens_edge_pv_up<2>, cudaFuncAttributePreferredSharedMemoryCarveout, TMC_ENS_UP_CARVEOUT);
+      cudaFuncSetAttribute(k_ens_edge_pv_up<1>, cudaFuncAttributePreferredSharedMemoryCarveout, TMC_ENS_UP_CARVEOUT);
+      carve = true;
+    }
+#endif
+    if (D.V == 2)
+      k_ens_edge_pv_up<2><<<g, th, 0, st>>>(Mh, D, S, *up);
+    else
+      k_ens_edge_pv_up<1><<<g, th, 0, st>>>(Mh, D, S, *up);
+    return;
+  }
   if (D.V == 2)
     k_ens_edge_pv<2><<<g, th, 0, st>>>(Mh, D, S);
   else

@@ -101,7 +101,19 @@ void launch_cell(const DevMesh& Mh, const Dims& D, const IO& S, RKStage rk, cons
                  cudaStream_t st);
 void launch_vertex(const DevMesh& Mh, const Dims& D, const IO& S, const Partials& P, bool diag, int bs,
                    cudaStream_t st);
-void launch_edge_pv(const DevMesh& Mh, const Dims& D, const IO& S, int bs, cudaStream_t st);
+// Upwind pv on edges (pv_scheme 3, interp_pv_order 3 or 4): the two-sided
+// vertex fit stencils of the edges, [width][2][nEdges] as DStencil, with FP32
+// weights; width at most kUpW.
+constexpr int kUpW = 16;
+struct Upwind {
+  const uint8_t* count;  // [2][nEdges]
+  const int32_t* idx;    // [width][2][nEdges]
+  const float* w;        // [width][2][nEdges]
+  int width;
+  float coef2;           // 1 for order 3, 0 for order 4
+};
+// centred pv (up null) or upwind pv on edges
+void launch_edge_pv(const DevMesh& Mh, const Dims& D, const IO& S, const Upwind* up, int bs, cudaStream_t st);
 void launch_edge_flux(const DevMesh& Mh, const Dims& D, const IO& S, RKStage rk, const Partials& P, int bs,
                       cudaStream_t st);
 // new = old + beta dt t_new for cells, then edges with the edge preparation
