@@ -100,8 +100,9 @@ def test_members_match_single_runs_with_beta(mesh4, members):
 
 
 # the reference namelist's pv scheme (upwind, interp_pv_order 3; its
-# apvm_weight 0.5 applies to pv_scheme 1 only), and order 4
-@pytest.mark.parametrize("members,order", [(M, 3), (2 * M, 3), (48, 4)])
+# apvm_weight 0.5 applies to pv_scheme 1 only), and order 4; 128 members:
+# four members per lane
+@pytest.mark.parametrize("members,order", [(M, 3), (2 * M, 3), (48, 4), (4 * M, 3)])
 def test_upwind_pv_members_match_single_runs(mesh4, members, order):
     from tmcore_gb300.gpu import TMCoreGPU
 

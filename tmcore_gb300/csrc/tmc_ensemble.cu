@@ -30,11 +30,12 @@
 #endif
 // vertices per warp iteration of the vertex pass (512 level-6 members:
 // 2 -> 4.85 ms per step, 1 -> 4.86, 4 -> 4.89)
-// shared-memory carveout (percent) of the upwind pv kernel: its stencil
-// gathers reuse lines in L1, which the carveout leaves to it (-1: the
-// driver's choice)
-#ifndef TMC_ENS_UP_CARVEOUT
-#define TMC_ENS_UP_CARVEOUT -1
+// members per lane of the upwind pv kernel: 4 (when M is a multiple of 128),
+// else the ensemble's V.  It issues more instructions per member than it
+// moves bytes: on 512 level-6 members its pass takes 0.45 ms with 4, 0.64 ms
+// with 2 and 0.61 ms with 8 (two float4 loads per gather)
+#ifndef TMC_ENS_UP_V
+#define TMC_ENS_UP_V 4
 #endif
 #ifndef TMC_ENS_VU
 #define TMC_ENS_VU 2
@@ -108,7 +109,13 @@ __device__ __forceinline__ double ff_to_double(FF a) { return (double)a.h + (dou
 // V consecutive members of one element: one load / store of V * 4 (or 8) bytes
 template <int V>
 __device__ __forceinline__ void ldv(const float* p, size_t i, float (&o)[V]) {
-  if constexpr (V == 2) {
+  if constexpr (V == 4) {
+    const float4 t = *reinterpret_cast<const float4*>(p + i);
+    o[0] = t.x;
+    o[1] = t.y;
+    o[2] = t.z;
+    o[3] = t.w;
+  } else if constexpr (V == 2) {
     const float2 t = *reinterpret_cast<const float2*>(p + i);
     o[0] = t.x;
     o[1] = t.y;
@@ -128,7 +135,9 @@ __device__ __forceinline__ void ldv(const double* p, size_t i, double (&o)[V]) {
 }
 template <int V>
 __device__ __forceinline__ void stv(float* p, size_t i, const float (&v)[V]) {
-  if constexpr (V == 2)
+  if constexpr (V == 4)
+    *reinterpret_cast<float4*>(p + i) = make_float4(v[0], v[1], v[2], v[3]);
+  else if constexpr (V == 2)
     *reinterpret_cast<float2*>(p + i) = make_float2(v[0], v[1]);
   else
     p[i] = v[0];
@@ -552,11 +561,9 @@ __global__ void __launch_bounds__(kMaxBS) k_ens_edge_pv(DevMesh Mh, Dims D, IO S
 template <int V>
 __global__ void __launch_bounds__(kMaxBS) k_ens_edge_pv_up(DevMesh Mh, Dims D, IO S, Upwind U) {
   __shared__ int s_v[2][kEnsEPB];
-  __shared__ int s_ep[kME2][kEnsEPB];
-  __shared__ float s_we[kME2][kEnsEPB];
+  __shared__ int2 s_ew[kME2][kEnsEPB];      // edgesOnEdge, weightsOnEdge (FP32 bits)
   __shared__ int s_n[2][kEnsEPB];
-  __shared__ int s_i[kUpW][2][kEnsEPB];
-  __shared__ float s_w[kUpW][2][kEnsEPB];
+  __shared__ int2 s_iw[kUpW][2][kEnsEPB];   // stencil point, weight (FP32 bits)
   __shared__ float s_dv[kEnsEPB];
   const int ne = Mh.ne, e0 = blockIdx.x * kEnsEPB, nel = min(kEnsEPB, ne - e0);
   for (int t = threadIdx.x; t < 2 * kEnsEPB; t += blockDim.x) {
@@ -570,16 +577,15 @@ __global__ void __launch_bounds__(kMaxBS) k_ens_edge_pv_up(DevMesh Mh, Dims D, I
     const int i = t / kEnsEPB, j = t - i * kEnsEPB;
     if (j < nel) {
       const size_t k = (size_t)i * ne + e0 + j;
-      s_ep[i][j] = Mh.edgesOnEdge[k];  // padded entries: the edge itself, weight 0
-      s_we[i][j] = Mh.weightsOnEdge_f[k];
+      // padded entries: the edge itself, weight 0
+      s_ew[i][j] = make_int2(Mh.edgesOnEdge[k], __float_as_int(Mh.weightsOnEdge_f[k]));
     }
   }
   for (int t = threadIdx.x; t < U.width * 2 * kEnsEPB; t += blockDim.x) {
     const int q = t / kEnsEPB, j = t - q * kEnsEPB;  // q = stencil point * 2 + side
     if (j < nel) {
       const size_t k = (size_t)q * ne + e0 + j;
-      s_i[q >> 1][q & 1][j] = U.idx[k];
-      s_w[q >> 1][q & 1][j] = U.w[k];
+      s_iw[q >> 1][q & 1][j] = make_int2(U.idx[k], __float_as_int(U.w[k]));
     }
   }
   for (int j = threadIdx.x; j < nel; j += blockDim.x) s_dv[j] = Mh.dvEdge_f[e0 + j];
@@ -596,9 +602,11 @@ __global__ void __launch_bounds__(kMaxBS) k_ens_edge_pv_up(DevMesh Mh, Dims D, I
 #pragma unroll
     for (int i = 0; i < kME2; ++i) {
       float uu[V];
-      ldv<V>(S.u, (size_t)s_ep[i][j] * Mm + L.m0, uu);
+      const int2 ew = s_ew[i][j];
+      ldv<V>(S.u, (size_t)ew.x * Mm + L.m0, uu);
+      const float w = __int_as_float(ew.y);
 #pragma unroll
-      for (int c = 0; c < V; ++c) ve[c] = ve[c] + uu[c] * s_we[i][j];
+      for (int c = 0; c < V; ++c) ve[c] = ve[c] + uu[c] * w;
     }
 #pragma unroll
     for (int sd = 0; sd < 2; ++sd) {
@@ -607,8 +615,9 @@ __global__ void __launch_bounds__(kMaxBS) k_ens_edge_pv_up(DevMesh Mh, Dims D, I
       const int n = s_n[sd][j];
       for (int q = 0; q < n; ++q) {
         float f[V];
-        ldv<V>(S.pv_v, (size_t)s_i[q][sd][j] * Mm + L.m0, f);
-        const float w = s_w[q][sd][j];
+        const int2 iw = s_iw[q][sd][j];
+        ldv<V>(S.pv_v, (size_t)iw.x * Mm + L.m0, f);
+        const float w = __int_as_float(iw.y);
 #pragma unroll
         for (int c = 0; c < V; ++c) d[sd][c] = d[sd][c] + w * (f[c] - p[sd][c]);
       }
@@ -1000,15 +1009,11 @@ void launch_edge_pv(const DevMesh& Mh, const Dims& D, const IO& S, const Upwind*
   int th;
   const dim3 g = grid_of(Mh.ne, D, bs, &th);
   if (up) {
-#if TMC_ENS_UP_CARVEOUT >= 0
-    static bool carve = false;
-    if (!carve) {
-      cudaFuncSetAttribute(k_ens_edge_pv_up<2>, cudaFuncAttributePreferredSharedMemoryCarveout, TMC_ENS_UP_CARVEOUT);
-      cudaFuncSetAttribute(k_ens_edge_pv_up<1>, cudaFuncAttributePreferredSharedMemoryCarveout, TMC_ENS_UP_CARVEOUT);
-      carve = true;
-    }
-#endif
-    if (D.V == 2)
+    // four members per lane when the member groups allow (the kernel issues
+    // more instructions per member than it moves bytes)
+    if (D.LPE == 32 && D.M % 128 == 0 && TMC_ENS_UP_V == 4)
+      k_ens_edge_pv_up<4><<<dim3(g.x, (unsigned)(D.M / 128)), th, 0, st>>>(Mh, D, S, *up);
+    else if (D.V == 2)
       k_ens_edge_pv_up<2><<<g, th, 0, st>>>(Mh, D, S, *up);
     else
       k_ens_edge_pv_up<1><<<g, th, 0, st>>>(Mh, D, S, *up);
