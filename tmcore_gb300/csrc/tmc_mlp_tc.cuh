@@ -317,6 +317,9 @@ __device__ bool forward_tiles(const Net& net, Src& src, long long ntiles, uint8_
     if (!ok) break;
     if (valid) src.output(row, y * net.yscale);
   }
+  // after a timed-out wait, the MMAs of that commit may still be running:
+  // wait for them (bounded) before the columns are freed
+  if (!ok) mbar_wait(mb, phase ^ 1u);
   fence_before_sync();
   __syncthreads();
   fence_after_sync();

@@ -343,6 +343,9 @@ __device__ bool train_tiles(const Net& net, const Src& src, long long ntiles, fl
     for (int i = r; i < kParams; i += blockDim.x) g[i] = 0.f;
   }
   if (r == 0) ploss[blockIdx.x] = loss;
+  // after a timed-out wait, the MMAs of that commit may still be running:
+  // wait for them (bounded) before the columns are freed
+  if (!ok) mbar_wait(mb, phase ^ 1u);
   fence_before_sync();
   __syncthreads();
   fence_after_sync();
