@@ -30,15 +30,15 @@
 #endif
 // vertices per warp iteration of the vertex pass (512 level-6 members:
 // 2 -> 4.85 ms per step, 1 -> 4.86, 4 -> 4.89)
+#ifndef TMC_ENS_VU
+#define TMC_ENS_VU 2
+#endif
 // members per lane of the upwind pv kernel: 4 (when M is a multiple of 128),
 // else the ensemble's V.  It issues more instructions per member than it
 // moves bytes: on 512 level-6 members its pass takes 0.45 ms with 4, 0.64 ms
 // with 2 and 0.61 ms with 8 (two float4 loads per gather)
 #ifndef TMC_ENS_UP_V
 #define TMC_ENS_UP_V 4
-#endif
-#ifndef TMC_ENS_VU
-#define TMC_ENS_VU 2
 #endif
 #define TMC_ENS_LB_0 __launch_bounds__(256)
 #define TMC_ENS_LB_1 __launch_bounds__(256, 1)
