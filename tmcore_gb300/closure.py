@@ -256,12 +256,14 @@ def main():
     ap.add_argument("--eval-members", type=int, default=16, help="held-out seeds of the comparison (0: skip)")
     ap.add_argument("--eval-days", type=float, default=5.0)
     ap.add_argument("--out", default=None, help="save the trained network (.npz)")
+    ap.add_argument("--trainer", choices=("tc", "cuda"), default="tc",
+                    help="gradients on the tensor cores (tc) or on the CUDA cores in FP32 (cuda)")
     a = ap.parse_args()
     t0 = time.time()
     X, Y = training_data(a.fine_level, a.coarse_level, a.runs, a.days, a.samples)
     t_data = time.time() - t0
     t0 = time.time()
-    net, losses, sc = train(X, Y, steps=a.steps)
+    net, losses, sc = train(X, Y, steps=a.steps, tensor_cores=a.trainer == "tc")
     t_train = time.time() - t0
     if a.out:
         save(a.out, net, sc)
@@ -287,7 +289,7 @@ def main():
     comparison = (evaluate(net, a.fine_level, a.coarse_level, members=a.eval_members, days=a.eval_days)
                   if a.eval_members > 0 else None)
     print(json.dumps({
-        "training_samples": int(len(Y)), "data_s": t_data, "train_s": t_train,
+        "training_samples": int(len(Y)), "data_s": t_data, "train_s": t_train, "trainer": a.trainer,
         "loss_first": float(losses[0]), "loss_last": float(np.mean(losses[-20:])),
         "ensemble": {"members": a.members, "level": a.coarse_level, "steps": nsteps, "wall_s": t_ens,
                      "member_days_per_s": a.members * nsteps * dt / DAY / t_ens,
