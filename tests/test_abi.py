@@ -67,3 +67,11 @@ def test_member_layout_arguments_checked_before_device_set_up():
         assert lib.tmc_create(ctypes.byref(d), ctypes.byref(p), ctypes.byref(h)) == code, kw
         assert h.value and lib.tmc_last_error(h)
         lib.tmc_destroy(h)
+    # accepted combinations pass these checks (here they then fail at the device)
+    for kw in (dict(pv_scheme=1, apvm_weight=0.0), dict(pv_scheme=3, interp_pv_order=3, apvm_weight=0.5),
+               dict(pv_scheme=3, interp_pv_order=4)):
+        p = default_params(dt=600.0, members=32, member_layout=1, precision=1, adv_order=2, **kw)
+        h = ctypes.c_void_p()
+        rc = lib.tmc_create(ctypes.byref(d), ctypes.byref(p), ctypes.byref(h))
+        assert rc not in (abi.TMC_E_ARG, abi.TMC_E_UNSUP), (kw, rc)
+        lib.tmc_destroy(h)
