@@ -208,6 +208,7 @@ class FallbackMonitor:
         self.ref = d[:, :2].copy()
         self.on = np.ones(members, bool)
         self.fallbacks: list[tuple[int, int]] = []
+        self.max_drift = np.zeros(members)  # largest relative energy/mass drift seen per member
         self.steps = 0
         self.ckpt = [self._save(m) for m in range(members)]
 
@@ -228,6 +229,7 @@ class FallbackMonitor:
     def check(self):
         d = self.model.diag_all()
         drift = np.abs(d[:, :2] - self.ref) / np.abs(self.ref)
+        self.max_drift = np.maximum(self.max_drift, np.where(np.isfinite(drift.max(1)), drift.max(1), np.inf))
         bad = np.flatnonzero(self.on & ((drift.max(1) > self.tol) | ~np.all(np.isfinite(d[:, :2]), 1)))
         for m in bad:
             self.model.set_member_closure(int(m), False)
@@ -258,15 +260,20 @@ def main():
     ap.add_argument("--out", default=None, help="save the trained network (.npz)")
     ap.add_argument("--trainer", choices=("tc", "cuda"), default="tc",
                     help="gradients on the tensor cores (tc) or on the CUDA cores in FP32 (cuda)")
+    ap.add_argument("--plain-ensemble", action="store_true",
+                    help="no training: the held-out ensemble without the network, under the same drift monitor")
     a = ap.parse_args()
-    t0 = time.time()
-    X, Y = training_data(a.fine_level, a.coarse_level, a.runs, a.days, a.samples)
-    t_data = time.time() - t0
-    t0 = time.time()
-    net, losses, sc = train(X, Y, steps=a.steps, tensor_cores=a.trainer == "tc")
-    t_train = time.time() - t0
-    if a.out:
-        save(a.out, net, sc)
+    net, losses, t_data, t_train, n_samples = None, None, 0.0, 0.0, 0
+    if not a.plain_ensemble:
+        t0 = time.time()
+        X, Y = training_data(a.fine_level, a.coarse_level, a.runs, a.days, a.samples)
+        t_data = time.time() - t0
+        n_samples = int(len(Y))
+        t0 = time.time()
+        net, losses, sc = train(X, Y, steps=a.steps, tensor_cores=a.trainer == "tc")
+        t_train = time.time() - t0
+        if a.out:
+            save(a.out, net, sc)
     # held-out ensemble on the coarse mesh with the closure and the fallback
     coarse = icos_mesh(a.coarse_level)
     dt = level_dt(a.coarse_level)
@@ -276,8 +283,9 @@ def main():
         gd, u, ghs = cases.jet_bumps(coarse, seed=10_000 + m)
         ens.select_member(m)
         ens.set_initial(gd, u, ghs)
-    ens.set_closure(net)
-    ens.set_closure_stages(a.every_stage)
+    if net is not None:
+        ens.set_closure(net)
+        ens.set_closure_stages(a.every_stage)
     mon = FallbackMonitor(ens, a.members)
     nsteps = int(round(a.ens_days * DAY / dt))
     t0 = time.time()
@@ -285,15 +293,22 @@ def main():
     ens.synchronize()
     t_ens = time.time() - t0
     fallbacks, timed_out = len(mon.fallbacks), ens.closure_status()
+    kept = mon.on
+    drift = {"max_kept": float(mon.max_drift[kept].max()) if kept.any() else None,
+             "median_kept": float(np.median(mon.max_drift[kept])) if kept.any() else None,
+             "max_all": float(mon.max_drift.max())}
     ens.close()
     comparison = (evaluate(net, a.fine_level, a.coarse_level, members=a.eval_members, days=a.eval_days)
-                  if a.eval_members > 0 else None)
+                  if a.eval_members > 0 and net is not None else None)
     print(json.dumps({
-        "training_samples": int(len(Y)), "data_s": t_data, "train_s": t_train, "trainer": a.trainer,
-        "loss_first": float(losses[0]), "loss_last": float(np.mean(losses[-20:])),
+        "training_samples": n_samples, "data_s": t_data, "train_s": t_train,
+        "trainer": None if net is None else a.trainer,
+        "loss_first": None if losses is None else float(losses[0]),
+        "loss_last": None if losses is None else float(np.mean(losses[-20:])),
         "ensemble": {"members": a.members, "level": a.coarse_level, "steps": nsteps, "wall_s": t_ens,
                      "member_days_per_s": a.members * nsteps * dt / DAY / t_ens,
-                     "every_stage": a.every_stage, "fallbacks": fallbacks, "closure_timed_out": timed_out},
+                     "closure": net is not None, "every_stage": a.every_stage, "fallbacks": fallbacks,
+                     "drift_limit": mon.tol, "max_rel_drift": drift, "closure_timed_out": timed_out},
         "comparison": comparison,
     }))
 
