@@ -116,3 +116,15 @@ def test_galewsky_balance_integral_matches_quadpack():
         # QUADPACK qags with the reference's tolerances (epsabs 1e-10, epsrel 1e-3)
         loose = integrate.quad(f, -0.5 * np.pi, lat, epsabs=1e-10, epsrel=1e-3, limit=50)[0]
         assert abs(v - tight) < 1e-12 * scale and abs(v - loose) < 1e-6 * scale, (lat, v, tight, loose)
+
+
+def test_cases_by_name():
+    from tmcore_gb300 import cases
+
+    m = icos(3)
+    for name in cases.SWM_CASES:
+        gd, u, ghs = cases.by_name(name, m, seed=1)
+        assert gd.shape == (m.nCells,) and u.shape == (m.nEdges,) and ghs.shape == (m.nCells,), name
+        assert np.all(np.isfinite(gd)) and np.all(np.isfinite(u)) and np.all(gd > 0), name
+    with pytest.raises(ValueError):
+        cases.by_name("no_such_case", m)

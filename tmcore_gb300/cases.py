@@ -334,3 +334,18 @@ def linearized_rossby_wave(mesh, t=0.0, radius=REF_RADIUS, g=REF_G, omega=REF_OM
     ue, ve = ut * np.cos(ph), vt * np.cos(ph - 0.5 * PI)
     u = ue * np.cos(mesh.angleEdge) + ve * np.sin(mesh.angleEdge)
     return h * g, u, np.zeros(mesh.nCells)
+
+
+# the shallow-water cases by their namelist name (test_cases_mod.F90:17-34), plus
+# the benchmark's seeded case; each returns (gd, u, ghs)
+SWM_CASES = ("jet_bumps", "mountain_zonal_flow", "steady_geostrophic_flow", "rossby_haurwitz_wave",
+             "linearized_rossby_wave", "jet_zonal_flow")
+
+
+def by_name(name: str, mesh, seed: int = 0):
+    """Initial (gd, u, ghs) of the named shallow-water case."""
+    if name == "jet_bumps":
+        return jet_bumps(mesh, seed=seed)
+    if name not in SWM_CASES:
+        raise ValueError(f"unknown case {name!r}; one of {', '.join(SWM_CASES)}")
+    return globals()[name](mesh)

@@ -5,6 +5,7 @@ invariants before and after.
 
     python -m tmcore_gb300.run --level 8 --precision 64 --steps 3
     python -m tmcore_gb300.run --level 9 --precision 32 --tracers 4 --dt 45 --steps 10
+    python -m tmcore_gb300.run --level 6 --case jet_zonal_flow --pv-scheme 3 --dt 240   # the shipped namelist
 """
 from __future__ import annotations
 
@@ -28,6 +29,7 @@ def main():
     ap.add_argument("--tracers", type=int, default=0)
     ap.add_argument("--pv-scheme", type=int, default=1)
     ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--case", default="jet_bumps", choices=cases.SWM_CASES)
     ap.add_argument("--autotune", action="store_true")
     a = ap.parse_args()
     m = icos_mesh(a.level)
@@ -36,7 +38,7 @@ def main():
     kw = dict(interp_pv_order=3) if a.pv_scheme == 3 else dict(apvm_weight=0.0)
     g = TMCoreGPU(m, dt=dt, precision=prec, pv_scheme=a.pv_scheme, adv_order=2, n_tracers=a.tracers,
                   diag_every=1, **kw)
-    gd, u, ghs = cases.jet_bumps(m, seed=a.seed)
+    gd, u, ghs = cases.by_name(a.case, m, seed=a.seed)
     g.set_initial(gd, u, ghs)
     if a.tracers:
         g.set_tracers(cases.smooth_tracers(m, a.tracers, seed=a.seed) * gd[None, :])
@@ -48,7 +50,7 @@ def main():
     passes = g.pass_times(2)
     d1 = g.diag()
     g.close()
-    print(json.dumps({"level": a.level, "nCells": m.nCells, "precision": a.precision, "dt_s": dt,
+    print(json.dumps({"level": a.level, "case": a.case, "nCells": m.nCells, "precision": a.precision, "dt_s": dt,
                       "tracers": a.tracers, "steps": a.steps, "ms_per_step": ms / a.steps,
                       "sim_days_per_s": dt / 86400.0 / (ms / a.steps / 1e3), "passes_ms": passes,
                       "gpu_launches": launches, "block_sizes": sizes,
