@@ -5,8 +5,8 @@ reference's per-element expression order, so single operators and one
 spatial_operators call must be BIT-IDENTICAL to the oracle.  Multi-step runs
 differ only through the order of the global sums (beta, invariants), which
 the device reduces with compensated double-double arithmetic: the bar there
-is the benchmark spec's 1e-11 relative max-norm on h and u after one simulated
-day (checked on level 5 with dt = 600 s, 144 steps).
+is a 1e-11 relative max-norm on h and u after one simulated day (checked on
+level 5 with dt = 600 s, 144 steps).
 """
 import numpy as np
 import pytest
