@@ -68,6 +68,12 @@ def dist_env():
     return rank, world, local
 
 
+def job_value(world: int, steps: int, dt: float, ms_max: float) -> float:
+    """Whole-job simulated days per wall-second: the days all `world` replicas
+    advanced (`steps` steps of `dt` s each) over the slowest rank's time."""
+    return world * steps * dt / DAY / (ms_max / 1e3)
+
+
 class Dist:
     def __init__(self, world):
         self.world = world
@@ -611,8 +617,8 @@ def main():
         if args.ensemble_members <= 0:
             ens_ics = None
     dist = Dist(world)
+    args.seed += rank  # independent replicas: rank r starts from seed + r
     m, gd, u, ghs, q, t_setup = setup(args)
-    args.seed += rank  # independent replicas
     qgd = q * gd[None, :] if args.tracers else None
 
     gpu = TMCoreGPU(m, **gpu_params(args, abi.TMC_FP32), device=local)
@@ -634,7 +640,7 @@ def main():
     clk = clocks.stop()
     ms_max = dist.max(ms_total)
     days = world * args.steps * args.dt / DAY
-    value = days / (ms_max / 1e3)
+    value = job_value(world, args.steps, args.dt, ms_max)
 
     gd32, _, u32 = gpu.get_state()
     d32 = gpu.diag()
