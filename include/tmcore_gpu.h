@@ -88,8 +88,9 @@ typedef struct tmc_params {
                                      prescribed wind 1 cosine-bell rotation, 2 deformation flow case 4 */
   int32_t members;                /* ensemble members sharing the mesh (FP32 shallow water, CRK4); 0 or 1: one */
   int32_t member_layout;          /* ensembles: 0 member-outermost arrays (every option), 1 member-innermost
-                                     (members a multiple of 16; pv_scheme 1 with apvm_weight 0, adv_order 2,
-                                     no tracers): whole-line neighbour gathers */
+                                     (members a multiple of 16; pv_scheme 1 with apvm_weight 0, or pv_scheme 3
+                                     with interp_pv_order 3 or 4; adv_order 2, no tracers; other options:
+                                     TMC_E_UNSUP): whole-line neighbour gathers */
   int32_t reserved[3];
 } tmc_params;
 
