@@ -3,7 +3,8 @@
  * Drop-in for the integrator and operator boundary of TMCORE
  * (TMCORE-Project/TMCORE).  The Fortran host keeps the namelist, mesh / state
  * I/O, logging and test cases; it calls these entry points through
- * iso_c_binding (binding module in INTEGRATION.md).  Every entry point returns
+ * iso_c_binding (a Fortran module of bind(C) interfaces, one per entry
+ * point, with the same argument order).  Every entry point returns
  * 0 on success or a negative TMC_E* code, never exits or aborts; the message
  * of the last failure is tmc_last_error(h).  A handle owns one CUDA stream;
  * calls on one handle must not overlap (one handle per host thread).
@@ -32,7 +33,8 @@ extern "C" {
 #define TMC_OK 0
 #define TMC_E_ARG (-1)      /* bad argument or configuration */
 #define TMC_E_CUDA (-2)     /* CUDA runtime error (message in tmc_last_error) */
-#define TMC_E_HEALTH (-3)   /* non-finite state detected (tmc_get_diag), or a tensor-core wait ran out */
+#define TMC_E_HEALTH (-3)   /* non-finite state (tmc_get_diag), or a tensor-core wait ran out (tmc_mlp_*, and for the
+                               closure in the step: tmc_get_diag, tmc_get_diag_all, tmc_time_integrate) */
 #define TMC_E_UNSUP (-4)    /* option combination not implemented on the device */
 #define TMC_E_STATE (-5)    /* call out of order (e.g. step before set_state) */
 
@@ -210,6 +212,27 @@ int tmc_mlp_gradient(tmc_mlp* n, const float* x, const float* y, int64_t rows, f
  * backward in FP32 from the BF16 weights.  TMC_E_HEALTH: a completion wait of
  * the tensor-core trainer timed out. */
 int tmc_mlp_set_train_mode(tmc_mlp* n, int32_t tensor_cores);
+/* No counterpart in the reference.  The output head: how the raw network
+ * output y of an edge becomes the correction added to pv_edge, and what the
+ * training loss fits (the mean of (correction - target)^2 / y_scale^2).
+ *   head 0 (the default): y * y_scale, unconstrained.
+ *   head 1: -softplus(y) dt (v (q_v2 - q_v1)/dvEdge + u (q_c2 - q_c1)/dcEdge),
+ *     the APVM correction of operators_mod.F90:296-316 with a learned
+ *     non-negative per-edge weight softplus(y) in place of apvm_weight; the
+ *     direction comes from the edge's raw features (1, 22, 0, 23), dt is the
+ *     model time step (> 0).  The correction keeps APVM's sign, so it can only
+ *     remove potential enstrophy as APVM does; inside the energy-conserving
+ *     q.F_perp form it leaves mass and energy unchanged. */
+int tmc_mlp_set_head(tmc_mlp* n, int32_t head, double dt);
+/* No counterpart in the reference (its errors abort, time_scheme_mod.F90:60).
+ * Poll limit of the tensor-core kernels' completion waits (mbarrier polls
+ * per MMA step; < 0 restores the default, 2^20).  A wait that runs out makes
+ * the kernel flag TMC_E_HEALTH, wait with the default limit for the MMAs it
+ * issued, free its tensor memory and return.  With 0 every such wait runs
+ * out at once: this exercises that error path without withholding any
+ * completion.  It applies to tmc_mlp_forward / train / gradient at once and
+ * to a handle's closure from its next tmc_set_closure. */
+int tmc_mlp_set_wait_limit(tmc_mlp* n, int32_t polls);
 
 /* The learned closure in the FP32 CRK4 step: after the pv-on-edge pass of
  * every stage, the network's output for each edge (features: the stage's
@@ -217,8 +240,13 @@ int tmc_mlp_set_train_mode(tmc_mlp* n, int32_t tensor_cores);
  * cells, E, ghs and f on them, dvEdge, dcEdge, u on four neighbour edges, the
  * two pv gradients) is added to pv_edge before q.F_perp.  net = NULL turns it
  * off; the network must outlive its use.  tmc_set_member_closure switches it
- * per ensemble member (the invariant-drift fallback).  tmc_closure_status
- * reports a tensor-core wait that ran out.  tmc_closure_features returns the
+ * per ensemble member (the invariant-drift fallback).  If a tensor-core
+ * completion wait of the network runs out (a bounded wait; the tile group
+ * that saw it leaves its remaining edges uncorrected and the step goes on),
+ * the next tmc_get_diag, tmc_get_diag_all or tmc_time_integrate returns
+ * TMC_E_HEALTH with its outputs filled; tmc_closure_status reports it as
+ * *timed_out = 1.  Each of these reads and clears the flag, so one timeout is
+ * reported once.  tmc_closure_features returns the
  * [nEdges][TMC_MLP_FEATURES] features and pv_edge of state(old) of the
  * selected member (caller's edge order), for training. */
 int tmc_set_closure(tmc_handle* h, const tmc_mlp* net);
@@ -228,6 +256,13 @@ int tmc_set_closure_stages(tmc_handle* h, int32_t every_stage);
 int tmc_set_member_closure(tmc_handle* h, int32_t member, int32_t on);
 int tmc_closure_status(tmc_handle* h, int32_t* timed_out);
 int tmc_closure_features(tmc_handle* h, float* features, double* pv_edge);
+/* No counterpart in the reference.  The correction the network added to
+ * pv_edge in stage 1 of the last step, for the selected member, [nEdges] in
+ * the caller's edge order; needs the closure held from stage 1
+ * (tmc_set_closure_stages(h, 0)) and a step taken with it.  With the state
+ * the step started from, it is the network applied to that state's
+ * tmc_closure_features. */
+int tmc_closure_correction(tmc_handle* h, float* dq);
 
 /* Coarse-graining of a fine-mesh state onto a coarser mesh (the closure's
  * training data and held-out truth).  Cells: kite-area-weighted means (each
@@ -343,10 +378,12 @@ int tmc_sizes(const tmc_handle* h, int64_t* nCells, int64_t* nEdges, int64_t* nV
  * out[1] = energy, a device pointer, written asynchronously on `stream`
  * (a cudaStream_t, NULL for the default stream).  Returns TMC_E_ARG when
  * nCells or nEdges is not in 1..TMC_NOALLOC_MAX_ELEMENTS.  The first call on
- * a device looks up the array's device address with that device current;
- * make that first call before any stream capture.  Calls that overlap on the
- * GPU (other streams, other host threads on the same device) race on the
- * shared array. */
+ * a device looks up the array's device address with that device current
+ * and caches it; make that first call before any stream capture.  After
+ * cudaDeviceReset of a device the cached address is stale: do not call it on
+ * that device again in the same process.  Calls that overlap on the GPU
+ * (other streams, other host threads on the same device) race on the shared
+ * array. */
 int tmc_mass_energy_noalloc(const double* gd, const double* ghs, const double* areaCell, int64_t nCells,
                             const double* iap_u, const double* areaEdge, int64_t nEdges, double* out, void* stream);
 

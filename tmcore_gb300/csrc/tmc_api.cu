@@ -989,6 +989,19 @@ int sync(tmc_handle* h, const char* where) {
   return TMC_OK;
 }
 
+// The closure network's timeout flag (set by k_closure / k_closure_inner when
+// a tensor-core completion wait ran out, after which that tile group skipped
+// its remaining rows): queue its read into *flag and its reset on the
+// handle's stream; the value is valid after the next sync.
+void closure_flag_fetch(tmc_handle* h, int* flag) {
+  *flag = 0;
+  if (!h->d_closure_err) return;
+  cudaMemcpyAsync(flag, h->d_closure_err, sizeof(int), cudaMemcpyDeviceToHost, h->st);
+  cudaMemsetAsync(h->d_closure_err, 0, sizeof(int), h->st);
+}
+constexpr const char* kClosureTimeout =
+    ": a tensor-core completion wait of the closure network timed out; edges after it got no correction";
+
 int h2d(tmc_handle* h, double* dst, const double* src, size_t n) {
   // cudaMemcpyDefault: the caller's array may be host or device memory
   // (unified addressing tells the direction)
@@ -1180,6 +1193,24 @@ int tmc_create(const tmc_mesh_desc* mesh, const tmc_params* params, tmc_handle**
   M.cell4 = upload_stencil(h.get(), hm.cell4);
   M.vert2 = upload_stencil(h.get(), hm.vert2);
   M.vert4 = upload_stencil(h.get(), hm.vert4);
+  if (p.precision == TMC_FP32 && p.pv_scheme == 3 && (p.interp_pv_order == 3 || p.interp_pv_order == 4) &&
+      hm.vert2.width > 0 && hm.vert2.width <= kUpW32) {
+    // the packed FP32 form of the vertex fit stencils (k_edge_pv_up32)
+    std::vector<int2> iw(hm.vert2.idx.size());
+    for (size_t k = 0; k < iw.size(); ++k) {
+      const float wf = (float)hm.vert2.w[k];
+      int wb;
+      std::memcpy(&wb, &wf, sizeof(wb));
+      iw[k] = make_int2(hm.vert2.idx[k], wb);
+    }
+    M.vert2_iw = h->upload(iw);
+    if (!M.vert2_iw) {
+      h->err = "device allocation failed";
+      cudaGetLastError();
+      *out = h.release();
+      return TMC_E_CUDA;
+    }
+  }
   h->d_cell_n2o = h->upload(hm.cell_n2o);
   h->d_edge_n2o = h->upload(hm.edge_n2o);
   h->d_vert_n2o = h->upload(hm.vert_n2o);
@@ -1235,11 +1266,17 @@ int tmc_create(const tmc_mesh_desc* mesh, const tmc_params* params, tmc_handle**
   cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, p.device);
   h->d_member_on = h->dalloc<int>(h->members);
   h->d_closure_err = h->dalloc<int>(1);
-  if (h->d_member_on) {
+  if (!h->d_member_on || !h->d_closure_err) {
+    h->err = "device allocation failed";
+    cudaGetLastError();
+    *out = h.release();
+    return TMC_E_CUDA;
+  }
+  {
     std::vector<int> on(h->members, 1);
     cudaMemcpy(h->d_member_on, on.data(), sizeof(int) * h->members, cudaMemcpyHostToDevice);
   }
-  if (h->d_closure_err) cudaMemset(h->d_closure_err, 0, sizeof(int));
+  cudaMemset(h->d_closure_err, 0, sizeof(int));
   cudaMemset(h->P.base, 0, sizeof(double) * h->P.member_stride() * h->members);
   if (p.member_layout == 1 && p.pv_scheme == 3 && h->hm.vert2.width > ens::kUpW) {
     h->err = "member_layout 1: vertex fit stencils wider than " + std::to_string(ens::kUpW);
@@ -1420,11 +1457,14 @@ int tmc_get_diag(tmc_handle* h, double out[5]) {
   h->eng->launch_diag_pass(true);
   cudaMemcpyAsync(h->h_diag, h->d_diag + (size_t)h->cur * kDiagStride, sizeof(double) * kDiagLen,
                   cudaMemcpyDeviceToHost, h->st);
+  int timed_out = 0;
+  closure_flag_fetch(h, &timed_out);
   int rc = sync(h, "tmc_get_diag");
   if (rc) return rc;
   for (int i = 0; i < 4; ++i) out[i] = h->h_diag[i];
   out[4] = h->step_count > 0 ? h->h_diag[4] : 1.0;
   if ((rc = h->cuda_check("tmc_get_diag"))) return rc;
+  if (timed_out) return h->fail(TMC_E_HEALTH, std::string("tmc_get_diag") + kClosureTimeout);
   // device health: a non-finite invariant means the state has left the
   // physical range (a negative depth makes sqrt(gd_edge) and everything
   // after it NaN); the outputs are filled all the same
@@ -1440,6 +1480,8 @@ int tmc_get_diag_all(tmc_handle* h, double* out) {
   h->eng->launch_diag_pass(true);
   std::vector<double> all((size_t)kDiagStride * h->members);
   cudaMemcpyAsync(all.data(), h->d_diag, sizeof(double) * all.size(), cudaMemcpyDeviceToHost, h->st);
+  int timed_out = 0;
+  closure_flag_fetch(h, &timed_out);
   int rc = sync(h, "tmc_get_diag_all");
   if (rc) return rc;
   for (int m = 0; m < h->members; ++m) {
@@ -1447,7 +1489,9 @@ int tmc_get_diag_all(tmc_handle* h, double* out) {
     for (int i = 0; i < 4; ++i) out[(size_t)m * 5 + i] = d[i];
     out[(size_t)m * 5 + 4] = h->step_count > 0 ? d[4] : 1.0;
   }
-  return h->cuda_check("tmc_get_diag_all");
+  if ((rc = h->cuda_check("tmc_get_diag_all"))) return rc;
+  if (timed_out) return h->fail(TMC_E_HEALTH, std::string("tmc_get_diag_all") + kClosureTimeout);
+  return TMC_OK;
 }
 
 int tmc_time_integrate(tmc_handle* h, const double* gd_old, const double* iap_u_old, const double* qgd_old,
@@ -1505,9 +1549,13 @@ int tmc_time_integrate(tmc_handle* h, const double* gd_old, const double* iap_u_
     if (cudaMemcpyAsync(io[i].out, io[i].raw, io[i].n * sizeof(double), cudaMemcpyDefault, cs) != cudaSuccess)
       return h->cuda_check("D2H");
   }
+  int timed_out = 0;
+  if (h->closure) closure_flag_fetch(h, &timed_out);
   if (cudaStreamSynchronize(cs) != cudaSuccess) return h->cuda_check("tmc_time_integrate");
   if ((rc = sync(h, "tmc_time_integrate"))) return rc;
-  return h->cuda_check("tmc_time_integrate");
+  if ((rc = h->cuda_check("tmc_time_integrate"))) return rc;
+  if (timed_out) return h->fail(TMC_E_HEALTH, std::string("tmc_time_integrate") + kClosureTimeout);
+  return TMC_OK;
 }
 
 int tmc_spatial_operators(tmc_handle* h, const double* gd, const double* iap_u, double* tend_gd,
@@ -1708,11 +1756,29 @@ int tmc_set_member_closure(tmc_handle* h, int32_t member, int32_t on) {
 int tmc_closure_status(tmc_handle* h, int32_t* timed_out) {
   TMC_REQUIRE_SWM(h);
   int v = 0;
-  cudaMemcpyAsync(&v, h->d_closure_err, sizeof(int), cudaMemcpyDeviceToHost, h->st);
+  closure_flag_fetch(h, &v);
   int rc = sync(h, "tmc_closure_status");
   if (rc) return rc;
   if (timed_out) *timed_out = v;
   return TMC_OK;
+}
+
+int tmc_closure_correction(tmc_handle* h, float* dq) {
+  TMC_REQUIRE_SWM(h);
+  if (!dq) return h->fail(TMC_E_ARG, "NULL array");
+  if (!h->closure || h->closure_every_stage || !h->d_closure_dq)
+    return h->fail(TMC_E_STATE, "tmc_closure_correction needs a closure held from stage 1 (tmc_set_closure_stages 0)");
+  if (h->step_count <= 0) return h->fail(TMC_E_STATE, "tmc_closure_correction: no step taken with the closure");
+  const int ne = h->M.ne, mem = h->members;
+  std::vector<float> all((size_t)ne * mem);
+  cudaMemcpyAsync(all.data(), h->d_closure_dq, sizeof(float) * all.size(), cudaMemcpyDeviceToHost, h->st);
+  int rc = sync(h, "tmc_closure_correction");
+  if (rc) return rc;
+  // member-outermost [member][edge] or member-innermost [edge][member]; caller's edge order
+  const bool inner = h->p.member_layout == 1;
+  for (int i = 0; i < ne; ++i)
+    dq[h->hm.edge_n2o[i]] = inner ? all[(size_t)i * mem + h->cur] : all[(size_t)h->cur * ne + i];
+  return h->cuda_check("tmc_closure_correction");
 }
 
 int tmc_closure_features(tmc_handle* h, float* features, double* pv_edge) {
@@ -1889,6 +1955,13 @@ int tmc_autotune(tmc_handle* h, int32_t steps, int32_t block_sizes[5]) {
   if (steps <= 0) steps = 3;
   int rc;
   if ((rc = sync(h, "tmc_autotune"))) return rc;
+  // events first: a failure here leaves nothing allocated and the state as it was
+  const size_t nev = (size_t)steps * 8 + 2;
+  while (h->ev_pool.size() < nev) {
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) return h->cuda_check("cudaEventCreate");
+    h->ev_pool.push_back(e);
+  }
   // save state(old) of every member; the timing steps advance it
   const size_t M_ = (size_t)h->members;
   const bool f32 = h->p.precision == TMC_FP32;
@@ -1908,12 +1981,6 @@ int tmc_autotune(tmc_handle* h, int32_t steps, int32_t block_sizes[5]) {
   cudaMemcpyAsync(sv_gd, gd0, b_gd, cudaMemcpyDeviceToDevice, h->st);
   cudaMemcpyAsync(sv_iap, iap0, b_iap, cudaMemcpyDeviceToDevice, h->st);
   if (q0) cudaMemcpyAsync(sv_q, q0, b_q, cudaMemcpyDeviceToDevice, h->st);
-  const size_t nev = (size_t)steps * 8 + 2;
-  while (h->ev_pool.size() < nev) {
-    cudaEvent_t e;
-    if (cudaEventCreate(&e) != cudaSuccess) return h->cuda_check("cudaEventCreate");
-    h->ev_pool.push_back(e);
-  }
   const int cand_all[6] = {64, 128, 192, 256, 384, 512};
   const int limit = h->members > 1 ? 256 : 512;
   const int order[P_COUNT] = {P_FLUX, P_CELL, P_VERTEX, P_PV, P_FINAL};
@@ -1935,6 +2002,9 @@ int tmc_autotune(tmc_handle* h, int32_t steps, int32_t block_sizes[5]) {
       size_t pos = 0;
       for (int i = 0; i < steps; ++i) h->eng->launch_step(false, &evs, &pos);
       if ((rc = sync(h, "tmc_autotune"))) break;
+      // a block size whose launches were refused (its events would time
+      // nothing) is not a candidate
+      if (cudaGetLastError() != cudaSuccess) continue;
       double sum = 0.0;
       for (size_t k = 0; k + 1 < pos; k += 2) {
         float dt = 0.f;

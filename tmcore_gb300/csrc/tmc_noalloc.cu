@@ -4,12 +4,15 @@
 // The per-block partial sums live in the file-scope array g_noalloc_partials
 // below instead of memory from cudaMalloc.  The array is part of the library
 // image: every GPU that loads the library holds it (TMC_NOALLOC_MAX_ELEMENTS
-// bounds it to 3 x 8192 blocks x 2 doubles = 384 KiB) until the process exits.
-// Its device address is looked up once per device with cudaGetSymbolAddress
-// on the first call made while that device is current.  Every call reuses
-// the same array, and each call overwrites the entries it later reads, so
-// nothing needs clearing; calls that overlap on the GPU (several streams, or
-// several host threads on one device) race on it.
+// bounds it to 3 regions x 8192 blocks x one double-double (hi, lo) block sum
+// = 384 KiB) until the process exits.  Its device address is looked up once
+// per device with cudaGetSymbolAddress on the first call made while that
+// device is current, and cached; cudaDeviceReset on that device unloads the
+// library's device image, so the cached address is stale afterwards and the
+// entry point must not be called again on that device in the same process.
+// Every call reuses the same array, and each call overwrites the entries it
+// later reads, so nothing needs clearing; calls that overlap on the GPU
+// (several streams, or several host threads on one device) race on it.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -34,18 +37,21 @@ constexpr int kMaxDevices = 64;
 std::mutex g_mutex;
 double* g_scratch[kMaxDevices] = {};
 
-__device__ __forceinline__ void store_block_sum(double v, double* slot) {
-  __shared__ double sm[kThreads / 32];
+// Compensated (double-double) sum of the block's per-thread sums, stored as
+// the (hi, lo) pair of one slot.
+__device__ __forceinline__ void store_block_sum(DD v, double* slot) {
+  __shared__ DD sm[kThreads / 32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+  v = warp_reduce_dd(v);
   if (lane == 0) sm[warp] = v;
   __syncthreads();
   if (warp == 0) {
-    double w = (lane < kThreads / 32) ? sm[lane] : 0.0;
-#pragma unroll
-    for (int off = 4; off > 0; off >>= 1) w += __shfl_down_sync(0xffffffffu, w, off);
-    if (lane == 0) slot[0] = w;
+    DD w = (lane < kThreads / 32) ? sm[lane] : DD{0.0, 0.0};
+    w = warp_reduce_dd(w);
+    if (lane == 0) {
+      slot[0] = w.hi;
+      slot[1] = w.lo;
+    }
   }
   __syncthreads();
 }
@@ -54,13 +60,13 @@ __device__ __forceinline__ void store_block_sum(double v, double* slot) {
 // (tmcore_swm_mod.F90:215-231)
 __global__ void __launch_bounds__(kThreads) k_cells(const double* gd, const double* ghs, const double* area,
                                                     int64_t n, double* part) {
-  double m = 0.0, e = 0.0;
+  DD m{0.0, 0.0}, e{0.0, 0.0};
   for (int k = 0; k < kPerThread; ++k) {
     const int64_t i = (int64_t)blockIdx.x * (kThreads * kPerThread) + (int64_t)k * kThreads + threadIdx.x;
     if (i < n) {
       const double g = gd[i], a = area[i];
-      m += g * a;
-      e += (g * g + 2.0 * g * ghs[i]) * a;
+      m = dd_add(m, DD{g * a, 0.0});
+      e = dd_add(e, DD{(g * g + 2.0 * g * ghs[i]) * a, 0.0});
     }
   }
   store_block_sum(m, part + 2 * (0 * kMaxBlocks + blockIdx.x));
@@ -69,10 +75,10 @@ __global__ void __launch_bounds__(kThreads) k_cells(const double* gd, const doub
 
 // edges: energy part sum iap_u^2 * areaEdge
 __global__ void __launch_bounds__(kThreads) k_edges(const double* iap, const double* area, int64_t n, double* part) {
-  double e = 0.0;
+  DD e{0.0, 0.0};
   for (int k = 0; k < kPerThread; ++k) {
     const int64_t i = (int64_t)blockIdx.x * (kThreads * kPerThread) + (int64_t)k * kThreads + threadIdx.x;
-    if (i < n) e += iap[i] * iap[i] * area[i];
+    if (i < n) e = dd_add(e, DD{iap[i] * iap[i] * area[i], 0.0});
   }
   store_block_sum(e, part + 2 * (2 * kMaxBlocks + blockIdx.x));
 }
@@ -83,7 +89,8 @@ __global__ void __launch_bounds__(kThreads) k_final(const double* part, int nb_c
   for (int r = 0; r < kRegions; ++r) {
     const int nb = (r < 2) ? nb_cells : nb_edges;
     DD acc{0.0, 0.0};
-    for (int b = threadIdx.x; b < nb; b += kThreads) acc = dd_add(acc, DD{part[2 * (r * kMaxBlocks + b)], 0.0});
+    for (int b = threadIdx.x; b < nb; b += kThreads)
+      acc = dd_add(acc, DD{part[2 * (r * kMaxBlocks + b)], part[2 * (r * kMaxBlocks + b) + 1]});
     __shared__ DD sm[kThreads / 32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     DD w = warp_reduce_dd(acc);
