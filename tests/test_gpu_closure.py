@@ -107,7 +107,7 @@ def test_training_data_and_training_small():
     X, Y = closure.training_data(fine_level=4, coarse_level=3, runs=1, days=0.25, samples_per_run=2)
     assert X.shape == (2 * 1920, 24) and Y.shape == (2 * 1920,)
     assert np.all(np.isfinite(X)) and np.all(np.isfinite(Y)) and np.std(Y) > 0
-    net, losses, sc = closure.train(X, Y, steps=150, batch=1920, lr=3e-3)
+    net, losses, sc = closure.train(X, Y, steps=150, batch=1920, lr=3e-3, head=0)
     assert losses[-10:].mean() < 0.7 * losses[:3].mean()
     net.close()
 
@@ -148,8 +148,8 @@ def test_trained_closure_gains_on_held_out_seeds():
     from tmcore_gb300 import closure
 
     X, Y = closure.training_data(fine_level=6, coarse_level=4, runs=8, days=2.0, samples_per_run=16)
-    net, losses, _ = closure.train(X, Y, steps=1500)
-    assert np.mean(losses[-20:]) < 0.5 * losses[0]
+    net, losses, _ = closure.train(X, Y, steps=1500, dt=closure.level_dt(4))
+    assert np.mean(losses[-20:]) < 0.9 * losses[0]
     r = closure.evaluate(net, fine_level=6, coarse_level=4, members=8, days=1.0, samples=1)
     e = {k: (v["h"][0], v["u"][0]) for k, v in r["error"].items()}
     assert not r["closure_timed_out"]
@@ -157,4 +157,102 @@ def test_trained_closure_gains_on_held_out_seeds():
         assert e[k][1] < 0.99 * e["plain"][1], e
         assert e[k][0] < 1.002 * e["plain"][0], e
     assert e["plain_finer"][0] < e["plain"][0] and e["plain_finer"][1] < e["plain"][1]
+    net.close()
+
+
+# ---------------------------------------------------------------------------
+# The APVM head (tmc_mlp_set_head(n, 1, dt)): the network predicts a
+# non-negative per-edge APVM weight, and the correction added to pv_edge is
+# -softplus(y) dt (v dq/dt + u dq/dn) (operators_mod.F90:296-316 with a
+# learned weight).  Mass and energy hold by construction; potential enstrophy
+# can only be removed.
+# ---------------------------------------------------------------------------
+def _apvm_net(dt, feats, seed=11):
+    from tmcore_gb300.gpu import ClosureMLP
+
+    net = ClosureMLP(seed=seed)
+    xs = feats.std(0).astype(np.float64)
+    xs[xs == 0] = 1.0
+    net.set_scaling(feats.mean(0), 1.0 / xs, 1.0)
+    net.set_head(1, dt)
+    return net
+
+
+def _numpy_apvm_correction(net, feats, dt):
+    """The network on the features, in numpy with its BF16 roundings, then the APVM head."""
+    from mlp_model import forward_np
+
+    xs = feats.std(0).astype(np.float64)
+    xs[xs == 0] = 1.0
+    xn = ((feats - feats.mean(0).astype(np.float32)) * (1.0 / xs).astype(np.float32)).astype(np.float32)
+    y, _, _ = forward_np(net.params, xn, round_act=True)
+    f = feats.astype(np.float64)
+    return -np.logaddexp(0.0, y) * dt * (f[:, 1] * f[:, 22] + f[:, 0] * f[:, 23])
+
+
+@pytest.mark.parametrize("layout,members", [(0, 1), (1, 16)])
+def test_apvm_head_correction_matches_numpy(mesh4, layout, members):
+    """The correction k_closure adds to pv_edge in the step equals the network
+    evaluated in numpy on the exported features (BF16 tolerance), in both
+    member layouts."""
+    from tmcore_gb300.gpu import TMCoreGPU
+
+    g = TMCoreGPU(mesh4, members=members, member_layout=layout, **KW)
+    for k in range(members):
+        gd, u, ghs = _ic(mesh4, 100 + k)
+        g.select_member(k)
+        g.set_initial(gd, u, ghs)
+    g.step(3)
+    m = members - 1
+    g.select_member(m)
+    feats, _ = g.closure_features()
+    net = _apvm_net(KW["dt"], feats)
+    g.set_closure(net)
+    g.set_closure_stages(False)
+    g.step(1)
+    g.select_member(m)
+    dq = g.closure_correction()
+    ref = _numpy_apvm_correction(net, feats, KW["dt"])
+    scale = np.max(np.abs(ref))
+    assert scale > 0 and np.all(np.isfinite(dq))
+    assert np.max(np.abs(dq - ref)) < 3e-2 * scale, np.max(np.abs(dq - ref)) / scale
+    assert np.sqrt(np.mean((dq - ref) ** 2)) < 1e-2 * np.sqrt(np.mean(ref ** 2))
+    # the head's sign: never against the APVM direction
+    d = feats[:, 1] * feats[:, 22] + feats[:, 0] * feats[:, 23]
+    assert np.all(dq * d <= 0.0)
+    g.close()
+    net.close()
+
+
+def test_apvm_head_conserves_mass_energy_and_dissipates_enstrophy(mesh4):
+    """50 FP32 steps with a nonzero APVM-head correction in every stage: mass
+    stays within 1e-13, energy drifts no more than the plain run's (beta and
+    the energy-conserving q.F_perp form), and potential enstrophy is never
+    above the plain run's after any step."""
+    from tmcore_gb300.gpu import TMCoreGPU
+
+    gd, u, ghs = _ic(mesh4, 120)
+    kw = dict(KW, diag_every=1)
+    a, b = TMCoreGPU(mesh4, **kw), TMCoreGPU(mesh4, **kw)
+    for m in (a, b):
+        m.set_initial(gd, u, ghs)
+    feats, _ = a.closure_features()
+    net = _apvm_net(KW["dt"], feats, seed=12)
+    a.set_closure(net)
+    d0a, d0b = a.diag(), b.diag()
+    moved = 0.0
+    for _ in range(50):
+        a.step(1)
+        b.step(1)
+        da, db = a.diag(), b.diag()
+        assert da[2] <= db[2] * (1.0 + 1e-12), (da[2], db[2])
+        moved = max(moved, abs(da[2] - db[2]) / db[2])
+    assert moved > 1e-7  # the correction did act
+    assert abs(da[0] - d0a[0]) / d0a[0] < 1e-13
+    drift_a = abs(da[1] - d0a[1]) / d0a[1]
+    drift_b = abs(db[1] - d0b[1]) / d0b[1]
+    assert drift_a <= max(10.0 * drift_b, 1e-11), (drift_a, drift_b)
+    assert not a.closure_status()
+    a.close()
+    b.close()
     net.close()

@@ -9,50 +9,7 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-NIN, NH = 24, 64
-
-
-def bf16(a):
-    a = np.ascontiguousarray(a, np.float32)
-    u = a.view(np.uint32).astype(np.uint64)
-    u = (u + 0x7FFF + ((u >> 16) & 1)) >> 16 << 16
-    return u.astype(np.uint32).view(np.float32)
-
-
-def unpack(p):
-    o = 0
-    out = {}
-    for name, shape in (("W1", (NH, NIN)), ("b1", (NH,)), ("W2", (NH, NH)), ("b2", (NH,)), ("W3", (NH, NH)),
-                        ("b3", (NH,)), ("W4", (NH,)), ("b4", (1,))):
-        n = int(np.prod(shape))
-        out[name] = p[o:o + n].reshape(shape)
-        o += n
-    assert o == p.size
-    return out
-
-
-def gelu(z):
-    return 0.5 * z * (1.0 + np.tanh(0.7978845608028654 * (z + 0.044715 * z ** 3)))
-
-
-def gelu_grad(z):
-    t = np.tanh(0.7978845608028654 * (z + 0.044715 * z ** 3))
-    return 0.5 * (1 + t) + 0.5 * z * (1 - t * t) * 0.7978845608028654 * (1 + 3 * 0.044715 * z * z)
-
-
-def forward_np(p, x, round_act):
-    P = unpack(p)
-    W = {k: bf16(P[k]).astype(np.float64) for k in ("W1", "W2", "W3", "W4")}
-    r = (lambda a: bf16(a).astype(np.float64)) if round_act else (lambda a: a)
-    h = r(x.astype(np.float64))
-    zs = []
-    for i, (Wk, bk) in enumerate((("W1", "b1"), ("W2", "b2"), ("W3", "b3"))):
-        z = h @ W[Wk].T + P[bk].astype(np.float64)
-        zs.append(z)
-        h = gelu(z)
-        if i < 2:
-            h = r(h)
-    return h @ W["W4"] + float(P["b4"][0]), zs, W
+from mlp_model import NIN, bf16, forward_np, gelu, gelu_grad, unpack  # noqa: F401
 
 
 def test_tensor_core_forward_matches_model():
@@ -212,4 +169,72 @@ def test_tensor_core_training_fits_a_smooth_target():
     assert losses[-20:].mean() < 0.05 * losses[:5].mean()
     pred = net.forward(x[:4096], tensor_cores=True)
     assert np.mean((pred - y[:4096]) ** 2) < 0.1 * np.var(y)
+    net.close()
+
+
+def apvm_exact_gradient(p, x, t, dt):
+    """FP64 gradient of the APVM head's loss, mean((-softplus(y) a - t)^2)
+    with a = dt (x1 x22 + x0 x23) from the raw features (y_scale 1)."""
+    y, zs, W = forward_np(p, x, round_act=False)
+    xd = x.astype(np.float64)
+    a = dt * (xd[:, 1] * xd[:, 22] + xd[:, 0] * xd[:, 23])
+    pred = -np.logaddexp(0.0, y) * a
+    e = pred - t
+    dy = 2 * e / len(t) * (-a / (1.0 + np.exp(-y)))
+    h = [xd, gelu(zs[0]), gelu(zs[1]), gelu(zs[2])]
+    ref = {"W4": dy @ h[3], "b4": np.array([dy.sum()])}
+    dz = np.outer(dy, W["W4"]) * gelu_grad(zs[2])
+    for layer in (3, 2, 1):
+        ref[f"W{layer}"] = dz.T @ h[layer - 1]
+        ref[f"b{layer}"] = dz.sum(0)
+        if layer > 1:
+            dz = (dz @ W[f"W{layer}"]) * gelu_grad(zs[layer - 2])
+    return ref, float(np.mean(e ** 2)), pred
+
+
+@pytest.mark.parametrize("tensor_cores", [False, True])
+def test_apvm_head_gradient_matches_numpy(tensor_cores):
+    """The APVM output head (a non-negative learned weight on the APVM
+    direction): the forward output and the gradient of its loss on the CUDA
+    cores (FP32) and on the tensor cores (BF16 operands) against FP64 numpy."""
+    from tmcore_gb300.gpu import ClosureMLP
+
+    net = ClosureMLP(seed=13)
+    net.set_train_mode(tensor_cores)
+    dt = 0.7
+    net.set_head(1, dt)
+    rng = np.random.default_rng(6)
+    rows = 160 * 128
+    x = rng.standard_normal((rows, NIN)).astype(np.float32)
+    t = (-0.5 * dt * (x[:, 1] * x[:, 22] + x[:, 0] * x[:, 23]) * (1 + 0.3 * np.tanh(x[:, 3]))).astype(np.float32)
+    g, loss = net.gradient(x, t)
+    p = net.params
+    ref, rloss, pred = apvm_exact_gradient(p, x, t, dt)
+    assert abs(loss - rloss) < 2e-3 * rloss
+    G = unpack(g)
+    for k in ref:
+        d = np.linalg.norm(G[k] - ref[k]) / np.linalg.norm(ref[k])
+        assert d < 3e-3, (k, d)
+    # the forward applies the same head
+    y = net.forward(x[:4096], tensor_cores=tensor_cores)
+    assert np.max(np.abs(y - pred[:4096])) < 3e-2 * np.max(np.abs(pred[:4096]))
+    assert np.all(y * (x[:4096, 1] * x[:4096, 22] + x[:4096, 0] * x[:4096, 23]) <= 0.0)
+    net.close()
+
+
+def test_apvm_head_training_lowers_its_loss():
+    from tmcore_gb300.gpu import ClosureMLP
+
+    net = ClosureMLP(seed=14)
+    dt = 0.7
+    net.set_head(1, dt)
+    rng = np.random.default_rng(7)
+    x = rng.standard_normal((65536, NIN)).astype(np.float32)
+    d = dt * (x[:, 1] * x[:, 22] + x[:, 0] * x[:, 23])
+    w = np.log1p(np.exp(1.5 * np.tanh(x[:, 2]) - 0.5))  # a smooth non-negative weight
+    t = (-w * d).astype(np.float32)
+    net.set_dataset(x, t)
+    losses = net.train(steps=300, batch=8192, lr=3e-3)
+    assert np.all(np.isfinite(losses))
+    assert losses[-20:].mean() < 0.1 * losses[:5].mean()
     net.close()

@@ -253,6 +253,32 @@ def test_fp32_path_error_small(mesh5):
     b.close()
 
 
+@pytest.mark.parametrize("order", [3, 4])
+def test_fp32_upwind_pv_error_small(mesh5, order):
+    """The FP32 path with upwind pv (pv_scheme 3, the shipped namelist's
+    scheme; packed FP32 stencils, one edge per thread) against the FP64 path,
+    which is the oracle's arithmetic: one simulated day at level 5."""
+    from tmcore_gb300.gpu import TMCoreGPU
+
+    gd, u, ghs = _ic(mesh5, seed=6)
+    kw = dict(dt=600.0, pv_scheme=3, interp_pv_order=order)
+    a = TMCoreGPU(mesh5, **kw, precision=0)
+    b = TMCoreGPU(mesh5, **kw, precision=1)
+    for m in (a, b):
+        m.set_initial(gd, u, ghs)
+    ta = a.spatial_operators(*a.get_state()[:2])
+    tb = b.spatial_operators(*a.get_state()[:2])
+    assert rel_max(tb[1], ta[1]) < 1e-4, rel_max(tb[1], ta[1])
+    for m in (a, b):
+        m.step(144)
+    ga, _, ua = a.get_state()
+    gb, _, ub = b.get_state()
+    assert rel_max(gb, ga) < 1e-5, rel_max(gb, ga)
+    assert rel_max(ub, ua) < 1e-3
+    a.close()
+    b.close()
+
+
 @pytest.mark.parametrize("cfg", [
     dict(pv_scheme=1, apvm_weight=0.0, adv_order=3, adv_mono=1),
     dict(pv_scheme=3, interp_pv_order=3, adv_order=4, adv_mono=1),

@@ -98,11 +98,14 @@ SYMBOLS = {
     "tmc_mlp_train": (ctypes.c_int, [vp, i32, i32, ctypes.c_float, vp]),
     "tmc_mlp_gradient": (ctypes.c_int, [vp, vp, vp, ctypes.c_int64, vp, dp]),
     "tmc_mlp_set_train_mode": (ctypes.c_int, [vp, i32]),
+    "tmc_mlp_set_wait_limit": (ctypes.c_int, [vp, i32]),
+    "tmc_mlp_set_head": (ctypes.c_int, [vp, i32, ctypes.c_double]),
     "tmc_set_closure": (ctypes.c_int, [vp, vp]),
     "tmc_set_closure_stages": (ctypes.c_int, [vp, i32]),
     "tmc_set_member_closure": (ctypes.c_int, [vp, i32, i32]),
     "tmc_closure_status": (ctypes.c_int, [vp, ctypes.POINTER(i32)]),
     "tmc_closure_features": (ctypes.c_int, [vp, vp, vp]),
+    "tmc_closure_correction": (ctypes.c_int, [vp, vp]),
     "tmc_coarsen_create": (ctypes.c_int, [ctypes.POINTER(MeshDesc), ctypes.POINTER(MeshDesc), i32,
                                            ctypes.POINTER(vp)]),
     "tmc_coarsen_apply": (ctypes.c_int, [vp, vp, vp, vp, vp, vp, vp]),

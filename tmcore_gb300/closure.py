@@ -70,9 +70,16 @@ def training_data(fine_level=8, coarse_level=6, runs=4, days=1.0, samples_per_ru
     return np.concatenate(X), np.concatenate(Y)
 
 
-def train(X, Y, steps=2000, batch=65536, lr=1e-3, seed=0, device=0, tensor_cores=True):
+def train(X, Y, steps=2000, batch=65536, lr=1e-3, seed=0, device=0, tensor_cores=True, head=1, dt=None):
     """A ClosureMLP fitted to (X, Y), its gradients on the tensor cores (or
-    the CUDA cores); returns (net, losses, scaling)."""
+    the CUDA cores); returns (net, losses, scaling).
+
+    head 1 (the default) fits a non-negative per-edge APVM weight: the
+    correction is -softplus(y) dt (v dq/dt + u dq/dn) with dt the coarse
+    model's time step, so it can only dissipate potential enstrophy; head 0
+    fits the residual itself, unconstrained."""
+    if head == 1 and not dt:
+        raise ValueError("the APVM head needs the coarse model's time step dt")
     rng = np.random.default_rng(seed)
     perm = rng.permutation(len(Y))
     X, Y = X[perm], Y[perm]
@@ -83,10 +90,11 @@ def train(X, Y, steps=2000, batch=65536, lr=1e-3, seed=0, device=0, tensor_cores
     net = ClosureMLP(device=device, seed=seed)
     net.set_train_mode(tensor_cores)
     net.set_scaling(xm, 1.0 / xs, ys)
+    net.set_head(head, dt or 0.0)
     net.set_dataset(X, Y)
     b = min(batch, (len(Y) // 128) * 128)
     losses = net.train(steps=steps, batch=b, lr=lr)
-    return net, losses, {"x_mean": xm, "x_inv_std": 1.0 / xs, "y_scale": ys}
+    return net, losses, {"x_mean": xm, "x_inv_std": 1.0 / xs, "y_scale": ys, "head": head, "head_dt": dt or 0.0}
 
 
 def save(path, net, scaling):
@@ -98,6 +106,8 @@ def load(path, device=0):
     net = ClosureMLP(device=device)
     net.params = z["params"]
     net.set_scaling(z["x_mean"], z["x_inv_std"], float(z["y_scale"]))
+    if "head" in z:
+        net.set_head(int(z["head"]), float(z["head_dt"]))
     return net
 
 
@@ -260,6 +270,8 @@ def main():
     ap.add_argument("--out", default=None, help="save the trained network (.npz)")
     ap.add_argument("--trainer", choices=("tc", "cuda"), default="tc",
                     help="gradients on the tensor cores (tc) or on the CUDA cores in FP32 (cuda)")
+    ap.add_argument("--head", type=int, choices=(0, 1), default=1,
+                    help="1: a learned non-negative APVM weight (enstrophy-dissipating); 0: the residual itself")
     ap.add_argument("--plain-ensemble", action="store_true",
                     help="no training: the held-out ensemble without the network, under the same drift monitor")
     a = ap.parse_args()
@@ -270,7 +282,8 @@ def main():
         t_data = time.time() - t0
         n_samples = int(len(Y))
         t0 = time.time()
-        net, losses, sc = train(X, Y, steps=a.steps, tensor_cores=a.trainer == "tc")
+        net, losses, sc = train(X, Y, steps=a.steps, tensor_cores=a.trainer == "tc", head=a.head,
+                                dt=level_dt(a.coarse_level))
         t_train = time.time() - t0
         if a.out:
             save(a.out, net, sc)

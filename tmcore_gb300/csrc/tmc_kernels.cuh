@@ -34,6 +34,7 @@
 namespace tmc {
 
 constexpr int kEPT = 4;  // elements per thread
+constexpr int kUpW32 = 16;  // widest vertex fit stencil of the packed FP32 upwind pv kernel
 
 struct DStencil {
   int width;
@@ -67,6 +68,10 @@ struct DevMesh {
   const int32_t* v2c_vertex;
   const double* v2c_kite;
   DStencil cell2, cell3, cell4, vert2, vert4;  // cell3: deriv3OnCell on the fit3 (= fit4) stencils
+  // FP32 path with upwind pv of order 3 or 4 (pv_scheme 3): vert2 packed as
+  // (stencil vertex, FP32 weight bits) entries [width][2][ne], width at most
+  // kUpW32 (null otherwise: the generic stencil loop runs)
+  const int2* vert2_iw;
   // FP32 path: FP32-rounded copies of the metrics used in FP32 arithmetic
   // and FP64 reciprocals of the areas used in FP64 arithmetic (null in FP64 mode)
   const float* weightsOnEdge_f;

@@ -716,6 +716,70 @@ __global__ void __launch_bounds__(kMaxBlock) k_edge_pv(DevMesh M, ModelOpt O, St
   }
 }
 
+// FP32 upwind pv on edges (pv_scheme 3, interp_pv_order 3 or 4;
+// operators_mod.F90:359-412, the tangential velocity :223-237): one edge per
+// thread.  The two-sided vertex fit stencils come as packed (index, FP32
+// weight) entries, one 8-byte load each, and every load of the edge is issued
+// up front: the tangential-velocity gathers over a fixed 10 slots (padded
+// slots are the edge itself with weight 0) and the stencil points up to the
+// width with the side's count as a predicate, so an edge's ~35 gathers are in
+// flight together instead of a count-dependent chain.  Sums in stencil order.
+#ifndef TMC_UP32_MINB
+#define TMC_UP32_MINB 2  // resident 256-thread blocks per SM the kernel is compiled for (128 registers)
+#endif
+template <bool kB>
+__global__ void __launch_bounds__(256, TMC_UP32_MINB) k_edge_pv_up32(DevMesh M, ModelOpt O, StageIO<float> S0) {
+  const StageIO<float> S = kB ? S0.at(blockIdx.y) : S0;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= M.ne) return;
+  const int ne = M.ne, W = M.vert2.width;
+  const int v1 = __ldg(M.verticesOnEdge + e), v2 = __ldg(M.verticesOnEdge + ne + e);
+  const int n0 = __ldg(M.vert2.count + e), n1 = __ldg(M.vert2.count + ne + e);
+  int eo[kME2];
+  float wo[kME2];
+#pragma unroll
+  for (int i = 0; i < kME2; ++i) {
+    eo[i] = __ldg(M.edgesOnEdge + (size_t)i * ne + e);
+    wo[i] = __ldg(M.weightsOnEdge_f + (size_t)i * ne + e);
+  }
+  const int m0 = min(n0, W), m1 = min(n1, W);
+  int2 iw[2][kUpW32];
+#pragma unroll
+  for (int j = 0; j < kUpW32; ++j) {
+    iw[0][j] = j < m0 ? __ldg(M.vert2_iw + ((size_t)j * 2 + 0) * ne + e) : make_int2(0, 0);
+    iw[1][j] = j < m1 ? __ldg(M.vert2_iw + ((size_t)j * 2 + 1) * ne + e) : make_int2(0, 0);
+  }
+  const float p1 = __ldg(S.pv_v + v1), p2 = __ldg(S.pv_v + v2);
+  float uo[kME2];
+#pragma unroll
+  for (int i = 0; i < kME2; ++i) uo[i] = __ldg(S.u + eo[i]);
+  float f[2][kUpW32];
+#pragma unroll
+  for (int j = 0; j < kUpW32; ++j) {
+    f[0][j] = j < m0 ? __ldg(S.pv_v + iw[0][j].x) : 0.f;
+    f[1][j] = j < m1 ? __ldg(S.pv_v + iw[1][j].x) : 0.f;
+  }
+  float ve = 0.f;
+#pragma unroll
+  for (int i = 0; i < kME2; ++i) ve = ve + uo[i] * wo[i];
+  float d[2];
+#pragma unroll
+  for (int sd = 0; sd < 2; ++sd) {
+    const float fc = sd == 0 ? p1 : p2;
+    const int n = sd == 0 ? m0 : m1;
+    float acc = 0.f;
+#pragma unroll
+    for (int j = 0; j < kUpW32; ++j)
+      if (j < n) acc = acc + __int_as_float(iw[sd][j].y) * (f[sd][j] - fc);
+    d[sd] = acc;
+  }
+  const float dist = __ldg(M.dvEdge_f + e);
+  const float pe = 0.5f * (p1 + p2) -
+                   dist * dist * ((d[0] + d[1]) - sgn1(ve) * (float)O.vert_coef2 * (d[1] - d[0])) / 12.f;
+  if (S.v_e) S.v_e[e] = ve;
+  S.pv_e[e] = pe;
+}
+
 // ---------------------------------------------------------------------------
 // conservative APVM (calc_pv_on_edge, pv_scheme 2, operators_mod.F90:318-357)
 // ---------------------------------------------------------------------------
@@ -1410,6 +1474,17 @@ template <class T>
 void launch_edge_pv(const DevMesh& M, const ModelOpt& O, const StageIO<T>& S, int bs, cudaStream_t st) {
   if ((O.pv_scheme == 1 && O.apvm_weight != 0.0) || O.pv_scheme == 2 || O.need_pv_c)
     k_v2c<T><<<dim3(grid_for(M.nc, bs), nmem(S)), bs, 0, st>>>(M, S.pv_v, S.pv_c, S.msv, S.msc);
+  if constexpr (!kF64<T>) {
+    if (O.pv_scheme == 3 && (O.interp_pv_order == 3 || O.interp_pv_order == 4) && M.vert2_iw) {
+      const int b = bs < 256 ? bs : 256;  // compiled for at most 256 threads per block
+      const dim3 g(nblk(M.ne, b), nmem(S));
+      if (S.members > 1)
+        k_edge_pv_up32<true><<<g, b, 0, st>>>(M, O, S);
+      else
+        k_edge_pv_up32<false><<<g, b, 0, st>>>(M, O, S);
+      return;
+    }
+  }
   TMC_LAUNCH(k_edge_pv, grid_for(M.ne, bs), M, O, S);
 }
 template <class T>

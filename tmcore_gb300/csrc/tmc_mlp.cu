@@ -258,8 +258,11 @@ __global__ void __launch_bounds__(128) k_mlp_fwd_simt(Net net, const float* x, f
   load_simt_weights(net, w);
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < rows; i += (long long)gridDim.x * blockDim.x) {
     float a[kH], b[kH];
-    float xs[kIn];
-    for (int k = 0; k < kIn; ++k) xs[k] = (x[i * kIn + k] - w.xm[k]) * w.xi[k];
+    float xr[kIn], xs[kIn];
+    for (int k = 0; k < kIn; ++k) {
+      xr[k] = x[i * kIn + k];
+      xs[k] = (xr[k] - w.xm[k]) * w.xi[k];
+    }
     for (int j = 0; j < kH; ++j) {
       float z = w.b[0][j];
       for (int k = 0; k < kIn; ++k) z += w.W1[j][k] * xs[k];
@@ -276,7 +279,7 @@ __global__ void __launch_bounds__(128) k_mlp_fwd_simt(Net net, const float* x, f
       for (int k = 0; k < kH; ++k) z += w.W3[j][k] * b[k];
       out += w.w4[j] * gelu_ref(z);
     }
-    y[i] = out * net.yscale;
+    y[i] = head_out(net, out, head_dir(net, xr));
   }
 }
 
@@ -321,7 +324,12 @@ __global__ void __launch_bounds__(kTile) k_mlp_train(Net net, const float* X, co
   const int t = threadIdx.x;
   const long long i = (offset + (long long)blockIdx.x * kTile + t) % rows;
   // forward
-  for (int k = 0; k < kIn; ++k) S.x[t][k] = (X[i * kIn + k] - S.w.xm[k]) * S.w.xi[k];
+  float xr[kIn];
+  for (int k = 0; k < kIn; ++k) {
+    xr[k] = X[i * kIn + k];
+    S.x[t][k] = (xr[k] - S.w.xm[k]) * S.w.xi[k];
+  }
+  const float dir = head_dir(net, xr);
   float a[kH];
   for (int j = 0; j < kH; ++j) {
     float z = S.w.b[0][j];
@@ -345,8 +353,9 @@ __global__ void __launch_bounds__(kTile) k_mlp_train(Net net, const float* X, co
     S.h[t][j] = h3;
     out += S.w.w4[j] * h3;
   }
-  const float e = out - Y[i] / net.yscale;
-  const float dy = 2.f * e * inv_batch;
+  float dpred;
+  const float e = head_pred(net, out, dir, dpred) - Y[i] / net.yscale;
+  const float dy = 2.f * e * inv_batch * dpred;
   S.dy[t] = dy;
   // loss: block sum of e^2
   {
@@ -406,11 +415,16 @@ __global__ void __launch_bounds__(kTile) k_mlp_train(Net net, const float* X, co
 }
 
 // Adam (Kingma & Ba 2015) on the FP32 master parameters; BF16 copy refreshed,
-// gradient cleared
+// gradient cleared.  A batch whose tensor-core gradient is incomplete (*err
+// set: a completion wait ran out) is not applied; its gradient is dropped.
 __global__ void k_adam(float* p, __nv_bfloat16* pb, float* g, float* m, float* v, int n, float lr, float b1c,
-                       float b2c) {
+                       float b2c, const int* err) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
+  if (*err) {
+    g[i] = 0.f;
+    return;
+  }
   const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
   const float gi = g[i];
   const float mi = b1 * m[i] + (1.f - b1) * gi;
@@ -538,6 +552,9 @@ struct tmc_mlp {
   float* part = nullptr;     // [sms][kParams] per-block partial gradients (tensor-core trainer)
   double* ploss = nullptr;   // [sms]
   int sms = 148;
+  int wait_polls = tmc::mlp::kWaitPolls;  // tmc_mlp_set_wait_limit
+  int head = tmc::mlp::kHeadPlain;        // tmc_mlp_set_head
+  float head_dt = 0.f;
   std::string err;
   int fail(int code, const std::string& s) {
     err = s;
@@ -548,7 +565,7 @@ struct tmc_mlp {
     if (e != cudaSuccess) return fail(TMC_E_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
     return TMC_OK;
   }
-  Net net() const { return Net{p, pb, xmean, xinv, yscale}; }
+  Net net() const { return Net{p, pb, xmean, xinv, yscale, wait_polls, head, head_dt}; }
 };
 
 tmc::mlp::Net tmc_mlp_net(const tmc_mlp* n) { return n->net(); }
@@ -732,6 +749,21 @@ static int train_status(tmc_mlp* n, const char* where) {
   return n->check(where);
 }
 
+int tmc_mlp_set_head(tmc_mlp* n, int32_t head, double dt) {
+  if (!n) return TMC_E_ARG;
+  if (head != kHeadPlain && head != kHeadApvm) return n->fail(TMC_E_ARG, "tmc_mlp_set_head: head must be 0 or 1");
+  if (head == kHeadApvm && !(dt > 0.0)) return n->fail(TMC_E_ARG, "tmc_mlp_set_head: the APVM head needs dt > 0");
+  n->head = head;
+  n->head_dt = head == kHeadApvm ? (float)dt : 0.f;
+  return TMC_OK;
+}
+
+int tmc_mlp_set_wait_limit(tmc_mlp* n, int32_t polls) {
+  if (!n) return TMC_E_ARG;
+  n->wait_polls = polls < 0 ? tmc::mlp::kWaitPolls : std::min<int32_t>(polls, tmc::mlp::kWaitPolls);
+  return TMC_OK;
+}
+
 int tmc_mlp_set_train_mode(tmc_mlp* n, int32_t tensor_cores) {
   if (!n || (tensor_cores != 0 && tensor_cores != 1)) return n ? n->fail(TMC_E_ARG, "tensor_cores must be 0 or 1") : TMC_E_ARG;
   n->train_tc = tensor_cores;
@@ -748,7 +780,8 @@ int tmc_mlp_train(tmc_mlp* n, int32_t batch, int32_t steps, float lr, float* los
     n->cursor = (n->cursor + batch) % n->rows;
     n->adam_t += 1;
     const float b1c = 1.f - std::pow(0.9f, (float)n->adam_t), b2c = 1.f - std::pow(0.999f, (float)n->adam_t);
-    k_adam<<<(kParams + 255) / 256, 256, 0, n->st>>>(n->p, n->pb, n->g, n->m, n->v, kParams, lr, b1c, b2c);
+    k_adam<<<(kParams + 255) / 256, 256, 0, n->st>>>(n->p, n->pb, n->g, n->m, n->v, kParams, lr, b1c, b2c,
+                                                     n->d_err);
     if (losses) {
       double l = 0.0;
       cudaMemcpyAsync(&l, n->d_loss, sizeof(double), cudaMemcpyDeviceToHost, n->st);

@@ -58,9 +58,10 @@ __device__ __forceinline__ void mbar_init(uint32_t mbar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mbar), "r"(count) : "memory");
 }
 
-// Bounded wait for the given phase parity; false when the limit ran out.
-__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
-  for (int i = 0; i < (1 << 20); ++i) {
+// Bounded wait for the given phase parity: at most `polls` polls; false when
+// the limit ran out.
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity, int polls = kWaitPolls) {
+  for (int i = 0; i < polls; ++i) {
     uint32_t done;
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
@@ -241,6 +242,7 @@ __device__ bool forward_tiles(const Net& net, Src& src, long long ntiles, uint8_
   for (; tile < ntiles; tile += stride) {
     const long long row = tile * kTile + r;
     const bool valid = vn;
+    const float dir = valid ? head_dir(net, xn) : 0.f;  // from the raw features, before the prefetch
     {
       float xs[kInPad];
 #pragma unroll
@@ -273,7 +275,7 @@ __device__ bool forward_tiles(const Net& net, Src& src, long long ntiles, uint8_
         }
         mma_commit(mb);
       }
-      const bool got = mbar_wait(mb, phase);
+      const bool got = mbar_wait(mb, phase, net.wait_polls);
       phase ^= 1u;
       ok = group_sync_and(bar, got);
       if (!ok) break;
@@ -315,11 +317,11 @@ __device__ bool forward_tiles(const Net& net, Src& src, long long ntiles, uint8_
       group_sync(bar);
     }
     if (!ok) break;
-    if (valid) src.output(row, y * net.yscale);
+    if (valid) src.output(row, head_out(net, y, dir));
   }
   // after a timed-out wait, the MMAs of that commit may still be running:
   // wait for them (bounded) before the columns are freed
-  if (!ok) mbar_wait(mb, phase ^ 1u);
+  if (!ok) mbar_wait(mb, phase ^ 1u, kWaitPolls);
   fence_before_sync();
   __syncthreads();
   fence_after_sync();

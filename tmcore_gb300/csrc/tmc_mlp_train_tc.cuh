@@ -5,7 +5,8 @@
 // A block of 128 threads takes tiles of 128 rows (thread r = row r = TMEM
 // lane r) in turn.  Per tile:
 //   forward   Z_l = H_{l-1} W_l^T       (M 128, N 64, K 32/64), Z_l kept in TMEM
-//   output    y = b4 + w4 . h3,  dy = 2 (y - t) / batch
+//   output    y = b4 + w4 . h3,  dy = 2 (p(y) - t) p'(y) / batch with p the
+//             output head (p(y) = y for kHeadPlain)
 //   backward  dZ3 = dy w4 * gelu'(z3)
 //             dH2 = dZ3 W3              (M 128, N 64, K 64) into Z3's columns
 //             dZ2 = dH2 * gelu'(z2),    dH1 = dZ2 W2 into Z2's columns
@@ -190,7 +191,7 @@ __device__ bool train_tiles(const Net& net, const Src& src, long long ntiles, fl
       issue();
       mma_commit(mb);
     }
-    const bool got = mbar_wait(mb, phase);
+    const bool got = mbar_wait(mb, phase, net.wait_polls);
     phase ^= 1u;
     const bool all = __syncthreads_and(got) != 0;
     fence_after_sync();
@@ -209,6 +210,7 @@ __device__ bool train_tiles(const Net& net, const Src& src, long long ntiles, fl
   bool vr = blockIdx.x < ntiles ? src.sample((long long)blockIdx.x * kTrTile + r, xr, tr) : false;
   for (long long tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
     const float tgt = vr ? tr : 0.f;
+    const float dir = vr ? head_dir(net, xr) : 0.f;  // from the raw features, before the prefetch
     {
       float xs[kInPad];
 #pragma unroll
@@ -261,9 +263,10 @@ __device__ bool train_tiles(const Net& net, const Src& src, long long ntiles, fl
       publish();
     }
     if (!ok) break;
-    // output layer and loss
-    const float e = y - tgt;
-    const float dy = 2.f * e * inv_batch;
+    // output head and loss
+    float dpred;
+    const float e = head_pred(net, y, dir, dpred) - tgt;
+    const float dy = 2.f * e * inv_batch * dpred;
     {
       float le = e * e;
       for (int off = 16; off > 0; off >>= 1) le += __shfl_down_sync(0xffffffffu, le, off);
@@ -345,7 +348,7 @@ __device__ bool train_tiles(const Net& net, const Src& src, long long ntiles, fl
   if (r == 0) ploss[blockIdx.x] = loss;
   // after a timed-out wait, the MMAs of that commit may still be running:
   // wait for them (bounded) before the columns are freed
-  if (!ok) mbar_wait(mb, phase ^ 1u);
+  if (!ok) mbar_wait(mb, phase ^ 1u, kWaitPolls);
   fence_before_sync();
   __syncthreads();
   fence_after_sync();

@@ -167,6 +167,13 @@ class TMCoreGPU:
         self._chk(self.lib.tmc_closure_status(self.h, ctypes.byref(v)))
         return bool(v.value)
 
+    def closure_correction(self):
+        """[nEdges] the correction the network added to pv_edge in stage 1 of
+        the last step (closure held from stage 1), selected member."""
+        dq = np.empty(self.ne, np.float32)
+        self._chk(self.lib.tmc_closure_correction(self.h, _ptr(dq)))
+        return dq
+
     def closure_features(self):
         """[nEdges, 24] features and pv_edge of state(old) of the selected member."""
         f = np.empty((self.ne, abi.TMC_MLP_FEATURES), np.float32)
@@ -319,6 +326,7 @@ class ClosureMLP:
 
     def __init__(self, device: int = 0, seed: int = 0):
         self.lib = _lib.gpu()
+        self.head, self.head_dt = 0, 0.0
         n = ctypes.c_void_p()
         rc = self.lib.tmc_mlp_create(int(device), int(seed), ctypes.byref(n))
         self.n = n
@@ -374,6 +382,17 @@ class ClosureMLP:
     def set_train_mode(self, tensor_cores: bool):
         """Run train() and gradient() on the tensor cores (True) or the CUDA cores."""
         self._chk(self.lib.tmc_mlp_set_train_mode(self.n, 1 if tensor_cores else 0))
+
+    def set_head(self, head: int, dt: float = 0.0):
+        """Output head: 0 the correction is y * y_scale; 1 it is
+        -softplus(y) dt (v dq/dt + u dq/dn), a learned non-negative APVM weight."""
+        self.head, self.head_dt = int(head), float(dt)
+        self._chk(self.lib.tmc_mlp_set_head(self.n, int(head), float(dt)))
+
+    def set_wait_limit(self, polls: int):
+        """Poll limit of the tensor-core completion waits (< 0: the default);
+        0 makes every wait run out at once, to exercise the error path."""
+        self._chk(self.lib.tmc_mlp_set_wait_limit(self.n, int(polls)))
 
     def train(self, steps: int, batch: int = 65536, lr: float = 1e-3) -> np.ndarray:
         losses = np.empty(max(int(steps), 1), np.float32)
