@@ -138,26 +138,32 @@ def test_fallback_switches_off_a_drifting_member(mesh4):
     bad.close()
 
 
-def test_trained_closure_gains_on_held_out_seeds():
-    """Level-6 FP64 runs coarse-grained to level 4 train the network; on 8
-    held-out seeds, one day on level 4 with the closure (in every stage, and
-    in stage 1 held for the others) has a lower u error against the
-    coarse-grained level-6 truth than level 4 without it, and no higher h
-    error; the plain level-5 run, scored the same way, is more accurate than
-    plain level 4 (the comparison itself is sound)."""
+def test_trained_closure_on_held_out_seeds():
+    """Level-6 FP64 runs coarse-grained to level 4 train the network with
+    both output heads; one day on 8 held-out seeds, scored against the
+    coarse-grained level-6 truth.  The unconstrained head (0) lowers the u
+    error of level 4 without it and keeps h; the APVM head (1, the shipped
+    form: a learned non-negative APVM weight) is no worse than level 4
+    without it.  The plain level-5 run, scored the same way, is more
+    accurate than plain level 4 (the comparison itself is sound)."""
     from tmcore_gb300 import closure
 
     X, Y = closure.training_data(fine_level=6, coarse_level=4, runs=8, days=2.0, samples_per_run=16)
-    net, losses, _ = closure.train(X, Y, steps=1500, dt=closure.level_dt(4))
-    assert np.mean(losses[-20:]) < 0.9 * losses[0]
-    r = closure.evaluate(net, fine_level=6, coarse_level=4, members=8, days=1.0, samples=1)
-    e = {k: (v["h"][0], v["u"][0]) for k, v in r["error"].items()}
-    assert not r["closure_timed_out"]
-    for k in ("closure", "closure_stage1"):
-        assert e[k][1] < 0.99 * e["plain"][1], e
-        assert e[k][0] < 1.002 * e["plain"][0], e
-    assert e["plain_finer"][0] < e["plain"][0] and e["plain_finer"][1] < e["plain"][1]
-    net.close()
+    for head in (0, 1):
+        net, losses, _ = closure.train(X, Y, steps=1500, head=head, dt=closure.level_dt(4))
+        assert np.mean(losses[-20:]) < 0.9 * losses[0]
+        r = closure.evaluate(net, fine_level=6, coarse_level=4, members=8, days=1.0, samples=1, apvm_weight=0.0)
+        e = {k: (v["h"][0], v["u"][0]) for k, v in r["error"].items()}
+        assert not r["closure_timed_out"]
+        for k in ("closure", "closure_stage1"):
+            if head == 0:
+                assert e[k][1] < 0.99 * e["plain"][1], e
+                assert e[k][0] < 1.002 * e["plain"][0], e
+            else:
+                assert e[k][1] <= 1.001 * e["plain"][1], e
+                assert e[k][0] <= 1.001 * e["plain"][0], e
+        assert e["plain_finer"][0] < e["plain"][0] and e["plain_finer"][1] < e["plain"][1]
+        net.close()
 
 
 # ---------------------------------------------------------------------------

@@ -17,6 +17,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import sys
 import time
 
 import numpy as np
@@ -125,52 +126,77 @@ def _member_states(model, members):
 
 
 def evaluate(net, fine_level=7, coarse_level=5, members=8, days=5.0, samples=5, seed0=10_000, device=0,
-             log=None):
+             log=None, truth="fp64", apvm_weight=0.5):
     """Held-out comparison of the learned coarse run with the plain method.
 
-    For `members` seeds not used in training, the FP64 run on the fine mesh,
-    coarse-grained onto the coarse mesh, is the truth.  Four FP32 ensembles
-    start from the coarse-grained initial state: the coarse mesh with the
-    closure in every stage ("closure"), the same with the closure run in stage
-    1 and its output held for the other stages ("closure_stage1"), the coarse
-    mesh without it ("plain"), and the plain method one level finer
-    ("plain_finer", coarse-grained onto the coarse mesh for scoring).  At `samples` evenly
-    spaced times each gets the member-mean relative L2 error of h (area
-    weighted) and of u (dvEdge dcEdge weighted); each gets its device time per
-    simulated day (CUDA events around its steps, all members).
+    For `members` seeds not used in training, the run on the fine mesh,
+    coarse-grained onto the coarse mesh, is the truth: FP64 runs one member at
+    a time (truth="fp64"), or one FP32 ensemble of all members (truth="fp32",
+    member-innermost when members is a multiple of 16; its difference from
+    FP64 is far below the coarse runs' errors).  FP32 ensembles start from the
+    coarse-grained initial state: the coarse mesh with the closure in every
+    stage ("closure"), the same with the closure run in stage 1 and its output
+    held for the other stages ("closure_stage1"), the coarse mesh without it
+    ("plain"), the coarse mesh with the reference's APVM at a fixed weight
+    ("apvm", pv_scheme 1 with `apvm_weight`; omitted when 0), and the plain
+    method one level finer ("plain_finer", coarse-grained onto the coarse mesh
+    for scoring).  At `samples` evenly spaced times each gets the member-mean
+    relative L2 error of h (area weighted) and of u (dvEdge dcEdge weighted);
+    each gets its device time per simulated day (CUDA events around its
+    steps, all members).
     """
     fine, coarse, mid = icos_mesh(fine_level), icos_mesh(coarse_level), icos_mesh(coarse_level + 1)
     kw = dict(pv_scheme=1, apvm_weight=0.0, adv_order=2, conserve_energy=1, renumber=1, device=device)
+    lay = dict(member_layout=1) if members % 16 == 0 else {}
     cg_c, cg_m = Coarsener(fine, coarse, device=device), Coarsener(fine, mid, device=device)
     cg_mc = Coarsener(mid, coarse, device=device)
     dt_f, dt_c, dt_m = level_dt(fine_level), level_dt(coarse_level), level_dt(coarse_level + 1)
     total = days * DAY
     n_f = int(round(total / samples / dt_f))
     n_c, n_m = int(round(total / samples / dt_c)), int(round(total / samples / dt_m))
+    ens = dict(members=members, precision=abi.TMC_FP32, diag_every=0, **lay)
     runs = {
-        "closure": TMCoreGPU(coarse, members=members, dt=dt_c, precision=abi.TMC_FP32, diag_every=0, **kw),
-        "closure_stage1": TMCoreGPU(coarse, members=members, dt=dt_c, precision=abi.TMC_FP32, diag_every=0, **kw),
-        "plain": TMCoreGPU(coarse, members=members, dt=dt_c, precision=abi.TMC_FP32, diag_every=0, **kw),
-        "plain_finer": TMCoreGPU(mid, members=members, dt=dt_m, precision=abi.TMC_FP32, diag_every=0, **kw),
+        "closure": TMCoreGPU(coarse, dt=dt_c, **ens, **kw),
+        "closure_stage1": TMCoreGPU(coarse, dt=dt_c, **ens, **kw),
+        "plain": TMCoreGPU(coarse, dt=dt_c, **ens, **kw),
     }
-    truth = []  # per member: list of (gd, u) on the coarse mesh at the sample times
+    if apvm_weight > 0:
+        runs["apvm"] = TMCoreGPU(coarse, dt=dt_c, **ens, **dict(kw, apvm_weight=apvm_weight))
+    runs["plain_finer"] = TMCoreGPU(mid, dt=dt_m, **ens, **kw)
+    ref = [[None] * samples for _ in range(members)]  # per member: truth (gd, u) on the coarse mesh per sample
+    fine_ics = []
     for k in range(members):
         gd, u, ghs = cases.jet_bumps(fine, seed=seed0 + k)
-        for name, cg in (("closure", cg_c), ("closure_stage1", cg_c), ("plain", cg_c), ("plain_finer", cg_m)):
+        fine_ics.append((gd, u, ghs))
+        for name, r in runs.items():
+            cg = cg_m if name == "plain_finer" else cg_c
             gd0, u0, _ = cg(gd=gd, u=u)
             ghs0, _, _ = cg(gd=ghs)
-            runs[name].select_member(k)
-            runs[name].set_initial(gd0, u0, ghs0)
-        fm = TMCoreGPU(fine, dt=dt_f, precision=abi.TMC_FP64, diag_every=0, **kw)
-        fm.set_initial(gd, u, ghs)
-        tk = []
+            r.select_member(k)
+            r.set_initial(gd0, u0, ghs0)
+    truth_is_fp64 = truth == "fp64"
+    if truth_is_fp64:
+        for k, (gd, u, ghs) in enumerate(fine_ics):
+            fm = TMCoreGPU(fine, dt=dt_f, precision=abi.TMC_FP64, diag_every=0, **kw)
+            fm.set_initial(gd, u, ghs)
+            for s in range(samples):
+                fm.step(n_f)
+                gdf, _, uf = fm.get_state()
+                ref[k][s] = cg_c(gd=gdf, u=uf)[:2]
+            fm.close()
+    else:
+        fm = TMCoreGPU(fine, dt=dt_f, **ens, **kw)
+        for k, (gd, u, ghs) in enumerate(fine_ics):
+            fm.select_member(k)
+            fm.set_initial(gd, u, ghs)
         for s in range(samples):
             fm.step(n_f)
-            gdf, _, uf = fm.get_state()
-            g_c, u_c, _ = cg_c(gd=gdf, u=uf)
-            tk.append((g_c, u_c))
+            for k in range(members):
+                fm.select_member(k)
+                gdf, _, uf = fm.get_state()
+                ref[k][s] = cg_c(gd=gdf, u=uf)[:2]
         fm.close()
-        truth.append(tk)
+    fine_ics = None
     runs["closure"].set_closure(net)
     runs["closure_stage1"].set_closure(net)
     runs["closure_stage1"].set_closure_stages(False)
@@ -185,8 +211,8 @@ def evaluate(net, fine_level=7, coarse_level=5, members=8, days=5.0, samples=5, 
             st = _member_states(r, members)
             if name == "plain_finer":
                 st = [cg_mc(gd=gd, u=u)[:2] for gd, u in st]
-            eh = np.mean([_rel_l2(st[k][0], truth[k][s][0], wa) for k in range(members)])
-            eu = np.mean([_rel_l2(st[k][1], truth[k][s][1], we) for k in range(members)])
+            eh = np.mean([_rel_l2(st[k][0], ref[k][s][0], wa) for k in range(members)])
+            eu = np.mean([_rel_l2(st[k][1], ref[k][s][1], we) for k in range(members)])
             err[name]["h"].append(float(eh))
             err[name]["u"].append(float(eu))
         if log:
@@ -199,6 +225,7 @@ def evaluate(net, fine_level=7, coarse_level=5, members=8, days=5.0, samples=5, 
         c.close()
     return {
         "fine_level": fine_level, "coarse_level": coarse_level, "members": members, "days": days,
+        "truth": "FP64 runs" if truth_is_fp64 else "FP32 ensemble", "apvm_weight": apvm_weight,
         "times_days": [(s + 1) * total / samples / DAY for s in range(samples)],
         "error": err,
         "device_s_per_day": {n: ms[n] / 1e3 / days for n in runs},
@@ -267,6 +294,11 @@ def main():
                     help="run the network in every stage (default: stage 1, its output held for stages 2-4)")
     ap.add_argument("--eval-members", type=int, default=16, help="held-out seeds of the comparison (0: skip)")
     ap.add_argument("--eval-days", type=float, default=5.0)
+    ap.add_argument("--eval-samples", type=int, default=5, help="scoring times of the comparison")
+    ap.add_argument("--truth", choices=("fp64", "fp32"), default="fp64",
+                    help="the comparison's fine-mesh truth: FP64 runs, or one FP32 ensemble")
+    ap.add_argument("--apvm-weight", type=float, default=0.5,
+                    help="the comparison's fixed-weight APVM baseline (0: none)")
     ap.add_argument("--out", default=None, help="save the trained network (.npz)")
     ap.add_argument("--trainer", choices=("tc", "cuda"), default="tc",
                     help="gradients on the tensor cores (tc) or on the CUDA cores in FP32 (cuda)")
@@ -278,7 +310,8 @@ def main():
     net, losses, t_data, t_train, n_samples = None, None, 0.0, 0.0, 0
     if not a.plain_ensemble:
         t0 = time.time()
-        X, Y = training_data(a.fine_level, a.coarse_level, a.runs, a.days, a.samples)
+        X, Y = training_data(a.fine_level, a.coarse_level, a.runs, a.days, a.samples,
+                             log=lambda t: print(t, file=sys.stderr, flush=True))
         t_data = time.time() - t0
         n_samples = int(len(Y))
         t0 = time.time()
@@ -291,7 +324,7 @@ def main():
     coarse = icos_mesh(a.coarse_level)
     dt = level_dt(a.coarse_level)
     ens = TMCoreGPU(coarse, members=a.members, dt=dt, precision=abi.TMC_FP32, pv_scheme=1, apvm_weight=0.0,
-                    diag_every=0)
+                    diag_every=0, member_layout=1 if a.members % 16 == 0 else 0)
     for m in range(a.members):
         gd, u, ghs = cases.jet_bumps(coarse, seed=10_000 + m)
         ens.select_member(m)
@@ -311,7 +344,9 @@ def main():
              "median_kept": float(np.median(mon.max_drift[kept])) if kept.any() else None,
              "max_all": float(mon.max_drift.max())}
     ens.close()
-    comparison = (evaluate(net, a.fine_level, a.coarse_level, members=a.eval_members, days=a.eval_days)
+    comparison = (evaluate(net, a.fine_level, a.coarse_level, members=a.eval_members, days=a.eval_days,
+                           samples=a.eval_samples, truth=a.truth, apvm_weight=a.apvm_weight,
+                           log=lambda t: print(t, file=sys.stderr, flush=True))
                   if a.eval_members > 0 and net is not None else None)
     print(json.dumps({
         "training_samples": n_samples, "data_s": t_data, "train_s": t_train,

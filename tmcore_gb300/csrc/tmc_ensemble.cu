@@ -859,28 +859,60 @@ struct RegionList {
   int count[R_COUNT];
 };
 
-__global__ void __launch_bounds__(256) k_ens_reduce(Partials P, RegionList RL, double* diag_out) {
+// One block per (region, group of 32 members), 32 warps: warp w takes slots
+// w, w + 32, ... in rounds of four with four independent accumulators (all
+// four loads in flight), which it combines in a fixed order; the warps'
+// sums are then combined in warp order.  Deterministic for a given slot
+// count.  (With 8 warps and one accumulator the 7,680 slots of a level-7
+// edge region took about 0.3 ms, a quarter of a 16-member step.)
+constexpr int kRedThreads = 1024;
+__global__ void __launch_bounds__(kRedThreads) k_ens_reduce(Partials P, RegionList RL, double* diag_out) {
   const int r = RL.r[blockIdx.x], count = RL.count[blockIdx.x];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const int m = blockIdx.y * 32 + lane;
   const bool in = m < P.M;
-  double hi = 0.0, lo = 0.0;
-  if (r <= R_44_E) {
-    float fh = 0.f, fl = 0.f;
-    for (int s = w; in && s < count; s += nw) two_sum_acc(fh, fl, P.f(r, s)[m]);
-    hi = (double)fh;
-    lo = (double)fl;
-  } else {
-    for (int s = w; in && s < count; s += nw) hi += P.d(r, s)[m];
+  DD acc{0.0, 0.0};
+  if (in) {
+    if (r <= R_44_E) {
+      float fh[4] = {0.f, 0.f, 0.f, 0.f}, fl[4] = {0.f, 0.f, 0.f, 0.f};
+      int s = w;
+      for (; s + 3 * nw < count; s += 4 * nw) {
+        float v[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) v[q] = P.f(r, s + q * nw)[m];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) two_sum_acc(fh[q], fl[q], v[q]);
+      }
+#pragma unroll
+      for (int q = 0; q < 3; ++q)  // the last at most 3 slots of this warp
+        if (s + q * nw < count) two_sum_acc(fh[q], fl[q], P.f(r, s + q * nw)[m]);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) acc = dd_add(acc, DD{(double)fh[q], (double)fl[q]});
+    } else {
+      double dh[4] = {0.0, 0.0, 0.0, 0.0};
+      int s = w;
+      for (; s + 3 * nw < count; s += 4 * nw) {
+        double v[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) v[q] = P.d(r, s + q * nw)[m];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) dh[q] += v[q];
+      }
+#pragma unroll
+      for (int q = 0; q < 3; ++q)
+        if (s + q * nw < count) dh[q] += P.d(r, s + q * nw)[m];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) acc = dd_add(acc, DD{dh[q], 0.0});
+    }
   }
-  __shared__ double sh[8][32], sl[8][32];
-  sh[w][lane] = hi;
-  sl[w][lane] = lo;
+  __shared__ double sh[kRedThreads / 32][32], sl[kRedThreads / 32][32];
+  sh[w][lane] = acc.hi;
+  sl[w][lane] = acc.lo;
   __syncthreads();
   if (w != 0 || !in) return;
-  DD acc{0.0, 0.0};
-  for (int k = 0; k < nw; ++k) acc = dd_add(acc, DD{sh[k][lane], sl[k][lane]});
-  diag_out[(size_t)m * kDiagStride + kDiagLen + r] = acc.hi + acc.lo;
+  DD tot{0.0, 0.0};
+  for (int k = 0; k < nw; ++k) tot = dd_add(tot, DD{sh[k][lane], sl[k][lane]});
+  diag_out[(size_t)m * kDiagStride + kDiagLen + r] = tot.hi + tot.lo;
 }
 
 // beta (time_scheme_mod.F90:144-150) and the invariants (tmcore_swm_mod.F90:215-255)
@@ -1080,7 +1112,7 @@ void launch_finalize(const Dims& D, const Partials& P, bool step, bool diag, boo
     add(R_AV, D.slots_v);
   }
   if (RL.n == 0) return;
-  k_ens_reduce<<<dim3(RL.n, D.G), 256, 0, st>>>(P, RL, diag_out);
+  k_ens_reduce<<<dim3(RL.n, D.G), kRedThreads, 0, st>>>(P, RL, diag_out);
   k_ens_beta<<<nb(D.M), 256, 0, st>>>(D.M, step ? 1 : 0, diag ? 1 : 0, conserve ? 1 : 0, totalArea,
                                       sumAreaTriangle, dt, diag_out);
 }
