@@ -329,16 +329,26 @@ def run_mixed(args, local, ics_by_level, peak):
         grp.synchronize()
         el = time.perf_counter() - t
         grp.close()
-        for e in models:
+        # each level alone: its steps of one cycle (CUDA events) and its passes
+        alone = {}
+        for L, e in zip(sorted(ics_by_level), models):
+            n = 2 ** (L - 4)  # steps per 1200-s cycle
+            ms, _, _, _ = e.time_steps(2 * n, total=True, flux=False)
+            alone[f"L{L}"] = {"ms_per_cycle": ms / 2, "passes_ms": e.pass_times(2)}
             e.close()
-        res[layout] = (el / cycles, members, desc, bytes_cycle)
-    lay = min(res, key=lambda k: res[k][0])  # the faster layout (16 members per level: close)
-    cyc_s, members, desc, bytes_cycle = res[lay]
+        res[layout] = (el / cycles, members, desc, bytes_cycle, alone)
+    lay = min(res, key=lambda k: res[k][0])  # the faster layout
+    cyc_s, members, desc, bytes_cycle, alone = res[lay]
+    pm = sum(2 ** (L - 4) * inner_ensemble_step_bytes(10 * 4 ** L + 2, 30 * 4 ** L,
+                                                                              20 * 4 ** L, len(ics))
+             for L, ics in ics_by_level.items())
     out = {"workload": "mixed batch " + ", ".join(desc) + ", one CUDA graph per 1200-s cycle",
            "member_layout": lay, "members": members, "cycles": args.mixed_cycles, "ms_per_cycle": cyc_s * 1e3,
            "member_days_per_s": members * 1200.0 / DAY / cyc_s, "sim_days_per_s": 1200.0 / DAY / cyc_s,
            "scope_model_bytes_per_cycle": bytes_cycle, "achieved_gbs": bytes_cycle / cyc_s / 1e9,
-           "frac": bytes_cycle / cyc_s / 1e9 / peak, "timing": "host wall clock around tmc_group_run + sync"}
+           "frac": bytes_cycle / cyc_s / 1e9 / peak, "pass_model_bytes_per_cycle": pm,
+           "pass_model_frac": pm / cyc_s / 1e9 / peak, "levels_alone": alone,
+           "timing": "host wall clock around tmc_group_run + sync; levels alone: CUDA events"}
     for other in res:
         if other != lay:
             c0 = res[other][0]

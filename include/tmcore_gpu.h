@@ -221,8 +221,11 @@ int tmc_mlp_set_train_mode(tmc_mlp* n, int32_t tensor_cores);
  *     non-negative per-edge weight softplus(y) in place of apvm_weight; the
  *     direction comes from the edge's raw features (1, 22, 0, 23), dt is the
  *     model time step (> 0).  The correction keeps APVM's sign, so it can only
- *     remove potential enstrophy as APVM does; inside the energy-conserving
- *     q.F_perp form it leaves mass and energy unchanged. */
+ *     remove potential enstrophy as APVM does.
+ *   head 2: y * y_scale on the edges where y v (q_v2 - q_v1) <= 0 (APVM's
+ *     sign along the edge: the correction removes potential enstrophy
+ *     through q.F_perp there), 0 elsewhere; dt is not used.
+ * Inside the energy-conserving q.F_perp form no head changes mass or energy. */
 int tmc_mlp_set_head(tmc_mlp* n, int32_t head, double dt);
 /* No counterpart in the reference (its errors abort, time_scheme_mod.F90:60).
  * Poll limit of the tensor-core kernels' completion waits (mbarrier polls

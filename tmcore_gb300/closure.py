@@ -160,8 +160,8 @@ def evaluate(net, fine_level=7, coarse_level=5, members=8, days=5.0, samples=5, 
         "closure_stage1": TMCoreGPU(coarse, dt=dt_c, **ens, **kw),
         "plain": TMCoreGPU(coarse, dt=dt_c, **ens, **kw),
     }
-    if apvm_weight > 0:
-        runs["apvm"] = TMCoreGPU(coarse, dt=dt_c, **ens, **dict(kw, apvm_weight=apvm_weight))
+    if apvm_weight > 0:  # APVM runs in the member-outermost layout
+        runs["apvm"] = TMCoreGPU(coarse, dt=dt_c, **dict(ens, member_layout=0), **dict(kw, apvm_weight=apvm_weight))
     runs["plain_finer"] = TMCoreGPU(mid, dt=dt_m, **ens, **kw)
     ref = [[None] * samples for _ in range(members)]  # per member: truth (gd, u) on the coarse mesh per sample
     fine_ics = []
@@ -302,8 +302,9 @@ def main():
     ap.add_argument("--out", default=None, help="save the trained network (.npz)")
     ap.add_argument("--trainer", choices=("tc", "cuda"), default="tc",
                     help="gradients on the tensor cores (tc) or on the CUDA cores in FP32 (cuda)")
-    ap.add_argument("--head", type=int, choices=(0, 1), default=1,
-                    help="1: a learned non-negative APVM weight (enstrophy-dissipating); 0: the residual itself")
+    ap.add_argument("--head", type=int, choices=(0, 1, 2), default=1,
+                    help="1: a learned non-negative APVM weight; 2: the residual where it has APVM's sign "
+                         "(both enstrophy-dissipating); 0: the residual itself")
     ap.add_argument("--plain-ensemble", action="store_true",
                     help="no training: the held-out ensemble without the network, under the same drift monitor")
     a = ap.parse_args()

@@ -680,8 +680,7 @@ struct EnsEngine : EngineBase {
     const size_t nc = h->M.nc * M_, ne = h->M.ne * M_, nv = h->M.nv * M_;
     D.M = h->members;
     D.G = (h->members + 31) / 32;
-    D.V = h->members % 64 == 0 ? 2 : 1;
-    D.LPE = h->members % 32 == 0 ? 32 : 16;
+    ens::lanes_for(h->members, &D.V, &D.LPE);
     D.slots_c = ens::slots_for(h->M.nc);
     D.slots_e = ens::slots_for(h->M.ne);
     D.slots_v = ens::slots_for(h->M.nv);

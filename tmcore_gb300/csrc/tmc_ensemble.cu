@@ -125,7 +125,13 @@ __device__ __forceinline__ void ldv(const float* p, size_t i, float (&o)[V]) {
 }
 template <int V>
 __device__ __forceinline__ void ldv(const double* p, size_t i, double (&o)[V]) {
-  if constexpr (V == 2) {
+  if constexpr (V == 4) {
+    const double2 a = *reinterpret_cast<const double2*>(p + i), b = *reinterpret_cast<const double2*>(p + i + 2);
+    o[0] = a.x;
+    o[1] = a.y;
+    o[2] = b.x;
+    o[3] = b.y;
+  } else if constexpr (V == 2) {
     const double2 t = *reinterpret_cast<const double2*>(p + i);
     o[0] = t.x;
     o[1] = t.y;
@@ -144,7 +150,10 @@ __device__ __forceinline__ void stv(float* p, size_t i, const float (&v)[V]) {
 }
 template <int V>
 __device__ __forceinline__ void stv(double* p, size_t i, const double (&v)[V]) {
-  if constexpr (V == 2)
+  if constexpr (V == 4) {
+    *reinterpret_cast<double2*>(p + i) = make_double2(v[0], v[1]);
+    *reinterpret_cast<double2*>(p + i + 2) = make_double2(v[2], v[3]);
+  } else if constexpr (V == 2)
     *reinterpret_cast<double2*>(p + i) = make_double2(v[0], v[1]);
   else
     p[i] = v[0];
@@ -169,20 +178,22 @@ __device__ __forceinline__ void stff(float* p, size_t i, size_t ffs, const FF (&
 
 // This thread's members and elements.  One block = one member group
 // (blockIdx.y) and kEnsEPB consecutive elements (blockIdx.x).  A warp covers
-// 32 / LPE elements at a time, LPE lanes each (LPE = 16 when the member
-// count is not a multiple of 32): its warps take elements j0, j0 + js, ...
+// 32 / LPE elements at a time, LPE lanes each (LPE = 32, 16, 8 or 4; see
+// Dims): its warps take elements j0, j0 + js, ...
 struct Lane {
   int m0;      // first member of the lane
   size_t M;    // member stride
   int j0, js;  // first element and element stride of the thread
   int slot, nslot;  // this thread's row of a block reduction, and the rows
   int ml;      // member lane (0 .. LPE-1)
+  int lpe;     // lanes per element
 };
 template <int V>
 __device__ __forceinline__ Lane lane_of(const Dims& D) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, W = blockDim.x >> 5;
   const int epw = 32 / D.LPE, sub = lane / D.LPE, ml = lane % D.LPE;
-  return Lane{(int)((blockIdx.y * D.LPE + ml) * V), (size_t)D.M, w * epw + sub, W * epw, w * epw + sub, W * epw, ml};
+  return Lane{(int)((blockIdx.y * D.LPE + ml) * V), (size_t)D.M, w * epw + sub, W * epw, w * epw + sub, W * epw, ml,
+              D.LPE};
 }
 
 inline dim3 grid_of(int n, const Dims& D, int bs, int* threads) {
@@ -194,17 +205,18 @@ inline dim3 grid_of(int n, const Dims& D, int bs, int* threads) {
 }
 
 // Per-member partial sums of one block: the rows (warps and the element
-// halves of a warp) of each member are combined in a fixed order (FP32
-// TwoSum, or FP64) and row 0 stores them.  Every thread of the block calls
-// these (they synchronise).
-constexpr int kRows = 2 * kMaxBS / 32;
+// groups of a warp) of each member are combined in a fixed order (FP32
+// TwoSum, or FP64) and row 0 stores them.  Entry (row, member lane) sits at
+// row * LPE + lane: rows x LPE = the block's threads.  Every thread of the
+// block calls these (they synchronise).
 template <int N, int V>
 __device__ __forceinline__ void block_partials_f(const Lane& L, const float (&v)[N][V], float* const (&dst)[N]) {
-  __shared__ float sh[N][V][kRows][32];
+  __shared__ float sh[N][V][kMaxBS];
+  const int at = L.slot * L.lpe + L.ml;
 #pragma unroll
   for (int k = 0; k < N; ++k)
 #pragma unroll
-    for (int c = 0; c < V; ++c) sh[k][c][L.slot][L.ml] = v[k][c];
+    for (int c = 0; c < V; ++c) sh[k][c][at] = v[k][c];
   __syncthreads();
   if (L.slot == 0) {
 #pragma unroll
@@ -214,7 +226,7 @@ __device__ __forceinline__ void block_partials_f(const Lane& L, const float (&v)
 #pragma unroll
       for (int c = 0; c < V; ++c) {
         float hi = 0.f, lo = 0.f;
-        for (int q = 0; q < L.nslot; ++q) two_sum_acc(hi, lo, sh[k][c][q][L.ml]);
+        for (int q = 0; q < L.nslot; ++q) two_sum_acc(hi, lo, sh[k][c][q * L.lpe + L.ml]);
         o[c] = hi + lo;
       }
       stv<V>(dst[k], (size_t)L.m0, o);
@@ -224,11 +236,12 @@ __device__ __forceinline__ void block_partials_f(const Lane& L, const float (&v)
 }
 template <int N, int V>
 __device__ __forceinline__ void block_partials_d(const Lane& L, const double (&v)[N][V], double* const (&dst)[N]) {
-  __shared__ double sh[N][V][kRows][32];
+  __shared__ double sh[N][V][kMaxBS];
+  const int at = L.slot * L.lpe + L.ml;
 #pragma unroll
   for (int k = 0; k < N; ++k)
 #pragma unroll
-    for (int c = 0; c < V; ++c) sh[k][c][L.slot][L.ml] = v[k][c];
+    for (int c = 0; c < V; ++c) sh[k][c][at] = v[k][c];
   __syncthreads();
   if (L.slot == 0) {
 #pragma unroll
@@ -237,7 +250,7 @@ __device__ __forceinline__ void block_partials_d(const Lane& L, const double (&v
 #pragma unroll
       for (int c = 0; c < V; ++c) {
         double a = 0.0;
-        for (int q = 0; q < L.nslot; ++q) a += sh[k][c][q][L.ml];
+        for (int q = 0; q < L.nslot; ++q) a += sh[k][c][q * L.lpe + L.ml];
         o[c] = a;
       }
       stv<V>(dst[k], (size_t)L.m0, o);

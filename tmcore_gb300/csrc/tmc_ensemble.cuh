@@ -40,10 +40,20 @@ constexpr int kEnsEPB = TMC_ENS_EPB;  // elements per block (and per partial-sum
 struct Dims {
   int M;    // members (a multiple of 16)
   int G;    // groups of 32 members for the reductions (the last may be partial)
-  int V;    // members per lane: 2 when M is a multiple of 64, else 1
-  int LPE;  // lanes per element: 32, or 16 when M is not a multiple of 32
+  int V;    // members per lane (lanes_for)
+  int LPE;  // lanes per element (lanes_for)
   int slots_c, slots_e, slots_v;  // partial slots: blocks along cells, edges, vertices
 };
+
+// Members per lane and lanes per element for M members (M a multiple of 16):
+// 2 and 32 when M is a multiple of 64, else 1 and 32 (M a multiple of 32) or
+// 16.  Four members per lane (16-byte loads, 4 or 8 lanes per element) made
+// a 16-member level-7 step 2.4x slower (2.87 against 1.20 ms): a warp then
+// gathers from 8 elements at once.
+inline void lanes_for(int M, int* V, int* LPE) {
+  *V = M % 64 == 0 ? 2 : 1;
+  *LPE = M % 32 == 0 ? 32 : 16;
+}
 
 __host__ __device__ inline int slots_for(int n) { return (n + kEnsEPB - 1) / kEnsEPB; }
 

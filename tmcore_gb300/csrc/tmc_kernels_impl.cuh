@@ -724,8 +724,12 @@ __global__ void __launch_bounds__(kMaxBlock) k_edge_pv(DevMesh M, ModelOpt O, St
 // slots are the edge itself with weight 0) and the stencil points up to the
 // width with the side's count as a predicate, so an edge's ~35 gathers are in
 // flight together instead of a count-dependent chain.  Sums in stencil order.
+// Resident 256-thread blocks per SM the kernel is compiled for.  It is
+// latency bound (two dependent loads per stencil point): at level 8 the pass
+// takes 0.295 ms with 2 (128 registers), 0.183 ms with 3 (80) and 0.171 ms
+// with 4 (64 registers, about 100 bytes spilled to L1).
 #ifndef TMC_UP32_MINB
-#define TMC_UP32_MINB 2  // resident 256-thread blocks per SM the kernel is compiled for (128 registers)
+#define TMC_UP32_MINB 4
 #endif
 template <bool kB>
 __global__ void __launch_bounds__(256, TMC_UP32_MINB) k_edge_pv_up32(DevMesh M, ModelOpt O, StageIO<float> S0) {

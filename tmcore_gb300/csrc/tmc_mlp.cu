@@ -751,7 +751,8 @@ static int train_status(tmc_mlp* n, const char* where) {
 
 int tmc_mlp_set_head(tmc_mlp* n, int32_t head, double dt) {
   if (!n) return TMC_E_ARG;
-  if (head != kHeadPlain && head != kHeadApvm) return n->fail(TMC_E_ARG, "tmc_mlp_set_head: head must be 0 or 1");
+  if (head != kHeadPlain && head != kHeadApvm && head != kHeadSign)
+    return n->fail(TMC_E_ARG, "tmc_mlp_set_head: head must be 0, 1 or 2");
   if (head == kHeadApvm && !(dt > 0.0)) return n->fail(TMC_E_ARG, "tmc_mlp_set_head: the APVM head needs dt > 0");
   n->head = head;
   n->head_dt = head == kHeadApvm ? (float)dt : 0.f;

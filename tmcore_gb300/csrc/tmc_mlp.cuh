@@ -56,9 +56,14 @@ struct Net {
   const float* xinv;          // [kIn]
   float yscale;               // output scale
   int wait_polls;             // poll limit of each tensor-core completion wait (kWaitPolls)
-  int head;                   // kHeadPlain or kHeadApvm
+  int head;                   // kHeadPlain, kHeadApvm or kHeadSign
   float head_dt;              // kHeadApvm: the model time step (s)
 };
+
+// Poll limit of a tensor-core completion wait (mbarrier try_wait loop).  A
+// wait that runs out flags an error; the wait that then drains the
+// outstanding MMAs before the tensor memory is freed always uses this limit.
+constexpr int kWaitPolls = 1 << 20;
 
 // Output heads: how the network's raw output y of an edge becomes the
 // correction added to pv_edge (and the prediction the training loss fits).
@@ -68,37 +73,45 @@ struct Net {
 //               operators_mod.F90:296-316 with a learned non-negative
 //               per-edge weight softplus(y) in place of apvm_weight.  The
 //               correction lies along APVM's upwinding direction with APVM's
-//               sign, so like APVM it can only remove potential enstrophy;
-//               inside the energy-conserving q.F_perp form it changes
-//               neither mass nor energy.
-constexpr int kHeadPlain = 0, kHeadApvm = 1;
+//               sign, so like APVM it can only remove potential enstrophy.
+//   kHeadSign   y * yscale where it has APVM's sign along the edge, i.e.
+//               where y v (q_v2 - q_v1) <= 0, else 0: the unconstrained
+//               correction restricted to the edges where it removes potential
+//               enstrophy through q.F_perp (the correction times the edge's
+//               tangential PV flux difference is never positive).
+// Inside the energy-conserving q.F_perp form no head changes mass or energy.
+constexpr int kHeadPlain = 0, kHeadApvm = 1, kHeadSign = 2;
 
-// the APVM direction dt (v dq/dt + u dq/dn) of an edge from its raw closure
-// features (1: v, 22: pv gradient along the edge, 0: u, 23: across it)
+// The head's auxiliary value of an edge from its raw closure features (1: v,
+// 22: pv gradient along the edge, 0: u, 23: across it): kHeadApvm the APVM
+// direction dt (v dq/dt + u dq/dn); kHeadSign v dq/dt.
 __device__ __forceinline__ float head_dir(const Net& net, const float (&x)[kIn]) {
-  return net.head == kHeadApvm ? net.head_dt * (x[1] * x[22] + x[0] * x[23]) : 0.f;
+  if (net.head == kHeadApvm) return net.head_dt * (x[1] * x[22] + x[0] * x[23]);
+  if (net.head == kHeadSign) return x[1] * x[22];
+  return 0.f;
 }
 __device__ __forceinline__ float softplus_f(float y) { return y > 20.f ? y : log1pf(__expf(y)); }
 // the correction from the raw output y (units of pv_edge)
 __device__ __forceinline__ float head_out(const Net& net, float y, float dir) {
-  return net.head == kHeadApvm ? -softplus_f(y) * dir : y * net.yscale;
+  if (net.head == kHeadApvm) return -softplus_f(y) * dir;
+  if (net.head == kHeadSign) return y * dir <= 0.f ? y * net.yscale : 0.f;
+  return y * net.yscale;
 }
 // the prediction in units of yscale and its derivative with respect to y
 // (the training loss is the mean of (prediction - target / yscale)^2)
 __device__ __forceinline__ float head_pred(const Net& net, float y, float dir, float& dpred) {
-  if (net.head != kHeadApvm) {
-    dpred = 1.f;
-    return y;
+  if (net.head == kHeadApvm) {
+    const float inv = 1.f / net.yscale;
+    dpred = -dir * inv / (1.f + __expf(-y));
+    return -softplus_f(y) * dir * inv;
   }
-  const float inv = 1.f / net.yscale;
-  dpred = -dir * inv / (1.f + __expf(-y));
-  return -softplus_f(y) * dir * inv;
+  if (net.head == kHeadSign && y * dir > 0.f) {
+    dpred = 0.f;
+    return 0.f;
+  }
+  dpred = 1.f;
+  return y;
 }
-
-// Poll limit of a tensor-core completion wait (mbarrier try_wait loop).  A
-// wait that runs out flags an error; the wait that then drains the
-// outstanding MMAs before the tensor memory is freed always uses this limit.
-constexpr int kWaitPolls = 1 << 20;
 
 __device__ __forceinline__ float gelu_tanh(float x, float t) { return 0.5f * x * (1.f + t); }
 __device__ __forceinline__ float gelu_arg(float x) { return 0.7978845608028654f * (x + 0.044715f * x * x * x); }

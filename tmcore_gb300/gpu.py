@@ -385,7 +385,8 @@ class ClosureMLP:
 
     def set_head(self, head: int, dt: float = 0.0):
         """Output head: 0 the correction is y * y_scale; 1 it is
-        -softplus(y) dt (v dq/dt + u dq/dn), a learned non-negative APVM weight."""
+        -softplus(y) dt (v dq/dt + u dq/dn), a learned non-negative APVM weight;
+        2 it is y * y_scale where y v dq/dt <= 0 (APVM's sign), else 0."""
         self.head, self.head_dt = int(head), float(dt)
         self._chk(self.lib.tmc_mlp_set_head(self.n, int(head), float(dt)))
 
