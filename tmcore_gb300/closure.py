@@ -71,14 +71,15 @@ def training_data(fine_level=8, coarse_level=6, runs=4, days=1.0, samples_per_ru
     return np.concatenate(X), np.concatenate(Y)
 
 
-def train(X, Y, steps=2000, batch=65536, lr=1e-3, seed=0, device=0, tensor_cores=True, head=1, dt=None):
+def train(X, Y, steps=2000, batch=65536, lr=1e-3, seed=0, device=0, tensor_cores=True, head=2, dt=None):
     """A ClosureMLP fitted to (X, Y), its gradients on the tensor cores (or
     the CUDA cores); returns (net, losses, scaling).
 
-    head 1 (the default) fits a non-negative per-edge APVM weight: the
-    correction is -softplus(y) dt (v dq/dt + u dq/dn) with dt the coarse
-    model's time step, so it can only dissipate potential enstrophy; head 0
-    fits the residual itself, unconstrained."""
+    head 2 (the default) fits the residual where the correction has APVM's
+    sign along the edge (it removes potential enstrophy through q.F_perp
+    there) and applies nothing elsewhere; head 1 fits a non-negative per-edge
+    APVM weight (the correction is -softplus(y) dt (v dq/dt + u dq/dn), dt the
+    coarse model's time step); head 0 fits the residual itself, unconstrained."""
     if head == 1 and not dt:
         raise ValueError("the APVM head needs the coarse model's time step dt")
     rng = np.random.default_rng(seed)
@@ -129,6 +130,9 @@ def evaluate(net, fine_level=7, coarse_level=5, members=8, days=5.0, samples=5, 
              log=None, truth="fp64", apvm_weight=0.5):
     """Held-out comparison of the learned coarse run with the plain method.
 
+    `net` is a ClosureMLP (runs "closure", every stage, and "closure_stage1",
+    stage 1 held), or a dict {name: ClosureMLP}, each run in stage 1 held.
+
     For `members` seeds not used in training, the run on the fine mesh,
     coarse-grained onto the coarse mesh, is the truth: FP64 runs one member at
     a time (truth="fp64"), or one FP32 ensemble of all members (truth="fp32",
@@ -155,11 +159,9 @@ def evaluate(net, fine_level=7, coarse_level=5, members=8, days=5.0, samples=5, 
     n_f = int(round(total / samples / dt_f))
     n_c, n_m = int(round(total / samples / dt_c)), int(round(total / samples / dt_m))
     ens = dict(members=members, precision=abi.TMC_FP32, diag_every=0, **lay)
-    runs = {
-        "closure": TMCoreGPU(coarse, dt=dt_c, **ens, **kw),
-        "closure_stage1": TMCoreGPU(coarse, dt=dt_c, **ens, **kw),
-        "plain": TMCoreGPU(coarse, dt=dt_c, **ens, **kw),
-    }
+    nets = net if isinstance(net, dict) else {"closure": net, "closure_stage1": net}
+    runs = {name: TMCoreGPU(coarse, dt=dt_c, **ens, **kw) for name in nets}
+    runs["plain"] = TMCoreGPU(coarse, dt=dt_c, **ens, **kw)
     if apvm_weight > 0:  # APVM runs in the member-outermost layout
         runs["apvm"] = TMCoreGPU(coarse, dt=dt_c, **dict(ens, member_layout=0), **dict(kw, apvm_weight=apvm_weight))
     runs["plain_finer"] = TMCoreGPU(mid, dt=dt_m, **ens, **kw)
@@ -197,9 +199,10 @@ def evaluate(net, fine_level=7, coarse_level=5, members=8, days=5.0, samples=5, 
                 ref[k][s] = cg_c(gd=gdf, u=uf)[:2]
         fm.close()
     fine_ics = None
-    runs["closure"].set_closure(net)
-    runs["closure_stage1"].set_closure(net)
-    runs["closure_stage1"].set_closure_stages(False)
+    for name, n in nets.items():
+        runs[name].set_closure(n)
+        # "closure" runs the network in every stage; the others in stage 1, held
+        runs[name].set_closure_stages(name == "closure")
     wa = coarse.vars["areaCell"]
     we = coarse.vars["dvEdge"] * coarse.vars["dcEdge"]
     err = {name: {"h": [], "u": []} for name in runs}
@@ -218,7 +221,7 @@ def evaluate(net, fine_level=7, coarse_level=5, members=8, days=5.0, samples=5, 
         if log:
             log(f"day {(s + 1) * total / samples / DAY:.2f}: " +
                 ", ".join(f"{n} h {err[n]['h'][-1]:.3e} u {err[n]['u'][-1]:.3e}" for n in runs))
-    timed_out = runs["closure"].closure_status() or runs["closure_stage1"].closure_status()
+    timed_out = any(runs[name].closure_status() for name in nets)
     for r in runs.values():
         r.close()
     for c in (cg_c, cg_m, cg_mc):
@@ -299,66 +302,78 @@ def main():
                     help="the comparison's fine-mesh truth: FP64 runs, or one FP32 ensemble")
     ap.add_argument("--apvm-weight", type=float, default=0.5,
                     help="the comparison's fixed-weight APVM baseline (0: none)")
-    ap.add_argument("--out", default=None, help="save the trained network (.npz)")
+    ap.add_argument("--out", default=None, help="save the trained networks (.npz; the head is appended)")
     ap.add_argument("--trainer", choices=("tc", "cuda"), default="tc",
                     help="gradients on the tensor cores (tc) or on the CUDA cores in FP32 (cuda)")
-    ap.add_argument("--head", type=int, choices=(0, 1, 2), default=1,
-                    help="1: a learned non-negative APVM weight; 2: the residual where it has APVM's sign "
-                         "(both enstrophy-dissipating); 0: the residual itself")
+    ap.add_argument("--heads", default="2",
+                    help="output heads to train on the same data, comma separated: 1 a learned non-negative "
+                         "APVM weight, 2 the residual where it has APVM's sign (both enstrophy-dissipating), "
+                         "0 the residual itself")
     ap.add_argument("--plain-ensemble", action="store_true",
-                    help="no training: the held-out ensemble without the network, under the same drift monitor")
+                    help="also run the held-out ensemble without a network, under the same drift monitor")
     a = ap.parse_args()
-    net, losses, t_data, t_train, n_samples = None, None, 0.0, 0.0, 0
-    if not a.plain_ensemble:
+    say = lambda t: print(t, file=sys.stderr, flush=True)  # noqa: E731
+    heads = [int(h) for h in a.heads.split(",") if h != ""]
+    dt = level_dt(a.coarse_level)
+    nets, losses, t_train = {}, {}, {}
+    t_data, n_samples = 0.0, 0
+    if heads:
         t0 = time.time()
-        X, Y = training_data(a.fine_level, a.coarse_level, a.runs, a.days, a.samples,
-                             log=lambda t: print(t, file=sys.stderr, flush=True))
+        X, Y = training_data(a.fine_level, a.coarse_level, a.runs, a.days, a.samples, log=say)
         t_data = time.time() - t0
         n_samples = int(len(Y))
-        t0 = time.time()
-        net, losses, sc = train(X, Y, steps=a.steps, tensor_cores=a.trainer == "tc", head=a.head,
-                                dt=level_dt(a.coarse_level))
-        t_train = time.time() - t0
-        if a.out:
-            save(a.out, net, sc)
-    # held-out ensemble on the coarse mesh with the closure and the fallback
+        for h in heads:
+            t0 = time.time()
+            net, ls, sc = train(X, Y, steps=a.steps, tensor_cores=a.trainer == "tc", head=h, dt=dt)
+            t_train[h] = time.time() - t0
+            nets[h], losses[h] = net, ls
+            if a.out:
+                save(a.out.replace(".npz", "") + f"_head{h}.npz", net, sc)
+            say(f"head {h}: loss {float(ls[0]):.4f} -> {float(np.mean(ls[-20:])):.4f} in {t_train[h]:.1f} s")
+        X = Y = None
+    # held-out ensembles on the coarse mesh with the closure and the fallback
     coarse = icos_mesh(a.coarse_level)
-    dt = level_dt(a.coarse_level)
-    ens = TMCoreGPU(coarse, members=a.members, dt=dt, precision=abi.TMC_FP32, pv_scheme=1, apvm_weight=0.0,
-                    diag_every=0, member_layout=1 if a.members % 16 == 0 else 0)
-    for m in range(a.members):
-        gd, u, ghs = cases.jet_bumps(coarse, seed=10_000 + m)
-        ens.select_member(m)
-        ens.set_initial(gd, u, ghs)
-    if net is not None:
-        ens.set_closure(net)
-        ens.set_closure_stages(a.every_stage)
-    mon = FallbackMonitor(ens, a.members)
-    nsteps = int(round(a.ens_days * DAY / dt))
-    t0 = time.time()
-    mon.step(nsteps)
-    ens.synchronize()
-    t_ens = time.time() - t0
-    fallbacks, timed_out = len(mon.fallbacks), ens.closure_status()
-    kept = mon.on
-    drift = {"max_kept": float(mon.max_drift[kept].max()) if kept.any() else None,
-             "median_kept": float(np.median(mon.max_drift[kept])) if kept.any() else None,
-             "max_all": float(mon.max_drift.max())}
-    ens.close()
-    comparison = (evaluate(net, a.fine_level, a.coarse_level, members=a.eval_members, days=a.eval_days,
-                           samples=a.eval_samples, truth=a.truth, apvm_weight=a.apvm_weight,
-                           log=lambda t: print(t, file=sys.stderr, flush=True))
-                  if a.eval_members > 0 and net is not None else None)
+    ensembles = {}
+    for key, net in ([("plain", None)] if a.plain_ensemble else []) + [(f"head{h}", nets[h]) for h in heads]:
+        ens = TMCoreGPU(coarse, members=a.members, dt=dt, precision=abi.TMC_FP32, pv_scheme=1, apvm_weight=0.0,
+                        diag_every=0, member_layout=1 if a.members % 16 == 0 else 0)
+        for m in range(a.members):
+            gd, u, ghs = cases.jet_bumps(coarse, seed=10_000 + m)
+            ens.select_member(m)
+            ens.set_initial(gd, u, ghs)
+        if net is not None:
+            ens.set_closure(net)
+            ens.set_closure_stages(a.every_stage)
+        mon = FallbackMonitor(ens, a.members)
+        nsteps = int(round(a.ens_days * DAY / dt))
+        t0 = time.time()
+        mon.step(nsteps)
+        ens.synchronize()
+        t_ens = time.time() - t0
+        kept = mon.on
+        ensembles[key] = {
+            "members": a.members, "level": a.coarse_level, "steps": nsteps, "wall_s": t_ens,
+            "member_days_per_s": a.members * nsteps * dt / DAY / t_ens, "closure": net is not None,
+            "every_stage": a.every_stage, "fallbacks": len(mon.fallbacks),
+            "fallback_members": len({m for m, _ in mon.fallbacks}), "drift_limit": mon.tol,
+            "max_rel_drift": {"max_kept": float(mon.max_drift[kept].max()) if kept.any() else None,
+                              "median_kept": float(np.median(mon.max_drift[kept])) if kept.any() else None,
+                              "max_all": float(mon.max_drift.max())},
+            "closure_timed_out": ens.closure_status()}
+        ens.close()
+        say(f"ensemble {key}: {ensembles[key]['fallback_members']} members fell back, {t_ens:.1f} s")
+    comparison = None
+    if a.eval_members > 0 and nets:
+        comparison = evaluate({f"closure_head{h}": n for h, n in nets.items()}, a.fine_level, a.coarse_level,
+                              members=a.eval_members, days=a.eval_days, samples=a.eval_samples, truth=a.truth,
+                              apvm_weight=a.apvm_weight, log=say)
+    for n in nets.values():
+        n.close()
     print(json.dumps({
-        "training_samples": n_samples, "data_s": t_data, "train_s": t_train,
-        "trainer": None if net is None else a.trainer,
-        "loss_first": None if losses is None else float(losses[0]),
-        "loss_last": None if losses is None else float(np.mean(losses[-20:])),
-        "ensemble": {"members": a.members, "level": a.coarse_level, "steps": nsteps, "wall_s": t_ens,
-                     "member_days_per_s": a.members * nsteps * dt / DAY / t_ens,
-                     "closure": net is not None, "every_stage": a.every_stage, "fallbacks": fallbacks,
-                     "drift_limit": mon.tol, "max_rel_drift": drift, "closure_timed_out": timed_out},
-        "comparison": comparison,
+        "training_samples": n_samples, "data_s": t_data, "train_s": t_train, "trainer": a.trainer,
+        "heads": heads, "loss_first": {h: float(l[0]) for h, l in losses.items()},
+        "loss_last": {h: float(np.mean(l[-20:])) for h, l in losses.items()},
+        "ensembles": ensembles, "comparison": comparison,
     }))
 
 
