@@ -127,7 +127,7 @@ def _member_states(model, members):
 
 
 def evaluate(net, fine_level=7, coarse_level=5, members=8, days=5.0, samples=5, seed0=10_000, device=0,
-             log=None, truth="fp64", apvm_weight=0.5):
+             log=None, truth="fp64", apvm_weight=0.5, truth_check=0):
     """Held-out comparison of the learned coarse run with the plain method.
 
     `net` is a ClosureMLP (runs "closure", every stage, and "closure_stage1",
@@ -144,7 +144,9 @@ def evaluate(net, fine_level=7, coarse_level=5, members=8, days=5.0, samples=5, 
     ("plain"), the coarse mesh with the reference's APVM at a fixed weight
     ("apvm", pv_scheme 1 with `apvm_weight`; omitted when 0), and the plain
     method one level finer ("plain_finer", coarse-grained onto the coarse mesh
-    for scoring).  At `samples` evenly spaced times each gets the member-mean
+    for scoring).  With truth="fp32" and truth_check = k > 0, the first k
+    members are also run in FP64 and the relative L2 difference of the two
+    coarse-grained truths is reported per sample ("truth_fp32_vs_fp64").  At `samples` evenly spaced times each gets the member-mean
     relative L2 error of h (area weighted) and of u (dvEdge dcEdge weighted);
     each gets its device time per simulated day (CUDA events around its
     steps, all members).
@@ -198,6 +200,19 @@ def evaluate(net, fine_level=7, coarse_level=5, members=8, days=5.0, samples=5, 
                 gdf, _, uf = fm.get_state()
                 ref[k][s] = cg_c(gd=gdf, u=uf)[:2]
         fm.close()
+    check = {"h": [[] for _ in range(samples)], "u": [[] for _ in range(samples)]}
+    wa0, we0 = coarse.vars["areaCell"], coarse.vars["dvEdge"] * coarse.vars["dcEdge"]
+    for k in range(min(truth_check, members) if not truth_is_fp64 else 0):
+        gd, u, ghs = fine_ics[k]
+        fm = TMCoreGPU(fine, dt=dt_f, precision=abi.TMC_FP64, diag_every=0, **kw)
+        fm.set_initial(gd, u, ghs)
+        for s in range(samples):
+            fm.step(n_f)
+            gdf, _, uf = fm.get_state()
+            g64, u64 = cg_c(gd=gdf, u=uf)[:2]
+            check["h"][s].append(_rel_l2(ref[k][s][0], g64, wa0))
+            check["u"][s].append(_rel_l2(ref[k][s][1], u64, we0))
+        fm.close()
     fine_ics = None
     for name, n in nets.items():
         runs[name].set_closure(n)
@@ -229,6 +244,10 @@ def evaluate(net, fine_level=7, coarse_level=5, members=8, days=5.0, samples=5, 
     return {
         "fine_level": fine_level, "coarse_level": coarse_level, "members": members, "days": days,
         "truth": "FP64 runs" if truth_is_fp64 else "FP32 ensemble", "apvm_weight": apvm_weight,
+        "truth_fp32_vs_fp64": ({"members": min(truth_check, members),
+                                "h_rel_l2_max": [float(max(v)) for v in check["h"]],
+                                "u_rel_l2_max": [float(max(v)) for v in check["u"]]}
+                               if check["h"][0] else None),
         "times_days": [(s + 1) * total / samples / DAY for s in range(samples)],
         "error": err,
         "device_s_per_day": {n: ms[n] / 1e3 / days for n in runs},
@@ -302,6 +321,8 @@ def main():
                     help="the comparison's fine-mesh truth: FP64 runs, or one FP32 ensemble")
     ap.add_argument("--apvm-weight", type=float, default=0.5,
                     help="the comparison's fixed-weight APVM baseline (0: none)")
+    ap.add_argument("--truth-check", type=int, default=0,
+                    help="with --truth fp32: members also run in FP64 to measure the truths' difference")
     ap.add_argument("--out", default=None, help="save the trained networks (.npz; the head is appended)")
     ap.add_argument("--trainer", choices=("tc", "cuda"), default="tc",
                     help="gradients on the tensor cores (tc) or on the CUDA cores in FP32 (cuda)")
@@ -366,7 +387,7 @@ def main():
     if a.eval_members > 0 and nets:
         comparison = evaluate({f"closure_head{h}": n for h, n in nets.items()}, a.fine_level, a.coarse_level,
                               members=a.eval_members, days=a.eval_days, samples=a.eval_samples, truth=a.truth,
-                              apvm_weight=a.apvm_weight, log=say)
+                              apvm_weight=a.apvm_weight, truth_check=a.truth_check, log=say)
     for n in nets.values():
         n.close()
     print(json.dumps({
