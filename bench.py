@@ -320,15 +320,20 @@ def run_mixed(args, local, ics_by_level, peak):
             members += len(ics)
             bytes_cycle += (1200.0 / dt) * ensemble_model_bytes(m.nCells, m.nEdges, m.nVertices, 4, len(ics))
             desc.append(f"L{L}x{len(ics)} dt={dt:g}s")
-        grp = TMCoreGroup(models, cycle_seconds=1200.0)
-        grp.run(1)
-        grp.synchronize()
         cycles = args.mixed_cycles
-        t = time.perf_counter()
-        grp.run(cycles)
-        grp.synchronize()
-        el = time.perf_counter() - t
-        grp.close()
+        by_mode = {}
+        for mode in ((0, 1) if layout == 1 else (0,)):
+            # mode 0: one graph branch per level; mode 1: one launch per pass over all levels
+            grp = TMCoreGroup(models, cycle_seconds=1200.0, mode=mode)
+            grp.run(1)
+            grp.synchronize()
+            t = time.perf_counter()
+            grp.run(cycles)
+            grp.synchronize()
+            by_mode[mode] = (time.perf_counter() - t) / cycles
+            grp.close()
+        group_mode = min(by_mode, key=by_mode.get)
+        el = by_mode[group_mode] * cycles
         # each level alone: its steps of one cycle (CUDA events) and its passes
         alone = {}
         for L, e in zip(sorted(ics_by_level), models):
@@ -336,14 +341,17 @@ def run_mixed(args, local, ics_by_level, peak):
             ms, _, _, _ = e.time_steps(2 * n, total=True, flux=False)
             alone[f"L{L}"] = {"ms_per_cycle": ms / 2, "passes_ms": e.pass_times(2)}
             e.close()
-        res[layout] = (el / cycles, members, desc, bytes_cycle, alone)
+        res[layout] = (el / cycles, members, desc, bytes_cycle, alone, group_mode, by_mode)
     lay = min(res, key=lambda k: res[k][0])  # the faster layout
-    cyc_s, members, desc, bytes_cycle, alone = res[lay]
+    cyc_s, members, desc, bytes_cycle, alone, group_mode, by_mode = res[lay]
     pm = sum(2 ** (L - 4) * inner_ensemble_step_bytes(10 * 4 ** L + 2, 30 * 4 ** L,
                                                                               20 * 4 ** L, len(ics))
              for L, ics in ics_by_level.items())
     out = {"workload": "mixed batch " + ", ".join(desc) + ", one CUDA graph per 1200-s cycle",
-           "member_layout": lay, "members": members, "cycles": args.mixed_cycles, "ms_per_cycle": cyc_s * 1e3,
+           "member_layout": lay, "group_mode": group_mode,
+           "group_mode_ms_per_cycle": {("one launch per pass over all levels" if k == 1 else "a graph branch per level"):
+                                       v * 1e3 for k, v in by_mode.items()},
+           "members": members, "cycles": args.mixed_cycles, "ms_per_cycle": cyc_s * 1e3,
            "member_days_per_s": members * 1200.0 / DAY / cyc_s, "sim_days_per_s": 1200.0 / DAY / cyc_s,
            "scope_model_bytes_per_cycle": bytes_cycle, "achieved_gbs": bytes_cycle / cyc_s / 1e9,
            "frac": bytes_cycle / cyc_s / 1e9 / peak, "pass_model_bytes_per_cycle": pm,

@@ -324,6 +324,25 @@ int tmc_history_close(tmc_history* hw);
  * group again. */
 typedef struct tmc_group tmc_group;
 int tmc_group_create(tmc_handle* const* handles, int32_t n, double cycle_seconds, tmc_group** out);
+/* The same with a choice of schedule (no counterpart in the serial
+ * reference, which runs one model; state_mod.F90:88).  mode 0 is
+ * tmc_group_create.  mode 1 advances the handles by one launch per pass over
+ * all of them: every pass of a CRK4 stage is one kernel launch whose blocks
+ * cover the element blocks of every handle that steps in that sub-step (the
+ * handles ordered by steps per cycle, sub-step s of a cycle stepping those
+ * with more than s steps), and the region sums, beta and the final update are
+ * one launch each as well.  Mode 1 needs member-innermost ensembles
+ * (member_layout 1) of one member count and one pv scheme, without the
+ * learned closure, and at most 8 handles; otherwise it returns TMC_E_UNSUP
+ * (with the reason in tmc_group_last_error of the returned group, which the
+ * caller destroys).  The block sizes are those of the handle with the most
+ * edges.  Members agree with mode 0 to FP32 rounding (the batch kernels run
+ * the same per-block code, compiled into other kernels).  Mode 0 is the
+ * faster schedule for a mixed batch whose largest level is latency bound:
+ * its branches let the small levels use the bandwidth the large one leaves
+ * idle, where mode 1 adds their work to every launch. */
+int tmc_group_create_ex(tmc_handle* const* handles, int32_t n, double cycle_seconds, int32_t mode,
+                        tmc_group** out);
 int tmc_group_run(tmc_group* g, int32_t cycles);
 int tmc_group_synchronize(tmc_group* g);
 const char* tmc_group_last_error(const tmc_group* g);

@@ -185,6 +185,60 @@ def test_autotune_and_group(mesh3, mesh4):
         x.close()
 
 
+@pytest.mark.parametrize("members,scheme", [(16, {}), (32, dict(pv_scheme=3, interp_pv_order=3)),
+                                            (64, dict(pv_scheme=3, interp_pv_order=4))])
+def test_batched_group_matches_separate_runs(mesh3, mesh4, members, scheme):
+    """tmc_group_create_ex mode 1: three ensembles (level 4 at dt 150 s and
+    300 s, level 3 at dt 600 s) advanced by one launch per pass over all of
+    them, two 600-s cycles (4, 2 and 1 steps per cycle: sub-steps with one,
+    two and three meshes), against each ensemble stepped alone.  The batch
+    kernels run the single-mesh kernels' per-block code, but the compiler
+    contracts multiplies and adds into FMAs differently in the two, so FP32
+    values differ in the last bit here and there (about 1e-9 relative in the
+    double-float gd after 8 steps); a block given the wrong mesh, member
+    group or block offset would be off by 1e-3 or more."""
+    from tmcore_gb300.gpu import TMCoreGroup
+
+    kw = dict(conserve_energy=1, diag_every=0, **scheme)
+    setups = [(mesh4, 150.0, 700), (mesh3, 600.0, 600), (mesh4, 300.0, 500)]
+    grouped = [_ensemble(m, _ics(m, members, s), 1, dt=dt, **kw) for m, dt, s in setups]
+    alone = [_ensemble(m, _ics(m, members, s), 1, dt=dt, **kw) for m, dt, s in setups]
+    grp = TMCoreGroup(grouped, cycle_seconds=600.0, mode=1)
+    grp.run(2)
+    for (m, dt, _), y in zip(setups, alone):
+        y.step(int(round(2 * 600.0 / dt)))
+    for x, y in zip(grouped, alone):
+        for m in (0, members - 1):
+            x.select_member(m)
+            y.select_member(m)
+            gx, ix, ux = x.get_state()
+            gy, iy, uy = y.get_state()
+            assert rel_max(gx, gy) < 1e-8, rel_max(gx, gy)
+            assert rel_max(ix, iy) < 1e-5 and rel_max(ux, uy) < 1e-5, (rel_max(ix, iy), rel_max(ux, uy))
+        # beta of the last step, per member
+        bx, by = x.diag_all()[:, 4], y.diag_all()[:, 4]
+        assert np.max(np.abs(bx - by)) < 1e-6, np.max(np.abs(bx - by))
+    grp.close()
+    for x in grouped + alone:
+        x.close()
+
+
+def test_batched_group_refusals(mesh3):
+    from tmcore_gb300 import abi
+    from tmcore_gb300.gpu import TMCError, TMCoreGroup
+
+    kw = dict(conserve_energy=1, diag_every=0, dt=600.0)
+    a = _ensemble(mesh3, _ics(mesh3, 16, 0), 1, **kw)
+    b = _ensemble(mesh3, _ics(mesh3, 32, 0), 1, **kw)
+    c = _ensemble(mesh3, _ics(mesh3, 16, 0), 0, **kw)
+    for pair in ((a, b), (a, c)):
+        with pytest.raises(TMCError) as e:
+            TMCoreGroup(list(pair), cycle_seconds=600.0, mode=1)
+        assert e.value.code == abi.TMC_E_UNSUP
+    for x in (a, b, c):
+        x.close()
+
+
 def test_member_layout_refusals(mesh3):
     from tmcore_gb300 import abi
     from tmcore_gb300.gpu import ClosureMLP, TMCError, TMCoreGPU

@@ -83,6 +83,7 @@ SYMBOLS = {
     "tmc_autotune": (ctypes.c_int, [vp, i32, ctypes.POINTER(i32)]),
     "tmc_pass_times": (ctypes.c_int, [vp, i32, vp]),
     "tmc_group_create": (ctypes.c_int, [ctypes.POINTER(vp), i32, ctypes.c_double, ctypes.POINTER(vp)]),
+    "tmc_group_create_ex": (ctypes.c_int, [ctypes.POINTER(vp), i32, ctypes.c_double, i32, ctypes.POINTER(vp)]),
     "tmc_group_run": (ctypes.c_int, [vp, i32]),
     "tmc_group_synchronize": (ctypes.c_int, [vp]),
     "tmc_group_last_error": (ctypes.c_char_p, [vp]),

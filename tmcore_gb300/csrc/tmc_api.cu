@@ -2043,12 +2043,23 @@ int tmc_autotune(tmc_handle* h, int32_t steps, int32_t block_sizes[5]) {
 }  // extern "C"
 
 // A group of handles (different meshes, each possibly an ensemble) advanced
-// together: one CUDA graph per cycle of `cycle_seconds`, with one branch per
-// handle that runs cycle_seconds / dt steps of that handle; the branches are
-// independent, so the levels' kernels overlap on the GPU.
+// together: one CUDA graph per cycle of `cycle_seconds`.
+//   mode 0: one branch per handle that runs cycle_seconds / dt steps of that
+//           handle; the branches are independent, so the levels' kernels
+//           overlap on the GPU.
+//   mode 1: one launch per pass over every handle (member-innermost
+//           ensembles of one member count and pv scheme).  The handles are
+//           ordered by steps per cycle, most first; sub-step s of a cycle
+//           advances the handles with more than s steps per cycle, each pass
+//           one launch over all their element blocks (ens::launch_jobs_step).
 struct tmc_group {
   std::vector<tmc_handle*> hs;
   std::vector<int> steps;  // per handle and cycle
+  int mode = 0;
+  tmc::ens::JobTable* d_jobs = nullptr;  // mode 1: the job table in device memory
+  std::unique_ptr<tmc::ens::JobTable> jobs;  // mode 1: its host copy
+  std::vector<int> order;                    // mode 1: handles by steps per cycle, most first
+  int big = 0;                               // mode 1: the job whose block sizes the launches use
   cudaStream_t st = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_done = nullptr;
   std::vector<cudaEvent_t> ev_join;
@@ -2056,12 +2067,98 @@ struct tmc_group {
   std::string err;
 };
 
+namespace {
+
+// mode 1: checks, and the job table (host copy in g->jobs, device copy in
+// g->d_jobs); returns TMC_OK or an error with g->err set
+int prepare_batched(tmc_group* g) {
+  using namespace tmc::ens;
+  const int n = (int)g->hs.size();
+  if (n > kMaxJobs) {
+    g->err = "tmc_group_create_ex: mode 1 takes at most " + std::to_string(kMaxJobs) + " handles";
+    return TMC_E_UNSUP;
+  }
+  const tmc_handle* h0 = g->hs[0];
+  for (const tmc_handle* h : g->hs) {
+    if (h->p.member_layout != 1) {
+      g->err = "tmc_group_create_ex: mode 1 runs member-innermost ensembles (member_layout 1)";
+      return TMC_E_UNSUP;
+    }
+    if (h->members != h0->members || h->p.pv_scheme != h0->p.pv_scheme) {
+      g->err = "tmc_group_create_ex: mode 1 needs one member count and one pv scheme for all handles";
+      return TMC_E_UNSUP;
+    }
+    if (h->closure) {
+      g->err = "tmc_group_create_ex: mode 1 runs without the learned closure";
+      return TMC_E_UNSUP;
+    }
+  }
+  std::vector<int>& order = g->order;
+  order.resize(n);
+  for (int i = 0; i < n; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return g->steps[a] > g->steps[b]; });
+  auto T = std::make_unique<JobTable>();
+  std::memset(T.get(), 0, sizeof(JobTable));
+  T->n = n;
+  int big = 0;  // the handle with the most edges lends its block sizes
+  for (int j = 0; j < n; ++j) {
+    tmc_handle* h = g->hs[order[j]];
+    const EnsEngine* e = static_cast<const EnsEngine*>(h->eng.get());
+    Job& J = T->job[j];
+    J.Mh = h->M;
+    J.D = e->D;
+    for (int k = 0; k <= 4; ++k) {
+      J.io[k] = e->io(k);
+      if (k >= 1) J.io[k].vor = J.io[k].gd_v = nullptr;  // kept only by the diagnostic pass
+    }
+    J.P = e->EP;
+    if (e->upwind()) J.up = *e->upwind();
+    J.diag = h->d_diag;
+    J.dt = h->O.dt;
+    J.totalArea = h->hm.totalArea;
+    J.sumAreaTriangle = h->hm.sumAreaTriangle;
+    J.conserve = h->p.conserve_energy != 0;
+    T->off[J_CELLS][j + 1] = T->off[J_CELLS][j] + e->D.slots_c;
+    T->off[J_EDGES][j + 1] = T->off[J_EDGES][j] + e->D.slots_e;
+    T->off[J_VERTS][j + 1] = T->off[J_VERTS][j] + e->D.slots_v;
+    if (h->M.ne > g->hs[order[big]]->M.ne) big = j;
+  }
+  if (cudaMalloc(&g->d_jobs, sizeof(JobTable)) != cudaSuccess ||
+      cudaMemcpy(g->d_jobs, T.get(), sizeof(JobTable), cudaMemcpyHostToDevice) != cudaSuccess) {
+    g->err = std::string("job table: ") + cudaGetErrorString(cudaGetLastError());
+    return TMC_E_CUDA;
+  }
+  g->jobs = std::move(T);
+  g->big = big;
+  return TMC_OK;
+}
+
+// mode 1: one cycle into the group's stream (capturing)
+void capture_batched(tmc_group* g) {
+  const int n = (int)g->hs.size();
+  const int* bsp = g->hs[g->order[g->big]]->bsp;
+  const bool upwind = g->hs[0]->p.pv_scheme == 3;
+  const int nsub = g->steps[g->order[0]];
+  for (int s = 0; s < nsub; ++s) {
+    int nj = 0;
+    while (nj < n && g->steps[g->order[nj]] > s) ++nj;
+    tmc::ens::launch_jobs_step(g->d_jobs, *g->jobs, nj, bsp, upwind, g->st);
+  }
+}
+
+}  // namespace
+
 extern "C" {
 
 int tmc_group_create(tmc_handle* const* handles, int32_t n, double cycle_seconds, tmc_group** out) {
-  if (!out || !handles || n <= 0 || !(cycle_seconds > 0.0)) return TMC_E_ARG;
+  return tmc_group_create_ex(handles, n, cycle_seconds, 0, out);
+}
+
+int tmc_group_create_ex(tmc_handle* const* handles, int32_t n, double cycle_seconds, int32_t mode, tmc_group** out) {
+  if (!out || !handles || n <= 0 || !(cycle_seconds > 0.0) || mode < 0 || mode > 1) return TMC_E_ARG;
   *out = nullptr;
   auto g = std::make_unique<tmc_group>();
+  g->mode = mode;
   for (int i = 0; i < n; ++i) {
     tmc_handle* h = handles[i];
     if (!h || !h->eng) return TMC_E_ARG;
@@ -2102,15 +2199,26 @@ int tmc_group_create(tmc_handle* const* handles, int32_t n, double cycle_seconds
     ensure_prep(h);
     if (cudaStreamSynchronize(h->st) != cudaSuccess) return cerr("cudaStreamSynchronize");
   }
+  if (mode == 1) {
+    const int rc = prepare_batched(g.get());
+    if (rc != TMC_OK) {
+      *out = g.release();
+      return rc;
+    }
+  }
   cudaGraph_t graph = nullptr;
   if (cudaStreamBeginCapture(g->st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return cerr("BeginCapture");
-  cudaEventRecord(g->ev_fork, g->st);
-  for (int i = 0; i < n; ++i) {
-    tmc_handle* h = g->hs[i];
-    cudaStreamWaitEvent(h->st, g->ev_fork, 0);
-    for (int k = 0; k < g->steps[i]; ++k) h->eng->launch_step(false, nullptr, nullptr);
-    cudaEventRecord(g->ev_join[i], h->st);
-    cudaStreamWaitEvent(g->st, g->ev_join[i], 0);
+  if (mode == 1) {
+    capture_batched(g.get());
+  } else {
+    cudaEventRecord(g->ev_fork, g->st);
+    for (int i = 0; i < n; ++i) {
+      tmc_handle* h = g->hs[i];
+      cudaStreamWaitEvent(h->st, g->ev_fork, 0);
+      for (int k = 0; k < g->steps[i]; ++k) h->eng->launch_step(false, nullptr, nullptr);
+      cudaEventRecord(g->ev_join[i], h->st);
+      cudaStreamWaitEvent(g->st, g->ev_join[i], 0);
+    }
   }
   if (cudaStreamEndCapture(g->st, &graph) != cudaSuccess) return cerr("EndCapture");
   cudaError_t e = cudaGraphInstantiate(&g->graph, graph, 0);
@@ -2162,6 +2270,7 @@ int tmc_group_destroy(tmc_group* g) {
   if (!g) return TMC_OK;
   if (g->st) cudaStreamSynchronize(g->st);
   if (g->graph) cudaGraphExecDestroy(g->graph);
+  if (g->d_jobs) cudaFree(g->d_jobs);
   for (cudaEvent_t e : g->ev_join) cudaEventDestroy(e);
   if (g->ev_fork) cudaEventDestroy(g->ev_fork);
   if (g->ev_done) cudaEventDestroy(g->ev_done);

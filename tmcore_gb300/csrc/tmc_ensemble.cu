@@ -285,7 +285,8 @@ __device__ __forceinline__ void prep(const float (&ia)[V], const float (&g1)[V],
 // calc_kinetic_energy :206-221, calc_gd_tend_on_cell tmcore_swm_mod.F90:127-139)
 // ---------------------------------------------------------------------------
 template <int V>
-__global__ void TMC_ENS_LB(TMC_ENS_CELL_MINB) k_ens_cell(DevMesh Mh, Dims D, IO S, RKStage rk, Partials P, int diag) {
+__device__ __forceinline__ void ens_cell(const DevMesh& Mh, const Dims& D, const IO& S, const RKStage& rk,
+                                         const Partials& P, int diag, int bx) {
   __shared__ int s_e[kME][kEnsEPB];
   __shared__ float s_ns[kME][kEnsEPB];
   __shared__ float s_dv[kME][kEnsEPB];
@@ -294,7 +295,7 @@ __global__ void TMC_ENS_LB(TMC_ENS_CELL_MINB) k_ens_cell(DevMesh Mh, Dims D, IO 
   __shared__ FF s_A[kEnsEPB];
   __shared__ float s_invAf[kEnsEPB];
   __shared__ float s_Af[kEnsEPB];
-  const int nc = Mh.nc, c0 = blockIdx.x * kEnsEPB, nel = min(kEnsEPB, nc - c0);
+  const int nc = Mh.nc, c0 = bx * kEnsEPB, nel = min(kEnsEPB, nc - c0);
   for (int t = threadIdx.x; t < kME * kEnsEPB; t += blockDim.x) {
     const int i = t / kEnsEPB, j = t - i * kEnsEPB;
     if (j < nel) {
@@ -393,7 +394,7 @@ __global__ void TMC_ENS_LB(TMC_ENS_CELL_MINB) k_ens_cell(DevMesh Mh, Dims D, IO 
     }
     if (mode >= 1 && mode <= 3) stff<V>(S.gd_next, cm, ffs, gnext);
   }
-  const int slot = blockIdx.x;
+  const int slot = bx;
   if (mode >= 2) {
     float v[2][V];
 #pragma unroll
@@ -408,6 +409,10 @@ __global__ void TMC_ENS_LB(TMC_ENS_CELL_MINB) k_ens_cell(DevMesh Mh, Dims D, IO 
     double* const dst[2] = {P.d(R_MASS, slot), P.d(R_EN_C, slot)};
     block_partials_d<2, V>(L, v, dst);
   }
+}
+template <int V>
+__global__ void TMC_ENS_LB(TMC_ENS_CELL_MINB) k_ens_cell(DevMesh Mh, Dims D, IO S, RKStage rk, Partials P, int diag) {
+  ens_cell<V>(Mh, D, S, rk, P, diag, blockIdx.x);
 }
 
 // invariants of a state only (the diagnostic pass): mass and cell energy
@@ -450,7 +455,8 @@ __global__ void __launch_bounds__(kMaxBS) k_ens_cell_diag(DevMesh Mh, Dims D, IO
 // :262-270); potential enstrophy and absolute vorticity on diag stages
 // ---------------------------------------------------------------------------
 template <int V>
-__global__ void TMC_ENS_LB(TMC_ENS_VERT_MINB) k_ens_vertex(DevMesh Mh, Dims D, IO S, Partials P, int diag) {
+__device__ __forceinline__ void ens_vertex(const DevMesh& Mh, const Dims& D, const IO& S, const Partials& P, int diag,
+                                           int bx) {
   constexpr int kVU = TMC_ENS_VU;  // vertices per warp iteration (their loads first)
   __shared__ int s_c[3][kEnsEPB];
   __shared__ int s_e[3][kEnsEPB];
@@ -460,7 +466,7 @@ __global__ void TMC_ENS_LB(TMC_ENS_VERT_MINB) k_ens_vertex(DevMesh Mh, Dims D, I
   __shared__ float s_iA[kEnsEPB];
   __shared__ float s_f[kEnsEPB];
   __shared__ float s_At[kEnsEPB];
-  const int nv = Mh.nv, v0 = blockIdx.x * kEnsEPB, nel = min(kEnsEPB, nv - v0);
+  const int nv = Mh.nv, v0 = bx * kEnsEPB, nel = min(kEnsEPB, nv - v0);
   for (int t = threadIdx.x; t < 3 * kEnsEPB; t += blockDim.x) {
     const int i = t / kEnsEPB, j = t - i * kEnsEPB;
     if (j < nel) {
@@ -525,19 +531,23 @@ __global__ void TMC_ENS_LB(TMC_ENS_VERT_MINB) k_ens_vertex(DevMesh Mh, Dims D, I
     double v[2][V];
 #pragma unroll
     for (int c = 0; c < V; ++c) v[0][c] = (double)ph[c] + (double)pl[c], v[1][c] = (double)ah[c] + (double)al[c];
-    double* const dst[2] = {P.d(R_PE, blockIdx.x), P.d(R_AV, blockIdx.x)};
+    double* const dst[2] = {P.d(R_PE, bx), P.d(R_AV, bx)};
     block_partials_d<2, V>(L, v, dst);
   }
+}
+template <int V>
+__global__ void TMC_ENS_LB(TMC_ENS_VERT_MINB) k_ens_vertex(DevMesh Mh, Dims D, IO S, Partials P, int diag) {
+  ens_vertex<V>(Mh, D, S, P, diag, blockIdx.x);
 }
 
 // ---------------------------------------------------------------------------
 // edge_pv: centred pv on edges (APVM weight 0, operators_mod.F90:296-316)
 // ---------------------------------------------------------------------------
 template <int V>
-__global__ void __launch_bounds__(kMaxBS) k_ens_edge_pv(DevMesh Mh, Dims D, IO S) {
+__device__ __forceinline__ void ens_edge_pv(const DevMesh& Mh, const Dims& D, const IO& S, int bx) {
   constexpr int kPU = 4;
   __shared__ int s_v[2][kEnsEPB];
-  const int ne = Mh.ne, e0 = blockIdx.x * kEnsEPB, nel = min(kEnsEPB, ne - e0);
+  const int ne = Mh.ne, e0 = bx * kEnsEPB, nel = min(kEnsEPB, ne - e0);
   for (int t = threadIdx.x; t < 2 * kEnsEPB; t += blockDim.x) {
     const int i = t / kEnsEPB, j = t - i * kEnsEPB;
     if (j < nel) s_v[i][j] = Mh.verticesOnEdge[(size_t)i * ne + e0 + j];
@@ -564,6 +574,10 @@ __global__ void __launch_bounds__(kMaxBS) k_ens_edge_pv(DevMesh Mh, Dims D, IO S
     }
   }
 }
+template <int V>
+__global__ void __launch_bounds__(kMaxBS) k_ens_edge_pv(DevMesh Mh, Dims D, IO S) {
+  ens_edge_pv<V>(Mh, D, S, blockIdx.x);
+}
 
 // ---------------------------------------------------------------------------
 // edge_pv, upwind (pv_scheme 3, orders 3 and 4; operators_mod.F90:359-412):
@@ -572,13 +586,14 @@ __global__ void __launch_bounds__(kMaxBS) k_ens_edge_pv(DevMesh Mh, Dims D, IO S
 // (operators_mod.F90:296-316 for the tangential velocity)
 // ---------------------------------------------------------------------------
 template <int V>
-__global__ void __launch_bounds__(kMaxBS) k_ens_edge_pv_up(DevMesh Mh, Dims D, IO S, Upwind U) {
+__device__ __forceinline__ void ens_edge_pv_up(const DevMesh& Mh, const Dims& D, const IO& S, const Upwind& U,
+                                               int bx) {
   __shared__ int s_v[2][kEnsEPB];
   __shared__ int2 s_ew[kME2][kEnsEPB];      // edgesOnEdge, weightsOnEdge (FP32 bits)
   __shared__ int s_n[2][kEnsEPB];
   __shared__ int2 s_iw[kUpW][2][kEnsEPB];   // stencil point, weight (FP32 bits)
   __shared__ float s_dv[kEnsEPB];
-  const int ne = Mh.ne, e0 = blockIdx.x * kEnsEPB, nel = min(kEnsEPB, ne - e0);
+  const int ne = Mh.ne, e0 = bx * kEnsEPB, nel = min(kEnsEPB, ne - e0);
   for (int t = threadIdx.x; t < 2 * kEnsEPB; t += blockDim.x) {
     const int i = t / kEnsEPB, j = t - i * kEnsEPB;
     if (j < nel) {
@@ -645,6 +660,10 @@ __global__ void __launch_bounds__(kMaxBS) k_ens_edge_pv_up(DevMesh Mh, Dims D, I
     stv<V>(S.pv_e, (size_t)(e0 + j) * Mm + L.m0, pe);
   }
 }
+template <int V>
+__global__ void __launch_bounds__(kMaxBS) k_ens_edge_pv_up(DevMesh Mh, Dims D, IO S, Upwind U) {
+  ens_edge_pv_up<V>(Mh, D, S, U, blockIdx.x);
+}
 
 // ---------------------------------------------------------------------------
 // edge_flux: q.F_perp over the 10 neighbours (calc_tangent_vor_flux,
@@ -654,13 +673,14 @@ __global__ void __launch_bounds__(kMaxBS) k_ens_edge_pv_up(DevMesh Mh, Dims D, I
 // prepare the next stage's gd_edge, u and F from its gd and iap_u.
 // ---------------------------------------------------------------------------
 template <int V>
-__global__ void TMC_ENS_LB(TMC_ENS_FLUX_MINB) k_ens_edge_flux(DevMesh Mh, Dims D, IO S, RKStage rk, Partials P) {
+__device__ __forceinline__ void ens_edge_flux(const DevMesh& Mh, const Dims& D, const IO& S, const RKStage& rk,
+                                              const Partials& P, int bx) {
   __shared__ int s_ep[kME2][kEnsEPB];
   __shared__ float s_w[kME2][kEnsEPB];
   __shared__ int s_c[2][kEnsEPB];
   __shared__ float s_dc[kEnsEPB];
   __shared__ float s_ae[kEnsEPB];
-  const int ne = Mh.ne, e0 = blockIdx.x * kEnsEPB, nel = min(kEnsEPB, ne - e0);
+  const int ne = Mh.ne, e0 = bx * kEnsEPB, nel = min(kEnsEPB, ne - e0);
   for (int t = threadIdx.x; t < kME2 * kEnsEPB; t += blockDim.x) {
     const int i = t / kEnsEPB, j = t - i * kEnsEPB;
     if (j < nel) {
@@ -757,9 +777,13 @@ __global__ void TMC_ENS_LB(TMC_ENS_FLUX_MINB) k_ens_edge_flux(DevMesh Mh, Dims D
     float v[2][V];
 #pragma unroll
     for (int c = 0; c < V; ++c) v[0][c] = rip[c], v[1][c] = r44[c];
-    float* const dst[2] = {P.f(R_IP_E + 2 * (mode - 2), blockIdx.x), mode == 4 ? P.f(R_44_E, blockIdx.x) : nullptr};
+    float* const dst[2] = {P.f(R_IP_E + 2 * (mode - 2), bx), mode == 4 ? P.f(R_44_E, bx) : nullptr};
     block_partials_f<2, V>(L, v, dst);
   }
+}
+template <int V>
+__global__ void TMC_ENS_LB(TMC_ENS_FLUX_MINB) k_ens_edge_flux(DevMesh Mh, Dims D, IO S, RKStage rk, Partials P) {
+  ens_edge_flux<V>(Mh, D, S, rk, P, blockIdx.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -769,13 +793,14 @@ __global__ void TMC_ENS_LB(TMC_ENS_FLUX_MINB) k_ens_edge_flux(DevMesh Mh, Dims D
 constexpr int kFU = 4;
 
 template <int V>
-__global__ void __launch_bounds__(kMaxBS) k_ens_final_cells(DevMesh Mh, Dims D, IO S, const double* diag) {
+__device__ __forceinline__ void ens_final_cells(const DevMesh& Mh, const Dims& D, const IO& S, const double* diag,
+                                                int bx) {
   const Lane L = lane_of<V>(D);
   const size_t Mm = L.M, ffs = S.ffs;
   FF bdt[V];
 #pragma unroll
   for (int c = 0; c < V; ++c) bdt[c] = ff_from(diag[(size_t)(L.m0 + c) * kDiagStride + 9]);
-  const int nc = Mh.nc, c0 = blockIdx.x * kEnsEPB, nel = min(kEnsEPB, nc - c0);
+  const int nc = Mh.nc, c0 = bx * kEnsEPB, nel = min(kEnsEPB, nc - c0);
   float* gd = const_cast<float*>(S.gd_old);
   for (int base = L.j0; base < nel; base += L.js * kFU) {
     FF g[kFU][V], a[kFU][V];
@@ -796,17 +821,21 @@ __global__ void __launch_bounds__(kMaxBS) k_ens_final_cells(DevMesh Mh, Dims D, 
     }
   }
 }
+template <int V>
+__global__ void __launch_bounds__(kMaxBS) k_ens_final_cells(DevMesh Mh, Dims D, IO S, const double* diag) {
+  ens_final_cells<V>(Mh, D, S, diag, blockIdx.x);
+}
 
 // Edges: iap_u of state(old) in place, then the edge preparation of the next
 // step's first stage and the edge energy iap_u^2 areaEdge of the new state
 // (tmcore_swm_mod.F90:229), FP32 terms, compensated.  kUpdate false: the
 // stand-alone edge preparation of S.iap_in (energy only when want_energy).
 template <int V, bool kUpdate>
-__global__ void __launch_bounds__(kMaxBS) k_ens_edges(DevMesh Mh, Dims D, IO S, const double* diag, Partials P,
-                                                      int want_energy) {
+__device__ __forceinline__ void ens_edges(const DevMesh& Mh, const Dims& D, const IO& S, const double* diag,
+                                          const Partials& P, int want_energy, int bx) {
   __shared__ int s_c[2][kEnsEPB];
   __shared__ float s_ae[kEnsEPB];
-  const int ne = Mh.ne, e0 = blockIdx.x * kEnsEPB, nel = min(kEnsEPB, ne - e0);
+  const int ne = Mh.ne, e0 = bx * kEnsEPB, nel = min(kEnsEPB, ne - e0);
   for (int t = threadIdx.x; t < 2 * kEnsEPB; t += blockDim.x) {
     const int i = t / kEnsEPB, j = t - i * kEnsEPB;
     if (j < nel) s_c[i][j] = Mh.cellsOnEdge[(size_t)i * ne + e0 + j];
@@ -854,9 +883,14 @@ __global__ void __launch_bounds__(kMaxBS) k_ens_edges(DevMesh Mh, Dims D, IO S, 
     double v[1][V];
 #pragma unroll
     for (int c = 0; c < V; ++c) v[0][c] = (double)eh[c] + (double)el[c];
-    double* const dst[1] = {P.d(R_EN_E, blockIdx.x)};
+    double* const dst[1] = {P.d(R_EN_E, bx)};
     block_partials_d<1, V>(L, v, dst);
   }
+}
+template <int V, bool kUpdate>
+__global__ void __launch_bounds__(kMaxBS) k_ens_edges(DevMesh Mh, Dims D, IO S, const double* diag, Partials P,
+                                                      int want_energy) {
+  ens_edges<V, kUpdate>(Mh, D, S, diag, P, want_energy, blockIdx.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -879,8 +913,7 @@ struct RegionList {
 // count.  (With 8 warps and one accumulator the 7,680 slots of a level-7
 // edge region took about 0.3 ms, a quarter of a 16-member step.)
 constexpr int kRedThreads = 1024;
-__global__ void __launch_bounds__(kRedThreads) k_ens_reduce(Partials P, RegionList RL, double* diag_out) {
-  const int r = RL.r[blockIdx.x], count = RL.count[blockIdx.x];
+__device__ __forceinline__ void ens_reduce(const Partials& P, int r, int count, double* diag_out) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const int m = blockIdx.y * 32 + lane;
   const bool in = m < P.M;
@@ -927,12 +960,14 @@ __global__ void __launch_bounds__(kRedThreads) k_ens_reduce(Partials P, RegionLi
   for (int k = 0; k < nw; ++k) tot = dd_add(tot, DD{sh[k][lane], sl[k][lane]});
   diag_out[(size_t)m * kDiagStride + kDiagLen + r] = tot.hi + tot.lo;
 }
+__global__ void __launch_bounds__(kRedThreads) k_ens_reduce(Partials P, RegionList RL, double* diag_out) {
+  ens_reduce(P, RL.r[blockIdx.x], RL.count[blockIdx.x], diag_out);
+}
 
 // beta (time_scheme_mod.F90:144-150) and the invariants (tmcore_swm_mod.F90:215-255)
 // of every member from its region sums
-__global__ void k_ens_beta(int M, int step, int diag, int conserve, double totalArea, double sumAreaTriangle,
-                           double dt, double* diag_out) {
-  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void ens_beta(int M, int step, int diag, int conserve, double totalArea,
+                                         double sumAreaTriangle, double dt, double* diag_out, int m) {
   if (m >= M) return;
   double* out = diag_out + (size_t)m * kDiagStride;
   const double* rv = out + kDiagLen;
@@ -954,6 +989,10 @@ __global__ void k_ens_beta(int M, int step, int diag, int conserve, double total
     out[2] = rv[R_PE];
     out[3] = rv[R_AV] / sumAreaTriangle;
   }
+}
+__global__ void k_ens_beta(int M, int step, int diag, int conserve, double totalArea, double sumAreaTriangle,
+                           double dt, double* diag_out) {
+  ens_beta(M, step, diag, conserve, totalArea, sumAreaTriangle, dt, diag_out, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // pv on cells for the learned closure: scalar_v2c_interp_operator as a
@@ -1020,6 +1059,91 @@ __global__ void k_ens_to_f32(size_t n, int M, int m, const double* src, float* d
 }
 
 inline unsigned nb(size_t n) { return (unsigned)((n + 255) / 256); }
+
+// ---------------------------------------------------------------------------
+// batch kernels: block b of kind K belongs to the job j with
+// off[K][j] <= b < off[K][j + 1] (j < nj), as block b - off[K][j] of that
+// job's mesh; the bodies are those of the single-mesh kernels
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int job_of(const JobTable* __restrict__ T, int kind, int nj, int* j) {
+  const int b = blockIdx.x;
+  int k = 0;
+  while (k + 1 < nj && b >= T->off[kind][k + 1]) ++k;
+  *j = k;
+  return b - T->off[kind][k];
+}
+__device__ __forceinline__ double stage_adt(int stage, double dt) {
+  return (stage == 1 || stage == 2) ? 0.5 * dt : (stage == 3 ? dt : 0.0);
+}
+
+template <int V>
+__global__ void TMC_ENS_LB(TMC_ENS_CELL_MINB) k_jobs_cell(const JobTable* __restrict__ T, int nj, int stage) {
+  int j;
+  const int bx = job_of(T, J_CELLS, nj, &j);
+  const Job& J = T->job[j];
+  ens_cell<V>(J.Mh, J.D, J.io[stage], RKStage{stage, stage_adt(stage, J.dt)}, J.P, 0, bx);
+}
+template <int V>
+__global__ void TMC_ENS_LB(TMC_ENS_VERT_MINB) k_jobs_vertex(const JobTable* __restrict__ T, int nj, int stage) {
+  int j;
+  const int bx = job_of(T, J_VERTS, nj, &j);
+  const Job& J = T->job[j];
+  ens_vertex<V>(J.Mh, J.D, J.io[stage], J.P, 0, bx);
+}
+template <int V>
+__global__ void __launch_bounds__(kMaxBS) k_jobs_edge_pv(const JobTable* __restrict__ T, int nj, int stage) {
+  int j;
+  const int bx = job_of(T, J_EDGES, nj, &j);
+  const Job& J = T->job[j];
+  ens_edge_pv<V>(J.Mh, J.D, J.io[stage], bx);
+}
+template <int V>
+__global__ void __launch_bounds__(kMaxBS) k_jobs_edge_pv_up(const JobTable* __restrict__ T, int nj, int stage) {
+  int j;
+  const int bx = job_of(T, J_EDGES, nj, &j);
+  const Job& J = T->job[j];
+  ens_edge_pv_up<V>(J.Mh, J.D, J.io[stage], J.up, bx);
+}
+template <int V>
+__global__ void TMC_ENS_LB(TMC_ENS_FLUX_MINB) k_jobs_edge_flux(const JobTable* __restrict__ T, int nj, int stage) {
+  int j;
+  const int bx = job_of(T, J_EDGES, nj, &j);
+  const Job& J = T->job[j];
+  ens_edge_flux<V>(J.Mh, J.D, J.io[stage], RKStage{stage, stage_adt(stage, J.dt)}, J.P, bx);
+}
+template <int V>
+__global__ void __launch_bounds__(kMaxBS) k_jobs_final_cells(const JobTable* __restrict__ T, int nj) {
+  int j;
+  const int bx = job_of(T, J_CELLS, nj, &j);
+  const Job& J = T->job[j];
+  ens_final_cells<V>(J.Mh, J.D, J.io[0], J.diag, bx);
+}
+template <int V>
+__global__ void __launch_bounds__(kMaxBS) k_jobs_final_edges(const JobTable* __restrict__ T, int nj) {
+  int j;
+  const int bx = job_of(T, J_EDGES, nj, &j);
+  const Job& J = T->job[j];
+  ens_edges<V, true>(J.Mh, J.D, J.io[0], J.diag, J.P, 1, bx);
+}
+// the step's region sums: block (job * nr + i, group of 32 members) sums
+// region r[i] of its job, over the job's blocks of the region's element kind
+struct StepRegions {
+  int n;
+  int r[8];
+  int kind[8];
+};
+__global__ void __launch_bounds__(kRedThreads) k_jobs_reduce(const JobTable* __restrict__ T, StepRegions R) {
+  const int j = blockIdx.x / R.n, i = blockIdx.x - j * R.n;
+  const Job& J = T->job[j];
+  const int count = R.kind[i] == J_CELLS ? J.D.slots_c : J.D.slots_e;
+  ens_reduce(J.P, R.r[i], count, J.diag);
+}
+// beta of every member of every job (blockIdx.y = job)
+__global__ void k_jobs_beta(const JobTable* __restrict__ T) {
+  const Job& J = T->job[blockIdx.y];
+  ens_beta(J.D.M, 1, 0, J.conserve, J.totalArea, J.sumAreaTriangle, J.dt, J.diag,
+           blockIdx.x * blockDim.x + threadIdx.x);
+}
 
 }  // namespace
 
@@ -1168,6 +1292,58 @@ void launch_iap_from_u(int ne, int M, int m, const double* gd_e, const double* u
 void launch_to_f32(int n, int M, int m, const double* src, float* dst, cudaStream_t st) {
   const size_t k = m < 0 ? (size_t)n * M : (size_t)n;
   k_ens_to_f32<<<nb(k), 256, 0, st>>>(k, M, m, src, dst);
+}
+
+
+// One CRK4 step of the first nj jobs of T, one launch per pass (the program
+// of EnsEngine::launch_step without the closure and the diagnostics).
+void launch_jobs_step(const JobTable* T, const JobTable& hT, int nj, const int* bsp, bool upwind, cudaStream_t st) {
+  const Dims& D = hT.job[0].D;  // every job has the same members, hence V and lanes
+  int th[5];
+  const unsigned gy = (unsigned)(D.M / (D.LPE * D.V));
+  for (int p = 0; p < 5; ++p) grid_of(1, D, bsp[p], &th[p]);
+  const dim3 gc((unsigned)hT.off[J_CELLS][nj], gy), ge((unsigned)hT.off[J_EDGES][nj], gy),
+      gv((unsigned)hT.off[J_VERTS][nj], gy);
+  const bool up4 = upwind && D.LPE == 32 && D.M % 128 == 0 && TMC_ENS_UP_V == 4;
+  for (int k = 1; k <= 4; ++k) {
+    if (D.V == 2) {
+      k_jobs_cell<2><<<gc, th[0], 0, st>>>(T, nj, k);
+      k_jobs_vertex<2><<<gv, th[1], 0, st>>>(T, nj, k);
+    } else {
+      k_jobs_cell<1><<<gc, th[0], 0, st>>>(T, nj, k);
+      k_jobs_vertex<1><<<gv, th[1], 0, st>>>(T, nj, k);
+    }
+    if (up4)
+      k_jobs_edge_pv_up<4><<<dim3(ge.x, (unsigned)(D.M / 128)), th[2], 0, st>>>(T, nj, k);
+    else if (upwind && D.V == 2)
+      k_jobs_edge_pv_up<2><<<ge, th[2], 0, st>>>(T, nj, k);
+    else if (upwind)
+      k_jobs_edge_pv_up<1><<<ge, th[2], 0, st>>>(T, nj, k);
+    else if (D.V == 2)
+      k_jobs_edge_pv<2><<<ge, th[2], 0, st>>>(T, nj, k);
+    else
+      k_jobs_edge_pv<1><<<ge, th[2], 0, st>>>(T, nj, k);
+    if (D.V == 2)
+      k_jobs_edge_flux<2><<<ge, th[3], 0, st>>>(T, nj, k);
+    else
+      k_jobs_edge_flux<1><<<ge, th[3], 0, st>>>(T, nj, k);
+  }
+  StepRegions R{};
+  for (int k = 0; k < 3; ++k) {
+    R.r[R.n] = R_IP_C + 2 * k, R.kind[R.n++] = J_CELLS;
+    R.r[R.n] = R_IP_E + 2 * k, R.kind[R.n++] = J_EDGES;
+  }
+  R.r[R.n] = R_44_C, R.kind[R.n++] = J_CELLS;
+  R.r[R.n] = R_44_E, R.kind[R.n++] = J_EDGES;
+  k_jobs_reduce<<<dim3((unsigned)(nj * R.n), (unsigned)D.G), kRedThreads, 0, st>>>(T, R);
+  k_jobs_beta<<<dim3(nb(D.M), (unsigned)nj), 256, 0, st>>>(T);
+  if (D.V == 2) {
+    k_jobs_final_cells<2><<<gc, th[4], 0, st>>>(T, nj);
+    k_jobs_final_edges<2><<<ge, th[4], 0, st>>>(T, nj);
+  } else {
+    k_jobs_final_cells<1><<<gc, th[4], 0, st>>>(T, nj);
+    k_jobs_final_edges<1><<<ge, th[4], 0, st>>>(T, nj);
+  }
 }
 
 }  // namespace ens

@@ -139,6 +139,39 @@ void launch_cell_diag(const DevMesh& Mh, const Dims& D, const IO& S, const Parti
 void launch_finalize(const Dims& D, const Partials& P, bool step, bool diag, bool conserve, double totalArea,
                      double sumAreaTriangle, double dt, double* diag_out, cudaStream_t st);
 
+// ---------------------------------------------------------------------------
+// Batches: the member-innermost ensembles of several meshes (different
+// resolutions and time steps, the same member count and pv scheme) advanced
+// by one launch per pass.  A batch kernel's blocks are the concatenation of
+// every active mesh's element blocks along one element kind; block b finds
+// its mesh j from the block offsets (off[kind][j] <= b < off[kind][j + 1])
+// and runs the same per-block body as the single-mesh kernel on mesh j's
+// tables and buffers.  The table lives in device memory; the first nj jobs
+// are active in a launch (the host orders the meshes by steps per cycle,
+// most first, so every sub-step's active set is a prefix).
+// ---------------------------------------------------------------------------
+constexpr int kMaxJobs = 8;
+enum JobKind { J_CELLS = 0, J_EDGES = 1, J_VERTS = 2 };
+struct Job {
+  DevMesh Mh;
+  Dims D;
+  IO io[5];  // the buffers of CRK4 stage k (1-4) and of the final update (0)
+  Partials P;
+  Upwind up;     // upwind pv tables (width 0: centred pv)
+  double* diag;  // per-member diag blocks (beta dt of the step at [m * kDiagStride + 9])
+  double dt, totalArea, sumAreaTriangle;
+  int conserve;
+};
+struct JobTable {
+  int n;
+  int off[3][kMaxJobs + 1];  // first block of each job along cells, edges and vertices
+  Job job[kMaxJobs];
+};
+// one CRK4 step of the first nj jobs (T: the table in device memory, hT: its
+// host copy for the grid sizes); bsp: block sizes of the cell, vertex,
+// edge_pv, edge_flux and final passes; upwind: the jobs run upwind pv
+void launch_jobs_step(const JobTable* T, const JobTable& hT, int nj, const int* bsp, bool upwind, cudaStream_t st);
+
 // The learned PV-on-edge closure (after the pv-on-edge pass): pv on cells
 // (the network reads it), then the network on rows [edge][member] with its
 // output added to pv_edge of members whose switch is on (a.mode 0 every stage;

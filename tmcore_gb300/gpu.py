@@ -280,15 +280,17 @@ class TMCoreGPU:
 
 class TMCoreGroup:
     """Several models (different meshes and dt) advanced together: one CUDA
-    graph per cycle of ``cycle_seconds`` with one branch per model
-    (tmc_group_*)."""
+    graph per cycle of ``cycle_seconds`` (tmc_group_*).  mode 0: one branch
+    per model; mode 1: one launch per pass over all models (member-innermost
+    ensembles of one member count and pv scheme, tmc_group_create_ex)."""
 
-    def __init__(self, models, cycle_seconds: float):
+    def __init__(self, models, cycle_seconds: float, mode: int = 0):
         self.lib = _lib.gpu()
         self.models = list(models)
+        self.mode = int(mode)
         arr = (ctypes.c_void_p * len(self.models))(*[m.h.value for m in self.models])
         g = ctypes.c_void_p()
-        rc = self.lib.tmc_group_create(arr, len(self.models), float(cycle_seconds), ctypes.byref(g))
+        rc = self.lib.tmc_group_create_ex(arr, len(self.models), float(cycle_seconds), self.mode, ctypes.byref(g))
         self.g = g
         if rc != 0:
             msg = self.lib.tmc_group_last_error(g).decode() if g.value else \
