@@ -112,6 +112,27 @@ def test_training_data_and_training_small():
     net.close()
 
 
+def test_training_data_from_an_fp32_ensemble():
+    """The training runs as one member-innermost FP32 ensemble (16 runs): the
+    run-0 samples agree with the FP64 run of the same seed to far below the
+    residual's size (FP32 edge state, double-float gd), and a kept fraction of
+    edges gives that many rows per sample."""
+    from tmcore_gb300 import closure
+
+    kw = dict(fine_level=4, coarse_level=3, days=0.25, samples_per_run=2)
+    X64, Y64 = closure.training_data(runs=1, **kw)
+    X32, Y32 = closure.training_data(runs=16, truth="fp32", **kw)
+    ne = 1920
+    assert X32.shape == (2 * 16 * ne, 24) and np.all(np.isfinite(X32)) and np.all(np.isfinite(Y32))
+    for s in range(2):  # FP64 rows: run-major; FP32 rows: sample-major
+        y64, y32 = Y64[s * ne:(s + 1) * ne], Y32[s * 16 * ne:s * 16 * ne + ne]
+        assert np.linalg.norm(y32 - y64) < 1e-2 * np.linalg.norm(y64), np.linalg.norm(y32 - y64) / np.linalg.norm(y64)
+        x64, x32 = X64[s * ne:(s + 1) * ne], X32[s * 16 * ne:s * 16 * ne + ne]
+        assert np.max(np.abs(x32 - x64) / (np.std(x64, 0) + 1e-30)) < 1e-2
+    Xh, Yh = closure.training_data(runs=16, truth="fp32", edge_frac=0.25, **kw)
+    assert Xh.shape == (2 * 16 * (ne // 4), 24) and np.all(np.isfinite(Yh))
+
+
 def test_fallback_switches_off_a_drifting_member(mesh4):
     from tmcore_gb300.closure import FallbackMonitor
     from tmcore_gb300.gpu import ClosureMLP, TMCoreGPU

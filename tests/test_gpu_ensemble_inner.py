@@ -29,7 +29,7 @@ def _ics(mesh, n, seed0):
 def _ensemble(mesh, ics, layout, **kw):
     from tmcore_gb300.gpu import TMCoreGPU
 
-    ens = TMCoreGPU(mesh, members=len(ics), member_layout=layout, **KW, **kw)
+    ens = TMCoreGPU(mesh, members=len(ics), member_layout=layout, **{**KW, **kw})
     for m, (gd, u, ghs) in enumerate(ics):
         ens.select_member(m)
         ens.set_initial(gd, u, ghs)

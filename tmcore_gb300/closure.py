@@ -39,36 +39,92 @@ def _edge_pv(mesh, pv_vertex):
     return 0.5 * (pv_vertex[v1] + pv_vertex[v2])
 
 
+def _jet_bumps_ic(job):
+    """Initial state of one seeded run (runs in a spawned worker)."""
+    level, seed = job
+    return cases.jet_bumps(icos_mesh(level), seed=seed)
+
+
+def _ics(level, seeds):
+    """Seeded initial states, in order, from a spawn pool (safe beside CUDA work)."""
+    import multiprocessing as mp
+    import os
+
+    jobs = [(level, s) for s in seeds]
+    if level <= 6 or len(jobs) < 4:  # a fraction of a second each: no pool
+        yield from map(_jet_bumps_ic, jobs)
+        return
+    with mp.get_context("spawn").Pool(min(16, os.cpu_count() or 1, len(jobs))) as pool:
+        yield from pool.imap(_jet_bumps_ic, jobs)
+
+
 def training_data(fine_level=8, coarse_level=6, runs=4, days=1.0, samples_per_run=8, seed0=0, device=0,
-                  log=None):
-    """(features [N, 24] float32, targets [N] float32) from FP64 fine runs."""
+                  log=None, truth="fp64", edge_frac=1.0):
+    """(features [N, 24] float32, targets [N] float32) from fine runs.
+
+    truth="fp64": FP64 runs, one at a time.  truth="fp32": all runs as one
+    FP32 ensemble (member-innermost when `runs` is a multiple of 16: FP32 edge
+    and vertex state, double-float gd), the way many runs fit the budget;
+    its difference from FP64 is measured by `evaluate(truth_check=...)`.
+    edge_frac < 1 keeps that fraction of each sample's coarse edges (seeded
+    random subset) to bound the dataset's size."""
     fine, coarse = icos_mesh(fine_level), icos_mesh(coarse_level)
-    cg = Coarsener(fine, coarse, device=device)
     dt_f = level_dt(fine_level)
     steps = max(1, int(round(days * DAY / dt_f / samples_per_run)))
     kw = dict(pv_scheme=1, apvm_weight=0.0, adv_order=2, conserve_energy=1, renumber=1, device=device)
+    ne_c = coarse.dims["nEdges"]
+    keep = max(1, int(round(edge_frac * ne_c)))
+    n_rows = runs * samples_per_run * keep
+    X = np.empty((n_rows, 24), np.float32)
+    Y = np.empty(n_rows, np.float32)
+    rng = np.random.default_rng(seed0 + 7)
+    cg = Coarsener(fine, coarse, device=device)
     cm = TMCoreGPU(coarse, dt=level_dt(coarse_level), precision=abi.TMC_FP32, **kw)
-    X, Y = [], []
-    for r in range(runs):
-        gd, u, ghs = cases.jet_bumps(fine, seed=seed0 + r)
-        fm = TMCoreGPU(fine, dt=dt_f, precision=abi.TMC_FP64, diag_every=0, **kw)
-        fm.set_initial(gd, u, ghs)
-        ghs_c, _, _ = cg(gd=ghs)
+    row = 0
+
+    def add_sample(gdf, uf, pvv, ghs_c, r, s):
+        nonlocal row
+        gd_c, u_c, pv_true = cg(gd=gdf, u=uf, pv_edge=_edge_pv(fine, pvv))
+        cm.set_initial(gd_c, u_c, ghs_c)
+        x, pv_c = cm.closure_features()
+        y = (pv_true - pv_c).astype(np.float32)
+        idx = np.sort(rng.choice(ne_c, keep, replace=False)) if keep < ne_c else slice(None)
+        X[row:row + keep] = x[idx]
+        Y[row:row + keep] = y[idx]
+        row += keep
+        if log and (truth == "fp64" or r % 16 == 0):
+            log(f"run {r} sample {s}: |residual| {np.sqrt(np.mean(y ** 2)):.3e}")
+
+    if truth == "fp64":
+        for r, (gd, u, ghs) in enumerate(_ics(fine_level, range(seed0, seed0 + runs))):
+            fm = TMCoreGPU(fine, dt=dt_f, precision=abi.TMC_FP64, diag_every=0, **kw)
+            fm.set_initial(gd, u, ghs)
+            ghs_c, _, _ = cg(gd=ghs)
+            for s in range(samples_per_run):
+                fm.step(steps)
+                gdf, _, uf = fm.get_state()
+                pvv, _ = fm.get_vertex()
+                add_sample(gdf, uf, pvv, ghs_c, r, s)
+            fm.close()
+    else:
+        fm = TMCoreGPU(fine, dt=dt_f, precision=abi.TMC_FP32, diag_every=0, members=runs,
+                       member_layout=1 if runs % 16 == 0 else 0, **kw)
+        ghs_c = []
+        for r, (gd, u, ghs) in enumerate(_ics(fine_level, range(seed0, seed0 + runs))):
+            fm.select_member(r)
+            fm.set_initial(gd, u, ghs)
+            ghs_c.append(cg(gd=ghs)[0])
         for s in range(samples_per_run):
             fm.step(steps)
-            gdf, _, uf = fm.get_state()
-            pvv, _ = fm.get_vertex()
-            gd_c, u_c, pv_true = cg(gd=gdf, u=uf, pv_edge=_edge_pv(fine, pvv))
-            cm.set_initial(gd_c, u_c, ghs_c)
-            x, pv_c = cm.closure_features()
-            X.append(x)
-            Y.append((pv_true - pv_c).astype(np.float32))
-            if log:
-                log(f"run {r} sample {s}: |residual| {np.sqrt(np.mean(Y[-1] ** 2)):.3e}")
+            for r in range(runs):
+                fm.select_member(r)
+                gdf, _, uf = fm.get_state()
+                pvv, _ = fm.get_vertex()
+                add_sample(gdf, uf, pvv, ghs_c[r], r, s)
         fm.close()
     cm.close()
     cg.close()
-    return np.concatenate(X), np.concatenate(Y)
+    return X, Y
 
 
 def train(X, Y, steps=2000, batch=65536, lr=1e-3, seed=0, device=0, tensor_cores=True, head=2, dt=None):
@@ -330,6 +386,10 @@ def main():
                     help="output heads to train on the same data, comma separated: 1 a learned non-negative "
                          "APVM weight, 2 the residual where it has APVM's sign (both enstrophy-dissipating), "
                          "0 the residual itself")
+    ap.add_argument("--train-truth", choices=("fp64", "fp32"), default="fp64",
+                    help="the training runs: FP64 one at a time, or one FP32 ensemble of all runs")
+    ap.add_argument("--edge-frac", type=float, default=1.0,
+                    help="fraction of each training sample's coarse edges kept (random subset)")
     ap.add_argument("--plain-ensemble", action="store_true",
                     help="also run the held-out ensemble without a network, under the same drift monitor")
     a = ap.parse_args()
@@ -340,7 +400,8 @@ def main():
     t_data, n_samples = 0.0, 0
     if heads:
         t0 = time.time()
-        X, Y = training_data(a.fine_level, a.coarse_level, a.runs, a.days, a.samples, log=say)
+        X, Y = training_data(a.fine_level, a.coarse_level, a.runs, a.days, a.samples, log=say,
+                             truth=a.train_truth, edge_frac=a.edge_frac)
         t_data = time.time() - t0
         n_samples = int(len(Y))
         for h in heads:
