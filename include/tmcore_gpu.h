@@ -93,7 +93,11 @@ typedef struct tmc_params {
                                      (members a multiple of 16; pv_scheme 1 with apvm_weight 0, or pv_scheme 3
                                      with interp_pv_order 3 or 4; adv_order 2, no tracers; other options:
                                      TMC_E_UNSUP): whole-line neighbour gathers */
-  int32_t reserved[3];
+  int32_t member_lanes;           /* member_layout 1: lanes of a warp per element, 8, 16 or 32, dividing
+                                     members; a lane takes two members when members is a multiple of twice
+                                     that, else one.  0 = automatic: 32 lanes (16 when members is not a
+                                     multiple of 32), two members per lane when members is a multiple of 64 */
+  int32_t reserved[2];
 } tmc_params;
 
 typedef struct tmc_handle tmc_handle;

@@ -308,14 +308,16 @@ def test_closure_matches_member_outermost(mesh4, every_stage):
 
 
 def test_ordering_autotuner(mesh4):
-    """The ordering autotuner times element orders x member layouts, skips
-    layouts the options do not allow, and its choice runs."""
+    """The ordering autotuner times element orders x member layouts (and the
+    lane layouts of member_layout 1), skips layouts the options do not allow,
+    and its choice runs."""
     from tmcore_gb300 import tune
     from tmcore_gb300.gpu import TMCoreGPU
 
     ics = _ics(mesh4, M, 700)
     best, timings = tune.autotune_ordering(mesh4, ics, steps=2, dt=600.0, **KW)
-    assert len(timings) == 6 and all("ms_per_step" in t for t in timings), timings
+    nl = len(tune.lane_candidates(M))
+    assert len(timings) == 3 * nl + 3 and all("ms_per_step" in t for t in timings), timings
     assert best["renumber"] in (0, 1, 2) and best["member_layout"] in (0, 1)
     ens = TMCoreGPU(mesh4, **best)
     for m, (gd, u, ghs) in enumerate(ics):
@@ -328,4 +330,4 @@ def test_ordering_autotuner(mesh4):
     kw = dict(KW, pv_scheme=2)
     best, timings = tune.autotune_ordering(mesh4, ics, steps=1, orders=(1,), dt=600.0, **kw)
     assert best["member_layout"] == 0
-    assert [t["member_layout"] for t in timings if "error" in t] == [1]
+    assert [t["member_layout"] for t in timings if "error" in t] == [1] * nl

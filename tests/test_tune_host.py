@@ -48,7 +48,7 @@ def test_autotune_ordering_picks_the_fastest(monkeypatch):
     monkeypatch.setattr(tune, "TMCoreGPU", FakeHandle)
     ics = [("gd0", "u0", "ghs0"), ("gd1", "u1", "ghs1")]
     best, timings = tune.autotune_ordering("mesh", ics, steps=3, dt=300.0, precision=1)
-    assert best == {"dt": 300.0, "precision": 1, "members": 2, "renumber": 2, "member_layout": 0}
+    assert best == {"dt": 300.0, "precision": 1, "members": 2, "renumber": 2, "member_layout": 0, "member_lanes": 0}
     assert len(timings) == 6
     refused = [(t["member_layout"], t["renumber"]) for t in timings if "error" in t]
     assert refused == [(1, 2)]
@@ -74,3 +74,18 @@ def test_autotune_ordering_single_model_and_nothing_buildable(monkeypatch):
         tune.autotune_ordering("mesh", [("gd", "u", "ghs")], dt=300.0)
     # one member: only member_layout 0 is tried, in every element order
     assert layouts == [0, 0, 0]
+
+
+def test_lane_layouts():
+    """member_layout 1's lane layouts (the library's lanes_for rule) and the
+    distinct ones the autotuner times."""
+    from tmcore_gb300 import tune
+
+    assert tune.lane_layout(16, 0) == (1, 16) and tune.lane_layout(16, 8) == (2, 8)
+    assert tune.lane_layout(16, 32) is None and tune.lane_layout(48, 32) is None
+    assert tune.lane_layout(512, 0) == (2, 32) and tune.lane_layout(96, 16) == (2, 16)
+    assert tune.lane_layout(32, 0) == (1, 32) and tune.lane_layout(32, 12) is None
+    assert tune.lane_candidates(16) == [0, 8]
+    assert tune.lane_candidates(48) == [0, 8]
+    assert tune.lane_candidates(32) == [0, 8, 16]
+    assert tune.lane_candidates(512) == [0, 8, 16]

@@ -44,7 +44,7 @@ class Params(ctypes.Structure):
                 ("tracer_adv_mono", i32), ("precision", i32), ("renumber", i32), ("use_graph", i32),
                 ("diag_every", i32), ("device", i32), ("block_size", i32), ("stencils", i32),
                 ("adv_wind", i32), ("members", i32), ("member_layout", i32),
-                ("reserved", i32 * 3)]
+                ("member_lanes", i32), ("reserved", i32 * 2)]
 
 
 # name -> (restype, argtypes)

@@ -82,12 +82,20 @@ def training_data(fine_level=8, coarse_level=6, runs=4, days=1.0, samples_per_ru
     cm = TMCoreGPU(coarse, dt=level_dt(coarse_level), precision=abi.TMC_FP32, **kw)
     row = 0
 
+    skipped = []  # (run, sample) of fine states that are no longer finite
+
     def add_sample(gdf, uf, pvv, ghs_c, r, s):
         nonlocal row
+        if not (np.all(np.isfinite(gdf)) and np.all(np.isfinite(uf)) and np.all(np.isfinite(pvv))):
+            skipped.append((r, s))
+            return
         gd_c, u_c, pv_true = cg(gd=gdf, u=uf, pv_edge=_edge_pv(fine, pvv))
         cm.set_initial(gd_c, u_c, ghs_c)
         x, pv_c = cm.closure_features()
         y = (pv_true - pv_c).astype(np.float32)
+        if not (np.all(np.isfinite(x)) and np.all(np.isfinite(y))):
+            skipped.append((r, s))
+            return
         idx = np.sort(rng.choice(ne_c, keep, replace=False)) if keep < ne_c else slice(None)
         X[row:row + keep] = x[idx]
         Y[row:row + keep] = y[idx]
@@ -124,7 +132,11 @@ def training_data(fine_level=8, coarse_level=6, runs=4, days=1.0, samples_per_ru
         fm.close()
     cm.close()
     cg.close()
-    return X, Y
+    if skipped and log:
+        runs_lost = sorted({r for r, _ in skipped})
+        log(f"{len(skipped)} samples of {len(runs_lost)} runs skipped (state not finite): runs {runs_lost[:20]}")
+    training_data.skipped = skipped
+    return X[:row], Y[:row]
 
 
 def train(X, Y, steps=2000, batch=65536, lr=1e-3, seed=0, device=0, tensor_cores=True, head=2, dt=None):
@@ -276,19 +288,25 @@ def evaluate(net, fine_level=7, coarse_level=5, members=8, days=5.0, samples=5, 
         runs[name].set_closure_stages(name == "closure")
     wa = coarse.vars["areaCell"]
     we = coarse.vars["dvEdge"] * coarse.vars["dcEdge"]
-    err = {name: {"h": [], "u": []} for name in runs}
+    err = {name: {"h": [], "u": [], "nonfinite": []} for name in runs}
     ms = {name: 0.0 for name in runs}
+    truth_members = []
     for s in range(samples):
+        # members whose truth is still finite (the fine runs have no diffusion)
+        valid = [k for k in range(members) if np.all(np.isfinite(ref[k][s][0])) and np.all(np.isfinite(ref[k][s][1]))]
+        truth_members.append(len(valid))
         for name, r in runs.items():
             t, _, _, _ = r.time_steps(n_m if name == "plain_finer" else n_c, total=True, flux=False)
             ms[name] += t
             st = _member_states(r, members)
             if name == "plain_finer":
                 st = [cg_mc(gd=gd, u=u)[:2] for gd, u in st]
-            eh = np.mean([_rel_l2(st[k][0], ref[k][s][0], wa) for k in range(members)])
-            eu = np.mean([_rel_l2(st[k][1], ref[k][s][1], we) for k in range(members)])
-            err[name]["h"].append(float(eh))
-            err[name]["u"].append(float(eu))
+            eh = np.array([_rel_l2(st[k][0], ref[k][s][0], wa) for k in valid])
+            eu = np.array([_rel_l2(st[k][1], ref[k][s][1], we) for k in valid])
+            fin = np.isfinite(eh) & np.isfinite(eu)
+            err[name]["h"].append(float(np.mean(eh[fin])) if fin.any() else float("nan"))
+            err[name]["u"].append(float(np.mean(eu[fin])) if fin.any() else float("nan"))
+            err[name]["nonfinite"].append(int(np.sum(~fin)))
         if log:
             log(f"day {(s + 1) * total / samples / DAY:.2f}: " +
                 ", ".join(f"{n} h {err[n]['h'][-1]:.3e} u {err[n]['u'][-1]:.3e}" for n in runs))
@@ -305,6 +323,7 @@ def evaluate(net, fine_level=7, coarse_level=5, members=8, days=5.0, samples=5, 
                                 "u_rel_l2_max": [float(max(v)) for v in check["u"]]}
                                if check["h"][0] else None),
         "times_days": [(s + 1) * total / samples / DAY for s in range(samples)],
+        "truth_members": truth_members,
         "error": err,
         "device_s_per_day": {n: ms[n] / 1e3 / days for n in runs},
         "closure_timed_out": timed_out,
@@ -397,13 +416,14 @@ def main():
     heads = [int(h) for h in a.heads.split(",") if h != ""]
     dt = level_dt(a.coarse_level)
     nets, losses, t_train = {}, {}, {}
-    t_data, n_samples = 0.0, 0
+    t_data, n_samples, skipped = 0.0, 0, []
     if heads:
         t0 = time.time()
         X, Y = training_data(a.fine_level, a.coarse_level, a.runs, a.days, a.samples, log=say,
                              truth=a.train_truth, edge_frac=a.edge_frac)
         t_data = time.time() - t0
         n_samples = int(len(Y))
+        skipped = list(getattr(training_data, "skipped", []))
         for h in heads:
             t0 = time.time()
             net, ls, sc = train(X, Y, steps=a.steps, tensor_cores=a.trainer == "tc", head=h, dt=dt)
@@ -452,7 +472,8 @@ def main():
     for n in nets.values():
         n.close()
     print(json.dumps({
-        "training_samples": n_samples, "data_s": t_data, "train_s": t_train, "trainer": a.trainer,
+        "training_samples": n_samples, "data_s": t_data, "skipped_samples": len(skipped),
+        "skipped_runs": sorted({r for r, _ in skipped}), "train_s": t_train, "trainer": a.trainer,
         "heads": heads, "loss_first": {h: float(l[0]) for h, l in losses.items()},
         "loss_last": {h: float(np.mean(l[-20:])) for h, l in losses.items()},
         "ensembles": ensembles, "comparison": comparison,

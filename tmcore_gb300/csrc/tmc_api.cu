@@ -680,7 +680,7 @@ struct EnsEngine : EngineBase {
     const size_t nc = h->M.nc * M_, ne = h->M.ne * M_, nv = h->M.nv * M_;
     D.M = h->members;
     D.G = (h->members + 31) / 32;
-    ens::lanes_for(h->members, &D.V, &D.LPE);
+    if (!ens::lanes_for(h->members, h->p.member_lanes, &D.V, &D.LPE)) return TMC_E_ARG;
     D.slots_c = ens::slots_for(h->M.nc);
     D.slots_e = ens::slots_for(h->M.ne);
     D.slots_v = ens::slots_for(h->M.nv);
@@ -1078,6 +1078,9 @@ int tmc_create(const tmc_mesh_desc* mesh, const tmc_params* params, tmc_handle**
   if (p.member_layout != 0) {
     if (p.member_layout != 1) return bad("member_layout must be 0 (member-outermost) or 1 (member-innermost)");
     if (h->members < 16 || h->members % 16 != 0) return bad("member_layout 1 needs members a multiple of 16");
+    int V_, L_;
+    if (!ens::lanes_for(h->members, p.member_lanes, &V_, &L_))
+      return bad("member_lanes must be 0, or 8, 16 or 32 dividing the member count");
     const bool centred = p.pv_scheme == 1 && p.apvm_weight == 0.0;
     const bool upwind = p.pv_scheme == 3 && (p.interp_pv_order == 3 || p.interp_pv_order == 4);
     if (!(centred || upwind) || p.adv_order != 2 || p.n_tracers != 0 || p.flux_4th_order_correct) {
@@ -2084,8 +2087,11 @@ int prepare_batched(tmc_group* g) {
       g->err = "tmc_group_create_ex: mode 1 runs member-innermost ensembles (member_layout 1)";
       return TMC_E_UNSUP;
     }
-    if (h->members != h0->members || h->p.pv_scheme != h0->p.pv_scheme) {
-      g->err = "tmc_group_create_ex: mode 1 needs one member count and one pv scheme for all handles";
+    const EnsEngine* e = static_cast<const EnsEngine*>(h->eng.get());
+    const EnsEngine* e0 = static_cast<const EnsEngine*>(h0->eng.get());
+    if (h->members != h0->members || h->p.pv_scheme != h0->p.pv_scheme || e->D.V != e0->D.V ||
+        e->D.LPE != e0->D.LPE) {
+      g->err = "tmc_group_create_ex: mode 1 needs one member count, lane layout and pv scheme for all handles";
       return TMC_E_UNSUP;
     }
     if (h->closure) {

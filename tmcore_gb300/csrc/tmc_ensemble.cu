@@ -206,7 +206,7 @@ inline dim3 grid_of(int n, const Dims& D, int bs, int* threads) {
 
 // Per-member partial sums of one block: the rows (warps and the element
 // groups of a warp) of each member are combined in a fixed order (FP32
-// TwoSum, or FP64) and row 0 stores them.  Entry (row, member lane) sits at
+// TwoSum here, double-float in block_partials_ff) and row 0 stores them.  Entry (row, member lane) sits at
 // row * LPE + lane: rows x LPE = the block's threads.  Every thread of the
 // block calls these (they synchronise).
 template <int N, int V>
@@ -234,14 +234,21 @@ __device__ __forceinline__ void block_partials_f(const Lane& L, const float (&v)
   }
   __syncthreads();
 }
+// The same for sums held as double-float pairs (compensated FP32 sums, or
+// FF values): the rows are combined in FF arithmetic on the FP32 pipes and
+// row 0 converts each member's pair to FP64 once.  Converting every thread's
+// pair and adding the rows in FP64 cost about 130 FP64 instructions per block
+// (each one warp-wide on GB300's 2-lane FP64 pipe, 16 cycles): on the
+// invariant stage that made the vertex pass of 256 level-6 members 115 us
+// against 78 us on the other stages.
 template <int N, int V>
-__device__ __forceinline__ void block_partials_d(const Lane& L, const double (&v)[N][V], double* const (&dst)[N]) {
-  __shared__ double sh[N][V][kMaxBS];
+__device__ __forceinline__ void block_partials_ff(const Lane& L, const FF (&v)[N][V], double* const (&dst)[N]) {
+  __shared__ float shh[N][V][kMaxBS], shl[N][V][kMaxBS];
   const int at = L.slot * L.lpe + L.ml;
 #pragma unroll
   for (int k = 0; k < N; ++k)
 #pragma unroll
-    for (int c = 0; c < V; ++c) sh[k][c][at] = v[k][c];
+    for (int c = 0; c < V; ++c) shh[k][c][at] = v[k][c].h, shl[k][c][at] = v[k][c].l;
   __syncthreads();
   if (L.slot == 0) {
 #pragma unroll
@@ -249,9 +256,9 @@ __device__ __forceinline__ void block_partials_d(const Lane& L, const double (&v
       double o[V];
 #pragma unroll
       for (int c = 0; c < V; ++c) {
-        double a = 0.0;
-        for (int q = 0; q < L.nslot; ++q) a += sh[k][c][q * L.lpe + L.ml];
-        o[c] = a;
+        FF a{0.f, 0.f};
+        for (int q = 0; q < L.nslot; ++q) a = ff_add(a, FF{shh[k][c][q * L.lpe + L.ml], shl[k][c][q * L.lpe + L.ml]});
+        o[c] = ff_to_double(a);
       }
       stv<V>(dst[k], (size_t)L.m0, o);
     }
@@ -403,11 +410,11 @@ __device__ __forceinline__ void ens_cell(const DevMesh& Mh, const Dims& D, const
     block_partials_f<2, V>(L, v, dst);
   }
   if (diag) {
-    double v[2][V];
+    FF v[2][V];
 #pragma unroll
-    for (int c = 0; c < V; ++c) v[0][c] = ff_to_double(mass[c]), v[1][c] = (double)eh[c] + (double)el[c];
+    for (int c = 0; c < V; ++c) v[0][c] = mass[c], v[1][c] = FF{eh[c], el[c]};
     double* const dst[2] = {P.d(R_MASS, slot), P.d(R_EN_C, slot)};
-    block_partials_d<2, V>(L, v, dst);
+    block_partials_ff<2, V>(L, v, dst);
   }
 }
 template <int V>
@@ -443,11 +450,11 @@ __global__ void __launch_bounds__(kMaxBS) k_ens_cell_diag(DevMesh Mh, Dims D, IO
       two_sum_acc(eh[c], el[c], g[c].h * (g[c].h + 2.f * ghf[c]) * s_Af[j]);
     }
   }
-  double v[2][V];
+  FF v[2][V];
 #pragma unroll
-  for (int c = 0; c < V; ++c) v[0][c] = ff_to_double(mass[c]), v[1][c] = (double)eh[c] + (double)el[c];
+  for (int c = 0; c < V; ++c) v[0][c] = mass[c], v[1][c] = FF{eh[c], el[c]};
   double* const dst[2] = {P.d(R_MASS, blockIdx.x), P.d(R_EN_C, blockIdx.x)};
-  block_partials_d<2, V>(L, v, dst);
+  block_partials_ff<2, V>(L, v, dst);
 }
 
 // ---------------------------------------------------------------------------
@@ -528,11 +535,11 @@ __device__ __forceinline__ void ens_vertex(const DevMesh& Mh, const Dims& D, con
     }
   }
   if (diag) {
-    double v[2][V];
+    FF v[2][V];
 #pragma unroll
-    for (int c = 0; c < V; ++c) v[0][c] = (double)ph[c] + (double)pl[c], v[1][c] = (double)ah[c] + (double)al[c];
+    for (int c = 0; c < V; ++c) v[0][c] = FF{ph[c], pl[c]}, v[1][c] = FF{ah[c], al[c]};
     double* const dst[2] = {P.d(R_PE, bx), P.d(R_AV, bx)};
-    block_partials_d<2, V>(L, v, dst);
+    block_partials_ff<2, V>(L, v, dst);
   }
 }
 template <int V>
@@ -880,11 +887,11 @@ __device__ __forceinline__ void ens_edges(const DevMesh& Mh, const Dims& D, cons
     }
   }
   if (want_energy) {
-    double v[1][V];
+    FF v[1][V];
 #pragma unroll
-    for (int c = 0; c < V; ++c) v[0][c] = (double)eh[c] + (double)el[c];
+    for (int c = 0; c < V; ++c) v[0][c] = FF{eh[c], el[c]};
     double* const dst[1] = {P.d(R_EN_E, bx)};
-    block_partials_d<1, V>(L, v, dst);
+    block_partials_ff<1, V>(L, v, dst);
   }
 }
 template <int V, bool kUpdate>

@@ -45,14 +45,23 @@ struct Dims {
   int slots_c, slots_e, slots_v;  // partial slots: blocks along cells, edges, vertices
 };
 
-// Members per lane and lanes per element for M members (M a multiple of 16):
-// 2 and 32 when M is a multiple of 64, else 1 and 32 (M a multiple of 32) or
-// 16.  Four members per lane (16-byte loads, 4 or 8 lanes per element) made
-// a 16-member level-7 step 2.4x slower (2.87 against 1.20 ms): a warp then
-// gathers from 8 elements at once.
-inline void lanes_for(int M, int* V, int* LPE) {
-  *V = M % 64 == 0 ? 2 : 1;
-  *LPE = M % 32 == 0 ? 32 : 16;
+// Members per lane and lanes per element for M members (M a multiple of 16).
+// lanes 0 (automatic): 2 and 32 when M is a multiple of 64, else 1 and 32 (M
+// a multiple of 32) or 16.  lanes 8, 16 or 32: that many lanes per element,
+// two members per lane when M is a multiple of 2 x lanes, else one.  Returns
+// false when M is not a multiple of lanes.  Four members per lane (16-byte
+// loads, 4 or 8 lanes per element) made a 16-member level-7 step 2.4x slower
+// (2.87 against 1.20 ms): a warp then gathers from 8 elements at once.
+inline bool lanes_for(int M, int lanes, int* V, int* LPE) {
+  if (lanes == 0) {
+    *V = M % 64 == 0 ? 2 : 1;
+    *LPE = M % 32 == 0 ? 32 : 16;
+    return true;
+  }
+  if ((lanes != 8 && lanes != 16 && lanes != 32) || M % lanes != 0) return false;
+  *LPE = lanes;
+  *V = M % (2 * lanes) == 0 ? 2 : 1;
+  return true;
 }
 
 __host__ __device__ inline int slots_for(int n) { return (n + kEnsEPB - 1) / kEnsEPB; }

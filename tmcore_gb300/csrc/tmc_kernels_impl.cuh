@@ -140,6 +140,54 @@ __device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float p) {
   lo = __fadd_rn(lo, err);
 }
 
+// block_store for compensated FP32 sums: the threads' (hi, lo) pairs are
+// combined over each warp and then over the block with FP32 TwoSum
+// arithmetic, and the block's pair is stored as (hi, lo) in FP64 (two
+// conversions per block).  An FP64 shuffle tree costs ten FP64 instructions
+// per warp, and GB300 runs each warp-wide FP64 instruction on a 2-lane pipe
+// (16 cycles), which in the final edge update was most of the FP64 pipe's
+// busy time.  Every thread of the block must call this (it synchronises).
+template <int N>
+__device__ __forceinline__ void block_store_ff(const float (&hi)[N], const float (&lo)[N], const Partials& P,
+                                               const int (&r)[N]) {
+  const int slot = blockIdx.x;
+  __shared__ float sh[N][kMaxBlock / 32], sl[N][kMaxBlock / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+  for (int k = 0; k < N; ++k) {
+    float h = hi[k], l = lo[k];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      const float oh = __shfl_down_sync(0xffffffffu, h, off), ol = __shfl_down_sync(0xffffffffu, l, off);
+      two_sum_acc(h, l, oh);
+      l = __fadd_rn(l, ol);
+    }
+    if (lane == 0) {
+      sh[k][warp] = h;
+      sl[k][warp] = l;
+    }
+  }
+  __syncthreads();
+  if (warp == 0) {
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+      float h = (lane < nw) ? sh[k][lane] : 0.f, l = (lane < nw) ? sl[k][lane] : 0.f;
+#pragma unroll
+      for (int off = kMaxBlock / 64; off > 0; off >>= 1) {
+        const float oh = __shfl_down_sync(0xffffffffu, h, off), ol = __shfl_down_sync(0xffffffffu, l, off);
+        two_sum_acc(h, l, oh);
+        l = __fadd_rn(l, ol);
+      }
+      if (lane == 0) {
+        double* reg = P.region(r[k]);
+        reg[2 * slot] = (double)h;
+        reg[2 * slot + 1] = (double)l;
+      }
+    }
+  }
+  __syncthreads();
+}
+
 // block-strided loop: thread handles i = base + k*blockDim.x, k < kEPT
 #define TMC_FOR_EPT(i, n)                                                              \
   for (int _k = 0, i = blockIdx.x * (kEPT * blockDim.x) + threadIdx.x; _k < kEPT; \
@@ -561,7 +609,8 @@ template <class T, bool kB>
 __global__ void __launch_bounds__(kMaxBlock) k_vertex(DevMesh M, ModelOpt O, StageIO<T> S0, Partials P0, int diag) {
   const StageIO<T> S = kB ? S0.at(blockIdx.y) : S0;
   const Partials P = kB ? P0.at(blockIdx.y) : P0;
-  double pe = 0.0, av = 0.0;
+  double pe = 0.0, av = 0.0;      // FP64 path
+  float ph = 0.f, pl = 0.f, ah = 0.f, al = 0.f;  // FP32 path: compensated sums
   if constexpr (kF64<T>) {
     TMC_FOR_EPT(v, M.nv) {
       // operators_mod.F90:106-123 (c2v), :76-91 (curl), :262-270 (pv)
@@ -592,7 +641,6 @@ __global__ void __launch_bounds__(kMaxBlock) k_vertex(DevMesh M, ModelOpt O, Sta
     // Every load is a read-only (non-coherent) load: nothing this kernel
     // stores aliases them, which lets the compiler issue a vertex's loads
     // ahead of the previous vertex's stores.
-    float ph = 0.f, pl = 0.f, ah = 0.f, al = 0.f;
     TMC_FOR_EPT(v, M.nv) {
       int ci[3], ei[3];
       float kt[3], ts[3];
@@ -629,14 +677,17 @@ __global__ void __launch_bounds__(kMaxBlock) k_vertex(DevMesh M, ModelOpt O, Sta
         two_sum_acc(ah, al, fv * At);
       }
     }
-    pe = (double)ph + (double)pl;
-    av = (double)ah + (double)al;
   }
   (void)O;
   if (diag) {
-    const double vv[2] = {pe, av};
     const int r[2] = {R_PE, R_AV};
-    block_store<double, 2>(vv, P, r);
+    if constexpr (kF64<T>) {
+      const double vv[2] = {pe, av};
+      block_store<double, 2>(vv, P, r);
+    } else {
+      const float h[2] = {ph, ah}, l[2] = {pl, al};
+      block_store_ff<2>(h, l, P, r);
+    }
   }
 }
 
@@ -1232,7 +1283,7 @@ __global__ void __launch_bounds__(kB ? kMemberBlock : kMaxBlock, kB ? TMC_FINAL_
       g2[j] = S.gdf_in[c2[j]];
     }
   }
-  T enT = T(0);  // FP32 path: the thread's few terms in FP32, FP64 from the block sum on
+  float eh = 0.f, el = 0.f;  // FP32 path: the thread's few terms, compensated
 #pragma unroll
   for (int j = 0; j < kEPT; ++j) {
     const int e = e0 + j * blockDim.x;
@@ -1243,12 +1294,16 @@ __global__ void __launch_bounds__(kB ? kMemberBlock : kMaxBlock, kB ? TMC_FINAL_
     if constexpr (kF64<T>)
       en = en + ia[j] * ia[j] * ae[j];
     else
-      enT += ia[j] * ia[j] * ae[j];
+      two_sum_acc(eh, el, ia[j] * ia[j] * ae[j]);
   }
-  if constexpr (!kF64<T>) en = (double)enT;
-  const double v[1] = {en};
   const int r[1] = {R_EN_E};
-  block_store<double, 1>(v, P, r);
+  if constexpr (kF64<T>) {
+    const double v[1] = {en};
+    block_store<double, 1>(v, P, r);
+  } else {
+    const float h[1] = {eh}, l[1] = {el};
+    block_store_ff<1>(h, l, P, r);
+  }
 }
 
 template <class T>

@@ -2,8 +2,8 @@
 // the forward and the backward of one batch in one kernel, BF16 operands in
 // shared memory, FP32 accumulators in tensor memory.
 //
-// A block of 128 threads takes tiles of 128 rows (thread r = row r = TMEM
-// lane r) in turn.  Per tile:
+// A block of 512 threads takes tiles of 128 rows in turn, four threads per
+// row (row r = TMEM lane r), each with 16 of the 64 hidden columns.  Per tile:
 //   forward   Z_l = H_{l-1} W_l^T       (M 128, N 64, K 32/64), Z_l kept in TMEM
 //   output    y = b4 + w4 . h3,  dy = 2 (p(y) - t) p'(y) / batch with p the
 //             output head (p(y) = y for kHeadPlain)
@@ -31,7 +31,9 @@
 namespace tmc {
 namespace mlp {
 
-constexpr int kTrTile = kTile;       // rows per tile = threads per block
+constexpr int kTrTile = kTile;       // rows per tile
+constexpr int kTrThreads = 512;      // threads per block: four per row, 16 hidden columns each
+constexpr int kTrCG = kTrThreads / kTrTile;  // column groups
 constexpr int kTrK = kTile;          // K of the weight-gradient products (rows)
 constexpr int kTrN3 = 144;           // D3: 64 (H2^T) + 1 (ones) + 15 (zero) + 64 (H3^T)
 constexpr int kTrN2 = 80;            // D2: 64 (H1^T) + 1 (ones) + 15 (zero)
@@ -84,11 +86,12 @@ __device__ __forceinline__ void mma_kloop(uint32_t tmem_d, uint32_t a, uint32_t 
 }
 
 // the block's partial gradient from one 64-row accumulator: row m (TMEM lane
-// m, threads 0..63) holds out-unit m; columns 0..nin-1 the weights, column
-// cb the bias.  Loads start at multiples of 16 columns.
-__device__ __forceinline__ void store_dw(uint32_t tl, int m, int nin, int cb, float* gW, float* gb) {
+// m) holds out-unit m; columns 0..nin-1 the weights, column cb the bias.
+// Loads start at multiples of 16 columns; column group cg takes the chunks
+// cg, cg + 4, ...
+__device__ __forceinline__ void store_dw(uint32_t tl, int m, int cg, int nin, int cb, float* gW, float* gb) {
   const int ncol = (nin > cb ? nin : cb + 1);
-  for (int c0 = 0; c0 < ncol; c0 += 16) {
+  for (int c0 = 16 * cg; c0 < ncol; c0 += 16 * kTrCG) {
     float d[16];
     tmem_ld16(tl + c0, d);
     tmem_wait_ld();
@@ -104,6 +107,14 @@ __device__ __forceinline__ void store_dw(uint32_t tl, int m, int nin, int cb, fl
 
 // Src: `bool sample(long long i, float (&x)[kIn], float& t)` for row i of the
 // batch.  part: [gridDim.x][kParams] partial gradients, ploss: [gridDim.x].
+//
+// Threads: kTrThreads = 512, four warps per TMEM lane quarter.  Warp w reads
+// lane quarter w % 4, so thread t owns row r = 32 (w % 4) + (t % 32) of the
+// tile (TMEM lane r) and, with the three other warps of its quarter, splits
+// that row's 64 hidden columns: column group cg = w / 4 takes columns
+// 16 cg .. 16 cg + 15 of every epilogue (and input columns 8 cg .. 8 cg + 7).
+// Each SM sub-partition then has four warps to interleave through the
+// epilogues' dependent bias / GELU / BF16 / store chains instead of one.
 template <class Src>
 __device__ bool train_tiles(const Net& net, const Src& src, long long ntiles, float inv_batch, float* part,
                             double* ploss, uint8_t* smem) {
@@ -115,12 +126,15 @@ __device__ bool train_tiles(const Net& net, const Src& src, long long ntiles, fl
   uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + kTrBar);
   uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + kTrBar + 8);
   __shared__ float sb[3][kH], sw4[kH], sxm[kIn], sxi[kIn], sred[4];
-  const int r = threadIdx.x, warp = r >> 5;
+  __shared__ float sy[kTrCG][kTile];  // the column groups' partial sums of the output
+  const int t = threadIdx.x, warp = t >> 5, quarter = warp & 3, cg = warp >> 2;
+  const int r = quarter * 32 + (t & 31);  // this thread's row of the tile (TMEM lane)
+  const int cc = 16 * cg;                 // its first hidden column
 
   // weights (BF16): forward operands K-major by input, backward operands
   // (W^T) K-major by output; layer 1's bias as a high and a low BF16 part
   // against the two input columns of ones
-  for (int i = r; i < kH * kInPad; i += blockDim.x) {
+  for (int i = t; i < kH * kInPad; i += blockDim.x) {
     const int n = i / kInPad, k = i % kInPad;
     __nv_bfloat16 w = __float2bfloat16_rn(0.f);
     if (k < kIn) {
@@ -132,25 +146,25 @@ __device__ bool train_tiles(const Net& net, const Src& src, long long ntiles, fl
     }
     *reinterpret_cast<__nv_bfloat16*>(smem + kTrW1 + core_off(n, k, kInPad)) = w;
   }
-  for (int i = r; i < kH * kH; i += blockDim.x) {
+  for (int i = t; i < kH * kH; i += blockDim.x) {
     const int n = i / kH, k = i % kH;
     *reinterpret_cast<__nv_bfloat16*>(smem + kTrW2 + core_off(n, k, kH)) = net.pb[kOffW2 + i];
     *reinterpret_cast<__nv_bfloat16*>(smem + kTrW3 + core_off(n, k, kH)) = net.pb[kOffW3 + i];
     *reinterpret_cast<__nv_bfloat16*>(smem + kTrW2T + core_off(k, n, kH)) = net.pb[kOffW2 + i];
     *reinterpret_cast<__nv_bfloat16*>(smem + kTrW3T + core_off(k, n, kH)) = net.pb[kOffW3 + i];
   }
-  for (int i = r; i < kH; i += blockDim.x) {
+  for (int i = t; i < kH; i += blockDim.x) {
     sb[0][i] = net.p[kOffB1 + i];
     sb[1][i] = net.p[kOffB2 + i];
     sb[2][i] = net.p[kOffB3 + i];
     sw4[i] = __bfloat162float(net.pb[kOffW4 + i]);
   }
-  for (int i = r; i < kIn; i += blockDim.x) {
+  for (int i = t; i < kIn; i += blockDim.x) {
     sxm[i] = net.xmean[i];
     sxi[i] = net.xinv[i];
   }
   // the constant rows of the B operands: ones at row 64, zeros at 65..79
-  for (int i = r; i < 16 * kTrK; i += blockDim.x) {
+  for (int i = t; i < 16 * kTrK; i += blockDim.x) {
     const int n = kH + i / kTrK, k = i % kTrK;
     const float v = n == kH ? 1.f : 0.f;
     st_bf16(sB3, n, k, kTrK, v);
@@ -158,7 +172,7 @@ __device__ bool train_tiles(const Net& net, const Src& src, long long ntiles, fl
   }
   const float b4 = net.p[kOffB4];
   const uint32_t mb = smem_u32(mbar);
-  if (r == 0) {
+  if (t == 0) {
     mbar_init(mb, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -173,7 +187,7 @@ __device__ bool train_tiles(const Net& net, const Src& src, long long ntiles, fl
   __syncthreads();
   fence_after_sync();
   const uint32_t tmem = *tslot;
-  const uint32_t tl = tmem + ((uint32_t)(warp * 32) << 16);  // this warp's lane quarter
+  const uint32_t tl = tmem + ((uint32_t)(quarter * 32) << 16);  // this warp's lane quarter
   const uint32_t aA = smem_u32(sA), aXT = smem_u32(sXT), aB2 = smem_u32(sB2), aB3 = smem_u32(sB3);
   const uint32_t aAT1 = smem_u32(sAT[0]), aAT2 = smem_u32(sAT[1]), aAT3 = smem_u32(sAT[2]);
   const uint32_t aW[3] = {smem_u32(smem + kTrW1), smem_u32(smem + kTrW2), smem_u32(smem + kTrW3)};
@@ -186,7 +200,7 @@ __device__ bool train_tiles(const Net& net, const Src& src, long long ntiles, fl
 
   // issue (thread 0), commit, and wait for the MMAs of one step
   auto run = [&](auto issue) -> bool {
-    if (r == 0) {
+    if (t == 0) {
       fence_after_sync();
       issue();
       mma_commit(mb);
@@ -212,16 +226,20 @@ __device__ bool train_tiles(const Net& net, const Src& src, long long ntiles, fl
     const float tgt = vr ? tr : 0.f;
     const float dir = vr ? head_dir(net, xr) : 0.f;  // from the raw features, before the prefetch
     {
+      // the 32 input columns of the row (24 normalised features, 2 ones, 6
+      // zeros); this thread stores columns 8 cg .. 8 cg + 7
       float xs[kInPad];
 #pragma unroll
       for (int k = 0; k < kIn; ++k) xs[k] = vr ? (xr[k] - sxm[k]) * sxi[k] : 0.f;
       xs[kIn] = xs[kIn + 1] = 1.f;
 #pragma unroll
       for (int k = kIn + 2; k < kInPad; ++k) xs[k] = 0.f;
+      float v[8];
 #pragma unroll
-      for (int k0 = 0; k0 < kInPad; k0 += 8) store8_bf16(sA, r, k0, kInPad, xs + k0);
+      for (int k = 0; k < 8; ++k) v[k] = cg == 0 ? xs[k] : cg == 1 ? xs[8 + k] : cg == 2 ? xs[16 + k] : xs[24 + k];
+      store8_bf16(sA, r, 8 * cg, kInPad, v);
 #pragma unroll
-      for (int k = 0; k < kInPad; ++k) st_bf16(sXT, k, r, kTrK, xs[k]);
+      for (int k = 0; k < 8; ++k) st_bf16(sXT, 8 * cg + k, r, kTrK, v[k]);
     }
     publish();
     {
@@ -229,7 +247,6 @@ __device__ bool train_tiles(const Net& net, const Src& src, long long ntiles, fl
       vr = nt < ntiles ? src.sample(nt * kTrTile + r, xr, tr) : false;
     }
     // forward
-    float y = b4;
 #pragma unroll 1
     for (int l = 0; l < 3 && ok; ++l) {
       const int K = l == 0 ? kInPad : kH;
@@ -239,55 +256,54 @@ __device__ bool train_tiles(const Net& net, const Src& src, long long ntiles, fl
       // B operand rows of this layer's transposed activations
       uint8_t* const hT = l == 0 ? sB2 : sB3;
       const int n0 = l == 2 ? kTrH3Row : 0;
-#pragma unroll 1
-      for (int c0 = 0; c0 < kH; c0 += 16) {
-        float d[16];
-        tmem_ld16(tl + (uint32_t)(kTmZ1 + 64 * l + c0), d);
-        tmem_wait_ld();
-        float h[16];
+      float d[16];
+      tmem_ld16(tl + (uint32_t)(kTmZ1 + 64 * l + cc), d);
+      tmem_wait_ld();
+      float h[16];
 #pragma unroll
-        for (int i = 0; i < 16; ++i) {
-          const float z = l == 0 ? d[i] : d[i] + sb[l][c0 + i];
-          h[i] = __bfloat162float(__float2bfloat16_rn(gelu_f(z)));
-        }
-        if (l < 2) {
-          store8_bf16(sA, r, c0, kH, h);
-          store8_bf16(sA, r, c0 + 8, kH, h + 8);
-        } else {
-#pragma unroll
-          for (int i = 0; i < 16; ++i) y += sw4[c0 + i] * h[i];
-        }
-#pragma unroll
-        for (int i = 0; i < 16; ++i) st_bf16(hT, n0 + c0 + i, r, kTrK, h[i]);
+      for (int i = 0; i < 16; ++i) {
+        const float z = l == 0 ? d[i] : d[i] + sb[l][cc + i];
+        h[i] = __bfloat162float(__float2bfloat16_rn(gelu_f(z)));
       }
+      if (l < 2) {
+        store8_bf16(sA, r, cc, kH, h);
+        store8_bf16(sA, r, cc + 8, kH, h + 8);
+      } else {
+        float yp = 0.f;
+#pragma unroll
+        for (int i = 0; i < 16; ++i) yp += sw4[cc + i] * h[i];
+        sy[cg][r] = yp;
+      }
+#pragma unroll
+      for (int i = 0; i < 16; ++i) st_bf16(hT, n0 + cc + i, r, kTrK, h[i]);
       publish();
     }
     if (!ok) break;
-    // output head and loss
+    // output head and loss (every thread of the row forms the same y)
+    const float y = b4 + sy[0][r] + sy[1][r] + sy[2][r] + sy[3][r];
     float dpred;
     const float e = head_pred(net, y, dir, dpred) - tgt;
     const float dy = 2.f * e * inv_batch * dpred;
-    {
+    if (cg == 0) {
       float le = e * e;
       for (int off = 16; off > 0; off >>= 1) le += __shfl_down_sync(0xffffffffu, le, off);
-      if ((r & 31) == 0) sred[warp] = le;
+      if ((t & 31) == 0) sred[quarter] = le;
+      st_bf16(sAT[2], kH, r, kTrK, dy);
     }
-    st_bf16(sAT[2], kH, r, kTrK, dy);
     // dZ3 = dy w4 gelu'(z3): row-major into sA (for dH2), transposed into AT3
-#pragma unroll 1
-    for (int c0 = 0; c0 < kH; c0 += 16) {
+    {
       float d[16], g[16];
-      tmem_ld16(tl + (uint32_t)(kTmZ3 + c0), d);
+      tmem_ld16(tl + (uint32_t)(kTmZ3 + cc), d);
       tmem_wait_ld();
 #pragma unroll
-      for (int i = 0; i < 16; ++i) g[i] = dy * sw4[c0 + i] * gelu_grad_f(d[i] + sb[2][c0 + i]);
-      store8_bf16(sA, r, c0, kH, g);
-      store8_bf16(sA, r, c0 + 8, kH, g + 8);
+      for (int i = 0; i < 16; ++i) g[i] = dy * sw4[cc + i] * gelu_grad_f(d[i] + sb[2][cc + i]);
+      store8_bf16(sA, r, cc, kH, g);
+      store8_bf16(sA, r, cc + 8, kH, g + 8);
 #pragma unroll
-      for (int i = 0; i < 16; ++i) st_bf16(sAT[2], c0 + i, r, kTrK, g[i]);
+      for (int i = 0; i < 16; ++i) st_bf16(sAT[2], cc + i, r, kTrK, g[i]);
     }
     publish();
-    if (r == 0) loss += (double)(sred[0] + sred[1] + sred[2] + sred[3]) * inv_batch;
+    if (t == 0) loss += (double)(sred[0] + sred[1] + sred[2] + sred[3]) * inv_batch;
     ok = run([&] {
       mma_kloop(tmem + kTmZ3, aA, aWT3, kH, kIdF, false);
       mma_kloop(tmem + kTmD3, aAT3, aB3, kTrK, idesc_bf16_f32(kTile, kTrN3), !first);
@@ -297,20 +313,19 @@ __device__ bool train_tiles(const Net& net, const Src& src, long long ntiles, fl
 #pragma unroll 1
     for (int l = 1; l >= 0 && ok; --l) {
       const uint32_t dh = (uint32_t)(kTmZ1 + 64 * (l + 1)), zc = (uint32_t)(kTmZ1 + 64 * l);
-#pragma unroll 1
-      for (int c0 = 0; c0 < kH; c0 += 16) {
+      {
         float d[16], z[16], g[16];
-        tmem_ld16(tl + dh + c0, d);
-        tmem_ld16(tl + zc + c0, z);
+        tmem_ld16(tl + dh + cc, d);
+        tmem_ld16(tl + zc + cc, z);
         tmem_wait_ld();
 #pragma unroll
-        for (int i = 0; i < 16; ++i) g[i] = d[i] * gelu_grad_f(l == 0 ? z[i] : z[i] + sb[l][c0 + i]);
+        for (int i = 0; i < 16; ++i) g[i] = d[i] * gelu_grad_f(l == 0 ? z[i] : z[i] + sb[l][cc + i]);
         if (l == 1) {
-          store8_bf16(sA, r, c0, kH, g);
-          store8_bf16(sA, r, c0 + 8, kH, g + 8);
+          store8_bf16(sA, r, cc, kH, g);
+          store8_bf16(sA, r, cc + 8, kH, g + 8);
         }
 #pragma unroll
-        for (int i = 0; i < 16; ++i) st_bf16(sAT[l], c0 + i, r, kTrK, g[i]);
+        for (int i = 0; i < 16; ++i) st_bf16(sAT[l], cc + i, r, kTrK, g[i]);
       }
       publish();
       if (l == 1)
@@ -326,26 +341,28 @@ __device__ bool train_tiles(const Net& net, const Src& src, long long ntiles, fl
   // the block's partial gradient (zeros when it had no tile) and loss
   float* const g = part + (size_t)blockIdx.x * kParams;
   if (ok && !first) {
-    store_dw(tl + kTmD3, r, kH, kH, g + kOffW3, g + kOffB3);
-    store_dw(tl + kTmD2, r, kH, kH, g + kOffW2, g + kOffB2);
-    store_dw(tl + kTmD1, r, kIn, kIn, g + kOffW1, g + kOffB1);
-    // D3 row 64 (warp 2, lane 0): the output layer
-    for (int c0 = 0; c0 < kH; c0 += 16) {
+    store_dw(tl + kTmD3, r, cg, kH, kH, g + kOffW3, g + kOffB3);
+    store_dw(tl + kTmD2, r, cg, kH, kH, g + kOffW2, g + kOffB2);
+    store_dw(tl + kTmD1, r, cg, kIn, kIn, g + kOffW1, g + kOffB1);
+    // D3 row 64 (lane 0 of quarter 2): the output layer, 16 columns per group
+    {
       float d[16];
-      tmem_ld16(tl + (uint32_t)(kTmD3 + kTrH3Row + c0), d);
+      tmem_ld16(tl + (uint32_t)(kTmD3 + kTrH3Row + cc), d);
       tmem_wait_ld();
       if (r == kH)
 #pragma unroll
-        for (int i = 0; i < 16; ++i) g[kOffW4 + c0 + i] = d[i];
+        for (int i = 0; i < 16; ++i) g[kOffW4 + cc + i] = d[i];
     }
-    float d[16];
-    tmem_ld16(tl + (uint32_t)(kTmD3 + kH), d);  // column 64: the ones
-    tmem_wait_ld();
-    if (r == kH) g[kOffB4] = d[0];
+    if (cg == 0) {
+      float d[16];
+      tmem_ld16(tl + (uint32_t)(kTmD3 + kH), d);  // column 64: the ones
+      tmem_wait_ld();
+      if (r == kH) g[kOffB4] = d[0];
+    }
   } else {
-    for (int i = r; i < kParams; i += blockDim.x) g[i] = 0.f;
+    for (int i = t; i < kParams; i += blockDim.x) g[i] = 0.f;
   }
-  if (r == 0) ploss[blockIdx.x] = loss;
+  if (t == 0) ploss[blockIdx.x] = loss;
   // after a timed-out wait, the MMAs of that commit may still be running:
   // wait for them (bounded) before the columns are freed
   if (!ok) mbar_wait(mb, phase ^ 1u, kWaitPolls);
