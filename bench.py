@@ -297,34 +297,64 @@ def run_mixed(args, local, ics_by_level, peak):
     """Config 3, mixed batch: ensembles on mesh levels 4-7 with dt = 1200 / 2^(L-4) s,
     advanced together as one CUDA graph per 1200-s cycle (tmc_group).  Both member
     layouts are timed when every level's member count is a multiple of 16; the
-    faster is reported, the other beside it."""
-    from tmcore_gb300 import abi, mesh
-    from tmcore_gb300.gpu import TMCoreGPU, TMCoreGroup
+    faster is reported, the other beside it.  In the member-innermost layout the
+    batch takes the lane layout (tune.lane_candidates, one for all levels, so that
+    both group schedules apply) whose slowest level, timed alone for its steps of
+    a cycle after tuning the block sizes, is fastest."""
+    from tmcore_gb300 import abi, mesh, tune
+    from tmcore_gb300.gpu import TMCError, TMCoreGPU, TMCoreGroup
 
     inner_ok = all(len(ics) % 16 == 0 for ics in ics_by_level.values())
     res = {}
     for layout in ((1, 0) if inner_ok else (0,)):
-        models, bytes_cycle, members, desc = [], 0.0, 0, []
-        for L, ics in sorted(ics_by_level.items()):
+        # lane layouts every level's member count allows
+        lanes_ok = [ln for ln in tune.LANES
+                    if all(ln in tune.lane_candidates(len(ics)) for ics in ics_by_level.values())] if layout == 1 else [0]
+        best, lanes_ms = None, {}  # best: (slowest level's ms per cycle, member_lanes, models)
+        for ln in lanes_ok:
+            cand, t_lv = [], {}
+            for L, ics in sorted(ics_by_level.items()):
+                m = mesh.icos_mesh(L)
+                dt = 1200.0 / 2 ** (L - 4)
+                c = TMCoreGPU(m, members=len(ics), dt=dt, pv_scheme=1, apvm_weight=0.0, adv_order=2,
+                              conserve_energy=1, precision=abi.TMC_FP32, diag_every=0, use_graph=1, renumber=1,
+                              device=local, member_layout=layout, member_lanes=ln)
+                for k, (gd, u, ghs) in enumerate(ics):
+                    c.select_member(k)
+                    c.set_initial(gd, u, ghs)
+                if not args.no_autotune:
+                    c.autotune(steps=2)
+                if len(lanes_ok) > 1:  # the level's steps of two cycles, alone
+                    ms, _, _, _ = c.time_steps(2 ** (L - 3), total=True, flux=False)
+                    t_lv[f"L{L}"] = ms / 2
+                cand.append(c)
+            worst = max(t_lv.values()) if t_lv else 0.0
+            lanes_ms[str(ln)] = t_lv
+            if best is None or worst < best[0]:
+                if best is not None:
+                    for c in best[2]:
+                        c.close()
+                best = (worst, ln, cand)
+            else:
+                for c in cand:
+                    c.close()
+        models, bytes_cycle, members, desc = best[2], 0.0, 0, []
+        for (L, ics), e in zip(sorted(ics_by_level.items()), models):
             m = mesh.icos_mesh(L)
             dt = 1200.0 / 2 ** (L - 4)
-            e = TMCoreGPU(m, members=len(ics), dt=dt, pv_scheme=1, apvm_weight=0.0, adv_order=2, conserve_energy=1,
-                          precision=abi.TMC_FP32, diag_every=0, use_graph=1, renumber=1, device=local,
-                          member_layout=layout)
-            for k, (gd, u, ghs) in enumerate(ics):
-                e.select_member(k)
-                e.set_initial(gd, u, ghs)
-            if not args.no_autotune:
-                e.autotune(steps=2)
-            models.append(e)
             members += len(ics)
             bytes_cycle += (1200.0 / dt) * ensemble_model_bytes(m.nCells, m.nEdges, m.nVertices, 4, len(ics))
             desc.append(f"L{L}x{len(ics)} dt={dt:g}s")
+        lanes_ms = {"member_lanes": best[1], "ms_per_cycle_by_lanes_and_level": lanes_ms} if layout == 1 else {}
         cycles = args.mixed_cycles
         by_mode = {}
         for mode in ((0, 1) if layout == 1 else (0,)):
             # mode 0: one graph branch per level; mode 1: one launch per pass over all levels
-            grp = TMCoreGroup(models, cycle_seconds=1200.0, mode=mode)
+            # (it refuses levels whose lane layouts differ)
+            try:
+                grp = TMCoreGroup(models, cycle_seconds=1200.0, mode=mode)
+            except TMCError:
+                continue
             grp.run(1)
             grp.synchronize()
             t = time.perf_counter()
@@ -341,9 +371,9 @@ def run_mixed(args, local, ics_by_level, peak):
             ms, _, _, _ = e.time_steps(2 * n, total=True, flux=False)
             alone[f"L{L}"] = {"ms_per_cycle": ms / 2, "passes_ms": e.pass_times(2)}
             e.close()
-        res[layout] = (el / cycles, members, desc, bytes_cycle, alone, group_mode, by_mode)
+        res[layout] = (el / cycles, members, desc, bytes_cycle, alone, group_mode, by_mode, lanes_ms)
     lay = min(res, key=lambda k: res[k][0])  # the faster layout
-    cyc_s, members, desc, bytes_cycle, alone, group_mode, by_mode = res[lay]
+    cyc_s, members, desc, bytes_cycle, alone, group_mode, by_mode, lanes_ms = res[lay]
     pm = sum(2 ** (L - 4) * inner_ensemble_step_bytes(10 * 4 ** L + 2, 30 * 4 ** L,
                                                                               20 * 4 ** L, len(ics))
              for L, ics in ics_by_level.items())
@@ -355,7 +385,7 @@ def run_mixed(args, local, ics_by_level, peak):
            "member_days_per_s": members * 1200.0 / DAY / cyc_s, "sim_days_per_s": 1200.0 / DAY / cyc_s,
            "scope_model_bytes_per_cycle": bytes_cycle, "achieved_gbs": bytes_cycle / cyc_s / 1e9,
            "frac": bytes_cycle / cyc_s / 1e9 / peak, "pass_model_bytes_per_cycle": pm,
-           "pass_model_frac": pm / cyc_s / 1e9 / peak, "levels_alone": alone,
+           "pass_model_frac": pm / cyc_s / 1e9 / peak, "levels_alone": alone, "member_lanes_by_level": lanes_ms,
            "timing": "host wall clock around tmc_group_run + sync; levels alone: CUDA events"}
     for other in res:
         if other != lay:

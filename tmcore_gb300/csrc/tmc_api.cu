@@ -111,6 +111,10 @@ struct tmc_handle {
   int sms = 148;
   double* d_hist = nullptr;    // history outputs on cells (5 x nCells)
   cudaStream_t cst = nullptr;  // host-copy stream of tmc_time_integrate
+  // second stream of the step program: the vertex and pv-on-edge passes of a
+  // stage run on it, concurrent with the cell pass (fork/join events)
+  cudaStream_t st2 = nullptr;
+  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
   cudaEvent_t cev[8] = {};
   double* d_hist_e = nullptr;  // history outputs on edges and vertices
   int timed_pass = 3;  // the pass tmc_time_steps brackets with events
@@ -138,6 +142,23 @@ struct tmc_handle {
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fail(TMC_E_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
     return TMC_OK;
+  }
+  // The vertex pass and the pv-on-edge pass of a CRK4 stage read only the
+  // stage's input state (gd and the edge set the previous pass prepared),
+  // nothing the stage's cell pass writes, and the cell pass reads nothing
+  // they write: between fork_side() and join_side() they run on st2 while
+  // the cell pass runs on st.  The two branches fill each other's tails and
+  // memory-latency gaps; the flux pass (and the closure, which reads E) come
+  // after the join.  In a captured step this is a fork and a join in the
+  // graph.
+  cudaStream_t fork_side() {
+    cudaEventRecord(fork_ev, st);
+    cudaStreamWaitEvent(st2, fork_ev, 0);
+    return st2;
+  }
+  void join_side() {
+    cudaEventRecord(join_ev, st2);
+    cudaStreamWaitEvent(st, join_ev, 0);
   }
 };
 
@@ -351,14 +372,19 @@ struct Engine : EngineBase {
       auto mark = [&](int pass) {
         if (flux_ev && h->timed_pass == pass) cudaEventRecord((*flux_ev)[(*ev_pos)++], h->st);
       };
+      // concurrent cell and vertex / pv-on-edge branches, except while passes
+      // are timed one by one and for the conservative APVM (its global sums)
+      const bool branch = !flux_ev && O.pv_scheme != 2;
+      const cudaStream_t side = branch ? h->fork_side() : h->st;
       mark(P_CELL);
       launch_cell<T>(M, O, s, rk, h->P, dg, b[P_CELL], h->st);
       mark(P_CELL);
       mark(P_VERTEX);
-      launch_vertex<T>(M, O, s, h->P, dg, b[P_VERTEX], h->st);
+      launch_vertex<T>(M, O, s, h->P, dg, b[P_VERTEX], side);
       mark(P_VERTEX);
       mark(P_PV);
-      launch_edge_pv<T>(M, O, s, b[P_PV], h->st);
+      launch_edge_pv<T>(M, O, s, b[P_PV], side);
+      if (branch) h->join_side();
       if (O.pv_scheme == 2) launch_cons_apvm<T>(M, O, s, h->P, h->d_diag, b[P_VERTEX], h->st);
       launch_closure_pass(s, k);
       mark(P_PV);
@@ -810,14 +836,18 @@ struct EnsEngine : EngineBase {
       s.gd_v = nullptr;
       const bool dg = diag && k == 1;
       const RKStage rk{k, adt[k]};
+      // concurrent cell and vertex / pv-on-edge branches (tmc_handle::fork_side),
+      // except while passes are timed one by one
+      const cudaStream_t side = ev ? h->st : h->fork_side();
       mark(P_CELL);
       ens::launch_cell(M, D, s, rk, EP, dg, b[P_CELL], h->st);
       mark(P_CELL);
       mark(P_VERTEX);
-      ens::launch_vertex(M, D, s, EP, dg, b[P_VERTEX], h->st);
+      ens::launch_vertex(M, D, s, EP, dg, b[P_VERTEX], side);
       mark(P_VERTEX);
       mark(P_PV);
-      ens::launch_edge_pv(M, D, s, upwind(), b[P_PV], h->st);
+      ens::launch_edge_pv(M, D, s, upwind(), b[P_PV], side);
+      if (!ev) h->join_side();
       if (h->closure) {
         // the learned closure on this stage's pv_edge: in every stage, or in
         // stage 1 with its output held for stages 2-4
@@ -1128,8 +1158,11 @@ int tmc_create(const tmc_mesh_desc* mesh, const tmc_params* params, tmc_handle**
     return TMC_E_ARG;
   }
   HostMesh& hm = h->hm;
-  if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess) {
-    h->err = "cudaStreamCreate failed";
+  if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&h->st2, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&h->fork_ev, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&h->join_ev, cudaEventDisableTiming) != cudaSuccess) {
+    h->err = "cudaStreamCreate / cudaEventCreate failed";
     *out = h.release();
     return TMC_E_CUDA;
   }
@@ -1318,6 +1351,12 @@ int tmc_destroy(tmc_handle* h) {
   h->eng.reset();
   for (void* q : h->dptrs) cudaFree(q);
   if (h->h_diag) cudaFreeHost(h->h_diag);
+  if (h->st2) {
+    cudaStreamSynchronize(h->st2);
+    cudaStreamDestroy(h->st2);
+  }
+  if (h->fork_ev) cudaEventDestroy(h->fork_ev);
+  if (h->join_ev) cudaEventDestroy(h->join_ev);
   if (h->st) cudaStreamDestroy(h->st);
   delete h;
   return TMC_OK;

@@ -454,14 +454,22 @@ struct TrainSrc {
   float yscale;
   __device__ bool sample(long long i, float (&x)[kIn], float& t) const {
     const long long j = (offset + i) % rows;
+    // a row is 96 bytes, 16-byte aligned: six 16-byte loads
+    const float4* xr = reinterpret_cast<const float4*>(X + j * kIn);
 #pragma unroll
-    for (int k = 0; k < kIn; ++k) x[k] = X[j * kIn + k];
+    for (int k = 0; k < kIn / 4; ++k) {
+      const float4 v = xr[k];
+      x[4 * k] = v.x;
+      x[4 * k + 1] = v.y;
+      x[4 * k + 2] = v.z;
+      x[4 * k + 3] = v.w;
+    }
     t = Y[j] / yscale;
     return true;
   }
 };
 
-__global__ void __launch_bounds__(kTrTile, 1) k_mlp_train_tc(Net net, TrainSrc src, long long ntiles, float inv_batch,
+__global__ void __launch_bounds__(kTrThreads, 1) k_mlp_train_tc(Net net, TrainSrc src, long long ntiles, float inv_batch,
                                                              float* part, double* ploss, int* err) {
   extern __shared__ __align__(128) uint8_t smem[];
   if (!train_tiles(net, src, ntiles, inv_batch, part, ploss, smem) && threadIdx.x == 0) atomicExch(err, 1);
@@ -548,6 +556,8 @@ struct tmc_mlp {
   long long io_cap = 0;
   int* d_err = nullptr;
   double* d_loss = nullptr;
+  double* d_losses = nullptr;  // tmc_mlp_train: one loss per step, read back once at the end
+  int losses_cap = 0;
   int train_tc = 1;          // tmc_mlp_train / tmc_mlp_gradient on the tensor cores (0: CUDA cores)
   float* part = nullptr;     // [sms][kParams] per-block partial gradients (tensor-core trainer)
   double* ploss = nullptr;   // [sms]
@@ -633,7 +643,7 @@ int tmc_mlp_destroy(tmc_mlp* n) {
   if (!n) return TMC_OK;
   if (n->st) cudaStreamSynchronize(n->st);
   void* ptrs[] = {n->p, n->pb, n->g, n->m, n->v, n->xmean, n->xinv, n->dx, n->dy, n->io_x, n->io_y, n->d_err, n->d_loss,
-                   n->part,  n->ploss};
+                   n->d_losses, n->part,  n->ploss};
   for (void* q : ptrs) cudaFree(q);
   if (n->st) cudaStreamDestroy(n->st);
   delete n;
@@ -662,7 +672,11 @@ int tmc_mlp_set_params(tmc_mlp* n, const float* params) {
 }
 
 int tmc_mlp_set_scaling(tmc_mlp* n, const float* x_mean, const float* x_inv_std, float y_scale) {
-  if (!n || !x_mean || !x_inv_std || !(y_scale > 0.f)) return TMC_E_ARG;
+  if (!n || !x_mean || !x_inv_std) return TMC_E_ARG;
+  if (!(y_scale > 0.f) || !std::isfinite(y_scale)) return n->fail(TMC_E_ARG, "tmc_mlp_set_scaling: y_scale must be finite and > 0");
+  for (int k = 0; k < kIn; ++k)
+    if (!std::isfinite(x_mean[k]) || !std::isfinite(x_inv_std[k]))
+      return n->fail(TMC_E_ARG, "tmc_mlp_set_scaling: non-finite feature scaling");
   cudaMemcpyAsync(n->xmean, x_mean, sizeof(float) * kIn, cudaMemcpyHostToDevice, n->st);
   cudaMemcpyAsync(n->xinv, x_inv_std, sizeof(float) * kIn, cudaMemcpyHostToDevice, n->st);
   n->yscale = y_scale;
@@ -724,18 +738,19 @@ int tmc_mlp_set_dataset(tmc_mlp* n, const float* x, const float* y, int64_t rows
 }
 
 // one gradient pass over `batch` rows of X/Y from row `offset` (wrapping at
-// `rows`), added into n->g and its loss into n->d_loss
-static void launch_gradient(tmc_mlp* n, const float* X, const float* Y, long long rows, long long offset, long long batch) {
+// `rows`), added into n->g and its loss into *loss (device)
+static void launch_gradient(tmc_mlp* n, const float* X, const float* Y, long long rows, long long offset, long long batch,
+                            double* loss) {
   const float inv_batch = 1.f / (float)batch;
   if (n->train_tc) {
     const long long ntiles = batch / kTile;
     const int grid = (int)std::min<long long>(ntiles, (long long)n->sms);
-    k_mlp_train_tc<<<grid, kTrTile, kSmemTrain, n->st>>>(n->net(), TrainSrc{X, Y, rows, offset, n->yscale}, ntiles,
+    k_mlp_train_tc<<<grid, kTrThreads, kSmemTrain, n->st>>>(n->net(), TrainSrc{X, Y, rows, offset, n->yscale}, ntiles,
                                                           inv_batch, n->part, n->ploss, n->d_err);
-    k_grad_reduce<<<(kParams + 255) / 256, 256, 0, n->st>>>(n->part, n->ploss, grid, n->g, n->d_loss);
+    k_grad_reduce<<<(kParams + 255) / 256, 256, 0, n->st>>>(n->part, n->ploss, grid, n->g, loss);
   } else {
     k_mlp_train<<<(unsigned)(batch / kTile), kTile, sizeof(TrainSmem), n->st>>>(n->net(), X, Y, rows, offset,
-                                                                                inv_batch, n->g, n->d_loss);
+                                                                                inv_batch, n->g, loss);
   }
 }
 
@@ -774,21 +789,31 @@ int tmc_mlp_set_train_mode(tmc_mlp* n, int32_t tensor_cores) {
 int tmc_mlp_train(tmc_mlp* n, int32_t batch, int32_t steps, float lr, float* losses) {
   if (!n || batch <= 0 || batch % kTile != 0 || steps < 0) return n ? n->fail(TMC_E_ARG, "batch must be a positive multiple of 128") : TMC_E_ARG;
   if (!n->dx) return n->fail(TMC_E_STATE, "tmc_mlp_train: no dataset");
+  // the steps' losses stay on the device until the last step: no host round
+  // trip between steps
+  if (losses && steps > n->losses_cap) {
+    cudaFree(n->d_losses);
+    n->d_losses = nullptr;
+    n->losses_cap = 0;
+    if (cudaMalloc(&n->d_losses, sizeof(double) * steps) != cudaSuccess) return n->check("tmc_mlp_train");
+    n->losses_cap = steps;
+  }
   cudaMemsetAsync(n->d_err, 0, sizeof(int), n->st);
   for (int s = 0; s < steps; ++s) {
-    cudaMemsetAsync(n->d_loss, 0, sizeof(double), n->st);
-    launch_gradient(n, n->dx, n->dy, n->rows, n->cursor, batch);
+    double* dl = losses ? n->d_losses + s : n->d_loss;
+    cudaMemsetAsync(dl, 0, sizeof(double), n->st);
+    launch_gradient(n, n->dx, n->dy, n->rows, n->cursor, batch, dl);
     n->cursor = (n->cursor + batch) % n->rows;
     n->adam_t += 1;
     const float b1c = 1.f - std::pow(0.9f, (float)n->adam_t), b2c = 1.f - std::pow(0.999f, (float)n->adam_t);
     k_adam<<<(kParams + 255) / 256, 256, 0, n->st>>>(n->p, n->pb, n->g, n->m, n->v, kParams, lr, b1c, b2c,
                                                      n->d_err);
-    if (losses) {
-      double l = 0.0;
-      cudaMemcpyAsync(&l, n->d_loss, sizeof(double), cudaMemcpyDeviceToHost, n->st);
-      if (cudaStreamSynchronize(n->st) != cudaSuccess) return n->check("tmc_mlp_train");
-      losses[s] = (float)l;
-    }
+  }
+  if (losses && steps > 0) {
+    std::vector<double> h(steps);
+    cudaMemcpyAsync(h.data(), n->d_losses, sizeof(double) * steps, cudaMemcpyDeviceToHost, n->st);
+    if (cudaStreamSynchronize(n->st) != cudaSuccess) return n->check("tmc_mlp_train");
+    for (int s = 0; s < steps; ++s) losses[s] = (float)h[s];
   }
   return train_status(n, "tmc_mlp_train");
 }
@@ -803,7 +828,7 @@ int tmc_mlp_gradient(tmc_mlp* n, const float* x, const float* y, int64_t rows, f
   cudaMemsetAsync(n->g, 0, sizeof(float) * kParams, n->st);
   cudaMemsetAsync(n->d_loss, 0, sizeof(double), n->st);
   cudaMemsetAsync(n->d_err, 0, sizeof(int), n->st);
-  launch_gradient(n, n->io_x, n->io_y, rows, 0, rows);
+  launch_gradient(n, n->io_x, n->io_y, rows, 0, rows, n->d_loss);
   cudaMemcpyAsync(grad, n->g, sizeof(float) * kParams, cudaMemcpyDeviceToHost, n->st);
   double l = 0.0;
   cudaMemcpyAsync(&l, n->d_loss, sizeof(double), cudaMemcpyDeviceToHost, n->st);
