@@ -59,7 +59,7 @@ def _ics(level, seeds):
 
 
 def training_data(fine_level=8, coarse_level=6, runs=4, days=1.0, samples_per_run=8, seed0=0, device=0,
-                  log=None, truth="fp64", edge_frac=1.0):
+                  log=None, truth="fp64", edge_frac=1.0, skipped=None):
     """(features [N, 24] float32, targets [N] float32) from fine runs.
 
     truth="fp64": FP64 runs, one at a time.  truth="fp32": all runs as one
@@ -67,7 +67,9 @@ def training_data(fine_level=8, coarse_level=6, runs=4, days=1.0, samples_per_ru
     and vertex state, double-float gd), the way many runs fit the budget;
     its difference from FP64 is measured by `evaluate(truth_check=...)`.
     edge_frac < 1 keeps that fraction of each sample's coarse edges (seeded
-    random subset) to bound the dataset's size."""
+    random subset) to bound the dataset's size.  A run no longer finite at a
+    sample (the dycore has no diffusion) gives no rows there; `skipped`, a
+    list, receives its (run, sample) pairs."""
     fine, coarse = icos_mesh(fine_level), icos_mesh(coarse_level)
     dt_f = level_dt(fine_level)
     steps = max(1, int(round(days * DAY / dt_f / samples_per_run)))
@@ -82,7 +84,8 @@ def training_data(fine_level=8, coarse_level=6, runs=4, days=1.0, samples_per_ru
     cm = TMCoreGPU(coarse, dt=level_dt(coarse_level), precision=abi.TMC_FP32, **kw)
     row = 0
 
-    skipped = []  # (run, sample) of fine states that are no longer finite
+    if skipped is None:
+        skipped = []  # (run, sample) of fine states that are no longer finite
 
     def add_sample(gdf, uf, pvv, ghs_c, r, s):
         nonlocal row
@@ -135,7 +138,6 @@ def training_data(fine_level=8, coarse_level=6, runs=4, days=1.0, samples_per_ru
     if skipped and log:
         runs_lost = sorted({r for r, _ in skipped})
         log(f"{len(skipped)} samples of {len(runs_lost)} runs skipped (state not finite): runs {runs_lost[:20]}")
-    training_data.skipped = skipped
     return X[:row], Y[:row]
 
 
@@ -399,6 +401,8 @@ def main():
     ap.add_argument("--truth-check", type=int, default=0,
                     help="with --truth fp32: members also run in FP64 to measure the truths' difference")
     ap.add_argument("--out", default=None, help="save the trained networks (.npz; the head is appended)")
+    ap.add_argument("--load", default=None,
+                    help="networks saved by --out, comma separated: use them instead of training")
     ap.add_argument("--trainer", choices=("tc", "cuda"), default="tc",
                     help="gradients on the tensor cores (tc) or on the CUDA cores in FP32 (cuda)")
     ap.add_argument("--heads", default="2",
@@ -417,13 +421,18 @@ def main():
     dt = level_dt(a.coarse_level)
     nets, losses, t_train = {}, {}, {}
     t_data, n_samples, skipped = 0.0, 0, []
-    if heads:
+    if a.load:
+        heads = []
+        for path in a.load.split(","):
+            net = load(path)
+            nets[net.head] = net
+            heads.append(net.head)
+    elif heads:
         t0 = time.time()
         X, Y = training_data(a.fine_level, a.coarse_level, a.runs, a.days, a.samples, log=say,
-                             truth=a.train_truth, edge_frac=a.edge_frac)
+                             truth=a.train_truth, edge_frac=a.edge_frac, skipped=skipped)
         t_data = time.time() - t0
         n_samples = int(len(Y))
-        skipped = list(getattr(training_data, "skipped", []))
         for h in heads:
             t0 = time.time()
             net, ls, sc = train(X, Y, steps=a.steps, tensor_cores=a.trainer == "tc", head=h, dt=dt)

@@ -294,30 +294,32 @@ __device__ __forceinline__ void prep(const float (&ia)[V], const float (&g1)[V],
 template <int V>
 __device__ __forceinline__ void ens_cell(const DevMesh& Mh, const Dims& D, const IO& S, const RKStage& rk,
                                          const Partials& P, int diag, int bx) {
-  __shared__ int s_e[kME][kEnsEPB];
-  __shared__ float s_ns[kME][kEnsEPB];
-  __shared__ float s_dv[kME][kEnsEPB];
-  __shared__ float s_ae[kME][kEnsEPB];
-  __shared__ FF s_invA[kEnsEPB];
-  __shared__ FF s_A[kEnsEPB];
-  __shared__ float s_invAf[kEnsEPB];
-  __shared__ float s_Af[kEnsEPB];
+  // A cell's staged stencil as 16-byte records (eight shared-memory loads per
+  // cell and lane instead of about thirty scalar ones); the edge indices are
+  // read before the gathers, the rest only in the arithmetic after them:
+  //   s_ei[j]  = edgesOnCell 0..5 (and two unused)
+  //   s_geo[j] = nSign 0..5, dvEdge 0..5, areaEdge 0..5, 1 / areaCell as FF (h, l)
+  //   s_ar[j]  = {areaCell as FF (h, l), 1 / areaCell, areaCell} (FP32)
+  __shared__ int4 s_ei[kEnsEPB][2];
+  __shared__ float4 s_geo[kEnsEPB][5];
+  __shared__ float4 s_ar[kEnsEPB];
   const int nc = Mh.nc, c0 = bx * kEnsEPB, nel = min(kEnsEPB, nc - c0);
   for (int t = threadIdx.x; t < kME * kEnsEPB; t += blockDim.x) {
     const int i = t / kEnsEPB, j = t - i * kEnsEPB;
     if (j < nel) {
       const size_t k = (size_t)i * nc + c0 + j;
-      s_e[i][j] = Mh.edgesOnCell[k];
-      s_ns[i][j] = (float)Mh.nSign[k];
-      s_dv[i][j] = S.cdv[k];  // dvEdge and areaEdge of the cell's edges, gathered at set-up
-      s_ae[i][j] = S.cae[k];
+      float* const geo = reinterpret_cast<float*>(&s_geo[j][0]);
+      reinterpret_cast<int*>(&s_ei[j][0])[i] = Mh.edgesOnCell[k];
+      geo[i] = (float)Mh.nSign[k];
+      geo[kME + i] = S.cdv[k];  // dvEdge and areaEdge of the cell's edges, gathered at set-up
+      geo[2 * kME + i] = S.cae[k];
     }
   }
   for (int j = threadIdx.x; j < nel; j += blockDim.x) {
-    s_invA[j] = FF{S.invA_hl[c0 + j], S.invA_hl[nc + c0 + j]};
-    s_A[j] = FF{S.A_hl[c0 + j], S.A_hl[nc + c0 + j]};
-    s_invAf[j] = Mh.invAreaCell_f[c0 + j];
-    s_Af[j] = Mh.areaCell_f[c0 + j];
+    float* const geo = reinterpret_cast<float*>(&s_geo[j][0]);
+    geo[3 * kME] = S.invA_hl[c0 + j];
+    geo[3 * kME + 1] = S.invA_hl[nc + c0 + j];
+    s_ar[j] = make_float4(S.A_hl[c0 + j], S.A_hl[nc + c0 + j], Mh.invAreaCell_f[c0 + j], Mh.areaCell_f[c0 + j]);
   }
   __syncthreads();
   const Lane L = lane_of<V>(D);
@@ -341,12 +343,24 @@ __device__ __forceinline__ void ens_cell(const DevMesh& Mh, const Dims& D, const
     ldv<V>(S.ghsf, cm, ghf);
     if (diag) ldv<V>(S.gd_in + ffs, cm, gdl);
     float uu[kME][V], Fv[kME][V];
+    {
+      const int4 a = s_ei[j][0], b = s_ei[j][1];
+      const int ei[kME] = {a.x, a.y, a.z, a.w, b.x, b.y};
 #pragma unroll
-    for (int i = 0; i < kME; ++i) {
-      const size_t k = (size_t)s_e[i][j] * Mm + L.m0;
-      ldv<V>(S.u, k, uu[i]);
-      ldv<V>(S.F, k, Fv[i]);
+      for (int i = 0; i < kME; ++i) {
+        const size_t k = (size_t)ei[i] * Mm + L.m0;
+        ldv<V>(S.u, k, uu[i]);
+        ldv<V>(S.F, k, Fv[i]);
+      }
     }
+    float geo[20];
+#pragma unroll
+    for (int h = 0; h < 5; ++h) {
+      const float4 q = s_geo[j][h];
+      geo[4 * h] = q.x, geo[4 * h + 1] = q.y, geo[4 * h + 2] = q.z, geo[4 * h + 3] = q.w;
+    }
+    const float4 ar = s_ar[j];
+    const FF invA{geo[3 * kME], geo[3 * kME + 1]}, Aff{ar.x, ar.y};
     FF acc_o[V], gnext[V];
     float Eo[V], tT[V];
 #pragma unroll
@@ -354,16 +368,16 @@ __device__ __forceinline__ void ens_cell(const DevMesh& Mh, const Dims& D, const
       float hi = 0.f, lo = 0.f, k = 0.f;
 #pragma unroll
       for (int i = 0; i < kME; ++i) {
-        const float ns = s_ns[i][j];
-        two_sum_acc(hi, lo, __fmul_rn(__fmul_rn(ns, Fv[i][c]), s_dv[i][j]));
-        k += fabsf(ns) * uu[i][c] * uu[i][c] * s_ae[i][j];
+        const float ns = geo[i];
+        two_sum_acc(hi, lo, __fmul_rn(__fmul_rn(ns, Fv[i][c]), geo[kME + i]));
+        k += fabsf(ns) * uu[i][c] * uu[i][c] * geo[2 * kME + i];
       }
       // gd tendency t = -(flux divergence) / areaCell
-      FF t = ff_mul(ff_two_sum(hi, lo), s_invA[j]);
+      FF t = ff_mul(ff_two_sum(hi, lo), invA);
       t = FF{-t.h, -t.l};
       tT[c] = t.h;
-      Eo[c] = k * 0.25f * s_invAf[j] + gdf[c] + ghf[c];
-      const float Af = s_Af[j];
+      Eo[c] = k * 0.25f * ar.z + gdf[c] + ghf[c];
+      const float Af = ar.w;
       gnext[c] = FF{0.f, 0.f};
       switch (mode) {
         case 0:  // E only (the closure's features of a state)
@@ -390,7 +404,7 @@ __device__ __forceinline__ void ens_cell(const DevMesh& Mh, const Dims& D, const
         // total mass from the FF gd (FF products, FF sum), and the cell part
         // of the total energy (gd^2 + 2 gd ghs) areaCell from FP32 terms,
         // compensated (tmcore_swm_mod.F90:215-231)
-        mass[c] = ff_add(mass[c], ff_mul(FF{gdf[c], gdl[c]}, s_A[j]));
+        mass[c] = ff_add(mass[c], ff_mul(FF{gdf[c], gdl[c]}, Aff));
         two_sum_acc(eh[c], el[c], gdf[c] * (gdf[c] + 2.f * ghf[c]) * Af);
       }
     }
@@ -465,30 +479,32 @@ template <int V>
 __device__ __forceinline__ void ens_vertex(const DevMesh& Mh, const Dims& D, const IO& S, const Partials& P, int diag,
                                            int bx) {
   constexpr int kVU = TMC_ENS_VU;  // vertices per warp iteration (their loads first)
-  __shared__ int s_c[3][kEnsEPB];
-  __shared__ int s_e[3][kEnsEPB];
-  __shared__ float s_kt[3][kEnsEPB];
-  __shared__ float s_ts[3][kEnsEPB];  // tSign
-  __shared__ float s_dc[3][kEnsEPB];  // dcEdge of the vertex's edges
-  __shared__ float s_iA[kEnsEPB];
-  __shared__ float s_f[kEnsEPB];
-  __shared__ float s_At[kEnsEPB];
+  // A vertex's staged stencil as five 16-byte records, so a lane reads it with
+  // five shared-memory loads instead of eighteen scalar ones:
+  //   s_ix[j] = {cell 0, cell 1, cell 2, edge 0}, {edge 1, edge 2, -, -}
+  //   s_w[j]  = {kite 0, kite 1, kite 2, tSign 0}, {tSign 1, tSign 2, dcEdge 0, dcEdge 1},
+  //             {dcEdge 2, 1 / areaTriangle, fVertex, areaTriangle}
+  __shared__ int4 s_ix[kEnsEPB][2];
+  __shared__ float4 s_w[kEnsEPB][3];
   const int nv = Mh.nv, v0 = bx * kEnsEPB, nel = min(kEnsEPB, nv - v0);
   for (int t = threadIdx.x; t < 3 * kEnsEPB; t += blockDim.x) {
     const int i = t / kEnsEPB, j = t - i * kEnsEPB;
     if (j < nel) {
       const size_t k = (size_t)i * nv + v0 + j;
-      s_c[i][j] = Mh.cellsOnVertex[k];
-      s_e[i][j] = Mh.edgesOnVertex[k];
-      s_kt[i][j] = Mh.kite_f[k];
-      s_ts[i][j] = (float)Mh.tSign[k];
-      s_dc[i][j] = S.vdc[k];  // dcEdge of the vertex's edges, gathered at set-up
+      int* const ix = reinterpret_cast<int*>(&s_ix[j][0]);
+      float* const w = reinterpret_cast<float*>(&s_w[j][0]);
+      ix[i] = Mh.cellsOnVertex[k];
+      ix[3 + i] = Mh.edgesOnVertex[k];
+      w[i] = Mh.kite_f[k];
+      w[3 + i] = (float)Mh.tSign[k];
+      w[6 + i] = S.vdc[k];  // dcEdge of the vertex's edges, gathered at set-up
     }
   }
   for (int j = threadIdx.x; j < nel; j += blockDim.x) {
-    s_iA[j] = Mh.invAreaTriangle_f[v0 + j];
-    s_f[j] = Mh.fVertex_f[v0 + j];
-    s_At[j] = (float)Mh.areaTriangle[v0 + j];
+    float* const w = reinterpret_cast<float*>(&s_w[j][0]);
+    w[9] = Mh.invAreaTriangle_f[v0 + j];
+    w[10] = Mh.fVertex_f[v0 + j];
+    w[11] = (float)Mh.areaTriangle[v0 + j];
   }
   __syncthreads();
   const Lane L = lane_of<V>(D);
@@ -501,31 +517,34 @@ __device__ __forceinline__ void ens_vertex(const DevMesh& Mh, const Dims& D, con
 #pragma unroll
     for (int q = 0; q < kVU; ++q) {
       const int j = min(base + q * L.js, nel - 1);
+      const int4 a = s_ix[j][0], b = s_ix[j][1];
+      const int cv[3] = {a.x, a.y, a.z}, ev[3] = {a.w, b.x, b.y};
 #pragma unroll
       for (int i = 0; i < 3; ++i) {
-        ldv<V>(S.gd_in, (size_t)s_c[i][j] * Mm + L.m0, g[q][i]);
-        ldv<V>(S.u, (size_t)s_e[i][j] * Mm + L.m0, uu[q][i]);
+        ldv<V>(S.gd_in, (size_t)cv[i] * Mm + L.m0, g[q][i]);
+        ldv<V>(S.u, (size_t)ev[i] * Mm + L.m0, uu[q][i]);
       }
     }
 #pragma unroll
     for (int q = 0; q < kVU; ++q) {
       const int j = base + q * L.js;
       if (j >= nel) break;
-      const float iA = s_iA[j];
+      const float4 w0 = s_w[j][0], w1 = s_w[j][1], w2 = s_w[j][2];
+      const float kt[3] = {w0.x, w0.y, w0.z}, ts[3] = {w0.w, w1.x, w1.y}, dc[3] = {w1.z, w1.w, w2.x};
+      const float iA = w2.y, fv = w2.z, At = w2.w;
       float pv[V], vo[V], gv[V];
 #pragma unroll
       for (int c = 0; c < V; ++c) {
-        gv[c] = (g[q][0][c] * s_kt[0][j] + g[q][1][c] * s_kt[1][j] + g[q][2][c] * s_kt[2][j]) * iA;
-        const float sv = s_ts[0][j] * uu[q][0][c] * s_dc[0][j] + s_ts[1][j] * uu[q][1][c] * s_dc[1][j] +
-                         s_ts[2][j] * uu[q][2][c] * s_dc[2][j];
+        gv[c] = (g[q][0][c] * kt[0] + g[q][1][c] * kt[1] + g[q][2][c] * kt[2]) * iA;
+        const float sv = ts[0] * uu[q][0][c] * dc[0] + ts[1] * uu[q][1][c] * dc[1] + ts[2] * uu[q][2][c] * dc[2];
         vo[c] = -sv * iA;
-        pv[c] = (s_f[j] + vo[c]) / gv[c];
+        pv[c] = (fv + vo[c]) / gv[c];
         if (diag) {
           // potential enstrophy and absolute vorticity (tmcore_swm_mod.F90:233-255),
           // FP32 terms, compensated; vorticity and f as separate terms
-          two_sum_acc(ph[c], pl[c], gv[c] * (pv[c] * pv[c]) * s_At[j]);
-          two_sum_acc(ah[c], al[c], vo[c] * s_At[j]);
-          two_sum_acc(ah[c], al[c], s_f[j] * s_At[j]);
+          two_sum_acc(ph[c], pl[c], gv[c] * (pv[c] * pv[c]) * At);
+          two_sum_acc(ah[c], al[c], vo[c] * At);
+          two_sum_acc(ah[c], al[c], fv * At);
         }
       }
       const size_t vm = (size_t)(v0 + j) * Mm + L.m0;
@@ -682,27 +701,32 @@ __global__ void __launch_bounds__(kMaxBS) k_ens_edge_pv_up(DevMesh Mh, Dims D, I
 template <int V>
 __device__ __forceinline__ void ens_edge_flux(const DevMesh& Mh, const Dims& D, const IO& S, const RKStage& rk,
                                               const Partials& P, int bx) {
-  __shared__ int s_ep[kME2][kEnsEPB];
-  __shared__ float s_w[kME2][kEnsEPB];
-  __shared__ int s_c[2][kEnsEPB];
-  __shared__ float s_dc[kEnsEPB];
-  __shared__ float s_ae[kEnsEPB];
+  // An edge's staged stencil as 16-byte records (a lane reads it with seven
+  // shared-memory loads instead of twenty-four scalar ones): the indices are
+  // read before the gathers, the weights only in the arithmetic after them,
+  // so the weights hold no registers while the gathers are in flight.
+  //   s_ei[j] = edgesOnEdge 0..9 (and two unused), s_wf[j] = their weights
+  //   s_cd[j] = {cell 1, cell 2, dcEdge, areaEdge}
+  constexpr int kQ = (kME2 + 3) / 4;
+  __shared__ int4 s_ei[kEnsEPB][kQ];
+  __shared__ float4 s_wf[kEnsEPB][kQ];
+  __shared__ int4 s_cd[kEnsEPB];
   const int ne = Mh.ne, e0 = bx * kEnsEPB, nel = min(kEnsEPB, ne - e0);
   for (int t = threadIdx.x; t < kME2 * kEnsEPB; t += blockDim.x) {
     const int i = t / kEnsEPB, j = t - i * kEnsEPB;
     if (j < nel) {
       const size_t k = (size_t)i * ne + e0 + j;
-      s_ep[i][j] = Mh.edgesOnEdge[k];  // padded entries: the edge itself, weight 0
-      s_w[i][j] = Mh.weightsOnEdge_f[k];
+      reinterpret_cast<int*>(&s_ei[j][0])[i] = Mh.edgesOnEdge[k];  // padded entries: the edge itself, weight 0
+      reinterpret_cast<float*>(&s_wf[j][0])[i] = Mh.weightsOnEdge_f[k];
     }
   }
   for (int t = threadIdx.x; t < 2 * kEnsEPB; t += blockDim.x) {
     const int i = t / kEnsEPB, j = t - i * kEnsEPB;
-    if (j < nel) s_c[i][j] = Mh.cellsOnEdge[(size_t)i * ne + e0 + j];
+    if (j < nel) reinterpret_cast<int*>(&s_cd[j])[i] = Mh.cellsOnEdge[(size_t)i * ne + e0 + j];
   }
   for (int j = threadIdx.x; j < nel; j += blockDim.x) {
-    s_dc[j] = Mh.dcEdge_f[e0 + j];
-    s_ae[j] = Mh.areaEdge_f[e0 + j];
+    s_cd[j].z = __float_as_int(Mh.dcEdge_f[e0 + j]);
+    s_cd[j].w = __float_as_int(Mh.areaEdge_f[e0 + j]);
   }
   __syncthreads();
   const Lane L = lane_of<V>(D);
@@ -715,7 +739,8 @@ __device__ __forceinline__ void ens_edge_flux(const DevMesh& Mh, const Dims& D, 
   for (int c = 0; c < V; ++c) rip[c] = r44[c] = 0.f;
   for (int j = L.j0; j < nel; j += L.js) {
     const size_t em = (size_t)(e0 + j) * Mm + L.m0;
-    const size_t c1m = (size_t)s_c[0][j] * Mm + L.m0, c2m = (size_t)s_c[1][j] * Mm + L.m0;
+    const int4 cd = s_cd[j];
+    const size_t c1m = (size_t)cd.x * Mm + L.m0, c2m = (size_t)cd.y * Mm + L.m0;
     float pe[V], uu[V], ge[V], tp[V], accv[V], oldv[V], gn1[V], gn2[V], E1[V], E2[V], t1[V], t2[V];
     ldv<V>(S.pv_e, em, pe);
     ldv<V>(S.u, em, uu);
@@ -734,19 +759,31 @@ __device__ __forceinline__ void ens_edge_flux(const DevMesh& Mh, const Dims& D, 
     ldv<V>(S.tendf, c1m, t1);
     ldv<V>(S.tendf, c2m, t2);
     float Fv[kME2][V], pp[kME2][V];
+    int ei[4 * kQ];
+#pragma unroll
+    for (int h = 0; h < kQ; ++h) {
+      const int4 q = s_ei[j][h];
+      ei[4 * h] = q.x, ei[4 * h + 1] = q.y, ei[4 * h + 2] = q.z, ei[4 * h + 3] = q.w;
+    }
 #pragma unroll
     for (int i = 0; i < kME2; ++i) {
-      const size_t k = (size_t)s_ep[i][j] * Mm + L.m0;
+      const size_t k = (size_t)ei[i] * Mm + L.m0;
       ldv<V>(S.F, k, Fv[i]);
       ldv<V>(S.pv_e, k, pp[i]);
     }
-    const float dc = s_dc[j], ae = s_ae[j];
+    float wv[4 * kQ];
+#pragma unroll
+    for (int h = 0; h < kQ; ++h) {
+      const float4 q = s_wf[j][h];
+      wv[4 * h] = q.x, wv[4 * h + 1] = q.y, wv[4 * h + 2] = q.z, wv[4 * h + 3] = q.w;
+    }
+    const float dc = __int_as_float(cd.z), ae = __int_as_float(cd.w);
     float acc_o[V], it_o[V], inext[V];
 #pragma unroll
     for (int c = 0; c < V; ++c) {
       float s = 0.f;
 #pragma unroll
-      for (int i = 0; i < kME2; ++i) s += s_w[i][j] * Fv[i][c] * (0.5f * (pe[c] + pp[i][c]));
+      for (int i = 0; i < kME2; ++i) s += wv[i] * Fv[i][c] * (0.5f * (pe[c] + pp[i][c]));
       const float dEdx = (E2[c] - E1[c]) / dc;
       const float tge = 0.5f * (t1[c] + t2[c]);
       const float ut = s - dEdx;
