@@ -294,32 +294,30 @@ __device__ __forceinline__ void prep(const float (&ia)[V], const float (&g1)[V],
 template <int V>
 __device__ __forceinline__ void ens_cell(const DevMesh& Mh, const Dims& D, const IO& S, const RKStage& rk,
                                          const Partials& P, int diag, int bx) {
-  // A cell's staged stencil as 16-byte records (eight shared-memory loads per
-  // cell and lane instead of about thirty scalar ones); the edge indices are
-  // read before the gathers, the rest only in the arithmetic after them:
-  //   s_ei[j]  = edgesOnCell 0..5 (and two unused)
-  //   s_geo[j] = nSign 0..5, dvEdge 0..5, areaEdge 0..5, 1 / areaCell as FF (h, l)
-  //   s_ar[j]  = {areaCell as FF (h, l), 1 / areaCell, areaCell} (FP32)
-  __shared__ int4 s_ei[kEnsEPB][2];
-  __shared__ float4 s_geo[kEnsEPB][5];
-  __shared__ float4 s_ar[kEnsEPB];
+  __shared__ int s_e[kME][kEnsEPB];
+  __shared__ float s_ns[kME][kEnsEPB];
+  __shared__ float s_dv[kME][kEnsEPB];
+  __shared__ float s_ae[kME][kEnsEPB];
+  __shared__ FF s_invA[kEnsEPB];
+  __shared__ FF s_A[kEnsEPB];
+  __shared__ float s_invAf[kEnsEPB];
+  __shared__ float s_Af[kEnsEPB];
   const int nc = Mh.nc, c0 = bx * kEnsEPB, nel = min(kEnsEPB, nc - c0);
   for (int t = threadIdx.x; t < kME * kEnsEPB; t += blockDim.x) {
     const int i = t / kEnsEPB, j = t - i * kEnsEPB;
     if (j < nel) {
       const size_t k = (size_t)i * nc + c0 + j;
-      float* const geo = reinterpret_cast<float*>(&s_geo[j][0]);
-      reinterpret_cast<int*>(&s_ei[j][0])[i] = Mh.edgesOnCell[k];
-      geo[i] = (float)Mh.nSign[k];
-      geo[kME + i] = S.cdv[k];  // dvEdge and areaEdge of the cell's edges, gathered at set-up
-      geo[2 * kME + i] = S.cae[k];
+      s_e[i][j] = Mh.edgesOnCell[k];
+      s_ns[i][j] = (float)Mh.nSign[k];
+      s_dv[i][j] = S.cdv[k];  // dvEdge and areaEdge of the cell's edges, gathered at set-up
+      s_ae[i][j] = S.cae[k];
     }
   }
   for (int j = threadIdx.x; j < nel; j += blockDim.x) {
-    float* const geo = reinterpret_cast<float*>(&s_geo[j][0]);
-    geo[3 * kME] = S.invA_hl[c0 + j];
-    geo[3 * kME + 1] = S.invA_hl[nc + c0 + j];
-    s_ar[j] = make_float4(S.A_hl[c0 + j], S.A_hl[nc + c0 + j], Mh.invAreaCell_f[c0 + j], Mh.areaCell_f[c0 + j]);
+    s_invA[j] = FF{S.invA_hl[c0 + j], S.invA_hl[nc + c0 + j]};
+    s_A[j] = FF{S.A_hl[c0 + j], S.A_hl[nc + c0 + j]};
+    s_invAf[j] = Mh.invAreaCell_f[c0 + j];
+    s_Af[j] = Mh.areaCell_f[c0 + j];
   }
   __syncthreads();
   const Lane L = lane_of<V>(D);
@@ -343,24 +341,12 @@ __device__ __forceinline__ void ens_cell(const DevMesh& Mh, const Dims& D, const
     ldv<V>(S.ghsf, cm, ghf);
     if (diag) ldv<V>(S.gd_in + ffs, cm, gdl);
     float uu[kME][V], Fv[kME][V];
-    {
-      const int4 a = s_ei[j][0], b = s_ei[j][1];
-      const int ei[kME] = {a.x, a.y, a.z, a.w, b.x, b.y};
 #pragma unroll
-      for (int i = 0; i < kME; ++i) {
-        const size_t k = (size_t)ei[i] * Mm + L.m0;
-        ldv<V>(S.u, k, uu[i]);
-        ldv<V>(S.F, k, Fv[i]);
-      }
+    for (int i = 0; i < kME; ++i) {
+      const size_t k = (size_t)s_e[i][j] * Mm + L.m0;
+      ldv<V>(S.u, k, uu[i]);
+      ldv<V>(S.F, k, Fv[i]);
     }
-    float geo[20];
-#pragma unroll
-    for (int h = 0; h < 5; ++h) {
-      const float4 q = s_geo[j][h];
-      geo[4 * h] = q.x, geo[4 * h + 1] = q.y, geo[4 * h + 2] = q.z, geo[4 * h + 3] = q.w;
-    }
-    const float4 ar = s_ar[j];
-    const FF invA{geo[3 * kME], geo[3 * kME + 1]}, Aff{ar.x, ar.y};
     FF acc_o[V], gnext[V];
     float Eo[V], tT[V];
 #pragma unroll
@@ -368,16 +354,16 @@ __device__ __forceinline__ void ens_cell(const DevMesh& Mh, const Dims& D, const
       float hi = 0.f, lo = 0.f, k = 0.f;
 #pragma unroll
       for (int i = 0; i < kME; ++i) {
-        const float ns = geo[i];
-        two_sum_acc(hi, lo, __fmul_rn(__fmul_rn(ns, Fv[i][c]), geo[kME + i]));
-        k += fabsf(ns) * uu[i][c] * uu[i][c] * geo[2 * kME + i];
+        const float ns = s_ns[i][j];
+        two_sum_acc(hi, lo, __fmul_rn(__fmul_rn(ns, Fv[i][c]), s_dv[i][j]));
+        k += fabsf(ns) * uu[i][c] * uu[i][c] * s_ae[i][j];
       }
       // gd tendency t = -(flux divergence) / areaCell
-      FF t = ff_mul(ff_two_sum(hi, lo), invA);
+      FF t = ff_mul(ff_two_sum(hi, lo), s_invA[j]);
       t = FF{-t.h, -t.l};
       tT[c] = t.h;
-      Eo[c] = k * 0.25f * ar.z + gdf[c] + ghf[c];
-      const float Af = ar.w;
+      Eo[c] = k * 0.25f * s_invAf[j] + gdf[c] + ghf[c];
+      const float Af = s_Af[j];
       gnext[c] = FF{0.f, 0.f};
       switch (mode) {
         case 0:  // E only (the closure's features of a state)
@@ -404,7 +390,7 @@ __device__ __forceinline__ void ens_cell(const DevMesh& Mh, const Dims& D, const
         // total mass from the FF gd (FF products, FF sum), and the cell part
         // of the total energy (gd^2 + 2 gd ghs) areaCell from FP32 terms,
         // compensated (tmcore_swm_mod.F90:215-231)
-        mass[c] = ff_add(mass[c], ff_mul(FF{gdf[c], gdl[c]}, Aff));
+        mass[c] = ff_add(mass[c], ff_mul(FF{gdf[c], gdl[c]}, s_A[j]));
         two_sum_acc(eh[c], el[c], gdf[c] * (gdf[c] + 2.f * ghf[c]) * Af);
       }
     }
@@ -701,32 +687,27 @@ __global__ void __launch_bounds__(kMaxBS) k_ens_edge_pv_up(DevMesh Mh, Dims D, I
 template <int V>
 __device__ __forceinline__ void ens_edge_flux(const DevMesh& Mh, const Dims& D, const IO& S, const RKStage& rk,
                                               const Partials& P, int bx) {
-  // An edge's staged stencil as 16-byte records (a lane reads it with seven
-  // shared-memory loads instead of twenty-four scalar ones): the indices are
-  // read before the gathers, the weights only in the arithmetic after them,
-  // so the weights hold no registers while the gathers are in flight.
-  //   s_ei[j] = edgesOnEdge 0..9 (and two unused), s_wf[j] = their weights
-  //   s_cd[j] = {cell 1, cell 2, dcEdge, areaEdge}
-  constexpr int kQ = (kME2 + 3) / 4;
-  __shared__ int4 s_ei[kEnsEPB][kQ];
-  __shared__ float4 s_wf[kEnsEPB][kQ];
-  __shared__ int4 s_cd[kEnsEPB];
+  __shared__ int s_ep[kME2][kEnsEPB];
+  __shared__ float s_w[kME2][kEnsEPB];
+  __shared__ int s_c[2][kEnsEPB];
+  __shared__ float s_dc[kEnsEPB];
+  __shared__ float s_ae[kEnsEPB];
   const int ne = Mh.ne, e0 = bx * kEnsEPB, nel = min(kEnsEPB, ne - e0);
   for (int t = threadIdx.x; t < kME2 * kEnsEPB; t += blockDim.x) {
     const int i = t / kEnsEPB, j = t - i * kEnsEPB;
     if (j < nel) {
       const size_t k = (size_t)i * ne + e0 + j;
-      reinterpret_cast<int*>(&s_ei[j][0])[i] = Mh.edgesOnEdge[k];  // padded entries: the edge itself, weight 0
-      reinterpret_cast<float*>(&s_wf[j][0])[i] = Mh.weightsOnEdge_f[k];
+      s_ep[i][j] = Mh.edgesOnEdge[k];  // padded entries: the edge itself, weight 0
+      s_w[i][j] = Mh.weightsOnEdge_f[k];
     }
   }
   for (int t = threadIdx.x; t < 2 * kEnsEPB; t += blockDim.x) {
     const int i = t / kEnsEPB, j = t - i * kEnsEPB;
-    if (j < nel) reinterpret_cast<int*>(&s_cd[j])[i] = Mh.cellsOnEdge[(size_t)i * ne + e0 + j];
+    if (j < nel) s_c[i][j] = Mh.cellsOnEdge[(size_t)i * ne + e0 + j];
   }
   for (int j = threadIdx.x; j < nel; j += blockDim.x) {
-    s_cd[j].z = __float_as_int(Mh.dcEdge_f[e0 + j]);
-    s_cd[j].w = __float_as_int(Mh.areaEdge_f[e0 + j]);
+    s_dc[j] = Mh.dcEdge_f[e0 + j];
+    s_ae[j] = Mh.areaEdge_f[e0 + j];
   }
   __syncthreads();
   const Lane L = lane_of<V>(D);
@@ -739,8 +720,7 @@ __device__ __forceinline__ void ens_edge_flux(const DevMesh& Mh, const Dims& D, 
   for (int c = 0; c < V; ++c) rip[c] = r44[c] = 0.f;
   for (int j = L.j0; j < nel; j += L.js) {
     const size_t em = (size_t)(e0 + j) * Mm + L.m0;
-    const int4 cd = s_cd[j];
-    const size_t c1m = (size_t)cd.x * Mm + L.m0, c2m = (size_t)cd.y * Mm + L.m0;
+    const size_t c1m = (size_t)s_c[0][j] * Mm + L.m0, c2m = (size_t)s_c[1][j] * Mm + L.m0;
     float pe[V], uu[V], ge[V], tp[V], accv[V], oldv[V], gn1[V], gn2[V], E1[V], E2[V], t1[V], t2[V];
     ldv<V>(S.pv_e, em, pe);
     ldv<V>(S.u, em, uu);
@@ -759,31 +739,19 @@ __device__ __forceinline__ void ens_edge_flux(const DevMesh& Mh, const Dims& D, 
     ldv<V>(S.tendf, c1m, t1);
     ldv<V>(S.tendf, c2m, t2);
     float Fv[kME2][V], pp[kME2][V];
-    int ei[4 * kQ];
-#pragma unroll
-    for (int h = 0; h < kQ; ++h) {
-      const int4 q = s_ei[j][h];
-      ei[4 * h] = q.x, ei[4 * h + 1] = q.y, ei[4 * h + 2] = q.z, ei[4 * h + 3] = q.w;
-    }
 #pragma unroll
     for (int i = 0; i < kME2; ++i) {
-      const size_t k = (size_t)ei[i] * Mm + L.m0;
+      const size_t k = (size_t)s_ep[i][j] * Mm + L.m0;
       ldv<V>(S.F, k, Fv[i]);
       ldv<V>(S.pv_e, k, pp[i]);
     }
-    float wv[4 * kQ];
-#pragma unroll
-    for (int h = 0; h < kQ; ++h) {
-      const float4 q = s_wf[j][h];
-      wv[4 * h] = q.x, wv[4 * h + 1] = q.y, wv[4 * h + 2] = q.z, wv[4 * h + 3] = q.w;
-    }
-    const float dc = __int_as_float(cd.z), ae = __int_as_float(cd.w);
+    const float dc = s_dc[j], ae = s_ae[j];
     float acc_o[V], it_o[V], inext[V];
 #pragma unroll
     for (int c = 0; c < V; ++c) {
       float s = 0.f;
 #pragma unroll
-      for (int i = 0; i < kME2; ++i) s += wv[i] * Fv[i][c] * (0.5f * (pe[c] + pp[i][c]));
+      for (int i = 0; i < kME2; ++i) s += s_w[i][j] * Fv[i][c] * (0.5f * (pe[c] + pp[i][c]));
       const float dEdx = (E2[c] - E1[c]) / dc;
       const float tge = 0.5f * (t1[c] + t2[c]);
       const float ut = s - dEdx;
