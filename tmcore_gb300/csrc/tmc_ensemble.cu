@@ -28,6 +28,13 @@
 #ifndef TMC_ENS_VERT_MINB
 #define TMC_ENS_VERT_MINB 1
 #endif
+// with one member per lane the flux pass needs 69 registers; a minimum of 4
+// resident blocks of 256 threads caps it at 64 without spills: 16 level-7
+// members 121.1 against 125.6 us per launch (the cell pass, capped the same
+// way from 66 registers, went from 52.5 to 54.6 us and is not capped)
+#ifndef TMC_ENS_MINB_V1
+#define TMC_ENS_MINB_V1 4
+#endif
 // vertices per warp iteration of the vertex pass (512 level-6 members:
 // 2 -> 4.85 ms per step, 1 -> 4.86, 4 -> 4.89)
 #ifndef TMC_ENS_VU
@@ -794,7 +801,8 @@ __device__ __forceinline__ void ens_edge_flux(const DevMesh& Mh, const Dims& D, 
   }
 }
 template <int V>
-__global__ void TMC_ENS_LB(TMC_ENS_FLUX_MINB) k_ens_edge_flux(DevMesh Mh, Dims D, IO S, RKStage rk, Partials P) {
+__global__ void __launch_bounds__(256, V == 1 ? TMC_ENS_MINB_V1 : TMC_ENS_FLUX_MINB)
+    k_ens_edge_flux(DevMesh Mh, Dims D, IO S, RKStage rk, Partials P) {
   ens_edge_flux<V>(Mh, D, S, rk, P, blockIdx.x);
 }
 
