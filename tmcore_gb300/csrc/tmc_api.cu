@@ -1280,6 +1280,7 @@ int tmc_create(const tmc_mesh_desc* mesh, const tmc_params* params, tmc_handle**
   const int minbs = 32;
   h->P.cap = (nmax + minbs - 1) / minbs;
   h->P.base = h->dalloc<double>(h->P.member_stride() * h->members);
+  h->P.fin = h->dalloc<double>((size_t)kFinalizeRegions * kFinSplit * 2 * h->members);
   for (int k = 0; k < P_COUNT; ++k) h->bsp[k] = h->bs;
   // the FP32 cell pass is compiled for at most 256 threads per block (its
   // register budget leaves room for 3 blocks per SM)
@@ -1291,7 +1292,7 @@ int tmc_create(const tmc_mesh_desc* mesh, const tmc_params* params, tmc_handle**
     for (int r = R_MASS; r <= R_AV; ++r) h->gen_counts[r] = bc;
   h->d_diag = h->dalloc<double>((size_t)kDiagStride * h->members);  // per member: outputs, region sums, counters
   if (cudaMallocHost(&h->h_diag, sizeof(double) * kDiagLen) != cudaSuccess) h->h_diag = nullptr;
-  if (!h->d_diag || !h->h_diag || !h->P.base) {
+  if (!h->d_diag || !h->h_diag || !h->P.base || !h->P.fin) {
     h->err = "device allocation failed";
     cudaGetLastError();
     *out = h.release();

@@ -132,13 +132,18 @@ enum Region {
   R_COUNT = 16
 };
 constexpr int kFinalizeRegions = R_C1;  // regions k_finalize reduces
+constexpr int kFinSplit = 16;            // blocks of k_finalize per region
 
 struct Partials {
   double* base;  // [member][R_COUNT][cap][2]
   int cap;
+  double* fin;   // [member][kFinalizeRegions][kFinSplit][2]: k_finalize's sums of one block's slots
   __host__ __device__ double* region(int r) const { return base + (size_t)r * cap * 2; }
   __host__ __device__ size_t member_stride() const { return (size_t)R_COUNT * cap * 2; }
-  __host__ __device__ Partials at(int m) const { return Partials{base + (size_t)m * member_stride(), cap}; }
+  __host__ __device__ Partials at(int m) const {
+    return Partials{base + (size_t)m * member_stride(), cap,
+                    fin ? fin + (size_t)m * kFinalizeRegions * kFinSplit * 2 : nullptr};
+  }
 };
 
 // device results: [0] mass [1] energy [2] enstrophy [3] abs vort [4] beta

@@ -14,9 +14,9 @@ struct FinalizeArgs {
   int step, diag, conserve, scheme;
 };
 
-// Fixed-order double-double sum of one region's per-block partials, by one
-// block; lane 0 of warp 0 returns it.
-__device__ double region_sum_dd(const double* reg, int count) {
+// Fixed-order double-double sum of `count` per-block partials (hi, lo pairs),
+// by one block; lane 0 of warp 0 returns it.
+__device__ DD region_sum_pair(const double* reg, int count) {
   double hi = 0.0, lo = 0.0;
   for (int i = threadIdx.x; i < count; i += blockDim.x) {
     hi = __dadd_rn(hi, reg[2 * i]);
@@ -27,20 +27,25 @@ __device__ double region_sum_dd(const double* reg, int count) {
   DD w = warp_reduce_dd(DD{hi, lo});
   if (lane == 0) sm[warp] = w;
   __syncthreads();
-  double r = 0.0;
   if (warp == 0) {
     w = (lane < nw) ? sm[lane] : DD{0.0, 0.0};
     w = warp_reduce_dd(w);
-    r = w.hi + w.lo;
   }
-  return r;
+  return w;
+}
+__device__ double region_sum_dd(const double* reg, int count) {
+  const DD w = region_sum_pair(reg, count);
+  return w.hi + w.lo;
 }
 
-// One block per partial region: a fixed-order double-double reduction of the
-// region's per-block partials; the last block to finish (atomic counter, no
-// waiting) combines the region sums into beta and the invariants
-// (time_scheme_mod.F90:144-150; tmcore_swm_mod.F90:215-255) and re-arms the
-// counter.
+// kFinSplit blocks per partial region, each a fixed-order double-double
+// reduction of a contiguous 1/kFinSplit of the region's per-block partials
+// into P.fin; the last block to finish (atomic counter, no waiting) combines
+// each region's kFinSplit sums in order (one thread per region), then the
+// region sums into beta and the invariants (time_scheme_mod.F90:144-150;
+// tmcore_swm_mod.F90:215-255), and re-arms the counter.  With one block per
+// region the widest region (15,360 partials at level 9) cost ~15,000 cycles
+// of one SM's 2-lane FP64 pipe, and the launch 28 us.
 __global__ void __launch_bounds__(256) k_finalize(Partials P0, FinalizeArgs a, double* out0, double* res0,
                                                   unsigned int* counter0) {
   // one member per blockIdx.y: its partials, outputs, region sums and counter
@@ -49,11 +54,16 @@ __global__ void __launch_bounds__(256) k_finalize(Partials P0, FinalizeArgs a, d
   double* res = res0 + (size_t)blockIdx.y * kDiagStride;
   unsigned int* counter = reinterpret_cast<unsigned int*>(reinterpret_cast<double*>(counter0) +
                                                           (size_t)blockIdx.y * kDiagStride);
-  const int r = blockIdx.x;
+  const int r = blockIdx.x / kFinSplit, part = blockIdx.x - r * kFinSplit;
   const bool want = (r <= R_44_E) ? a.step : a.diag;
   if (want) {
-    const double v = region_sum_dd(P.region(r), a.counts[r]);
-    if (threadIdx.x == 0) res[r] = v;
+    const int count = a.counts[r], chunk = (count + kFinSplit - 1) / kFinSplit;
+    const int i0 = min(count, part * chunk), i1 = min(count, i0 + chunk);
+    const DD v = region_sum_pair(P.region(r) + 2 * (size_t)i0, i1 - i0);
+    if (threadIdx.x == 0) {
+      P.fin[2 * (r * kFinSplit + part)] = v.hi;
+      P.fin[2 * (r * kFinSplit + part) + 1] = v.lo;
+    }
   }
   __shared__ bool last;
   if (threadIdx.x == 0) {
@@ -61,9 +71,21 @@ __global__ void __launch_bounds__(256) k_finalize(Partials P0, FinalizeArgs a, d
     last = (atomicAdd(counter, 1u) == gridDim.x - 1);
   }
   __syncthreads();
-  if (!last || threadIdx.x != 0) return;
+  if (!last) return;
   __threadfence();
-  volatile const double* rv = res;
+  __shared__ double rs[kFinalizeRegions];
+  if (threadIdx.x < kFinalizeRegions) {
+    const int q = threadIdx.x;
+    DD acc{0.0, 0.0};
+    if ((q <= R_44_E) ? a.step : a.diag)
+      for (int k = 0; k < kFinSplit; ++k)  // L2 loads: the other blocks wrote them
+        acc = dd_add(acc, DD{__ldcg(P.fin + 2 * (q * kFinSplit + k)), __ldcg(P.fin + 2 * (q * kFinSplit + k) + 1)});
+    rs[q] = acc.hi + acc.lo;
+    res[q] = rs[q];
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  const double* rv = rs;
   if (a.step) {
     double R[4];
     for (int k = 0; k < 3; ++k) R[k] = (rv[R_IP_E + 2 * k] + rv[R_IP_C + 2 * k]) / a.totalArea;
@@ -108,7 +130,8 @@ void launch_finalize(Partials P, const int* counts_host, double totalArea, doubl
   // scratch after the kDiagLen outputs: R_COUNT region sums, then the counter
   double* res = diag_out + kDiagLen;
   unsigned int* counter = reinterpret_cast<unsigned int*>(diag_out + kDiagLen + R_COUNT);
-  k_finalize<<<dim3(kFinalizeRegions, members > 1 ? members : 1), 256, 0, st>>>(P, a, diag_out, res, counter);
+  k_finalize<<<dim3(kFinalizeRegions * kFinSplit, members > 1 ? members : 1), 256, 0, st>>>(P, a, diag_out, res,
+                                                                                           counter);
 }
 
 // Conservative APVM epsilon (operators_mod.F90:349-354): one block per sum
