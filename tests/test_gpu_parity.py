@@ -218,6 +218,33 @@ def test_time_integrate_host_arrays(mesh4):
     b.close()
 
 
+@pytest.mark.parametrize("tracer_order", [2, 3])
+def test_time_integrate_host_arrays_with_tracers(mesh4, tracer_order):
+    """FP32 with two coupled tracers: tmc_time_integrate on host arrays (with
+    second-order tracers the edge preparation runs before the tracer copy has
+    arrived) equals the same steps of the device-resident state, bit for bit."""
+    from tmcore_gb300 import cases
+    from tmcore_gb300.gpu import TMCoreGPU
+
+    gd, u, ghs = _ic(mesh4, seed=5)
+    qgd = cases.smooth_tracers(mesh4, 2, seed=1) * gd[None, :]
+    kw = dict(dt=600.0, precision=1, pv_scheme=1, apvm_weight=0.0, n_tracers=2, tracer_adv_order=tracer_order)
+    a, b = TMCoreGPU(mesh4, **kw), TMCoreGPU(mesh4, **kw)
+    for g in (a, b):
+        g.set_initial(gd, u, ghs)
+        g.set_tracers(qgd)
+    g0, i0, _ = a.get_state()
+    q0 = a.get_tracers()
+    for _ in range(3):
+        g0, i0, q0 = a.time_integrate(g0, i0, q0)
+        b.step(1)
+    gb, ib, _ = b.get_state()
+    assert np.array_equal(g0, gb) and np.array_equal(i0, ib)
+    assert np.array_equal(q0, b.get_tracers())
+    a.close()
+    b.close()
+
+
 def test_renumbering_is_invisible(mesh4):
     from tmcore_gb300.gpu import TMCoreGPU
 

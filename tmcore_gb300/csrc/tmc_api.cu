@@ -43,7 +43,8 @@ struct EngineBase {
   virtual void get_field(int which, double* raw_out) = 0;                       // scatter to raw
   virtual void set_iap_from_u(const double* ge_new, const double* u_new) = 0;
   virtual void set_tracers_dev(const double* raw_q) = 0;
-  virtual void refresh_shadows(int slot) = 0;
+  // FP32 shadows of state slot `slot` (gd, and the tracer ratios unless !tracers)
+  virtual void refresh_shadows(int slot, bool tracers = true) = 0;
   virtual void get_tracers_dev(double* raw_q) = 0;
   virtual void set_ghs_dev(const double* raw) = 0;
   virtual int launches_per_step() const = 0;
@@ -635,10 +636,10 @@ struct Engine : EngineBase {
     launch_gather<T>(h->M.ne, raw_iap, h->d_edge_n2o, iap[0] + oe(), h->st);
     refresh_shadows(0);
   }
-  void refresh_shadows(int slot) override {
+  void refresh_shadows(int slot, bool tracers = true) override {
     if constexpr (!std::is_same<T, double>::value)
-      launch_shadows(h->M.nc, h->O.n_tracers, gd[slot] + oc(), q[slot] + oq(), gdf[slot] + oc(), qr[slot] + oq(),
-                     h->st);
+      launch_shadows(h->M.nc, tracers ? h->O.n_tracers : 0, gd[slot] + oc(), q[slot] + oq(), gdf[slot] + oc(),
+                     qr[slot] + oq(), h->st);
   }
   void get_field(int which, double* raw) override {
     switch (which) {
@@ -906,7 +907,7 @@ struct EnsEngine : EngineBase {
   }
   void set_tracers_dev(const double*) override {}  // member_layout 1 has no tracers
   void get_tracers_dev(double*) override {}
-  void refresh_shadows(int) override {}  // the h halves of gd are its FP32 values
+  void refresh_shadows(int, bool) override {}  // the h halves of gd are its FP32 values
   void set_ghs_dev(const double* raw) override {
     ens::launch_gather_f64(h->M.nc, D.M, h->cur, raw, h->d_cell_n2o, ghs, h->st);
     ens::launch_to_f32(h->M.nc, D.M, h->cur, ghs, ghsf, h->st);
@@ -1572,13 +1573,21 @@ int tmc_time_integrate(tmc_handle* h, const double* gd_old, const double* iap_u_
       return h->cuda_check("H2D");
     cudaEventRecord(h->cev[1 + i], cs);
   }
+  // The step's edge preparation reads gd and iap_u only (second-order tracers
+  // are fluxed in the cell pass): with such tracers it runs before their
+  // copy has arrived, beside it.
+  const bool prep_early = trc && h->O.tr_order < 3 && !h->generic;
+  h->have_state = true;
+  h->prep_valid = false;
   for (int i = 0; i < nio; ++i) {
     cudaStreamWaitEvent(h->st, h->cev[1 + i], 0);
     h->eng->gather_field(io[i].field, io[i].raw);
+    if (prep_early && io[i].field == F_IAP) {
+      h->eng->refresh_shadows(0, false);
+      ensure_prep(h);
+    }
   }
   h->eng->refresh_shadows(0);
-  h->have_state = true;
-  h->prep_valid = false;
   int rc;
   if ((rc = launch_one_step(h))) return rc;
   for (int i = 0; i < nio; ++i) {
