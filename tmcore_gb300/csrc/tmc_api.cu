@@ -2176,6 +2176,7 @@ int prepare_batched(tmc_group* g) {
     T->off[J_CELLS][j + 1] = T->off[J_CELLS][j] + e->D.slots_c;
     T->off[J_EDGES][j + 1] = T->off[J_EDGES][j] + e->D.slots_e;
     T->off[J_VERTS][j + 1] = T->off[J_VERTS][j] + e->D.slots_v;
+    T->off[J_EDGES_UP][j + 1] = T->off[J_EDGES_UP][j] + ens::slots_up(h->M.ne);
     if (h->M.ne > g->hs[order[big]]->M.ne) big = j;
   }
   if (cudaMalloc(&g->d_jobs, sizeof(JobTable)) != cudaSuccess ||

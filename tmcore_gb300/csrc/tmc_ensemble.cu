@@ -2,7 +2,8 @@
 // CRK4 (time_scheme_mod.F90:109-154), centred pv on edges (APVM weight 0,
 // operators_mod.F90:296-316), second-order gd on edges, no tracers.
 //
-// Thread layout of every pass: blockIdx.x = kEnsEPB consecutive elements
+// Thread layout of every pass: blockIdx.x = kEnsEPB consecutive elements (kUpEPB
+// edges in the upwind pv pass)
 // (space-filling-curve order), blockIdx.y = a group of 32 V members, lane l
 // = members (32 blockIdx.y + l) V ... + V - 1 (V = 2 when the member count
 // is a multiple of 64: a lane's two members are one 8-byte load, and the
@@ -607,29 +608,30 @@ __global__ void __launch_bounds__(kMaxBS) k_ens_edge_pv(DevMesh Mh, Dims D, IO S
 template <int V>
 __device__ __forceinline__ void ens_edge_pv_up(const DevMesh& Mh, const Dims& D, const IO& S, const Upwind& U,
                                                int bx) {
-  __shared__ int s_v[2][kEnsEPB];
-  __shared__ int2 s_ew[kME2][kEnsEPB];      // edgesOnEdge, weightsOnEdge (FP32 bits)
-  __shared__ int s_n[2][kEnsEPB];
-  __shared__ int2 s_iw[kUpW][2][kEnsEPB];   // stencil point, weight (FP32 bits)
-  __shared__ float s_dv[kEnsEPB];
-  const int ne = Mh.ne, e0 = bx * kEnsEPB, nel = min(kEnsEPB, ne - e0);
-  for (int t = threadIdx.x; t < 2 * kEnsEPB; t += blockDim.x) {
-    const int i = t / kEnsEPB, j = t - i * kEnsEPB;
+  // blocks of kUpEPB edges: the stencils take kUpW x 2 entries per edge
+  __shared__ int s_v[2][kUpEPB];
+  __shared__ int2 s_ew[kME2][kUpEPB];      // edgesOnEdge, weightsOnEdge (FP32 bits)
+  __shared__ int s_n[2][kUpEPB];
+  __shared__ int2 s_iw[kUpW][2][kUpEPB];   // stencil point, weight (FP32 bits)
+  __shared__ float s_dv[kUpEPB];
+  const int ne = Mh.ne, e0 = bx * kUpEPB, nel = min(kUpEPB, ne - e0);
+  for (int t = threadIdx.x; t < 2 * kUpEPB; t += blockDim.x) {
+    const int i = t / kUpEPB, j = t - i * kUpEPB;
     if (j < nel) {
       s_v[i][j] = Mh.verticesOnEdge[(size_t)i * ne + e0 + j];
       s_n[i][j] = U.count[(size_t)i * ne + e0 + j];
     }
   }
-  for (int t = threadIdx.x; t < kME2 * kEnsEPB; t += blockDim.x) {
-    const int i = t / kEnsEPB, j = t - i * kEnsEPB;
+  for (int t = threadIdx.x; t < kME2 * kUpEPB; t += blockDim.x) {
+    const int i = t / kUpEPB, j = t - i * kUpEPB;
     if (j < nel) {
       const size_t k = (size_t)i * ne + e0 + j;
       // padded entries: the edge itself, weight 0
       s_ew[i][j] = make_int2(Mh.edgesOnEdge[k], __float_as_int(Mh.weightsOnEdge_f[k]));
     }
   }
-  for (int t = threadIdx.x; t < U.width * 2 * kEnsEPB; t += blockDim.x) {
-    const int q = t / kEnsEPB, j = t - q * kEnsEPB;  // q = stencil point * 2 + side
+  for (int t = threadIdx.x; t < U.width * 2 * kUpEPB; t += blockDim.x) {
+    const int q = t / kUpEPB, j = t - q * kUpEPB;  // q = stencil point * 2 + side
     if (j < nel) {
       const size_t k = (size_t)q * ne + e0 + j;
       s_iw[q >> 1][q & 1][j] = make_int2(U.idx[k], __float_as_int(U.w[k]));
@@ -1120,7 +1122,7 @@ __global__ void __launch_bounds__(kMaxBS) k_jobs_edge_pv(const JobTable* __restr
 template <int V>
 __global__ void __launch_bounds__(kMaxBS) k_jobs_edge_pv_up(const JobTable* __restrict__ T, int nj, int stage) {
   int j;
-  const int bx = job_of(T, J_EDGES, nj, &j);
+  const int bx = job_of(T, J_EDGES_UP, nj, &j);
   const Job& J = T->job[j];
   ens_edge_pv_up<V>(J.Mh, J.D, J.io[stage], J.up, bx);
 }
@@ -1199,13 +1201,14 @@ void launch_edge_pv(const DevMesh& Mh, const Dims& D, const IO& S, const Upwind*
   const dim3 g = grid_of(Mh.ne, D, bs, &th);
   if (up) {
     // four members per lane when the member groups allow (the kernel issues
-    // more instructions per member than it moves bytes)
+    // more instructions per member than it moves bytes); blocks of kUpEPB edges
+    const dim3 gu((unsigned)slots_up(Mh.ne), g.y);
     if (D.LPE == 32 && D.M % 128 == 0 && TMC_ENS_UP_V == 4)
-      k_ens_edge_pv_up<4><<<dim3(g.x, (unsigned)(D.M / 128)), th, 0, st>>>(Mh, D, S, *up);
+      k_ens_edge_pv_up<4><<<dim3(gu.x, (unsigned)(D.M / 128)), th, 0, st>>>(Mh, D, S, *up);
     else if (D.V == 2)
-      k_ens_edge_pv_up<2><<<g, th, 0, st>>>(Mh, D, S, *up);
+      k_ens_edge_pv_up<2><<<gu, th, 0, st>>>(Mh, D, S, *up);
     else
-      k_ens_edge_pv_up<1><<<g, th, 0, st>>>(Mh, D, S, *up);
+      k_ens_edge_pv_up<1><<<gu, th, 0, st>>>(Mh, D, S, *up);
     return;
   }
   if (D.V == 2)
@@ -1323,7 +1326,7 @@ void launch_jobs_step(const JobTable* T, const JobTable& hT, int nj, const int* 
   const unsigned gy = (unsigned)(D.M / (D.LPE * D.V));
   for (int p = 0; p < 5; ++p) grid_of(1, D, bsp[p], &th[p]);
   const dim3 gc((unsigned)hT.off[J_CELLS][nj], gy), ge((unsigned)hT.off[J_EDGES][nj], gy),
-      gv((unsigned)hT.off[J_VERTS][nj], gy);
+      gv((unsigned)hT.off[J_VERTS][nj], gy), gu((unsigned)hT.off[J_EDGES_UP][nj], gy);
   const bool up4 = upwind && D.LPE == 32 && D.M % 128 == 0 && TMC_ENS_UP_V == 4;
   for (int k = 1; k <= 4; ++k) {
     if (D.V == 2) {
@@ -1334,11 +1337,11 @@ void launch_jobs_step(const JobTable* T, const JobTable& hT, int nj, const int* 
       k_jobs_vertex<1><<<gv, th[1], 0, st>>>(T, nj, k);
     }
     if (up4)
-      k_jobs_edge_pv_up<4><<<dim3(ge.x, (unsigned)(D.M / 128)), th[2], 0, st>>>(T, nj, k);
+      k_jobs_edge_pv_up<4><<<dim3(gu.x, (unsigned)(D.M / 128)), th[2], 0, st>>>(T, nj, k);
     else if (upwind && D.V == 2)
-      k_jobs_edge_pv_up<2><<<ge, th[2], 0, st>>>(T, nj, k);
+      k_jobs_edge_pv_up<2><<<gu, th[2], 0, st>>>(T, nj, k);
     else if (upwind)
-      k_jobs_edge_pv_up<1><<<ge, th[2], 0, st>>>(T, nj, k);
+      k_jobs_edge_pv_up<1><<<gu, th[2], 0, st>>>(T, nj, k);
     else if (D.V == 2)
       k_jobs_edge_pv<2><<<ge, th[2], 0, st>>>(T, nj, k);
     else

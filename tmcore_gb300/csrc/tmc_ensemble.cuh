@@ -31,9 +31,11 @@
 namespace tmc {
 namespace ens {
 
-// elements per block: on 512 level-6 members 64 -> 4.92 ms per step, 128 -> 4.91, 32 -> 5.12
+// elements per block: on 512 level-6 members 64 -> 4.92 ms per step, 128 -> 4.91, 32 -> 5.12;
+// on the 16-member level-7 ensemble of the mixed batch 64 -> 7.55-7.71 ms per
+// 1200-s cycle, 128 -> 7.17
 #ifndef TMC_ENS_EPB
-#define TMC_ENS_EPB 64
+#define TMC_ENS_EPB 128
 #endif
 constexpr int kEnsEPB = TMC_ENS_EPB;  // elements per block (and per partial-sum slot)
 
@@ -124,6 +126,11 @@ void launch_vertex(const DevMesh& Mh, const Dims& D, const IO& S, const Partials
 // vertex fit stencils of the edges, [width][2][nEdges] as DStencil, with FP32
 // weights; width at most kUpW.
 constexpr int kUpW = 16;
+// edges per block of the upwind pv pass: its stencils take kUpW x 2 entries
+// per edge, and blocks of kEnsEPB edges would cost it a resident block per SM
+// (512 level-6 members: 0.43-0.46 ms per pass with 64, 0.55 with 128)
+constexpr int kUpEPB = 64;
+__host__ __device__ inline int slots_up(int n) { return (n + kUpEPB - 1) / kUpEPB; }
 struct Upwind {
   const uint8_t* count;  // [2][nEdges]
   const int32_t* idx;    // [width][2][nEdges]
@@ -160,7 +167,8 @@ void launch_finalize(const Dims& D, const Partials& P, bool step, bool diag, boo
 // most first, so every sub-step's active set is a prefix).
 // ---------------------------------------------------------------------------
 constexpr int kMaxJobs = 8;
-enum JobKind { J_CELLS = 0, J_EDGES = 1, J_VERTS = 2 };
+// J_EDGES_UP: the edges in the upwind pv pass's blocks of kUpEPB
+enum JobKind { J_CELLS = 0, J_EDGES = 1, J_VERTS = 2, J_EDGES_UP = 3 };
 struct Job {
   DevMesh Mh;
   Dims D;
@@ -173,7 +181,7 @@ struct Job {
 };
 struct JobTable {
   int n;
-  int off[3][kMaxJobs + 1];  // first block of each job along cells, edges and vertices
+  int off[4][kMaxJobs + 1];  // first block of each job along each JobKind
   Job job[kMaxJobs];
 };
 // one CRK4 step of the first nj jobs (T: the table in device memory, hT: its
