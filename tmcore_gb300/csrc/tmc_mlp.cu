@@ -452,18 +452,24 @@ struct TrainSrc {
   const float* Y;
   long long rows, offset;
   float yscale;
-  __device__ bool sample(long long i, float (&x)[kIn], float& t) const {
+  // row i of the batch as the trainer's column group cg (0..3) needs it: the
+  // eight features 8 cg .. 8 cg + 7 (none for cg 3, whose columns are the
+  // constants), the four the output heads use (x0, x1, x22, x23) and the
+  // target.  A row is 96 bytes, 16-byte aligned.
+  __device__ bool sample(long long i, int cg, float (&x)[8], float (&xd)[4], float& t) const {
     const long long j = (offset + i) % rows;
-    // a row is 96 bytes, 16-byte aligned: six 16-byte loads
-    const float4* xr = reinterpret_cast<const float4*>(X + j * kIn);
+    const float* xr = X + j * kIn;
+    if (cg < 3) {
+      const float4 a = *reinterpret_cast<const float4*>(xr + 8 * cg);
+      const float4 b = *reinterpret_cast<const float4*>(xr + 8 * cg + 4);
+      x[0] = a.x, x[1] = a.y, x[2] = a.z, x[3] = a.w, x[4] = b.x, x[5] = b.y, x[6] = b.z, x[7] = b.w;
+    } else {
 #pragma unroll
-    for (int k = 0; k < kIn / 4; ++k) {
-      const float4 v = xr[k];
-      x[4 * k] = v.x;
-      x[4 * k + 1] = v.y;
-      x[4 * k + 2] = v.z;
-      x[4 * k + 3] = v.w;
+      for (int k = 0; k < 8; ++k) x[k] = 0.f;
     }
+    const float2 d0 = *reinterpret_cast<const float2*>(xr);
+    const float2 d1 = *reinterpret_cast<const float2*>(xr + 22);
+    xd[0] = d0.x, xd[1] = d0.y, xd[2] = d1.x, xd[3] = d1.y;
     t = Y[j] / yscale;
     return true;
   }
@@ -475,19 +481,69 @@ __global__ void __launch_bounds__(kTrThreads, 1) k_mlp_train_tc(Net net, TrainSr
   if (!train_tiles(net, src, ntiles, inv_batch, part, ploss, smem) && threadIdx.x == 0) atomicExch(err, 1);
 }
 
-// grad += the blocks' partial gradients, summed in block order; loss += their losses
-__global__ void k_grad_reduce(const float* part, const double* ploss, int nblk, float* grad, double* loss) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+// The tensor-core trainer's per-block partial gradients and losses, summed
+// in a fixed order (the result does not depend on scheduling).  A block of
+// 256 threads takes 32 parameters: warp q adds the partials of blocks q,
+// q + 8, q + 16, ... (independent loads), and warp 0 adds the eight chains
+// in order.  Warp 0 of block 0 sums the losses (lane chains, then a fixed
+// shuffle tree).
+constexpr int kRedChains = 8;
+__device__ __forceinline__ float grad_sum(const float* part, int nblk, int i) {
+  __shared__ float red[kRedChains][32];
+  const int c = threadIdx.x & 31, q = threadIdx.x >> 5;
+  float s = 0.f;
   if (i < kParams) {
-    float s = 0.f;
-    for (int b = 0; b < nblk; ++b) s += part[(size_t)b * kParams + i];
-    grad[i] += s;
+#pragma unroll 4
+    for (int b = q; b < nblk; b += kRedChains) s += part[(size_t)b * kParams + i];
   }
-  if (i == 0) {
-    double l = 0.0;
-    for (int b = 0; b < nblk; ++b) l += ploss[b];
-    *loss += l;
+  red[q][c] = s;
+  __syncthreads();
+  float g = 0.f;
+  if (q == 0)
+#pragma unroll
+    for (int k = 0; k < kRedChains; ++k) g += red[k][c];
+  return g;
+}
+__device__ __forceinline__ double loss_sum(const double* ploss, int nblk) {
+  double l = 0.0;
+  for (int b = threadIdx.x; b < nblk; b += 32) l += ploss[b];
+  for (int off = 16; off > 0; off >>= 1) l += __shfl_down_sync(0xffffffffu, l, off);
+  return l;
+}
+// grad += the summed partial gradient; loss += the summed loss
+__global__ void __launch_bounds__(32 * kRedChains) k_grad_reduce(const float* part, const double* ploss, int nblk,
+                                                                 float* grad, double* loss) {
+  const int i = blockIdx.x * 32 + (threadIdx.x & 31);
+  const float g = grad_sum(part, nblk, i);
+  if (threadIdx.x < 32 && i < kParams) grad[i] += g;
+  if (blockIdx.x == 0 && threadIdx.x < 32) {
+    const double l = loss_sum(ploss, nblk);
+    if (threadIdx.x == 0) *loss += l;
   }
+}
+// the summed partial gradient applied by Adam (as k_adam), the summed loss
+// stored in *loss; nothing is applied when *err is set (a completion wait of
+// the batch ran out)
+__global__ void __launch_bounds__(32 * kRedChains) k_grad_adam(const float* part, const double* ploss, int nblk,
+                                                               float* p, __nv_bfloat16* pb, float* m, float* v,
+                                                               float lr, float b1c, float b2c, const int* err,
+                                                               double* loss) {
+  const int i = blockIdx.x * 32 + (threadIdx.x & 31);
+  const float gi = grad_sum(part, nblk, i);
+  if (blockIdx.x == 0 && threadIdx.x < 32) {
+    const double l = loss_sum(ploss, nblk);
+    if (threadIdx.x == 0) *loss = l;
+  }
+  if (threadIdx.x >= 32 || i >= kParams || *err) return;
+  const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+  const float mi = b1 * m[i] + (1.f - b1) * gi;
+  const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+  m[i] = mi;
+  v[i] = vi;
+  const float mh = mi / b1c, vh = vi / b2c;
+  const float pi = p[i] - lr * mh / (sqrtf(vh) + eps);
+  p[i] = pi;
+  pb[i] = __float2bfloat16_rn(pi);
 }
 
 }  // namespace
@@ -739,15 +795,23 @@ int tmc_mlp_set_dataset(tmc_mlp* n, const float* x, const float* y, int64_t rows
 
 // one gradient pass over `batch` rows of X/Y from row `offset` (wrapping at
 // `rows`), added into n->g and its loss into *loss (device)
+// the tensor-core gradient tiles of one batch into n->part / n->ploss; returns
+// the number of blocks (partials)
+static int launch_train_tc(tmc_mlp* n, const float* X, const float* Y, long long rows, long long offset,
+                           long long batch) {
+  const long long ntiles = batch / kTile;
+  const int grid = (int)std::min<long long>(ntiles, (long long)n->sms);
+  k_mlp_train_tc<<<grid, kTrThreads, kSmemTrain, n->st>>>(n->net(), TrainSrc{X, Y, rows, offset, n->yscale}, ntiles,
+                                                        1.f / (float)batch, n->part, n->ploss, n->d_err);
+  return grid;
+}
+
 static void launch_gradient(tmc_mlp* n, const float* X, const float* Y, long long rows, long long offset, long long batch,
                             double* loss) {
   const float inv_batch = 1.f / (float)batch;
   if (n->train_tc) {
-    const long long ntiles = batch / kTile;
-    const int grid = (int)std::min<long long>(ntiles, (long long)n->sms);
-    k_mlp_train_tc<<<grid, kTrThreads, kSmemTrain, n->st>>>(n->net(), TrainSrc{X, Y, rows, offset, n->yscale}, ntiles,
-                                                          inv_batch, n->part, n->ploss, n->d_err);
-    k_grad_reduce<<<(kParams + 255) / 256, 256, 0, n->st>>>(n->part, n->ploss, grid, n->g, loss);
+    const int grid = launch_train_tc(n, X, Y, rows, offset, batch);
+    k_grad_reduce<<<(kParams + 31) / 32, 32 * kRedChains, 0, n->st>>>(n->part, n->ploss, grid, n->g, loss);
   } else {
     k_mlp_train<<<(unsigned)(batch / kTile), kTile, sizeof(TrainSmem), n->st>>>(n->net(), X, Y, rows, offset,
                                                                                 inv_batch, n->g, loss);
@@ -801,13 +865,21 @@ int tmc_mlp_train(tmc_mlp* n, int32_t batch, int32_t steps, float lr, float* los
   cudaMemsetAsync(n->d_err, 0, sizeof(int), n->st);
   for (int s = 0; s < steps; ++s) {
     double* dl = losses ? n->d_losses + s : n->d_loss;
-    cudaMemsetAsync(dl, 0, sizeof(double), n->st);
-    launch_gradient(n, n->dx, n->dy, n->rows, n->cursor, batch, dl);
-    n->cursor = (n->cursor + batch) % n->rows;
     n->adam_t += 1;
     const float b1c = 1.f - std::pow(0.9f, (float)n->adam_t), b2c = 1.f - std::pow(0.999f, (float)n->adam_t);
-    k_adam<<<(kParams + 255) / 256, 256, 0, n->st>>>(n->p, n->pb, n->g, n->m, n->v, kParams, lr, b1c, b2c,
-                                                     n->d_err);
+    if (n->train_tc) {
+      // two launches per step: the gradient tiles, then the fixed-order sum
+      // of their partials with Adam
+      const int grid = launch_train_tc(n, n->dx, n->dy, n->rows, n->cursor, batch);
+      k_grad_adam<<<(kParams + 31) / 32, 32 * kRedChains, 0, n->st>>>(n->part, n->ploss, grid, n->p, n->pb, n->m,
+                                                                      n->v, lr, b1c, b2c, n->d_err, dl);
+    } else {
+      cudaMemsetAsync(dl, 0, sizeof(double), n->st);
+      launch_gradient(n, n->dx, n->dy, n->rows, n->cursor, batch, dl);
+      k_adam<<<(kParams + 255) / 256, 256, 0, n->st>>>(n->p, n->pb, n->g, n->m, n->v, kParams, lr, b1c, b2c,
+                                                       n->d_err);
+    }
+    n->cursor = (n->cursor + batch) % n->rows;
   }
   if (losses && steps > 0) {
     std::vector<double> h(steps);

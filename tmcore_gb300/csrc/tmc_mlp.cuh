@@ -85,10 +85,14 @@ constexpr int kHeadPlain = 0, kHeadApvm = 1, kHeadSign = 2;
 // The head's auxiliary value of an edge from its raw closure features (1: v,
 // 22: pv gradient along the edge, 0: u, 23: across it): kHeadApvm the APVM
 // direction dt (v dq/dt + u dq/dn); kHeadSign v dq/dt.
-__device__ __forceinline__ float head_dir(const Net& net, const float (&x)[kIn]) {
-  if (net.head == kHeadApvm) return net.head_dt * (x[1] * x[22] + x[0] * x[23]);
-  if (net.head == kHeadSign) return x[1] * x[22];
+// from the four features the heads use: x0, x1, x22, x23
+__device__ __forceinline__ float head_dir4(const Net& net, float x0, float x1, float x22, float x23) {
+  if (net.head == kHeadApvm) return net.head_dt * (x1 * x22 + x0 * x23);
+  if (net.head == kHeadSign) return x1 * x22;
   return 0.f;
+}
+__device__ __forceinline__ float head_dir(const Net& net, const float (&x)[kIn]) {
+  return head_dir4(net, x[0], x[1], x[22], x[23]);
 }
 __device__ __forceinline__ float softplus_f(float y) { return y > 20.f ? y : log1pf(__expf(y)); }
 // the correction from the raw output y (units of pv_edge)
