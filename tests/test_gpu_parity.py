@@ -218,17 +218,23 @@ def test_time_integrate_host_arrays(mesh4):
     b.close()
 
 
-@pytest.mark.parametrize("tracer_order", [2, 3])
-def test_time_integrate_host_arrays_with_tracers(mesh4, tracer_order):
-    """FP32 with two coupled tracers: tmc_time_integrate on host arrays (with
-    second-order tracers the edge preparation runs before the tracer copy has
-    arrived) equals the same steps of the device-resident state, bit for bit."""
+@pytest.mark.parametrize("tracer_order,n_tracers,use_graph,diag_every",
+                         [(2, 2, 1, 1), (3, 2, 1, 1), (2, 4, 1, 1), (2, 1, 1, 2), (2, 4, 0, 1), (2, 3, 1, 1)])
+def test_time_integrate_host_arrays_with_tracers(mesh4, tracer_order, n_tracers, use_graph, diag_every):
+    """FP32 with coupled tracers: tmc_time_integrate on host arrays equals the
+    same steps of the device-resident state, bit for bit.  With second-order
+    tracers the edge preparation runs before the tracer copy has arrived; with
+    1, 2 or 4 of them all of stage 1 but its tracer terms does (a tracer-free
+    cell pass, then k_tracers_fast), in the step graph's tail or launched one
+    by one, on diagnostic steps and others.  Three tracers keep the fused
+    program."""
     from tmcore_gb300 import cases
     from tmcore_gb300.gpu import TMCoreGPU
 
     gd, u, ghs = _ic(mesh4, seed=5)
-    qgd = cases.smooth_tracers(mesh4, 2, seed=1) * gd[None, :]
-    kw = dict(dt=600.0, precision=1, pv_scheme=1, apvm_weight=0.0, n_tracers=2, tracer_adv_order=tracer_order)
+    qgd = cases.smooth_tracers(mesh4, n_tracers, seed=1) * gd[None, :]
+    kw = dict(dt=600.0, precision=1, pv_scheme=1, apvm_weight=0.0, n_tracers=n_tracers,
+              tracer_adv_order=tracer_order, use_graph=use_graph, diag_every=diag_every)
     a, b = TMCoreGPU(mesh4, **kw), TMCoreGPU(mesh4, **kw)
     for g in (a, b):
         g.set_initial(gd, u, ghs)

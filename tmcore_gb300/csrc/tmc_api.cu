@@ -35,6 +35,15 @@ struct EngineBase {
   virtual ~EngineBase() {}
   virtual int alloc() = 0;
   virtual void launch_step(bool diag, std::vector<cudaEvent_t>* flux_ev, size_t* ev_pos) = 0;
+  // The fused step split for tmc_time_integrate, whose tracers arrive after
+  // gd and iap_u: stage 1 with a tracer-free cell pass (launch_stage1_early),
+  // the stage's tracer terms once the tracers are in (launch_late_tracers),
+  // then stages 2-4 and the final update (launch_step with first_stage 2).
+  // can_split: the FP32 fused program with 1, 2 or 4 second-order tracers.
+  virtual bool can_split() const { return false; }
+  virtual void launch_stage1_early(bool) {}
+  virtual void launch_late_tracers() {}
+  int first_stage = 1;
   virtual void launch_diag_pass(bool finalize) = 0;
   virtual void launch_prep() = 0;
   virtual void launch_spatial_only() = 0;
@@ -86,6 +95,15 @@ struct tmc_handle {
   bool prep_valid = false;  // edge set 0 holds the preparation of state(old)
   std::unique_ptr<EngineBase> eng;
   cudaGraphExec_t g_step = nullptr, g_step_diag = nullptr;
+  // stages 2-4 and the final update, after a stage 1 launched outside the
+  // graph (tmc_time_integrate with late tracers); [diag]
+  cudaGraphExec_t g_tail[2] = {nullptr, nullptr};
+  void drop_graphs() {
+    for (cudaGraphExec_t* g : {&g_step, &g_step_diag, &g_tail[0], &g_tail[1]}) {
+      if (*g) cudaGraphExecDestroy(*g);
+      *g = nullptr;
+    }
+  }
   long step_count = 0;
   double cell_coef4 = 0.25, vert_coef4 = 0.25;  // SAVE'd coef4 of the upwind routines
   // ensemble members of this mesh (member-outermost arrays) and the member the
@@ -362,42 +380,66 @@ struct Engine : EngineBase {
     const DevMesh& M = h->M;
     const ModelOpt& O = h->O;
     const double dt = O.dt;
-    const double adt[5] = {0.0, 0.5 * dt, 0.5 * dt, dt, 0.0};
-    for (int k = 1; k <= 4; ++k) {
-      StageIO<T> s = io(k);
-      s.vor = nullptr;  // vorticity and gd on vertices are kept only by the diagnostic pass
-      s.gd_v = nullptr;
-      const bool dg = diag && k == 1;
-      RKStage rk{k, adt[k]};
-      const int* b = h->bsp;
-      auto mark = [&](int pass) {
-        if (flux_ev && h->timed_pass == pass) cudaEventRecord((*flux_ev)[(*ev_pos)++], h->st);
-      };
-      // concurrent cell and vertex / pv-on-edge branches, except while passes
-      // are timed one by one and for the conservative APVM (its global sums)
-      const bool branch = !flux_ev && O.pv_scheme != 2;
-      const cudaStream_t side = branch ? h->fork_side() : h->st;
-      mark(P_CELL);
-      launch_cell<T>(M, O, s, rk, h->P, dg, b[P_CELL], h->st);
-      mark(P_CELL);
-      mark(P_VERTEX);
-      launch_vertex<T>(M, O, s, h->P, dg, b[P_VERTEX], side);
-      mark(P_VERTEX);
-      mark(P_PV);
-      launch_edge_pv<T>(M, O, s, b[P_PV], side);
-      if (branch) h->join_side();
-      if (O.pv_scheme == 2) launch_cons_apvm<T>(M, O, s, h->P, h->d_diag, b[P_VERTEX], h->st);
-      launch_closure_pass(s, k);
-      mark(P_PV);
-      mark(P_FLUX);
-      launch_edge_flux<T>(M, O, s, rk, h->P, b[P_FLUX], h->st);
-      mark(P_FLUX);
-    }
+    for (int k = first_stage; k <= 4; ++k) launch_stage(k, diag && k == 1, false, flux_ev, ev_pos);
     launch_finalize(h->P, h->counts, h->hm.totalArea, h->hm.sumAreaTriangle, dt, true, diag,
                     h->p.conserve_energy != 0, h->d_diag, h->st, 2, h->members);
     if (flux_ev && h->timed_pass == P_FINAL) cudaEventRecord((*flux_ev)[(*ev_pos)++], h->st);
     launch_final_update<T>(M, O, io(0), h->d_diag, h->P, h->bsp[P_FINAL], h->st);
     if (flux_ev && h->timed_pass == P_FINAL) cudaEventRecord((*flux_ev)[(*ev_pos)++], h->st);
+  }
+
+  // stage k of the fused CRK4 program; with no_tracers its cell pass leaves
+  // the tracer terms out (launch_late_tracers adds them)
+  void launch_stage(int k, bool dg, bool no_tracers, std::vector<cudaEvent_t>* flux_ev, size_t* ev_pos) {
+    const DevMesh& M = h->M;
+    const ModelOpt& O = h->O;
+    const double dt = O.dt;
+    const double adt[5] = {0.0, 0.5 * dt, 0.5 * dt, dt, 0.0};
+    StageIO<T> s = io(k);
+    s.vor = nullptr;  // vorticity and gd on vertices are kept only by the diagnostic pass
+    s.gd_v = nullptr;
+    RKStage rk{k, adt[k]};
+    const int* b = h->bsp;
+    auto mark = [&](int pass) {
+      if (flux_ev && h->timed_pass == pass) cudaEventRecord((*flux_ev)[(*ev_pos)++], h->st);
+    };
+    // concurrent cell and vertex / pv-on-edge branches, except while passes
+    // are timed one by one and for the conservative APVM (its global sums)
+    const bool branch = !flux_ev && O.pv_scheme != 2;
+    const cudaStream_t side = branch ? h->fork_side() : h->st;
+    mark(P_CELL);
+    if (no_tracers) {
+      ModelOpt O0 = O;
+      O0.n_tracers = 0;
+      launch_cell<T>(M, O0, s, rk, h->P, dg, b[P_CELL], h->st);
+    } else {
+      launch_cell<T>(M, O, s, rk, h->P, dg, b[P_CELL], h->st);
+    }
+    mark(P_CELL);
+    mark(P_VERTEX);
+    launch_vertex<T>(M, O, s, h->P, dg, b[P_VERTEX], side);
+    mark(P_VERTEX);
+    mark(P_PV);
+    launch_edge_pv<T>(M, O, s, b[P_PV], side);
+    if (branch) h->join_side();
+    if (O.pv_scheme == 2) launch_cons_apvm<T>(M, O, s, h->P, h->d_diag, b[P_VERTEX], h->st);
+    launch_closure_pass(s, k);
+    mark(P_PV);
+    mark(P_FLUX);
+    launch_edge_flux<T>(M, O, s, rk, h->P, b[P_FLUX], h->st);
+    mark(P_FLUX);
+  }
+
+  bool can_split() const override {
+    const int n = h->O.n_tracers;
+    return std::is_same<T, float>::value && !h->generic && h->members <= 1 && h->O.tr_order == 2 &&
+           (n == 1 || n == 2 || n == 4);
+  }
+  void launch_stage1_early(bool diag) override { launch_stage(1, diag, true, nullptr, nullptr); }
+  // stage 1's tracer terms: its F (edge set 0) and next gd (slot 1) stay as
+  // the stage left them until stage 2
+  void launch_late_tracers() override {
+    launch_tracers_fast<T>(h->M, h->O, io(1), RKStage{1, 0.5 * h->O.dt}, h->bsp[P_CELL], h->st);
   }
 
   // the learned closure on this stage's pv_edge (FP32 path)
@@ -963,11 +1005,14 @@ DStencil upload_stencil(tmc_handle* h, const Stencil& S) {
   return d;
 }
 
-int build_graph(tmc_handle* h, bool diag, cudaGraphExec_t* out) {
+// the step program from stage first_stage on, captured as one graph
+int build_graph(tmc_handle* h, bool diag, cudaGraphExec_t* out, int first_stage = 1) {
   cudaGraph_t g = nullptr;
   if (cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
     return h->cuda_check("cudaStreamBeginCapture");
+  h->eng->first_stage = first_stage;
   h->eng->launch_step(diag, nullptr, nullptr);
+  h->eng->first_stage = 1;
   if (cudaStreamEndCapture(h->st, &g) != cudaSuccess) return h->cuda_check("cudaStreamEndCapture");
   cudaError_t e = cudaGraphInstantiate(out, g, 0);
   cudaGraphDestroy(g);
@@ -1008,6 +1053,34 @@ int launch_one_step(tmc_handle* h) {
     if (cudaGraphLaunch(*g, h->st) != cudaSuccess) return h->cuda_check("cudaGraphLaunch");
   } else {
     h->eng->launch_step(diag, nullptr, nullptr);
+  }
+  h->step_count++;
+  return h->cuda_check("step");
+}
+
+// One step split around the late arrival of the tracers (tmc_time_integrate):
+// stage 1 without its tracer terms, then tracers_in() (which queues the
+// tracers' gather and shadows on the stream), the stage's tracer terms, and
+// stages 2-4 with the final update as one graph.  Same results as
+// launch_one_step.
+template <class F>
+int launch_one_step_split(tmc_handle* h, F&& tracers_in) {
+  ensure_prep(h);
+  const bool diag = h->p.diag_every > 0 && (h->step_count % h->p.diag_every) == 0;
+  h->eng->launch_stage1_early(diag);
+  tracers_in();
+  h->eng->launch_late_tracers();
+  if (h->p.use_graph) {
+    cudaGraphExec_t* g = &h->g_tail[diag ? 1 : 0];
+    if (!*g) {
+      int rc = build_graph(h, diag, g, 2);
+      if (rc) return rc;
+    }
+    if (cudaGraphLaunch(*g, h->st) != cudaSuccess) return h->cuda_check("cudaGraphLaunch");
+  } else {
+    h->eng->first_stage = 2;
+    h->eng->launch_step(diag, nullptr, nullptr);
+    h->eng->first_stage = 1;
   }
   h->step_count++;
   return h->cuda_check("step");
@@ -1347,8 +1420,7 @@ int tmc_destroy(tmc_handle* h) {
       if (e) cudaEventDestroy(e);
     cudaStreamDestroy(h->cst);
   }
-  if (h->g_step) cudaGraphExecDestroy(h->g_step);
-  if (h->g_step_diag) cudaGraphExecDestroy(h->g_step_diag);
+  h->drop_graphs();
   for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
   h->eng.reset();
   for (void* q : h->dptrs) cudaFree(q);
@@ -1575,11 +1647,15 @@ int tmc_time_integrate(tmc_handle* h, const double* gd_old, const double* iap_u_
   }
   // The step's edge preparation reads gd and iap_u only (second-order tracers
   // are fluxed in the cell pass): with such tracers it runs before their
-  // copy has arrived, beside it.
+  // copy has arrived, beside it.  Where the fused program allows (FP32, 1, 2
+  // or 4 tracers), so does all of stage 1 but its tracer terms, which follow
+  // the tracers' arrival.
   const bool prep_early = trc && h->O.tr_order < 3 && !h->generic;
+  const bool split = trc && h->eng->can_split();
   h->have_state = true;
   h->prep_valid = false;
   for (int i = 0; i < nio; ++i) {
+    if (split && io[i].field == -1) break;  // the tracers: after stage 1
     cudaStreamWaitEvent(h->st, h->cev[1 + i], 0);
     h->eng->gather_field(io[i].field, io[i].raw);
     if (prep_early && io[i].field == F_IAP) {
@@ -1587,9 +1663,18 @@ int tmc_time_integrate(tmc_handle* h, const double* gd_old, const double* iap_u_
       ensure_prep(h);
     }
   }
-  h->eng->refresh_shadows(0);
   int rc;
-  if ((rc = launch_one_step(h))) return rc;
+  if (split) {
+    rc = launch_one_step_split(h, [&] {
+      cudaStreamWaitEvent(h->st, h->cev[3], 0);
+      h->eng->gather_field(-1, h->raw_q);
+      h->eng->refresh_shadows(0);
+    });
+    if (rc) return rc;
+  } else {
+    h->eng->refresh_shadows(0);
+    if ((rc = launch_one_step(h))) return rc;
+  }
   for (int i = 0; i < nio; ++i) {
     if (io[i].field == F_GD || io[i].field == F_IAP)
       h->eng->get_field(io[i].field, io[i].raw);
@@ -1773,9 +1858,7 @@ int tmc_set_closure(tmc_handle* h, const tmc_mlp* net) {
   h->closure = net;
   if (net) h->closure_net = tmc_mlp_net(net);
   h->O.need_pv_c = net ? 1 : 0;
-  if (h->g_step) cudaGraphExecDestroy(h->g_step);
-  if (h->g_step_diag) cudaGraphExecDestroy(h->g_step_diag);
-  h->g_step = h->g_step_diag = nullptr;
+  h->drop_graphs();
   return TMC_OK;
 }
 
@@ -1789,9 +1872,7 @@ int tmc_set_closure_stages(tmc_handle* h, int32_t every_stage) {
     h->d_closure_dq = h->dalloc<float>((size_t)h->members * h->M.ne);
     if (!h->d_closure_dq) return h->cuda_check("tmc_set_closure_stages: allocation");
   }
-  if (h->g_step) cudaGraphExecDestroy(h->g_step);
-  if (h->g_step_diag) cudaGraphExecDestroy(h->g_step_diag);
-  h->g_step = h->g_step_diag = nullptr;
+  h->drop_graphs();
   return TMC_OK;
 }
 
@@ -2082,9 +2163,7 @@ int tmc_autotune(tmc_handle* h, int32_t steps, int32_t block_sizes[5]) {
   cudaFree(sv_gd);
   cudaFree(sv_iap);
   cudaFree(sv_q);
-  if (h->g_step) cudaGraphExecDestroy(h->g_step);
-  if (h->g_step_diag) cudaGraphExecDestroy(h->g_step_diag);
-  h->g_step = h->g_step_diag = nullptr;
+  h->drop_graphs();
   if (rc) return rc;
   if (rc2) return rc2;
   if (block_sizes)

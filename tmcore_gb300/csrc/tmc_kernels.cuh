@@ -272,6 +272,12 @@ void launch_edge_prep(const DevMesh& M, const ModelOpt& O, const StageIO<T>& S, 
 template <class T>
 void launch_cell(const DevMesh& M, const ModelOpt& O, const StageIO<T>& S, RKStage rk, Partials P, bool diag,
                  int bs, cudaStream_t st);
+// FP32, single member, 1, 2 or 4 second-order tracers: the tracer terms of
+// the cell pass of stage rk, after a tracer-free cell pass of that stage
+// (launch_cell with n_tracers 0); a no-op otherwise
+template <class T>
+void launch_tracers_fast(const DevMesh& M, const ModelOpt& O, const StageIO<T>& S, RKStage rk, int bs,
+                         cudaStream_t st);
 template <class T>
 void launch_vertex(const DevMesh& M, const ModelOpt& O, const StageIO<T>& S, Partials P, bool diag, int bs,
                    cudaStream_t st);

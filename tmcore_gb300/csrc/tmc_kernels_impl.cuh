@@ -1333,6 +1333,44 @@ void launch_edge_prep(const DevMesh& M, const ModelOpt& O, const StageIO<T>& S, 
                       cudaStream_t st) {
   TMC_LAUNCH(k_edge_prep, grid_for(M.ne, bs), M, O, S, P, diag ? 1 : 0);
 }
+// The second-order tracer terms of the FP32 cell pass (the mass-weighted
+// form d(gd q)/dt = div_operator(F q_edge), q_edge the mean of the two
+// cells' mixing ratios): the tendency of each tracer of one cell ...
+template <int NTR, int NQ>
+__device__ __forceinline__ void tracer_tend_f(const float (&ns)[kME], const float (&Fv)[kME], const float (&dv)[kME],
+                                              const float (&qs)[NQ], const float (&qn)[NQ][kME], float invAf,
+                                              float (&tq)[NQ]) {
+#pragma unroll
+  for (int j = 0; j < NTR; ++j) {
+    float sq = 0.f;
+#pragma unroll
+    for (int i = 0; i < kME; ++i) sq += ns[i] * Fv[i] * (0.5f * (qs[j] + qn[j][i])) * dv[i];
+    tq[j] = -sq * invAf;
+  }
+}
+// ... and its RK update (mode as RKStage; gnf the stage's next gd in FP32)
+template <int NTR, int NQ>
+__device__ __forceinline__ void tracer_update_f(const StageIO<float>& S, size_t nc, int c, int mode, float adt,
+                                                const float (&tq)[NQ], const float (&qo)[NQ], const float (&qa)[NQ],
+                                                float gnf) {
+#pragma unroll
+  for (int j = 0; j < NTR; ++j) {
+    const size_t qi = (size_t)j * nc + c;
+    if (mode == 1) {
+      S.q_acc[qi] = tq[j];
+    } else if (mode <= 3) {
+      S.q_acc[qi] = qa[j] + 2.f * tq[j];
+    } else {
+      S.q_acc[qi] = (qa[j] + tq[j]) * (1.0f / 6.0f);
+    }
+    if (mode <= 3) {
+      const float qnext = qo[j] + adt * tq[j];
+      S.q_next[qi] = qnext;
+      S.qr_next[qi] = qnext / gnf;
+    }
+  }
+}
+
 // FP32 cell pass of the CRK4 stages (modes 1-4) with NTR second-order
 // tracers: every load is issued before the first store, in two waves
 // (indices and the cell's own values, then the gathers of the edges' u, F,
@@ -1402,13 +1440,7 @@ __device__ __forceinline__ void cell_fast_body(const DevMesh& M, const StageIO<f
     const float tT = (float)t;
     S.E[c] = k * 0.25f * invAf + gdf + ghf;
     float tq[NQ];
-#pragma unroll
-    for (int j = 0; j < NTR; ++j) {
-      float sq = 0.f;
-#pragma unroll
-      for (int i = 0; i < kME; ++i) sq += ns[i] * Fv[i] * (0.5f * (qs[j] + qn[j][i])) * dv[i];
-      tq[j] = -sq * invAf;
-    }
+    tracer_tend_f<NTR, NQ>(ns, Fv, dv, qs, qn, invAf, tq);
     double gnext = 0.0;
     switch (mode) {
       case 1:
@@ -1437,23 +1469,7 @@ __device__ __forceinline__ void cell_fast_body(const DevMesh& M, const StageIO<f
       S.gd_next[c] = gnext;
       S.gdf_next[c] = gnf;
     }
-    const float adt = (float)rk.a_dt;
-#pragma unroll
-    for (int j = 0; j < NTR; ++j) {
-      const size_t qi = (size_t)j * M.nc + c;
-      if (mode == 1) {
-        S.q_acc[qi] = tq[j];
-      } else if (mode <= 3) {
-        S.q_acc[qi] = qa[j] + 2.f * tq[j];
-      } else {
-        S.q_acc[qi] = (qa[j] + tq[j]) * (1.0f / 6.0f);
-      }
-      if (mode <= 3) {
-        const float qnext = qo[j] + adt * tq[j];
-        S.q_next[qi] = qnext;
-        S.qr_next[qi] = qnext / gnf;
-      }
-    }
+    tracer_update_f<NTR, NQ>(S, M.nc, c, mode, (float)rk.a_dt, tq, qo, qa, gnf);
     if (diag) {
       // total mass from the FP64 gd; the cell part of the total energy
       // (gd^2 + 2 gd ghs) areaCell (tmcore_swm_mod.F90:215-231) from FP32
@@ -1480,6 +1496,48 @@ __global__ void __launch_bounds__(kCellBlock, TMC_CELL_SINGLE_MIN_BLOCKS) k_cell
                                                          int diag) {
   cell_fast_body<NTR, false>(M, S0, rk, P0, diag);
 }
+// The tracer terms of the FP32 cell pass alone, for a stage whose cell pass
+// ran tracer-free (k_cell_fast<0>): the same loads and the same arithmetic
+// (tracer_tend_f, tracer_update_f) as k_cell_fast<NTR>, with the stage's next
+// gd in FP32 read back from S.gdf_next.  Single member.
+template <int NTR>
+__global__ void __launch_bounds__(kCellBlock) k_tracers_fast(DevMesh M, StageIO<float> S, RKStage rk) {
+  const int mode = rk.mode;
+  TMC_FOR_EPT(c, M.nc) {
+    int ei[kME], ci[kME];
+    float ns[kME];
+#pragma unroll
+    for (int i = 0; i < kME; ++i) {
+      ei[i] = M.edgesOnCell[(size_t)i * M.nc + c];
+      ns[i] = (float)M.nSign[(size_t)i * M.nc + c];
+      ci[i] = M.cellsOnCell[(size_t)i * M.nc + c];
+    }
+    const float invAf = M.invAreaCell_f[c];
+    const float gnf = (mode <= 3) ? S.gdf_next[c] : 0.f;
+    float qs[NTR], qo[NTR], qa[NTR];
+#pragma unroll
+    for (int j = 0; j < NTR; ++j) {
+      const size_t qi = (size_t)j * M.nc + c;
+      qs[j] = S.qr_in[qi];
+      qo[j] = (mode <= 3) ? S.q_old[qi] : 0.f;
+      qa[j] = (mode >= 2) ? S.q_acc[qi] : 0.f;
+    }
+    float Fv[kME], dv[kME], qn[NTR][kME];
+#pragma unroll
+    for (int i = 0; i < kME; ++i) {
+      Fv[i] = S.F[ei[i]];
+      dv[i] = M.dvEdge_f[ei[i]];
+    }
+#pragma unroll
+    for (int j = 0; j < NTR; ++j)
+#pragma unroll
+      for (int i = 0; i < kME; ++i) qn[j][i] = S.qr_in[(size_t)j * M.nc + ci[i]];
+    float tq[NTR];
+    tracer_tend_f<NTR, NTR>(ns, Fv, dv, qs, qn, invAf, tq);
+    tracer_update_f<NTR, NTR>(S, M.nc, c, mode, (float)rk.a_dt, tq, qo, qa, gnf);
+  }
+}
+
 template <int NTR>
 __global__ void __launch_bounds__(kMemberBlock, NTR == 0 ? TMC_CELL_MIN_BLOCKS : 3) k_cell_fast_members(DevMesh M, StageIO<float> S0, RKStage rk,
                                                                     Partials P0, int diag) {
@@ -1523,6 +1581,19 @@ void launch_cell(const DevMesh& M, const ModelOpt& O, const StageIO<T>& S, RKSta
     }
   }
   TMC_LAUNCH(k_cell, grid_for(M.nc, bs), M, O, S, rk, P, diag ? 1 : 0);
+}
+template <class T>
+void launch_tracers_fast(const DevMesh& M, const ModelOpt& O, const StageIO<T>& S, RKStage rk, int bs,
+                         cudaStream_t st) {
+  if constexpr (!kF64<T>) {
+    const int g = grid_for(M.nc, bs);
+    switch (O.n_tracers) {
+      case 1: k_tracers_fast<1><<<g, bs, 0, st>>>(M, S, rk); return;
+      case 2: k_tracers_fast<2><<<g, bs, 0, st>>>(M, S, rk); return;
+      case 4: k_tracers_fast<4><<<g, bs, 0, st>>>(M, S, rk); return;
+      default: return;
+    }
+  }
 }
 template <class T>
 void launch_vertex(const DevMesh& M, const ModelOpt& O, const StageIO<T>& S, Partials P, bool diag, int bs,
@@ -1621,6 +1692,8 @@ void launch_to_f64(size_t n, const T* src, double* dst, cudaStream_t st) {
                                     cudaStream_t);                                                                \
   template void launch_cell<T>(const DevMesh&, const ModelOpt&, const StageIO<T>&, RKStage, Partials, bool, int, \
                                cudaStream_t);                                                                     \
+  template void launch_tracers_fast<T>(const DevMesh&, const ModelOpt&, const StageIO<T>&, RKStage, int,           \
+                                       cudaStream_t);                                                             \
   template void launch_vertex<T>(const DevMesh&, const ModelOpt&, const StageIO<T>&, Partials, bool, int,        \
                                  cudaStream_t);                                                                   \
   template void launch_edge_pv<T>(const DevMesh&, const ModelOpt&, const StageIO<T>&, int, cudaStream_t);        \
