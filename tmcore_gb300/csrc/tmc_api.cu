@@ -41,6 +41,9 @@ struct EngineBase {
   // then stages 2-4 and the final update (launch_step with first_stage 2).
   // can_split: the FP32 fused program with 1, 2 or 4 second-order tracers.
   virtual bool can_split() const { return false; }
+  // the tracers gathered from raw (original order) into state slot 0 and
+  // their FP32 ratios, on stream s; gd's FP32 shadow is left as it is
+  virtual void gather_tracers_on(const double*, cudaStream_t) {}
   virtual void launch_stage1_early(bool) {}
   virtual void launch_late_tracers() {}
   int first_stage = 1;
@@ -436,6 +439,14 @@ struct Engine : EngineBase {
            (n == 1 || n == 2 || n == 4);
   }
   void launch_stage1_early(bool diag) override { launch_stage(1, diag, true, nullptr, nullptr); }
+  void gather_tracers_on(const double* raw_q, cudaStream_t s) override {
+    if constexpr (std::is_same<T, float>::value) {
+      for (int k = 0; k < h->O.n_tracers; ++k)
+        launch_gather<T>(h->M.nc, raw_q + (size_t)k * h->M.nc, h->d_cell_n2o, q[0] + oq() + (size_t)k * h->M.nc,
+                         s);
+      launch_shadows(h->M.nc, h->O.n_tracers, gd[0] + oc(), q[0] + oq(), nullptr, qr[0] + oq(), s);
+    }
+  }
   // stage 1's tracer terms: its F (edge set 0) and next gd (slot 1) stay as
   // the stage left them until stage 2
   void launch_late_tracers() override {
@@ -1059,8 +1070,8 @@ int launch_one_step(tmc_handle* h) {
 }
 
 // One step split around the late arrival of the tracers (tmc_time_integrate):
-// stage 1 without its tracer terms, then tracers_in() (which queues the
-// tracers' gather and shadows on the stream), the stage's tracer terms, and
+// stage 1 without its tracer terms, then tracers_in() (which makes the stream
+// wait for the tracers and their FP32 ratios), the stage's tracer terms, and
 // stages 2-4 with the final update as one graph.  Same results as
 // launch_one_step.
 template <class F>
@@ -1655,9 +1666,17 @@ int tmc_time_integrate(tmc_handle* h, const double* gd_old, const double* iap_u_
   h->have_state = true;
   h->prep_valid = false;
   for (int i = 0; i < nio; ++i) {
-    if (split && io[i].field == -1) break;  // the tracers: after stage 1
+    if (split && io[i].field == -1) break;  // the tracers: beside stage 1
     cudaStreamWaitEvent(h->st, h->cev[1 + i], 0);
     h->eng->gather_field(io[i].field, io[i].raw);
+    if (split && io[i].field == F_GD) {
+      // the tracers' gather and ratios (which read gd) on the copy stream,
+      // behind their copy; stage 1 without its tracer terms reads neither
+      cudaEventRecord(h->cev[7], h->st);
+      cudaStreamWaitEvent(cs, h->cev[7], 0);
+      h->eng->gather_tracers_on(h->raw_q, cs);
+      cudaEventRecord(h->cev[3], cs);
+    }
     if (prep_early && io[i].field == F_IAP) {
       h->eng->refresh_shadows(0, false);
       ensure_prep(h);
@@ -1665,11 +1684,7 @@ int tmc_time_integrate(tmc_handle* h, const double* gd_old, const double* iap_u_
   }
   int rc;
   if (split) {
-    rc = launch_one_step_split(h, [&] {
-      cudaStreamWaitEvent(h->st, h->cev[3], 0);
-      h->eng->gather_field(-1, h->raw_q);
-      h->eng->refresh_shadows(0);
-    });
+    rc = launch_one_step_split(h, [&] { cudaStreamWaitEvent(h->st, h->cev[3], 0); });
     if (rc) return rc;
   } else {
     h->eng->refresh_shadows(0);

@@ -270,11 +270,12 @@ void launch_h_field(int nc, const double* gd, const double* ghs, double g, doubl
   k_h_field<<<nblk(nc, 256), 256, 0, st>>>(nc, gd, ghs, g, h);
 }
 
+// gdf = FP32 gd (skipped when null), qr = q / FP32 gd
 __global__ void k_shadows(int nc, int ntr, const double* gd, const float* q, float* gdf, float* qr) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nc) return;
   const float g = (float)gd[c];
-  gdf[c] = g;
+  if (gdf) gdf[c] = g;
   for (int k = 0; k < ntr; ++k) qr[(size_t)k * nc + c] = q[(size_t)k * nc + c] / g;
 }
 
