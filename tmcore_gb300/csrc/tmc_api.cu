@@ -2202,8 +2202,7 @@ struct tmc_group {
   std::vector<tmc_handle*> hs;
   std::vector<int> steps;  // per handle and cycle
   int mode = 0;
-  tmc::ens::JobTable* d_jobs = nullptr;  // mode 1: the job table in device memory
-  std::unique_ptr<tmc::ens::JobTable> jobs;  // mode 1: its host copy
+  std::unique_ptr<tmc::ens::JobTable> jobs;  // mode 1: the job table (the kernels' parameter)
   std::vector<int> order;                    // mode 1: handles by steps per cycle, most first
   int big = 0;                               // mode 1: the job whose block sizes the launches use
   cudaStream_t st = nullptr;
@@ -2215,8 +2214,8 @@ struct tmc_group {
 
 namespace {
 
-// mode 1: checks, and the job table (host copy in g->jobs, device copy in
-// g->d_jobs); returns TMC_OK or an error with g->err set
+// mode 1: checks, and the job table (g->jobs); returns TMC_OK or an error
+// with g->err set
 int prepare_batched(tmc_group* g) {
   using namespace tmc::ens;
   const int n = (int)g->hs.size();
@@ -2273,11 +2272,6 @@ int prepare_batched(tmc_group* g) {
     T->off[J_EDGES_UP][j + 1] = T->off[J_EDGES_UP][j] + ens::slots_up(h->M.ne);
     if (h->M.ne > g->hs[order[big]]->M.ne) big = j;
   }
-  if (cudaMalloc(&g->d_jobs, sizeof(JobTable)) != cudaSuccess ||
-      cudaMemcpy(g->d_jobs, T.get(), sizeof(JobTable), cudaMemcpyHostToDevice) != cudaSuccess) {
-    g->err = std::string("job table: ") + cudaGetErrorString(cudaGetLastError());
-    return TMC_E_CUDA;
-  }
   g->jobs = std::move(T);
   g->big = big;
   return TMC_OK;
@@ -2292,7 +2286,7 @@ void capture_batched(tmc_group* g) {
   for (int s = 0; s < nsub; ++s) {
     int nj = 0;
     while (nj < n && g->steps[g->order[nj]] > s) ++nj;
-    tmc::ens::launch_jobs_step(g->d_jobs, *g->jobs, nj, bsp, upwind, g->st);
+    tmc::ens::launch_jobs_step(*g->jobs, nj, bsp, upwind, g->st);
   }
 }
 
@@ -2420,7 +2414,6 @@ int tmc_group_destroy(tmc_group* g) {
   if (!g) return TMC_OK;
   if (g->st) cudaStreamSynchronize(g->st);
   if (g->graph) cudaGraphExecDestroy(g->graph);
-  if (g->d_jobs) cudaFree(g->d_jobs);
   for (cudaEvent_t e : g->ev_join) cudaEventDestroy(e);
   if (g->ev_fork) cudaEventDestroy(g->ev_fork);
   if (g->ev_done) cudaEventDestroy(g->ev_done);

@@ -13,6 +13,8 @@
 // time, and every neighbour gather of a warp reads whole 128-byte lines.
 #include <cuda_runtime.h>
 
+#include <cstring>
+
 #include "tmc_ensemble.cuh"
 
 // Minimum resident blocks per SM the heavy passes are compiled for (0: none
@@ -1087,65 +1089,81 @@ inline unsigned nb(size_t n) { return (unsigned)((n + 255) / 256); }
 // off[K][j] <= b < off[K][j + 1] (j < nj), as block b - off[K][j] of that
 // job's mesh; the bodies are those of the single-mesh kernels
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ int job_of(const JobTable* __restrict__ T, int kind, int nj, int* j) {
+__device__ __forceinline__ int job_of(const int (&off)[4][kMaxJobs + 1], int kind, int nj, int* j) {
   const int b = blockIdx.x;
   int k = 0;
-  while (k + 1 < nj && b >= T->off[kind][k + 1]) ++k;
+  while (k + 1 < nj && b >= off[kind][k + 1]) ++k;
   *j = k;
-  return b - T->off[kind][k];
+  return b - off[kind][k];
 }
 __device__ __forceinline__ double stage_adt(int stage, double dt) {
   return (stage == 1 || stage == 2) ? 0.5 * dt : (stage == 3 ? dt : 0.0);
 }
 
+// f(job j of T) with j a constant in each branch: the body then reads the
+// job's pointers at fixed offsets of the parameter (constant-bank operands,
+// as in the single-mesh kernels) rather than into registers
+template <class F>
+__device__ __forceinline__ void on_job(const StageTable& T, int j, F&& f) {
+  static_assert(kMaxJobs == 8, "one branch per job slot");
+  switch (j) {
+    case 0: f(T.job[0]); break;
+    case 1: f(T.job[1]); break;
+    case 2: f(T.job[2]); break;
+    case 3: f(T.job[3]); break;
+    case 4: f(T.job[4]); break;
+    case 5: f(T.job[5]); break;
+    case 6: f(T.job[6]); break;
+    default: f(T.job[7]); break;
+  }
+}
+
 template <int V>
-__global__ void TMC_ENS_LB(TMC_ENS_CELL_MINB) k_jobs_cell(const JobTable* __restrict__ T, int nj, int stage) {
+__global__ void TMC_ENS_LB(TMC_ENS_CELL_MINB) k_jobs_cell(const __grid_constant__ StageTable T, int nj, int stage) {
   int j;
-  const int bx = job_of(T, J_CELLS, nj, &j);
-  const Job& J = T->job[j];
-  ens_cell<V>(J.Mh, J.D, J.io[stage], RKStage{stage, stage_adt(stage, J.dt)}, J.P, 0, bx);
+  const int bx = job_of(T.off, J_CELLS, nj, &j);
+  on_job(T, j, [&](const JobStage& J) {
+    ens_cell<V>(J.Mh, J.D, J.io, RKStage{stage, stage_adt(stage, J.dt)}, J.P, 0, bx);
+  });
 }
 template <int V>
-__global__ void TMC_ENS_LB(TMC_ENS_VERT_MINB) k_jobs_vertex(const JobTable* __restrict__ T, int nj, int stage) {
+__global__ void TMC_ENS_LB(TMC_ENS_VERT_MINB) k_jobs_vertex(const __grid_constant__ StageTable T, int nj) {
   int j;
-  const int bx = job_of(T, J_VERTS, nj, &j);
-  const Job& J = T->job[j];
-  ens_vertex<V>(J.Mh, J.D, J.io[stage], J.P, 0, bx);
+  const int bx = job_of(T.off, J_VERTS, nj, &j);
+  on_job(T, j, [&](const JobStage& J) { ens_vertex<V>(J.Mh, J.D, J.io, J.P, 0, bx); });
 }
 template <int V>
-__global__ void __launch_bounds__(kMaxBS) k_jobs_edge_pv(const JobTable* __restrict__ T, int nj, int stage) {
+__global__ void __launch_bounds__(kMaxBS) k_jobs_edge_pv(const __grid_constant__ StageTable T, int nj) {
   int j;
-  const int bx = job_of(T, J_EDGES, nj, &j);
-  const Job& J = T->job[j];
-  ens_edge_pv<V>(J.Mh, J.D, J.io[stage], bx);
+  const int bx = job_of(T.off, J_EDGES, nj, &j);
+  on_job(T, j, [&](const JobStage& J) { ens_edge_pv<V>(J.Mh, J.D, J.io, bx); });
 }
 template <int V>
-__global__ void __launch_bounds__(kMaxBS) k_jobs_edge_pv_up(const JobTable* __restrict__ T, int nj, int stage) {
+__global__ void __launch_bounds__(kMaxBS) k_jobs_edge_pv_up(const __grid_constant__ StageTable T, int nj) {
   int j;
-  const int bx = job_of(T, J_EDGES_UP, nj, &j);
-  const Job& J = T->job[j];
-  ens_edge_pv_up<V>(J.Mh, J.D, J.io[stage], J.up, bx);
+  const int bx = job_of(T.off, J_EDGES_UP, nj, &j);
+  on_job(T, j, [&](const JobStage& J) { ens_edge_pv_up<V>(J.Mh, J.D, J.io, J.up, bx); });
 }
 template <int V>
-__global__ void TMC_ENS_LB(TMC_ENS_FLUX_MINB) k_jobs_edge_flux(const JobTable* __restrict__ T, int nj, int stage) {
+__global__ void TMC_ENS_LB(TMC_ENS_FLUX_MINB) k_jobs_edge_flux(const __grid_constant__ StageTable T, int nj,
+                                                               int stage) {
   int j;
-  const int bx = job_of(T, J_EDGES, nj, &j);
-  const Job& J = T->job[j];
-  ens_edge_flux<V>(J.Mh, J.D, J.io[stage], RKStage{stage, stage_adt(stage, J.dt)}, J.P, bx);
+  const int bx = job_of(T.off, J_EDGES, nj, &j);
+  on_job(T, j, [&](const JobStage& J) {
+    ens_edge_flux<V>(J.Mh, J.D, J.io, RKStage{stage, stage_adt(stage, J.dt)}, J.P, bx);
+  });
 }
 template <int V>
-__global__ void __launch_bounds__(kMaxBS) k_jobs_final_cells(const JobTable* __restrict__ T, int nj) {
+__global__ void __launch_bounds__(kMaxBS) k_jobs_final_cells(const __grid_constant__ StageTable T, int nj) {
   int j;
-  const int bx = job_of(T, J_CELLS, nj, &j);
-  const Job& J = T->job[j];
-  ens_final_cells<V>(J.Mh, J.D, J.io[0], J.diag, bx);
+  const int bx = job_of(T.off, J_CELLS, nj, &j);
+  on_job(T, j, [&](const JobStage& J) { ens_final_cells<V>(J.Mh, J.D, J.io, J.diag, bx); });
 }
 template <int V>
-__global__ void __launch_bounds__(kMaxBS) k_jobs_final_edges(const JobTable* __restrict__ T, int nj) {
+__global__ void __launch_bounds__(kMaxBS) k_jobs_final_edges(const __grid_constant__ StageTable T, int nj) {
   int j;
-  const int bx = job_of(T, J_EDGES, nj, &j);
-  const Job& J = T->job[j];
-  ens_edges<V, true>(J.Mh, J.D, J.io[0], J.diag, J.P, 1, bx);
+  const int bx = job_of(T.off, J_EDGES, nj, &j);
+  on_job(T, j, [&](const JobStage& J) { ens_edges<V, true>(J.Mh, J.D, J.io, J.diag, J.P, 1, bx); });
 }
 // the step's region sums: block (job * nr + i, group of 32 members) sums
 // region r[i] of its job, over the job's blocks of the region's element kind
@@ -1154,15 +1172,15 @@ struct StepRegions {
   int r[8];
   int kind[8];
 };
-__global__ void __launch_bounds__(kRedThreads) k_jobs_reduce(const JobTable* __restrict__ T, StepRegions R) {
+__global__ void __launch_bounds__(kRedThreads) k_jobs_reduce(const __grid_constant__ JobTable T, StepRegions R) {
   const int j = blockIdx.x / R.n, i = blockIdx.x - j * R.n;
-  const Job& J = T->job[j];
+  const Job& J = T.job[j];
   const int count = R.kind[i] == J_CELLS ? J.D.slots_c : J.D.slots_e;
   ens_reduce(J.P, R.r[i], count, J.diag);
 }
 // beta of every member of every job (blockIdx.y = job)
-__global__ void k_jobs_beta(const JobTable* __restrict__ T) {
-  const Job& J = T->job[blockIdx.y];
+__global__ void k_jobs_beta(const __grid_constant__ JobTable T) {
+  const Job& J = T.job[blockIdx.y];
   ens_beta(J.D.M, 1, 0, J.conserve, J.totalArea, J.sumAreaTriangle, J.dt, J.diag,
            blockIdx.x * blockDim.x + threadIdx.x);
 }
@@ -1320,36 +1338,49 @@ void launch_to_f32(int n, int M, int m, const double* src, float* dst, cudaStrea
 
 // One CRK4 step of the first nj jobs of T, one launch per pass (the program
 // of EnsEngine::launch_step without the closure and the diagnostics).
-void launch_jobs_step(const JobTable* T, const JobTable& hT, int nj, const int* bsp, bool upwind, cudaStream_t st) {
-  const Dims& D = hT.job[0].D;  // every job has the same members, hence V and lanes
+// the table of stage k (0: the final update) of the first nj jobs of T
+static StageTable stage_table(const JobTable& T, int nj, int k) {
+  StageTable S;
+  std::memset(&S, 0, sizeof(S));
+  std::memcpy(S.off, T.off, sizeof(S.off));
+  for (int j = 0; j < nj; ++j) {
+    const Job& J = T.job[j];
+    S.job[j] = JobStage{J.Mh, J.D, J.io[k], J.P, J.up, J.diag, J.dt};
+  }
+  return S;
+}
+
+void launch_jobs_step(const JobTable& T, int nj, const int* bsp, bool upwind, cudaStream_t st) {
+  const Dims& D = T.job[0].D;  // every job has the same members, hence V and lanes
   int th[5];
   const unsigned gy = (unsigned)(D.M / (D.LPE * D.V));
   for (int p = 0; p < 5; ++p) grid_of(1, D, bsp[p], &th[p]);
-  const dim3 gc((unsigned)hT.off[J_CELLS][nj], gy), ge((unsigned)hT.off[J_EDGES][nj], gy),
-      gv((unsigned)hT.off[J_VERTS][nj], gy), gu((unsigned)hT.off[J_EDGES_UP][nj], gy);
+  const dim3 gc((unsigned)T.off[J_CELLS][nj], gy), ge((unsigned)T.off[J_EDGES][nj], gy),
+      gv((unsigned)T.off[J_VERTS][nj], gy), gu((unsigned)T.off[J_EDGES_UP][nj], gy);
   const bool up4 = upwind && D.LPE == 32 && D.M % 128 == 0 && TMC_ENS_UP_V == 4;
   for (int k = 1; k <= 4; ++k) {
+    const StageTable S = stage_table(T, nj, k);
     if (D.V == 2) {
-      k_jobs_cell<2><<<gc, th[0], 0, st>>>(T, nj, k);
-      k_jobs_vertex<2><<<gv, th[1], 0, st>>>(T, nj, k);
+      k_jobs_cell<2><<<gc, th[0], 0, st>>>(S, nj, k);
+      k_jobs_vertex<2><<<gv, th[1], 0, st>>>(S, nj);
     } else {
-      k_jobs_cell<1><<<gc, th[0], 0, st>>>(T, nj, k);
-      k_jobs_vertex<1><<<gv, th[1], 0, st>>>(T, nj, k);
+      k_jobs_cell<1><<<gc, th[0], 0, st>>>(S, nj, k);
+      k_jobs_vertex<1><<<gv, th[1], 0, st>>>(S, nj);
     }
     if (up4)
-      k_jobs_edge_pv_up<4><<<dim3(gu.x, (unsigned)(D.M / 128)), th[2], 0, st>>>(T, nj, k);
+      k_jobs_edge_pv_up<4><<<dim3(gu.x, (unsigned)(D.M / 128)), th[2], 0, st>>>(S, nj);
     else if (upwind && D.V == 2)
-      k_jobs_edge_pv_up<2><<<gu, th[2], 0, st>>>(T, nj, k);
+      k_jobs_edge_pv_up<2><<<gu, th[2], 0, st>>>(S, nj);
     else if (upwind)
-      k_jobs_edge_pv_up<1><<<gu, th[2], 0, st>>>(T, nj, k);
+      k_jobs_edge_pv_up<1><<<gu, th[2], 0, st>>>(S, nj);
     else if (D.V == 2)
-      k_jobs_edge_pv<2><<<ge, th[2], 0, st>>>(T, nj, k);
+      k_jobs_edge_pv<2><<<ge, th[2], 0, st>>>(S, nj);
     else
-      k_jobs_edge_pv<1><<<ge, th[2], 0, st>>>(T, nj, k);
+      k_jobs_edge_pv<1><<<ge, th[2], 0, st>>>(S, nj);
     if (D.V == 2)
-      k_jobs_edge_flux<2><<<ge, th[3], 0, st>>>(T, nj, k);
+      k_jobs_edge_flux<2><<<ge, th[3], 0, st>>>(S, nj, k);
     else
-      k_jobs_edge_flux<1><<<ge, th[3], 0, st>>>(T, nj, k);
+      k_jobs_edge_flux<1><<<ge, th[3], 0, st>>>(S, nj, k);
   }
   StepRegions R{};
   for (int k = 0; k < 3; ++k) {
@@ -1360,12 +1391,13 @@ void launch_jobs_step(const JobTable* T, const JobTable& hT, int nj, const int* 
   R.r[R.n] = R_44_E, R.kind[R.n++] = J_EDGES;
   k_jobs_reduce<<<dim3((unsigned)(nj * R.n), (unsigned)D.G), kRedThreads, 0, st>>>(T, R);
   k_jobs_beta<<<dim3(nb(D.M), (unsigned)nj), 256, 0, st>>>(T);
+  const StageTable S0 = stage_table(T, nj, 0);
   if (D.V == 2) {
-    k_jobs_final_cells<2><<<gc, th[4], 0, st>>>(T, nj);
-    k_jobs_final_edges<2><<<ge, th[4], 0, st>>>(T, nj);
+    k_jobs_final_cells<2><<<gc, th[4], 0, st>>>(S0, nj);
+    k_jobs_final_edges<2><<<ge, th[4], 0, st>>>(S0, nj);
   } else {
-    k_jobs_final_cells<1><<<gc, th[4], 0, st>>>(T, nj);
-    k_jobs_final_edges<1><<<ge, th[4], 0, st>>>(T, nj);
+    k_jobs_final_cells<1><<<gc, th[4], 0, st>>>(S0, nj);
+    k_jobs_final_edges<1><<<ge, th[4], 0, st>>>(S0, nj);
   }
 }
 

@@ -162,7 +162,9 @@ void launch_finalize(const Dims& D, const Partials& P, bool step, bool diag, boo
 // every active mesh's element blocks along one element kind; block b finds
 // its mesh j from the block offsets (off[kind][j] <= b < off[kind][j + 1])
 // and runs the same per-block body as the single-mesh kernel on mesh j's
-// tables and buffers.  The table lives in device memory; the first nj jobs
+// tables and buffers.  The table (14 KB) is the kernels' __grid_constant__
+// parameter: a block reads its mesh's pointers from the constant bank as it
+// needs them instead of holding them in registers.  The first nj jobs
 // are active in a launch (the host orders the meshes by steps per cycle,
 // most first, so every sub-step's active set is a prefix).
 // ---------------------------------------------------------------------------
@@ -184,10 +186,25 @@ struct JobTable {
   int off[4][kMaxJobs + 1];  // first block of each job along each JobKind
   Job job[kMaxJobs];
 };
-// one CRK4 step of the first nj jobs (T: the table in device memory, hT: its
-// host copy for the grid sizes); bsp: block sizes of the cell, vertex,
-// edge_pv, edge_flux and final passes; upwind: the jobs run upwind pv
-void launch_jobs_step(const JobTable* T, const JobTable& hT, int nj, const int* bsp, bool upwind, cudaStream_t st);
+// What the pass kernels of one CRK4 stage (or of the final update, k = 0)
+// read of each job: that stage's buffers only, so that every pointer sits at
+// a fixed offset of the kernel parameter
+struct JobStage {
+  DevMesh Mh;
+  Dims D;
+  IO io;
+  Partials P;
+  Upwind up;
+  double* diag;
+  double dt;
+};
+struct StageTable {
+  int off[4][kMaxJobs + 1];
+  JobStage job[kMaxJobs];
+};
+// one CRK4 step of the first nj jobs of T; bsp: block sizes of the cell,
+// vertex, edge_pv, edge_flux and final passes; upwind: the jobs run upwind pv
+void launch_jobs_step(const JobTable& T, int nj, const int* bsp, bool upwind, cudaStream_t st);
 
 // The learned PV-on-edge closure (after the pv-on-edge pass): pv on cells
 // (the network reads it), then the network on rows [edge][member] with its
