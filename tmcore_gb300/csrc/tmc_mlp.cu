@@ -123,6 +123,13 @@ struct ClosureSrc {
 // Rows of the member-innermost layout: row i = element i / M, member i % M,
 // the order of the arrays, so the 128 rows of a tile read whole lines.  The
 // features are those of closure_features, from [element][member] arrays.
+// log2(n) for a power of two n, else -1
+inline int pow2_shift(int n) {
+  if (n <= 0 || (n & (n - 1))) return -1;
+  int k = 0;
+  while ((1 << k) < n) ++k;
+  return k;
+}
 struct EnsClosureSrc {
   DevMesh M;
   tmc::ens::IO S;
@@ -131,9 +138,20 @@ struct EnsClosureSrc {
   float* dq;  // non-null: the correction is also held here (0 for members switched off)
   int mem;
   long long rows;
+  int mshift;  // log2(mem) when mem is a power of two (shift and mask), else -1 (division)
+  __device__ __forceinline__ void split(long long i, int& e, int& m) const {
+    if (mshift >= 0) {
+      e = (int)(i >> mshift);
+      m = (int)i & (mem - 1);
+    } else {
+      e = (int)(i / mem);
+      m = (int)(i - (long long)e * mem);
+    }
+  }
   __device__ bool features(long long i, float (&x)[kIn]) const {
     if (i >= rows) return false;
-    const int e = (int)(i / mem), m = (int)(i - (long long)e * mem);
+    int e, m;
+    split(i, e, m);
     const size_t W = (size_t)mem;
     const int c1 = M.cellsOnEdge[e], c2 = M.cellsOnEdge[M.ne + e];
     const int v1 = M.verticesOnEdge[e], v2 = M.verticesOnEdge[M.ne + e];
@@ -172,7 +190,8 @@ struct EnsClosureSrc {
   }
   __device__ void output(long long i, float r) const {
     if (i >= rows) return;
-    const int m = (int)(i % mem);
+    int e, m;
+    split(i, e, m);
     const float v = on[m] ? r : 0.f;
     if (dq) dq[i] = v;
     if (on[m]) S.pv_e[i] = S.pv_e[i] + v;
@@ -574,7 +593,7 @@ void launch_closure(const DevMesh& Mh, const Dims& D, const IO& S, const float* 
     return;
   }
   const long long rows = (long long)Mh.ne * D.M;
-  EnsClosureSrc src{Mh, S, pv_c, a.member_on, a.mode == 1 ? a.dq : nullptr, D.M, rows};
+  EnsClosureSrc src{Mh, S, pv_c, a.member_on, a.mode == 1 ? a.dq : nullptr, D.M, rows, pow2_shift(D.M)};
   const long long ntiles = (rows + kTile - 1) / kTile;
   const int grid = (int)std::min<long long>((ntiles + kGroups - 1) / kGroups, (long long)a.sms * 4);
   static bool attr = false;
@@ -586,7 +605,7 @@ void launch_closure(const DevMesh& Mh, const Dims& D, const IO& S, const float* 
 }
 void launch_closure_features(const DevMesh& Mh, const Dims& D, const IO& S, const float* pv_c, int m, float* feat,
                              float* pv, cudaStream_t st) {
-  const EnsClosureSrc src{Mh, S, pv_c, nullptr, nullptr, D.M, (long long)Mh.ne * D.M};
+  const EnsClosureSrc src{Mh, S, pv_c, nullptr, nullptr, D.M, (long long)Mh.ne * D.M, pow2_shift(D.M)};
   k_closure_features_inner<<<(Mh.ne + 255) / 256, 256, 0, st>>>(src, m, feat, pv);
 }
 }  // namespace ens
