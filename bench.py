@@ -198,16 +198,27 @@ def pass_bytes(nc: int, ne: int, nv: int, S: int, ntr: int, diag: bool = True) -
     cell = vert = epv = flux = 0.0
     for k in (1, 2, 3, 4):
         dg = diag and k == 1
-        # cell: nEdgesOnCell, edgesOnCell, nSign, cellsOnCell (tracers), 1/areaCell (f64) [+ f32 copies],
-        # gd, ghs, E out; per edge u, F, dvEdge, areaEdge; tracer values of the neighbours;
-        # RK of gd (f64) and tracers (S)
-        rk_gd = {1: 8 + 8 + sh + 8 + sh, 2: Mw + 2 * sh + 16 + 8 + 8 + sh,
-                 3: Mw + 2 * sh + 16 + 8 + 8 + sh, 4: Mw + 2 * sh + 16}[k]
-        if S == 8:
-            rk_gd = {1: 8 * 4, 2: 8 * 6, 3: 8 * 6, 4: 8 * 4}[k]
-        rk_q = {1: 4 * S, 2: 5 * S, 3: 5 * S, 4: 2 * S}[k] + (sh if k <= 3 else 0)
-        cell += nc * (1 + 24 + 6 + (24 if ntr else 0) + 8 + 2 * sh + S + S + S + rk_gd + ntr * (S + rk_q)
-                      + (24 if dg else 0)) + ne * (2 * S + 2 * Mw)
+        # cell, access by access; per edge u, F, dvEdge, areaEdge (16 B FP32); the neighbours'
+        # tracer values come from the same array as the cell's own (perfect reuse)
+        if S == 4:
+            # k_cell_fast: edgesOnCell, nSign, cellsOnCell (tracers), 1/areaCell (f64 and f32), the
+            # gd and ghs shadows, E out; RK of gd: old r (stages 1-3), acc r (2-4) and w, tendency
+            # shadow r (2-4) and w, areaCell_f (2-4), next gd and its shadow w (1-3); per tracer:
+            # ratio r, mass of old r (1-3), acc r (2-4) and w, next ratio w (1-3); invariants
+            # (stage 1): gd, areaCell, areaCell_f
+            base = 24 + 6 + (24 if ntr else 0) + 8 + 4 + 4 + 4 + 4
+            rk_gd = {1: 32, 2: 48, 3: 48, 4: 28}[k]
+            trq = {1: 16, 2: 20, 3: 20, 4: 12}[k]
+            dgb = 20
+        else:
+            # k_cell<double>: nEdgesOnCell, edgesOnCell, nSign, cellsOnCell (tracers), areaCell, gd,
+            # ghs, E out; RK of gd; per tracer: mass of the stage r (= old in stage 1), old r
+            # (2-3), acc r (2-4) and w, next w (1-3)
+            base = 1 + 24 + 6 + (24 if ntr else 0) + 8 + 3 * 8
+            rk_gd = {1: 32, 2: 48, 3: 48, 4: 32}[k]
+            trq = {1: 24, 2: 40, 3: 40, 4: 24}[k]
+            dgb = 24
+        cell += nc * (base + rk_gd + ntr * trq + (dgb if dg else 0)) + ne * (2 * S + 2 * Mw)
         # vertex: cellsOnVertex, edgesOnVertex, kite, tSign, 1/areaTriangle, fVertex; pv out;
         # gd and u, dcEdge gathered
         vert += nv * (12 + 12 + 3 * Mw + 3 + Mw + Mw + S + (16 if dg else 0)) + nc * S + ne * (S + Mw)

@@ -563,13 +563,13 @@ __global__ void __launch_bounds__(kMaxBlock) k_cell(DevMesh M, ModelOpt O, Stage
           case 1:
             S.q_acc[qi] = tq[j];
             qnext = qo[j] + adt * tq[j];
-            S.q_next[qi] = qnext;
+            if constexpr (kF64<T>) S.q_next[qi] = qnext;  // FP32: the next stage reads the ratio only
             break;
           case 2:
           case 3:
             S.q_acc[qi] = qa[j] + T(2) * tq[j];
             qnext = qo[j] + adt * tq[j];
-            S.q_next[qi] = qnext;
+            if constexpr (kF64<T>) S.q_next[qi] = qnext;
             break;
           case 4:
             if constexpr (kF64<T>)
@@ -1348,7 +1348,9 @@ __device__ __forceinline__ void tracer_tend_f(const float (&ns)[kME], const floa
     tq[j] = -sq * invAf;
   }
 }
-// ... and its RK update (mode as RKStage; gnf the stage's next gd in FP32)
+// ... and its RK update (mode as RKStage; gnf the stage's next gd in FP32).
+// The next stage reads the mixing ratio only (and q_old, q_acc), so the
+// stage's tracer mass itself is not stored.
 template <int NTR, int NQ>
 __device__ __forceinline__ void tracer_update_f(const StageIO<float>& S, size_t nc, int c, int mode, float adt,
                                                 const float (&tq)[NQ], const float (&qo)[NQ], const float (&qa)[NQ],
@@ -1365,7 +1367,6 @@ __device__ __forceinline__ void tracer_update_f(const StageIO<float>& S, size_t 
     }
     if (mode <= 3) {
       const float qnext = qo[j] + adt * tq[j];
-      S.q_next[qi] = qnext;
       S.qr_next[qi] = qnext / gnf;
     }
   }
