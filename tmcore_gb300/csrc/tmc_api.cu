@@ -2208,6 +2208,9 @@ struct tmc_group {
   cudaStream_t st = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_done = nullptr;
   std::vector<cudaEvent_t> ev_join;
+  // mode 1: the stages' vertex and pv-on-edge passes beside the cell pass
+  cudaStream_t side = nullptr;
+  cudaEvent_t side_fork = nullptr, side_join = nullptr;
   cudaGraphExec_t graph = nullptr;
   std::string err;
 };
@@ -2286,7 +2289,7 @@ void capture_batched(tmc_group* g) {
   for (int s = 0; s < nsub; ++s) {
     int nj = 0;
     while (nj < n && g->steps[g->order[nj]] > s) ++nj;
-    tmc::ens::launch_jobs_step(*g->jobs, nj, bsp, upwind, g->st);
+    tmc::ens::launch_jobs_step(*g->jobs, nj, bsp, upwind, g->st, g->side, g->side_fork, g->side_join);
   }
 }
 
@@ -2349,6 +2352,10 @@ int tmc_group_create_ex(tmc_handle* const* handles, int32_t n, double cycle_seco
       *out = g.release();
       return rc;
     }
+    if (cudaStreamCreateWithFlags(&g->side, cudaStreamNonBlocking) != cudaSuccess) return cerr("cudaStreamCreate");
+    if (cudaEventCreateWithFlags(&g->side_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&g->side_join, cudaEventDisableTiming) != cudaSuccess)
+      return cerr("cudaEventCreate");
   }
   cudaGraph_t graph = nullptr;
   if (cudaStreamBeginCapture(g->st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return cerr("BeginCapture");
@@ -2417,6 +2424,9 @@ int tmc_group_destroy(tmc_group* g) {
   for (cudaEvent_t e : g->ev_join) cudaEventDestroy(e);
   if (g->ev_fork) cudaEventDestroy(g->ev_fork);
   if (g->ev_done) cudaEventDestroy(g->ev_done);
+  if (g->side_fork) cudaEventDestroy(g->side_fork);
+  if (g->side_join) cudaEventDestroy(g->side_join);
+  if (g->side) cudaStreamDestroy(g->side);
   if (g->st) cudaStreamDestroy(g->st);
   delete g;
   return TMC_OK;

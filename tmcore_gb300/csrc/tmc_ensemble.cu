@@ -1350,7 +1350,8 @@ static StageTable stage_table(const JobTable& T, int nj, int k) {
   return S;
 }
 
-void launch_jobs_step(const JobTable& T, int nj, const int* bsp, bool upwind, cudaStream_t st) {
+void launch_jobs_step(const JobTable& T, int nj, const int* bsp, bool upwind, cudaStream_t st, cudaStream_t side,
+                      cudaEvent_t fork, cudaEvent_t join) {
   const Dims& D = T.job[0].D;  // every job has the same members, hence V and lanes
   int th[5];
   const unsigned gy = (unsigned)(D.M / (D.LPE * D.V));
@@ -1358,25 +1359,35 @@ void launch_jobs_step(const JobTable& T, int nj, const int* bsp, bool upwind, cu
   const dim3 gc((unsigned)T.off[J_CELLS][nj], gy), ge((unsigned)T.off[J_EDGES][nj], gy),
       gv((unsigned)T.off[J_VERTS][nj], gy), gu((unsigned)T.off[J_EDGES_UP][nj], gy);
   const bool up4 = upwind && D.LPE == 32 && D.M % 128 == 0 && TMC_ENS_UP_V == 4;
+  const bool branch = side && fork && join;
+  const cudaStream_t sv = branch ? side : st;
   for (int k = 1; k <= 4; ++k) {
     const StageTable S = stage_table(T, nj, k);
+    if (branch) {
+      cudaEventRecord(fork, st);
+      cudaStreamWaitEvent(side, fork, 0);
+    }
     if (D.V == 2) {
       k_jobs_cell<2><<<gc, th[0], 0, st>>>(S, nj, k);
-      k_jobs_vertex<2><<<gv, th[1], 0, st>>>(S, nj);
+      k_jobs_vertex<2><<<gv, th[1], 0, sv>>>(S, nj);
     } else {
       k_jobs_cell<1><<<gc, th[0], 0, st>>>(S, nj, k);
-      k_jobs_vertex<1><<<gv, th[1], 0, st>>>(S, nj);
+      k_jobs_vertex<1><<<gv, th[1], 0, sv>>>(S, nj);
     }
     if (up4)
-      k_jobs_edge_pv_up<4><<<dim3(gu.x, (unsigned)(D.M / 128)), th[2], 0, st>>>(S, nj);
+      k_jobs_edge_pv_up<4><<<dim3(gu.x, (unsigned)(D.M / 128)), th[2], 0, sv>>>(S, nj);
     else if (upwind && D.V == 2)
-      k_jobs_edge_pv_up<2><<<gu, th[2], 0, st>>>(S, nj);
+      k_jobs_edge_pv_up<2><<<gu, th[2], 0, sv>>>(S, nj);
     else if (upwind)
-      k_jobs_edge_pv_up<1><<<gu, th[2], 0, st>>>(S, nj);
+      k_jobs_edge_pv_up<1><<<gu, th[2], 0, sv>>>(S, nj);
     else if (D.V == 2)
-      k_jobs_edge_pv<2><<<ge, th[2], 0, st>>>(S, nj);
+      k_jobs_edge_pv<2><<<ge, th[2], 0, sv>>>(S, nj);
     else
-      k_jobs_edge_pv<1><<<ge, th[2], 0, st>>>(S, nj);
+      k_jobs_edge_pv<1><<<ge, th[2], 0, sv>>>(S, nj);
+    if (branch) {
+      cudaEventRecord(join, side);
+      cudaStreamWaitEvent(st, join, 0);
+    }
     if (D.V == 2)
       k_jobs_edge_flux<2><<<ge, th[3], 0, st>>>(S, nj, k);
     else

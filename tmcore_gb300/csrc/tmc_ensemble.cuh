@@ -203,8 +203,12 @@ struct StageTable {
   JobStage job[kMaxJobs];
 };
 // one CRK4 step of the first nj jobs of T; bsp: block sizes of the cell,
-// vertex, edge_pv, edge_flux and final passes; upwind: the jobs run upwind pv
-void launch_jobs_step(const JobTable& T, int nj, const int* bsp, bool upwind, cudaStream_t st);
+// vertex, edge_pv, edge_flux and final passes; upwind: the jobs run upwind pv.
+// With a side stream (and two events for the fork and the join) each stage's
+// vertex and pv-on-edge passes run on it beside the cell pass: they read only
+// the stage's input gd and edge set, and the cell pass reads nothing they write.
+void launch_jobs_step(const JobTable& T, int nj, const int* bsp, bool upwind, cudaStream_t st,
+                      cudaStream_t side = nullptr, cudaEvent_t fork = nullptr, cudaEvent_t join = nullptr);
 
 // The learned PV-on-edge closure (after the pv-on-edge pass): pv on cells
 // (the network reads it), then the network on rows [edge][member] with its
