@@ -12,6 +12,7 @@ struct FinalizeArgs {
   int counts[R_COUNT];
   double totalArea, sumAreaTriangle, dt;
   int step, diag, conserve, scheme;
+  int split;  // blocks per region (1..kFinSplit)
 };
 
 // Fixed-order double-double sum of `count` per-block partials (hi, lo pairs),
@@ -38,10 +39,11 @@ __device__ double region_sum_dd(const double* reg, int count) {
   return w.hi + w.lo;
 }
 
-// kFinSplit blocks per partial region, each a fixed-order double-double
-// reduction of a contiguous 1/kFinSplit of the region's per-block partials
-// into P.fin; the last block to finish (atomic counter, no waiting) combines
-// each region's kFinSplit sums in order (one thread per region), then the
+// a.split blocks per partial region (kFinSplit for one model, 1 per member
+// of a batch), each a fixed-order double-double reduction of a contiguous
+// 1/a.split of the region's per-block partials into P.fin; the last block to
+// finish (atomic counter, no waiting) combines each region's a.split sums in
+// order (one thread per region), then the
 // region sums into beta and the invariants (time_scheme_mod.F90:144-150;
 // tmcore_swm_mod.F90:215-255), and re-arms the counter.  With one block per
 // region the widest region (15,360 partials at level 9) cost ~15,000 cycles
@@ -54,10 +56,10 @@ __global__ void __launch_bounds__(256) k_finalize(Partials P0, FinalizeArgs a, d
   double* res = res0 + (size_t)blockIdx.y * kDiagStride;
   unsigned int* counter = reinterpret_cast<unsigned int*>(reinterpret_cast<double*>(counter0) +
                                                           (size_t)blockIdx.y * kDiagStride);
-  const int r = blockIdx.x / kFinSplit, part = blockIdx.x - r * kFinSplit;
+  const int r = blockIdx.x / a.split, part = blockIdx.x - r * a.split;
   const bool want = (r <= R_44_E) ? a.step : a.diag;
   if (want) {
-    const int count = a.counts[r], chunk = (count + kFinSplit - 1) / kFinSplit;
+    const int count = a.counts[r], chunk = (count + a.split - 1) / a.split;
     const int i0 = min(count, part * chunk), i1 = min(count, i0 + chunk);
     const DD v = region_sum_pair(P.region(r) + 2 * (size_t)i0, i1 - i0);
     if (threadIdx.x == 0) {
@@ -78,7 +80,7 @@ __global__ void __launch_bounds__(256) k_finalize(Partials P0, FinalizeArgs a, d
     const int q = threadIdx.x;
     DD acc{0.0, 0.0};
     if ((q <= R_44_E) ? a.step : a.diag)
-      for (int k = 0; k < kFinSplit; ++k)  // L2 loads: the other blocks wrote them
+      for (int k = 0; k < a.split; ++k)  // L2 loads: the other blocks wrote them
         acc = dd_add(acc, DD{__ldcg(P.fin + 2 * (q * kFinSplit + k)), __ldcg(P.fin + 2 * (q * kFinSplit + k) + 1)});
     rs[q] = acc.hi + acc.lo;
     res[q] = rs[q];
@@ -127,11 +129,18 @@ void launch_finalize(Partials P, const int* counts_host, double totalArea, doubl
   a.diag = diag ? 1 : 0;
   a.conserve = conserve ? 1 : 0;
   a.scheme = scheme;
+  // A single model's widest region (the edge partials of level 9: 15,360)
+  // would leave one block's FP64 additions on one SM's 2-lane FP64 pipe, so
+  // each region is split over kFinSplit blocks.  A batch of members already
+  // has a block per region and member; splitting it too multiplies the
+  // blocks' fixed cost of a double-double block reduction (512 level-6
+  // members: 0.2 -> 4 ms per step).
+  a.split = members > 1 ? 1 : kFinSplit;
   // scratch after the kDiagLen outputs: R_COUNT region sums, then the counter
   double* res = diag_out + kDiagLen;
   unsigned int* counter = reinterpret_cast<unsigned int*>(diag_out + kDiagLen + R_COUNT);
-  k_finalize<<<dim3(kFinalizeRegions * kFinSplit, members > 1 ? members : 1), 256, 0, st>>>(P, a, diag_out, res,
-                                                                                           counter);
+  k_finalize<<<dim3(kFinalizeRegions * a.split, members > 1 ? members : 1), 256, 0, st>>>(P, a, diag_out, res,
+                                                                                         counter);
 }
 
 // Conservative APVM epsilon (operators_mod.F90:349-354): one block per sum
