@@ -39,8 +39,8 @@ __device__ double region_sum_dd(const double* reg, int count) {
   return w.hi + w.lo;
 }
 
-// a.split blocks per partial region (kFinSplit for one model, 1 per member
-// of a batch), each a fixed-order double-double reduction of a contiguous
+// a.split blocks per partial region (kFinSplit for one model, fewer for a
+// batch of members), each a fixed-order double-double reduction of a contiguous
 // 1/a.split of the region's per-block partials into P.fin; the last block to
 // finish (atomic counter, no waiting) combines each region's a.split sums in
 // order (one thread per region), then the
@@ -132,10 +132,12 @@ void launch_finalize(Partials P, const int* counts_host, double totalArea, doubl
   // A single model's widest region (the edge partials of level 9: 15,360)
   // would leave one block's FP64 additions on one SM's 2-lane FP64 pipe, so
   // each region is split over kFinSplit blocks.  A batch of members already
-  // has a block per region and member; splitting it too multiplies the
+  // has a block per region and member; splitting it as much multiplies the
   // blocks' fixed cost of a double-double block reduction (512 level-6
-  // members: 0.2 -> 4 ms per step).
-  a.split = members > 1 ? 1 : kFinSplit;
+  // members: 0.2 -> 4 ms per step), so the split shrinks with the members
+  // (about kFinSplit x the regions' blocks in all).
+  const int nm = members > 1 ? members : 1;
+  a.split = kFinSplit / nm > 1 ? kFinSplit / nm : 1;
   // scratch after the kDiagLen outputs: R_COUNT region sums, then the counter
   double* res = diag_out + kDiagLen;
   unsigned int* counter = reinterpret_cast<unsigned int*>(diag_out + kDiagLen + R_COUNT);
