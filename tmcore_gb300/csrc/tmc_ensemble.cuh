@@ -202,6 +202,8 @@ struct StageTable {
   int off[4][kMaxJobs + 1];
   JobStage job[kMaxJobs];
 };
+// both are kernel parameters (__grid_constant__), whose size CUDA caps
+static_assert(sizeof(JobTable) <= 32764 && sizeof(StageTable) <= 32764, "job tables exceed the kernel parameter limit");
 // one CRK4 step of the first nj jobs of T; bsp: block sizes of the cell,
 // vertex, edge_pv, edge_flux and final passes; upwind: the jobs run upwind pv.
 // With a side stream (and two events for the fork and the join) each stage's
