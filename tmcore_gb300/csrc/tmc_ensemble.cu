@@ -21,7 +21,8 @@
 // given).  Any minimum changes the compiler's register heuristics: on 512
 // level-6 members, 1 (flux 96, cell 110 registers with two members per
 // lane) measured 4.87 ms per step, none 5.07, 3 4.94, flux 4 (64 registers,
-// spilled) 5.50.
+// spilled) 5.50; vertex 4 (64 registers against 71, 44 bytes of spill
+// loads) 125.7 against 122.7 us per launch.
 #ifndef TMC_ENS_FLUX_MINB
 #define TMC_ENS_FLUX_MINB 1
 #endif
