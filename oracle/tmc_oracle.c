@@ -957,7 +957,11 @@ static void crk4(orc_model* m, spatial_fn so, update_fn up) {
     double R1R2 = inner_product_tend(m, TD(one), TD(two));
     double R2R3 = inner_product_tend(m, TD(two), TD(three));
     double R3R4 = inner_product_tend(m, TD(three), TD(four));
-    beta = (R1R2 + R2R3 + R3R4) / (3.0 * R4R4);
+    /* Divergence: the reference divides 0 / 0 here when the tendency is zero
+     * everywhere (a state at rest), and the step turns NaN; its PC2 guards
+     * the same case with beta = 1 (time_scheme_mod.F90:178), which CRK4 and
+     * CRK3 take here too. */
+    beta = R4R4 != 0.0 ? (R1R2 + R2R3 + R3R4) / (3.0 * R4R4) : 1.0;
   }
   m->beta = beta;
   up(m, beta * dt, TD(new_), ST(old), ST(new_));
@@ -985,7 +989,7 @@ static void crk3(orc_model* m, spatial_fn so, update_fn up) {
     double R1R2 = inner_product_tend(m, TD(one), TD(two));
     double R1R3 = inner_product_tend(m, TD(one), TD(three));
     double R2R3 = inner_product_tend(m, TD(two), TD(three));
-    beta = (2.0 * R1R2 - R1R3 + 2.0 * R2R3) / (3.0 * R4R4);
+    beta = R4R4 != 0.0 ? (2.0 * R1R2 - R1R3 + 2.0 * R2R3) / (3.0 * R4R4) : 1.0; /* as in crk4 */
   }
   m->beta = beta;
   up(m, beta * dt, TD(new_), ST(old), ST(new_));

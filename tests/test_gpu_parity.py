@@ -481,3 +481,46 @@ def test_concurrent_branches_match_the_serial_program(mesh4, prec, layout, membe
     assert np.array_equal(a.diag_all() if members > 1 else a.diag(), b.diag_all() if members > 1 else b.diag())
     a.close()
     b.close()
+
+
+@pytest.mark.parametrize("kw", [
+    dict(precision=0),
+    dict(precision=1, n_tracers=2),
+    dict(precision=1, time_scheme=1),
+    dict(precision=1, members=2),
+    dict(precision=1, members=16, member_layout=1),
+])
+def test_state_at_rest_stays_at_rest(mesh4, kw):
+    """A flat depth and no wind: every tendency is zero, so CRK4's (and
+    CRK3's) beta would be 0 / 0 (time_scheme_mod.F90:145, :99).  The device
+    takes beta = 1 there, as the reference's PC2 does (:178) and the oracle
+    does: the state stays exactly as it was, with finite invariants."""
+    from tmcore_gb300 import cases
+    from tmcore_gb300.gpu import TMCoreGPU
+
+    gd = np.full(mesh4.nCells, 9.80616 * 5000.0)
+    u = np.zeros(mesh4.nEdges)
+    ghs = np.zeros(mesh4.nCells)
+    g = TMCoreGPU(mesh4, dt=600.0, pv_scheme=1, apvm_weight=0.0, conserve_energy=1, **kw)
+    members = kw.get("members", 1)
+    for m in range(members):
+        if members > 1:
+            g.select_member(m)
+        g.set_initial(gd, u, ghs)
+        if kw.get("n_tracers"):
+            g.set_tracers(cases.smooth_tracers(mesh4, kw["n_tracers"], seed=3) * gd[None, :])
+    before = []
+    for m in range(members):
+        if members > 1:
+            g.select_member(m)
+        before.append(g.get_state()[0])
+    g.step(3)
+    d = g.diag_all() if members > 1 else g.diag()[None, :]
+    assert np.all(np.isfinite(d))
+    assert np.all(d[:, 4] == 1.0)
+    for m in range(members):
+        if members > 1:
+            g.select_member(m)
+        g1, i1, _ = g.get_state()
+        assert np.array_equal(g1, before[m]) and not np.any(i1)
+    g.close()

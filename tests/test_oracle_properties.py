@@ -1,0 +1,126 @@
+"""Property tests of the CPU FP64 oracle on random fields (hypothesis).
+
+The reference's design guarantees these for any input, not only for the
+seeded fields of test_oracle.py; hypothesis draws the fields:
+
+* the operators are linear (div_operator, curl_operator, the c2e / c2v
+  interpolations: operators_mod.F90:40-55, 76-123);
+* the curl of a discrete gradient vanishes and the area-weighted divergence
+  of any edge flux sums to zero over the sphere;
+* q.F_perp does no work for any flux and any edge pv
+  (calc_tangent_vor_flux, operators_mod.F90:239-260);
+* interpolation keeps constants;
+* CRK4 with beta (time_scheme_mod.F90:109-154) conserves mass and energy to
+  round-off from any positive-depth state.
+"""
+import numpy as np
+import pytest
+
+from conftest import icos
+
+hyp = pytest.importorskip("hypothesis")
+st = pytest.importorskip("hypothesis.strategies")
+ORACLE = pytest.importorskip("oracle.oracle")
+
+from hypothesis import given, settings  # noqa: E402
+
+RADIUS = 6371220.0
+SETTINGS = dict(max_examples=25, deadline=None, derandomize=True)
+
+
+@pytest.fixture(scope="module")
+def mesh():
+    return icos(2)
+
+
+@pytest.fixture(scope="module")
+def oracle(mesh):
+    o = ORACLE.Oracle(mesh)
+    yield o
+    o.close()
+
+
+def fields(seed, n, scale):
+    return scale * np.random.default_rng(seed).standard_normal(n)
+
+
+seeds = st.integers(min_value=0, max_value=2**31 - 1)
+scales = st.floats(min_value=1e-3, max_value=1e3)
+coefs = st.floats(min_value=-10.0, max_value=10.0)
+
+
+@settings(**SETTINGS)
+@given(seed=seeds, a=coefs, b=coefs, scale=scales)
+def test_operators_are_linear(mesh, oracle, seed, a, b, scale):
+    nc, ne, nv = mesh.nCells, mesh.nEdges, mesh.nVertices
+    cases = [("div", ne, nc), ("curl", ne, nv), ("c2e", nc, ne), ("c2v", nc, nv)]
+    for k, (name, nin, nout) in enumerate(cases):
+        x = fields(seed + 2 * k, nin, scale)
+        y = fields(seed + 2 * k + 1, nin, scale)
+        lhs = oracle.op(name, a * x + b * y, out_size=nout)
+        rhs = a * oracle.op(name, x, out_size=nout) + b * oracle.op(name, y, out_size=nout)
+        ref = np.max(np.abs(a * oracle.op(name, x, out_size=nout))) + np.max(
+            np.abs(b * oracle.op(name, y, out_size=nout))) + 1e-300
+        assert np.max(np.abs(lhs - rhs)) <= 1e-13 * ref, name
+
+
+@settings(**SETTINGS)
+@given(seed=seeds, scale=scales, offset=coefs)
+def test_curl_of_gradient_vanishes(mesh, oracle, seed, scale, offset):
+    f = fields(seed, mesh.nCells, scale) + offset * scale
+    dc = mesh.dcEdge * RADIUS
+    c1, c2 = mesh.cellsOnEdge[:, 0] - 1, mesh.cellsOnEdge[:, 1] - 1
+    grad = (f[c2] - f[c1]) / dc
+    curl = oracle.op("curl", grad, out_size=mesh.nVertices)
+    assert np.max(np.abs(curl)) <= 1e-12 * np.max(np.abs(grad)) / np.min(dc)
+
+
+@settings(**SETTINGS)
+@given(seed=seeds, scale=scales)
+def test_divergence_sums_to_zero(mesh, oracle, seed, scale):
+    fe = fields(seed, mesh.nEdges, scale)
+    div = oracle.op("div", fe, out_size=mesh.nCells)
+    area = mesh.areaCell * RADIUS ** 2
+    assert abs(np.sum(div * area)) <= 1e-12 * np.sum(np.abs(div * area))
+
+
+@settings(**SETTINGS)
+@given(seed=seeds, scale=scales, depth=st.floats(min_value=0.5, max_value=5e4))
+def test_tangent_vor_flux_does_no_work(mesh, oracle, seed, scale, depth):
+    rng = np.random.default_rng(seed)
+    u = scale * rng.standard_normal(mesh.nEdges)
+    ge = depth * rng.uniform(0.5, 2.0, mesh.nEdges)
+    pe = rng.standard_normal(mesh.nEdges)
+    flx = oracle.op("tangent_vor_flux", u, ge, pe, out_size=mesh.nEdges)
+    terms = oracle.area_edge() * u * ge * flx
+    assert abs(np.sum(terms)) <= 1e-13 * np.sum(np.abs(terms))
+
+
+@settings(**SETTINGS)
+@given(c=st.floats(min_value=-1e6, max_value=1e6, allow_subnormal=False))
+def test_interpolation_keeps_constants(mesh, oracle, c):
+    one = np.full(mesh.nCells, c)
+    tol = 1e-14 * max(abs(c), 1e-300)
+    assert np.max(np.abs(oracle.op("c2e", one, out_size=mesh.nEdges) - c)) <= tol
+    assert np.max(np.abs(oracle.op("c2v", one, out_size=mesh.nVertices) - c)) <= 10 * tol
+
+
+@settings(max_examples=8, deadline=None, derandomize=True)
+@given(seed=seeds, amp=st.floats(min_value=0.0, max_value=0.05), umax=st.floats(min_value=0.0, max_value=20.0))
+def test_crk4_conserves_mass_and_energy(mesh, seed, amp, umax):
+    """From a random positive-depth state with a random (divergent) wind."""
+    rng = np.random.default_rng(seed)
+    g, h0 = 9.80616, 5000.0
+    gd = g * h0 * (1.0 + amp * rng.uniform(-1.0, 1.0, mesh.nCells))
+    u = umax * rng.uniform(-1.0, 1.0, mesh.nEdges)
+    ghs = np.zeros(mesh.nCells)
+    o = ORACLE.Oracle(mesh, dt=600.0, pv_scheme=1, apvm_weight=0.0, adv_order=2, conserve_energy=1)
+    try:
+        o.set_initial(gd, u, ghs)
+        m0, e0 = o.diag()[:2]
+        o.step(3)
+        m1, e1 = o.diag()[:2]
+    finally:
+        o.close()
+    assert abs(m1 - m0) <= 1e-13 * abs(m0)
+    assert abs(e1 - e0) <= 1e-12 * abs(e0)

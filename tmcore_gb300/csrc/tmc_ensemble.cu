@@ -1000,7 +1000,8 @@ __device__ __forceinline__ void ens_beta(int M, int step, int diag, int conserve
     double R[4];
     for (int k = 0; k < 3; ++k) R[k] = (rv[R_IP_E + 2 * k] + rv[R_IP_C + 2 * k]) / totalArea;
     R[3] = (rv[R_44_E] + rv[R_44_C]) / totalArea;
-    const double beta = conserve ? (R[0] + R[1] + R[2]) / (3.0 * R[3]) : 1.0;
+    // beta = 1 for a member whose tendency is zero everywhere (k_finalize)
+    const double beta = conserve && R[3] != 0.0 ? (R[0] + R[1] + R[2]) / (3.0 * R[3]) : 1.0;
     out[4] = beta;
     out[5] = R[0];
     out[6] = R[1];

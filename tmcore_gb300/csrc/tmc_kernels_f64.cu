@@ -95,11 +95,14 @@ __global__ void __launch_bounds__(256) k_finalize(Partials P0, FinalizeArgs a, d
     double beta = 1.0;
     if (a.conserve) {
       if (a.scheme == 1)  // CRK3: R[0] = <t1,t2>, R[1] = <t1,t3>, R[2] = <t2,t3>
-        beta = (2.0 * R[0] - R[1] + 2.0 * R[2]) / (3.0 * R[3]);
+        beta = R[3] != 0.0 ? (2.0 * R[0] - R[1] + 2.0 * R[2]) / (3.0 * R[3]) : 1.0;
       else if (a.scheme == 3)  // PC2: R[0] = <t_old,t_new>, R[3] = <t_new,t_new>
         beta = (R[0] != 0.0 && R[3] != 0.0) ? R[0] / R[3] : 1.0;
-      else
-        beta = (R[0] + R[1] + R[2]) / (3.0 * R[3]);
+      else  // CRK4
+        beta = R[3] != 0.0 ? (R[0] + R[1] + R[2]) / (3.0 * R[3]) : 1.0;
+      // time_scheme_mod.F90:145 (CRK4) and :94-100 (CRK3) divide 0 / 0 when the
+      // tendency is zero everywhere (a state at rest); beta = 1 there, as the
+      // reference's PC2 has it (:178)
     }
     out[4] = beta;
     out[5] = R[0];
