@@ -690,7 +690,11 @@ static void pv_on_edge_conservative_apvm(orc_model* m, const double* u, const do
   for (int k = 0; k < m->nv; ++k) s1 = s1 + pv_v[k] * pv_v[k] * gd_tend_v[k] * m->areaTriangle[k];
   for (int k = 0; k < m->nv; ++k) s2 = s2 + pv_v[k] * vt[k] * m->areaTriangle[k];
   for (int k = 0; k < m->nv; ++k) s3 = s3 + pv_v[k] * dvt[k] * m->areaTriangle[k];
-  double eps = -(s1 - s2 * 2.0) / (2.0 * dt * s3);
+  /* Divergence: with no wind dpv is zero on every edge, s3 = 0 and the
+   * reference's eps is 0 / 0 (operators_mod.F90:349-351), which turns pv_edge
+   * and the step NaN; eps = 0 here (pv_edge - eps dt dpv is then the same for
+   * any finite eps). */
+  double eps = s3 != 0.0 ? -(s1 - s2 * 2.0) / (2.0 * dt * s3) : 0.0;
   for (int e = 0; e < m->ne; ++e) pv_e[e] = pv_e[e] - eps * dt * dpv[e];
   free(dpv);
   free(pvf);

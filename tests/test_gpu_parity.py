@@ -489,19 +489,24 @@ def test_concurrent_branches_match_the_serial_program(mesh4, prec, layout, membe
     dict(precision=1, time_scheme=1),
     dict(precision=1, members=2),
     dict(precision=1, members=16, member_layout=1),
+    dict(precision=0, pv_scheme=2),
+    dict(precision=1, pv_scheme=2),
 ])
 def test_state_at_rest_stays_at_rest(mesh4, kw):
     """A flat depth and no wind: every tendency is zero, so CRK4's (and
-    CRK3's) beta would be 0 / 0 (time_scheme_mod.F90:145, :99).  The device
-    takes beta = 1 there, as the reference's PC2 does (:178) and the oracle
-    does: the state stays exactly as it was, with finite invariants."""
+    CRK3's) beta would be 0 / 0 (time_scheme_mod.F90:145, :99), and so would
+    the conservative APVM's epsilon (operators_mod.F90:349-351).  The device
+    takes beta = 1 there, as the reference's PC2 does (:178), and epsilon = 0,
+    as the oracle does: the state stays exactly as it was, with finite
+    invariants."""
     from tmcore_gb300 import cases
     from tmcore_gb300.gpu import TMCoreGPU
 
     gd = np.full(mesh4.nCells, 9.80616 * 5000.0)
     u = np.zeros(mesh4.nEdges)
     ghs = np.zeros(mesh4.nCells)
-    g = TMCoreGPU(mesh4, dt=600.0, pv_scheme=1, apvm_weight=0.0, conserve_energy=1, **kw)
+    kw = {"pv_scheme": 1, **kw}
+    g = TMCoreGPU(mesh4, dt=600.0, apvm_weight=0.0, conserve_energy=1, **kw)
     members = kw.get("members", 1)
     for m in range(members):
         if members > 1:

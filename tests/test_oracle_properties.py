@@ -106,15 +106,18 @@ def test_interpolation_keeps_constants(mesh, oracle, c):
 
 
 @settings(max_examples=8, deadline=None, derandomize=True)
-@given(seed=seeds, amp=st.floats(min_value=0.0, max_value=0.05), umax=st.floats(min_value=0.0, max_value=20.0))
-def test_crk4_conserves_mass_and_energy(mesh, seed, amp, umax):
-    """From a random positive-depth state with a random (divergent) wind."""
+@given(seed=seeds, amp=st.floats(min_value=0.0, max_value=0.05), umax=st.floats(min_value=0.0, max_value=20.0),
+       pv_scheme=st.sampled_from([1, 2, 3]))
+def test_crk4_conserves_mass_and_energy(mesh, seed, amp, umax, pv_scheme):
+    """From a random positive-depth state with a random (divergent) wind, for
+    the three pv-on-edge schemes (all inside the energy-neutral q.F_perp)."""
     rng = np.random.default_rng(seed)
     g, h0 = 9.80616, 5000.0
     gd = g * h0 * (1.0 + amp * rng.uniform(-1.0, 1.0, mesh.nCells))
     u = umax * rng.uniform(-1.0, 1.0, mesh.nEdges)
     ghs = np.zeros(mesh.nCells)
-    o = ORACLE.Oracle(mesh, dt=600.0, pv_scheme=1, apvm_weight=0.0, adv_order=2, conserve_energy=1)
+    o = ORACLE.Oracle(mesh, dt=600.0, pv_scheme=pv_scheme, apvm_weight=0.0, adv_order=2, conserve_energy=1,
+                      interp_pv_order=3)
     try:
         o.set_initial(gd, u, ghs)
         m0, e0 = o.diag()[:2]
@@ -124,3 +127,25 @@ def test_crk4_conserves_mass_and_energy(mesh, seed, amp, umax):
         o.close()
     assert abs(m1 - m0) <= 1e-13 * abs(m0)
     assert abs(e1 - e0) <= 1e-12 * abs(e0)
+
+
+@pytest.mark.parametrize("kw", [dict(pv_scheme=1), dict(pv_scheme=2), dict(pv_scheme=3, interp_pv_order=3),
+                                dict(pv_scheme=1, time_scheme=1), dict(pv_scheme=1, time_scheme=3),
+                                dict(pv_scheme=1, apvm_weight=0.5), dict(pv_scheme=1, adv_order=3)])
+def test_state_at_rest_stays_at_rest(mesh, kw):
+    """A flat depth and no wind make every tendency zero.  The reference's
+    CRK4 and CRK3 beta (time_scheme_mod.F90:145, :99) and its conservative
+    APVM epsilon (operators_mod.F90:349-351) are then 0 / 0; the oracle takes
+    beta = 1 (as the reference's PC2 does, :178) and epsilon = 0, so the state
+    stays exactly at rest."""
+    gd = np.full(mesh.nCells, 9.80616 * 5000.0)
+    o = ORACLE.Oracle(mesh, dt=600.0, conserve_energy=1, **kw)
+    try:
+        o.set_initial(gd, np.zeros(mesh.nEdges), np.zeros(mesh.nCells))
+        o.step(2)
+        g1, i1 = o.state()[:2]
+        d = o.diag()
+    finally:
+        o.close()
+    assert np.array_equal(g1, gd) and not np.any(i1)
+    assert np.all(np.isfinite(d)) and d[4] == 1.0

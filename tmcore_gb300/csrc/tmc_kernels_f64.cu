@@ -171,7 +171,9 @@ __global__ void __launch_bounds__(256) k_cons_eps(Partials P0, int count, double
   __threadfence();
   volatile const double* rv = res;
   const double s1 = rv[R_C1], s2 = rv[R_C2], s3 = rv[R_C3];
-  out[10] = -(s1 - s2 * 2.0) / (2.0 * dt * s3);
+  // eps = 0 when s3 = 0: with no wind the correction dpv is zero on every
+  // edge and the reference's quotient is 0 / 0 (operators_mod.F90:349-351)
+  out[10] = s3 != 0.0 ? -(s1 - s2 * 2.0) / (2.0 * dt * s3) : 0.0;
   *counter = 0u;
 }
 
