@@ -105,19 +105,26 @@ def test_interpolation_keeps_constants(mesh, oracle, c):
     assert np.max(np.abs(oracle.op("c2v", one, out_size=mesh.nVertices) - c)) <= 10 * tol
 
 
-@settings(max_examples=8, deadline=None, derandomize=True)
+@settings(max_examples=20, deadline=None, derandomize=True)
 @given(seed=seeds, amp=st.floats(min_value=0.0, max_value=0.05), umax=st.floats(min_value=0.0, max_value=20.0),
-       pv_scheme=st.sampled_from([1, 2, 3]))
-def test_crk4_conserves_mass_and_energy(mesh, seed, amp, umax, pv_scheme):
-    """From a random positive-depth state with a random (divergent) wind, for
-    the three pv-on-edge schemes (all inside the energy-neutral q.F_perp)."""
+       hs=st.floats(min_value=0.0, max_value=2000.0), time_scheme=st.sampled_from([1, 2, 3]),
+       pv=st.sampled_from([(1, 3, 0.0), (1, 3, 0.5), (2, 3, 0.0), (3, 3, 0.0), (3, 4, 0.0), (3, 5, 0.0),
+                           (3, 6, 0.0)]))
+def test_time_schemes_conserve_mass_and_energy(mesh, seed, amp, umax, hs, time_scheme, pv):
+    """From a random positive-depth state, random (divergent) wind and random
+    topography: CRK3, CRK4 and PC2 with their energy-conserving beta
+    (time_scheme_mod.F90:94-100, :139-146, :174-180) keep total mass and total
+    energy (tmcore_swm_mod.F90:215-231) to round-off, for centred pv with and
+    without APVM, the conservative APVM and upwind pv of orders 3-6 (each a pv
+    on edges inside the energy-neutral q.F_perp)."""
+    pv_scheme, order, apvm = pv
     rng = np.random.default_rng(seed)
     g, h0 = 9.80616, 5000.0
-    gd = g * h0 * (1.0 + amp * rng.uniform(-1.0, 1.0, mesh.nCells))
+    ghs = g * hs * rng.uniform(0.0, 1.0, mesh.nCells)
+    gd = g * h0 * (1.0 + amp * rng.uniform(-1.0, 1.0, mesh.nCells)) - ghs
     u = umax * rng.uniform(-1.0, 1.0, mesh.nEdges)
-    ghs = np.zeros(mesh.nCells)
-    o = ORACLE.Oracle(mesh, dt=600.0, pv_scheme=pv_scheme, apvm_weight=0.0, adv_order=2, conserve_energy=1,
-                      interp_pv_order=3)
+    o = ORACLE.Oracle(mesh, dt=600.0, pv_scheme=pv_scheme, interp_pv_order=order, apvm_weight=apvm, adv_order=2,
+                      time_scheme=time_scheme, conserve_energy=1)
     try:
         o.set_initial(gd, u, ghs)
         m0, e0 = o.diag()[:2]
@@ -149,3 +156,39 @@ def test_state_at_rest_stays_at_rest(mesh, kw):
         o.close()
     assert np.array_equal(g1, gd) and not np.any(i1)
     assert np.all(np.isfinite(d)) and d[4] == 1.0
+
+
+@pytest.fixture(scope="module")
+def mesh3():
+    return icos(3)
+
+
+@settings(max_examples=12, deadline=None, derandomize=True)
+@given(seed=seeds, order=st.sampled_from([2, 3, 4, 5, 6]), mono=st.sampled_from([0, 1]),
+       c=st.floats(min_value=1e-3, max_value=1e3), umax=st.floats(min_value=0.0, max_value=30.0))
+def test_tracers_keep_constants_and_mass(mesh3, seed, order, mono, c, umax):
+    """Coupled tracers from a random state, random wind: a constant mixing
+    ratio stays that constant (the sg11 edge value of a constant is the
+    constant, adv_scheme_sg11_mod.F90:42-45 with the upwind correction of
+    operators_mod.F90:423-472), and a random tracer's mass is conserved."""
+    m = mesh3
+    rng = np.random.default_rng(seed)
+    gd = 9.80616 * 5000.0 * (1.0 + 0.05 * rng.uniform(-1.0, 1.0, m.nCells))
+    u = umax * rng.uniform(-1.0, 1.0, m.nEdges)
+    q = np.stack([np.full(m.nCells, c), rng.uniform(0.0, 1.0, m.nCells)])
+    o = ORACLE.Oracle(m, dt=600.0, pv_scheme=1, apvm_weight=0.0, n_tracers=2, tracer_adv_order=order,
+                      tracer_adv_mono=mono)
+    try:
+        o.set_initial(gd, u, np.zeros(m.nCells))
+        o.set_tracers(q * gd[None, :])
+        g0 = o.state()[0]
+        m0 = np.sum(o.tracers()[1] * m.areaCell)
+        o.step(3)
+        g1 = o.state()[0]
+        qt = o.tracers()
+    finally:
+        o.close()
+    assert np.all(np.isfinite(qt)) and np.all(np.isfinite(g1))
+    assert np.max(np.abs(qt[0] / g1 - c)) <= 1e-12 * c
+    assert abs(np.sum(qt[1] * m.areaCell) - m0) <= 1e-12 * abs(m0)
+    assert np.all(g0 > 0)
