@@ -3,6 +3,7 @@ against scipy's reader and writer."""
 import os
 
 import numpy as np
+import pytest
 
 
 def _same(a, b):
@@ -28,14 +29,19 @@ def test_write_then_read_both_ways(tmp_path):
         assert np.array_equal(np.asarray(b.vars[name]).reshape(ref.shape), ref), name
 
 
-def test_reads_a_scipy_written_file(tmp_path):
+@pytest.mark.parametrize("version", [1, 2])
+def test_reads_a_scipy_written_file(tmp_path, version):
+    """CDF-1 (32-bit offsets) and CDF-2 (64-bit offsets) files from scipy."""
     from conftest import icos
     from tmcore_gb300.gpu import read_mesh_file
 
     m = icos(2)
     p = os.path.join(tmp_path, "x1.162.grid.nc")
-    m.write(p)
+    m.write(p, version=version)
+    with open(p, "rb") as f:
+        assert f.read(4) == b"CDF" + bytes([version])
     b = read_mesh_file(p)
-    for name in ("verticesOnEdge", "cellsOnVertex", "dvEdge", "latCell", "zVertex"):
+    for name in ("verticesOnEdge", "cellsOnVertex", "dvEdge", "latCell", "zVertex", "weightsOnEdge",
+                 "kiteAreasOnVertex", "nEdgesOnCell"):
         ref = np.asarray(m.vars[name])
         assert np.array_equal(np.asarray(b.vars[name]).reshape(ref.shape), ref), name

@@ -72,11 +72,12 @@ class MPASMesh:
         return lev if 10 * 4 ** lev + 2 == self.dims["nCells"] else None
 
     # ------------------------------------------------------------------ I/O
-    def write(self, path: str) -> None:
-        """Write an MPAS grid NetCDF file (CDF-2, 64-bit offset)."""
+    def write(self, path: str, version: int = 2) -> None:
+        """Write an MPAS grid NetCDF file (version 2: CDF-2, 64-bit offsets;
+        1: CDF-1, 32-bit offsets)."""
         from scipy.io import netcdf_file
 
-        with netcdf_file(path, "w", version=2) as f:
+        with netcdf_file(path, "w", version=version) as f:
             for k, n in self.dims.items():
                 f.createDimension(k, n)
             if "TWO" not in self.dims:
