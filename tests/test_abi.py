@@ -75,3 +75,39 @@ def test_member_layout_arguments_checked_before_device_set_up():
         rc = lib.tmc_create(ctypes.byref(d), ctypes.byref(p), ctypes.byref(h))
         assert rc not in (abi.TMC_E_ARG, abi.TMC_E_UNSUP), (kw, rc)
         lib.tmc_destroy(h)
+
+
+def test_every_entry_point_refuses_null_arguments():
+    """Every exported function, called with null pointers and zero scalars,
+    returns an error code (the destroy and close functions return TMC_OK for
+    a null handle, and the error-message functions a message) and does not
+    crash: it runs in a child process, which must exit normally."""
+    import json
+    import subprocess
+    import sys
+
+    code = (
+        "import ctypes, json\n"
+        "from tmcore_gb300 import _lib, abi\n"
+        "lib = _lib.gpu()\n"
+        "ints = (ctypes.c_int32, ctypes.c_int, ctypes.c_int64, ctypes.c_uint64)\n"
+        "out = {}\n"
+        "for name, (res, args) in abi.SYMBOLS.items():\n"
+        "    vals = [0 if a in ints else 0.0 if a in (ctypes.c_double, ctypes.c_float) else None for a in args]\n"
+        "    r = getattr(lib, name)(*vals)\n"
+        "    out[name] = r.decode() if isinstance(r, bytes) else r\n"
+        "print(json.dumps(out))\n"
+    )
+    p = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True, timeout=300)
+    assert p.returncode == 0, p.stderr[-2000:]
+    out = json.loads(p.stdout.strip().splitlines()[-1])
+    from tmcore_gb300 import abi
+
+    assert set(out) == set(abi.SYMBOLS)
+    for name, r in out.items():
+        if name.endswith(("_destroy", "_close")):
+            assert r == abi.TMC_OK, name
+        elif name.endswith(("last_error", "_error")):
+            assert isinstance(r, str) and r, name
+        else:
+            assert isinstance(r, int) and r < 0, (name, r)
